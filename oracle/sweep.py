@@ -1,0 +1,158 @@
+"""Two-site ground-state sweep of the oracle (tests only).
+
+Restates the live sweep driver: ``SweepBasedEnergyMinimization`` over
+``GenericSweepSimulation::runSingleSweep``
+(``sba/GenericSweepSimulation.h:73-152, 212-268``), the microiteration
+schedule of ``SweepOptimizationTypeTrait<TwoSite>``
+(``sba/SweepOptimizationTypeTrait.h:85-142``), the boundary bookkeeping of
+``BoundaryPropagator`` (``sba/BoundaryPropagator.h:36-150``) and the
+truncate/merge steps of ``SweepMPSUpdater<TwoSite>``
+(``sba/SweepMPSUpdater.h:180-258``).  Energies follow ``get_energy``
+(``fw/sim/interface_sim.h:355-360``): <psi|H|psi>/<psi|psi> + core energy.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional
+
+import numpy as np
+
+from qcmaquis_gb300.mpo import MPO, make_ts_cache_mpo
+
+from . import dmrg_ref as R
+
+
+@dataclass
+class SweepParams:
+    nsweeps: int = 2
+    max_bond_dimension: int = 64
+    sweep_bond_dimensions: Optional[List[int]] = None
+    init_bond_dimension: int = 5
+    truncation_initial: float = 1e-16
+    truncation_final: float = 1e-16
+    ngrowsweeps: int = 2
+    ietl_jcd_tol: float = 1e-8
+    ietl_jcd_maxiter: int = 10
+    seed: int = 42
+
+
+def log_interpolate(y0, y1, N, i):
+    if N < 2:
+        return y1
+    if y0 == 0:
+        return 0.0
+    x = math.log(y1 / y0) / (N - 1)
+    return y0 * math.exp(x * i)
+
+
+def get_cutoff(p: SweepParams, sweep: int) -> float:
+    if sweep >= p.ngrowsweeps:
+        return p.truncation_final
+    return log_interpolate(p.truncation_initial, p.truncation_final, p.ngrowsweeps, sweep)
+
+
+def get_Mmax(p: SweepParams, sweep: int) -> int:
+    if p.sweep_bond_dimensions:
+        return p.sweep_bond_dimensions[min(sweep, len(p.sweep_bond_dimensions) - 1)]
+    return p.max_bond_dimension
+
+
+@dataclass
+class SweepRecord:
+    energies: List[float] = field(default_factory=list)
+    truncated_weight: List[float] = field(default_factory=list)
+    bond_dimension: List[int] = field(default_factory=list)
+    sweep_energy: List[float] = field(default_factory=list)
+    sweep_truncated_weight: List[float] = field(default_factory=list)
+
+
+def expval(mps: List[R.MPSTensor], mpo: MPO) -> float:
+    """``expval`` (``mp_tensors/mps_mpo_ops.h:57-68``) without the core energy."""
+    left = R.left_boundary(mps[0])
+    for i in range(len(mps)):
+        left = R.overlap_mpo_left_step(mps[i], mps[i], left, mpo[i], is_hermitian=False)
+    return sum(b.trace() for b in left[:1])
+
+
+def overlap(mps: List[R.MPSTensor]) -> float:
+    """<psi|psi> through the plain overlap steps."""
+    left = R.left_boundary(mps[0])[0]
+    for t in mps:
+        a = t.copy().make_left_paired()
+        # left^T-contracted transfer: L' = A^T (L (x) 1) A for a real MPS
+        rp = t.copy().make_right_paired()
+        t1 = R.bm_gemm(left, rp.data)
+        t3 = R.reshape_right_to_left(t.phys_i, t.left_i, t.right_i, t1)
+        left = R.bm_gemm(a.data.transpose(), t3)
+    return left.trace()
+
+
+def initial_state(model, mpo, p: SweepParams, nelec: int, twoS: int):
+    phys = model.phys
+    mps = R.default_mps_init(model.L, phys, (nelec, twoS), p.init_bond_dimension, p.seed)
+    R.normalize_right(mps)
+    return mps
+
+
+def run_dmrg(model, mpo: MPO, p: SweepParams, nelec: int, twoS: int = 0, mps=None,
+             callback=None) -> (SweepRecord, List[R.MPSTensor]):
+    L = model.L
+    phys = model.phys
+    if mps is None:
+        mps = initial_state(model, mpo, p, nelec, twoS)
+    ts_mpo = make_ts_cache_mpo(mpo, phys)
+    left: List = [None] * (L + 1)
+    right: List = [None] * (L + 1)
+    left[0] = R.left_boundary(mps[0])
+    right[L] = R.right_boundary(mps[L - 1])
+    for i in range(L - 1, 0, -1):
+        right[i] = R.overlap_mpo_right_step(mps[i], mps[i], right[i + 1], mpo[i])
+    rec = SweepRecord()
+    nmicro = 2 * (L - 2) if L > 2 else 1
+    for sweep in range(p.nsweeps):
+        Mmax = get_Mmax(p, sweep)
+        cutoff = get_cutoff(p, sweep)
+        for mi in range(nmicro):
+            site = mi if mi < L - 1 else 2 * L - 4 - mi
+            forward = mi < L - 1
+            change = (mi == L - 2) or (mi == nmicro - 1)
+            l2r = forward and not change
+            ts = ts_mpo[site]
+            psi = R.make_two_site_mps(mps[site], mps[site + 1])
+
+            def apply_h(x, _l=left[site], _r=right[site + 2], _w=ts):
+                return R.site_hamil2(x, _l, _r, _w)
+
+            theta, u, iters = R.jcd_solve(apply_h, psi, p.ietl_jcd_tol, p.ietl_jcd_maxiter)
+            rec.energies.append(theta + mpo.core_energy)
+            u.make_left_paired()
+            A0, B0 = mps[site], mps[site + 1]
+            _, tst = R.unreduce_left(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, u.data)
+            A, B, trunc = R.split_mps(tst, A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, Mmax, cutoff, l2r)
+            mps[site], mps[site + 1] = A, B
+            rec.truncated_weight.append(trunc.truncated_weight)
+            rec.bond_dimension.append(trunc.bond_dimension)
+            if l2r:
+                left[site + 1] = R.overlap_mpo_left_step(mps[site], mps[site], left[site], mpo[site])
+            else:
+                right[site + 1] = R.overlap_mpo_right_step(mps[site + 1], mps[site + 1], right[site + 2],
+                                                           mpo[site + 1])
+            if l2r:
+                if site + 2 < L:
+                    t = R.left_normalize_and_return(mps[site + 1])
+                    R.multiply_from_left(mps[site + 2], t)
+                else:
+                    R.left_normalize_and_return(mps[site + 1])
+            else:
+                if site > 0:
+                    t = R.right_normalize_and_return(mps[site])
+                    R.multiply_from_right(mps[site - 1], t)
+                else:
+                    R.right_normalize_and_return(mps[site])
+            if callback:
+                callback(sweep, mi, rec)
+        e = expval(mps, mpo) / overlap(mps) + mpo.core_energy
+        rec.sweep_energy.append(e)
+        rec.sweep_truncated_weight.append(max(rec.truncated_weight[-nmicro:]))
+    return rec, mps

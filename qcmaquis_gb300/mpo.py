@@ -1,0 +1,407 @@
+"""MPO tensors and the tagged MPO builder for the chemistry Hamiltonian.
+
+* ``MPOTensor`` restates ``mp_tensors/mpotensor.h:23-107`` /
+  ``mpotensor.hpp:10-75``: a column-major sparse matrix of (tag, scale) lists,
+  row/column non-zero counts, left/right bond spins and the Hermitian pairing
+  ``Hermitian`` of ``mp_tensors/mpotensor_detail.h:124-170``.
+* ``TaggedMPOMaker`` restates
+  ``models/generate_mpo/tagged_mpo_maker_optim.hpp:97-735``: prempo keys,
+  fork/merge insertion, filling strings, bond numbering in key order,
+  bond spins and Hermitian-conjugate bond pairs with their phases.
+* ``make_twosite_mpo`` restates ``mp_tensors/ts_ops.h:36-125`` (two-site MPO as
+  spin-coupled Kronecker products of neighbouring tensors).
+"""
+from __future__ import annotations
+
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+
+from .model import QCModel, TagHandler, Term
+from .site_operator import SiteOperator, SpinDescriptor, allowed_spins, op_kron_su2
+from .symmetry import Index, particle_number
+
+TRIVIAL_LEFT, BULK, BULK_NO_MERGE, TRIVIAL_RIGHT = 0, 1, 2, 3
+KEY_TL = (TRIVIAL_LEFT, (), 0)
+KEY_TR = (TRIVIAL_RIGHT, (), 0)
+
+
+def bulk_key(pos_op):
+    return (BULK, tuple(pos_op), 0)
+
+
+class Hermitian:
+    def __init__(self, left_herm, right_herm, left_phase, right_phase):
+        self.LeftHerm = list(left_herm)
+        self.RightHerm = list(right_herm)
+        self.LeftPhase = list(left_phase)
+        self.RightPhase = list(right_phase)
+
+    @classmethod
+    def identity(cls, ld, rd):
+        return cls(range(ld), range(rd), [1] * ld, [1] * rd)
+
+    def left_skip(self, b):
+        return self.LeftHerm[b] < b
+
+    def right_skip(self, b):
+        return self.RightHerm[b] < b
+
+    def left_conj(self, b):
+        return self.LeftHerm[b]
+
+    def right_conj(self, b):
+        return self.RightHerm[b]
+
+    def left_phase(self, b):
+        return self.LeftPhase[b]
+
+    def right_phase(self, b):
+        return self.RightPhase[b]
+
+    def __mul__(self, other: "Hermitian") -> "Hermitian":
+        return Hermitian(self.LeftHerm, other.RightHerm, self.LeftPhase, other.RightPhase)
+
+
+class MPOTensor:
+    """Sparse (b1, b2) -> [(op, scale), ...] tensor with SU(2) bond spins."""
+
+    def __init__(self, ld: int, rd: int, prempo: List[Tuple[int, int, int, float]], op_table: List[SiteOperator],
+                 herm: Optional[Hermitian], left_spins: List[SpinDescriptor], right_spins: List[SpinDescriptor]):
+        self.row_dim = ld
+        self.col_dim = rd
+        self.op_table = op_table
+        self.left_spins = list(left_spins)
+        self.right_spins = list(right_spins)
+        # element lists: later entries (in column-major order) are prepended
+        entries = sorted(prempo, key=lambda t: (t[1], t[0]))
+        self.elements: Dict[Tuple[int, int], List[Tuple[int, float]]] = {}
+        self.row_index: List[set] = [set() for _ in range(ld)]
+        for b1, b2, tag, scale in entries:
+            key = (b1, b2)
+            if key not in self.elements:
+                self.elements[key] = [(tag, scale)]
+                self.row_index[b1].add(b2)
+            else:
+                self.elements[key].insert(0, (tag, scale))
+        self.cols: List[List[int]] = [[] for _ in range(rd)]
+        for (b1, b2) in sorted(self.elements, key=lambda k: (k[1], k[0])):
+            self.cols[b2].append(b1)
+        self.row_nnz = [0] * ld
+        self.col_nnz = [0] * rd
+        for (b1, b2) in self.elements:
+            self.row_nnz[b1] += 1
+            self.col_nnz[b2] += 1
+        self.num_one_rows = sum(1 for x in self.row_nnz if x == 1)
+        self.num_one_cols = sum(1 for x in self.col_nnz if x == 1)
+        if herm is not None and len(herm.LeftHerm) == ld and len(herm.RightHerm) == rd:
+            self.herm = herm
+        else:
+            self.herm = Hermitian.identity(ld, rd)
+        self._sparse_cache: Dict[int, list] = {}
+
+    def has(self, b1, b2) -> bool:
+        return (b1, b2) in self.elements
+
+    def at(self, b1, b2) -> List[Tuple[int, float]]:
+        return self.elements[(b1, b2)]
+
+    def column(self, b2) -> List[int]:
+        return self.cols[b2]
+
+    def row(self, b1) -> List[int]:
+        return sorted(self.row_index[b1])
+
+    def left_spin(self, b) -> SpinDescriptor:
+        return self.left_spins[b]
+
+    def right_spin(self, b) -> SpinDescriptor:
+        return self.right_spins[b]
+
+    def op(self, tag) -> SiteOperator:
+        return self.op_table[tag]
+
+    def sparse(self, tag):
+        s = self._sparse_cache.get(tag)
+        if s is None:
+            s = self.op_table[tag].sparse()
+            self._sparse_cache[tag] = s
+        return s
+
+
+class MPO(list):
+    core_energy: float = 0.0
+
+
+class TaggedMPOMaker:
+    def __init__(self, model: QCModel):
+        self.L = model.L
+        self.th: TagHandler = model.tag_handler
+        self.identity = model.ops.ident
+        self.identity_full = model.ops.ident_full
+        self.filling = model.ops.fill
+        self.prempo: List[Dict] = [dict() for _ in range(self.L)]
+        self.site_terms: Dict[int, SiteOperator] = {}
+        self.leftmost_right = self.L
+        self.rightmost_left = 0
+        self.core_energy = 0.0
+        self.finalized = False
+        for t in model.terms:
+            self.add_term(t)
+
+    # -- prempo helpers ------------------------------------------------------
+    def _insert(self, p, kk, val, attach):
+        d = self.prempo[p]
+        if attach:
+            if kk not in d:
+                d[kk] = [val]
+        else:
+            d.setdefault(kk, []).append(val)
+        return kk[1]
+
+    def _insert_filling(self, i, j, k, trivial_fill, spin_gt_one):
+        for s in range(i, j):
+            use_ident = self.identity_full if spin_gt_one else self.identity
+            op = use_ident if trivial_fill else self.filling
+            d = self.prempo[s]
+            kk = (k, k)
+            if kk not in d:
+                d[kk] = [(op, 1.0)]
+            elif d[kk][0] != (op, 1.0):
+                raise RuntimeError(f"Pre-existing term at site {s}")
+
+    def add_term(self, term: Term):
+        term.ops.sort(key=lambda x: x[0])
+        n = len(term)
+        if n == 1:
+            self._add_1term(term)
+        elif n == 2:
+            self._add_2term(term)
+        else:
+            self._add_generic_term(term)
+        self.leftmost_right = min(self.leftmost_right, term.ops[-1][0])
+        self.rightmost_left = max(self.rightmost_left, term.ops[0][0])
+
+    def _add_1term(self, term):
+        if term.tag(0) == self.identity:
+            self.core_energy += term.coeff
+        else:
+            op = self.th.get_op(term.tag(0)).scaled(term.coeff)
+            p = term.position(0)
+            if p in self.site_terms:
+                self.site_terms[p].iadd(op)
+            else:
+                cur = SiteOperator()
+                cur.iadd(op)
+                self.site_terms[p] = cur
+
+    def _add_2term(self, term):
+        th = self.th
+        nferm = sum(1 for i in range(2) if th.is_fermionic(term.tag(i)))
+        mpo_spin = SpinDescriptor()
+        k1 = KEY_TL
+        mpo_spin = mpo_spin.couple(th.get_op(term.tag(0)).spin)
+        k2 = bulk_key([term.ops[1]])
+        k1 = self._insert(term.position(0), (k1, k2), (term.tag(0), term.coeff), attach=False)
+        if th.is_fermionic(term.tag(0)):
+            nferm -= 1
+        trivial = (nferm % 2 == 0)
+        self._insert_filling(term.position(0) + 1, term.position(1), k1, trivial, mpo_spin.get() > 1)
+        mpo_spin = mpo_spin.couple(th.get_op(term.tag(1)).spin)
+        self._insert(term.position(1), (k1, KEY_TR), (term.tag(1), 1.0), attach=True)
+        assert mpo_spin.get() == 0
+
+    def _add_generic_term(self, term):
+        th = self.th
+        nops = len(term)
+        nferm = sum(1 for i in range(nops) if th.is_fermionic(term.tag(i)))
+        mpo_spin = SpinDescriptor()
+        thresh = nops // 2  # prefer_fork
+        ops_left = []
+        k1 = KEY_TL
+        for i in range(thresh):
+            mpo_spin = mpo_spin.couple(th.get_op(term.tag(i)).spin)
+            ops_left.append(term.ops[i])
+            k2 = bulk_key(ops_left)
+            k1 = self._insert(term.position(i), (k1, k2), (term.tag(i), 1.0), attach=True)
+            if th.is_fermionic(term.tag(i)):
+                nferm -= 1
+            self._insert_filling(term.position(i) + 1, term.position(i + 1), k1, nferm % 2 == 0, mpo_spin.get() > 1)
+        ops_right = [term.ops[j] for j in range(thresh + 1, nops)]
+        k2 = bulk_key(ops_right)
+        mpo_spin = mpo_spin.couple(th.get_op(term.tag(thresh)).spin)
+        k1 = self._insert(term.position(thresh), (k1, k2), (term.tag(thresh), term.coeff), attach=False)
+        if th.is_fermionic(term.tag(thresh)):
+            nferm -= 1
+        self._insert_filling(term.position(thresh) + 1, term.position(thresh + 1), k1, nferm % 2 == 0,
+                             mpo_spin.get() > 1)
+        for i in range(thresh + 1, nops):
+            if i == nops - 1:
+                k2 = KEY_TR
+            else:
+                k2 = bulk_key([term.ops[j] for j in range(i + 1, nops)])
+            mpo_spin = mpo_spin.couple(th.get_op(term.tag(i)).spin)
+            k1 = self._insert(term.position(i), (k1, k2), (term.tag(i), 1.0), attach=True)
+            if th.is_fermionic(term.tag(i)):
+                nferm -= 1
+            if i != nops - 1:
+                self._insert_filling(term.position(i) + 1, term.position(i + 1), k1, nferm % 2 == 0,
+                                     mpo_spin.get() > 1)
+        assert mpo_spin.get() == 0
+
+    def _finalize(self):
+        kk = (KEY_TL, KEY_TR)
+        for p in sorted(self.site_terms):
+            tag = self.th.register_op(self.site_terms[p], 0)
+            d = self.prempo[p]
+            if kk in d:
+                raise RuntimeError("another site term already existing!")
+            d[kk] = [(tag, 1.0)]
+        for p in range(self.rightmost_left):
+            d = self.prempo[p]
+            d.setdefault((KEY_TL, KEY_TL), []).append((self.identity, 1.0))
+        for p in range(self.leftmost_right + 1, self.L):
+            d = self.prempo[p]
+            d.setdefault((KEY_TR, KEY_TR), []).append((self.identity, 1.0))
+        self.finalized = True
+
+    def _conjugate_key(self, k, p):
+        th = self.th
+        kind, pos_op, off = k
+        conj = (kind, tuple((pp, th.herm_conj(t)) for pp, t in pos_op), off)
+        phase = (1, 1)
+        if len(pos_op) == 1:
+            op1 = th.get_op(pos_op[0][1])
+            if p < pos_op[0][0]:
+                pdiff = particle_number(op1.bm.keys[0][0]) - particle_number(op1.bm.keys[0][1])
+                if pdiff == 1:
+                    phase = (1, -1)
+                elif pdiff == -1:
+                    phase = (-1, 1)
+            else:
+                if op1.spin.get() == 1:
+                    phase = (-1, 1)
+        if len(pos_op) == 2:
+            op1 = th.get_op(pos_op[0][1])
+            op2 = th.get_op(pos_op[1][1])
+            d1 = particle_number(op1.bm.keys[0][0]) - particle_number(op1.bm.keys[0][1])
+            d2 = particle_number(op2.bm.keys[0][0]) - particle_number(op2.bm.keys[0][1])
+            if op1.spin.get() == 1 and op2.spin.get() == 1 and op2.spin.action() == -1 and d1 == -d2:
+                phase = (-1, -1)
+            if op1.spin.get() == 1 and op2.spin.get() == 1 and op2.spin.action() == 1 and d1 == d2:
+                phase = (-1, -1)
+        return conj, phase
+
+    def create_mpo(self) -> MPO:
+        if not self.finalized:
+            self._finalize()
+        mpo = MPO()
+        left = {KEY_TL: 0}
+        left_spins = [SpinDescriptor()]
+        LeftHerm = [0]
+        LeftPhase = [1]
+        L = self.L
+        table = self.th.ops
+        for p in range(L):
+            pre = []
+            herm_pairs = {}
+            herm_phases = {}
+            right = {}
+            r = 2
+            for kk in sorted(self.prempo[p], key=lambda x: (x[1], x[0])):
+                k1, k2 = kk
+                for val in self.prempo[p][kk]:
+                    if k1 not in left:
+                        raise RuntimeError("k1 not found!")
+                    ll = left[k1]
+                    if k2 not in right:
+                        if k2 == KEY_TL:
+                            right[k2] = 0
+                        elif k2 == KEY_TR:
+                            right[k2] = 1
+                        else:
+                            right[k2] = r
+                            r += 1
+                    rr_dim = 0 if p == L - 1 else right[k2]
+                    pre.append((ll, rr_dim, val[0], val[1]))
+                    ck2, phase = self._conjugate_key(k2, p)
+                    if k2 != ck2:
+                        herm_pairs[k2] = ck2
+                        herm_phases[k2] = phase
+            ldim = max(x[0] for x in pre) + 1
+            rdim = max(x[1] for x in pre) + 1
+            right_spins = [SpinDescriptor() for _ in range(rdim)]
+            for (b1, b2, tag, _) in pre:
+                out_spin = left_spins[b1].couple(table[tag].spin)
+                assert right_spins[b2].get() == 0 or right_spins[b2].get() == out_spin.get()
+                right_spins[b2] = out_spin
+            RightHerm = list(range(rdim))
+            RightPhase = [1] * rdim
+            for hk in sorted(herm_pairs):
+                romeo = right.get(hk, 0)
+                julia = right.get(herm_pairs[hk], 0)
+                if romeo < julia:
+                    RightHerm[romeo], RightHerm[julia] = RightHerm[julia], RightHerm[romeo]
+                    RightPhase[romeo] = herm_phases[hk][0]
+                    RightPhase[julia] = herm_phases[hk][1]
+            h = Hermitian(LeftHerm, RightHerm, LeftPhase, RightPhase)
+            if p == 0:
+                t = MPOTensor(1, rdim, pre, table, h, left_spins, right_spins)
+            elif p == L - 1:
+                t = MPOTensor(ldim, 1, pre, table, h, left_spins, right_spins)
+            else:
+                t = MPOTensor(ldim, rdim, pre, table, h, left_spins, right_spins)
+            mpo.append(t)
+            left = right
+            left_spins = right_spins
+            LeftHerm = RightHerm
+            LeftPhase = RightPhase
+        mpo.core_energy = self.core_energy
+        return mpo
+
+
+def make_mpo(model: QCModel) -> MPO:
+    return TaggedMPOMaker(model).create_mpo()
+
+
+def make_twosite_mpo(mpo1: MPOTensor, mpo2: MPOTensor, phys1: Index, phys2: Index) -> MPOTensor:
+    """Two-site MPO tensor W(b1,b3) = sum_b2 W1(b1,b2) (x) W2(b2,b3) per operator spin."""
+    assert mpo1.col_dim == mpo2.row_dim
+    table: List[SiteOperator] = []
+    prempo = []
+    for b1 in range(mpo1.row_dim):
+        row1 = mpo1.row(b1)
+        for b3 in range(mpo2.col_dim):
+            summands = [b2 for b2 in row1 if mpo2.has(b2, b3)]
+            ret: Dict[int, SiteOperator] = {}
+            for b2 in summands:
+                p1 = mpo1.at(b1, b2)
+                p2 = mpo2.at(b2, b3)
+                for tag1, s1 in p1:
+                    op1 = mpo1.op(tag1)
+                    for tag2, s2 in p2:
+                        op2 = mpo2.op(tag2)
+                        spins = allowed_spins(mpo1.left_spin(b1).get(), mpo2.right_spin(b3).get(),
+                                              op1.spin.get(), op2.spin.get())
+                        for s in spins:
+                            prod_spin = SpinDescriptor(s, mpo1.left_spin(b1).get(), mpo2.right_spin(b3).get())
+                            prod = op_kron_su2(phys1, phys2, op1, op2, mpo1.left_spin(b1), mpo1.right_spin(b2),
+                                               mpo2.right_spin(b3), prod_spin)
+                            prod.remove_empty_blocks()
+                            prod = prod.scaled(s1 * s2)
+                            if s not in ret:
+                                ret[s] = SiteOperator()
+                            ret[s].iadd(prod)
+            for s in sorted(ret):
+                table.append(ret[s])
+                prempo.append((b1, b3, len(table) - 1, 1.0))
+    return MPOTensor(mpo1.row_dim, mpo2.col_dim, prempo, table, mpo1.herm * mpo2.herm,
+                     mpo1.left_spins, mpo2.right_spins)
+
+
+def make_ts_cache_mpo(mpo: MPO, phys: Index) -> List[MPOTensor]:
+    return [make_twosite_mpo(mpo[p], mpo[p + 1], phys, phys) for p in range(len(mpo) - 1)]
+
+
+__all__ = ["MPOTensor", "MPO", "Hermitian", "TaggedMPOMaker", "make_mpo", "make_twosite_mpo",
+           "make_ts_cache_mpo"]

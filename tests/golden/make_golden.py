@@ -1,0 +1,63 @@
+"""Extract the reference's own golden values into ``reference_fixtures.json``.
+
+Reads, as text, the reference test sources:
+
+* ``dmrg/tests/Fixtures/LiHFixture.h:29-94`` -- LiH CAS integrals (L=4, N=2)
+  and ``:112`` reference energy;
+* ``dmrg/tests/Fixtures/H2Fixture.h:26-35`` -- H2 integrals (L=2, N=2);
+* ``dmrg/tests/test1.cpp:93`` -- H2 ground-state energy;
+* ``dmrg/tests/test_wigner.cpp:21-45`` -- 24 Wigner 9j values.
+
+Run from the repository root with the reference mounted at REFERENCE (default
+``/root/reference``); the JSON it writes is committed so tests never need the
+reference tree at run time.
+"""
+import json
+import os
+import re
+import sys
+
+REF = os.environ.get("REFERENCE", "/root/reference")
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+NUM = r"[-+]?\d*\.?\d+(?:[eE][-+]?\d+)?"
+
+
+def parse_integral_map(text):
+    out = []
+    for m in re.finditer(r"\{\s*\{\s*(\d+)\s*,\s*(\d+)\s*,\s*(\d+)\s*,\s*(\d+)\s*\}\s*,\s*(" + NUM + r")\s*\}", text):
+        out.append([int(m.group(1)), int(m.group(2)), int(m.group(3)), int(m.group(4)), float(m.group(5))])
+    return out
+
+
+def main():
+    lih = open(os.path.join(REF, "dmrg/tests/Fixtures/LiHFixture.h")).read()
+    h2 = open(os.path.join(REF, "dmrg/tests/Fixtures/H2Fixture.h")).read()
+    t1 = open(os.path.join(REF, "dmrg/tests/test1.cpp")).read()
+    tw = open(os.path.join(REF, "dmrg/tests/test_wigner.cpp")).read()
+
+    lih_ints = parse_integral_map(lih)
+    lih_e = float(re.search(r"referenceEnergy\s*=\s*(" + NUM + ")", lih).group(1))
+    h2_ints = parse_integral_map(h2)
+    h2_e = float(re.search(r"BOOST_CHECK_CLOSE\(interface\.energy\(\),\s*(" + NUM + ")", t1).group(1))
+    wig = []
+    for m in re.finditer(r"\{\s*\{([-\d,\s]+)\}\s*,\s*(" + NUM + r")\s*\}", tw):
+        args = [int(x) for x in m.group(1).replace(" ", "").split(",") if x]
+        if len(args) == 9:
+            wig.append([args, float(m.group(2))])
+
+    data = {
+        "source": "values read from the reference test sources by tests/golden/make_golden.py",
+        "lih": {"L": 4, "nelec": 2, "spin": 0, "integrals": lih_ints, "energy": lih_e,
+                "cite": "dmrg/tests/Fixtures/LiHFixture.h:29-94,112; dmrg/tests/test2.cpp:57"},
+        "h2": {"L": 2, "nelec": 2, "spin": 0, "integrals": h2_ints, "energy": h2_e,
+               "cite": "dmrg/tests/Fixtures/H2Fixture.h:26-35; dmrg/tests/test1.cpp:93"},
+        "wigner9j": {"cases": wig, "rel_tol_percent": 1e-6, "cite": "dmrg/tests/test_wigner.cpp:21-45"},
+    }
+    with open(os.path.join(HERE, "reference_fixtures.json"), "w") as f:
+        json.dump(data, f, indent=1)
+    print(f"LiH {len(lih_ints)} integrals E={lih_e}; H2 {len(h2_ints)} integrals E={h2_e}; {len(wig)} 9j cases")
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,113 @@
+"""The oracle against the reference's golden values and exact diagonalisation."""
+import numpy as np
+import pytest
+
+from qcmaquis_gb300.integrals import synthetic_integral_map
+from qcmaquis_gb300.model import QCModel
+from qcmaquis_gb300.mpo import make_mpo, make_ts_cache_mpo
+from qcmaquis_gb300.wigner import wigner9j
+
+from oracle import dmrg_ref as R
+from oracle.fci import fci_energies
+from oracle.sweep import SweepParams, run_dmrg, initial_state
+
+from conftest import integral_map
+
+
+def test_wigner9j_reference_table(golden):
+    # dmrg/tests/test_wigner.cpp:21-45, BOOST_CHECK_CLOSE tolerance 1e-6 percent
+    for args, val in golden["wigner9j"]["cases"]:
+        got = wigner9j(*args)
+        if val == 0.0:
+            assert abs(got) < 1e-12
+        else:
+            assert abs(got - val) <= 1e-8 * abs(val) + 5e-11, (args, got, val)
+
+
+@pytest.mark.parametrize("name", ["lih", "h2"])
+def test_fci_pins_golden_energy(golden, name):
+    g = golden[name]
+    ints = integral_map(g["integrals"])
+    e = fci_energies(g["L"], ints, g["nelec"], g["spin"])[0]
+    assert abs(e - g["energy"]) < 1e-9
+
+
+@pytest.mark.parametrize("name", ["lih", "h2"])
+def test_oracle_dmrg_golden_energy(golden, name):
+    # dmrg/tests/test2.cpp:57 (LiH) and dmrg/tests/test1.cpp:93 (H2), BOOST_CHECK_CLOSE 1e-7 percent
+    g = golden[name]
+    ints = integral_map(g["integrals"])
+    m = QCModel(g["L"], ints, g["nelec"])
+    mpo = make_mpo(m)
+    rec, _ = run_dmrg(m, mpo, SweepParams(nsweeps=2, max_bond_dimension=100), nelec=g["nelec"])
+    assert abs(rec.sweep_energy[-1] - g["energy"]) < 1e-9 * abs(g["energy"])
+
+
+def test_oracle_dmrg_matches_fci_L6():
+    L, N = 6, 6
+    ints = synthetic_integral_map(L, seed=3)
+    e_fci = fci_energies(L, ints, N, 0)[0]
+    m = QCModel(L, ints, N)
+    mpo = make_mpo(m)
+    rec, _ = run_dmrg(m, mpo, SweepParams(nsweeps=2, max_bond_dimension=64), nelec=N)
+    assert abs(rec.sweep_energy[-1] - e_fci) < 1e-10
+
+
+def test_oracle_triplet_matches_fci():
+    L, N = 5, 4
+    ints = synthetic_integral_map(L, seed=5)
+    e_fci = fci_energies(L, ints, N, 2)[0]
+    m = QCModel(L, ints, N)
+    mpo = make_mpo(m)
+    rec, _ = run_dmrg(m, mpo, SweepParams(nsweeps=2, max_bond_dimension=64), nelec=N, twoS=2)
+    assert abs(rec.sweep_energy[-1] - e_fci) < 1e-10
+
+
+def _random_site_problem(L=6, N=6, seed=3, m=16, site=2, herm=True):
+    ints = synthetic_integral_map(L, seed=seed)
+    model = QCModel(L, ints, N)
+    mpo = make_mpo(model)
+    p = SweepParams(init_bond_dimension=m, seed=11)
+    mps = initial_state(model, mpo, p, N, 0)
+    left = R.left_boundary(mps[0])
+    for i in range(site):
+        # move the orthogonality centre along with the boundary
+        t = R.left_normalize_and_return(mps[i])
+        R.multiply_from_left(mps[i + 1], t)
+        left = R.overlap_mpo_left_step(mps[i], mps[i], left, mpo[i], is_hermitian=herm)
+    right = R.right_boundary(mps[L - 1])
+    for i in range(L - 1, site + 1, -1):
+        right = R.overlap_mpo_right_step(mps[i], mps[i], right, mpo[i], is_hermitian=herm)
+    ts = make_ts_cache_mpo(mpo, model.phys)[site]
+    psi = R.make_two_site_mps(mps[site], mps[site + 1])
+    return psi, left, right, ts
+
+
+def test_lbtm_equals_rbtm():
+    psi, left, right, ts = _random_site_problem()
+    a = R.site_hamil_lbtm(psi, left, right, ts)
+    b = R.site_hamil_rbtm(psi, left, right, ts)
+    diff = a.copy().axpy(-1.0, b)
+    assert diff.norm() <= 1e-12 * a.norm()
+
+
+def test_sigma_is_symmetric():
+    psi, left, right, ts = _random_site_problem()
+    rng = np.random.default_rng(0)
+    x = psi.copy().make_left_paired()
+    y = psi.copy().make_left_paired()
+    for k in range(y.data.n_blocks()):
+        y.data.blocks[k] = rng.standard_normal(y.data.blocks[k].shape)
+    hx = R.site_hamil2(x, left, right, ts)
+    hy = R.site_hamil2(y, left, right, ts)
+    assert abs(y.dot(hx) - x.dot(hy)) < 1e-12 * max(1.0, abs(y.dot(hx)))
+
+
+def test_hermitian_skip_matches_full_boundary():
+    # dmrg/tests/test_mps_mpo_ops/test_mps_mpo_ops_electronic.cpp:39-99: skipping
+    # Hermitian partners must not change sigma
+    psi, left, right, ts = _random_site_problem(herm=True)
+    psi2, left2, right2, ts2 = _random_site_problem(herm=False)
+    a = R.site_hamil_lbtm(psi, left, right, ts, is_hermitian=True)
+    b = R.site_hamil_lbtm(psi2, left2, right2, ts2, is_hermitian=False)
+    assert a.copy().axpy(-1.0, b).norm() <= 1e-12 * a.norm()
