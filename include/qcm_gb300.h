@@ -1,0 +1,195 @@
+/*
+ * qcm_gb300.h -- C ABI of the GB300 two-site SU2U1 DMRG hot path.
+ *
+ * All entry points are plain C: integer status codes, plain pointers and
+ * sizes.  Tensor *layouts* (quantum-number block lists) travel as host
+ * arrays; tensor *data* are device pointers to FP64 arrays in which every
+ * block is stored column-major (ld = rows) at the element offset given in its
+ * layout, blocks in the reference's DualIndex order (descending on the
+ * (left, right) charge pair).  A charge is the pair (N, 2S).
+ *
+ * The reference interfaces these entry points replace (paths relative to the
+ * QCMaquis source tree):
+ *   contraction::Engine<..., SU2>::site_hamil2
+ *       dmrg/framework/dmrg/mp_tensors/contractions/non-abelian/engine.hpp:197-207
+ *       -> qcm_plan_sigma + qcm_plan_run
+ *   contraction::Engine<..., SU2>::overlap_mpo_left_step
+ *       .../non-abelian/engine.hpp:104-113 -> qcm_plan_boundary_left + qcm_plan_run
+ *   contraction::Engine<..., SU2>::overlap_mpo_right_step
+ *       .../non-abelian/engine.hpp:115-124 -> qcm_plan_boundary_right + qcm_plan_run
+ *   ietl::dot / ietl::two_norm on MPSTensor (scalar_overlap, norm)
+ *       dmrg/framework/dmrg/mp_tensors/mpstensor.hpp:365-380 -> qcm_dot, qcm_nrm2
+ *   vector updates inside jacobi_davidson::calculate_eigenvalue
+ *       dmrg/framework/ietl/jacobi.h:385-435 -> qcm_axpby
+ *
+ * Error behaviour: every call returns QCM_OK (0) or a negative QCM_E_* code;
+ * qcm_last_error() returns a message for the calling thread.  The reference
+ * throws std::runtime_error in the same situations.
+ */
+#ifndef QCM_GB300_H
+#define QCM_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QCM_OK 0
+#define QCM_E_INVALID (-1)   /* malformed layout / MPO / argument */
+#define QCM_E_CUDA (-2)      /* a CUDA runtime call failed */
+#define QCM_E_NOMEM (-3)     /* device allocation failed */
+#define QCM_E_STATE (-4)     /* plan not uploaded / wrong plan kind */
+#define QCM_E_RANGE (-5)     /* request exceeds a fixed capacity */
+
+/* Quantum-number index: n sectors, charges q[2*i], q[2*i+1] = (N, 2S), sizes. */
+typedef struct {
+    int32_t n;
+    const int32_t* q;
+    const int64_t* size;
+} qcm_index_t;
+
+/* Block list of one block-sparse matrix.
+ * q[4*k..4*k+3] = (lc.N, lc.2S, rc.N, rc.2S); off[k] = element offset. */
+typedef struct {
+    int32_t n;
+    const int32_t* q;
+    const int64_t* rows;
+    const int64_t* cols;
+    const int64_t* off;
+} qcm_blocks_t;
+
+/* Boundary = one block matrix per MPO bond index b (mp_tensors/boundary.h:20-145).
+ * Blocks of b occupy [blk_ptr[b], blk_ptr[b+1]) of the flattened arrays;
+ * offsets index one arena holding all b. */
+typedef struct {
+    int32_t aux;
+    const int32_t* blk_ptr;
+    const int32_t* q;
+    const int64_t* rows;
+    const int64_t* cols;
+    const int64_t* off;
+} qcm_boundary_t;
+
+/* MPO tensor (mp_tensors/mpotensor.h:23-107) flattened.
+ * Elements (b1,b2) are listed column by column: column b2 owns
+ * [col_ptr[b2], col_ptr[b2+1]); row_of[e] = b1; its (op, scale) terms are
+ * [term_ptr[e], term_ptr[e+1]).  Operator o has SU(2) rank op_spin[o] and
+ * blocks [op_blk_ptr[o], op_blk_ptr[o+1]); block k maps phys charge
+ * (blk_q[4k], blk_q[4k+1]) to (blk_q[4k+2], blk_q[4k+3]) and owns sparse
+ * entries [blk_ent_ptr[k], blk_ent_ptr[k+1]) with ent[4e..4e+3] =
+ * (row, col, row_spin, col_spin) and value ent_coeff[e]
+ * (block_matrix/sparse_operator.h:105-168).  Hermitian data follow
+ * mp_tensors/mpotensor_detail.h:124-160 (partner index and phase). */
+typedef struct {
+    int32_t row_dim, col_dim;
+    const int32_t* left_spin;
+    const int32_t* right_spin;
+    const int32_t* left_herm;
+    const int32_t* right_herm;
+    const int32_t* left_phase;
+    const int32_t* right_phase;
+    const int32_t* col_ptr;
+    const int32_t* row_of;
+    const int32_t* term_ptr;
+    const int32_t* term_op;
+    const double* term_scale;
+    int32_t n_ops;
+    const int32_t* op_spin;
+    const int32_t* op_blk_ptr;
+    const int32_t* blk_q;
+    const int32_t* blk_ent_ptr;
+    const int32_t* ent;
+    const double* ent_coeff;
+} qcm_mpo_t;
+
+typedef struct qcm_plan qcm_plan;
+
+/* Buffer slots a plan reads and writes. */
+enum {
+    QCM_BUF_KET = 0,     /* input MPS tensor data (left-paired layout) */
+    QCM_BUF_LEFT = 1,    /* left boundary arena */
+    QCM_BUF_RIGHT = 2,   /* right boundary arena */
+    QCM_BUF_OUT = 3,     /* output: sigma (ket layout) or new boundary arena */
+    QCM_BUF_S0 = 4,      /* scratch 0 */
+    QCM_BUF_S1 = 5,      /* scratch 1 */
+    QCM_BUF_S2 = 6,      /* scratch 2 */
+    QCM_NBUF = 7
+};
+
+/* Precision of the dense block products of a plan. */
+enum {
+    QCM_PREC_FP64 = 0,      /* all arithmetic FP64 */
+    QCM_PREC_TF32 = 1,      /* tcgen05 kind::tf32 products, FP32 accumulation */
+    QCM_PREC_BF16X3 = 2     /* 3-slice BF16 split products, FP32 accumulation */
+};
+
+const char* qcm_last_error(void);
+int qcm_version(void);
+
+/* sigma = H_eff psi for a two-site (reduced) tensor; bra = ket.
+ * psi/sigma layout: left-paired blocks of the ket.  hermitian != 0 uses the
+ * MPO's Hermitian partners (boundaries then hold no blocks at skipped b). */
+int qcm_plan_sigma(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                   const qcm_blocks_t* psi, const qcm_boundary_t* left, const qcm_boundary_t* right,
+                   const qcm_mpo_t* mpo, int32_t hermitian, qcm_plan** plan);
+
+/* New left boundary L[i+1] from L[i], site tensor (bra = ket, left-paired) and W[i]. */
+int qcm_plan_boundary_left(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                           const qcm_blocks_t* mps, const qcm_boundary_t* left, const qcm_mpo_t* mpo,
+                           int32_t hermitian, qcm_plan** plan);
+
+/* New right boundary R[i] from R[i+1], site tensor (left-paired) and W[i]. */
+int qcm_plan_boundary_right(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                            const qcm_blocks_t* mps, const qcm_boundary_t* right, const qcm_mpo_t* mpo,
+                            int32_t hermitian, qcm_plan** plan);
+
+/* Sizes (elements) of the output and of the three scratch slots. */
+int qcm_plan_sizes(const qcm_plan* plan, int64_t* out_elems, int64_t* scratch_elems3);
+
+/* Work counters: algorithmic FLOPs of the block products, FLOPs and bytes of the
+ * gather/axpy stages, and the number of kernel launches of one run. */
+int qcm_plan_work(const qcm_plan* plan, double* gemm_flops, double* axpy_flops, double* axpy_bytes,
+                  int32_t* launches);
+
+/* Output boundary layout of a boundary plan (aux, then per-block arrays of
+ * length nblocks).  Call first with NULL arrays to get aux and nblocks. */
+int qcm_plan_out_layout(const qcm_plan* plan, int32_t* aux, int32_t* nblocks, int32_t* blk_ptr,
+                        int32_t* q, int64_t* rows, int64_t* cols, int64_t* off);
+
+/* Stage export for host-side inspection: kind 0 = gather-axpy, 1 = grouped GEMM. */
+int qcm_plan_num_stages(const qcm_plan* plan, int32_t* n);
+int qcm_plan_stage_info(const qcm_plan* plan, int32_t stage, int32_t* kind, int64_t* n_out, int64_t* n_terms);
+int qcm_plan_stage_axpy(const qcm_plan* plan, int32_t stage, int64_t* out_desc /*6*n_out*/,
+                        int64_t* term_desc /*3*n_terms*/, double* term_alpha);
+int qcm_plan_stage_gemm(const qcm_plan* plan, int32_t stage, int64_t* out_desc /*7*n_out*/,
+                        int64_t* seg_desc /*8*n_terms*/, double* seg_alpha);
+
+/* Copy the plan's task tables to the current device (once per plan). */
+int qcm_plan_upload(qcm_plan* plan);
+
+/* Run the plan on a CUDA stream (NULL = default stream); bufs[QCM_NBUF] are
+ * device pointers.  precision selects FP64 or a tensor-core form. */
+int qcm_plan_run(qcm_plan* plan, double* const* bufs, int32_t precision, void* stream);
+
+void qcm_plan_destroy(qcm_plan* plan);
+
+/* FP64 vector kernels over n elements (deterministic reductions).
+ * The result of qcm_dot / qcm_nrm2 is written to a device double. */
+int qcm_dot(const double* x, const double* y, int64_t n, double* result_dev, void* stream);
+int qcm_nrm2(const double* x, int64_t n, double* result_dev, void* stream);
+/* y = a*x + b*y */
+int qcm_axpby(double a, const double* x, double b, double* y, int64_t n, void* stream);
+/* y[i] = sum_k coef[k] * X[k][i]  for k < nvec (coef on the host) */
+int qcm_lincomb(const double* const* x_dev_ptrs, const double* coef, int32_t nvec, double* y, int64_t n,
+                void* stream);
+/* out[k] = dot(V_k, y) for k < nvec, results in a device array of nvec doubles */
+int qcm_multi_dot(const double* const* v_dev_ptrs, int32_t nvec, const double* y, int64_t n, double* out_dev,
+                  void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QCM_GB300_H */

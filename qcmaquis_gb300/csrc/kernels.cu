@@ -1,0 +1,436 @@
+// Device executors for contraction plans and the FP64 vector kernels of the
+// eigensolver.  Compiled for sm_103a only.
+//
+// * gather_axpy_kernel   -- the lbtm/rbtm micro-axpys (ct/non-abelian/micro_kernels.hpp:19-198)
+//   regrouped per output tile: each work item owns one column range of one
+//   output tile and writes it once (sum of scaled source stripes, fixed order).
+// * gemm_f64_kernel      -- grouped, segmented FP64 block products (the dgemm calls
+//   of ct/non-abelian/gemm.hpp:48-204): every work item owns one 64x64 output
+//   tile and sums all its segments (split-K over MPO bond indices) in registers.
+// * dot/nrm2/axpby/...   -- ietl::dot / two_norm / vector updates of the
+//   Jacobi-Davidson loop (dmrg/framework/ietl/jacobi.h:385-435), with
+//   deterministic two-pass reductions (warp shuffles, fixed combine order).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "plan.hpp"
+
+
+namespace qcm {
+
+#define QCM_CUDA(call)                                                                  \
+    do {                                                                                \
+        cudaError_t err__ = (call);                                                     \
+        if (err__ != cudaSuccess) {                                                     \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(err__));           \
+            return QCM_E_CUDA;                                                          \
+        }                                                                               \
+    } while (0)
+
+struct DevAxpyOut { int64_t dst_off, ldd, rows, cols, t_begin, t_end; int32_t dst_buf, pad; };
+struct DevAxpyTerm { int64_t src_off, lds; double alpha; int32_t src_buf, pad; };
+struct DevAxpyWork { int64_t out, c0, c1; };
+struct DevGemmOut { int64_t c_off, ldc, M, N, s_begin, s_end; int32_t c_buf, pad; };
+struct DevGemmSeg { int64_t a_off, lda, b_off, ldb, K; double alpha; int32_t a_buf, ta, b_buf, tb; };
+struct DevGemmWork { int64_t out, m0, n0; };
+
+struct BufTable { double* p[QCM_NBUF]; };
+
+// ------------------------------------------------------------------ gather-axpy
+constexpr int AXPY_THREADS = 256;
+constexpr int AXPY_TERM_CACHE = 128;
+
+__global__ void __launch_bounds__(AXPY_THREADS)
+gather_axpy_kernel(BufTable bufs, const DevAxpyOut* __restrict__ outs, const DevAxpyTerm* __restrict__ terms,
+                   const DevAxpyWork* __restrict__ work) {
+    __shared__ double s_alpha[AXPY_TERM_CACHE];
+    __shared__ const double* s_src[AXPY_TERM_CACHE];
+    __shared__ int64_t s_lds[AXPY_TERM_CACHE];
+    const DevAxpyWork w = work[blockIdx.x];
+    const DevAxpyOut o = outs[w.out];
+    double* __restrict__ dst = bufs.p[o.dst_buf] + o.dst_off;
+    const int64_t rows = o.rows;
+    const int64_t nel = rows * (w.c1 - w.c0);
+    const int64_t nterm = o.t_end - o.t_begin;
+    // each thread keeps up to 4 accumulators (elements e, e+256, ...)
+    for (int64_t base = 0; base < nel; base += 4 * AXPY_THREADS) {
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        int64_t ii[4], jj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            int64_t e = base + threadIdx.x + (int64_t)u * AXPY_THREADS;
+            ii[u] = e % rows;
+            jj[u] = w.c0 + e / rows;
+        }
+        for (int64_t t0 = 0; t0 < nterm; t0 += AXPY_TERM_CACHE) {
+            const int64_t tn = min((int64_t)AXPY_TERM_CACHE, nterm - t0);
+            __syncthreads();
+            for (int64_t t = threadIdx.x; t < tn; t += AXPY_THREADS) {
+                const DevAxpyTerm tt = terms[o.t_begin + t0 + t];
+                s_alpha[t] = tt.alpha;
+                s_src[t] = bufs.p[tt.src_buf] + tt.src_off;
+                s_lds[t] = tt.lds;
+            }
+            __syncthreads();
+            for (int64_t t = 0; t < tn; ++t) {
+                const double a = s_alpha[t];
+                const double* __restrict__ src = s_src[t];
+                const int64_t lds = s_lds[t];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    int64_t e = base + threadIdx.x + (int64_t)u * AXPY_THREADS;
+                    if (e < nel) acc[u] = fma(a, __ldg(src + ii[u] + jj[u] * lds), acc[u]);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            int64_t e = base + threadIdx.x + (int64_t)u * AXPY_THREADS;
+            if (e < nel) dst[ii[u] + jj[u] * o.ldd] = acc[u];
+        }
+    }
+}
+
+// ------------------------------------------------------------------ FP64 grouped GEMM
+constexpr int GT_M = 64, GT_N = 64, GT_K = 16;
+
+__global__ void __launch_bounds__(256)
+gemm_f64_kernel(BufTable bufs, const DevGemmOut* __restrict__ outs, const DevGemmSeg* __restrict__ segs,
+                const DevGemmWork* __restrict__ work) {
+    __shared__ double sA[GT_K][GT_M + 1];
+    __shared__ double sB[GT_K][GT_N + 1];
+    const DevGemmWork w = work[blockIdx.x];
+    const DevGemmOut o = outs[w.out];
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+    for (int64_t s = o.s_begin; s < o.s_end; ++s) {
+        const DevGemmSeg g = segs[s];
+        const double* __restrict__ A = bufs.p[g.a_buf] + g.a_off;
+        const double* __restrict__ B = bufs.p[g.b_buf] + g.b_off;
+        const double alpha = g.alpha;
+        for (int64_t k0 = 0; k0 < g.K; k0 += GT_K) {
+            // load A tile (GT_M x GT_K): element (m, k)
+            for (int idx = threadIdx.x; idx < GT_M * GT_K; idx += 256) {
+                int m, k;
+                if (g.ta) { k = idx % GT_K; m = idx / GT_K; } else { m = idx % GT_M; k = idx / GT_M; }
+                int64_t gm = w.m0 + m, gk = k0 + k;
+                double v = 0.0;
+                if (gm < o.M && gk < g.K) v = g.ta ? A[gk + gm * g.lda] : A[gm + gk * g.lda];
+                sA[k][m] = v * alpha;
+            }
+            for (int idx = threadIdx.x; idx < GT_N * GT_K; idx += 256) {
+                int n, k;
+                if (g.tb) { n = idx % GT_N; k = idx / GT_N; } else { k = idx % GT_K; n = idx / GT_K; }
+                int64_t gn = w.n0 + n, gk = k0 + k;
+                double v = 0.0;
+                if (gn < o.N && gk < g.K) v = g.tb ? B[gn + gk * g.ldb] : B[gk + gn * g.ldb];
+                sB[k][n] = v;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < GT_K; ++k) {
+                double a[4], b[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) a[i] = sA[k][tx + 16 * i];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) b[j] = sB[k][ty + 16 * j];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+            }
+            __syncthreads();
+        }
+    }
+    double* __restrict__ C = bufs.p[o.c_buf] + o.c_off;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int64_t gm = w.m0 + tx + 16 * i, gn = w.n0 + ty + 16 * j;
+            if (gm < o.M && gn < o.N) C[gm + gn * o.ldc] = acc[i][j];
+        }
+}
+
+// ------------------------------------------------------------------ plan upload / run
+void free_stage_device(Stage& st) {
+    if (st.d_a) cudaFree(st.d_a);
+    if (st.d_b) cudaFree(st.d_b);
+    if (st.d_c) cudaFree(st.d_c);
+    st.d_a = st.d_b = st.d_c = nullptr;
+}
+
+template <class T>
+static int upload_vec(const std::vector<T>& v, void** d) {
+    size_t bytes = std::max<size_t>(v.size(), 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(d, bytes);
+    if (e != cudaSuccess) { set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e)); return QCM_E_NOMEM; }
+    if (!v.empty()) QCM_CUDA(cudaMemcpy(*d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return QCM_OK;
+}
+
+static int upload_stage(Stage& st) {
+    int rc = QCM_OK;
+    if (st.kind == ST_AXPY) {
+        std::vector<DevAxpyOut> o(st.aout.size());
+        std::vector<DevAxpyTerm> t(st.aterm.size());
+        std::vector<DevAxpyWork> w;
+        for (size_t i = 0; i < st.aout.size(); ++i) {
+            const AxpyOut& a = st.aout[i];
+            o[i] = {a.dst_off, a.ldd, a.rows, a.cols, a.t_begin, a.t_end, a.dst_buf, 0};
+            // column chunks of at most ~8192 elements per work item
+            int64_t cc = std::max<int64_t>(1, 8192 / std::max<int64_t>(1, a.rows));
+            for (int64_t c0 = 0; c0 < a.cols; c0 += cc) w.push_back({(int64_t)i, c0, std::min(a.cols, c0 + cc)});
+        }
+        for (size_t i = 0; i < st.aterm.size(); ++i) {
+            const AxpyTerm& a = st.aterm[i];
+            t[i] = {a.src_off, a.lds, a.alpha, a.src_buf, 0};
+        }
+        if ((rc = upload_vec(o, &st.d_a))) return rc;
+        if ((rc = upload_vec(t, &st.d_b))) return rc;
+        if ((rc = upload_vec(w, &st.d_c))) return rc;
+        st.n_work = (int64_t)w.size();
+    } else if (st.kind == ST_GEMM) {
+        std::vector<DevGemmOut> o(st.gout.size());
+        std::vector<DevGemmSeg> s(st.gseg.size());
+        std::vector<DevGemmWork> w;
+        for (size_t i = 0; i < st.gout.size(); ++i) {
+            const GemmOut& g = st.gout[i];
+            o[i] = {g.c_off, g.ldc, g.M, g.N, g.s_begin, g.s_end, g.c_buf, 0};
+            for (int64_t m0 = 0; m0 < g.M; m0 += GT_M)
+                for (int64_t n0 = 0; n0 < g.N; n0 += GT_N) w.push_back({(int64_t)i, m0, n0});
+        }
+        for (size_t i = 0; i < st.gseg.size(); ++i) {
+            const GemmSeg& g = st.gseg[i];
+            s[i] = {g.a_off, g.lda, g.b_off, g.ldb, g.K, g.alpha, g.a_buf, g.ta, g.b_buf, g.tb};
+        }
+        if ((rc = upload_vec(o, &st.d_a))) return rc;
+        if ((rc = upload_vec(s, &st.d_b))) return rc;
+        if ((rc = upload_vec(w, &st.d_c))) return rc;
+        st.n_work = (int64_t)w.size();
+    }
+    return QCM_OK;
+}
+
+static int launch_axpy(const Stage& st, const BufTable& bt, cudaStream_t s) {
+    if (st.n_work == 0) return QCM_OK;
+    if (st.n_work > 0x7fffffffLL) { set_error("axpy work list too large"); return QCM_E_RANGE; }
+    gather_axpy_kernel<<<(unsigned)st.n_work, AXPY_THREADS, 0, s>>>(
+        bt, (const DevAxpyOut*)st.d_a, (const DevAxpyTerm*)st.d_b, (const DevAxpyWork*)st.d_c);
+    QCM_CUDA(cudaGetLastError());
+    return QCM_OK;
+}
+
+static int launch_gemm(const Stage& st, const BufTable& bt, int precision, cudaStream_t s) {
+    if (st.n_work == 0) return QCM_OK;
+    if (st.n_work > 0x7fffffffLL) { set_error("gemm work list too large"); return QCM_E_RANGE; }
+    if (precision != QCM_PREC_FP64) {
+        set_error("tensor-core precisions are not available in this build");
+        return QCM_E_STATE;
+    }
+    gemm_f64_kernel<<<(unsigned)st.n_work, 256, 0, s>>>(bt, (const DevGemmOut*)st.d_a, (const DevGemmSeg*)st.d_b,
+                                                         (const DevGemmWork*)st.d_c);
+    QCM_CUDA(cudaGetLastError());
+    return QCM_OK;
+}
+
+// ------------------------------------------------------------------ vector kernels
+constexpr int RED_THREADS = 256;
+constexpr int RED_BLOCKS = 304;  // 2 x 152 SMs
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double block_sum(double v) {
+    __shared__ double ws[RED_THREADS / 32];
+    v = warp_sum(v);
+    const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
+    __syncthreads();
+    if (lane == 0) ws[wid] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (wid == 0) {
+        r = (lane < RED_THREADS / 32) ? ws[lane] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;  // valid in thread 0
+}
+
+__global__ void __launch_bounds__(RED_THREADS)
+multi_dot_partial(const double* const* __restrict__ v, int nvec, const double* __restrict__ y, int64_t n,
+                  double* __restrict__ partial) {
+    // partial[k * gridDim.x + blockIdx.x]
+    for (int k = 0; k < nvec; ++k) {
+        const double* __restrict__ x = v[k];
+        double s = 0.0;
+        for (int64_t i = (int64_t)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += (int64_t)gridDim.x * RED_THREADS)
+            s = fma(x[i], y[i], s);
+        s = block_sum(s);
+        if (threadIdx.x == 0) partial[(int64_t)k * gridDim.x + blockIdx.x] = s;
+    }
+}
+
+__global__ void __launch_bounds__(RED_THREADS)
+multi_dot_final(const double* __restrict__ partial, int nparts, int nvec, double* __restrict__ out, int do_sqrt) {
+    for (int k = 0; k < nvec; ++k) {
+        double s = 0.0;
+        for (int i = threadIdx.x; i < nparts; i += RED_THREADS) s += partial[(int64_t)k * nparts + i];
+        s = block_sum(s);
+        if (threadIdx.x == 0) out[k] = do_sqrt ? sqrt(s) : s;
+    }
+}
+
+__global__ void axpby_kernel(double a, const double* __restrict__ x, double b, double* __restrict__ y, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = (b == 0.0) ? a * x[i] : fma(a, x[i], b * y[i]);
+}
+
+constexpr int LIN_MAX = 32;
+struct LinArgs { const double* x[LIN_MAX]; double c[LIN_MAX]; int n; };
+
+__global__ void lincomb_kernel(LinArgs args, double* __restrict__ y, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int k = 0; k < args.n; ++k) s = fma(args.c[k], args.x[k][i], s);
+        y[i] = s;
+    }
+}
+
+// per-device reduction workspace owned by the library (allocated on first use)
+struct RedWs { double* partial = nullptr; const double** ptrs = nullptr; };
+static std::mutex g_ws_mu;
+static RedWs g_ws[64];
+
+static int get_ws(RedWs** ws) {
+    int dev = 0;
+    QCM_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) { set_error("device ordinal out of range"); return QCM_E_RANGE; }
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    RedWs& w = g_ws[dev];
+    if (!w.partial) {
+        if (cudaMalloc(&w.partial, sizeof(double) * RED_BLOCKS * LIN_MAX) != cudaSuccess) {
+            set_error("cudaMalloc of the reduction workspace failed");
+            return QCM_E_NOMEM;
+        }
+        if (cudaMalloc((void**)&w.ptrs, sizeof(double*) * LIN_MAX) != cudaSuccess) {
+            set_error("cudaMalloc of the pointer table failed");
+            return QCM_E_NOMEM;
+        }
+    }
+    *ws = &w;
+    return QCM_OK;
+}
+
+}  // namespace qcm
+
+using namespace qcm;
+
+extern "C" {
+
+int qcm_plan_upload(qcm_plan* p) {
+    if (!p) { set_error("null plan"); return QCM_E_INVALID; }
+    if (p->uploaded) return QCM_OK;
+    int dev = 0;
+    QCM_CUDA(cudaGetDevice(&dev));
+    for (auto& st : p->stages) {
+        int rc = upload_stage(st);
+        if (rc) return rc;
+    }
+    p->uploaded = true;
+    p->device = dev;
+    return QCM_OK;
+}
+
+int qcm_plan_run(qcm_plan* p, double* const* bufs, int32_t precision, void* stream) {
+    if (!p || !bufs) { set_error("null argument"); return QCM_E_INVALID; }
+    if (!p->uploaded) { set_error("plan not uploaded"); return QCM_E_STATE; }
+    int dev = 0;
+    QCM_CUDA(cudaGetDevice(&dev));
+    if (dev != p->device) { set_error("plan was uploaded to another device"); return QCM_E_STATE; }
+    BufTable bt;
+    for (int i = 0; i < QCM_NBUF; ++i) bt.p[i] = bufs[i];
+    cudaStream_t s = (cudaStream_t)stream;
+    for (auto& st : p->stages) {
+        int rc = QCM_OK;
+        if (st.kind == ST_ZERO) {
+            if (st.zlen > 0) {
+                if (!bufs[st.zbuf]) { set_error("missing scratch buffer"); return QCM_E_INVALID; }
+                QCM_CUDA(cudaMemsetAsync(bufs[st.zbuf], 0, sizeof(double) * st.zlen, s));
+            }
+        } else if (st.kind == ST_AXPY) {
+            rc = launch_axpy(st, bt, s);
+        } else {
+            rc = launch_gemm(st, bt, precision, s);
+        }
+        if (rc) return rc;
+    }
+    return QCM_OK;
+}
+
+int qcm_multi_dot(const double* const* v, int32_t nvec, const double* y, int64_t n, double* out, void* stream) {
+    if (nvec < 0 || nvec > LIN_MAX) { set_error("qcm_multi_dot: nvec out of range"); return QCM_E_RANGE; }
+    if (nvec == 0) return QCM_OK;
+    RedWs* ws = nullptr;
+    int rc = get_ws(&ws);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    QCM_CUDA(cudaMemcpyAsync(ws->ptrs, v, sizeof(double*) * nvec, cudaMemcpyHostToDevice, s));
+    multi_dot_partial<<<RED_BLOCKS, RED_THREADS, 0, s>>>(ws->ptrs, nvec, y, n, ws->partial);
+    QCM_CUDA(cudaGetLastError());
+    multi_dot_final<<<1, RED_THREADS, 0, s>>>(ws->partial, RED_BLOCKS, nvec, out, 0);
+    QCM_CUDA(cudaGetLastError());
+    return QCM_OK;
+}
+
+int qcm_dot(const double* x, const double* y, int64_t n, double* out, void* stream) {
+    const double* v[1] = {x};
+    return qcm_multi_dot(v, 1, y, n, out, stream);
+}
+
+int qcm_nrm2(const double* x, int64_t n, double* out, void* stream) {
+    RedWs* ws = nullptr;
+    int rc = get_ws(&ws);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const double* v[1] = {x};
+    QCM_CUDA(cudaMemcpyAsync(ws->ptrs, v, sizeof(double*), cudaMemcpyHostToDevice, s));
+    multi_dot_partial<<<RED_BLOCKS, RED_THREADS, 0, s>>>(ws->ptrs, 1, x, n, ws->partial);
+    QCM_CUDA(cudaGetLastError());
+    multi_dot_final<<<1, RED_THREADS, 0, s>>>(ws->partial, RED_BLOCKS, 1, out, 1);
+    QCM_CUDA(cudaGetLastError());
+    return QCM_OK;
+}
+
+int qcm_axpby(double a, const double* x, double b, double* y, int64_t n, void* stream) {
+    if (n <= 0) return QCM_OK;
+    int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    axpby_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(a, x, b, y, n);
+    QCM_CUDA(cudaGetLastError());
+    return QCM_OK;
+}
+
+int qcm_lincomb(const double* const* x, const double* coef, int32_t nvec, double* y, int64_t n, void* stream) {
+    if (nvec < 1 || nvec > LIN_MAX) { set_error("qcm_lincomb: nvec out of range"); return QCM_E_RANGE; }
+    LinArgs args;
+    for (int k = 0; k < nvec; ++k) { args.x[k] = x[k]; args.c[k] = coef[k]; }
+    args.n = nvec;
+    int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    if (blocks < 1) return QCM_OK;
+    lincomb_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(args, y, n);
+    QCM_CUDA(cudaGetLastError());
+    return QCM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,1058 @@
+// Contraction-plan builder: quantum-number block pairing and index maps for the
+// SU2U1 sigma vector and boundary updates, emitted as deterministic task lists.
+//
+// The traversals restate, block for block:
+//   BoundaryMPSProduct / MPSBoundaryProduct  ct/common/boundary_times_mps.hpp:163-385
+//   SU2::gemm_trim_left / gemm_trim_right / gemm_trim / gemm
+//                                            ct/non-abelian/gemm.hpp:48-204
+//   SU2::lbtm_kernel + detail::lbtm          ct/non-abelian/apply_op.hpp:23-101,
+//                                            ct/non-abelian/micro_kernels.hpp:19-45
+//   SU2::rbtm_tasks + rbtm_axpy + task_axpy  ct/non-abelian/apply_op.hpp:114-232,
+//                                            ct/non-abelian/micro_kernels.hpp:143-198
+//   site_hamil_lbtm                          ct/non-abelian/site_hamil.hpp:57-147
+//   overlap_mpo_left_step / _right_step      ct/common/move_boundary.hpp:128-229
+//   reshape_left_to_right_new                mp_tensors/reshapes.h:178-221
+// but instead of performing each axpy/GEMM immediately they record it, grouped
+// by the output tile it writes, so the device executes every output exactly
+// once without atomics.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <stdexcept>
+#include <thread>
+#include <tuple>
+#include <unordered_map>
+
+#include "plan.hpp"
+
+namespace qcm {
+
+static thread_local std::string g_err;
+void set_error(const std::string& msg) { g_err = msg; }
+
+// ------------------------------------------------------------------ indices
+size_t Idx::position(Q c) const {
+    // descending order: binary search
+    size_t lo = 0, hi = d.size();
+    while (lo < hi) {
+        size_t mid = (lo + hi) / 2;
+        if (d[mid].first > c) lo = mid + 1; else hi = mid;
+    }
+    if (lo < d.size() && d[lo].first == c) return lo;
+    return d.size();
+}
+int64_t Idx::size_of(Q c) const {
+    size_t p = position(c);
+    if (p == d.size()) throw std::runtime_error("charge not in index");
+    return d[p].second;
+}
+void Idx::insert(Q c, int64_t s) {
+    size_t pos = 0;
+    while (pos < d.size() && !(d[pos].first < c)) ++pos;
+    d.insert(d.begin() + pos, {c, s});
+}
+void Idx::sort() {
+    std::stable_sort(d.begin(), d.end(), [](const std::pair<Q, int64_t>& a, const std::pair<Q, int64_t>& b) {
+        return a.first > b.first;
+    });
+}
+Idx index_product(const Idx& a, const Idx& b) {
+    std::map<Q, int64_t> acc;
+    for (auto& x : a.d)
+        for (auto& y : b.d) acc[fuse(x.first, y.first)] += x.second * y.second;
+    Idx r;
+    for (auto it = acc.rbegin(); it != acc.rend(); ++it) r.d.push_back({it->first, it->second});
+    return r;
+}
+Idx adjoin(const Idx& a) {
+    Idx r;
+    for (auto& x : a.d) r.d.push_back({neg(x.first), x.second});
+    r.sort();
+    return r;
+}
+void common_subset(Idx& a, Idx& b) {
+    Idx na, nb;
+    for (auto& x : a.d)
+        if (b.has(x.first)) na.d.push_back(x);
+    for (auto& x : b.d)
+        if (na.has(x.first)) nb.d.push_back(x);
+    a = na;
+    b = nb;
+}
+PB::PB(const Idx& a, const Idx& b, bool neg_first) {
+    for (auto& x : a.d)
+        for (auto& y : b.d) {
+            Q pc = neg_first ? fuse(neg(x.first), y.first) : fuse(x.first, y.first);
+            int64_t cur = sizes.count(pc) ? sizes[pc] : 0;
+            keys[{x.first, y.first}] = cur;
+            sizes[pc] = cur + x.second * y.second;
+        }
+}
+int64_t PB::operator()(Q a, Q b) const {
+    auto it = keys.find({a, b});
+    if (it == keys.end()) throw std::runtime_error("product basis key missing");
+    return it->second;
+}
+int64_t PB::size(Q c) const {
+    auto it = sizes.find(c);
+    if (it == sizes.end()) throw std::runtime_error("product basis sector missing");
+    return it->second;
+}
+
+static bool key_gt(const Blk& a, Q lc, Q rc) { return a.lc > lc || (a.lc == lc && a.rc > rc); }
+
+size_t BM::find(Q lc, Q rc) const {
+    size_t lo = 0, hi = b.size();
+    while (lo < hi) {
+        size_t mid = (lo + hi) / 2;
+        if (key_gt(b[mid], lc, rc)) lo = mid + 1; else hi = mid;
+    }
+    if (lo < b.size() && b[lo].lc == lc && b[lo].rc == rc) return lo;
+    return b.size();
+}
+size_t BM::left_lower_bound(Q lc) const {
+    size_t lo = 0, hi = b.size();
+    while (lo < hi) {
+        size_t mid = (lo + hi) / 2;
+        if (b[mid].lc > lc) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+size_t BM::insert(Blk x) {
+    size_t lo = 0, hi = b.size();
+    while (lo < hi) {
+        size_t mid = (lo + hi) / 2;
+        if (key_gt(b[mid], x.lc, x.rc)) lo = mid + 1; else hi = mid;
+    }
+    b.insert(b.begin() + lo, x);
+    return lo;
+}
+int64_t BM::assign_offsets(int64_t base) {
+    for (auto& x : b) {
+        x.off = base;
+        base += x.rows * x.cols;
+    }
+    return base;
+}
+
+// ------------------------------------------------------------------ Wigner symbols (Racah)
+static long double lfact(int n) {
+    static std::vector<long double> t;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        t.resize(400);
+        t[0] = 1.0L;
+        for (int i = 1; i < 400; ++i) t[i] = t[i - 1] * (long double)i;
+    });
+    if (n < 0 || n >= 400) throw std::runtime_error("factorial argument out of range");
+    return t[n];
+}
+static long double delta2(int a, int b, int c) {
+    return lfact((a + b - c) / 2) * lfact((a - b + c) / 2) * lfact((-a + b + c) / 2) / lfact((a + b + c) / 2 + 1);
+}
+static long double sixj_ld(int j1, int j2, int j3, int j4, int j5, int j6) {
+    if (!(triangle(j1, j2, j3) && triangle(j1, j5, j6) && triangle(j4, j2, j6) && triangle(j4, j5, j3))) return 0.0L;
+    int a1 = (j1 + j2 + j3) / 2, a2 = (j1 + j5 + j6) / 2, a3 = (j4 + j2 + j6) / 2, a4 = (j4 + j5 + j3) / 2;
+    int b1 = (j1 + j2 + j4 + j5) / 2, b2 = (j2 + j3 + j5 + j6) / 2, b3 = (j3 + j1 + j6 + j4) / 2;
+    int tmin = std::max(std::max(a1, a2), std::max(a3, a4)), tmax = std::min(b1, std::min(b2, b3));
+    long double s = 0.0L;
+    for (int t = tmin; t <= tmax; ++t) {
+        long double term = lfact(t + 1) / (lfact(t - a1) * lfact(t - a2) * lfact(t - a3) * lfact(t - a4) *
+                                           lfact(b1 - t) * lfact(b2 - t) * lfact(b3 - t));
+        s += (t % 2) ? -term : term;
+    }
+    long double pref = delta2(j1, j2, j3) * delta2(j1, j5, j6) * delta2(j4, j2, j6) * delta2(j4, j5, j3);
+    return s * sqrtl(pref);
+}
+double wigner6j(int a, int b, int c, int d, int e, int f) { return (double)sixj_ld(a, b, c, d, e, f); }
+double wigner9j(int a, int b, int c, int d, int e, int f, int g, int h, int i) {
+    if (!(triangle(a, b, c) && triangle(d, e, f) && triangle(g, h, i) && triangle(a, d, g) && triangle(b, e, h) &&
+          triangle(c, f, i)))
+        return 0.0;
+    int xmin = std::max(std::abs(a - i), std::max(std::abs(h - d), std::abs(b - f)));
+    int xmax = std::min(a + i, std::min(h + d, b + f));
+    long double tot = 0.0L;
+    for (int x = xmin; x <= xmax; x += 2) {
+        long double t = sixj_ld(a, d, g, h, i, x) * sixj_ld(b, e, h, d, x, f) * sixj_ld(c, f, i, x, a, b);
+        t *= (long double)(x + 1);
+        tot += (x % 2) ? -t : t;
+    }
+    return (double)tot;
+}
+static double mod_coupling(int a, int b, int c, int d, int e, int f, int g, int h, int i) {
+    return std::sqrt((g + 1.0) * (h + 1.0) * (c + 1.0) * (f + 1.0)) * wigner9j(a, b, c, d, e, f, g, h, i);
+}
+void set_coupling(int a, int b, int c, int d, int e, int f, int g, int h, int i, double init, double out[4]) {
+    double pref = std::sqrt((i + 1.0) * (a + 1.0) / ((g + 1.0) * (c + 1.0))) * init;
+    out[0] = out[1] = out[2] = out[3] = 0.0;
+    if (triangle(a, b, c)) {
+        out[0] = pref * mod_coupling(a, b, c, d, e, f, g, h, i);
+        out[2] = pref * mod_coupling(a, b, c, d, e, f, g, 2, i);
+    }
+    if (triangle(a, 2, c)) {
+        out[1] = pref * mod_coupling(a, 2, c, d, e, f, g, h, i);
+        out[3] = pref * mod_coupling(a, 2, c, d, e, f, g, 2, i);
+    }
+}
+double conjugate_correction(int lc, int rc, int S) {
+    int Sm = std::min(rc, lc), diff = rc - lc;
+    if (S == 0) return 1.0;
+    if (S == 1) {
+        if (diff > 0) return -std::sqrt((Sm + 1.0) / (Sm + 2.0));
+        if (diff < 0) return std::sqrt((Sm + 2.0) / (Sm + 1.0));
+        return 0.0;
+    }
+    if (S == 2) {
+        if (diff > 0) return -std::sqrt((Sm + 1.0) / (Sm + 3.0));
+        if (diff < 0) return -std::sqrt((Sm + 3.0) / (Sm + 1.0));
+        return 1.0;
+    }
+    throw std::runtime_error("hermitian conjugate for reduced tensor operators only implemented up to rank 1");
+}
+
+// ------------------------------------------------------------------ views of the C-ABI inputs
+static Idx read_index(const qcm_index_t* x) {
+    Idx r;
+    if (!x) throw std::runtime_error("null index");
+    for (int i = 0; i < x->n; ++i) r.d.push_back({Q(x->q[2 * i], x->q[2 * i + 1]), x->size[i]});
+    for (size_t i = 1; i < r.d.size(); ++i)
+        if (!(r.d[i - 1].first > r.d[i].first)) throw std::runtime_error("index not sorted descending");
+    return r;
+}
+static BM read_blocks(const qcm_blocks_t* x) {
+    BM r;
+    if (!x) throw std::runtime_error("null block list");
+    for (int k = 0; k < x->n; ++k) {
+        Blk b;
+        b.lc = Q(x->q[4 * k], x->q[4 * k + 1]);
+        b.rc = Q(x->q[4 * k + 2], x->q[4 * k + 3]);
+        b.rows = x->rows[k];
+        b.cols = x->cols[k];
+        b.off = x->off[k];
+        if (b.rows < 0 || b.cols < 0 || b.off < 0) throw std::runtime_error("negative block extent");
+        if (!r.b.empty() && !key_gt(r.b.back(), b.lc, b.rc)) throw std::runtime_error("blocks not in DualIndex order");
+        r.b.push_back(b);
+    }
+    return r;
+}
+static std::vector<BM> read_boundary(const qcm_boundary_t* x) {
+    if (!x) throw std::runtime_error("null boundary");
+    std::vector<BM> r(x->aux);
+    for (int b = 0; b < x->aux; ++b) {
+        for (int k = x->blk_ptr[b]; k < x->blk_ptr[b + 1]; ++k) {
+            Blk bl;
+            bl.lc = Q(x->q[4 * k], x->q[4 * k + 1]);
+            bl.rc = Q(x->q[4 * k + 2], x->q[4 * k + 3]);
+            bl.rows = x->rows[k];
+            bl.cols = x->cols[k];
+            bl.off = x->off[k];
+            if (!r[b].b.empty() && !key_gt(r[b].b.back(), bl.lc, bl.rc))
+                throw std::runtime_error("boundary blocks not in DualIndex order");
+            r[b].b.push_back(bl);
+        }
+    }
+    return r;
+}
+
+struct MpoV {
+    const qcm_mpo_t* m;
+    std::vector<std::vector<int>> row_b2;        // b1 -> sorted b2
+    std::vector<std::vector<int>> row_elem;      // b1 -> element ids (matching row_b2)
+    MpoV(const qcm_mpo_t* m_) : m(m_) {
+        if (!m) throw std::runtime_error("null mpo");
+        row_b2.resize(m->row_dim);
+        row_elem.resize(m->row_dim);
+        for (int b2 = 0; b2 < m->col_dim; ++b2)
+            for (int e = m->col_ptr[b2]; e < m->col_ptr[b2 + 1]; ++e) {
+                int b1 = m->row_of[e];
+                if (b1 < 0 || b1 >= m->row_dim) throw std::runtime_error("mpo row index out of range");
+                row_b2[b1].push_back(b2);
+                row_elem[b1].push_back(e);
+            }
+        for (int o = 0; o < m->n_ops; ++o)
+            for (int k = m->op_blk_ptr[o]; k < m->op_blk_ptr[o + 1]; ++k)
+                if (m->blk_ent_ptr[k] > m->blk_ent_ptr[k + 1]) throw std::runtime_error("bad op entries");
+    }
+    int lspin(int b) const { return m->left_spin[b]; }
+    int rspin(int b) const { return m->right_spin[b]; }
+    bool lskip(int b) const { return m->left_herm[b] < b; }
+    bool rskip(int b) const { return m->right_herm[b] < b; }
+    int lconj(int b) const { return m->left_herm[b]; }
+    int rconj(int b) const { return m->right_herm[b]; }
+    int lphase(int b) const { return m->left_phase[b]; }
+    int rphase(int b) const { return m->right_phase[b]; }
+};
+
+static inline int spin_case(int rs, int cs) {
+    if (rs == 2 && cs == 2) return 3;
+    if (rs == 2) return 1;
+    if (cs == 2) return 2;
+    return 0;
+}
+
+// ------------------------------------------------------------------ shared building blocks
+// Right-paired copy of a left-paired MPS (reshape_left_to_right_new), as gather tiles into `buf`.
+static BM plan_reshape_l2r(const Idx& phys, const Idx& left_i, const Idx& right_i, const BM& lp, int src_buf,
+                           int dst_buf, Stage& st, qcm_plan* P, int64_t& end) {
+    PB in_left(phys, left_i, false), out_right(phys, right_i, true);
+    BM rp;
+    struct Tile { Q ol, orr; int64_t col0, ld, rd; int64_t src; int64_t lds; };
+    std::vector<Tile> tiles;
+    for (auto& blk : lp.b) {
+        size_t r = right_i.position(blk.rc);
+        if (r == right_i.size()) continue;
+        Q in_r = right_i.d[r].first;
+        for (auto& ps : phys.d) {
+            size_t l = left_i.position(fuse(blk.lc, neg(ps.first)));
+            if (l == left_i.size()) continue;
+            Q ol = left_i.d[l].first, orr = fuse(neg(ps.first), in_r);
+            if (rp.find(ol, orr) == rp.b.size()) {
+                Blk nb;
+                nb.lc = ol;
+                nb.rc = orr;
+                nb.rows = left_i.d[l].second;
+                nb.cols = out_right.size(orr);
+                rp.insert(nb);
+            }
+            int64_t ilo = in_left(ps.first, ol), oro = out_right(ps.first, in_r);
+            int64_t ld = left_i.d[l].second, rd = right_i.d[r].second;
+            for (int64_t ss = 0; ss < ps.second; ++ss)
+                tiles.push_back({ol, orr, oro + ss * rd, ld, rd, blk.off + ilo + ss * ld, blk.rows});
+        }
+    }
+    end = rp.assign_offsets(0);
+    st.kind = ST_AXPY;
+    for (auto& t : tiles) {
+        const Blk& d = rp.b[rp.find(t.ol, t.orr)];
+        AxpyOut o;
+        o.dst_buf = dst_buf;
+        o.dst_off = d.off + t.col0 * d.rows;
+        o.ldd = d.rows;
+        o.rows = t.ld;
+        o.cols = t.rd;
+        o.t_begin = (int64_t)st.aterm.size();
+        st.aterm.push_back({src_buf, t.src, t.lds, 1.0});
+        o.t_end = (int64_t)st.aterm.size();
+        st.aout.push_back(o);
+        P->axpy_bytes += 16.0 * t.ld * t.rd;
+    }
+    return rp;
+}
+
+// K1: T[b1] = A(b1) . rp (BoundaryMPSProduct with gemm_trim_left).
+static std::vector<BM> plan_k1(const std::vector<BM>& L, const MpoV& W, bool herm, const BM& rp, int rp_buf,
+                               const Idx& ref, int t_buf, Stage& st, qcm_plan* P, int64_t& end) {
+    std::vector<BM> T(L.size());
+    struct Job { int b1; Q a, l; int64_t a_off, lda; int ta; double scale; int64_t M, K; size_t rpk; };
+    std::vector<Job> jobs;
+    for (size_t b1 = 0; b1 < L.size(); ++b1) {
+        std::vector<Job> Ab;
+        bool use_conj = herm && (int)b1 < W.m->row_dim && W.lskip((int)b1);
+        if (use_conj) {
+            const BM& src = L[W.lconj((int)b1)];
+            for (auto& x : src.b) {
+                double sc = conjugate_correction(x.lc.s, x.rc.s, W.lspin((int)b1)) * W.lphase((int)b1);
+                Ab.push_back({(int)b1, x.lc, x.rc, x.off, x.rows, 0, sc, x.rows, x.cols, 0});
+            }
+        } else {
+            for (auto& x : L[b1].b) Ab.push_back({(int)b1, x.rc, x.lc, x.off, x.rows, 1, 1.0, x.cols, x.rows, 0});
+        }
+        std::stable_sort(Ab.begin(), Ab.end(), [](const Job& p, const Job& q) {
+            return p.a > q.a || (p.a == q.a && p.l > q.l);
+        });
+        for (auto& j : Ab) {
+            if (!ref.has(j.a)) continue;
+            size_t it = rp.left_lower_bound(j.l);
+            for (; it < rp.b.size() && rp.b[it].lc == j.l; ++it) {
+                Blk nb;
+                nb.lc = j.a;
+                nb.rc = rp.b[it].rc;
+                nb.rows = j.M;
+                nb.cols = rp.b[it].cols;
+                if (T[b1].find(nb.lc, nb.rc) != T[b1].b.size()) throw std::runtime_error("duplicate T block");
+                T[b1].insert(nb);
+                Job jj = j;
+                jj.rpk = it;
+                jobs.push_back(jj);
+            }
+        }
+    }
+    int64_t base = 0;
+    for (auto& t : T) base = t.assign_offsets(base);
+    end = base;
+    st.kind = ST_GEMM;
+    for (auto& j : jobs) {
+        const Blk& rb = rp.b[j.rpk];
+        const Blk& c = T[j.b1].b[T[j.b1].find(j.a, rb.rc)];
+        GemmOut o;
+        o.c_buf = t_buf;
+        o.c_off = c.off;
+        o.ldc = c.rows;
+        o.M = c.rows;
+        o.N = c.cols;
+        o.s_begin = (int64_t)st.gseg.size();
+        GemmSeg s;
+        s.a_buf = QCM_BUF_LEFT;
+        s.ta = j.ta;
+        s.a_off = j.a_off;
+        s.lda = j.lda;
+        s.b_buf = rp_buf;
+        s.tb = 0;
+        s.b_off = rb.off;
+        s.ldb = rb.rows;
+        s.K = j.K;
+        s.alpha = j.scale;
+        if (rb.rows != j.K) throw std::runtime_error("K1 inner dimension mismatch");
+        st.gseg.push_back(s);
+        o.s_end = (int64_t)st.gseg.size();
+        st.gout.push_back(o);
+        P->gemm_flops += 2.0 * c.rows * c.cols * j.K;
+    }
+    return T;
+}
+
+// K2: contr[b2] = sum_{b1,op} couplings x stripes of T[b1]  (lbtm_kernel).
+static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const std::vector<int>& b2list,
+                               const Idx& right_i, const Idx& out_left_i, const PB& in_right_pb,
+                               const PB& out_left_pb, int t_buf, int c_buf, Stage& st, qcm_plan* P, int64_t& end) {
+    const qcm_mpo_t* m = W.m;
+    std::vector<BM> C(m->col_dim);
+    using TileKey = std::tuple<int, Q, Q, int64_t>;  // b2, out_l, out_r, row offset
+    struct TileKeyLess {
+        bool operator()(const TileKey& a, const TileKey& b) const {
+            if (std::get<0>(a) != std::get<0>(b)) return std::get<0>(a) < std::get<0>(b);
+            if (std::get<1>(a) != std::get<1>(b)) return std::get<1>(a) > std::get<1>(b);
+            if (std::get<2>(a) != std::get<2>(b)) return std::get<2>(a) > std::get<2>(b);
+            return std::get<3>(a) < std::get<3>(b);
+        }
+    };
+    struct TileVal { int64_t rows, cols; std::vector<AxpyTerm> terms; };
+    std::map<TileKey, TileVal, TileKeyLess> tiles;
+    for (int b2 : b2list) {
+        int ap = W.rspin(b2);
+        for (int e = m->col_ptr[b2]; e < m->col_ptr[b2 + 1]; ++e) {
+            int b1 = m->row_of[e];
+            if (b1 >= (int)T.size()) throw std::runtime_error("mpo row beyond boundary aux dimension");
+            int a = W.lspin(b1);
+            for (int tt = m->term_ptr[e]; tt < m->term_ptr[e + 1]; ++tt) {
+                int op = m->term_op[tt];
+                double scale = m->term_scale[tt];
+                int k = m->op_spin[op];
+                for (auto& tb : T[b1].b) {
+                    Q lc = tb.lc, rc = tb.rc, mc = tb.rc;
+                    int64_t l_size = tb.rows;
+                    for (int wb = m->op_blk_ptr[op]; wb < m->op_blk_ptr[op + 1]; ++wb) {
+                        Q pin(m->blk_q[4 * wb], m->blk_q[4 * wb + 1]), pout(m->blk_q[4 * wb + 2], m->blk_q[4 * wb + 3]);
+                        Q out_r = fuse(rc, pin);
+                        size_t rb = right_i.position(out_r);
+                        if (rb == right_i.size()) continue;
+                        Q out_l = fuse(lc, pout);
+                        if (!triangle(out_r.s, ap, out_l.s)) continue;
+                        if (!out_left_i.has(out_l)) continue;
+                        int64_t r_size = right_i.d[rb].second;
+                        if (C[b2].find(out_l, out_r) == C[b2].b.size()) {
+                            Blk nb;
+                            nb.lc = out_l;
+                            nb.rc = out_r;
+                            nb.rows = out_left_i.size_of(out_l);
+                            nb.cols = r_size;
+                            C[b2].insert(nb);
+                        }
+                        int i = lc.s, ip = out_l.s, j = mc.s, jp = out_r.s;
+                        double cpl[4];
+                        set_coupling(j, std::abs(j - jp), jp, a, k, ap, i, std::abs(i - ip), ip, scale, cpl);
+                        int64_t iro = in_right_pb(pin, out_r), olo = out_left_pb(pout, lc);
+                        for (int en = m->blk_ent_ptr[wb]; en < m->blk_ent_ptr[wb + 1]; ++en) {
+                            int ss1 = m->ent[4 * en], ss2 = m->ent[4 * en + 1];
+                            double alfa = m->ent_coeff[en] * cpl[spin_case(m->ent[4 * en + 2], m->ent[4 * en + 3])];
+                            if (alfa == 0.0) continue;
+                            TileKey key(b2, out_l, out_r, olo + ss2 * l_size);
+                            auto& tv = tiles[key];
+                            tv.rows = l_size;
+                            tv.cols = r_size;
+                            tv.terms.push_back({t_buf, tb.off + (iro + (int64_t)ss1 * r_size) * l_size, l_size, alfa});
+                            P->axpy_flops += 2.0 * l_size * r_size;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    int64_t base = 0;
+    for (auto& c : C) base = c.assign_offsets(base);
+    end = base;
+    st.kind = ST_AXPY;
+    for (auto& kv : tiles) {
+        int b2 = std::get<0>(kv.first);
+        const BM& cb = C[b2];
+        const Blk& d = cb.b[cb.find(std::get<1>(kv.first), std::get<2>(kv.first))];
+        AxpyOut o;
+        o.dst_buf = c_buf;
+        o.dst_off = d.off + std::get<3>(kv.first);
+        o.ldd = d.rows;
+        o.rows = kv.second.rows;
+        o.cols = kv.second.cols;
+        o.t_begin = (int64_t)st.aterm.size();
+        for (auto& t : kv.second.terms) st.aterm.push_back(t);
+        o.t_end = (int64_t)st.aterm.size();
+        st.aout.push_back(o);
+        P->axpy_bytes += 8.0 * o.rows * o.cols * (double)(kv.second.terms.size() + 1);
+    }
+    return C;
+}
+
+static void finalize_boundary_layout(qcm_plan* P, std::vector<BM>& out) {
+    int64_t base = 0;
+    P->out_blk_ptr.assign(1, 0);
+    for (auto& bm : out) {
+        base = bm.assign_offsets(base);
+        for (auto& b : bm.b) P->out_blocks.push_back(b);
+        P->out_blk_ptr.push_back((int32_t)P->out_blocks.size());
+    }
+    P->out_elems = base;
+}
+
+// ------------------------------------------------------------------ plan kinds
+static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& right_i, const BM& psi,
+                             const std::vector<BM>& L, const std::vector<BM>& R, const MpoV& W, bool herm) {
+    auto* P = new qcm_plan();
+    P->kind = PK_SIGMA;
+    const qcm_mpo_t* m = W.m;
+    if ((int)L.size() != m->row_dim || (int)R.size() != m->col_dim)
+        throw std::runtime_error("boundary aux dimensions do not match the MPO");
+    // output sigma: same layout as psi
+    int64_t psi_end = 0;
+    for (auto& b : psi.b) psi_end = std::max(psi_end, b.off + b.rows * b.cols);
+    P->out_elems = psi_end;
+
+    Idx out_left_i = index_product(phys, left_i);
+    Idx rib = right_i;
+    common_subset(out_left_i, rib);
+    PB out_left_pb(phys, left_i, false), in_right_pb(phys, right_i, true);
+
+    Stage z0; z0.kind = ST_ZERO; z0.zbuf = QCM_BUF_S0;
+    Stage s0; int64_t rp_end = 0;
+    BM rp = plan_reshape_l2r(phys, left_i, right_i, psi, QCM_BUF_KET, QCM_BUF_S0, s0, P, rp_end);
+    z0.zlen = rp_end;
+    Idx ref;
+    for (auto& b : rp.b) ref.d.push_back({b.lc, b.rows});
+    Stage s1; int64_t t_end = 0;
+    std::vector<BM> T = plan_k1(L, W, herm, rp, QCM_BUF_S0, ref, QCM_BUF_S1, s1, P, t_end);
+    std::vector<int> b2list;
+    for (int b2 = 0; b2 < m->col_dim; ++b2) b2list.push_back(b2);
+    Stage s2; int64_t c_end = 0;
+    std::vector<BM> C = plan_k2(T, W, b2list, right_i, out_left_i, in_right_pb, out_left_pb, QCM_BUF_S1,
+                                QCM_BUF_S2, s2, P, c_end);
+    Stage z2; z2.kind = ST_ZERO; z2.zbuf = QCM_BUF_S2; z2.zlen = c_end;
+    // K3: sigma(al,al) = sum_b2 contr[b2](al,ar) . R'[b2](ar,al)  (gemm_trim)
+    Stage s3; s3.kind = ST_GEMM;
+    for (auto& ob : psi.b) {
+        if (!(ob.lc == ob.rc)) throw std::runtime_error("psi layout is not block diagonal (left-paired)");
+        Q al = ob.lc;
+        GemmOut o;
+        o.c_buf = QCM_BUF_OUT;
+        o.c_off = ob.off;
+        o.ldc = ob.rows;
+        o.M = ob.rows;
+        o.N = ob.cols;
+        o.s_begin = (int64_t)s3.gseg.size();
+        for (int b2 = 0; b2 < m->col_dim; ++b2) {
+            const BM& cb = C[b2];
+            size_t it = cb.left_lower_bound(al);
+            for (; it < cb.b.size() && cb.b[it].lc == al; ++it) {
+                const Blk& a = cb.b[it];
+                Q ar = a.rc;
+                GemmSeg s;
+                s.a_buf = QCM_BUF_S2; s.ta = 0; s.a_off = a.off; s.lda = a.rows; s.K = a.cols;
+                if (herm && W.rskip(b2)) {
+                    const BM& rs = R[W.rconj(b2)];
+                    size_t k = rs.find(al, ar);
+                    if (k == rs.b.size()) continue;
+                    s.b_buf = QCM_BUF_RIGHT; s.tb = 1; s.b_off = rs.b[k].off; s.ldb = rs.b[k].rows;
+                    s.alpha = conjugate_correction(ar.s, al.s, W.rspin(b2)) * W.rphase(W.rconj(b2));
+                    if (rs.b[k].cols != a.cols || rs.b[k].rows != ob.cols)
+                        throw std::runtime_error("K3 dimension mismatch (adjoint)");
+                } else {
+                    const BM& rs = R[b2];
+                    size_t k = rs.find(ar, al);
+                    if (k == rs.b.size()) continue;
+                    s.b_buf = QCM_BUF_RIGHT; s.tb = 0; s.b_off = rs.b[k].off; s.ldb = rs.b[k].rows;
+                    s.alpha = 1.0;
+                    if (rs.b[k].rows != a.cols || rs.b[k].cols != ob.cols)
+                        throw std::runtime_error("K3 dimension mismatch");
+                }
+                if (a.rows != ob.rows) throw std::runtime_error("K3 row mismatch");
+                s3.gseg.push_back(s);
+                P->gemm_flops += 2.0 * ob.rows * ob.cols * a.cols;
+            }
+        }
+        o.s_end = (int64_t)s3.gseg.size();
+        s3.gout.push_back(o);
+    }
+    P->scratch[0] = rp_end;
+    P->scratch[1] = t_end;
+    P->scratch[2] = c_end;
+    P->stages.push_back(std::move(z0));
+    P->stages.push_back(std::move(s0));
+    P->stages.push_back(std::move(s1));
+    P->stages.push_back(std::move(z2));
+    P->stages.push_back(std::move(s2));
+    P->stages.push_back(std::move(s3));
+    return P;
+}
+
+static qcm_plan* build_bleft(const Idx& phys, const Idx& left_i, const Idx& right_i, const BM& mps,
+                             const std::vector<BM>& L, const MpoV& W, bool herm) {
+    auto* P = new qcm_plan();
+    P->kind = PK_BLEFT;
+    const qcm_mpo_t* m = W.m;
+    if ((int)L.size() != m->row_dim) throw std::runtime_error("left boundary aux dimension does not match the MPO");
+    Idx out_left_i = index_product(phys, left_i);
+    Idx rib = right_i;
+    common_subset(out_left_i, rib);
+    PB out_left_pb(phys, left_i, false), in_right_pb(phys, right_i, true);
+    Stage z0; z0.kind = ST_ZERO; z0.zbuf = QCM_BUF_S0;
+    Stage s0; int64_t rp_end = 0;
+    BM rp = plan_reshape_l2r(phys, left_i, right_i, mps, QCM_BUF_KET, QCM_BUF_S0, s0, P, rp_end);
+    z0.zlen = rp_end;
+    Idx ref;
+    for (auto& b : rp.b) ref.d.push_back({b.lc, b.rows});
+    Stage s1; int64_t t_end = 0;
+    std::vector<BM> T = plan_k1(L, W, herm, rp, QCM_BUF_S0, ref, QCM_BUF_S1, s1, P, t_end);
+    std::vector<int> b2list;
+    for (int b2 = 0; b2 < m->col_dim; ++b2)
+        if (!(herm && W.rskip(b2))) b2list.push_back(b2);
+    Stage s2; int64_t c_end = 0;
+    std::vector<BM> C = plan_k2(T, W, b2list, right_i, out_left_i, in_right_pb, out_left_pb, QCM_BUF_S1,
+                                QCM_BUF_S2, s2, P, c_end);
+    Stage z2; z2.kind = ST_ZERO; z2.zbuf = QCM_BUF_S2; z2.zlen = c_end;
+    // ret[b2] = SU2::gemm(transpose(contr[b2]), bra_lp, right_spin(b2))
+    std::vector<BM> out(m->col_dim);
+    struct Job { int b2; Q lc, rc; int64_t a_off, a_rows, a_cols; size_t bk; };
+    std::vector<Job> jobs;
+    for (int b2 : b2list) {
+        // transposed blocks in sorted order
+        std::vector<Blk> At;
+        for (auto& x : C[b2].b) { Blk t = x; std::swap(t.lc, t.rc); At.push_back(t); }
+        std::stable_sort(At.begin(), At.end(), [](const Blk& p, const Blk& q) {
+            return p.lc > q.lc || (p.lc == q.lc && p.rc > q.rc);
+        });
+        for (auto& a : At) {
+            Q ar = a.rc;  // out_l
+            size_t it = mps.left_lower_bound(ar);
+            for (; it < mps.b.size() && mps.b[it].lc == ar; ++it) {
+                if (!triangle(a.lc.s, W.rspin(b2), mps.b[it].rc.s)) continue;
+                Blk nb;
+                nb.lc = a.lc;
+                nb.rc = mps.b[it].rc;
+                nb.rows = a.cols;       // transposed: rows of A^T = cols of contr block
+                nb.cols = mps.b[it].cols;
+                if (out[b2].find(nb.lc, nb.rc) != out[b2].b.size()) throw std::runtime_error("duplicate L block");
+                out[b2].insert(nb);
+                jobs.push_back({b2, nb.lc, nb.rc, a.off, a.rows, a.cols, it});
+            }
+        }
+    }
+    finalize_boundary_layout(P, out);
+    Stage s3; s3.kind = ST_GEMM;
+    for (auto& j : jobs) {
+        const Blk& c = out[j.b2].b[out[j.b2].find(j.lc, j.rc)];
+        const Blk& bb = mps.b[j.bk];
+        GemmOut o;
+        o.c_buf = QCM_BUF_OUT; o.c_off = c.off; o.ldc = c.rows; o.M = c.rows; o.N = c.cols;
+        o.s_begin = (int64_t)s3.gseg.size();
+        GemmSeg s;
+        s.a_buf = QCM_BUF_S2; s.ta = 1; s.a_off = j.a_off; s.lda = j.a_rows;
+        s.b_buf = QCM_BUF_KET; s.tb = 0; s.b_off = bb.off; s.ldb = bb.rows;
+        s.K = j.a_rows; s.alpha = 1.0;
+        if (bb.rows != j.a_rows) throw std::runtime_error("left step inner dimension mismatch");
+        s3.gseg.push_back(s);
+        o.s_end = (int64_t)s3.gseg.size();
+        s3.gout.push_back(o);
+        P->gemm_flops += 2.0 * c.rows * c.cols * j.a_rows;
+    }
+    P->scratch[0] = rp_end;
+    P->scratch[1] = t_end;
+    P->scratch[2] = c_end;
+    P->stages.push_back(std::move(z0));
+    P->stages.push_back(std::move(s0));
+    P->stages.push_back(std::move(s1));
+    P->stages.push_back(std::move(z2));
+    P->stages.push_back(std::move(s2));
+    P->stages.push_back(std::move(s3));
+    return P;
+}
+
+static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& right_i, const BM& mps,
+                              const std::vector<BM>& R, const MpoV& W, bool herm) {
+    auto* P = new qcm_plan();
+    P->kind = PK_BRIGHT;
+    const qcm_mpo_t* m = W.m;
+    if ((int)R.size() != m->col_dim) throw std::runtime_error("right boundary aux dimension does not match the MPO");
+    Idx out_right_i = index_product(adjoin(phys), right_i);
+    Idx bli = left_i;
+    common_subset(out_right_i, bli);
+    PB in_left_pb(phys, left_i, false), out_right_pb(phys, right_i, true);
+    Idx ref;  // bra (left-paired) right basis
+    for (auto& b : mps.b) ref.d.push_back({b.rc, b.cols});
+    // t[b2] = mps_lp . R'[b2]  (gemm_trim_right)
+    std::vector<BM> t(m->col_dim);
+    struct Job { int b2; Q lc, rc; size_t ak; int64_t b_off, ldb; int tb; double sc; int64_t N; };
+    std::vector<Job> jobs;
+    for (int b2 = 0; b2 < m->col_dim; ++b2) {
+        bool use_conj = herm && W.rskip(b2);
+        std::vector<Blk> Bb;
+        std::vector<double> sc;
+        std::vector<int> tbv;
+        if (use_conj) {
+            const BM& src = R[W.rconj(b2)];
+            for (auto& x : src.b) { Blk tt = x; std::swap(tt.lc, tt.rc); Bb.push_back(tt); }
+        } else {
+            Bb = R[b2].b;
+        }
+        std::vector<size_t> order(Bb.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](size_t p, size_t q) {
+            return Bb[p].lc > Bb[q].lc || (Bb[p].lc == Bb[q].lc && Bb[p].rc > Bb[q].rc);
+        });
+        BM Bs;
+        for (size_t i : order) Bs.b.push_back(Bb[i]);
+        for (size_t ak = 0; ak < mps.b.size(); ++ak) {
+            const Blk& a = mps.b[ak];
+            size_t it = Bs.left_lower_bound(a.rc);
+            for (; it < Bs.b.size() && Bs.b[it].lc == a.rc; ++it) {
+                const Blk& bb = Bs.b[it];
+                if (!ref.has(bb.rc)) continue;
+                Blk nb;
+                nb.lc = a.lc;
+                nb.rc = bb.rc;
+                nb.rows = a.rows;
+                // conj: stored block is (rc, lc) of R[conj] with rows = its own rows -> N = stored rows
+                nb.cols = use_conj ? bb.rows : bb.cols;
+                if (t[b2].find(nb.lc, nb.rc) != t[b2].b.size()) throw std::runtime_error("duplicate t block");
+                t[b2].insert(nb);
+                double s = use_conj ? conjugate_correction(bb.lc.s, bb.rc.s, W.rspin(b2)) * W.rphase(W.rconj(b2)) : 1.0;
+                jobs.push_back({b2, nb.lc, nb.rc, ak, bb.off, bb.rows, use_conj ? 1 : 0, s, nb.cols});
+            }
+        }
+    }
+    int64_t t_end = 0;
+    for (auto& x : t) t_end = x.assign_offsets(t_end);
+    Stage s1; s1.kind = ST_GEMM;
+    for (auto& j : jobs) {
+        const Blk& c = t[j.b2].b[t[j.b2].find(j.lc, j.rc)];
+        const Blk& a = mps.b[j.ak];
+        GemmOut o;
+        o.c_buf = QCM_BUF_S1; o.c_off = c.off; o.ldc = c.rows; o.M = c.rows; o.N = c.cols;
+        o.s_begin = (int64_t)s1.gseg.size();
+        GemmSeg s;
+        s.a_buf = QCM_BUF_KET; s.ta = 0; s.a_off = a.off; s.lda = a.rows;
+        s.b_buf = QCM_BUF_RIGHT; s.tb = j.tb; s.b_off = j.b_off; s.ldb = j.ldb;
+        s.K = a.cols; s.alpha = j.sc;
+        s1.gseg.push_back(s);
+        o.s_end = (int64_t)s1.gseg.size();
+        s1.gout.push_back(o);
+        P->gemm_flops += 2.0 * c.rows * c.cols * a.cols;
+    }
+    // rbtm tasks into buf[b1](out_l, out_r)
+    using TileKey = std::tuple<int, Q, Q, int64_t>;  // b1, out_l, out_r, col offset
+    struct TileKeyLess {
+        bool operator()(const TileKey& a, const TileKey& b) const {
+            if (std::get<0>(a) != std::get<0>(b)) return std::get<0>(a) < std::get<0>(b);
+            if (std::get<1>(a) != std::get<1>(b)) return std::get<1>(a) > std::get<1>(b);
+            if (std::get<2>(a) != std::get<2>(b)) return std::get<2>(a) > std::get<2>(b);
+            return std::get<3>(a) < std::get<3>(b);
+        }
+    };
+    struct TileVal { int64_t rows, cols; std::vector<AxpyTerm> terms; };
+    std::map<TileKey, TileVal, TileKeyLess> tiles;
+    std::vector<BM> buf(m->row_dim);
+    MpoV const& Wv = W;
+    for (int b1 = 0; b1 < m->row_dim; ++b1) {
+        if (herm && Wv.lskip(b1)) continue;
+        int a = Wv.lspin(b1);
+        for (size_t r = 0; r < Wv.row_b2[b1].size(); ++r) {
+            int b2 = Wv.row_b2[b1][r];
+            int e = Wv.row_elem[b1][r];
+            int ap = Wv.rspin(b2);
+            for (int tt = m->term_ptr[e]; tt < m->term_ptr[e + 1]; ++tt) {
+                int op = m->term_op[tt];
+                double scale = m->term_scale[tt];
+                int k = m->op_spin[op];
+                for (auto& tb : t[b2].b) {
+                    Q lc = tb.lc, rc = tb.rc, mc = tb.lc;
+                    for (int wb = m->op_blk_ptr[op]; wb < m->op_blk_ptr[op + 1]; ++wb) {
+                        Q pin(m->blk_q[4 * wb], m->blk_q[4 * wb + 1]), pout(m->blk_q[4 * wb + 2], m->blk_q[4 * wb + 3]);
+                        Q out_l = fuse(lc, neg(pin));
+                        size_t lb = left_i.position(out_l);
+                        if (lb == left_i.size()) continue;
+                        Q out_r = fuse(rc, neg(pout));
+                        if (!triangle(out_l.s, a, out_r.s)) continue;
+                        if (!out_right_i.has(out_r)) continue;
+                        int64_t l_size = left_i.d[lb].second;
+                        int i = out_r.s, ip = rc.s, j = out_l.s, jp = mc.s;
+                        double cpl[4];
+                        set_coupling(j, std::abs(j - jp), jp, a, k, ap, i, std::abs(i - ip), ip, scale, cpl);
+                        int64_t ilo = in_left_pb(pin, out_l), oro = out_right_pb(pout, rc);
+                        int64_t r_size = tb.cols;
+                        if (buf[b1].find(out_l, out_r) == buf[b1].b.size()) {
+                            Blk nb;
+                            nb.lc = out_l; nb.rc = out_r; nb.rows = l_size; nb.cols = out_right_i.size_of(out_r);
+                            buf[b1].insert(nb);
+                        }
+                        for (int en = m->blk_ent_ptr[wb]; en < m->blk_ent_ptr[wb + 1]; ++en) {
+                            int ss1 = m->ent[4 * en], ss2 = m->ent[4 * en + 1];
+                            double alfa = m->ent_coeff[en] * cpl[spin_case(m->ent[4 * en + 2], m->ent[4 * en + 3])];
+                            if (alfa == 0.0) continue;
+                            TileKey key(b1, out_l, out_r, oro + (int64_t)ss2 * r_size);
+                            auto& tv = tiles[key];
+                            tv.rows = l_size;
+                            tv.cols = r_size;
+                            tv.terms.push_back({QCM_BUF_S1, tb.off + ilo + (int64_t)ss1 * l_size, tb.rows, alfa});
+                            P->axpy_flops += 2.0 * l_size * r_size;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    int64_t b_end = 0;
+    for (auto& x : buf) b_end = x.assign_offsets(b_end);
+    Stage z2; z2.kind = ST_ZERO; z2.zbuf = QCM_BUF_S2; z2.zlen = b_end;
+    Stage s2; s2.kind = ST_AXPY;
+    for (auto& kv : tiles) {
+        int b1 = std::get<0>(kv.first);
+        const Blk& d = buf[b1].b[buf[b1].find(std::get<1>(kv.first), std::get<2>(kv.first))];
+        AxpyOut o;
+        o.dst_buf = QCM_BUF_S2;
+        o.dst_off = d.off + std::get<3>(kv.first) * d.rows;
+        o.ldd = d.rows;
+        o.rows = kv.second.rows;
+        o.cols = kv.second.cols;
+        o.t_begin = (int64_t)s2.aterm.size();
+        for (auto& x : kv.second.terms) s2.aterm.push_back(x);
+        o.t_end = (int64_t)s2.aterm.size();
+        s2.aout.push_back(o);
+        P->axpy_bytes += 8.0 * o.rows * o.cols * (double)(kv.second.terms.size() + 1);
+    }
+    // bra right-paired copy for the final product
+    Stage z0; z0.kind = ST_ZERO; z0.zbuf = QCM_BUF_S0;
+    Stage s0; int64_t rp_end = 0;
+    BM rp = plan_reshape_l2r(phys, left_i, right_i, mps, QCM_BUF_KET, QCM_BUF_S0, s0, P, rp_end);
+    z0.zlen = rp_end;
+    // ret[b1] = SU2::gemm(buf[b1], transpose(bra_rp), left_spin(b1))
+    std::vector<BM> out(m->row_dim);
+    struct J3 { int b1; Q lc, rc; int64_t a_off, a_rows, a_cols; size_t bk; };
+    std::vector<J3> j3;
+    for (int b1 = 0; b1 < m->row_dim; ++b1) {
+        for (auto& a : buf[b1].b) {
+            Q ar = a.rc;
+            size_t k = rp.find(ar, ar);
+            if (k == rp.b.size()) continue;
+            if (!triangle(a.lc.s, Wv.lspin(b1), ar.s)) continue;
+            Blk nb;
+            nb.lc = a.lc; nb.rc = ar; nb.rows = a.rows; nb.cols = rp.b[k].rows;
+            out[b1].insert(nb);
+            if (rp.b[k].cols != a.cols) throw std::runtime_error("right step inner dimension mismatch");
+            j3.push_back({b1, nb.lc, nb.rc, a.off, a.rows, a.cols, k});
+        }
+    }
+    finalize_boundary_layout(P, out);
+    Stage s3; s3.kind = ST_GEMM;
+    for (auto& j : j3) {
+        const Blk& c = out[j.b1].b[out[j.b1].find(j.lc, j.rc)];
+        const Blk& bb = rp.b[j.bk];
+        GemmOut o;
+        o.c_buf = QCM_BUF_OUT; o.c_off = c.off; o.ldc = c.rows; o.M = c.rows; o.N = c.cols;
+        o.s_begin = (int64_t)s3.gseg.size();
+        GemmSeg s;
+        s.a_buf = QCM_BUF_S2; s.ta = 0; s.a_off = j.a_off; s.lda = j.a_rows;
+        s.b_buf = QCM_BUF_S0; s.tb = 1; s.b_off = bb.off; s.ldb = bb.rows;
+        s.K = j.a_cols; s.alpha = 1.0;
+        s3.gseg.push_back(s);
+        o.s_end = (int64_t)s3.gseg.size();
+        s3.gout.push_back(o);
+        P->gemm_flops += 2.0 * c.rows * c.cols * j.a_cols;
+    }
+    P->scratch[0] = rp_end;
+    P->scratch[1] = t_end;
+    P->scratch[2] = b_end;
+    P->stages.push_back(std::move(s1));
+    P->stages.push_back(std::move(z2));
+    P->stages.push_back(std::move(s2));
+    P->stages.push_back(std::move(z0));
+    P->stages.push_back(std::move(s0));
+    P->stages.push_back(std::move(s3));
+    return P;
+}
+
+}  // namespace qcm
+
+// ------------------------------------------------------------------ C entry points (host part)
+using namespace qcm;
+
+extern "C" {
+
+const char* qcm_last_error(void) { return g_err.c_str(); }
+int qcm_version(void) { return 100; }
+
+int qcm_plan_sigma(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                   const qcm_blocks_t* psi, const qcm_boundary_t* left, const qcm_boundary_t* right,
+                   const qcm_mpo_t* mpo, int32_t hermitian, qcm_plan** plan) {
+    if (!plan) { set_error("null plan pointer"); return QCM_E_INVALID; }
+    try {
+        MpoV W(mpo);
+        *plan = build_sigma(read_index(phys), read_index(left_i), read_index(right_i), read_blocks(psi),
+                            read_boundary(left), read_boundary(right), W, hermitian != 0);
+        return QCM_OK;
+    } catch (const std::exception& e) {
+        set_error(std::string("qcm_plan_sigma: ") + e.what());
+        *plan = nullptr;
+        return QCM_E_INVALID;
+    }
+}
+
+int qcm_plan_boundary_left(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                           const qcm_blocks_t* mps, const qcm_boundary_t* left, const qcm_mpo_t* mpo,
+                           int32_t hermitian, qcm_plan** plan) {
+    if (!plan) { set_error("null plan pointer"); return QCM_E_INVALID; }
+    try {
+        MpoV W(mpo);
+        *plan = build_bleft(read_index(phys), read_index(left_i), read_index(right_i), read_blocks(mps),
+                            read_boundary(left), W, hermitian != 0);
+        return QCM_OK;
+    } catch (const std::exception& e) {
+        set_error(std::string("qcm_plan_boundary_left: ") + e.what());
+        *plan = nullptr;
+        return QCM_E_INVALID;
+    }
+}
+
+int qcm_plan_boundary_right(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                            const qcm_blocks_t* mps, const qcm_boundary_t* right, const qcm_mpo_t* mpo,
+                            int32_t hermitian, qcm_plan** plan) {
+    if (!plan) { set_error("null plan pointer"); return QCM_E_INVALID; }
+    try {
+        MpoV W(mpo);
+        *plan = build_bright(read_index(phys), read_index(left_i), read_index(right_i), read_blocks(mps),
+                             read_boundary(right), W, hermitian != 0);
+        return QCM_OK;
+    } catch (const std::exception& e) {
+        set_error(std::string("qcm_plan_boundary_right: ") + e.what());
+        *plan = nullptr;
+        return QCM_E_INVALID;
+    }
+}
+
+int qcm_plan_sizes(const qcm_plan* p, int64_t* out_elems, int64_t* scratch3) {
+    if (!p) { set_error("null plan"); return QCM_E_INVALID; }
+    if (out_elems) *out_elems = p->out_elems;
+    if (scratch3) for (int i = 0; i < 3; ++i) scratch3[i] = p->scratch[i];
+    return QCM_OK;
+}
+
+int qcm_plan_work(const qcm_plan* p, double* gf, double* af, double* ab, int32_t* launches) {
+    if (!p) { set_error("null plan"); return QCM_E_INVALID; }
+    if (gf) *gf = p->gemm_flops;
+    if (af) *af = p->axpy_flops;
+    if (ab) *ab = p->axpy_bytes;
+    if (launches) {
+        int n = 0;
+        for (auto& s : p->stages) {
+            if (s.kind == ST_ZERO) { if (s.zlen > 0) ++n; }
+            else if ((s.kind == ST_AXPY && !s.aout.empty()) || (s.kind == ST_GEMM && !s.gout.empty())) ++n;
+        }
+        *launches = n;
+    }
+    return QCM_OK;
+}
+
+int qcm_plan_out_layout(const qcm_plan* p, int32_t* aux, int32_t* nblocks, int32_t* blk_ptr, int32_t* q,
+                        int64_t* rows, int64_t* cols, int64_t* off) {
+    if (!p) { set_error("null plan"); return QCM_E_INVALID; }
+    if (p->kind == PK_SIGMA) { set_error("sigma plans have no boundary output layout"); return QCM_E_STATE; }
+    if (aux) *aux = (int32_t)p->out_blk_ptr.size() - 1;
+    if (nblocks) *nblocks = (int32_t)p->out_blocks.size();
+    if (blk_ptr) for (size_t i = 0; i < p->out_blk_ptr.size(); ++i) blk_ptr[i] = p->out_blk_ptr[i];
+    for (size_t k = 0; k < p->out_blocks.size(); ++k) {
+        const Blk& b = p->out_blocks[k];
+        if (q) { q[4 * k] = b.lc.n; q[4 * k + 1] = b.lc.s; q[4 * k + 2] = b.rc.n; q[4 * k + 3] = b.rc.s; }
+        if (rows) rows[k] = b.rows;
+        if (cols) cols[k] = b.cols;
+        if (off) off[k] = b.off;
+    }
+    return QCM_OK;
+}
+
+int qcm_plan_num_stages(const qcm_plan* p, int32_t* n) {
+    if (!p || !n) { set_error("null argument"); return QCM_E_INVALID; }
+    *n = (int32_t)p->stages.size();
+    return QCM_OK;
+}
+
+int qcm_plan_stage_info(const qcm_plan* p, int32_t s, int32_t* kind, int64_t* n_out, int64_t* n_terms) {
+    if (!p || s < 0 || s >= (int32_t)p->stages.size()) { set_error("bad stage"); return QCM_E_INVALID; }
+    const Stage& st = p->stages[s];
+    if (kind) *kind = st.kind;
+    if (st.kind == ST_AXPY) {
+        if (n_out) *n_out = (int64_t)st.aout.size();
+        if (n_terms) *n_terms = (int64_t)st.aterm.size();
+    } else if (st.kind == ST_GEMM) {
+        if (n_out) *n_out = (int64_t)st.gout.size();
+        if (n_terms) *n_terms = (int64_t)st.gseg.size();
+    } else {
+        if (n_out) *n_out = st.zbuf;
+        if (n_terms) *n_terms = st.zlen;
+    }
+    return QCM_OK;
+}
+
+int qcm_plan_stage_axpy(const qcm_plan* p, int32_t s, int64_t* od, int64_t* td, double* ta) {
+    if (!p || s < 0 || s >= (int32_t)p->stages.size() || p->stages[s].kind != ST_AXPY) {
+        set_error("not an axpy stage");
+        return QCM_E_INVALID;
+    }
+    const Stage& st = p->stages[s];
+    for (size_t i = 0; i < st.aout.size(); ++i) {
+        const AxpyOut& o = st.aout[i];
+        int64_t* d = od + 7 * i;
+        d[0] = o.dst_buf; d[1] = o.dst_off; d[2] = o.ldd; d[3] = o.rows; d[4] = o.cols; d[5] = o.t_begin; d[6] = o.t_end;
+    }
+    for (size_t i = 0; i < st.aterm.size(); ++i) {
+        td[3 * i] = st.aterm[i].src_buf;
+        td[3 * i + 1] = st.aterm[i].src_off;
+        td[3 * i + 2] = st.aterm[i].lds;
+        ta[i] = st.aterm[i].alpha;
+    }
+    return QCM_OK;
+}
+
+int qcm_plan_stage_gemm(const qcm_plan* p, int32_t s, int64_t* od, int64_t* sd, double* sa) {
+    if (!p || s < 0 || s >= (int32_t)p->stages.size() || p->stages[s].kind != ST_GEMM) {
+        set_error("not a gemm stage");
+        return QCM_E_INVALID;
+    }
+    const Stage& st = p->stages[s];
+    for (size_t i = 0; i < st.gout.size(); ++i) {
+        const GemmOut& o = st.gout[i];
+        int64_t* d = od + 7 * i;
+        d[0] = o.c_buf; d[1] = o.c_off; d[2] = o.ldc; d[3] = o.M; d[4] = o.N; d[5] = o.s_begin; d[6] = o.s_end;
+    }
+    for (size_t i = 0; i < st.gseg.size(); ++i) {
+        const GemmSeg& g = st.gseg[i];
+        int64_t* d = sd + 9 * i;
+        d[0] = g.a_buf; d[1] = g.ta; d[2] = g.a_off; d[3] = g.lda; d[4] = g.b_buf; d[5] = g.tb; d[6] = g.b_off;
+        d[7] = g.ldb; d[8] = g.K;
+        sa[i] = g.alpha;
+    }
+    return QCM_OK;
+}
+
+void qcm_plan_destroy(qcm_plan* p) {
+    if (!p) return;
+    for (auto& s : p->stages) free_stage_device(s);
+    delete p;
+}
+
+}  // extern "C"

@@ -1,0 +1,139 @@
+// Internal data structures of the contraction plans.
+//
+// A plan is a list of stages.  Each stage is one of
+//   ZERO  : clear a range of a buffer,
+//   AXPY  : gather-accumulate tiles  D = sum_t alpha_t * S_t   (overwrite),
+//   GEMM  : grouped block products   C = sum_s alpha_s * op(A_s) op(B_s) (overwrite).
+// Every output tile is owned by exactly one work item, so results do not
+// depend on scheduling (the reference accumulates under an OpenMP critical
+// section, ct/non-abelian/site_hamil.hpp:141-143, whose order varies).
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "qcm_gb300.h"
+
+namespace qcm {
+
+struct Q {
+    int n = 0, s = 0;  // (N, 2S)
+    Q() = default;
+    Q(int n_, int s_) : n(n_), s(s_) {}
+    bool operator<(const Q& o) const { return n < o.n || (n == o.n && s < o.s); }
+    bool operator>(const Q& o) const { return o < *this; }
+    bool operator==(const Q& o) const { return n == o.n && s == o.s; }
+    bool operator!=(const Q& o) const { return !(*this == o); }
+};
+inline Q fuse(Q a, Q b) { return Q(a.n + b.n, a.s + b.s); }
+inline Q neg(Q a) { return Q(-a.n, -a.s); }
+inline bool triangle(int a, int b, int c) { return ((a + b + c) % 2 == 0) && std::abs(a - b) <= c && c <= a + b; }
+
+// Sorted-descending quantum-number index.
+struct Idx {
+    std::vector<std::pair<Q, int64_t>> d;
+    size_t size() const { return d.size(); }
+    size_t position(Q c) const;
+    bool has(Q c) const { return position(c) < d.size(); }
+    int64_t size_of(Q c) const;
+    void insert(Q c, int64_t s);
+    void sort();
+};
+Idx index_product(const Idx& a, const Idx& b);
+Idx adjoin(const Idx& a);
+void common_subset(Idx& a, Idx& b);
+
+struct PB {
+    std::map<std::pair<Q, Q>, int64_t> keys;
+    std::map<Q, int64_t> sizes;
+    PB(const Idx& a, const Idx& b, bool neg_first);
+    int64_t operator()(Q a, Q b) const;
+    int64_t size(Q c) const;
+};
+
+struct Blk {
+    Q lc, rc;
+    int64_t rows = 0, cols = 0, off = 0;
+};
+
+// Block list in DualIndex order (descending on (lc, rc)).
+struct BM {
+    std::vector<Blk> b;
+    size_t find(Q lc, Q rc) const;
+    size_t left_lower_bound(Q lc) const;
+    size_t insert(Blk x);  // returns position
+    int64_t assign_offsets(int64_t base);  // sequential offsets, returns end
+};
+
+struct AxpyOut {
+    int32_t dst_buf;
+    int64_t dst_off, ldd, rows, cols;
+    int64_t t_begin, t_end;
+};
+struct AxpyTerm {
+    int32_t src_buf;
+    int64_t src_off, lds;
+    double alpha;
+};
+struct GemmOut {
+    int32_t c_buf;
+    int64_t c_off, ldc, M, N;
+    int64_t s_begin, s_end;
+};
+struct GemmSeg {
+    int32_t a_buf, ta;
+    int64_t a_off, lda;
+    int32_t b_buf, tb;
+    int64_t b_off, ldb;
+    int64_t K;
+    double alpha;
+};
+
+enum StageKind { ST_AXPY = 0, ST_GEMM = 1, ST_ZERO = 2 };
+
+struct Stage {
+    int kind;
+    // ZERO
+    int32_t zbuf = 0;
+    int64_t zoff = 0, zlen = 0;
+    // AXPY
+    std::vector<AxpyOut> aout;
+    std::vector<AxpyTerm> aterm;
+    // GEMM
+    std::vector<GemmOut> gout;
+    std::vector<GemmSeg> gseg;
+    // device copies (owned)
+    void* d_a = nullptr;
+    void* d_b = nullptr;
+    void* d_c = nullptr;  // work list
+    int64_t n_work = 0;
+};
+
+enum PlanKind { PK_SIGMA = 0, PK_BLEFT = 1, PK_BRIGHT = 2 };
+
+}  // namespace qcm
+
+struct qcm_plan {
+    int kind;
+    std::vector<qcm::Stage> stages;
+    int64_t out_elems = 0;
+    int64_t scratch[3] = {0, 0, 0};
+    // output boundary layout (boundary plans)
+    std::vector<int32_t> out_blk_ptr;
+    std::vector<qcm::Blk> out_blocks;
+    double gemm_flops = 0, axpy_flops = 0, axpy_bytes = 0;
+    bool uploaded = false;
+    int device = -1;
+};
+
+namespace qcm {
+void set_error(const std::string& msg);
+double wigner6j(int, int, int, int, int, int);
+double wigner9j(int, int, int, int, int, int, int, int, int);
+void set_coupling(int a, int b, int c, int d, int e, int f, int g, int h, int i, double init, double out[4]);
+double conjugate_correction(int lc_spin, int rc_spin, int tensor_spin);
+void free_stage_device(Stage& st);
+}  // namespace qcm

@@ -1,0 +1,181 @@
+"""GPU engine mirroring the reference's ``contraction::Engine`` surface.
+
+``Engine.site_hamil2`` / ``overlap_mpo_left_step`` / ``overlap_mpo_right_step``
+take the same roles as ``contraction::Engine<Matrix, OtherMatrix, SU2U1>``
+(``dmrg/framework/dmrg/mp_tensors/contractions/non-abelian/engine.hpp:104-207``)
+and ``SiteProblem`` / ``ietl::mult`` (``mp_tensors/siteproblem.h:22-53``,
+``optimize/ietl_lanczos_solver.h:108-115``).  Tensors live on the GPU as one
+flat FP64 buffer per tensor with a host-side block layout; every contraction
+goes through a native plan of ``libqcm_gb300.so`` (no CPU path).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import native as N
+from .symmetry import Index
+
+
+def _require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("qcmaquis_gb300 engine needs a CUDA device (sm_103a); there is no CPU path")
+
+
+@dataclass
+class DeviceMPSTensor:
+    """An MPS tensor in left-paired layout on the device (``MPSTensor``)."""
+    phys_i: Index
+    left_i: Index
+    right_i: Index
+    layout: N.Layout
+    data: torch.Tensor  # float64, flat
+
+    @classmethod
+    def from_host(cls, t, device="cuda"):
+        """From an MPSTensor-like object with ``phys_i/left_i/right_i`` and a left-paired ``data``."""
+        lay = N.Layout.of(t.data)
+        flat = torch.from_numpy(lay.pack(t.data)).to(device)
+        return cls(t.phys_i, t.left_i, t.right_i, lay, flat)
+
+    def to_block_matrix(self):
+        return self.layout.unpack(self.data.detach().cpu().numpy())
+
+    def like(self, data: torch.Tensor) -> "DeviceMPSTensor":
+        return DeviceMPSTensor(self.phys_i, self.left_i, self.right_i, self.layout, data)
+
+    @property
+    def n(self) -> int:
+        return int(self.data.numel())
+
+
+@dataclass
+class DeviceBoundary:
+    """A boundary (one block matrix per MPO bond index) in one device arena."""
+    layout: N.BoundaryLayout
+    data: torch.Tensor
+
+    @classmethod
+    def from_host(cls, boundary, device="cuda"):
+        lay = N.BoundaryLayout.of(boundary)
+        flat = torch.from_numpy(lay.pack(boundary) if lay.size else np.zeros(1)).to(device)
+        return cls(lay, flat)
+
+    def to_host(self):
+        return self.layout.unpack(self.data.detach().cpu().numpy())
+
+
+def _ptr(t: Optional[torch.Tensor]) -> int:
+    return 0 if t is None else int(t.data_ptr())
+
+
+class Workspace:
+    """Grow-only scratch buffers for the three plan scratch slots."""
+
+    def __init__(self, device):
+        self.device = device
+        self.bufs = [None, None, None]
+
+    def get(self, sizes):
+        out = []
+        for i, s in enumerate(sizes):
+            s = max(int(s), 1)
+            b = self.bufs[i]
+            if b is None or b.numel() < s:
+                self.bufs[i] = None
+                b = torch.empty(s, dtype=torch.float64, device=self.device)
+                self.bufs[i] = b
+            out.append(b)
+        return out
+
+
+class Engine:
+    """Plan cache + execution of the SU2U1 contractions on one GPU."""
+
+    def __init__(self, device="cuda", precision: int = N.PREC_FP64, hermitian: bool = True):
+        _require_cuda()
+        N.lib()
+        self.device = torch.device(device)
+        self.precision = precision
+        self.hermitian = hermitian
+        self.ws = Workspace(self.device)
+        self._plans: Dict[tuple, N.Plan] = {}
+        self._mpo_cache: Dict[int, N.FMpo] = {}
+        self.launches = 0
+
+    # -- helpers ---------------------------------------------------------
+    def fmpo(self, mpo) -> N.FMpo:
+        f = self._mpo_cache.get(id(mpo))
+        if f is None or f.mpo is not mpo:
+            f = N.FMpo(mpo)
+            self._mpo_cache[id(mpo)] = f
+        return f
+
+    def _stream(self) -> int:
+        return int(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def sigma_plan(self, ket: DeviceMPSTensor, L: DeviceBoundary, R: DeviceBoundary, mpo) -> N.Plan:
+        key = ("s", id(ket.layout), id(L.layout), id(R.layout), id(mpo), self.hermitian)
+        p = self._plans.get(key)
+        if p is None:
+            p = N.plan_sigma(ket.phys_i, ket.left_i, ket.right_i, ket.layout, L.layout, R.layout, self.fmpo(mpo),
+                             self.hermitian)
+            p.upload()
+            p._keep = (ket.layout, L.layout, R.layout)
+            self._plans[key] = p
+        return p
+
+    def run(self, plan: N.Plan, ket=None, left=None, right=None, out=None, precision=None):
+        s0, s1, s2 = self.ws.get(plan.scratch)
+        plan.run([_ptr(ket), _ptr(left), _ptr(right), _ptr(out), _ptr(s0), _ptr(s1), _ptr(s2)],
+                 self.precision if precision is None else precision, self._stream())
+        self.launches += plan.launches
+
+    # -- Engine surface ----------------------------------------------------
+    def site_hamil2(self, ket: DeviceMPSTensor, L: DeviceBoundary, R: DeviceBoundary, mpo,
+                    out: Optional[torch.Tensor] = None, precision=None) -> DeviceMPSTensor:
+        """sigma = H_eff ket (``Engine::site_hamil2``); result in the ket's layout."""
+        p = self.sigma_plan(ket, L, R, mpo)
+        if out is None:
+            out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=self.device)
+        self.run(p, ket=ket.data, left=L.data, right=R.data, out=out, precision=precision)
+        return ket.like(out)
+
+    def overlap_mpo_left_step(self, mps: DeviceMPSTensor, L: DeviceBoundary, mpo) -> DeviceBoundary:
+        """L[i+1] from L[i], A[i], W[i] (``Engine::overlap_mpo_left_step``, bra = ket)."""
+        p = N.plan_boundary_left(mps.phys_i, mps.left_i, mps.right_i, mps.layout, L.layout, self.fmpo(mpo),
+                                 self.hermitian)
+        p.upload()
+        lay = p.out_layout()
+        out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=self.device)
+        self.run(p, ket=mps.data, left=L.data, out=out, precision=N.PREC_FP64)
+        return DeviceBoundary(lay, out)
+
+    def overlap_mpo_right_step(self, mps: DeviceMPSTensor, R: DeviceBoundary, mpo) -> DeviceBoundary:
+        """R[i] from R[i+1], B[i], W[i] (``Engine::overlap_mpo_right_step``, bra = ket)."""
+        p = N.plan_boundary_right(mps.phys_i, mps.left_i, mps.right_i, mps.layout, R.layout, self.fmpo(mpo),
+                                  self.hermitian)
+        p.upload()
+        lay = p.out_layout()
+        out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=self.device)
+        self.run(p, ket=mps.data, right=R.data, out=out, precision=N.PREC_FP64)
+        return DeviceBoundary(lay, out)
+
+
+class SiteProblem:
+    """``SiteProblem{left, right, mpo}`` with ``ietl::mult`` = ``apply``."""
+
+    def __init__(self, engine: Engine, left: DeviceBoundary, right: DeviceBoundary, mpo):
+        self.engine = engine
+        self.left = left
+        self.right = right
+        self.mpo = mpo
+
+    def apply(self, x: DeviceMPSTensor, out: Optional[torch.Tensor] = None) -> DeviceMPSTensor:
+        return self.engine.site_hamil2(x, self.left, self.right, self.mpo, out=out)
+
+
+__all__ = ["Engine", "SiteProblem", "DeviceMPSTensor", "DeviceBoundary"]

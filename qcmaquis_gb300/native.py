@@ -1,0 +1,371 @@
+"""ctypes binding of ``libqcm_gb300.so`` (the C ABI declared in ``include/qcm_gb300.h``).
+
+Loading fails loudly when the library is missing: the GPU path has no
+fallback.  The flatteners turn host-side layouts (``Index``, block lists,
+boundaries, ``MPOTensor``) into the plain arrays the ABI takes; the arrays
+are kept alive on the returned objects.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import List, Sequence
+
+import numpy as np
+
+from .symmetry import Index
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libqcm_gb300.so")
+
+QCM_BUF_KET, QCM_BUF_LEFT, QCM_BUF_RIGHT, QCM_BUF_OUT, QCM_BUF_S0, QCM_BUF_S1, QCM_BUF_S2 = range(7)
+QCM_NBUF = 7
+PREC_FP64, PREC_TF32, PREC_BF16X3 = 0, 1, 2
+
+i32p = C.POINTER(C.c_int32)
+i64p = C.POINTER(C.c_int64)
+f64p = C.POINTER(C.c_double)
+
+
+class CIndex(C.Structure):
+    _fields_ = [("n", C.c_int32), ("q", i32p), ("size", i64p)]
+
+
+class CBlocks(C.Structure):
+    _fields_ = [("n", C.c_int32), ("q", i32p), ("rows", i64p), ("cols", i64p), ("off", i64p)]
+
+
+class CBoundary(C.Structure):
+    _fields_ = [("aux", C.c_int32), ("blk_ptr", i32p), ("q", i32p), ("rows", i64p), ("cols", i64p), ("off", i64p)]
+
+
+class CMpo(C.Structure):
+    _fields_ = [("row_dim", C.c_int32), ("col_dim", C.c_int32),
+                ("left_spin", i32p), ("right_spin", i32p), ("left_herm", i32p), ("right_herm", i32p),
+                ("left_phase", i32p), ("right_phase", i32p),
+                ("col_ptr", i32p), ("row_of", i32p), ("term_ptr", i32p), ("term_op", i32p), ("term_scale", f64p),
+                ("n_ops", C.c_int32), ("op_spin", i32p), ("op_blk_ptr", i32p), ("blk_q", i32p),
+                ("blk_ent_ptr", i32p), ("ent", i32p), ("ent_coeff", f64p)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"native library {LIB_PATH} is missing: run __graft_entry__.build() (no CPU fallback)")
+    L = C.CDLL(LIB_PATH)
+    L.qcm_last_error.restype = C.c_char_p
+    L.qcm_version.restype = C.c_int
+    for name in ("qcm_plan_sigma",):
+        getattr(L, name).argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks), C.POINTER(CBoundary),
+                                                               C.POINTER(CBoundary), C.POINTER(CMpo), C.c_int32,
+                                                               C.POINTER(C.c_void_p)]
+    for name in ("qcm_plan_boundary_left", "qcm_plan_boundary_right"):
+        getattr(L, name).argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks), C.POINTER(CBoundary),
+                                                               C.POINTER(CMpo), C.c_int32, C.POINTER(C.c_void_p)]
+    L.qcm_plan_sizes.argtypes = [C.c_void_p, i64p, i64p]
+    L.qcm_plan_work.argtypes = [C.c_void_p, f64p, f64p, f64p, i32p]
+    L.qcm_plan_out_layout.argtypes = [C.c_void_p, i32p, i32p, i32p, i32p, i64p, i64p, i64p]
+    L.qcm_plan_num_stages.argtypes = [C.c_void_p, i32p]
+    L.qcm_plan_stage_info.argtypes = [C.c_void_p, C.c_int32, i32p, i64p, i64p]
+    L.qcm_plan_stage_axpy.argtypes = [C.c_void_p, C.c_int32, i64p, i64p, f64p]
+    L.qcm_plan_stage_gemm.argtypes = [C.c_void_p, C.c_int32, i64p, i64p, f64p]
+    L.qcm_plan_upload.argtypes = [C.c_void_p]
+    L.qcm_plan_run.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.c_int32, C.c_void_p]
+    L.qcm_plan_destroy.argtypes = [C.c_void_p]
+    L.qcm_plan_destroy.restype = None
+    L.qcm_dot.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+    L.qcm_nrm2.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+    L.qcm_axpby.argtypes = [C.c_double, C.c_void_p, C.c_double, C.c_void_p, C.c_int64, C.c_void_p]
+    L.qcm_lincomb.argtypes = [C.POINTER(C.c_void_p), f64p, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]
+    L.qcm_multi_dot.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+    _lib = L
+    return L
+
+
+def check(rc: int, what: str = ""):
+    if rc != 0:
+        msg = lib().qcm_last_error().decode()
+        raise RuntimeError(f"{what} failed ({rc}): {msg}")
+
+
+def _p(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
+
+
+# ------------------------------------------------------------------ flatteners
+class FIndex:
+    def __init__(self, idx: Index):
+        n = len(idx)
+        self.q = np.array([x for c, _ in idx for x in c], dtype=np.int32).reshape(-1)
+        if self.q.size == 0:
+            self.q = np.zeros(2, dtype=np.int32)
+        self.size = np.array([s for _, s in idx] or [0], dtype=np.int64)
+        self.c = CIndex(n, _p(self.q, i32p), _p(self.size, i64p))
+
+
+class Layout:
+    """Block list of one block-sparse tensor with sequential offsets."""
+
+    def __init__(self, keys: Sequence, shapes: Sequence, offsets=None):
+        self.keys = [tuple(k) for k in keys]
+        self.shapes = [tuple(int(x) for x in s) for s in shapes]
+        if offsets is None:
+            offsets = []
+            o = 0
+            for r, c in self.shapes:
+                offsets.append(o)
+                o += r * c
+        self.offsets = [int(o) for o in offsets]
+        self.size = max([o + r * c for o, (r, c) in zip(self.offsets, self.shapes)] or [0])
+        self._make_c()
+
+    def _make_c(self):
+        n = len(self.keys)
+        self.q = np.array([[k[0][0], k[0][1], k[1][0], k[1][1]] for k in self.keys] or [[0, 0, 0, 0]],
+                          dtype=np.int32).reshape(-1)
+        self.rows = np.array([s[0] for s in self.shapes] or [0], dtype=np.int64)
+        self.cols = np.array([s[1] for s in self.shapes] or [0], dtype=np.int64)
+        self.off = np.array(self.offsets or [0], dtype=np.int64)
+        self.c = CBlocks(n, _p(self.q, i32p), _p(self.rows, i64p), _p(self.cols, i64p), _p(self.off, i64p))
+
+    @classmethod
+    def of(cls, bm):
+        return cls(bm.keys, [b.shape for b in bm.blocks])
+
+    def pack(self, bm) -> np.ndarray:
+        out = np.zeros(self.size)
+        for k, o, (r, c) in zip(self.keys, self.offsets, self.shapes):
+            p = bm.find_block(*k)
+            if p < bm.n_blocks():
+                out[o:o + r * c] = np.asarray(bm.blocks[p]).ravel(order="F")
+        return out
+
+    def unpack(self, flat: np.ndarray):
+        from .block_matrix import BlockMatrix
+        bm = BlockMatrix()
+        for k, o, (r, c) in zip(self.keys, self.offsets, self.shapes):
+            bm.keys.append(k)
+            bm.blocks.append(np.asarray(flat[o:o + r * c]).reshape((r, c), order="F").copy())
+        return bm
+
+
+class BoundaryLayout:
+    """One block list per MPO bond index, all in one arena."""
+
+    def __init__(self, per_b: List[Layout] = None, *, blk_ptr=None, keys=None, shapes=None, offsets=None):
+        if per_b is not None:
+            keys, shapes, offsets, blk_ptr = [], [], [], [0]
+            base = 0
+            for lay in per_b:
+                for k, s in zip(lay.keys, lay.shapes):
+                    keys.append(k)
+                    shapes.append(s)
+                    offsets.append(base)
+                    base += s[0] * s[1]
+                blk_ptr.append(len(keys))
+        self.keys = [tuple(k) for k in keys]
+        self.shapes = [tuple(s) for s in shapes]
+        self.offsets = list(offsets)
+        self.blk_ptr = list(blk_ptr)
+        self.aux = len(self.blk_ptr) - 1
+        self.size = max([o + r * c for o, (r, c) in zip(self.offsets, self.shapes)] or [0])
+        n = len(self.keys)
+        self.q = np.array([[k[0][0], k[0][1], k[1][0], k[1][1]] for k in self.keys] or [[0, 0, 0, 0]],
+                          dtype=np.int32).reshape(-1)
+        self.rows = np.array([s[0] for s in self.shapes] or [0], dtype=np.int64)
+        self.cols = np.array([s[1] for s in self.shapes] or [0], dtype=np.int64)
+        self.off = np.array(self.offsets or [0], dtype=np.int64)
+        self.ptr = np.array(self.blk_ptr, dtype=np.int32)
+        self.c = CBoundary(self.aux, _p(self.ptr, i32p), _p(self.q, i32p), _p(self.rows, i64p),
+                           _p(self.cols, i64p), _p(self.off, i64p))
+
+    @classmethod
+    def of(cls, boundary):
+        return cls([Layout.of(bm) for bm in boundary])
+
+    def pack(self, boundary) -> np.ndarray:
+        out = np.zeros(self.size)
+        for b in range(self.aux):
+            bm = boundary[b]
+            for k in range(self.blk_ptr[b], self.blk_ptr[b + 1]):
+                key = self.keys[k]
+                p = bm.find_block(*key)
+                r, c = self.shapes[k]
+                if p < bm.n_blocks():
+                    out[self.offsets[k]:self.offsets[k] + r * c] = np.asarray(bm.blocks[p]).ravel(order="F")
+        return out
+
+    def unpack(self, flat: np.ndarray):
+        from .block_matrix import BlockMatrix
+        out = []
+        for b in range(self.aux):
+            bm = BlockMatrix()
+            for k in range(self.blk_ptr[b], self.blk_ptr[b + 1]):
+                r, c = self.shapes[k]
+                o = self.offsets[k]
+                bm.keys.append(self.keys[k])
+                bm.blocks.append(np.asarray(flat[o:o + r * c]).reshape((r, c), order="F").copy())
+            out.append(bm)
+        return out
+
+
+class FMpo:
+    """Flattened MPOTensor (see ``qcm_mpo_t``)."""
+
+    def __init__(self, mpo):
+        self.mpo = mpo
+        self.left_spin = np.array([s.get() for s in mpo.left_spins], dtype=np.int32)
+        self.right_spin = np.array([s.get() for s in mpo.right_spins], dtype=np.int32)
+        self.left_herm = np.array(mpo.herm.LeftHerm, dtype=np.int32)
+        self.right_herm = np.array(mpo.herm.RightHerm, dtype=np.int32)
+        self.left_phase = np.array(mpo.herm.LeftPhase, dtype=np.int32)
+        self.right_phase = np.array(mpo.herm.RightPhase, dtype=np.int32)
+        col_ptr, row_of, term_ptr, term_op, term_scale = [0], [], [0], [], []
+        used_ops = {}
+        for b2 in range(mpo.col_dim):
+            for b1 in mpo.column(b2):
+                row_of.append(b1)
+                for tag, scale in mpo.at(b1, b2):
+                    if tag not in used_ops:
+                        used_ops[tag] = len(used_ops)
+                    term_op.append(used_ops[tag])
+                    term_scale.append(scale)
+                term_ptr.append(len(term_op))
+            col_ptr.append(len(row_of))
+        op_spin, op_blk_ptr, blk_q, blk_ent_ptr, ent, ent_coeff = [], [0], [], [0], [], []
+        for tag, oid in sorted(used_ops.items(), key=lambda kv: kv[1]):
+            op = mpo.op(tag)
+            sp = mpo.sparse(tag)
+            op_spin.append(op.spin.get())
+            for (pin, pout), ents in zip(op.bm.keys, sp):
+                blk_q += [pin[0], pin[1], pout[0], pout[1]]
+                for (r, c, rs, cs, v) in ents:
+                    ent += [r, c, rs, cs]
+                    ent_coeff.append(v)
+                blk_ent_ptr.append(len(ent_coeff))
+            op_blk_ptr.append(len(blk_ent_ptr) - 1)
+        a32 = lambda x: np.array(x or [0], dtype=np.int32)
+        self.col_ptr = a32(col_ptr)
+        self.row_of = a32(row_of)
+        self.term_ptr = a32(term_ptr)
+        self.term_op = a32(term_op)
+        self.term_scale = np.array(term_scale or [0.0], dtype=np.float64)
+        self.op_spin = a32(op_spin)
+        self.op_blk_ptr = a32(op_blk_ptr)
+        self.blk_q = a32(blk_q)
+        self.blk_ent_ptr = a32(blk_ent_ptr)
+        self.ent = a32(ent)
+        self.ent_coeff = np.array(ent_coeff or [0.0], dtype=np.float64)
+        self.c = CMpo(mpo.row_dim, mpo.col_dim, _p(self.left_spin, i32p), _p(self.right_spin, i32p),
+                      _p(self.left_herm, i32p), _p(self.right_herm, i32p), _p(self.left_phase, i32p),
+                      _p(self.right_phase, i32p), _p(self.col_ptr, i32p), _p(self.row_of, i32p),
+                      _p(self.term_ptr, i32p), _p(self.term_op, i32p), _p(self.term_scale, f64p),
+                      len(op_spin), _p(self.op_spin, i32p), _p(self.op_blk_ptr, i32p), _p(self.blk_q, i32p),
+                      _p(self.blk_ent_ptr, i32p), _p(self.ent, i32p), _p(self.ent_coeff, f64p))
+
+
+# ------------------------------------------------------------------ plans
+class Plan:
+    """Owner of a native plan handle."""
+
+    def __init__(self, handle, kind: str):
+        self.h = handle
+        self.kind = kind
+        out = C.c_int64()
+        sc = (C.c_int64 * 3)()
+        check(lib().qcm_plan_sizes(self.h, C.byref(out), sc), "qcm_plan_sizes")
+        self.out_elems = out.value
+        self.scratch = [sc[0], sc[1], sc[2]]
+        gf, af, ab, nl = C.c_double(), C.c_double(), C.c_double(), C.c_int32()
+        check(lib().qcm_plan_work(self.h, C.byref(gf), C.byref(af), C.byref(ab), C.byref(nl)), "qcm_plan_work")
+        self.gemm_flops, self.axpy_flops, self.axpy_bytes, self.launches = gf.value, af.value, ab.value, nl.value
+        self.uploaded = False
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.qcm_plan_destroy(self.h)
+            self.h = None
+
+    def out_layout(self) -> BoundaryLayout:
+        aux, nb = C.c_int32(), C.c_int32()
+        check(lib().qcm_plan_out_layout(self.h, C.byref(aux), C.byref(nb), None, None, None, None, None),
+              "qcm_plan_out_layout")
+        n = max(nb.value, 1)
+        ptr = np.zeros(aux.value + 1, dtype=np.int32)
+        q = np.zeros(4 * n, dtype=np.int32)
+        rows = np.zeros(n, dtype=np.int64)
+        cols = np.zeros(n, dtype=np.int64)
+        off = np.zeros(n, dtype=np.int64)
+        check(lib().qcm_plan_out_layout(self.h, C.byref(aux), C.byref(nb), _p(ptr, i32p), _p(q, i32p),
+                                        _p(rows, i64p), _p(cols, i64p), _p(off, i64p)), "qcm_plan_out_layout")
+        nb = nb.value
+        keys = [((int(q[4 * k]), int(q[4 * k + 1])), (int(q[4 * k + 2]), int(q[4 * k + 3]))) for k in range(nb)]
+        shapes = [(int(rows[k]), int(cols[k])) for k in range(nb)]
+        return BoundaryLayout(blk_ptr=list(ptr), keys=keys, shapes=shapes, offsets=[int(x) for x in off[:nb]])
+
+    def stages(self):
+        """Export the task tables (for host-side inspection and tests)."""
+        n = C.c_int32()
+        check(lib().qcm_plan_num_stages(self.h, C.byref(n)), "qcm_plan_num_stages")
+        out = []
+        for s in range(n.value):
+            kind, no, nt = C.c_int32(), C.c_int64(), C.c_int64()
+            check(lib().qcm_plan_stage_info(self.h, s, C.byref(kind), C.byref(no), C.byref(nt)), "stage_info")
+            if kind.value == 0:
+                od = np.zeros((max(no.value, 1), 7), dtype=np.int64)
+                td = np.zeros((max(nt.value, 1), 3), dtype=np.int64)
+                ta = np.zeros(max(nt.value, 1))
+                check(lib().qcm_plan_stage_axpy(self.h, s, _p(od, i64p), _p(td, i64p), _p(ta, f64p)), "stage_axpy")
+                out.append(("axpy", od[:no.value], td[:nt.value], ta[:nt.value]))
+            elif kind.value == 1:
+                od = np.zeros((max(no.value, 1), 7), dtype=np.int64)
+                sd = np.zeros((max(nt.value, 1), 9), dtype=np.int64)
+                sa = np.zeros(max(nt.value, 1))
+                check(lib().qcm_plan_stage_gemm(self.h, s, _p(od, i64p), _p(sd, i64p), _p(sa, f64p)), "stage_gemm")
+                out.append(("gemm", od[:no.value], sd[:nt.value], sa[:nt.value]))
+            else:
+                out.append(("zero", int(no.value), int(nt.value)))
+        return out
+
+    def upload(self):
+        if not self.uploaded:
+            check(lib().qcm_plan_upload(self.h), "qcm_plan_upload")
+            self.uploaded = True
+
+    def run(self, ptrs: Sequence[int], precision: int = PREC_FP64, stream: int = 0):
+        arr = (C.c_void_p * QCM_NBUF)(*[C.c_void_p(int(p)) if p else None for p in ptrs])
+        check(lib().qcm_plan_run(self.h, arr, precision, C.c_void_p(stream) if stream else None), "qcm_plan_run")
+
+
+def plan_sigma(phys: Index, left_i: Index, right_i: Index, psi: Layout, L: BoundaryLayout, R: BoundaryLayout,
+               mpo: FMpo, hermitian: bool = True) -> Plan:
+    fp, fl, fr = FIndex(phys), FIndex(left_i), FIndex(right_i)
+    h = C.c_void_p()
+    check(lib().qcm_plan_sigma(C.byref(fp.c), C.byref(fl.c), C.byref(fr.c), C.byref(psi.c), C.byref(L.c),
+                               C.byref(R.c), C.byref(mpo.c), 1 if hermitian else 0, C.byref(h)), "qcm_plan_sigma")
+    return Plan(h, "sigma")
+
+
+def plan_boundary_left(phys, left_i, right_i, mps: Layout, L: BoundaryLayout, mpo: FMpo, hermitian=True) -> Plan:
+    fp, fl, fr = FIndex(phys), FIndex(left_i), FIndex(right_i)
+    h = C.c_void_p()
+    check(lib().qcm_plan_boundary_left(C.byref(fp.c), C.byref(fl.c), C.byref(fr.c), C.byref(mps.c), C.byref(L.c),
+                                       C.byref(mpo.c), 1 if hermitian else 0, C.byref(h)), "qcm_plan_boundary_left")
+    return Plan(h, "bleft")
+
+
+def plan_boundary_right(phys, left_i, right_i, mps: Layout, R: BoundaryLayout, mpo: FMpo, hermitian=True) -> Plan:
+    fp, fl, fr = FIndex(phys), FIndex(left_i), FIndex(right_i)
+    h = C.c_void_p()
+    check(lib().qcm_plan_boundary_right(C.byref(fp.c), C.byref(fl.c), C.byref(fr.c), C.byref(mps.c), C.byref(R.c),
+                                        C.byref(mpo.c), 1 if hermitian else 0, C.byref(h)), "qcm_plan_boundary_right")
+    return Plan(h, "bright")
+
+
+__all__ = ["lib", "check", "Layout", "BoundaryLayout", "FMpo", "FIndex", "Plan", "plan_sigma",
+           "plan_boundary_left", "plan_boundary_right", "PREC_FP64", "PREC_TF32", "PREC_BF16X3"]

@@ -1,0 +1,103 @@
+"""The C-ABI library on the CPU: it loads, exports every declared symbol, and
+its plan builder produces the reference layouts and sums (checked by
+interpreting the exported task tables against the oracle)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from qcmaquis_gb300 import native as N
+from qcmaquis_gb300.integrals import synthetic_integral_map
+from qcmaquis_gb300.model import QCModel
+from qcmaquis_gb300.mpo import make_mpo
+
+from oracle import dmrg_ref as R
+from oracle.sweep import SweepParams, initial_state
+from plan_interp import run_plan
+from test_oracle import _random_site_problem
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_declared_symbol():
+    hdr = open(os.path.join(ROOT, "include", "qcm_gb300.h")).read()
+    names = set(re.findall(r"\b(qcm_[a-z0-9_]+)\s*\(", hdr))
+    assert len(names) >= 15
+    lib = N.lib()
+    for n in sorted(names):
+        assert hasattr(lib, n), n
+
+
+def test_invalid_layout_is_rejected():
+    psi, left, right, ts = _random_site_problem()
+    psi = psi.copy().make_left_paired()
+    lay = N.Layout.of(psi.data)
+    bad = N.Layout(list(reversed(lay.keys)), list(reversed(lay.shapes)))
+    with pytest.raises(RuntimeError, match="DualIndex order"):
+        N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, bad, N.BoundaryLayout.of(left),
+                     N.BoundaryLayout.of(right), N.FMpo(ts))
+
+
+@pytest.mark.parametrize("herm", [True, False])
+@pytest.mark.parametrize("site,m", [(1, 8), (2, 16), (3, 12)])
+def test_sigma_plan_matches_oracle(herm, site, m):
+    psi, left, right, ts = _random_site_problem(site=site, m=m, herm=herm)
+    psi = psi.copy().make_left_paired()
+    lay = N.Layout.of(psi.data)
+    Ll, Rl = N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
+    p = N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, N.FMpo(ts), herm)
+    bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.zeros(p.out_elems)] + \
+        [np.zeros(max(s, 1)) for s in p.scratch]
+    run_plan(p, bufs)
+    ref = lay.pack(R.site_hamil2(psi, left, right, ts, is_hermitian=herm).data)
+    assert np.linalg.norm(bufs[3] - ref) <= 1e-13 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("herm", [True, False])
+def test_boundary_plans_match_oracle_layout_and_values(herm):
+    L, Ne = 6, 6
+    m = QCModel(L, synthetic_integral_map(L, seed=3), Ne)
+    mpo = make_mpo(m)
+    mps = initial_state(m, mpo, SweepParams(init_bond_dimension=16, seed=11), Ne, 0)
+    left = R.left_boundary(mps[0])
+    for i in range(3):
+        A = mps[i].copy().make_left_paired()
+        lay, Ll = N.Layout.of(A.data), N.BoundaryLayout.of(left)
+        p = N.plan_boundary_left(A.phys_i, A.left_i, A.right_i, lay, Ll, N.FMpo(mpo[i]), herm)
+        ol = p.out_layout()
+        bufs = [lay.pack(A.data), Ll.pack(left), None, np.zeros(max(p.out_elems, 1))] + \
+            [np.zeros(max(s, 1)) for s in p.scratch]
+        run_plan(p, bufs)
+        ref = R.overlap_mpo_left_step(mps[i], mps[i], left, mpo[i], herm)
+        got = ol.unpack(bufs[3])
+        assert [g.keys for g in got] == [r.keys for r in ref]
+        assert np.allclose(ol.pack(ref), bufs[3][:ol.size], rtol=0, atol=1e-13)
+        left = ref
+    right = R.right_boundary(mps[L - 1])
+    for i in range(L - 1, 2, -1):
+        A = mps[i].copy().make_left_paired()
+        lay, Rl = N.Layout.of(A.data), N.BoundaryLayout.of(right)
+        p = N.plan_boundary_right(A.phys_i, A.left_i, A.right_i, lay, Rl, N.FMpo(mpo[i]), herm)
+        ol = p.out_layout()
+        bufs = [lay.pack(A.data), None, Rl.pack(right), np.zeros(max(p.out_elems, 1))] + \
+            [np.zeros(max(s, 1)) for s in p.scratch]
+        run_plan(p, bufs)
+        ref = R.overlap_mpo_right_step(mps[i], mps[i], right, mpo[i], herm)
+        got = ol.unpack(bufs[3])
+        assert [g.keys for g in got] == [r.keys for r in ref]
+        assert np.allclose(ol.pack(ref), bufs[3][:ol.size], rtol=0, atol=1e-13)
+        right = ref
+
+
+def test_plan_work_counters_match_oracle():
+    psi, left, right, ts = _random_site_problem()
+    psi = psi.copy().make_left_paired()
+    lay = N.Layout.of(psi.data)
+    p = N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, lay, N.BoundaryLayout.of(left),
+                     N.BoundaryLayout.of(right), N.FMpo(ts))
+    R.FLOPS.reset()
+    R.site_hamil_lbtm(psi, left, right, ts)
+    # the plan computes every T row eagerly, as the oracle does; the sums match
+    assert p.gemm_flops == R.FLOPS.gemm_flops
+    assert p.axpy_flops <= R.FLOPS.axpy_flops
