@@ -1,0 +1,309 @@
+"""Sigma-vector benchmark of the two-site SU2U1 DMRG hot path on one GB300.
+
+Workload: one H_eff.psi on the middle two sites (11, 12) of an L=24, N=24,
+S=0 SU2U1 chemistry Hamiltonian (seeded synthetic integrals, diagonal in
+[-3, -0.3] Eh), random normalised MPS at bond dimension m=1024, boundaries
+built on the GPU from that MPS.  A step is one sigma vector.  The inputs
+(boundaries: several GB) are larger than L2, so no flush is needed between
+steps.
+
+Prints one JSON line (see the keys below).  ``--impl reference`` times the
+CPU restatement of the reference algorithm (the oracle) on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "H_eff.psi TFLOP/s (sigma vector, L=24 N=24 S=0 SU2U1, m=1024, middle sites)"
+UNIT = "TFLOP/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "tf32", "bf16x3"])
+    ap.add_argument("--L", type=int, default=24)
+    ap.add_argument("--m", type=int, default=1024)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--stage-times", action="store_true", default=True)
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = []
+        mx = None
+        reasons = set()
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+                for name, v in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"],
+                                   r[4:8]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+            except (ValueError, IndexError):
+                pass
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return {}
+
+
+def dgemm_peak_tflops():
+    """cuBLAS FP64 GEMM rate on this GPU, measured live (4096^3, best of 3)."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        a @ b
+    best = 1e9
+    for _ in range(3):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        s.record()
+        a @ b
+        e.record()
+        torch.cuda.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def cpu_oracle_sample(L: int, budget_s: float = 20.0):
+    """Oracle sigma on the host cores: same Hamiltonian family, bond dimension
+    reduced until the boundaries can be built in the time budget."""
+    import numpy as np
+    from oracle import dmrg_ref as R
+    from qcmaquis_gb300.workloads import build_sigma_host
+    m = 96
+    w = build_sigma_host(L=L, m=m)
+    t0 = time.time()
+    left = [R.BlockMatrix.from_indices(R.Index([((0, 0), 1)]), R.Index([((0, 0), 1)]), fill=1.0)]
+    for i, t in enumerate(w.left_sites):
+        ot = R.MPSTensor(t.phys_i, t.left_i, t.right_i, t.data.copy(), R.LEFT_PAIRED)
+        left = R.overlap_mpo_left_step(ot, ot, left, w.mpo[i])
+    right = [R.BlockMatrix.from_indices(R.Index([((w.nelec, 0), 1)]), R.Index([((w.nelec, 0), 1)]), fill=1.0)]
+    for k in range(len(w.right_sites) - 1, -1, -1):
+        i = w.site + 2 + k
+        t = w.right_sites[k]
+        ot = R.MPSTensor(t.phys_i, t.left_i, t.right_i, t.data.copy(), R.LEFT_PAIRED)
+        right = R.overlap_mpo_right_step(ot, ot, right, w.mpo[i])
+    tb = time.time() - t0
+    p = w.psi_host
+    psi = R.MPSTensor(p.phys_i, p.left_i, p.right_i, p.data.copy(), R.LEFT_PAIRED)
+    calls, flops, tt = 0, 0.0, 0.0
+    while tt < budget_s and calls < 50:
+        R.FLOPS.reset()
+        t1 = time.time()
+        R.site_hamil2(psi, left, right, w.ts_mpo)
+        tt += time.time() - t1
+        flops += R.FLOPS.gemm_flops + R.FLOPS.axpy_flops
+        calls += 1
+    return {"value": flops / tt / 1e12, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"numpy oracle sigma, L={L} N={w.nelec} middle sites, bond dimension m={m} (m=1024 "
+                      f"boundaries do not build in a bounded CPU time); {calls} calls in {tt:.1f}s, "
+                      f"boundaries {tb:.1f}s; BLAS threads = host cores"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cpu = cpu_oracle_sample(args.L, budget_s=max(5.0, 3.0 * args.steps))
+    line = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "sigma vector, L=24 N=24 S=0 SU2U1 middle sites (bounded CPU sample)",
+                       "L": args.L, "m": args.m},
+            "cpu_baseline": cpu,
+            "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import numpy as np
+    import torch
+    from qcmaquis_gb300 import native as N
+    from qcmaquis_gb300.engine import Engine
+    from qcmaquis_gb300.workloads import build_sigma_host, upload_sigma_workload
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    prec = {"fp64": N.PREC_FP64, "tf32": N.PREC_TF32, "bf16x3": N.PREC_BF16X3}[args.precision]
+
+    t0 = time.time()
+    w = build_sigma_host(L=args.L, m=args.m, seed=1 + rank * 0)
+    eng = Engine(f"cuda:{local}", precision=prec)
+    upload_sigma_workload(w, eng)
+    plan = eng.sigma_plan(w.psi, w.left, w.right, w.ts_mpo)
+    setup_s = time.time() - t0
+    flops = plan.gemm_flops + plan.axpy_flops
+    out = torch.empty(plan.out_elems, dtype=torch.float64, device=eng.device)
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        eng.site_hamil2(w.psi, w.left, w.right, w.ts_mpo, out=out)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches0 = eng.launches
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            eng.site_hamil2(w.psi, w.left, w.right, w.ts_mpo, out=out)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    t_step = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    gpu_launches = eng.launches - launches0
+    if world > 1:
+        tt = torch.tensor([t_step], device=eng.device)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(tt.item())
+
+    # per-stage times (CUDA events on the launching stream), for the roofline
+    kinds = plan.stage_kinds()
+    stage_t = [0.0] * len(kinds)
+    reps = max(2, min(args.steps, 5))
+    for _ in range(reps):
+        for si in range(len(kinds)):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            eng.run(plan, ket=w.psi.data, left=w.left.data, right=w.right.data, out=out, first=si, last=si)
+            b.record(stream)
+            torch.cuda.synchronize()
+            stage_t[si] += a.elapsed_time(b) / 1e3 / reps
+    gemm_t = sum(t for t, k in zip(stage_t, kinds) if k == "gemm")
+    axpy_t = sum(t for t, k in zip(stage_t, kinds) if k == "axpy")
+
+    # end to end through the public API: pinned host psi -> device, sigma, -> host
+    host_in = torch.from_numpy(N.Layout.of(w.psi_host.data).pack(w.psi_host.data)).pin_memory()
+    host_out = torch.empty(plan.out_elems, dtype=torch.float64).pin_memory()
+    dev_in = torch.empty_like(w.psi.data)
+    from qcmaquis_gb300.engine import DeviceMPSTensor
+    ket = DeviceMPSTensor(w.psi.phys_i, w.psi.left_i, w.psi.right_i, w.psi.layout, dev_in)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        dev_in.copy_(host_in, non_blocking=True)
+        eng.site_hamil2(ket, w.left, w.right, w.ts_mpo, out=out)
+        host_out.copy_(out, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = e0.elapsed_time(e1) / 1e3 / args.steps
+
+    peaks = measured_peaks()
+    if prec == N.PREC_FP64:
+        peak = dgemm_peak_tflops()
+        roof = {"bound": "tensor", "achieved": plan.gemm_flops / gemm_t / 1e12, "peak": peak, "unit": "TFLOP/s",
+                "frac": plan.gemm_flops / gemm_t / 1e12 / peak, "traffic": None,
+                "kernel": "gemm_f64_kernel (K1 + K3 grouped block products)",
+                "peak_source": "cuBLAS FP64 DGEMM 4096^3 measured in this run (no FP64 entry in MEASURED_PEAKS.json)"}
+    else:
+        peak = peaks.get("bf16_tflops", 1900.0)
+        roof = {"bound": "tensor", "achieved": plan.gemm_flops / gemm_t / 1e12, "peak": peak, "unit": "TFLOP/s",
+                "frac": plan.gemm_flops / gemm_t / 1e12 / peak, "traffic": None,
+                "kernel": "tensor-core grouped block products (K1 + K3)",
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"}
+    axpy_gbs = plan.axpy_bytes / axpy_t / 1e9 if axpy_t > 0 else None
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_oracle_sample(args.L, budget_s=15.0)
+        except Exception as e:  # the baseline must not hide the GPU line
+            cpu = {"error": str(e)}
+
+    value = flops / t_step / 1e12 * world
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+        "scaling": "weak" if world > 1 else "weak", "vs_baseline": None,
+        "dtype": {"fp64": "f64", "tf32": "tf32", "bf16x3": "bf16x3"}[args.precision],
+        "data": "synthetic (seeded integrals and random MPS; no dataset)",
+        "config": {"workload": "sigma vector H_eff.psi, L=24 N=24 S=0 SU2U1, middle sites (11,12), m=1024",
+                   **w.describe(), "precision": args.precision,
+                   "l2": "inputs (boundaries, several GB) larger than L2; no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "setup_s": round(setup_s, 1)},
+        "e2e": {"value": flops / t_e2e / 1e12 * world, "unit": UNIT,
+                "h2d_bytes_per_step": int(w.psi.data.numel() * 8), "d2h_bytes_per_step": int(plan.out_elems * 8)},
+        "gpu_launches": int(gpu_launches),
+        "roofline": roof,
+        "stages_ms": {f"{i}:{k}": round(t * 1e3, 3) for i, (k, t) in enumerate(zip(kinds, stage_t))},
+        "axpy_gather_gbs": axpy_gbs,
+        "work": {"gemm_flops": plan.gemm_flops, "axpy_flops": plan.axpy_flops, "axpy_bytes": plan.axpy_bytes},
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

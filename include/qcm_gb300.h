@@ -161,10 +161,10 @@ int qcm_plan_out_layout(const qcm_plan* plan, int32_t* aux, int32_t* nblocks, in
 /* Stage export for host-side inspection: kind 0 = gather-axpy, 1 = grouped GEMM. */
 int qcm_plan_num_stages(const qcm_plan* plan, int32_t* n);
 int qcm_plan_stage_info(const qcm_plan* plan, int32_t stage, int32_t* kind, int64_t* n_out, int64_t* n_terms);
-int qcm_plan_stage_axpy(const qcm_plan* plan, int32_t stage, int64_t* out_desc /*6*n_out*/,
+int qcm_plan_stage_axpy(const qcm_plan* plan, int32_t stage, int64_t* out_desc /*7*n_out*/,
                         int64_t* term_desc /*3*n_terms*/, double* term_alpha);
 int qcm_plan_stage_gemm(const qcm_plan* plan, int32_t stage, int64_t* out_desc /*7*n_out*/,
-                        int64_t* seg_desc /*8*n_terms*/, double* seg_alpha);
+                        int64_t* seg_desc /*9*n_terms*/, double* seg_alpha);
 
 /* Copy the plan's task tables to the current device (once per plan). */
 int qcm_plan_upload(qcm_plan* plan);
@@ -172,6 +172,11 @@ int qcm_plan_upload(qcm_plan* plan);
 /* Run the plan on a CUDA stream (NULL = default stream); bufs[QCM_NBUF] are
  * device pointers.  precision selects FP64 or a tensor-core form. */
 int qcm_plan_run(qcm_plan* plan, double* const* bufs, int32_t precision, void* stream);
+
+/* Run only stages [first, last] (last < 0: through the final stage); used to
+ * time individual kernels.  Stage kinds are reported by qcm_plan_stage_info. */
+int qcm_plan_run_stages(qcm_plan* plan, double* const* bufs, int32_t precision, void* stream, int32_t first,
+                        int32_t last);
 
 void qcm_plan_destroy(qcm_plan* plan);
 

@@ -354,7 +354,14 @@ int qcm_plan_upload(qcm_plan* p) {
 }
 
 int qcm_plan_run(qcm_plan* p, double* const* bufs, int32_t precision, void* stream) {
+    return qcm_plan_run_stages(p, bufs, precision, stream, 0, -1);
+}
+
+int qcm_plan_run_stages(qcm_plan* p, double* const* bufs, int32_t precision, void* stream, int32_t first,
+                        int32_t last) {
     if (!p || !bufs) { set_error("null argument"); return QCM_E_INVALID; }
+    if (last < 0 || last >= (int32_t)p->stages.size()) last = (int32_t)p->stages.size() - 1;
+    if (first < 0) first = 0;
     if (!p->uploaded) { set_error("plan not uploaded"); return QCM_E_STATE; }
     int dev = 0;
     QCM_CUDA(cudaGetDevice(&dev));
@@ -362,7 +369,8 @@ int qcm_plan_run(qcm_plan* p, double* const* bufs, int32_t precision, void* stre
     BufTable bt;
     for (int i = 0; i < QCM_NBUF; ++i) bt.p[i] = bufs[i];
     cudaStream_t s = (cudaStream_t)stream;
-    for (auto& st : p->stages) {
+    for (int32_t si = first; si <= last; ++si) {
+        Stage& st = p->stages[si];
         int rc = QCM_OK;
         if (st.kind == ST_ZERO) {
             if (st.zlen > 0) {

@@ -128,11 +128,12 @@ class Engine:
             self._plans[key] = p
         return p
 
-    def run(self, plan: N.Plan, ket=None, left=None, right=None, out=None, precision=None):
+    def run(self, plan: N.Plan, ket=None, left=None, right=None, out=None, precision=None, first=0, last=-1):
         s0, s1, s2 = self.ws.get(plan.scratch)
         plan.run([_ptr(ket), _ptr(left), _ptr(right), _ptr(out), _ptr(s0), _ptr(s1), _ptr(s2)],
-                 self.precision if precision is None else precision, self._stream())
-        self.launches += plan.launches
+                 self.precision if precision is None else precision, self._stream(), first, last)
+        if first == 0 and last == -1:
+            self.launches += plan.launches
 
     # -- Engine surface ----------------------------------------------------
     def site_hamil2(self, ket: DeviceMPSTensor, L: DeviceBoundary, R: DeviceBoundary, mpo,

@@ -76,6 +76,8 @@ def lib():
     L.qcm_plan_stage_gemm.argtypes = [C.c_void_p, C.c_int32, i64p, i64p, f64p]
     L.qcm_plan_upload.argtypes = [C.c_void_p]
     L.qcm_plan_run.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.c_int32, C.c_void_p]
+    L.qcm_plan_run_stages.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.c_int32, C.c_void_p, C.c_int32,
+                                      C.c_int32]
     L.qcm_plan_destroy.argtypes = [C.c_void_p]
     L.qcm_plan_destroy.restype = None
     L.qcm_dot.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
@@ -337,9 +339,21 @@ class Plan:
             check(lib().qcm_plan_upload(self.h), "qcm_plan_upload")
             self.uploaded = True
 
-    def run(self, ptrs: Sequence[int], precision: int = PREC_FP64, stream: int = 0):
+    def run(self, ptrs: Sequence[int], precision: int = PREC_FP64, stream: int = 0, first: int = 0,
+            last: int = -1):
         arr = (C.c_void_p * QCM_NBUF)(*[C.c_void_p(int(p)) if p else None for p in ptrs])
-        check(lib().qcm_plan_run(self.h, arr, precision, C.c_void_p(stream) if stream else None), "qcm_plan_run")
+        check(lib().qcm_plan_run_stages(self.h, arr, precision, C.c_void_p(stream) if stream else None, first, last),
+              "qcm_plan_run_stages")
+
+    def stage_kinds(self):
+        n = C.c_int32()
+        check(lib().qcm_plan_num_stages(self.h, C.byref(n)), "qcm_plan_num_stages")
+        kinds = []
+        for s in range(n.value):
+            k, a, b = C.c_int32(), C.c_int64(), C.c_int64()
+            check(lib().qcm_plan_stage_info(self.h, s, C.byref(k), C.byref(a), C.byref(b)), "stage_info")
+            kinds.append(("axpy", "gemm", "zero")[k.value])
+        return kinds
 
 
 def plan_sigma(phys: Index, left_i: Index, right_i: Index, psi: Layout, L: BoundaryLayout, R: BoundaryLayout,
