@@ -193,6 +193,23 @@ int qcm_lincomb(const double* const* x_dev_ptrs, const double* coef, int32_t nve
 int qcm_multi_dot(const double* const* v_dev_ptrs, int32_t nvec, const double* y, int64_t n, double* out_dev,
                   void* stream);
 
+/* Allocation-free variant of qcm_multi_dot.  No counterpart in the reference:
+ * it exists for callers that cannot allocate device memory during a solve --
+ * hosts that hand the whole device budget to their own memory pool up front
+ * and forbid cudaMalloc afterwards (an allocation there would synchronise the
+ * device and break the pool's accounting).  It computes the same
+ * out[k] = dot(V_k, y) with the same reduction order as qcm_multi_dot, but its
+ * partial sums live in a fixed library-owned device array of 32 x 304 doubles
+ * instead of a workspace allocated on first use; every GPU that loads the
+ * library holds that array until the process exits.
+ * Limits: nvec <= 32, otherwise QCM_E_RANGE and nothing is launched.
+ * The first call on each device looks up the array's device address; make
+ * that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU (different streams, no ordering between them)
+ * race on it and must be serialised by the caller. */
+int qcm_multi_dot_noalloc(const double* const* v_dev_ptrs, int32_t nvec, const double* y, int64_t n,
+                          double* out_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

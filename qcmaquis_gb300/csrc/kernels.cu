@@ -308,6 +308,52 @@ __global__ void lincomb_kernel(LinArgs args, double* __restrict__ y, int64_t n) 
     }
 }
 
+// ------------------------------------------------------------------ allocation-free multi-dot
+// Scratch of qcm_multi_dot_noalloc: one partial sum per (vector, block).  It is
+// a file-scope device array, so every GPU that loads this library holds it
+// (NOALLOC_MAX_VEC * RED_BLOCKS doubles = 76 KiB) until the process exits.
+constexpr int NOALLOC_MAX_VEC = 32;
+static __device__ __align__(256) double g_noalloc_partial[NOALLOC_MAX_VEC * RED_BLOCKS];
+
+struct DotPtrs { const double* x[NOALLOC_MAX_VEC]; };
+
+// Same reduction as multi_dot_partial, with the vector pointers passed by value
+// instead of through a device-side pointer table.
+__global__ void __launch_bounds__(RED_THREADS)
+multi_dot_partial_byval(DotPtrs v, int nvec, const double* __restrict__ y, int64_t n, double* __restrict__ partial) {
+    for (int k = 0; k < nvec; ++k) {
+        const double* __restrict__ x = v.x[k];
+        double s = 0.0;
+        for (int64_t i = (int64_t)blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += (int64_t)gridDim.x * RED_THREADS)
+            s = fma(x[i], y[i], s);
+        s = block_sum(s);
+        if (threadIdx.x == 0) partial[(int64_t)k * gridDim.x + blockIdx.x] = s;
+    }
+}
+
+// Device address of g_noalloc_partial per device, looked up once (set-up of the
+// first call on that device).
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_ptr[64] = {nullptr};
+
+static int noalloc_scratch(double** out) {
+    int dev = 0;
+    QCM_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) { set_error("device ordinal out of range"); return QCM_E_RANGE; }
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partial);
+        if (e != cudaSuccess || !p) {
+            set_error(std::string("cudaGetSymbolAddress(g_noalloc_partial): ") + cudaGetErrorString(e));
+            return QCM_E_CUDA;
+        }
+        g_noalloc_ptr[dev] = (double*)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return QCM_OK;
+}
+
 // per-device reduction workspace owned by the library (allocated on first use)
 struct RedWs { double* partial = nullptr; const double** ptrs = nullptr; };
 static std::mutex g_ws_mu;
@@ -398,6 +444,32 @@ int qcm_multi_dot(const double* const* v, int32_t nvec, const double* y, int64_t
     multi_dot_partial<<<RED_BLOCKS, RED_THREADS, 0, s>>>(ws->ptrs, nvec, y, n, ws->partial);
     QCM_CUDA(cudaGetLastError());
     multi_dot_final<<<1, RED_THREADS, 0, s>>>(ws->partial, RED_BLOCKS, nvec, out, 0);
+    QCM_CUDA(cudaGetLastError());
+    return QCM_OK;
+}
+
+int qcm_multi_dot_noalloc(const double* const* v, int32_t nvec, const double* y, int64_t n, double* out,
+                          void* stream) {
+    if (nvec < 0 || nvec > NOALLOC_MAX_VEC) {
+        set_error("qcm_multi_dot_noalloc: nvec " + std::to_string(nvec) + " exceeds the fixed scratch capacity of " +
+                  std::to_string(NOALLOC_MAX_VEC) + " vectors");
+        return QCM_E_RANGE;
+    }
+    if (n < 0) { set_error("qcm_multi_dot_noalloc: negative length"); return QCM_E_INVALID; }
+    if (nvec == 0) return QCM_OK;
+    if (!v || !y || !out) { set_error("qcm_multi_dot_noalloc: null pointer"); return QCM_E_INVALID; }
+    double* partial = nullptr;
+    int rc = noalloc_scratch(&partial);
+    if (rc) return rc;
+    DotPtrs args;
+    for (int k = 0; k < NOALLOC_MAX_VEC; ++k) args.x[k] = (k < nvec) ? v[k] : nullptr;
+    for (int k = 0; k < nvec; ++k)
+        if (!args.x[k]) { set_error("qcm_multi_dot_noalloc: null vector pointer"); return QCM_E_INVALID; }
+    cudaStream_t s = (cudaStream_t)stream;
+    // every partial read by multi_dot_final is written by this launch first: nothing to clear
+    multi_dot_partial_byval<<<RED_BLOCKS, RED_THREADS, 0, s>>>(args, nvec, y, n, partial);
+    QCM_CUDA(cudaGetLastError());
+    multi_dot_final<<<1, RED_THREADS, 0, s>>>(partial, RED_BLOCKS, nvec, out, 0);
     QCM_CUDA(cudaGetLastError());
     return QCM_OK;
 }
