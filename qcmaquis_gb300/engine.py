@@ -125,6 +125,9 @@ class Engine:
                              self.hermitian)
             p.upload()
             p._keep = (ket.layout, L.layout, R.layout)
+            # keep the two most recent sigma plans (a plan's task tables can be hundreds of MB)
+            while len(self._plans) >= 2:
+                self._plans.pop(next(iter(self._plans)))
             self._plans[key] = p
         return p
 

@@ -1,0 +1,444 @@
+"""GPU-resident MPS tensor operations around the optimisation step.
+
+Each tensor is one flat FP64 CUDA buffer plus a block layout; blocks are
+column-major views into the buffer.  These operations restate:
+
+* ``TwoSiteTensor(mps1, mps2)`` + ``make_mps`` (theta = A.B, both->right
+  reshape, SU(2) ``reduce_right``): ``mp_tensors/twositetensor.hpp:22-31, 132-139``,
+  ``mp_tensors/ts_reshape.h:231-290``, ``mp_tensors/ts_reduction.h:42-141``;
+* ``operator<<`` (``unreduce_left``) and ``reshape_left_to_both``:
+  ``mp_tensors/twositetensor.hpp:372-389``, ``ts_reduction.h:143-251``,
+  ``ts_reshape.h:89-145``;
+* ``split_mps_l2r/r2l`` with ``svd_truncate``: ``twositetensor.hpp:141-180``,
+  ``block_matrix/block_matrix_algorithms.h:163-333``;
+* ``leftNormalizeAndReturn`` / ``rightNormalizeAndReturn`` / ``multiply_from_*``:
+  ``mp_tensors/mpstensor.hpp:219-330``.
+
+Dense factorisations (SVD, QR) run on the GPU through torch.linalg (cuSOLVER);
+block products through torch.matmul (cuBLAS).  Nothing here runs on the CPU
+except index bookkeeping and the truncation decision on the singular values.
+"""
+from __future__ import annotations
+
+import math
+from typing import Dict, List, Tuple
+
+import numpy as np
+import torch
+
+from . import native as N
+from .engine import DeviceMPSTensor
+from .symmetry import (Index, ProductBasis, adjoin, common_subset, fuse, fuse_neg_first, index_product, neg,
+                       spin)
+from .wigner import wigner6j
+
+
+class DBM:
+    """Block matrix on the device: sorted keys, per-block tensors (views allowed)."""
+
+    def __init__(self):
+        self.keys: List = []
+        self.blocks: List[torch.Tensor] = []
+
+    def find(self, lc, rc) -> int:
+        k = (lc, rc)
+        lo, hi = 0, len(self.keys)
+        while lo < hi:
+            mid = (lo + hi) // 2
+            if self.keys[mid] > k:
+                lo = mid + 1
+            else:
+                hi = mid
+        return lo if lo < len(self.keys) and self.keys[lo] == k else len(self.keys)
+
+    def insert(self, t: torch.Tensor, lc, rc) -> int:
+        k = (lc, rc)
+        lo, hi = 0, len(self.keys)
+        while lo < hi:
+            mid = (lo + hi) // 2
+            if self.keys[mid] > k:
+                lo = mid + 1
+            else:
+                hi = mid
+        self.keys.insert(lo, k)
+        self.blocks.insert(lo, t)
+        return lo
+
+    def get_or_zeros(self, lc, rc, shape, device):
+        p = self.find(lc, rc)
+        if p == len(self.keys):
+            p = self.insert(torch.zeros(shape, dtype=torch.float64, device=device), lc, rc)
+        return self.blocks[p]
+
+    def left_lower_bound(self, lc) -> int:
+        lo, hi = 0, len(self.keys)
+        while lo < hi:
+            mid = (lo + hi) // 2
+            if self.keys[mid][0] > lc:
+                lo = mid + 1
+            else:
+                hi = mid
+        return lo
+
+    def left_basis(self) -> Index:
+        return Index.from_sorted([(k[0], b.shape[0]) for k, b in zip(self.keys, self.blocks)])
+
+    def right_basis(self) -> Index:
+        return Index.from_sorted([(k[1], b.shape[1]) for k, b in zip(self.keys, self.blocks)])
+
+    def to_flat(self) -> Tuple[N.Layout, torch.Tensor]:
+        lay = N.Layout(self.keys, [tuple(b.shape) for b in self.blocks])
+        dev = self.blocks[0].device if self.blocks else torch.device("cuda")
+        flat = torch.empty(max(lay.size, 1), dtype=torch.float64, device=dev)
+        for o, b in zip(lay.offsets, self.blocks):
+            r, c = b.shape
+            flat[o:o + r * c].view(c, r).copy_(b.t())
+        return lay, flat
+
+
+def block_views(layout: N.Layout, flat: torch.Tensor) -> DBM:
+    d = DBM()
+    for k, o, (r, c) in zip(layout.keys, layout.offsets, layout.shapes):
+        d.keys.append(k)
+        d.blocks.append(flat[o:o + r * c].view(c, r).t())
+    return d
+
+
+def gemm(A: DBM, B: DBM) -> DBM:
+    """Charge-matched block product (``block_matrix_algorithms.h:47-80``)."""
+    C = DBM()
+    for k, (ka, a) in enumerate(zip(A.keys, A.blocks)):
+        ar = ka[1]
+        it = B.left_lower_bound(ar)
+        while it < len(B.keys) and B.keys[it][0] == ar:
+            lc, rc = ka[0], B.keys[it][1]
+            prod = a @ B.blocks[it]
+            p = C.find(lc, rc)
+            if p < len(C.keys):
+                C.blocks[p] = C.blocks[p] + prod
+            else:
+                C.insert(prod, lc, rc)
+            it += 1
+    return C
+
+
+# ------------------------------------------------------------------ reshapes
+def reshape_l2r(phys: Index, left_i: Index, right_i: Index, m1: DBM) -> DBM:
+    m2 = DBM()
+    in_left = ProductBasis(phys, left_i)
+    out_right = ProductBasis(phys, right_i, fuse_neg_first)
+    for k, b in zip(m1.keys, m1.blocks):
+        r = right_i.position(k[1])
+        if r == len(right_i):
+            continue
+        in_r = right_i[r][0]
+        for ps, sd in phys:
+            l = left_i.position(fuse(k[0], neg(ps)))
+            if l == len(left_i):
+                continue
+            ol, orr = left_i[l][0], fuse(neg(ps), in_r)
+            ld, rd = left_i[l][1], right_i[r][1]
+            ob = m2.get_or_zeros(ol, orr, (ld, out_right.size(orr)), b.device)
+            ilo, oro = in_left(ps, ol), out_right(ps, in_r)
+            for ss in range(sd):
+                ob[:ld, oro + ss * rd:oro + (ss + 1) * rd] = b[ilo + ss * ld:ilo + (ss + 1) * ld, :rd]
+    return m2
+
+
+def reshape_r2l(phys: Index, left_i: Index, right_i: Index, m1: DBM) -> DBM:
+    m2 = DBM()
+    in_right = ProductBasis(phys, right_i, fuse_neg_first)
+    out_left = ProductBasis(phys, left_i)
+    for k, b in zip(m1.keys, m1.blocks):
+        l = left_i.position(k[0])
+        if l == len(left_i):
+            continue
+        in_l = left_i[l][0]
+        for ps, sd in phys:
+            r = right_i.position(fuse(k[1], ps))
+            if r == len(right_i):
+                continue
+            ol, orr = fuse(ps, in_l), right_i[r][0]
+            ld, rd = left_i[l][1], right_i[r][1]
+            ob = m2.get_or_zeros(ol, orr, (out_left.size(ol), rd), b.device)
+            iro, olo = in_right(ps, orr), out_left(ps, in_l)
+            for ss in range(sd):
+                ob[olo + ss * ld:olo + (ss + 1) * ld, :rd] = b[:ld, iro + ss * rd:iro + (ss + 1) * rd]
+    return m2
+
+
+def _both_to_right(p1: Index, p2: Index, left_i: Index, right_i: Index, m1: DBM) -> DBM:
+    phys2 = index_product(p1, p2)
+    phys_pb = ProductBasis(p1, p2)
+    in_left = ProductBasis(p1, left_i)
+    in_right = ProductBasis(p2, right_i, fuse_neg_first)
+    out_right = ProductBasis(phys2, right_i, fuse_neg_first)
+    m2 = DBM()
+    for k, b in zip(m1.keys, m1.blocks):
+        for c1, sd1 in p1:
+            l = left_i.position(fuse(k[0], neg(c1)))
+            if l == len(left_i):
+                continue
+            for c2, sd2 in p2:
+                r = right_i.position(fuse(k[1], c2))
+                if r == len(right_i):
+                    continue
+                s_charge = fuse(c1, c2)
+                ol, orr = left_i[l][0], fuse(neg(s_charge), right_i[r][0])
+                ld, rd = left_i[l][1], right_i[r][1]
+                ob = m2.get_or_zeros(ol, orr, (ld, out_right.size(orr)), b.device)
+                ilo, iro = in_left(c1, left_i[l][0]), in_right(c2, right_i[r][0])
+                oro, opo = out_right(s_charge, right_i[r][0]), phys_pb(c1, c2)
+                for ss1 in range(sd1):
+                    for ss2 in range(sd2):
+                        so = opo + ss1 * sd2 + ss2
+                        ob[:ld, oro + so * rd:oro + (so + 1) * rd] = \
+                            b[ilo + ss1 * ld:ilo + (ss1 + 1) * ld, iro + ss2 * rd:iro + (ss2 + 1) * rd]
+    return m2
+
+
+def _left_to_both(p1: Index, p2: Index, left_i: Index, right_i: Index, m1: DBM) -> DBM:
+    phys2 = index_product(p1, p2)
+    phys_pb = ProductBasis(p1, p2)
+    in_left = ProductBasis(phys2, left_i)
+    out_right = ProductBasis(p2, right_i, fuse_neg_first)
+    out_left = ProductBasis(p1, left_i)
+    m2 = DBM()
+    for k, b in zip(m1.keys, m1.blocks):
+        r = right_i.position(k[1])
+        if r == len(right_i):
+            raise RuntimeError("two-site tensor inconsistent with right index")
+        for c1, sd1 in p1:
+            for c2, sd2 in p2:
+                s_charge = fuse(c1, c2)
+                l = left_i.position(fuse(k[0], neg(s_charge)))
+                if l == len(left_i):
+                    continue
+                ol, orr = fuse(c1, left_i[l][0]), fuse(neg(c2), right_i[r][0])
+                ld, rd = left_i[l][1], right_i[r][1]
+                ob = m2.get_or_zeros(ol, orr, (out_left.size(ol), out_right.size(orr)), b.device)
+                ilo, ipo = in_left(s_charge, left_i[l][0]), phys_pb(c1, c2)
+                olo, oro = out_left(c1, left_i[l][0]), out_right(c2, right_i[r][0])
+                for ss1 in range(sd1):
+                    for ss2 in range(sd2):
+                        si = ipo + ss1 * sd2 + ss2
+                        ob[olo + ss1 * ld:olo + (ss1 + 1) * ld, oro + ss2 * rd:oro + (ss2 + 1) * rd] = \
+                            b[ilo + si * ld:ilo + (si + 1) * ld, :rd]
+    return m2
+
+
+def _sign6(jl, jr, S1, S2):
+    return -1.0 if ((jl + jr + S1 + S2) // 2) % 2 else 1.0
+
+
+def reduce_right(p1: Index, p2: Index, left_i: Index, right_i: Index, m1: DBM):
+    phys2 = index_product(p1, p2)
+    phys_pb = ProductBasis(p1, p2)
+    in_right = ProductBasis(phys2, right_i, fuse_neg_first)
+    m2 = DBM()
+    for k, ib in zip(m1.keys, m1.blocks):
+        lc, in_r = k
+        ob = torch.zeros_like(ib)
+        m2.insert(ob, lc, in_r)
+        for s_charge, _ in phys2:
+            r = right_i.position(fuse(in_r, s_charge))
+            if r == len(right_i):
+                continue
+            iro, rs = in_right(s_charge, right_i[r][0]), right_i[r][1]
+            for c1, sd1 in p1:
+                for c2, sd2 in p2:
+                    if s_charge != fuse(c1, c2):
+                        continue
+                    ipo = phys_pb(c1, c2)
+                    S1, S2 = abs(spin(c1)), abs(spin(c2))
+                    jl, jm, jr = spin(lc), spin(lc) + spin(c1), spin(right_i[r][0])
+                    if jm < 0:
+                        continue
+                    if jl == jr and jl > 0 and S1 == 1 and S2 == 1:
+                        base = ipo if spin(c1) == 1 else ipo - 1
+                        outs = [(base + j // 2, j) for j in range(abs(S1 - S2), abs(S1 + S2) + 1, 2)]
+                    else:
+                        outs = [(ipo, abs(spin(c1) + spin(c2)))]
+                    for opo, j in outs:
+                        cc = math.sqrt((j + 1) * (jm + 1)) * wigner6j(jl, jr, j, S2, S1, jm) * _sign6(jl, jr, S1, S2)
+                        for ss1 in range(sd1):
+                            for ss2 in range(sd2):
+                                si, so = ipo + ss1 * sd2 + ss2, opo + ss1 * sd2 + ss2
+                                ob[:, iro + so * rs:iro + (so + 1) * rs] += cc * ib[:, iro + si * rs:iro + (si + 1) * rs]
+    return phys2, m2
+
+
+def unreduce_left(p1: Index, p2: Index, left_i: Index, right_i: Index, m1: DBM):
+    phys2 = index_product(p1, p2)
+    phys_pb = ProductBasis(p1, p2)
+    in_left = ProductBasis(phys2, left_i)
+    m2 = DBM()
+    for k, ib in zip(m1.keys, m1.blocks):
+        in_l, rc = k
+        ob = torch.zeros_like(ib)
+        m2.insert(ob, in_l, rc)
+        for s_charge, _ in phys2:
+            l = left_i.position(fuse(in_l, neg(s_charge)))
+            if l == len(left_i):
+                continue
+            ilo, ld = in_left(s_charge, left_i[l][0]), left_i[l][1]
+            for c1, sd1 in p1:
+                for c2, sd2 in p2:
+                    if s_charge != fuse(c1, c2):
+                        continue
+                    ipo = phys_pb(c1, c2)
+                    S1, S2 = abs(spin(c1)), abs(spin(c2))
+                    jl, jr = spin(left_i[l][0]), spin(rc)
+                    if jl == jr and jl > 0 and S1 == 1 and S2 == 1:
+                        j = 0 if spin(c1) == 1 else 2
+                        base = ipo if j == 0 else ipo - 1
+                        outs = [((base + 1) if jm == jl - 1 else base, j, jm) for jm in (jl - 1, jl + 1)]
+                    else:
+                        j = abs(spin(c1) + spin(c2))
+                        jm = jl + spin(c1)
+                        if jm < 0:
+                            continue
+                        outs = [(ipo, j, jm)]
+                    for opo, j, jm in outs:
+                        cc = math.sqrt((j + 1) * (jm + 1)) * wigner6j(jl, jr, j, S2, S1, jm) * _sign6(jl, jr, S1, S2)
+                        for ss1 in range(sd1):
+                            for ss2 in range(sd2):
+                                si, so = ipo + ss1 * sd2 + ss2, opo + ss1 * sd2 + ss2
+                                ob[ilo + so * ld:ilo + (so + 1) * ld, :] += cc * ib[ilo + si * ld:ilo + (si + 1) * ld, :]
+    return phys2, m2
+
+
+# ------------------------------------------------------------------ MPS-level operations
+def from_dbm(phys: Index, left_i: Index, right_i: Index, lp: DBM, layout_like=None) -> DeviceMPSTensor:
+    lay, flat = lp.to_flat()
+    return DeviceMPSTensor(phys, left_i, right_i, lay, flat)
+
+
+def as_dbm(t: DeviceMPSTensor) -> DBM:
+    return block_views(t.layout, t.data)
+
+
+def make_two_site_mps(A: DeviceMPSTensor, B: DeviceMPSTensor) -> DeviceMPSTensor:
+    """theta = A(lp).B(rp), reshaped both->right and SU(2)-reduced, returned left-paired."""
+    Brp = reshape_l2r(B.phys_i, B.left_i, B.right_i, as_dbm(B))
+    theta = gemm(as_dbm(A), Brp)
+    rp = _both_to_right(A.phys_i, B.phys_i, A.left_i, B.right_i, theta)
+    phys2, red = reduce_right(A.phys_i, B.phys_i, A.left_i, B.right_i, rp)
+    # MPSTensor(phys2, left, right, red, RightPaired): left index from the blocks
+    new_left = red.left_basis()
+    possible_right = index_product(phys2, new_left)
+    right = B.right_i.copy()
+    common_subset(right, possible_right)
+    lp = reshape_r2l(phys2, new_left, right, red)
+    return from_dbm(phys2, new_left, right, lp)
+
+
+class Trunc:
+    def __init__(self, bond_dimension, truncated_weight, truncated_fraction, smallest_ev):
+        self.bond_dimension = bond_dimension
+        self.truncated_weight = truncated_weight
+        self.truncated_fraction = truncated_fraction
+        self.smallest_ev = smallest_ev
+
+
+def svd_truncate(M: DBM, rel_tol: float, Mmax: int):
+    """Per-block SVD on the GPU, global cut on the host (``block_matrix_algorithms.h:210-333``)."""
+    Us, Ss, Vs = [], [], []
+    for b in M.blocks:
+        u, s, vh = torch.linalg.svd(b, full_matrices=False)
+        Us.append(u)
+        Ss.append(s)
+        Vs.append(vh)
+    svals = [s.detach().cpu().numpy() for s in Ss]
+    allv = np.sort(np.concatenate(svals))[::-1]
+    evalscut = rel_tol * allv[0]
+    if allv.size > Mmax:
+        evalscut = max(evalscut, allv[Mmax])
+    smallest_ev = evalscut / allv[0]
+    disc = allv[allv < evalscut]
+    tfrac = float(disc.sum() / allv.sum())
+    tw = float((disc * disc).sum() / (allv * allv).sum())
+    keeps = [int(np.argmax(s < evalscut)) if np.any(s < evalscut) else s.size for s in svals]
+    U, V = DBM(), DBM()
+    S: Dict = {}
+    for k, (key, kk) in enumerate(zip(M.keys, keeps)):
+        if kk == 0:
+            continue
+        lc, rc = key
+        U.insert(Us[k][:, :kk], lc, rc)
+        V.insert(Vs[k][:kk, :], rc, rc)
+        S[rc] = Ss[k][:kk]
+    return U, S, V, Trunc(sum(keeps), tw, tfrac, smallest_ev)
+
+
+def split(u: DeviceMPSTensor, A0: DeviceMPSTensor, B0: DeviceMPSTensor, Mmax: int, cutoff: float, l2r: bool):
+    """``tst << u`` then ``split_mps_l2r/r2l``; returns new (A, B, truncation)."""
+    _, tst = unreduce_left(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, as_dbm(u))
+    both = _left_to_both(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, tst)
+    U, S, V, tr = svd_truncate(both, cutoff, Mmax)
+    p1, p2 = A0.phys_i, B0.phys_i
+    if l2r:
+        SV = DBM()
+        for (lc, rc), b in zip(V.keys, V.blocks):
+            SV.insert(S[lc][:, None] * b, lc, rc)
+        A_lp = U
+        B_rp = SV
+    else:
+        US = DBM()
+        for (lc, rc), b in zip(U.keys, U.blocks):
+            US.insert(b * S[rc][None, :], lc, rc)
+        A_lp = US
+        B_rp = V
+    # A: MPSTensor(p1, left, A_lp.right_basis(), A_lp, LeftPaired)
+    a_right = A_lp.right_basis()
+    a_left = A0.left_i.copy()
+    common_subset(a_left, index_product(adjoin(p1), a_right))
+    A = from_dbm(p1, a_left, a_right, A_lp)
+    # B: MPSTensor(p2, B_rp.left_basis(), right, B_rp, RightPaired)
+    b_left = B_rp.left_basis()
+    b_right = B0.right_i.copy()
+    common_subset(b_right, index_product(p2, b_left))
+    B = from_dbm(p2, b_left, b_right, reshape_r2l(p2, b_left, b_right, B_rp))
+    return A, B, tr
+
+
+def left_normalize_and_return(t: DeviceMPSTensor) -> Tuple[DeviceMPSTensor, DBM]:
+    Q, R = DBM(), DBM()
+    for (lc, rc), b in zip(t.layout.keys, as_dbm(t).blocks):
+        q, r = torch.linalg.qr(b, mode="reduced")
+        Q.insert(q, lc, rc)
+        R.insert(r, rc, rc)
+    new_right = Q.right_basis()
+    return from_dbm(t.phys_i, t.left_i, new_right, Q), R
+
+
+def right_normalize_and_return(t: DeviceMPSTensor) -> Tuple[DeviceMPSTensor, DBM]:
+    rp = reshape_l2r(t.phys_i, t.left_i, t.right_i, as_dbm(t))
+    Lm, Q = DBM(), DBM()
+    for (lc, rc), b in zip(rp.keys, rp.blocks):
+        q, r = torch.linalg.qr(b.t(), mode="reduced")
+        Lm.insert(r.t(), lc, lc)
+        Q.insert(q.t(), lc, rc)
+    new_left = Q.left_basis()
+    return from_dbm(t.phys_i, new_left, t.right_i, reshape_r2l(t.phys_i, new_left, t.right_i, Q)), Lm
+
+
+def multiply_from_left(t: DeviceMPSTensor, Nm: DBM) -> DeviceMPSTensor:
+    rp = reshape_l2r(t.phys_i, t.left_i, t.right_i, as_dbm(t))
+    tmp = gemm(Nm, rp)
+    new_left = tmp.left_basis()
+    right = t.right_i.copy()
+    common_subset(right, index_product(t.phys_i, new_left))
+    return from_dbm(t.phys_i, new_left, right, reshape_r2l(t.phys_i, new_left, right, tmp))
+
+
+def multiply_from_right(t: DeviceMPSTensor, Nm: DBM) -> DeviceMPSTensor:
+    tmp = gemm(as_dbm(t), Nm)
+    new_right = tmp.right_basis()
+    left = t.left_i.copy()
+    common_subset(left, index_product(adjoin(t.phys_i), new_right))
+    return from_dbm(t.phys_i, left, new_right, tmp)
+
+
+__all__ = ["DBM", "block_views", "make_two_site_mps", "split", "svd_truncate", "left_normalize_and_return",
+           "right_normalize_and_return", "multiply_from_left", "multiply_from_right", "reshape_l2r", "reshape_r2l"]

@@ -1,0 +1,63 @@
+"""GPU two-site sweeps against the oracle: per-microiteration and per-sweep
+energies to 1e-10 Eh, truncated weights to 1e-8 relative (absolute 1e-14
+floor), starting from the identical initial MPS."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from qcmaquis_gb300.integrals import synthetic_integral_map
+from qcmaquis_gb300.model import QCModel
+from qcmaquis_gb300.mpo import make_mpo
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+E_TOL = 1e-10
+TW_REL = 1e-8
+TW_ABS = 1e-14
+
+
+def _gpu_sweep(L, N, m, nsweeps, seed_ints, twoS=0):
+    from qcmaquis_gb300 import sweep as G
+    model = QCModel(L, synthetic_integral_map(L, seed=seed_ints), N)
+    mpo = make_mpo(model)
+    rec, _ = G.run_dmrg(model, mpo, G.SweepParams(nsweeps=nsweeps, max_bond_dimension=m), nelec=N, twoS=twoS)
+    return model, mpo, rec
+
+
+def _check(gpu, ref_energies, ref_sweep, ref_tw):
+    assert np.max(np.abs(np.array(gpu.energies) - np.array(ref_energies))) < E_TOL
+    assert np.max(np.abs(np.array(gpu.sweep_energy) - np.array(ref_sweep))) < E_TOL
+    tw_g, tw_r = np.array(gpu.truncated_weight), np.array(ref_tw)
+    assert np.all(np.abs(tw_g - tw_r) <= TW_REL * np.abs(tw_r) + TW_ABS)
+
+
+def test_gpu_sweep_matches_oracle_L6():
+    from oracle.sweep import SweepParams, run_dmrg
+    L, N, m = 6, 6, 24
+    model, mpo, gpu = _gpu_sweep(L, N, m, 2, seed_ints=3)
+    ref, _ = run_dmrg(model, mpo, SweepParams(nsweeps=2, max_bond_dimension=m), nelec=N)
+    _check(gpu, ref.energies, ref.sweep_energy, ref.truncated_weight)
+    assert gpu.bond_dimension == ref.bond_dimension
+
+
+def test_gpu_sweep_golden_lih(golden):
+    from conftest import integral_map
+    from qcmaquis_gb300 import sweep as G
+    g = golden["lih"]
+    model = QCModel(g["L"], integral_map(g["integrals"]), g["nelec"])
+    mpo = make_mpo(model)
+    rec, _ = G.run_dmrg(model, mpo, G.SweepParams(nsweeps=2, max_bond_dimension=100), nelec=g["nelec"])
+    assert abs(rec.sweep_energy[-1] - g["energy"]) < 1e-9 * abs(g["energy"])
+
+
+def test_gpu_sweep_matches_oracle_config0():
+    """Plain two-site DMRG, L=8 N=8 S=0, m=64, 6 sweeps (oracle values committed)."""
+    with open(os.path.join(HERE, "golden", "oracle_L8_m64.json")) as f:
+        ref = json.load(f)
+    from qcmaquis_gb300 import sweep as G
+    model = QCModel(8, synthetic_integral_map(8, seed=0, diag_range=(-2.0, -0.5)), 8)
+    gpu, _ = G.run_dmrg(model, make_mpo(model), G.SweepParams(nsweeps=6, max_bond_dimension=64), nelec=8)
+    _check(gpu, ref["energies"], ref["sweep_energy"], ref["tw"])
