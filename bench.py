@@ -33,7 +33,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "tf32", "bf16x3"])
+    ap.add_argument("--precision", default="bf16x3", choices=["fp64", "tf32", "bf16x3"])
+    ap.add_argument("--compare-steps", type=int, default=2, help="FP64 sigma calls timed for the comparison")
     ap.add_argument("--L", type=int, default=24)
     ap.add_argument("--m", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -92,6 +93,14 @@ class ClockSampler:
         sm.sort()
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def ctypes_status():
+    import ctypes
+    from qcmaquis_gb300 import native as N
+    v = ctypes.c_int32(-1)
+    N.check(N.lib().qcm_device_status(ctypes.byref(v)), "qcm_device_status")
+    return v.value
 
 
 def measured_peaks():
@@ -255,6 +264,29 @@ def main():
     torch.cuda.synchronize()
     t_e2e = e0.elapsed_time(e1) / 1e3 / args.steps
 
+    # the same sigma in plain FP64 on the GPU: speedup and relative error of this precision
+    compare = None
+    if prec != N.PREC_FP64 and args.compare_steps > 0:
+        ref = torch.empty_like(out)
+        eng.site_hamil2(w.psi, w.left, w.right, w.ts_mpo, out=ref, precision=N.PREC_FP64)
+        torch.cuda.synchronize()
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        for _ in range(args.compare_steps):
+            eng.site_hamil2(w.psi, w.left, w.right, w.ts_mpo, out=ref, precision=N.PREC_FP64)
+        c1.record(stream)
+        torch.cuda.synchronize()
+        t64 = c0.elapsed_time(c1) / 1e3 / args.compare_steps
+        eng.site_hamil2(w.psi, w.left, w.right, w.ts_mpo, out=out)
+        torch.cuda.synchronize()
+        rel = float((torch.linalg.norm(out - ref) / torch.linalg.norm(ref)).item())
+        e_ref = float(torch.dot(w.psi.data, ref).item())
+        e_mix = float(torch.dot(w.psi.data, out).item())
+        compare = {"fp64_ms_per_step": t64 * 1e3, "speedup_vs_fp64_gpu": t64 / t_step,
+                   "sigma_rel_err_vs_fp64": rel, "rayleigh_quotient_err_eh": abs(e_mix - e_ref),
+                   "fp64_tflops": flops / t64 / 1e12}
+    st = ctypes_status()
+
     peaks = measured_peaks()
     if prec == N.PREC_FP64:
         peak = dgemm_peak_tflops()
@@ -264,9 +296,12 @@ def main():
                 "peak_source": "cuBLAS FP64 DGEMM 4096^3 measured in this run (no FP64 entry in MEASURED_PEAKS.json)"}
     else:
         peak = peaks.get("bf16_tflops", 1900.0)
-        roof = {"bound": "tensor", "achieved": plan.gemm_flops / gemm_t / 1e12, "peak": peak, "unit": "TFLOP/s",
-                "frac": plan.gemm_flops / gemm_t / 1e12 / peak, "traffic": None,
-                "kernel": "tensor-core grouped block products (K1 + K3)",
+        nprod = 6 if prec == N.PREC_BF16X3 else 1
+        ach = plan.gemm_flops * nprod / gemm_t / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "traffic": None,
+                "kernel": "tc_gemm_kernel (tcgen05 K1 + K3 grouped block products)",
+                "achieved_counts": f"{nprod} tensor-core products per FP64-equivalent product",
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"}
     axpy_gbs = plan.axpy_bytes / axpy_t / 1e9 if axpy_t > 0 else None
 
@@ -297,6 +332,8 @@ def main():
         "axpy_gather_gbs": axpy_gbs,
         "work": {"gemm_flops": plan.gemm_flops, "axpy_flops": plan.axpy_flops, "axpy_bytes": plan.axpy_bytes},
         "clocks": clk.summary(),
+        "vs_fp64_gpu": compare,
+        "device_status": st,
         "cpu_baseline": cpu,
     }
     if rank == 0:

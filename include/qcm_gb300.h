@@ -180,6 +180,11 @@ int qcm_plan_run_stages(qcm_plan* plan, double* const* bufs, int32_t precision, 
 
 void qcm_plan_destroy(qcm_plan* plan);
 
+/* Sticky status word of the tensor-core executor: 0 = ok, 1 = a bounded wait
+ * for tensor-core completion timed out (the kernel released its TMEM and
+ * returned without writing its tile). */
+int qcm_device_status(int32_t* status);
+
 /* FP64 vector kernels over n elements (deterministic reductions).
  * The result of qcm_dot / qcm_nrm2 is written to a device double. */
 int qcm_dot(const double* x, const double* y, int64_t n, double* result_dev, void* stream);

@@ -166,7 +166,8 @@ void free_stage_device(Stage& st) {
     if (st.d_a) cudaFree(st.d_a);
     if (st.d_b) cudaFree(st.d_b);
     if (st.d_c) cudaFree(st.d_c);
-    st.d_a = st.d_b = st.d_c = nullptr;
+    if (st.d_tcw) cudaFree(st.d_tcw);
+    st.d_a = st.d_b = st.d_c = st.d_tcw = nullptr;
 }
 
 template <class T>
@@ -217,6 +218,10 @@ static int upload_stage(Stage& st) {
         if ((rc = upload_vec(s, &st.d_b))) return rc;
         if ((rc = upload_vec(w, &st.d_c))) return rc;
         st.n_work = (int64_t)w.size();
+        std::vector<int64_t> tw;
+        tc_build_work(st, tw);
+        if ((rc = upload_vec(tw, &st.d_tcw))) return rc;
+        st.n_tcw = (int64_t)tw.size() / 3;
     }
     return QCM_OK;
 }
@@ -233,10 +238,8 @@ static int launch_axpy(const Stage& st, const BufTable& bt, cudaStream_t s) {
 static int launch_gemm(const Stage& st, const BufTable& bt, int precision, cudaStream_t s) {
     if (st.n_work == 0) return QCM_OK;
     if (st.n_work > 0x7fffffffLL) { set_error("gemm work list too large"); return QCM_E_RANGE; }
-    if (precision != QCM_PREC_FP64) {
-        set_error("tensor-core precisions are not available in this build");
-        return QCM_E_STATE;
-    }
+    if (precision != QCM_PREC_FP64)
+        return tc_launch(st.d_a, st.d_b, st.d_tcw, st.n_tcw, bt.p, precision, (void*)s);
     gemm_f64_kernel<<<(unsigned)st.n_work, 256, 0, s>>>(bt, (const DevGemmOut*)st.d_a, (const DevGemmSeg*)st.d_b,
                                                          (const DevGemmWork*)st.d_c);
     QCM_CUDA(cudaGetLastError());

@@ -108,8 +108,10 @@ struct Stage {
     // device copies (owned)
     void* d_a = nullptr;
     void* d_b = nullptr;
-    void* d_c = nullptr;  // work list
+    void* d_c = nullptr;  // work list (FP64 executor, 64 x 64 tiles)
     int64_t n_work = 0;
+    void* d_tcw = nullptr;  // work list (tensor-core executor, 128 x 64 tiles)
+    int64_t n_tcw = 0;
 };
 
 enum PlanKind { PK_SIGMA = 0, PK_BLEFT = 1, PK_BRIGHT = 2 };
@@ -136,4 +138,7 @@ double wigner9j(int, int, int, int, int, int, int, int, int);
 void set_coupling(int a, int b, int c, int d, int e, int f, int g, int h, int i, double init, double out[4]);
 double conjugate_correction(int lc_spin, int rc_spin, int tensor_spin);
 void free_stage_device(Stage& st);
+int tc_build_work(const Stage& st, std::vector<int64_t>& w);
+int tc_launch(const void* d_out, const void* d_seg, const void* d_work, int64_t n_work, double* const* bufs,
+              int precision, void* stream);
 }  // namespace qcm

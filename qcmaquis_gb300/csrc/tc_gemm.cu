@@ -1,0 +1,339 @@
+// Tensor-core (tcgen05 / TMEM) grouped block products for the mixed-precision
+// sigma vector on sm_103a.
+//
+// Same work list as the FP64 executor: every CTA owns one 128 x 64 output tile
+// of one output block and accumulates all of its segments (the split-K over
+// MPO bond indices) in a TMEM accumulator (FP32), then writes the tile once in
+// FP64.  Operands are FP64 in HBM; each K-chunk is loaded, scaled, split into
+// low-precision slices and stored in shared memory in the canonical K-major
+// "no swizzle" UMMA layout (8-row x 16-byte core matrices), from where one
+// elected thread issues tcgen05.mma:
+//   PREC_TF32   : 1 slice, kind::tf32 (round-to-nearest TF32), 1 product;
+//   PREC_BF16X3 : 3 BF16 slices a = a0+a1+a2, 6 products a_i b_j with i+j <= 2.
+// FP32 accumulation in TMEM; completion through tcgen05.commit on an mbarrier.
+// Every wait is bounded: on timeout the kernel records an error code in
+// g_tc_status, still releases its TMEM and returns.
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include <cstdint>
+#include <string>
+
+#include "plan.hpp"
+
+namespace qcm {
+
+constexpr int TC_BM = 128;      // MMA M (one TMEM lane per row)
+constexpr int TC_BN = 64;       // MMA N (64 FP32 TMEM columns)
+constexpr int TC_KB = 64;       // bytes of K per shared-memory chunk (4 core-matrix columns)
+constexpr int TC_THREADS = 128;
+constexpr unsigned TC_SPIN_LIMIT = 1u << 26;
+
+__device__ int g_tc_status = 0;
+
+struct TcOut { int64_t c_off, ldc, M, N, s_begin, s_end; int32_t c_buf, pad; };
+struct TcSeg { int64_t a_off, lda, b_off, ldb, K; double alpha; int32_t a_buf, ta, b_buf, tb; };
+struct TcWork { int64_t out, m0, n0; };
+struct TcBufs { double* p[QCM_NBUF]; };
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// UMMA shared-memory matrix descriptor, K-major, no swizzle (layout type 0), version 1.
+__device__ __forceinline__ uint64_t make_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1u << 46;
+    return d;
+}
+
+// Instruction descriptor: D=F32, A/B format, K-major A and B, N>>3, M>>4.
+__host__ __device__ constexpr uint32_t make_idesc(uint32_t ab_format, int M, int N) {
+    return (1u << 4) | (ab_format << 7) | (ab_format << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// byte offset of element (r, k) of a K-major tile whose rows hold TC_KB bytes, element size E
+template <int E>
+__device__ __forceinline__ uint32_t kmajor_off(int r, int k) {
+    constexpr int T = 16 / E;                 // elements per 16-byte core row
+    constexpr int CPR = TC_KB / 16;           // core-matrix columns per chunk
+    return (uint32_t)((((r >> 3) * CPR) + (k / T)) * 128 + (r & 7) * 16 + (k % T) * E);
+}
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+    for (unsigned it = 0; it < TC_SPIN_LIMIT; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done) : "r"(mbar), "r"(phase) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+template <int PREC>
+struct TcCfg;
+template <>
+struct TcCfg<QCM_PREC_TF32> {
+    static constexpr int E = 4, SLICES = 1, NPROD = 1, KSTEP = 8;
+    static constexpr uint32_t FMT = 2;  // TF32
+};
+template <>
+struct TcCfg<QCM_PREC_BF16X3> {
+    static constexpr int E = 2, SLICES = 3, NPROD = 6, KSTEP = 16;
+    static constexpr uint32_t FMT = 1;  // BF16
+};
+
+template <int PREC>
+__global__ void __launch_bounds__(TC_THREADS)
+tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restrict__ segs,
+               const TcWork* __restrict__ work) {
+    using Cfg = TcCfg<PREC>;
+    constexpr int E = Cfg::E;
+    constexpr int KC = TC_KB / E;                       // elements of K per chunk
+    constexpr uint32_t A_BYTES = TC_BM * TC_KB;         // one slice of the A tile
+    constexpr uint32_t B_BYTES = TC_BN * TC_KB;
+    constexpr uint32_t LBO = 128;                       // next core matrix along K
+    constexpr uint32_t SBO = (TC_KB / 16) * 128;        // next 8-row group
+    constexpr uint32_t IDESC = make_idesc(Cfg::FMT, TC_BM, TC_BN);
+
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* sA = smem;                                  // SLICES x A_BYTES
+    uint8_t* sB = smem + Cfg::SLICES * A_BYTES;          // SLICES x B_BYTES
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base_sh;
+    __shared__ int abort_sh;
+
+    const int tid = threadIdx.x;
+    const int warp = tid / 32, lane = tid % 32;
+    const TcWork w = work[blockIdx.x];
+    const TcOut o = outs[w.out];
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(&tmem_base_sh)), "r"((uint32_t)TC_BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        abort_sh = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base_sh;
+    const uint32_t mbar_a = smem_u32(&mbar);
+
+    uint32_t phase = 0;
+    // FP64 accumulators of this thread's output row (TMEM lane 32*warp + lane),
+    // one per tile column: each segment (one block product of the split-K sum)
+    // is accumulated in FP32 in TMEM, then drained into these.
+    double acc64[TC_BN];
+#pragma unroll
+    for (int j = 0; j < TC_BN; ++j) acc64[j] = 0.0;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+
+    for (int64_t s = o.s_begin; s < o.s_end && !abort_sh; ++s) {
+        const TcSeg g = segs[s];
+        if (g.K <= 0) continue;
+        const double* __restrict__ A = bufs.p[g.a_buf] + g.a_off;
+        const double* __restrict__ B = bufs.p[g.b_buf] + g.b_off;
+        bool first = true;  // first MMA of this segment overwrites the accumulator
+        for (int64_t k0 = 0; k0 < g.K; k0 += KC) {
+            // ---- A chunk: TC_BM x KC, scaled by alpha, split into slices
+            for (int idx = tid; idx < TC_BM * KC; idx += TC_THREADS) {
+                int m, k;
+                if (g.ta) { k = idx % KC; m = idx / KC; } else { m = idx % TC_BM; k = idx / TC_BM; }
+                const int64_t gm = w.m0 + m, gk = k0 + k;
+                double v = 0.0;
+                if (gm < o.M && gk < g.K) v = g.alpha * (g.ta ? A[gk + gm * g.lda] : A[gm + gk * g.lda]);
+                const uint32_t off = kmajor_off<E>(m, k);
+                if constexpr (PREC == QCM_PREC_TF32) {
+                    *reinterpret_cast<uint32_t*>(sA + off) = to_tf32((float)v);
+                } else {
+                    __nv_bfloat16 h0 = __double2bfloat16(v);
+                    double r1 = v - (double)__bfloat162float(h0);
+                    __nv_bfloat16 h1 = __double2bfloat16(r1);
+                    double r2 = r1 - (double)__bfloat162float(h1);
+                    __nv_bfloat16 h2 = __double2bfloat16(r2);
+                    *reinterpret_cast<__nv_bfloat16*>(sA + off) = h0;
+                    *reinterpret_cast<__nv_bfloat16*>(sA + A_BYTES + off) = h1;
+                    *reinterpret_cast<__nv_bfloat16*>(sA + 2 * A_BYTES + off) = h2;
+                }
+            }
+            // ---- B chunk: stored as N x K (K-major), element (n, k) = op(B)[k][n]
+            for (int idx = tid; idx < TC_BN * KC; idx += TC_THREADS) {
+                int n, k;
+                if (g.tb) { n = idx % TC_BN; k = idx / TC_BN; } else { k = idx % KC; n = idx / KC; }
+                const int64_t gn = w.n0 + n, gk = k0 + k;
+                double v = 0.0;
+                if (gn < o.N && gk < g.K) v = g.tb ? B[gn + gk * g.ldb] : B[gk + gn * g.ldb];
+                const uint32_t off = kmajor_off<E>(n, k);
+                if constexpr (PREC == QCM_PREC_TF32) {
+                    *reinterpret_cast<uint32_t*>(sB + off) = to_tf32((float)v);
+                } else {
+                    __nv_bfloat16 h0 = __double2bfloat16(v);
+                    double r1 = v - (double)__bfloat162float(h0);
+                    __nv_bfloat16 h1 = __double2bfloat16(r1);
+                    double r2 = r1 - (double)__bfloat162float(h1);
+                    __nv_bfloat16 h2 = __double2bfloat16(r2);
+                    *reinterpret_cast<__nv_bfloat16*>(sB + off) = h0;
+                    *reinterpret_cast<__nv_bfloat16*>(sB + B_BYTES + off) = h1;
+                    *reinterpret_cast<__nv_bfloat16*>(sB + 2 * B_BYTES + off) = h2;
+                }
+            }
+            // make the generic-proxy smem writes visible to the tensor core (async proxy)
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncthreads();
+            if (tid == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+#pragma unroll
+                for (int kk = 0; kk < KC / Cfg::KSTEP; ++kk) {
+                    const uint32_t koff = kk * Cfg::KSTEP * E / 16 * LBO;  // core columns per K step
+#pragma unroll
+                    for (int p = 0; p < Cfg::NPROD; ++p) {
+                        // products a_i b_j with i + j <= 2, largest first
+                        const int ia = (Cfg::NPROD == 1) ? 0 : (p == 0 ? 0 : p == 1 ? 0 : p == 2 ? 1 : p == 3 ? 0 : p == 4 ? 1 : 2);
+                        const int ib = (Cfg::NPROD == 1) ? 0 : (p == 0 ? 0 : p == 1 ? 1 : p == 2 ? 0 : p == 3 ? 2 : p == 4 ? 1 : 0);
+                        const uint64_t da = make_sdesc(a0 + ia * A_BYTES + koff, LBO, SBO);
+                        const uint64_t db = make_sdesc(b0 + ib * B_BYTES + koff, LBO, SBO);
+                        const uint32_t accf = first ? 0u : 1u;
+                        if constexpr (PREC == QCM_PREC_TF32) {
+                            asm volatile(
+                                "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
+                                :: "r"(tmem), "l"(da), "l"(db), "r"(IDESC), "r"(accf));
+                        } else {
+                            asm volatile(
+                                "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+                                :: "r"(tmem), "l"(da), "l"(db), "r"(IDESC), "r"(accf));
+                        }
+                        first = false;
+                    }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                             :: "r"(mbar_a) : "memory");
+            }
+            first = false;
+            // all threads: wait until the MMAs have consumed shared memory
+            if (!mbar_wait(mbar_a, phase)) {
+                if (tid == 0) { atomicExch(&g_tc_status, 1); abort_sh = 1; }
+            }
+            phase ^= 1u;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            __syncthreads();
+            if (abort_sh) break;
+        }
+        if (abort_sh) break;
+        // ---- drain this segment's FP32 partial product into the FP64 accumulators
+#pragma unroll
+        for (int c0 = 0; c0 < TC_BN; c0 += 16) {
+            uint32_t r[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(trow + (uint32_t)c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < 16; ++j) acc64[c0 + j] += (double)__uint_as_float(r[j]);
+        }
+        // the next segment's first MMA overwrites TMEM: all reads must be done
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+    }
+
+    // ---- epilogue: FP64 accumulators -> output tile
+    double* __restrict__ C = bufs.p[o.c_buf] + o.c_off;
+    const int64_t row = w.m0 + warp * 32 + lane;
+    if (!abort_sh && row < o.M) {
+#pragma unroll
+        for (int j = 0; j < TC_BN; ++j) {
+            const int64_t col = w.n0 + j;
+            if (col < o.N) C[row + col * o.ldc] = acc64[j];
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"((uint32_t)TC_BN));
+    }
+}
+
+// Dynamic shared memory per CTA.  Padded to at least 32 KiB so that no more than
+// 7 CTAs share an SM: each holds 64 TMEM columns and an SM has 512.
+static int tc_smem_bytes(int precision) {
+    int slices = (precision == QCM_PREC_BF16X3) ? 3 : 1;
+    int need = slices * (TC_BM + TC_BN) * TC_KB;
+    return need < 32768 ? 32768 : need;
+}
+
+// Work list for the tensor-core executor: 128 x 64 tiles.
+int tc_build_work(const Stage& st, std::vector<int64_t>& w) {
+    w.clear();
+    for (size_t i = 0; i < st.gout.size(); ++i) {
+        const GemmOut& g = st.gout[i];
+        for (int64_t m0 = 0; m0 < g.M; m0 += TC_BM)
+            for (int64_t n0 = 0; n0 < g.N; n0 += TC_BN) {
+                w.push_back((int64_t)i);
+                w.push_back(m0);
+                w.push_back(n0);
+            }
+    }
+    return QCM_OK;
+}
+
+int tc_launch(const void* d_out, const void* d_seg, const void* d_work, int64_t n_work, double* const* bufs,
+              int precision, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_work == 0) return QCM_OK;
+    if (n_work > 0x7fffffffLL) { set_error("tensor-core work list too large"); return QCM_E_RANGE; }
+    TcBufs tb;
+    for (int i = 0; i < QCM_NBUF; ++i) tb.p[i] = bufs[i];
+    const int smem = tc_smem_bytes(precision);
+    cudaError_t e;
+    if (precision == QCM_PREC_TF32) {
+        e = cudaFuncSetAttribute(tc_gemm_kernel<QCM_PREC_TF32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) { set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e)); return QCM_E_CUDA; }
+        tc_gemm_kernel<QCM_PREC_TF32><<<(unsigned)n_work, TC_THREADS, smem, s>>>(
+            tb, (const TcOut*)d_out, (const TcSeg*)d_seg, (const TcWork*)d_work);
+    } else if (precision == QCM_PREC_BF16X3) {
+        e = cudaFuncSetAttribute(tc_gemm_kernel<QCM_PREC_BF16X3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) { set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e)); return QCM_E_CUDA; }
+        tc_gemm_kernel<QCM_PREC_BF16X3><<<(unsigned)n_work, TC_THREADS, smem, s>>>(
+            tb, (const TcOut*)d_out, (const TcSeg*)d_seg, (const TcWork*)d_work);
+    } else {
+        set_error("unknown tensor-core precision");
+        return QCM_E_INVALID;
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) { set_error(std::string("tc_gemm launch: ") + cudaGetErrorString(e)); return QCM_E_CUDA; }
+    return QCM_OK;
+}
+
+}  // namespace qcm
+
+extern "C" int qcm_device_status(int32_t* status) {
+    if (!status) { qcm::set_error("null status"); return QCM_E_INVALID; }
+    int v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, qcm::g_tc_status, sizeof(int));
+    if (e != cudaSuccess) { qcm::set_error(std::string("cudaMemcpyFromSymbol: ") + cudaGetErrorString(e)); return QCM_E_CUDA; }
+    *status = v;
+    return QCM_OK;
+}

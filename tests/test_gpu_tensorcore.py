@@ -1,0 +1,60 @@
+"""Mixed-precision sigma vectors on the tcgen05 tensor cores against the FP64
+sigma: BF16x3 (6 split products, FP32 accumulation) within 2e-5 relative,
+TF32 within 5e-3 relative; the executor's bounded waits never time out."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from qcmaquis_gb300 import native as N
+
+from test_oracle import _random_site_problem
+
+pytestmark = pytest.mark.gpu
+
+TOL = {N.PREC_BF16X3: 2e-5, N.PREC_TF32: 5e-3}
+
+
+def _status():
+    s = C.c_int32(-1)
+    N.check(N.lib().qcm_device_status(C.byref(s)), "qcm_device_status")
+    return s.value
+
+
+def _sigma_all_precisions(eng, psi, L, R, W):
+    outs = {}
+    for prec in (N.PREC_FP64, N.PREC_TF32, N.PREC_BF16X3):
+        outs[prec] = eng.site_hamil2(psi, L, R, W, precision=prec).data.clone()
+    torch.cuda.synchronize()
+    return outs
+
+
+@pytest.mark.parametrize("site,m", [(2, 16), (2, 40)])
+def test_tensorcore_sigma_small(site, m):
+    from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
+    psi, left, right, ts = _random_site_problem(site=site, m=m)
+    psi = psi.copy().make_left_paired()
+    eng = Engine("cuda:0")
+    o = _sigma_all_precisions(eng, DeviceMPSTensor.from_host(psi), DeviceBoundary.from_host(left),
+                              DeviceBoundary.from_host(right), ts)
+    ref = o[N.PREC_FP64]
+    for prec, tol in TOL.items():
+        err = (torch.linalg.norm(o[prec] - ref) / torch.linalg.norm(ref)).item()
+        assert err < tol, (prec, err)
+    assert _status() == 0
+
+
+def test_tensorcore_sigma_multi_tile():
+    """L=12, m=256: output blocks span several 128 x 64 tiles."""
+    from qcmaquis_gb300.engine import Engine
+    from qcmaquis_gb300.workloads import build_sigma_host, upload_sigma_workload
+    w = build_sigma_host(L=12, nelec=12, m=256)
+    eng = Engine("cuda:0")
+    upload_sigma_workload(w, eng)
+    o = _sigma_all_precisions(eng, w.psi, w.left, w.right, w.ts_mpo)
+    ref = o[N.PREC_FP64]
+    for prec, tol in TOL.items():
+        err = (torch.linalg.norm(o[prec] - ref) / torch.linalg.norm(ref)).item()
+        assert err < tol, (prec, err)
+    assert _status() == 0
