@@ -221,8 +221,10 @@ def main():
         torch.cuda.synchronize()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
+        torch.cuda.nvtx.range_push("sigma")
         for _ in range(args.steps):
             eng.site_hamil2(w.psi, w.left, w.right, w.ts_mpo, out=out)
+        torch.cuda.nvtx.range_pop()
         ev1.record(stream)
         torch.cuda.synchronize()
     t_step = ev0.elapsed_time(ev1) / 1e3 / args.steps

@@ -502,6 +502,47 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
     return C;
 }
 
+// Split-K for grouped GEMM outputs with long segment lists: every output with
+// more than `max_segs` segments is cut into parts of at most `max_segs`
+// segments; each part writes its partial tile to `buf` (dense, ld = M) and a
+// gather stage sums the parts into the output in part order.  Outputs that are
+// short enough keep writing the output directly.  Results stay independent of
+// scheduling; the FP64 sums differ from the unsplit order only by rounding.
+static void split_k(Stage& g, int buf, int64_t base, int64_t max_segs, Stage& red, int64_t& end) {
+    std::vector<GemmOut> outs;
+    red.kind = ST_AXPY;
+    int64_t off = base;
+    for (const GemmOut& o : g.gout) {
+        int64_t nseg = o.s_end - o.s_begin;
+        if (nseg <= max_segs) {
+            outs.push_back(o);
+            continue;
+        }
+        AxpyOut r;
+        r.dst_buf = o.c_buf;
+        r.dst_off = o.c_off;
+        r.ldd = o.ldc;
+        r.rows = o.M;
+        r.cols = o.N;
+        r.t_begin = (int64_t)red.aterm.size();
+        for (int64_t s0 = o.s_begin; s0 < o.s_end; s0 += max_segs) {
+            GemmOut p = o;
+            p.c_buf = buf;
+            p.c_off = off;
+            p.ldc = o.M;
+            p.s_begin = s0;
+            p.s_end = std::min(o.s_end, s0 + max_segs);
+            outs.push_back(p);
+            red.aterm.push_back({buf, off, o.M, 1.0});
+            off += o.M * o.N;
+        }
+        r.t_end = (int64_t)red.aterm.size();
+        red.aout.push_back(r);
+    }
+    g.gout.swap(outs);
+    end = off;
+}
+
 static void finalize_boundary_layout(qcm_plan* P, std::vector<BM>& out) {
     int64_t base = 0;
     P->out_blk_ptr.assign(1, 0);
@@ -590,8 +631,13 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
         o.s_end = (int64_t)s3.gseg.size();
         s3.gout.push_back(o);
     }
+    // split-K over the MPO bond sum: partial tiles in scratch 1 (T is dead after K2)
+    Stage s4;
+    int64_t part_end = 0;
+    split_k(s3, QCM_BUF_S1, 0, 32, s4, part_end);
+    for (auto& a : s4.aout) P->axpy_bytes += 8.0 * a.rows * a.cols * (double)(a.t_end - a.t_begin + 1);
     P->scratch[0] = rp_end;
-    P->scratch[1] = t_end;
+    P->scratch[1] = std::max(t_end, part_end);
     P->scratch[2] = c_end;
     P->stages.push_back(std::move(z0));
     P->stages.push_back(std::move(s0));
@@ -599,6 +645,7 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
     P->stages.push_back(std::move(z2));
     P->stages.push_back(std::move(s2));
     P->stages.push_back(std::move(s3));
+    if (!s4.aout.empty()) P->stages.push_back(std::move(s4));
     return P;
 }
 

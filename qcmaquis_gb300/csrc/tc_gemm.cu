@@ -26,7 +26,7 @@ namespace qcm {
 constexpr int TC_BM = 128;      // MMA M (one TMEM lane per row)
 constexpr int TC_BN = 64;       // MMA N (64 FP32 TMEM columns)
 constexpr int TC_KB = 64;       // bytes of K per shared-memory chunk (4 core-matrix columns)
-constexpr int TC_THREADS = 128;
+constexpr int TC_THREADS = 256;
 constexpr unsigned TC_SPIN_LIMIT = 1u << 26;
 
 __device__ int g_tc_status = 0;
@@ -95,6 +95,24 @@ struct TcCfg<QCM_PREC_BF16X3> {
     static constexpr uint32_t FMT = 1;  // BF16
 };
 
+// Split one FP64 value into the operand format and store it at byte offset `off`
+// of slice 0 (further slices follow at `slice_bytes` strides).
+template <int PREC>
+__device__ __forceinline__ void put_operand(uint8_t* base, uint32_t off, uint32_t slice_bytes, double v) {
+    if constexpr (PREC == QCM_PREC_TF32) {
+        *reinterpret_cast<uint32_t*>(base + off) = to_tf32((float)v);
+    } else {
+        __nv_bfloat16 h0 = __double2bfloat16(v);
+        double r1 = v - (double)__bfloat162float(h0);
+        __nv_bfloat16 h1 = __double2bfloat16(r1);
+        double r2 = r1 - (double)__bfloat162float(h1);
+        __nv_bfloat16 h2 = __double2bfloat16(r2);
+        *reinterpret_cast<__nv_bfloat16*>(base + off) = h0;
+        *reinterpret_cast<__nv_bfloat16*>(base + slice_bytes + off) = h1;
+        *reinterpret_cast<__nv_bfloat16*>(base + 2 * slice_bytes + off) = h2;
+    }
+}
+
 template <int PREC>
 __global__ void __launch_bounds__(TC_THREADS)
 tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restrict__ segs,
@@ -104,19 +122,20 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
     constexpr int KC = TC_KB / E;                       // elements of K per chunk
     constexpr uint32_t A_BYTES = TC_BM * TC_KB;         // one slice of the A tile
     constexpr uint32_t B_BYTES = TC_BN * TC_KB;
+    constexpr uint32_t STAGE_BYTES = Cfg::SLICES * (A_BYTES + B_BYTES);
     constexpr uint32_t LBO = 128;                       // next core matrix along K
     constexpr uint32_t SBO = (TC_KB / 16) * 128;        // next 8-row group
     constexpr uint32_t IDESC = make_idesc(Cfg::FMT, TC_BM, TC_BN);
+    constexpr int NSTAGE = 2;
 
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t* sA = smem;                                  // SLICES x A_BYTES
-    uint8_t* sB = smem + Cfg::SLICES * A_BYTES;          // SLICES x B_BYTES
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[NSTAGE];
     __shared__ uint32_t tmem_base_sh;
-    __shared__ int abort_sh;
 
     const int tid = threadIdx.x;
     const int warp = tid / 32, lane = tid % 32;
+    const int quad = warp & 3;      // TMEM lanes 32*quad .. 32*quad+31 (tile rows)
+    const int chalf = warp >> 2;    // tile columns 32*chalf .. 32*chalf+31
     const TcWork w = work[blockIdx.x];
     const TcOut o = outs[w.out];
 
@@ -126,75 +145,60 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar)));
+        for (int i = 0; i < NSTAGE; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar[i])));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        abort_sh = 0;
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_sh;
-    const uint32_t mbar_a = smem_u32(&mbar);
+    const uint32_t trow = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(chalf * 32);
 
-    uint32_t phase = 0;
-    // FP64 accumulators of this thread's output row (TMEM lane 32*warp + lane),
-    // one per tile column: each segment (one block product of the split-K sum)
-    // is accumulated in FP32 in TMEM, then drained into these.
-    double acc64[TC_BN];
+    uint32_t phase[NSTAGE] = {0u, 0u};
+    bool pending[NSTAGE] = {false, false};
+    bool aborted = false;
+    // FP64 accumulators of this thread's row and 32 columns: each segment (one
+    // block product of the split-K sum) accumulates in FP32 in TMEM, then is
+    // drained into these.
+    double acc64[32];
 #pragma unroll
-    for (int j = 0; j < TC_BN; ++j) acc64[j] = 0.0;
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int j = 0; j < 32; ++j) acc64[j] = 0.0;
+    int chunk = 0;
 
-    for (int64_t s = o.s_begin; s < o.s_end && !abort_sh; ++s) {
+    for (int64_t s = o.s_begin; s < o.s_end && !aborted; ++s) {
         const TcSeg g = segs[s];
         if (g.K <= 0) continue;
         const double* __restrict__ A = bufs.p[g.a_buf] + g.a_off;
         const double* __restrict__ B = bufs.p[g.b_buf] + g.b_off;
-        bool first = true;  // first MMA of this segment overwrites the accumulator
+        bool first = true;  // the first MMA of a segment overwrites the accumulator
         for (int64_t k0 = 0; k0 < g.K; k0 += KC) {
-            // ---- A chunk: TC_BM x KC, scaled by alpha, split into slices
+            const int st = chunk & 1;
+            uint8_t* sA = smem + st * STAGE_BYTES;
+            uint8_t* sB = sA + Cfg::SLICES * A_BYTES;
+            // the MMAs that last read this stage must have finished before it is overwritten
+            if (pending[st]) {
+                int to = mbar_wait(smem_u32(&mbar[st]), phase[st]) ? 0 : 1;
+                phase[st] ^= 1u;
+                pending[st] = false;
+                if (__syncthreads_or(to)) { aborted = true; break; }
+            }
             for (int idx = tid; idx < TC_BM * KC; idx += TC_THREADS) {
                 int m, k;
                 if (g.ta) { k = idx % KC; m = idx / KC; } else { m = idx % TC_BM; k = idx / TC_BM; }
                 const int64_t gm = w.m0 + m, gk = k0 + k;
                 double v = 0.0;
                 if (gm < o.M && gk < g.K) v = g.alpha * (g.ta ? A[gk + gm * g.lda] : A[gm + gk * g.lda]);
-                const uint32_t off = kmajor_off<E>(m, k);
-                if constexpr (PREC == QCM_PREC_TF32) {
-                    *reinterpret_cast<uint32_t*>(sA + off) = to_tf32((float)v);
-                } else {
-                    __nv_bfloat16 h0 = __double2bfloat16(v);
-                    double r1 = v - (double)__bfloat162float(h0);
-                    __nv_bfloat16 h1 = __double2bfloat16(r1);
-                    double r2 = r1 - (double)__bfloat162float(h1);
-                    __nv_bfloat16 h2 = __double2bfloat16(r2);
-                    *reinterpret_cast<__nv_bfloat16*>(sA + off) = h0;
-                    *reinterpret_cast<__nv_bfloat16*>(sA + A_BYTES + off) = h1;
-                    *reinterpret_cast<__nv_bfloat16*>(sA + 2 * A_BYTES + off) = h2;
-                }
+                put_operand<PREC>(sA, kmajor_off<E>(m, k), A_BYTES, v);
             }
-            // ---- B chunk: stored as N x K (K-major), element (n, k) = op(B)[k][n]
             for (int idx = tid; idx < TC_BN * KC; idx += TC_THREADS) {
                 int n, k;
                 if (g.tb) { n = idx % TC_BN; k = idx / TC_BN; } else { k = idx % KC; n = idx / KC; }
                 const int64_t gn = w.n0 + n, gk = k0 + k;
                 double v = 0.0;
                 if (gn < o.N && gk < g.K) v = g.tb ? B[gn + gk * g.ldb] : B[gk + gn * g.ldb];
-                const uint32_t off = kmajor_off<E>(n, k);
-                if constexpr (PREC == QCM_PREC_TF32) {
-                    *reinterpret_cast<uint32_t*>(sB + off) = to_tf32((float)v);
-                } else {
-                    __nv_bfloat16 h0 = __double2bfloat16(v);
-                    double r1 = v - (double)__bfloat162float(h0);
-                    __nv_bfloat16 h1 = __double2bfloat16(r1);
-                    double r2 = r1 - (double)__bfloat162float(h1);
-                    __nv_bfloat16 h2 = __double2bfloat16(r2);
-                    *reinterpret_cast<__nv_bfloat16*>(sB + off) = h0;
-                    *reinterpret_cast<__nv_bfloat16*>(sB + B_BYTES + off) = h1;
-                    *reinterpret_cast<__nv_bfloat16*>(sB + 2 * B_BYTES + off) = h2;
-                }
+                put_operand<PREC>(sB, kmajor_off<E>(n, k), B_BYTES, v);
             }
-            // make the generic-proxy smem writes visible to the tensor core (async proxy)
+            // generic-proxy shared-memory writes -> visible to the tensor core (async proxy)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncthreads();
@@ -203,7 +207,7 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
                 const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
 #pragma unroll
                 for (int kk = 0; kk < KC / Cfg::KSTEP; ++kk) {
-                    const uint32_t koff = kk * Cfg::KSTEP * E / 16 * LBO;  // core columns per K step
+                    const uint32_t koff = kk * Cfg::KSTEP * E / 16 * LBO;
 #pragma unroll
                     for (int p = 0; p < Cfg::NPROD; ++p) {
                         // products a_i b_j with i + j <= 2, largest first
@@ -211,7 +215,7 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
                         const int ib = (Cfg::NPROD == 1) ? 0 : (p == 0 ? 0 : p == 1 ? 1 : p == 2 ? 0 : p == 3 ? 2 : p == 4 ? 1 : 0);
                         const uint64_t da = make_sdesc(a0 + ia * A_BYTES + koff, LBO, SBO);
                         const uint64_t db = make_sdesc(b0 + ib * B_BYTES + koff, LBO, SBO);
-                        const uint32_t accf = first ? 0u : 1u;
+                        const uint32_t accf = (first && kk == 0 && p == 0) ? 0u : 1u;
                         if constexpr (PREC == QCM_PREC_TF32) {
                             asm volatile(
                                 "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -223,26 +227,29 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
                                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
                                 :: "r"(tmem), "l"(da), "l"(db), "r"(IDESC), "r"(accf));
                         }
-                        first = false;
                     }
                 }
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                             :: "r"(mbar_a) : "memory");
+                             :: "r"(smem_u32(&mbar[st])) : "memory");
             }
             first = false;
-            // all threads: wait until the MMAs have consumed shared memory
-            if (!mbar_wait(mbar_a, phase)) {
-                if (tid == 0) { atomicExch(&g_tc_status, 1); abort_sh = 1; }
-            }
-            phase ^= 1u;
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            __syncthreads();
-            if (abort_sh) break;
+            pending[st] = true;
+            ++chunk;
         }
-        if (abort_sh) break;
-        // ---- drain this segment's FP32 partial product into the FP64 accumulators
+        if (aborted) break;
+        // segment complete: wait for its MMAs, then drain TMEM into the FP64 accumulators
+        int to = 0;
+        for (int i = 0; i < NSTAGE; ++i) {
+            if (pending[i]) {
+                if (!mbar_wait(smem_u32(&mbar[i]), phase[i])) to = 1;
+                phase[i] ^= 1u;
+                pending[i] = false;
+            }
+        }
+        if (__syncthreads_or(to)) { aborted = true; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-        for (int c0 = 0; c0 < TC_BN; c0 += 16) {
+        for (int c0 = 0; c0 < 32; c0 += 16) {
             uint32_t r[16];
             asm volatile(
                 "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -254,18 +261,19 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
 #pragma unroll
             for (int j = 0; j < 16; ++j) acc64[c0 + j] += (double)__uint_as_float(r[j]);
         }
-        // the next segment's first MMA overwrites TMEM: all reads must be done
+        // the next segment's first MMA overwrites TMEM: all reads must be complete
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
     }
+    if (aborted && tid == 0) atomicExch(&g_tc_status, 1);
 
-    // ---- epilogue: FP64 accumulators -> output tile
+    // ---- epilogue: FP64 accumulators -> output tile (written once)
     double* __restrict__ C = bufs.p[o.c_buf] + o.c_off;
-    const int64_t row = w.m0 + warp * 32 + lane;
-    if (!abort_sh && row < o.M) {
+    const int64_t row = w.m0 + quad * 32 + lane;
+    if (!aborted && row < o.M) {
 #pragma unroll
-        for (int j = 0; j < TC_BN; ++j) {
-            const int64_t col = w.n0 + j;
+        for (int j = 0; j < 32; ++j) {
+            const int64_t col = w.n0 + chalf * 32 + j;
             if (col < o.N) C[row + col * o.ldc] = acc64[j];
         }
     }
@@ -280,7 +288,7 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
 // 7 CTAs share an SM: each holds 64 TMEM columns and an SM has 512.
 static int tc_smem_bytes(int precision) {
     int slices = (precision == QCM_PREC_BF16X3) ? 3 : 1;
-    int need = slices * (TC_BM + TC_BN) * TC_KB;
+    int need = 2 * slices * (TC_BM + TC_BN) * TC_KB;  // two pipeline stages
     return need < 32768 ? 32768 : need;
 }
 
