@@ -242,7 +242,7 @@ def main():
         for si in range(len(kinds)):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            eng.run(plan, ket=w.psi.data, left=w.left.data, right=w.right.data, out=out, first=si, last=si)
+            eng.run(plan, ket=w.psi.data, left=w.left, right=w.right, out=out, first=si, last=si)
             b.record(stream)
             torch.cuda.synchronize()
             stage_t[si] += a.elapsed_time(b) / 1e3 / reps

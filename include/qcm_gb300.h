@@ -178,6 +178,13 @@ int qcm_plan_run(qcm_plan* plan, double* const* bufs, int32_t precision, void* s
 int qcm_plan_run_stages(qcm_plan* plan, double* const* bufs, int32_t precision, void* stream, int32_t first,
                         int32_t last);
 
+/* Run with explicit element types: bit i of f32mask marks buffer slot i as FP32.
+ * The FP64 form requires f32mask == 0.  The mixed forms accept FP32 or FP64 for
+ * every slot; qcm_plan_run uses FP32 scratch and FP64 caller slots, and callers
+ * that keep FP32 copies of the boundaries set the LEFT/RIGHT bits as well. */
+int qcm_plan_run_typed(qcm_plan* plan, double* const* bufs, uint32_t f32mask, int32_t precision, void* stream,
+                       int32_t first, int32_t last);
+
 void qcm_plan_destroy(qcm_plan* plan);
 
 /* Sticky status word of the tensor-core executor: 0 = ok, 1 = a bounded wait

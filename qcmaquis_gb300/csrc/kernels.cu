@@ -39,27 +39,34 @@ struct DevGemmOut { int64_t c_off, ldc, M, N, s_begin, s_end; int32_t c_buf, pad
 struct DevGemmSeg { int64_t a_off, lda, b_off, ldb, K; double alpha; int32_t a_buf, ta, b_buf, tb; };
 struct DevGemmWork { int64_t out, m0, n0; };
 
-struct BufTable { double* p[QCM_NBUF]; };
+// Buffer table of one plan run.  Bit i of f32mask marks slot i as FP32 (the
+// mixed-precision forms keep boundary shadows and all intermediates in FP32);
+// every other slot holds FP64.
+struct BufTable { double* p[QCM_NBUF]; uint32_t f32mask; };
+
+__device__ __forceinline__ bool slot_f32(const BufTable& b, int slot) { return (b.f32mask >> slot) & 1u; }
 
 // ------------------------------------------------------------------ gather-axpy
 constexpr int AXPY_THREADS = 256;
 constexpr int AXPY_TERM_CACHE = 128;
 
+// ACC = double for the FP64 form, float for the mixed forms (FP32 intermediates).
+template <class ACC>
 __global__ void __launch_bounds__(AXPY_THREADS)
 gather_axpy_kernel(BufTable bufs, const DevAxpyOut* __restrict__ outs, const DevAxpyTerm* __restrict__ terms,
                    const DevAxpyWork* __restrict__ work) {
-    __shared__ double s_alpha[AXPY_TERM_CACHE];
-    __shared__ const double* s_src[AXPY_TERM_CACHE];
+    __shared__ ACC s_alpha[AXPY_TERM_CACHE];
+    __shared__ const void* s_src[AXPY_TERM_CACHE];
     __shared__ int64_t s_lds[AXPY_TERM_CACHE];
+    __shared__ int s_f32[AXPY_TERM_CACHE];
     const DevAxpyWork w = work[blockIdx.x];
     const DevAxpyOut o = outs[w.out];
-    double* __restrict__ dst = bufs.p[o.dst_buf] + o.dst_off;
+    const bool dst32 = slot_f32(bufs, o.dst_buf);
     const int64_t rows = o.rows;
     const int64_t nel = rows * (w.c1 - w.c0);
     const int64_t nterm = o.t_end - o.t_begin;
-    // each thread keeps up to 4 accumulators (elements e, e+256, ...)
     for (int64_t base = 0; base < nel; base += 4 * AXPY_THREADS) {
-        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        ACC acc[4] = {ACC(0), ACC(0), ACC(0), ACC(0)};
         int64_t ii[4], jj[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -72,26 +79,41 @@ gather_axpy_kernel(BufTable bufs, const DevAxpyOut* __restrict__ outs, const Dev
             __syncthreads();
             for (int64_t t = threadIdx.x; t < tn; t += AXPY_THREADS) {
                 const DevAxpyTerm tt = terms[o.t_begin + t0 + t];
-                s_alpha[t] = tt.alpha;
-                s_src[t] = bufs.p[tt.src_buf] + tt.src_off;
+                const bool f32 = slot_f32(bufs, tt.src_buf);
+                s_alpha[t] = (ACC)tt.alpha;
+                s_src[t] = f32 ? (const void*)((const float*)bufs.p[tt.src_buf] + tt.src_off)
+                               : (const void*)(bufs.p[tt.src_buf] + tt.src_off);
                 s_lds[t] = tt.lds;
+                s_f32[t] = f32 ? 1 : 0;
             }
             __syncthreads();
             for (int64_t t = 0; t < tn; ++t) {
-                const double a = s_alpha[t];
-                const double* __restrict__ src = s_src[t];
+                const ACC a = s_alpha[t];
                 const int64_t lds = s_lds[t];
+                if (s_f32[t]) {
+                    const float* __restrict__ src = (const float*)s_src[t];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    int64_t e = base + threadIdx.x + (int64_t)u * AXPY_THREADS;
-                    if (e < nel) acc[u] = fma(a, __ldg(src + ii[u] + jj[u] * lds), acc[u]);
+                    for (int u = 0; u < 4; ++u) {
+                        int64_t e = base + threadIdx.x + (int64_t)u * AXPY_THREADS;
+                        if (e < nel) acc[u] = fma(a, (ACC)__ldg(src + ii[u] + jj[u] * lds), acc[u]);
+                    }
+                } else {
+                    const double* __restrict__ src = (const double*)s_src[t];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        int64_t e = base + threadIdx.x + (int64_t)u * AXPY_THREADS;
+                        if (e < nel) acc[u] = fma(a, (ACC)__ldg(src + ii[u] + jj[u] * lds), acc[u]);
+                    }
                 }
             }
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             int64_t e = base + threadIdx.x + (int64_t)u * AXPY_THREADS;
-            if (e < nel) dst[ii[u] + jj[u] * o.ldd] = acc[u];
+            if (e < nel) {
+                if (dst32) ((float*)bufs.p[o.dst_buf])[o.dst_off + ii[u] + jj[u] * o.ldd] = (float)acc[u];
+                else bufs.p[o.dst_buf][o.dst_off + ii[u] + jj[u] * o.ldd] = (double)acc[u];
+            }
         }
     }
 }
@@ -226,11 +248,15 @@ static int upload_stage(Stage& st) {
     return QCM_OK;
 }
 
-static int launch_axpy(const Stage& st, const BufTable& bt, cudaStream_t s) {
+static int launch_axpy(const Stage& st, const BufTable& bt, int precision, cudaStream_t s) {
     if (st.n_work == 0) return QCM_OK;
     if (st.n_work > 0x7fffffffLL) { set_error("axpy work list too large"); return QCM_E_RANGE; }
-    gather_axpy_kernel<<<(unsigned)st.n_work, AXPY_THREADS, 0, s>>>(
-        bt, (const DevAxpyOut*)st.d_a, (const DevAxpyTerm*)st.d_b, (const DevAxpyWork*)st.d_c);
+    if (precision == QCM_PREC_FP64)
+        gather_axpy_kernel<double><<<(unsigned)st.n_work, AXPY_THREADS, 0, s>>>(
+            bt, (const DevAxpyOut*)st.d_a, (const DevAxpyTerm*)st.d_b, (const DevAxpyWork*)st.d_c);
+    else
+        gather_axpy_kernel<float><<<(unsigned)st.n_work, AXPY_THREADS, 0, s>>>(
+            bt, (const DevAxpyOut*)st.d_a, (const DevAxpyTerm*)st.d_b, (const DevAxpyWork*)st.d_c);
     QCM_CUDA(cudaGetLastError());
     return QCM_OK;
 }
@@ -239,7 +265,8 @@ static int launch_gemm(const Stage& st, const BufTable& bt, int precision, cudaS
     if (st.n_work == 0) return QCM_OK;
     if (st.n_work > 0x7fffffffLL) { set_error("gemm work list too large"); return QCM_E_RANGE; }
     if (precision != QCM_PREC_FP64)
-        return tc_launch(st.d_a, st.d_b, st.d_tcw, st.n_tcw, bt.p, precision, (void*)s);
+        return tc_launch(st.d_a, st.d_b, st.d_tcw, st.n_tcw, bt.p, bt.f32mask, precision, (void*)s);
+    if (bt.f32mask) { set_error("the FP64 form takes FP64 buffers only"); return QCM_E_INVALID; }
     gemm_f64_kernel<<<(unsigned)st.n_work, 256, 0, s>>>(bt, (const DevGemmOut*)st.d_a, (const DevGemmSeg*)st.d_b,
                                                          (const DevGemmWork*)st.d_c);
     QCM_CUDA(cudaGetLastError());
@@ -408,6 +435,14 @@ int qcm_plan_run(qcm_plan* p, double* const* bufs, int32_t precision, void* stre
 
 int qcm_plan_run_stages(qcm_plan* p, double* const* bufs, int32_t precision, void* stream, int32_t first,
                         int32_t last) {
+    // FP64 form: every slot FP64.  Mixed forms: scratch slots FP32, caller slots FP64.
+    uint32_t mask = (precision == QCM_PREC_FP64) ? 0u
+                                                 : ((1u << QCM_BUF_S0) | (1u << QCM_BUF_S1) | (1u << QCM_BUF_S2));
+    return qcm_plan_run_typed(p, bufs, mask, precision, stream, first, last);
+}
+
+int qcm_plan_run_typed(qcm_plan* p, double* const* bufs, uint32_t f32mask, int32_t precision, void* stream,
+                       int32_t first, int32_t last) {
     if (!p || !bufs) { set_error("null argument"); return QCM_E_INVALID; }
     if (last < 0 || last >= (int32_t)p->stages.size()) last = (int32_t)p->stages.size() - 1;
     if (first < 0) first = 0;
@@ -415,8 +450,13 @@ int qcm_plan_run_stages(qcm_plan* p, double* const* bufs, int32_t precision, voi
     int dev = 0;
     QCM_CUDA(cudaGetDevice(&dev));
     if (dev != p->device) { set_error("plan was uploaded to another device"); return QCM_E_STATE; }
+    if (precision != QCM_PREC_FP64 && precision != QCM_PREC_TF32 && precision != QCM_PREC_BF16X3) {
+        set_error("unknown precision");
+        return QCM_E_INVALID;
+    }
     BufTable bt;
     for (int i = 0; i < QCM_NBUF; ++i) bt.p[i] = bufs[i];
+    bt.f32mask = f32mask;
     cudaStream_t s = (cudaStream_t)stream;
     for (int32_t si = first; si <= last; ++si) {
         Stage& st = p->stages[si];
@@ -424,10 +464,11 @@ int qcm_plan_run_stages(qcm_plan* p, double* const* bufs, int32_t precision, voi
         if (st.kind == ST_ZERO) {
             if (st.zlen > 0) {
                 if (!bufs[st.zbuf]) { set_error("missing scratch buffer"); return QCM_E_INVALID; }
-                QCM_CUDA(cudaMemsetAsync(bufs[st.zbuf], 0, sizeof(double) * st.zlen, s));
+                const size_t esz = ((f32mask >> st.zbuf) & 1u) ? sizeof(float) : sizeof(double);
+                QCM_CUDA(cudaMemsetAsync(bufs[st.zbuf], 0, esz * st.zlen, s));
             }
         } else if (st.kind == ST_AXPY) {
-            rc = launch_axpy(st, bt, s);
+            rc = launch_axpy(st, bt, precision, s);
         } else {
             rc = launch_gemm(st, bt, precision, s);
         }

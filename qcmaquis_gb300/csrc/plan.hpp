@@ -140,5 +140,5 @@ double conjugate_correction(int lc_spin, int rc_spin, int tensor_spin);
 void free_stage_device(Stage& st);
 int tc_build_work(const Stage& st, std::vector<int64_t>& w);
 int tc_launch(const void* d_out, const void* d_seg, const void* d_work, int64_t n_work, double* const* bufs,
-              int precision, void* stream);
+              uint32_t f32mask, int precision, void* stream);
 }  // namespace qcm

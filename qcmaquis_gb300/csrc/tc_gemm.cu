@@ -34,7 +34,7 @@ __device__ int g_tc_status = 0;
 struct TcOut { int64_t c_off, ldc, M, N, s_begin, s_end; int32_t c_buf, pad; };
 struct TcSeg { int64_t a_off, lda, b_off, ldb, K; double alpha; int32_t a_buf, ta, b_buf, tb; };
 struct TcWork { int64_t out, m0, n0; };
-struct TcBufs { double* p[QCM_NBUF]; };
+struct TcBufs { double* p[QCM_NBUF]; uint32_t f32mask; };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -95,18 +95,20 @@ struct TcCfg<QCM_PREC_BF16X3> {
     static constexpr uint32_t FMT = 1;  // BF16
 };
 
-// Split one FP64 value into the operand format and store it at byte offset `off`
-// of slice 0 (further slices follow at `slice_bytes` strides).
+// Split one operand value into the MMA format and store it at byte offset `off`
+// of slice 0 (further slices follow at `slice_bytes` strides).  All splitting
+// arithmetic is FP32: the FP64 pipe of this part is far narrower than the FP32
+// one, and three BF16 slices carry the 24 bits an FP32 value has.
 template <int PREC>
-__device__ __forceinline__ void put_operand(uint8_t* base, uint32_t off, uint32_t slice_bytes, double v) {
+__device__ __forceinline__ void put_operand(uint8_t* base, uint32_t off, uint32_t slice_bytes, float v) {
     if constexpr (PREC == QCM_PREC_TF32) {
-        *reinterpret_cast<uint32_t*>(base + off) = to_tf32((float)v);
+        *reinterpret_cast<uint32_t*>(base + off) = to_tf32(v);
     } else {
-        __nv_bfloat16 h0 = __double2bfloat16(v);
-        double r1 = v - (double)__bfloat162float(h0);
-        __nv_bfloat16 h1 = __double2bfloat16(r1);
-        double r2 = r1 - (double)__bfloat162float(h1);
-        __nv_bfloat16 h2 = __double2bfloat16(r2);
+        __nv_bfloat16 h0 = __float2bfloat16_rn(v);
+        float r1 = v - __bfloat162float(h0);
+        __nv_bfloat16 h1 = __float2bfloat16_rn(r1);
+        float r2 = r1 - __bfloat162float(h1);
+        __nv_bfloat16 h2 = __float2bfloat16_rn(r2);
         *reinterpret_cast<__nv_bfloat16*>(base + off) = h0;
         *reinterpret_cast<__nv_bfloat16*>(base + slice_bytes + off) = h1;
         *reinterpret_cast<__nv_bfloat16*>(base + 2 * slice_bytes + off) = h2;
@@ -168,8 +170,12 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
     for (int64_t s = o.s_begin; s < o.s_end && !aborted; ++s) {
         const TcSeg g = segs[s];
         if (g.K <= 0) continue;
-        const double* __restrict__ A = bufs.p[g.a_buf] + g.a_off;
-        const double* __restrict__ B = bufs.p[g.b_buf] + g.b_off;
+        const bool a32 = (bufs.f32mask >> g.a_buf) & 1u, b32 = (bufs.f32mask >> g.b_buf) & 1u;
+        const double* __restrict__ A = bufs.p[g.a_buf] + (a32 ? 0 : g.a_off);
+        const double* __restrict__ B = bufs.p[g.b_buf] + (b32 ? 0 : g.b_off);
+        const float* __restrict__ Af = (const float*)bufs.p[g.a_buf] + (a32 ? g.a_off : 0);
+        const float* __restrict__ Bf = (const float*)bufs.p[g.b_buf] + (b32 ? g.b_off : 0);
+        const float alpha = (float)g.alpha;
         bool first = true;  // the first MMA of a segment overwrites the accumulator
         for (int64_t k0 = 0; k0 < g.K; k0 += KC) {
             const int st = chunk & 1;
@@ -186,16 +192,22 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
                 int m, k;
                 if (g.ta) { k = idx % KC; m = idx / KC; } else { m = idx % TC_BM; k = idx / TC_BM; }
                 const int64_t gm = w.m0 + m, gk = k0 + k;
-                double v = 0.0;
-                if (gm < o.M && gk < g.K) v = g.alpha * (g.ta ? A[gk + gm * g.lda] : A[gm + gk * g.lda]);
+                float v = 0.0f;
+                if (gm < o.M && gk < g.K) {
+                    const int64_t ix = g.ta ? gk + gm * g.lda : gm + gk * g.lda;
+                    v = alpha * (a32 ? Af[ix] : (float)A[ix]);
+                }
                 put_operand<PREC>(sA, kmajor_off<E>(m, k), A_BYTES, v);
             }
             for (int idx = tid; idx < TC_BN * KC; idx += TC_THREADS) {
                 int n, k;
                 if (g.tb) { n = idx % TC_BN; k = idx / TC_BN; } else { k = idx % KC; n = idx / KC; }
                 const int64_t gn = w.n0 + n, gk = k0 + k;
-                double v = 0.0;
-                if (gn < o.N && gk < g.K) v = g.tb ? B[gn + gk * g.ldb] : B[gk + gn * g.ldb];
+                float v = 0.0f;
+                if (gn < o.N && gk < g.K) {
+                    const int64_t ix = g.tb ? gn + gk * g.ldb : gk + gn * g.ldb;
+                    v = b32 ? Bf[ix] : (float)B[ix];
+                }
                 put_operand<PREC>(sB, kmajor_off<E>(n, k), B_BYTES, v);
             }
             // generic-proxy shared-memory writes -> visible to the tensor core (async proxy)
@@ -268,13 +280,23 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
     if (aborted && tid == 0) atomicExch(&g_tc_status, 1);
 
     // ---- epilogue: FP64 accumulators -> output tile (written once)
-    double* __restrict__ C = bufs.p[o.c_buf] + o.c_off;
+    const bool c32 = (bufs.f32mask >> o.c_buf) & 1u;
     const int64_t row = w.m0 + quad * 32 + lane;
     if (!aborted && row < o.M) {
+        if (c32) {
+            float* __restrict__ C = (float*)bufs.p[o.c_buf] + o.c_off;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            const int64_t col = w.n0 + chalf * 32 + j;
-            if (col < o.N) C[row + col * o.ldc] = acc64[j];
+            for (int j = 0; j < 32; ++j) {
+                const int64_t col = w.n0 + chalf * 32 + j;
+                if (col < o.N) C[row + col * o.ldc] = (float)acc64[j];
+            }
+        } else {
+            double* __restrict__ C = bufs.p[o.c_buf] + o.c_off;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const int64_t col = w.n0 + chalf * 32 + j;
+                if (col < o.N) C[row + col * o.ldc] = acc64[j];
+            }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -308,12 +330,13 @@ int tc_build_work(const Stage& st, std::vector<int64_t>& w) {
 }
 
 int tc_launch(const void* d_out, const void* d_seg, const void* d_work, int64_t n_work, double* const* bufs,
-              int precision, void* stream) {
+              uint32_t f32mask, int precision, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     if (n_work == 0) return QCM_OK;
     if (n_work > 0x7fffffffLL) { set_error("tensor-core work list too large"); return QCM_E_RANGE; }
     TcBufs tb;
     for (int i = 0; i < QCM_NBUF; ++i) tb.p[i] = bufs[i];
+    tb.f32mask = f32mask;
     const int smem = tc_smem_bytes(precision);
     cudaError_t e;
     if (precision == QCM_PREC_TF32) {

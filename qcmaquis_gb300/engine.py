@@ -67,6 +67,14 @@ class DeviceBoundary:
     def to_host(self):
         return self.layout.unpack(self.data.detach().cpu().numpy())
 
+    def f32(self) -> torch.Tensor:
+        """FP32 shadow of the arena for the mixed-precision forms (made once, then cached)."""
+        sh = getattr(self, "_f32", None)
+        if sh is None or sh.numel() != self.data.numel():
+            sh = self.data.float()
+            self._f32 = sh
+        return sh
+
 
 def _ptr(t: Optional[torch.Tensor]) -> int:
     return 0 if t is None else int(t.data_ptr())
@@ -132,9 +140,23 @@ class Engine:
         return p
 
     def run(self, plan: N.Plan, ket=None, left=None, right=None, out=None, precision=None, first=0, last=-1):
+        """Run a plan.  ``left`` / ``right`` are DeviceBoundary objects or raw FP64 tensors;
+        the mixed forms read FP32 boundary shadows and keep every intermediate in FP32."""
+        prec = self.precision if precision is None else precision
         s0, s1, s2 = self.ws.get(plan.scratch)
-        plan.run([_ptr(ket), _ptr(left), _ptr(right), _ptr(out), _ptr(s0), _ptr(s1), _ptr(s2)],
-                 self.precision if precision is None else precision, self._stream(), first, last)
+        mask = 0
+        lt = left.data if isinstance(left, DeviceBoundary) else left
+        rt = right.data if isinstance(right, DeviceBoundary) else right
+        if prec != N.PREC_FP64:
+            mask = (1 << N.QCM_BUF_S0) | (1 << N.QCM_BUF_S1) | (1 << N.QCM_BUF_S2)
+            if isinstance(left, DeviceBoundary):
+                lt = left.f32()
+                mask |= 1 << N.QCM_BUF_LEFT
+            if isinstance(right, DeviceBoundary):
+                rt = right.f32()
+                mask |= 1 << N.QCM_BUF_RIGHT
+        plan.run_typed([_ptr(ket), _ptr(lt), _ptr(rt), _ptr(out), _ptr(s0), _ptr(s1), _ptr(s2)], mask, prec,
+                       self._stream(), first, last)
         if first == 0 and last == -1:
             self.launches += plan.launches
 
@@ -145,7 +167,7 @@ class Engine:
         p = self.sigma_plan(ket, L, R, mpo)
         if out is None:
             out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=self.device)
-        self.run(p, ket=ket.data, left=L.data, right=R.data, out=out, precision=precision)
+        self.run(p, ket=ket.data, left=L, right=R, out=out, precision=precision)
         return ket.like(out)
 
     def overlap_mpo_left_step(self, mps: DeviceMPSTensor, L: DeviceBoundary, mpo) -> DeviceBoundary:
@@ -155,7 +177,7 @@ class Engine:
         p.upload()
         lay = p.out_layout()
         out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=self.device)
-        self.run(p, ket=mps.data, left=L.data, out=out, precision=N.PREC_FP64)
+        self.run(p, ket=mps.data, left=L, out=out, precision=N.PREC_FP64)
         return DeviceBoundary(lay, out)
 
     def overlap_mpo_right_step(self, mps: DeviceMPSTensor, R: DeviceBoundary, mpo) -> DeviceBoundary:
@@ -165,7 +187,7 @@ class Engine:
         p.upload()
         lay = p.out_layout()
         out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=self.device)
-        self.run(p, ket=mps.data, right=R.data, out=out, precision=N.PREC_FP64)
+        self.run(p, ket=mps.data, right=R, out=out, precision=N.PREC_FP64)
         return DeviceBoundary(lay, out)
 
 

@@ -78,6 +78,8 @@ def lib():
     L.qcm_plan_run.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.c_int32, C.c_void_p]
     L.qcm_plan_run_stages.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.c_int32, C.c_void_p, C.c_int32,
                                       C.c_int32]
+    L.qcm_plan_run_typed.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, C.c_int32, C.c_void_p,
+                                     C.c_int32, C.c_int32]
     L.qcm_plan_destroy.argtypes = [C.c_void_p]
     L.qcm_plan_destroy.restype = None
     L.qcm_dot.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
@@ -347,6 +349,12 @@ class Plan:
         arr = (C.c_void_p * QCM_NBUF)(*[C.c_void_p(int(p)) if p else None for p in ptrs])
         check(lib().qcm_plan_run_stages(self.h, arr, precision, C.c_void_p(stream) if stream else None, first, last),
               "qcm_plan_run_stages")
+
+    def run_typed(self, ptrs: Sequence[int], f32mask: int, precision: int, stream: int = 0, first: int = 0,
+                  last: int = -1):
+        arr = (C.c_void_p * QCM_NBUF)(*[C.c_void_p(int(p)) if p else None for p in ptrs])
+        check(lib().qcm_plan_run_typed(self.h, arr, f32mask, precision, C.c_void_p(stream) if stream else None,
+                                       first, last), "qcm_plan_run_typed")
 
     def stage_kinds(self):
         n = C.c_int32()
