@@ -118,6 +118,81 @@ gather_axpy_kernel(BufTable bufs, const DevAxpyOut* __restrict__ outs, const Dev
     }
 }
 
+// Fast path for stages whose terms all read buffers of one element type SRC:
+// term loop unrolled by 4 so that 16 independent loads per thread are in flight
+// (the gathers re-read their sources mostly from L2 and are latency bound).
+template <class ACC, class SRC>
+__global__ void __launch_bounds__(AXPY_THREADS)
+gather_axpy_uniform(BufTable bufs, const DevAxpyOut* __restrict__ outs, const DevAxpyTerm* __restrict__ terms,
+                    const DevAxpyWork* __restrict__ work) {
+    __shared__ ACC s_alpha[AXPY_TERM_CACHE];
+    __shared__ const SRC* s_src[AXPY_TERM_CACHE];
+    __shared__ int64_t s_lds[AXPY_TERM_CACHE];
+    const DevAxpyWork w = work[blockIdx.x];
+    const DevAxpyOut o = outs[w.out];
+    const bool dst32 = slot_f32(bufs, o.dst_buf);
+    const int64_t rows = o.rows;
+    const int64_t nel = rows * (w.c1 - w.c0);
+    const int64_t nterm = o.t_end - o.t_begin;
+    for (int64_t base = 0; base < nel; base += 4 * AXPY_THREADS) {
+        ACC acc[4] = {ACC(0), ACC(0), ACC(0), ACC(0)};
+        int64_t eo[4];  // element offset within a source tile (lds applied per term)
+        int64_t ii[4], jj[4];
+        bool ok[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            int64_t e = base + threadIdx.x + (int64_t)u * AXPY_THREADS;
+            ok[u] = e < nel;
+            ii[u] = ok[u] ? e % rows : 0;
+            jj[u] = ok[u] ? w.c0 + e / rows : w.c0;
+            eo[u] = 0;
+        }
+        for (int64_t t0 = 0; t0 < nterm; t0 += AXPY_TERM_CACHE) {
+            const int64_t tn = min((int64_t)AXPY_TERM_CACHE, nterm - t0);
+            __syncthreads();
+            for (int64_t t = threadIdx.x; t < tn; t += AXPY_THREADS) {
+                const DevAxpyTerm tt = terms[o.t_begin + t0 + t];
+                s_alpha[t] = (ACC)tt.alpha;
+                s_src[t] = (const SRC*)bufs.p[tt.src_buf] + tt.src_off;
+                s_lds[t] = tt.lds;
+            }
+            __syncthreads();
+            int64_t t = 0;
+            for (; t + 4 <= tn; t += 4) {
+                SRC x[4][4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const SRC* __restrict__ src = s_src[t + q];
+                    const int64_t lds = s_lds[t + q];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) x[q][u] = ok[u] ? __ldg(src + ii[u] + jj[u] * lds) : SRC(0);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const ACC a = s_alpha[t + q];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) acc[u] = fma(a, (ACC)x[q][u], acc[u]);
+                }
+            }
+            for (; t < tn; ++t) {
+                const SRC* __restrict__ src = s_src[t];
+                const int64_t lds = s_lds[t];
+                const ACC a = s_alpha[t];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (ok[u]) acc[u] = fma(a, (ACC)__ldg(src + ii[u] + jj[u] * lds), acc[u]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (ok[u]) {
+                if (dst32) ((float*)bufs.p[o.dst_buf])[o.dst_off + ii[u] + jj[u] * o.ldd] = (float)acc[u];
+                else bufs.p[o.dst_buf][o.dst_off + ii[u] + jj[u] * o.ldd] = (double)acc[u];
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------------ FP64 grouped GEMM
 constexpr int GT_M = 64, GT_N = 64, GT_K = 16;
 
@@ -222,6 +297,9 @@ static int upload_stage(Stage& st) {
         if ((rc = upload_vec(t, &st.d_b))) return rc;
         if ((rc = upload_vec(w, &st.d_c))) return rc;
         st.n_work = (int64_t)w.size();
+        st.src_buf = st.aterm.empty() ? -1 : st.aterm[0].src_buf;
+        for (const AxpyTerm& a : st.aterm)
+            if (a.src_buf != st.src_buf) { st.src_buf = -2; break; }
     } else if (st.kind == ST_GEMM) {
         std::vector<DevGemmOut> o(st.gout.size());
         std::vector<DevGemmSeg> s(st.gseg.size());
@@ -251,12 +329,25 @@ static int upload_stage(Stage& st) {
 static int launch_axpy(const Stage& st, const BufTable& bt, int precision, cudaStream_t s) {
     if (st.n_work == 0) return QCM_OK;
     if (st.n_work > 0x7fffffffLL) { set_error("axpy work list too large"); return QCM_E_RANGE; }
-    if (precision == QCM_PREC_FP64)
-        gather_axpy_kernel<double><<<(unsigned)st.n_work, AXPY_THREADS, 0, s>>>(
-            bt, (const DevAxpyOut*)st.d_a, (const DevAxpyTerm*)st.d_b, (const DevAxpyWork*)st.d_c);
-    else
-        gather_axpy_kernel<float><<<(unsigned)st.n_work, AXPY_THREADS, 0, s>>>(
-            bt, (const DevAxpyOut*)st.d_a, (const DevAxpyTerm*)st.d_b, (const DevAxpyWork*)st.d_c);
+    const auto* O = (const DevAxpyOut*)st.d_a;
+    const auto* T = (const DevAxpyTerm*)st.d_b;
+    const auto* W = (const DevAxpyWork*)st.d_c;
+    const unsigned g = (unsigned)st.n_work;
+    if (st.src_buf >= 0) {
+        const bool src32 = (bt.f32mask >> st.src_buf) & 1u;
+        if (precision == QCM_PREC_FP64) {
+            if (src32) { set_error("the FP64 form takes FP64 buffers only"); return QCM_E_INVALID; }
+            gather_axpy_uniform<double, double><<<g, AXPY_THREADS, 0, s>>>(bt, O, T, W);
+        } else if (src32) {
+            gather_axpy_uniform<float, float><<<g, AXPY_THREADS, 0, s>>>(bt, O, T, W);
+        } else {
+            gather_axpy_uniform<float, double><<<g, AXPY_THREADS, 0, s>>>(bt, O, T, W);
+        }
+    } else if (precision == QCM_PREC_FP64) {
+        gather_axpy_kernel<double><<<g, AXPY_THREADS, 0, s>>>(bt, O, T, W);
+    } else {
+        gather_axpy_kernel<float><<<g, AXPY_THREADS, 0, s>>>(bt, O, T, W);
+    }
     QCM_CUDA(cudaGetLastError());
     return QCM_OK;
 }

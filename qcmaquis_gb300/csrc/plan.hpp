@@ -112,6 +112,7 @@ struct Stage {
     int64_t n_work = 0;
     void* d_tcw = nullptr;  // work list (tensor-core executor, 128 x 64 tiles)
     int64_t n_tcw = 0;
+    int32_t src_buf = -1;   // AXPY: the one buffer all terms read (-2: several)
 };
 
 enum PlanKind { PK_SIGMA = 0, PK_BLEFT = 1, PK_BRIGHT = 2 };

@@ -95,23 +95,68 @@ struct TcCfg<QCM_PREC_BF16X3> {
     static constexpr uint32_t FMT = 1;  // BF16
 };
 
-// Split one operand value into the MMA format and store it at byte offset `off`
-// of slice 0 (further slices follow at `slice_bytes` strides).  All splitting
-// arithmetic is FP32: the FP64 pipe of this part is far narrower than the FP32
-// one, and three BF16 slices carry the 24 bits an FP32 value has.
+// Split T = 16/E consecutive-K operand values into the MMA format and store
+// them as one 16-byte vector per slice at byte offset `off` of slice 0 (further
+// slices follow at `slice_bytes` strides).  All splitting arithmetic is FP32:
+// the FP64 pipe of this part is far narrower than the FP32 one, and three BF16
+// slices carry the 24 bits an FP32 value has.
 template <int PREC>
-__device__ __forceinline__ void put_operand(uint8_t* base, uint32_t off, uint32_t slice_bytes, float v) {
+__device__ __forceinline__ void put_vec(uint8_t* base, uint32_t off, uint32_t slice_bytes, const float* v) {
     if constexpr (PREC == QCM_PREC_TF32) {
-        *reinterpret_cast<uint32_t*>(base + off) = to_tf32(v);
+        uint4 q;
+        q.x = to_tf32(v[0]); q.y = to_tf32(v[1]); q.z = to_tf32(v[2]); q.w = to_tf32(v[3]);
+        *reinterpret_cast<uint4*>(base + off) = q;
     } else {
-        __nv_bfloat16 h0 = __float2bfloat16_rn(v);
-        float r1 = v - __bfloat162float(h0);
-        __nv_bfloat16 h1 = __float2bfloat16_rn(r1);
-        float r2 = r1 - __bfloat162float(h1);
-        __nv_bfloat16 h2 = __float2bfloat16_rn(r2);
-        *reinterpret_cast<__nv_bfloat16*>(base + off) = h0;
-        *reinterpret_cast<__nv_bfloat16*>(base + slice_bytes + off) = h1;
-        *reinterpret_cast<__nv_bfloat16*>(base + 2 * slice_bytes + off) = h2;
+        uint32_t s0[4], s1[4], s2[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            __nv_bfloat16 h[3][2];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const float x = v[2 * i + j];
+                h[0][j] = __float2bfloat16_rn(x);
+                const float r1 = x - __bfloat162float(h[0][j]);
+                h[1][j] = __float2bfloat16_rn(r1);
+                const float r2 = r1 - __bfloat162float(h[1][j]);
+                h[2][j] = __float2bfloat16_rn(r2);
+            }
+            s0[i] = (uint32_t)__bfloat16_as_ushort(h[0][0]) | ((uint32_t)__bfloat16_as_ushort(h[0][1]) << 16);
+            s1[i] = (uint32_t)__bfloat16_as_ushort(h[1][0]) | ((uint32_t)__bfloat16_as_ushort(h[1][1]) << 16);
+            s2[i] = (uint32_t)__bfloat16_as_ushort(h[2][0]) | ((uint32_t)__bfloat16_as_ushort(h[2][1]) << 16);
+        }
+        *reinterpret_cast<uint4*>(base + off) = make_uint4(s0[0], s0[1], s0[2], s0[3]);
+        *reinterpret_cast<uint4*>(base + slice_bytes + off) = make_uint4(s1[0], s1[1], s1[2], s1[3]);
+        *reinterpret_cast<uint4*>(base + 2 * slice_bytes + off) = make_uint4(s2[0], s2[1], s2[2], s2[3]);
+    }
+}
+
+// Load a K-chunk of one operand into shared memory.  Rows R (the M or N extent of
+// the tile), KC elements of K; each work unit is T consecutive K of one row,
+// written as one 16-byte vector.  `tr` selects the global storage order:
+// tr == 0: element (r, k) at P[r + k*ld] (rows contiguous -> warps span rows);
+// tr == 1: element (r, k) at P[k + r*ld] (K contiguous -> warps span K first).
+template <int PREC, int R, int KC, int T>
+__device__ __forceinline__ void load_chunk(uint8_t* sbase, uint32_t slice_bytes, const double* P64, const float* P32,
+                                           bool f32, int tr, int64_t ld, int64_t r0, int64_t rlim, int64_t k0,
+                                           int64_t klim, float scale) {
+    constexpr int E = 16 / T;
+    constexpr int KV = KC / T;  // vectors per row
+    for (int u = threadIdx.x; u < R * KV; u += TC_THREADS) {
+        int r, kv;
+        if (tr) { kv = u % KV; r = u / KV; } else { r = u % R; kv = u / R; }
+        const int64_t gr = r0 + r;
+        float v[T];
+#pragma unroll
+        for (int j = 0; j < T; ++j) {
+            const int64_t gk = k0 + kv * T + j;
+            float x = 0.0f;
+            if (gr < rlim && gk < klim) {
+                const int64_t ix = tr ? gk + gr * ld : gr + gk * ld;
+                x = f32 ? __ldg(P32 + ix) : (float)__ldg(P64 + ix);
+            }
+            v[j] = scale * x;
+        }
+        put_vec<PREC>(sbase, kmajor_off<E>(r, kv * T), slice_bytes, v);
     }
 }
 
@@ -159,12 +204,12 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
     uint32_t phase[NSTAGE] = {0u, 0u};
     bool pending[NSTAGE] = {false, false};
     bool aborted = false;
-    // FP64 accumulators of this thread's row and 32 columns: each segment (one
-    // block product of the split-K sum) accumulates in FP32 in TMEM, then is
-    // drained into these.
-    double acc64[32];
+    // Accumulators of this thread's row and 32 columns: each segment (one block
+    // product of the split-K sum) accumulates in FP32 in TMEM, then is drained
+    // into these with a compensated (two-sum) FP32 addition.
+    float acc_hi[32], acc_lo[32];  // compensated (two-sum) FP32 accumulation across segments
 #pragma unroll
-    for (int j = 0; j < 32; ++j) acc64[j] = 0.0;
+    for (int j = 0; j < 32; ++j) { acc_hi[j] = 0.0f; acc_lo[j] = 0.0f; }
     int chunk = 0;
 
     for (int64_t s = o.s_begin; s < o.s_end && !aborted; ++s) {
@@ -188,28 +233,8 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
                 pending[st] = false;
                 if (__syncthreads_or(to)) { aborted = true; break; }
             }
-            for (int idx = tid; idx < TC_BM * KC; idx += TC_THREADS) {
-                int m, k;
-                if (g.ta) { k = idx % KC; m = idx / KC; } else { m = idx % TC_BM; k = idx / TC_BM; }
-                const int64_t gm = w.m0 + m, gk = k0 + k;
-                float v = 0.0f;
-                if (gm < o.M && gk < g.K) {
-                    const int64_t ix = g.ta ? gk + gm * g.lda : gm + gk * g.lda;
-                    v = alpha * (a32 ? Af[ix] : (float)A[ix]);
-                }
-                put_operand<PREC>(sA, kmajor_off<E>(m, k), A_BYTES, v);
-            }
-            for (int idx = tid; idx < TC_BN * KC; idx += TC_THREADS) {
-                int n, k;
-                if (g.tb) { n = idx % TC_BN; k = idx / TC_BN; } else { k = idx % KC; n = idx / KC; }
-                const int64_t gn = w.n0 + n, gk = k0 + k;
-                float v = 0.0f;
-                if (gn < o.N && gk < g.K) {
-                    const int64_t ix = g.tb ? gn + gk * g.ldb : gk + gn * g.ldb;
-                    v = b32 ? Bf[ix] : (float)B[ix];
-                }
-                put_operand<PREC>(sB, kmajor_off<E>(n, k), B_BYTES, v);
-            }
+            load_chunk<PREC, TC_BM, KC, 16 / E>(sA, A_BYTES, A, Af, a32, g.ta, g.lda, w.m0, o.M, k0, g.K, alpha);
+            load_chunk<PREC, TC_BN, KC, 16 / E>(sB, B_BYTES, B, Bf, b32, g.tb ? 0 : 1, g.ldb, w.n0, o.N, k0, g.K, 1.0f);
             // generic-proxy shared-memory writes -> visible to the tensor core (async proxy)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -271,7 +296,14 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
                 : "r"(trow + (uint32_t)c0));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int j = 0; j < 16; ++j) acc64[c0 + j] += (double)__uint_as_float(r[j]);
+            for (int j = 0; j < 16; ++j) {
+                const float x = __uint_as_float(r[j]);
+                const float t = acc_hi[c0 + j] + x;                         // Knuth two-sum
+                const float bp = t - acc_hi[c0 + j];
+                const float err = (acc_hi[c0 + j] - (t - bp)) + (x - bp);
+                acc_hi[c0 + j] = t;
+                acc_lo[c0 + j] += err;
+            }
         }
         // the next segment's first MMA overwrites TMEM: all reads must be complete
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -288,14 +320,14 @@ tc_gemm_kernel(TcBufs bufs, const TcOut* __restrict__ outs, const TcSeg* __restr
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
                 const int64_t col = w.n0 + chalf * 32 + j;
-                if (col < o.N) C[row + col * o.ldc] = (float)acc64[j];
+                if (col < o.N) C[row + col * o.ldc] = acc_hi[j] + acc_lo[j];
             }
         } else {
             double* __restrict__ C = bufs.p[o.c_buf] + o.c_off;
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
                 const int64_t col = w.n0 + chalf * 32 + j;
-                if (col < o.N) C[row + col * o.ldc] = acc64[j];
+                if (col < o.N) C[row + col * o.ldc] = (double)acc_hi[j] + (double)acc_lo[j];
             }
         }
     }
