@@ -127,7 +127,7 @@ gather_axpy_uniform(BufTable bufs, const DevAxpyOut* __restrict__ outs, const De
                     const DevAxpyWork* __restrict__ work) {
     __shared__ ACC s_alpha[AXPY_TERM_CACHE];
     __shared__ const SRC* s_src[AXPY_TERM_CACHE];
-    __shared__ int64_t s_lds[AXPY_TERM_CACHE];
+    __shared__ int s_lds[AXPY_TERM_CACHE];
     const DevAxpyWork w = work[blockIdx.x];
     const DevAxpyOut o = outs[w.out];
     const bool dst32 = slot_f32(bufs, o.dst_buf);
@@ -136,16 +136,14 @@ gather_axpy_uniform(BufTable bufs, const DevAxpyOut* __restrict__ outs, const De
     const int64_t nterm = o.t_end - o.t_begin;
     for (int64_t base = 0; base < nel; base += 4 * AXPY_THREADS) {
         ACC acc[4] = {ACC(0), ACC(0), ACC(0), ACC(0)};
-        int64_t eo[4];  // element offset within a source tile (lds applied per term)
-        int64_t ii[4], jj[4];
+        int ii[4], jj[4];  // in-tile row and column (tiles are far below 2^31 elements)
         bool ok[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             int64_t e = base + threadIdx.x + (int64_t)u * AXPY_THREADS;
             ok[u] = e < nel;
-            ii[u] = ok[u] ? e % rows : 0;
-            jj[u] = ok[u] ? w.c0 + e / rows : w.c0;
-            eo[u] = 0;
+            ii[u] = ok[u] ? (int)(e % rows) : 0;
+            jj[u] = ok[u] ? (int)(w.c0 + e / rows) : (int)w.c0;
         }
         for (int64_t t0 = 0; t0 < nterm; t0 += AXPY_TERM_CACHE) {
             const int64_t tn = min((int64_t)AXPY_TERM_CACHE, nterm - t0);
@@ -154,7 +152,7 @@ gather_axpy_uniform(BufTable bufs, const DevAxpyOut* __restrict__ outs, const De
                 const DevAxpyTerm tt = terms[o.t_begin + t0 + t];
                 s_alpha[t] = (ACC)tt.alpha;
                 s_src[t] = (const SRC*)bufs.p[tt.src_buf] + tt.src_off;
-                s_lds[t] = tt.lds;
+                s_lds[t] = (int)tt.lds;
             }
             __syncthreads();
             int64_t t = 0;
@@ -163,7 +161,7 @@ gather_axpy_uniform(BufTable bufs, const DevAxpyOut* __restrict__ outs, const De
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const SRC* __restrict__ src = s_src[t + q];
-                    const int64_t lds = s_lds[t + q];
+                    const int lds = s_lds[t + q];
 #pragma unroll
                     for (int u = 0; u < 4; ++u) x[q][u] = ok[u] ? __ldg(src + ii[u] + jj[u] * lds) : SRC(0);
                 }
@@ -176,7 +174,7 @@ gather_axpy_uniform(BufTable bufs, const DevAxpyOut* __restrict__ outs, const De
             }
             for (; t < tn; ++t) {
                 const SRC* __restrict__ src = s_src[t];
-                const int64_t lds = s_lds[t];
+                const int lds = s_lds[t];
                 const ACC a = s_alpha[t];
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
@@ -186,8 +184,9 @@ gather_axpy_uniform(BufTable bufs, const DevAxpyOut* __restrict__ outs, const De
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             if (ok[u]) {
-                if (dst32) ((float*)bufs.p[o.dst_buf])[o.dst_off + ii[u] + jj[u] * o.ldd] = (float)acc[u];
-                else bufs.p[o.dst_buf][o.dst_off + ii[u] + jj[u] * o.ldd] = (double)acc[u];
+                const int64_t d = o.dst_off + ii[u] + (int64_t)jj[u] * o.ldd;
+                if (dst32) ((float*)bufs.p[o.dst_buf])[d] = (float)acc[u];
+                else bufs.p[o.dst_buf][d] = (double)acc[u];
             }
         }
     }

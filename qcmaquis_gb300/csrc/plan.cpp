@@ -128,8 +128,15 @@ size_t BM::insert(Blk x) {
     b.insert(b.begin() + lo, x);
     return lo;
 }
+static void check_block_extent(const Blk& x) {
+    // the executors use 32-bit in-block offsets
+    if (x.rows * x.cols >= (int64_t(1) << 31) || x.rows >= (int64_t(1) << 31) || x.cols >= (int64_t(1) << 31))
+        throw std::runtime_error("block larger than 2^31 elements");
+}
+
 int64_t BM::assign_offsets(int64_t base) {
     for (auto& x : b) {
+        check_block_extent(x);
         x.off = base;
         base += x.rows * x.cols;
     }
@@ -231,6 +238,7 @@ static BM read_blocks(const qcm_blocks_t* x) {
         b.cols = x->cols[k];
         b.off = x->off[k];
         if (b.rows < 0 || b.cols < 0 || b.off < 0) throw std::runtime_error("negative block extent");
+        check_block_extent(b);
         if (!r.b.empty() && !key_gt(r.b.back(), b.lc, b.rc)) throw std::runtime_error("blocks not in DualIndex order");
         r.b.push_back(b);
     }
@@ -247,6 +255,8 @@ static std::vector<BM> read_boundary(const qcm_boundary_t* x) {
             bl.rows = x->rows[k];
             bl.cols = x->cols[k];
             bl.off = x->off[k];
+            if (bl.rows < 0 || bl.cols < 0 || bl.off < 0) throw std::runtime_error("negative block extent");
+            check_block_extent(bl);
             if (!r[b].b.empty() && !key_gt(r[b].b.back(), bl.lc, bl.rc))
                 throw std::runtime_error("boundary blocks not in DualIndex order");
             r[b].b.push_back(bl);

@@ -144,14 +144,16 @@ __device__ __forceinline__ void load_chunk(uint8_t* sbase, uint32_t slice_bytes,
     for (int u = threadIdx.x; u < R * KV; u += TC_THREADS) {
         int r, kv;
         if (tr) { kv = u % KV; r = u / KV; } else { r = u % R; kv = u / R; }
-        const int64_t gr = r0 + r;
+        // in-block offsets fit in 32 bits (the plan builder keeps blocks below 2^31 elements)
+        const int gr = (int)(r0 + r);
+        const int ld32 = (int)ld;
         float v[T];
 #pragma unroll
         for (int j = 0; j < T; ++j) {
-            const int64_t gk = k0 + kv * T + j;
+            const int gk = (int)(k0 + kv * T + j);
             float x = 0.0f;
             if (gr < rlim && gk < klim) {
-                const int64_t ix = tr ? gk + gr * ld : gr + gk * ld;
+                const int ix = tr ? gk + gr * ld32 : gr + gk * ld32;
                 x = f32 ? __ldg(P32 + ix) : (float)__ldg(P64 + ix);
             }
             v[j] = scale * x;

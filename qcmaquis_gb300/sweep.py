@@ -144,10 +144,14 @@ def expval(mps: List[DeviceMPSTensor], mpo, engine_full: Engine, right_end) -> f
 
 
 def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optional[List[DeviceMPSTensor]] = None,
-             engine: Optional[Engine] = None, device="cuda", callback=None):
+             engine: Optional[Engine] = None, device="cuda", callback=None, precision: int = 0):
+    """Two-site sweeps.  ``precision`` selects the sigma-vector form (0 = FP64,
+    1 = TF32, 2 = BF16x3 tensor cores); boundary updates, the eigensolver's
+    vector algebra, the subspace problem, the SVD truncation and the per-sweep
+    energy stay FP64."""
     L = model.L
     phys = model.phys
-    engine = engine or Engine(device)
+    engine = engine or Engine(device, precision=precision)
     engine_full = Engine(device, hermitian=False)
     right_end = (nelec, twoS)
     if mps is None:
