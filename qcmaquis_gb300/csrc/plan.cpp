@@ -190,8 +190,36 @@ double wigner9j(int a, int b, int c, int d, int e, int f, int g, int h, int i) {
 static double mod_coupling(int a, int b, int c, int d, int e, int f, int g, int h, int i) {
     return std::sqrt((g + 1.0) * (h + 1.0) * (c + 1.0) * (f + 1.0)) * wigner9j(a, b, c, d, e, f, g, h, i);
 }
+// set_coupling(..., init) = init * F(a..i); F depends only on the nine doubled
+// spins (all small), so it is cached per thread.
+struct CouplingVal { double v[4]; };
+static void coupling_unit(int a, int b, int c, int d, int e, int f, int g, int h, int i, double out[4]);
+
 void set_coupling(int a, int b, int c, int d, int e, int f, int g, int h, int i, double init, double out[4]) {
-    double pref = std::sqrt((i + 1.0) * (a + 1.0) / ((g + 1.0) * (c + 1.0))) * init;
+    static thread_local std::unordered_map<uint64_t, CouplingVal> cache;
+    const int args[9] = {a, b, c, d, e, f, g, h, i};
+    uint64_t key = 0;
+    bool packable = true;
+    for (int x : args) {
+        if (x < 0 || x >= 128) { packable = false; break; }
+        key = (key << 7) | (uint64_t)x;
+    }
+    if (packable) {
+        auto it = cache.find(key);
+        if (it == cache.end()) {
+            CouplingVal cv;
+            coupling_unit(a, b, c, d, e, f, g, h, i, cv.v);
+            it = cache.emplace(key, cv).first;
+        }
+        for (int k = 0; k < 4; ++k) out[k] = init * it->second.v[k];
+        return;
+    }
+    coupling_unit(a, b, c, d, e, f, g, h, i, out);
+    for (int k = 0; k < 4; ++k) out[k] *= init;
+}
+
+static void coupling_unit(int a, int b, int c, int d, int e, int f, int g, int h, int i, double out[4]) {
+    double pref = std::sqrt((i + 1.0) * (a + 1.0) / ((g + 1.0) * (c + 1.0)));
     out[0] = out[1] = out[2] = out[3] = 0.0;
     if (triangle(a, b, c)) {
         out[0] = pref * mod_coupling(a, b, c, d, e, f, g, h, i);
