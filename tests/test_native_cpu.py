@@ -101,3 +101,18 @@ def test_plan_work_counters_match_oracle():
     # the plan computes every T row eagerly, as the oracle does; the sums match
     assert p.gemm_flops == R.FLOPS.gemm_flops
     assert p.axpy_flops <= R.FLOPS.axpy_flops
+
+
+def test_cpp_layer_builds_a_plan(tmp_path):
+    """The header-only C++ layer compiles with g++, links the library and builds a plan."""
+    import subprocess
+    exe = tmp_path / "capi_example"
+    src = os.path.join(ROOT, "tests", "capi_example.cpp")
+    libdir = os.path.join(ROOT, "qcmaquis_gb300")
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"), src, "-o", str(exe),
+                        "-L" + libdir, "-lqcm_gb300", "-Wl,-rpath," + libdir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "out=4" in out.stdout
