@@ -12,10 +12,13 @@
 //   deterministic two-pass reductions (warp shuffles, fixed combine order).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <mutex>
+#include <numeric>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "plan.hpp"
@@ -35,6 +38,7 @@ namespace qcm {
 struct DevAxpyOut { int64_t dst_off, ldd, rows, cols, t_begin, t_end; int32_t dst_buf, pad; };
 struct DevAxpyTerm { int64_t src_off, lds; double alpha; int32_t src_buf, pad; };
 struct DevAxpyWork { int64_t out, c0, c1; };
+struct DevAxpyChunk { int32_t out, e0, n, pad; };
 struct DevGemmOut { int64_t c_off, ldc, M, N, s_begin, s_end; int32_t c_buf, pad; };
 struct DevGemmSeg { int64_t a_off, lda, b_off, ldb, K; double alpha; int32_t a_buf, ta, b_buf, tb; };
 struct DevGemmWork { int64_t out, m0, n0; };
@@ -192,6 +196,147 @@ gather_axpy_uniform(BufTable bufs, const DevAxpyOut* __restrict__ outs, const De
     }
 }
 
+// Contiguous-source executor.  Every term of the stage reads a source tile
+// stored contiguously (ld = rows), so element e of an output tile is
+// sum_t alpha_t * src_t[e] over the tile's terms in order.  A work item owns
+// CG_CHUNK consecutive elements of one output tile; each thread keeps
+// CG_PER accumulators at stride CG_THREADS and reads every source with
+// immediate offsets from one per-term pointer (cached in shared memory).
+constexpr int CG_THREADS = 256;
+constexpr int CG_PER = 8;
+constexpr int CG_CHUNK = CG_THREADS * CG_PER;
+constexpr int CG_TCACHE = 256;
+
+template <class ACC, class SRC>
+__global__ void __launch_bounds__(CG_THREADS)
+gather_axpy_contig(BufTable bufs, const DevAxpyOut* __restrict__ outs, const DevAxpyTerm* __restrict__ terms,
+                   const DevAxpyChunk* __restrict__ work) {
+    __shared__ const SRC* s_ptr[CG_TCACHE];
+    __shared__ ACC s_alpha[CG_TCACHE];
+    const DevAxpyChunk w = work[blockIdx.x];
+    const DevAxpyOut o = outs[w.out];
+    const int tid = threadIdx.x;
+    const int n = w.n;
+    ACC acc[CG_PER];
+#pragma unroll
+    for (int u = 0; u < CG_PER; ++u) acc[u] = ACC(0);
+    const int64_t nterm = o.t_end - o.t_begin;
+    for (int64_t t0 = 0; t0 < nterm; t0 += CG_TCACHE) {
+        const int tn = (int)min((int64_t)CG_TCACHE, nterm - t0);
+        __syncthreads();
+        if (tid < tn) {
+            const DevAxpyTerm tt = terms[o.t_begin + t0 + tid];
+            s_ptr[tid] = (const SRC*)bufs.p[tt.src_buf] + tt.src_off + w.e0;
+            s_alpha[tid] = (ACC)tt.alpha;
+        }
+        __syncthreads();
+        if (n == CG_CHUNK) {
+            int t = 0;
+            for (; t + 2 <= tn; t += 2) {
+                const SRC* __restrict__ p0 = s_ptr[t] + tid;
+                const SRC* __restrict__ p1 = s_ptr[t + 1] + tid;
+                SRC x0[CG_PER], x1[CG_PER];
+#pragma unroll
+                for (int u = 0; u < CG_PER; ++u) {
+                    x0[u] = __ldg(p0 + u * CG_THREADS);
+                    x1[u] = __ldg(p1 + u * CG_THREADS);
+                }
+                const ACC a0 = s_alpha[t], a1 = s_alpha[t + 1];
+#pragma unroll
+                for (int u = 0; u < CG_PER; ++u) {
+                    acc[u] = fma(a0, (ACC)x0[u], acc[u]);
+                    acc[u] = fma(a1, (ACC)x1[u], acc[u]);
+                }
+            }
+            if (t < tn) {
+                const SRC* __restrict__ p0 = s_ptr[t] + tid;
+                const ACC a0 = s_alpha[t];
+#pragma unroll
+                for (int u = 0; u < CG_PER; ++u) acc[u] = fma(a0, (ACC)__ldg(p0 + u * CG_THREADS), acc[u]);
+            }
+        } else {
+            for (int t = 0; t < tn; ++t) {
+                const SRC* __restrict__ p0 = s_ptr[t] + tid;
+                const ACC a0 = s_alpha[t];
+#pragma unroll
+                for (int u = 0; u < CG_PER; ++u)
+                    if (tid + u * CG_THREADS < n) acc[u] = fma(a0, (ACC)__ldg(p0 + u * CG_THREADS), acc[u]);
+            }
+        }
+    }
+    const bool dst32 = slot_f32(bufs, o.dst_buf);
+    const int rows = (int)o.rows;
+#pragma unroll
+    for (int u = 0; u < CG_PER; ++u) {
+        const int el = tid + u * CG_THREADS;
+        if (el < n) {
+            const int e = w.e0 + el;
+            const int64_t d = o.dst_off + (e % rows) + (int64_t)(e / rows) * o.ldd;
+            if (dst32) ((float*)bufs.p[o.dst_buf])[d] = (float)acc[u];
+            else bufs.p[o.dst_buf][d] = (double)acc[u];
+        }
+    }
+}
+
+// Work list of the contiguous-source executor, ordered so that CTAs running
+// at the same time read the same source chunks: output tiles that share a
+// source tile (transitively) form one group; groups run one after another,
+// and inside a group all tiles' chunk 0 runs before any chunk 1, and so on.
+// Returns false (and no list) when some term's source is not contiguous.
+static bool build_chunk_work(const Stage& st, std::vector<DevAxpyChunk>& w) {
+    const size_t nO = st.aout.size();
+    for (size_t i = 0; i < nO; ++i) {
+        const AxpyOut& a = st.aout[i];
+        if (a.rows * a.cols > 0x7fffffffLL || a.rows <= 0) return false;
+        for (int64_t t = a.t_begin; t < a.t_end; ++t)
+            if (st.aterm[t].lds != a.rows && a.cols > 1) return false;
+    }
+    std::vector<int32_t> parent(nO);
+    std::iota(parent.begin(), parent.end(), 0);
+    auto find = [&](int32_t x) {
+        while (parent[x] != x) { parent[x] = parent[parent[x]]; x = parent[x]; }
+        return x;
+    };
+    std::unordered_map<int64_t, int32_t> first_user;
+    first_user.reserve(st.aterm.size() / 4 + 16);
+    for (size_t i = 0; i < nO; ++i) {
+        const AxpyOut& a = st.aout[i];
+        for (int64_t t = a.t_begin; t < a.t_end; ++t) {
+            const int64_t key = ((int64_t)st.aterm[t].src_buf << 56) ^ st.aterm[t].src_off;
+            auto it = first_user.emplace(key, (int32_t)i);
+            if (!it.second) {
+                const int32_t r1 = find((int32_t)i), r2 = find(it.first->second);
+                if (r1 != r2) parent[std::max(r1, r2)] = std::min(r1, r2);
+            }
+        }
+    }
+    // groups in order of their first output; members in output order
+    std::vector<int32_t> order(nO);
+    std::iota(order.begin(), order.end(), 0);
+    std::vector<int32_t> root(nO);
+    for (size_t i = 0; i < nO; ++i) root[i] = find((int32_t)i);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return root[x] < root[y]; });
+    w.clear();
+    for (size_t g0 = 0; g0 < nO;) {
+        size_t g1 = g0;
+        int64_t maxc = 0;
+        while (g1 < nO && root[order[g1]] == root[order[g0]]) {
+            const AxpyOut& a = st.aout[order[g1]];
+            maxc = std::max<int64_t>(maxc, (a.rows * a.cols + CG_CHUNK - 1) / CG_CHUNK);
+            ++g1;
+        }
+        for (int64_t c = 0; c < maxc; ++c)
+            for (size_t k = g0; k < g1; ++k) {
+                const AxpyOut& a = st.aout[order[k]];
+                const int64_t nel = a.rows * a.cols;
+                if (c * CG_CHUNK < nel)
+                    w.push_back({order[k], (int32_t)(c * CG_CHUNK), (int32_t)std::min<int64_t>(CG_CHUNK, nel - c * CG_CHUNK), 0});
+            }
+        g0 = g1;
+    }
+    return true;
+}
+
 // ------------------------------------------------------------------ FP64 grouped GEMM
 constexpr int GT_M = 64, GT_N = 64, GT_K = 16;
 
@@ -263,7 +408,9 @@ void free_stage_device(Stage& st) {
     if (st.d_b) cudaFree(st.d_b);
     if (st.d_c) cudaFree(st.d_c);
     if (st.d_tcw) cudaFree(st.d_tcw);
-    st.d_a = st.d_b = st.d_c = st.d_tcw = nullptr;
+    if (st.d_cw) cudaFree(st.d_cw);
+    st.d_a = st.d_b = st.d_c = st.d_tcw = st.d_cw = nullptr;
+    st.n_cw = 0;
 }
 
 template <class T>
@@ -299,6 +446,11 @@ static int upload_stage(Stage& st) {
         st.src_buf = st.aterm.empty() ? -1 : st.aterm[0].src_buf;
         for (const AxpyTerm& a : st.aterm)
             if (a.src_buf != st.src_buf) { st.src_buf = -2; break; }
+        std::vector<DevAxpyChunk> cw;
+        if (st.src_buf >= 0 && build_chunk_work(st, cw) && !cw.empty() && cw.size() < 0x7fffffffULL) {
+            if ((rc = upload_vec(cw, &st.d_cw))) return rc;
+            st.n_cw = (int64_t)cw.size();
+        }
     } else if (st.kind == ST_GEMM) {
         std::vector<DevGemmOut> o(st.gout.size());
         std::vector<DevGemmSeg> s(st.gseg.size());
@@ -332,7 +484,18 @@ static int launch_axpy(const Stage& st, const BufTable& bt, int precision, cudaS
     const auto* T = (const DevAxpyTerm*)st.d_b;
     const auto* W = (const DevAxpyWork*)st.d_c;
     const unsigned g = (unsigned)st.n_work;
-    if (st.src_buf >= 0) {
+    // FP64 form: the column-chunk executor (it is FP64-FMA bound either way and
+    // measured faster); mixed forms: the contiguous-chunk executor.
+    if (st.src_buf >= 0 && st.n_cw > 0 && precision != QCM_PREC_FP64) {
+        const bool src32 = (bt.f32mask >> st.src_buf) & 1u;
+        const auto* CW = (const DevAxpyChunk*)st.d_cw;
+        const unsigned gc = (unsigned)st.n_cw;
+        if (src32) {
+            gather_axpy_contig<float, float><<<gc, CG_THREADS, 0, s>>>(bt, O, T, CW);
+        } else {
+            gather_axpy_contig<float, double><<<gc, CG_THREADS, 0, s>>>(bt, O, T, CW);
+        }
+    } else if (st.src_buf >= 0) {
         const bool src32 = (bt.f32mask >> st.src_buf) & 1u;
         if (precision == QCM_PREC_FP64) {
             if (src32) { set_error("the FP64 form takes FP64 buffers only"); return QCM_E_INVALID; }

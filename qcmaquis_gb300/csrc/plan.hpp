@@ -113,6 +113,8 @@ struct Stage {
     void* d_tcw = nullptr;  // work list (tensor-core executor, 128 x 64 tiles)
     int64_t n_tcw = 0;
     int32_t src_buf = -1;   // AXPY: the one buffer all terms read (-2: several)
+    void* d_cw = nullptr;   // AXPY: chunk work list of the contiguous-source executor
+    int64_t n_cw = 0;       // 0: some term's source is not contiguous (generic executor)
 };
 
 enum PlanKind { PK_SIGMA = 0, PK_BLEFT = 1, PK_BRIGHT = 2 };
