@@ -34,6 +34,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="bf16x3", choices=["fp64", "tf32", "bf16x3"])
+    ap.add_argument("--no-images", action="store_true",
+                    help="BF16x3: split operands inside the block-product kernel instead of pre-split images")
     ap.add_argument("--compare-steps", type=int, default=2, help="FP64 sigma calls timed for the comparison")
     ap.add_argument("--L", type=int, default=24)
     ap.add_argument("--m", type=int, default=1024)
@@ -203,7 +205,7 @@ def main():
 
     t0 = time.time()
     w = build_sigma_host(L=args.L, m=args.m, seed=1 + rank * 0)
-    eng = Engine(f"cuda:{local}", precision=prec)
+    eng = Engine(f"cuda:{local}", precision=prec, use_images=not args.no_images)
     upload_sigma_workload(w, eng)
     plan = eng.sigma_plan(w.psi, w.left, w.right, w.ts_mpo)
     setup_s = time.time() - t0
@@ -302,7 +304,9 @@ def main():
         ach = plan.gemm_flops * nprod / gemm_t / 1e12
         roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                 "traffic": None,
-                "kernel": "tc_gemm_kernel (tcgen05 K1 + K3 grouped block products)",
+                "kernel": ("tc_img_kernel + build_images_kernel (tcgen05 K1 + K3 block products from "
+                           "bulk-copied BF16 slice images)" if (prec == N.PREC_BF16X3 and not args.no_images)
+                           else "tc_gemm_kernel (tcgen05 K1 + K3 grouped block products)"),
                 "achieved_counts": f"{nprod} tensor-core products per FP64-equivalent product",
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"}
     axpy_gbs = plan.axpy_bytes / axpy_t / 1e9 if axpy_t > 0 else None

@@ -115,7 +115,8 @@ enum {
     QCM_BUF_S0 = 4,      /* scratch 0 */
     QCM_BUF_S1 = 5,      /* scratch 1 */
     QCM_BUF_S2 = 6,      /* scratch 2 */
-    QCM_NBUF = 7
+    QCM_BUF_IMG = 7,     /* operand images of the BF16x3 form (qcm_plan_image_bytes); may be NULL */
+    QCM_NBUF = 8
 };
 
 /* Precision of the dense block products of a plan. */
@@ -148,6 +149,12 @@ int qcm_plan_boundary_right(const qcm_index_t* phys, const qcm_index_t* left_i, 
 /* Sizes (elements) of the output and of the three scratch slots. */
 int qcm_plan_sizes(const qcm_plan* plan, int64_t* out_elems, int64_t* scratch_elems3);
 
+/* Bytes of the operand-image buffer (slot QCM_BUF_IMG) that the BF16x3 form
+ * uses to feed its block products to the tensor cores by bulk copies.  When
+ * that slot is NULL the BF16x3 form splits operands inside its block-product
+ * kernel instead (same results, slower). */
+int qcm_plan_image_bytes(const qcm_plan* plan, int64_t* bytes);
+
 /* Work counters: algorithmic FLOPs of the block products, FLOPs and bytes of the
  * gather/axpy stages, and the number of kernel launches of one run. */
 int qcm_plan_work(const qcm_plan* plan, double* gemm_flops, double* axpy_flops, double* axpy_bytes,
@@ -165,6 +172,15 @@ int qcm_plan_stage_axpy(const qcm_plan* plan, int32_t stage, int64_t* out_desc /
                         int64_t* term_desc /*3*n_terms*/, double* term_alpha);
 int qcm_plan_stage_gemm(const qcm_plan* plan, int32_t stage, int64_t* out_desc /*7*n_out*/,
                         int64_t* seg_desc /*9*n_terms*/, double* seg_alpha);
+
+/* Export the BF16x3 image-executor tables of a GEMM stage (host-side
+ * inspection and tests).  counts4 = (panels, outputs, segments, tiles); call
+ * with NULL arrays first.  panel: (src_off, img_off, src_buf, ld, R, K, kcontig, G);
+ * output: (c_off, si, sj, c_buf, mrows, ncols); segment: (a_img, b_img, a_G, b_G, kc)
+ * with seg_alpha; tile: (out, m0, n0, nt, s_begin, s_end). */
+int qcm_plan_stage_images(const qcm_plan* plan, int32_t stage, int64_t* counts4, int64_t* panel_desc /*8*n*/,
+                          int64_t* out_desc /*6*n*/, int64_t* seg_desc /*5*n*/, double* seg_alpha,
+                          int64_t* tile_desc /*6*n*/);
 
 /* Copy the plan's task tables to the current device (once per plan). */
 int qcm_plan_upload(qcm_plan* plan);

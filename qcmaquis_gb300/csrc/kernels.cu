@@ -409,6 +409,10 @@ void free_stage_device(Stage& st) {
     if (st.d_c) cudaFree(st.d_c);
     if (st.d_tcw) cudaFree(st.d_tcw);
     if (st.d_cw) cudaFree(st.d_cw);
+    for (void** d : {&st.d_ipanel, &st.d_ibuild, &st.d_iout, &st.d_iseg, &st.d_iunit}) {
+        if (*d) cudaFree(*d);
+        *d = nullptr;
+    }
     st.d_a = st.d_b = st.d_c = st.d_tcw = st.d_cw = nullptr;
     st.n_cw = 0;
 }
@@ -473,6 +477,13 @@ static int upload_stage(Stage& st) {
         tc_build_work(st, tw);
         if ((rc = upload_vec(tw, &st.d_tcw))) return rc;
         st.n_tcw = (int64_t)tw.size() / 3;
+        if (!st.img.units.empty()) {
+            if ((rc = upload_vec(st.img.panels, &st.d_ipanel))) return rc;
+            if ((rc = upload_vec(st.img.build, &st.d_ibuild))) return rc;
+            if ((rc = upload_vec(st.img.outs, &st.d_iout))) return rc;
+            if ((rc = upload_vec(st.img.segs, &st.d_iseg))) return rc;
+            if ((rc = upload_vec(st.img.units, &st.d_iunit))) return rc;
+        }
     }
     return QCM_OK;
 }
@@ -517,6 +528,8 @@ static int launch_axpy(const Stage& st, const BufTable& bt, int precision, cudaS
 static int launch_gemm(const Stage& st, const BufTable& bt, int precision, cudaStream_t s) {
     if (st.n_work == 0) return QCM_OK;
     if (st.n_work > 0x7fffffffLL) { set_error("gemm work list too large"); return QCM_E_RANGE; }
+    if (precision == QCM_PREC_BF16X3 && bt.p[QCM_BUF_IMG] && st.d_iunit)
+        return tc_img_launch(st, bt.p, bt.f32mask, (void*)s);
     if (precision != QCM_PREC_FP64)
         return tc_launch(st.d_a, st.d_b, st.d_tcw, st.n_tcw, bt.p, bt.f32mask, precision, (void*)s);
     if (bt.f32mask) { set_error("the FP64 form takes FP64 buffers only"); return QCM_E_INVALID; }

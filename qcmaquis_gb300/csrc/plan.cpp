@@ -677,6 +677,9 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
     P->scratch[0] = rp_end;
     P->scratch[1] = std::max(t_end, part_end);
     P->scratch[2] = c_end;
+    build_image_tables(s1, s1.img);
+    build_image_tables(s3, s3.img);
+    P->image_bytes = std::max(s1.img.bytes, s3.img.bytes);
     P->stages.push_back(std::move(z0));
     P->stages.push_back(std::move(s0));
     P->stages.push_back(std::move(s1));
@@ -972,6 +975,101 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
     return P;
 }
 
+// Image tables of one GEMM stage.  Each output is computed as a D tile of
+// the MMA with the larger of (M, N) on the 128-row MMA side: when N > M the
+// stage's C = op(A) op(B) is computed as C^T = op(B)^T op(A)^T.  Panels that
+// several segments read with the same orientation share one image.
+void build_image_tables(const Stage& st, ImgTables& t) {
+    t = ImgTables();
+    struct Key {
+        int32_t buf, ld, R, K, kc;
+        int64_t off;
+        bool operator==(const Key& o) const {
+            return buf == o.buf && ld == o.ld && R == o.R && K == o.K && kc == o.kc && off == o.off;
+        }
+    };
+    struct KeyHash {
+        size_t operator()(const Key& k) const {
+            uint64_t h = (uint64_t)k.off * 0x9E3779B97F4A7C15ull;
+            h ^= ((uint64_t)k.buf << 48) ^ ((uint64_t)k.kc << 47) ^ ((uint64_t)k.R << 24) ^ (uint64_t)k.K;
+            h ^= (uint64_t)k.ld * 0xC2B2AE3D27D4EB4Full;
+            return (size_t)(h ^ (h >> 29));
+        }
+    };
+    std::unordered_map<Key, int32_t, KeyHash> ids;
+    auto panel = [&](int32_t buf, int64_t off, int64_t ld, int kcontig, int64_t R, int64_t K) -> int32_t {
+        Key k{buf, (int32_t)ld, (int32_t)R, (int32_t)K, kcontig, off};
+        auto it = ids.find(k);
+        if (it != ids.end()) return it->second;
+        ImgPanel p;
+        p.src_off = off;
+        p.src_buf = buf;
+        p.ld = (int32_t)ld;
+        p.R = (int32_t)R;
+        p.K = (int32_t)K;
+        p.kcontig = kcontig;
+        p.G = (int32_t)((R + 7) / 8);
+        p.img_off = t.bytes;
+        const int64_t kc = (K + 31) / 32;
+        t.bytes += kc * 3 * (int64_t)p.G * 512;
+        const int32_t id = (int32_t)t.panels.size();
+        for (int64_t c = 0; c < kc; ++c) { t.build.push_back(id); t.build.push_back((int32_t)c); }
+        t.panels.push_back(p);
+        ids.emplace(k, id);
+        return id;
+    };
+    for (const GemmOut& o : st.gout) {
+        if (o.M > 0x7fffffff || o.N > 0x7fffffff || o.ldc > 0x7fffffff)
+            throw std::runtime_error("image executor: block too large");
+        const bool tr = o.N > o.M;
+        ImgOut io;
+        io.c_off = o.c_off;
+        io.c_buf = o.c_buf;
+        io.si = tr ? o.ldc : 1;
+        io.sj = tr ? 1 : o.ldc;
+        io.mrows = (int32_t)(tr ? o.N : o.M);
+        io.ncols = (int32_t)(tr ? o.M : o.N);
+        io.pad = 0;
+        const int32_t oid = (int32_t)t.outs.size();
+        t.outs.push_back(io);
+        const int32_t s_begin = (int32_t)t.segs.size();
+        for (int64_t si = o.s_begin; si < o.s_end; ++si) {
+            const GemmSeg& g = st.gseg[si];
+            if (g.K <= 0) continue;
+            if (g.lda > 0x7fffffff || g.ldb > 0x7fffffff || g.K > 0x7fffffff)
+                throw std::runtime_error("image executor: block too large");
+            // op(A): rows m, element (m,k) at ta ? k + m*lda : m + k*lda
+            const int32_t pa = panel(g.a_buf, g.a_off, g.lda, g.ta ? 1 : 0, o.M, g.K);
+            // op(B)^T: rows n, element (n,k) = op(B)(k,n) at tb ? n + k*ldb : k + n*ldb
+            const int32_t pb = panel(g.b_buf, g.b_off, g.ldb, g.tb ? 0 : 1, o.N, g.K);
+            const ImgPanel& A = t.panels[tr ? pb : pa];
+            const ImgPanel& B = t.panels[tr ? pa : pb];
+            ImgSeg s;
+            s.a_img = A.img_off;
+            s.b_img = B.img_off;
+            s.a_G = A.G;
+            s.b_G = B.G;
+            s.kc = (int32_t)((g.K + 31) / 32);
+            s.alpha = (float)g.alpha;
+            t.segs.push_back(s);
+        }
+        const int32_t s_end = (int32_t)t.segs.size();
+        for (int32_t m0 = 0; m0 < io.mrows; m0 += 128)
+            for (int32_t n0 = 0; n0 < io.ncols; n0 += 128) {
+                ImgUnit u;
+                u.out = oid;
+                u.m0 = m0;
+                u.n0 = n0;
+                u.nt = std::min(128, (io.ncols - n0 + 15) / 16 * 16);
+                u.s_begin = s_begin;
+                u.s_end = s_end;
+                t.units.push_back(u);
+            }
+    }
+    if (t.build.size() / 2 > 0x7fffffffULL || t.units.size() > 0x7fffffffULL || t.segs.size() > 0x7fffffffULL)
+        throw std::runtime_error("image executor: tables too large");
+}
+
 }  // namespace qcm
 
 // ------------------------------------------------------------------ C entry points (host part)
@@ -980,7 +1078,7 @@ using namespace qcm;
 extern "C" {
 
 const char* qcm_last_error(void) { return g_err.c_str(); }
-int qcm_version(void) { return 100; }
+int qcm_version(void) { return 110; }
 
 int qcm_plan_sigma(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
                    const qcm_blocks_t* psi, const qcm_boundary_t* left, const qcm_boundary_t* right,
@@ -1034,6 +1132,49 @@ int qcm_plan_sizes(const qcm_plan* p, int64_t* out_elems, int64_t* scratch3) {
     if (!p) { set_error("null plan"); return QCM_E_INVALID; }
     if (out_elems) *out_elems = p->out_elems;
     if (scratch3) for (int i = 0; i < 3; ++i) scratch3[i] = p->scratch[i];
+    return QCM_OK;
+}
+
+int qcm_plan_stage_images(const qcm_plan* p, int32_t stage, int64_t* counts, int64_t* pd, int64_t* od,
+                          int64_t* sd, double* sa, int64_t* td) {
+    if (!p || !counts) { set_error("null argument"); return QCM_E_INVALID; }
+    if (stage < 0 || stage >= (int32_t)p->stages.size()) { set_error("stage out of range"); return QCM_E_RANGE; }
+    const ImgTables& t = p->stages[stage].img;
+    counts[0] = (int64_t)t.panels.size();
+    counts[1] = (int64_t)t.outs.size();
+    counts[2] = (int64_t)t.segs.size();
+    counts[3] = (int64_t)t.units.size();
+    if (pd)
+        for (size_t i = 0; i < t.panels.size(); ++i) {
+            const ImgPanel& x = t.panels[i];
+            const int64_t v[8] = {x.src_off, x.img_off, x.src_buf, x.ld, x.R, x.K, x.kcontig, x.G};
+            for (int j = 0; j < 8; ++j) pd[8 * i + j] = v[j];
+        }
+    if (od)
+        for (size_t i = 0; i < t.outs.size(); ++i) {
+            const ImgOut& x = t.outs[i];
+            const int64_t v[6] = {x.c_off, x.si, x.sj, x.c_buf, x.mrows, x.ncols};
+            for (int j = 0; j < 6; ++j) od[6 * i + j] = v[j];
+        }
+    if (sd)
+        for (size_t i = 0; i < t.segs.size(); ++i) {
+            const ImgSeg& x = t.segs[i];
+            const int64_t v[5] = {x.a_img, x.b_img, x.a_G, x.b_G, x.kc};
+            for (int j = 0; j < 5; ++j) sd[5 * i + j] = v[j];
+            if (sa) sa[i] = x.alpha;
+        }
+    if (td)
+        for (size_t i = 0; i < t.units.size(); ++i) {
+            const ImgUnit& x = t.units[i];
+            const int64_t v[6] = {x.out, x.m0, x.n0, x.nt, x.s_begin, x.s_end};
+            for (int j = 0; j < 6; ++j) td[6 * i + j] = v[j];
+        }
+    return QCM_OK;
+}
+
+int qcm_plan_image_bytes(const qcm_plan* p, int64_t* bytes) {
+    if (!p || !bytes) { set_error("null argument"); return QCM_E_INVALID; }
+    *bytes = p->image_bytes;
     return QCM_OK;
 }
 

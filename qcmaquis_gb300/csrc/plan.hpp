@@ -94,6 +94,43 @@ struct GemmSeg {
 
 enum StageKind { ST_AXPY = 0, ST_GEMM = 1, ST_ZERO = 2 };
 
+// ---- operand images of the BF16x3 tensor-core executor
+// An image holds one operand panel (R rows x K, K-major as the MMA reads it)
+// split into three BF16 slices, in the shared-memory order of the UMMA
+// canonical K-major no-swizzle layout: for K-chunk c (32 elements, 64 bytes
+// per row) and slice s, 8-row group g occupies 512 bytes at
+// img_off + ((c*3 + s)*G + g)*512; inside it, core matrix q (8 K-elements)
+// at q*128, row r%8 at 16-byte steps.  Rows are padded to G*8, K to the chunk
+// size, with zeros.
+struct ImgPanel {
+    int64_t src_off;   // element offset of the source block in its buffer
+    int64_t img_off;   // byte offset of the image in the image buffer (multiple of 512)
+    int32_t src_buf, ld, R, K, kcontig, G;  // kcontig: element (r,k) at r*ld+k, else r+k*ld
+};
+// One output of the image executor: tile element (i, j) (i along the MMA M
+// side, j along N) goes to c_off + i*si + j*sj.
+struct ImgOut {
+    int64_t c_off, si, sj;
+    int32_t c_buf, mrows, ncols, pad;
+};
+struct ImgSeg {
+    int64_t a_img, b_img;   // byte offsets of the A and B panel images
+    int32_t a_G, b_G, kc;   // row groups of the panels, K-chunks
+    float alpha;
+};
+struct ImgUnit {
+    int32_t out, m0, n0, nt, s_begin, s_end;  // nt: MMA N (multiple of 16, <= 128)
+};
+struct ImgTables {
+    std::vector<ImgPanel> panels;
+    std::vector<int32_t> build;   // (panel, chunk) pairs, one image-builder CTA each
+    std::vector<ImgOut> outs;
+    std::vector<ImgSeg> segs;
+    std::vector<ImgUnit> units;
+    int64_t bytes = 0;
+};
+void build_image_tables(const struct Stage& st, ImgTables& t);
+
 struct Stage {
     int kind;
     // ZERO
@@ -115,6 +152,13 @@ struct Stage {
     int32_t src_buf = -1;   // AXPY: the one buffer all terms read (-2: several)
     void* d_cw = nullptr;   // AXPY: chunk work list of the contiguous-source executor
     int64_t n_cw = 0;       // 0: some term's source is not contiguous (generic executor)
+    // GEMM: tables of the BF16x3 image executor (host copies until upload)
+    ImgTables img;
+    void* d_ipanel = nullptr;
+    void* d_ibuild = nullptr;
+    void* d_iout = nullptr;
+    void* d_iseg = nullptr;
+    void* d_iunit = nullptr;
 };
 
 enum PlanKind { PK_SIGMA = 0, PK_BLEFT = 1, PK_BRIGHT = 2 };
@@ -126,6 +170,7 @@ struct qcm_plan {
     std::vector<qcm::Stage> stages;
     int64_t out_elems = 0;
     int64_t scratch[3] = {0, 0, 0};
+    int64_t image_bytes = 0;  // image buffer of the BF16x3 image executor
     // output boundary layout (boundary plans)
     std::vector<int32_t> out_blk_ptr;
     std::vector<qcm::Blk> out_blocks;
@@ -142,6 +187,7 @@ void set_coupling(int a, int b, int c, int d, int e, int f, int g, int h, int i,
 double conjugate_correction(int lc_spin, int rc_spin, int tensor_spin);
 void free_stage_device(Stage& st);
 int tc_build_work(const Stage& st, std::vector<int64_t>& w);
+int tc_img_launch(const Stage& st, double* const* bufs, uint32_t f32mask, void* stream);
 int tc_launch(const void* d_out, const void* d_seg, const void* d_work, int64_t n_work, double* const* bufs,
               uint32_t f32mask, int precision, void* stream);
 }  // namespace qcm

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <string>
 
@@ -389,6 +390,380 @@ int tc_launch(const void* d_out, const void* d_seg, const void* d_work, int64_t 
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) { set_error(std::string("tc_gemm launch: ") + cudaGetErrorString(e)); return QCM_E_CUDA; }
+    return QCM_OK;
+}
+
+// ------------------------------------------------------------------ image executor (BF16x3)
+// Operands are split once per call into BF16 slice images laid out exactly as
+// the MMA reads them from shared memory (ImgPanel).  A persistent kernel, one
+// CTA per SM, then runs a warp-specialised pipeline over its share of the
+// output tiles: warp 0 (one lane) streams image chunks into TI_NS shared-memory
+// stages with cp.async.bulk (completion by transaction count on an mbarrier),
+// warp 1 (one lane) issues the six BF16 products per K-step into one of two
+// TMEM accumulators, and warps 2..9 drain each finished segment (one block
+// product of the split-K sum) into compensated FP32 register sums, scaled by
+// the segment's coefficient, and store the tile once.
+constexpr int TI_NS = 4;
+constexpr int TI_THREADS = 320;
+constexpr uint32_t TI_SLICE = 16 * 512;         // one slice of a 128-row x 64-byte chunk
+constexpr uint32_t TI_STAGE = 6 * TI_SLICE;     // A and B, three slices each
+constexpr int TI_EPI_LD = 17;                   // epilogue staging row stride (floats)
+constexpr uint32_t TI_SMEM = TI_NS * TI_STAGE + 8 * 32 * TI_EPI_LD * 4 + 1024;
+constexpr uint64_t TI_WAIT_NS = 4000000000ull;  // a wait that lasts this long gives up
+
+struct TiArgs {
+    const ImgUnit* units;
+    const ImgSeg* segs;
+    const ImgOut* outs;
+    const uint8_t* img;
+    double* p[QCM_NBUF];
+    uint32_t f32mask;
+    int32_t n_units;
+};
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done) : "r"(mbar), "r"(parity) : "memory");
+    return done != 0;
+}
+
+// Bounded wait: gives up after TI_WAIT_NS, or early when another role of the
+// CTA has raised the abort flag (abort == nullptr: no early exit).
+__device__ __forceinline__ bool ti_wait(uint32_t mbar, uint32_t parity, const volatile int* abort) {
+    uint64_t t0 = 0;
+    for (uint32_t it = 0; it < TC_SPIN_LIMIT; ++it) {
+        if (mbar_try(mbar, parity)) return true;
+        if ((it & 255u) == 255u) {
+            if (abort && *abort) return false;
+            const uint64_t t = global_ns();
+            if (t0 == 0) t0 = t;
+            else if (t - t0 > TI_WAIT_NS) return false;
+        }
+    }
+    return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(mbar), "r"(bytes) : "memory");
+}
+
+// global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(dst), "l"(src), "r"(bytes), "r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(mbar)
+                 : "memory");
+}
+
+// One CTA per (panel, K-chunk): warp w builds 8-row groups w, w+8, ...; lane
+// (rr, q) reads the 8 K-values of core matrix q of row rr and writes them as
+// one 16-byte vector per slice.
+__global__ void __launch_bounds__(256)
+build_images_kernel(const ImgPanel* __restrict__ panels, const int32_t* __restrict__ items,
+                    uint8_t* __restrict__ img, TcBufs bufs) {
+    const ImgPanel P = panels[items[2 * blockIdx.x]];
+    const int c = items[2 * blockIdx.x + 1];
+    const bool f32 = (bufs.f32mask >> P.src_buf) & 1u;
+    const float* __restrict__ S32 = (const float*)bufs.p[P.src_buf] + P.src_off;
+    const double* __restrict__ S64 = bufs.p[P.src_buf] + P.src_off;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rr = lane & 7, q = lane >> 3;
+    const int k0 = c * 32 + q * 8;
+    const uint32_t sstride = (uint32_t)P.G * 512u;
+    uint8_t* base = img + P.img_off + (size_t)c * 3 * sstride + q * 128 + rr * 16;
+    for (int g = warp; g < P.G; g += 8) {
+        const int r = g * 8 + rr;
+        float v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int k = k0 + j;
+            float x = 0.0f;
+            if (r < P.R && k < P.K) {
+                const int ix = P.kcontig ? r * P.ld + k : r + k * P.ld;
+                x = f32 ? __ldg(S32 + ix) : (float)__ldg(S64 + ix);
+            }
+            v[j] = x;
+        }
+        put_vec<QCM_PREC_BF16X3>(base + (size_t)g * 512, 0, sstride, v);
+    }
+}
+
+__global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
+    extern __shared__ uint8_t ti_smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)ti_smem_raw + 1023) & ~(uintptr_t)1023);
+    float* epi = (float*)(smem + TI_NS * TI_STAGE);
+    __shared__ __align__(8) uint64_t bar_full[TI_NS], bar_empty[TI_NS], bar_accf[2], bar_acce[2], bar_fin;
+    __shared__ uint32_t tmem_sh;
+    __shared__ int abort_sh;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    volatile int* abort_flag = &abort_sh;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(&tmem_sh)), "r"(256u));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 32) {
+        for (int i = 0; i < TI_NS; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bar_full[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bar_empty[i])));
+        }
+        for (int i = 0; i < 2; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bar_accf[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;" :: "r"(smem_u32(&bar_acce[i])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bar_fin)));
+        abort_sh = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_sh;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---------------- producer
+            uint32_t it = 0;
+            bool ok = true;
+            for (int u = blockIdx.x; u < a.n_units && ok; u += gridDim.x) {
+                const ImgUnit U = a.units[u];
+                const int gA0 = U.m0 >> 3, gB0 = U.n0 >> 3;
+                for (int s = U.s_begin; s < U.s_end && ok; ++s) {
+                    const ImgSeg S = a.segs[s];
+                    const uint32_t bA = (uint32_t)min(16, S.a_G - gA0) * 512u;
+                    const uint32_t bB = (uint32_t)min(U.nt >> 3, S.b_G - gB0) * 512u;
+                    for (int c = 0; c < S.kc; ++c, ++it) {
+                        const uint32_t st = it % TI_NS, ph = (it / TI_NS) & 1u;
+                        if (!ti_wait(smem_u32(&bar_empty[st]), ph ^ 1u, abort_flag)) { ok = false; break; }
+                        const uint32_t fb = smem_u32(&bar_full[st]);
+                        mbar_expect_tx(fb, 3u * (bA + bB));
+                        const uint32_t dst = smem_u32(smem + st * TI_STAGE);
+#pragma unroll
+                        for (int sl = 0; sl < 3; ++sl) {
+                            bulk_g2s(dst + sl * TI_SLICE,
+                                     a.img + S.a_img + ((int64_t)(c * 3 + sl) * S.a_G + gA0) * 512, bA, fb);
+                            bulk_g2s(dst + (3 + sl) * TI_SLICE,
+                                     a.img + S.b_img + ((int64_t)(c * 3 + sl) * S.b_G + gB0) * 512, bB, fb);
+                        }
+                    }
+                }
+            }
+            if (!ok) { *abort_flag = 1; atomicExch(&g_tc_status, 2); }
+            // the copies of every stage's latest round must have landed before the CTA exits
+            for (uint32_t k = 0; k < (uint32_t)TI_NS && k < it; ++k) {
+                const uint32_t j = it - 1 - k;
+                if (!ti_wait(smem_u32(&bar_full[j % TI_NS]), (j / TI_NS) & 1u, nullptr)) atomicExch(&g_tc_status, 2);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---------------- MMA issuer
+            uint32_t it = 0, sc = 0;
+            bool ok = true;
+            for (int u = blockIdx.x; u < a.n_units && ok; u += gridDim.x) {
+                const ImgUnit U = a.units[u];
+                const uint32_t idesc = make_idesc(1u, TC_BM, U.nt);
+                for (int s = U.s_begin; s < U.s_end && ok; ++s) {
+                    const int kc = a.segs[s].kc;
+                    const uint32_t b = sc & 1u;
+                    if (!ti_wait(smem_u32(&bar_acce[b]), ((sc >> 1) & 1u) ^ 1u, abort_flag)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t d = tmem + b * 128u;
+                    for (int c = 0; c < kc; ++c, ++it) {
+                        const uint32_t st = it % TI_NS, ph = (it / TI_NS) & 1u;
+                        if (!ti_wait(smem_u32(&bar_full[st]), ph, abort_flag)) { ok = false; break; }
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        const uint32_t a0 = smem_u32(smem + st * TI_STAGE), b0 = a0 + 3 * TI_SLICE;
+#pragma unroll
+                        for (int kk = 0; kk < 2; ++kk) {
+#pragma unroll
+                            for (int p = 0; p < 6; ++p) {
+                                const int ia = p == 2 ? 1 : p == 4 ? 1 : p == 5 ? 2 : 0;
+                                const int ib = p == 1 ? 1 : p == 3 ? 2 : p == 4 ? 1 : 0;
+                                const uint64_t da = make_sdesc(a0 + ia * TI_SLICE + kk * 256, 128, 512);
+                                const uint64_t db = make_sdesc(b0 + ib * TI_SLICE + kk * 256, 128, 512);
+                                const uint32_t accum = (c == 0 && kk == 0 && p == 0) ? 0u : 1u;
+                                asm volatile(
+                                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+                                    :: "r"(d), "l"(da), "l"(db), "r"(idesc), "r"(accum));
+                            }
+                        }
+                        mma_commit(smem_u32(&bar_empty[st]));
+                    }
+                    if (!ok) break;
+                    mma_commit(smem_u32(&bar_accf[b]));
+                    ++sc;
+                }
+            }
+            if (!ok) { *abort_flag = 1; atomicExch(&g_tc_status, 2); }
+            // every MMA issued must be complete before TMEM is released
+            mma_commit(smem_u32(&bar_fin));
+            if (!ti_wait(smem_u32(&bar_fin), 0u, nullptr)) atomicExch(&g_tc_status, 2);
+        }
+    } else {
+        // ---------------- epilogue: warps 2..9; TMEM lanes 32*(warp%4).., columns 64*h..
+        const int e = warp - 2, q = warp & 3, h = e >> 2;
+        float* stg = epi + e * 32 * TI_EPI_LD;
+        uint32_t sc = 0;
+        bool ok = true;
+        for (int u = blockIdx.x; u < a.n_units && ok; u += gridDim.x) {
+            const ImgUnit U = a.units[u];
+            const ImgOut O = a.outs[U.out];
+            const int ncw = max(0, min(64, U.nt - h * 64));
+            float hi[64], lo[64];
+#pragma unroll
+            for (int j = 0; j < 64; ++j) { hi[j] = 0.0f; lo[j] = 0.0f; }
+            for (int s = U.s_begin; s < U.s_end; ++s) {
+                const float alpha = a.segs[s].alpha;
+                const uint32_t b = sc & 1u;
+                ok = __all_sync(0xffffffffu, ti_wait(smem_u32(&bar_accf[b]), (sc >> 1) & 1u, abort_flag));
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * 128u + (uint32_t)(h * 64);
+#pragma unroll
+                for (int c16 = 0; c16 < 4; ++c16) {
+                    if (c16 * 16 < ncw) {
+                        uint32_t r[16];
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                              "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                              "=r"(r[14]), "=r"(r[15])
+                            : "r"(taddr + (uint32_t)(c16 * 16)));
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const float x = alpha * __uint_as_float(r[j]);
+                            const float t = hi[c16 * 16 + j] + x;  // Knuth two-sum
+                            const float bp = t - hi[c16 * 16 + j];
+                            const float err = (hi[c16 * 16 + j] - (t - bp)) + (x - bp);
+                            hi[c16 * 16 + j] = t;
+                            lo[c16 * 16 + j] += err;
+                        }
+                    }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&bar_acce[b]));
+                ++sc;
+            }
+            if (!ok) break;
+            const bool c32 = (a.f32mask >> O.c_buf) & 1u;
+            float* __restrict__ C32 = (float*)a.p[O.c_buf] + O.c_off;
+            double* __restrict__ C64 = a.p[O.c_buf] + O.c_off;
+            const int i0 = U.m0 + q * 32;
+            if (O.si == 1) {
+                // lanes hold consecutive rows i: each column store is coalesced
+                const int i = i0 + lane;
+#pragma unroll
+                for (int c16 = 0; c16 < 4; ++c16) {
+                    if (c16 * 16 < ncw) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const int col = U.n0 + h * 64 + c16 * 16 + j;
+                            if (i < O.mrows && col < O.ncols) {
+                                const int64_t off = (int64_t)i + (int64_t)col * O.sj;
+                                const float v = hi[c16 * 16 + j] + lo[c16 * 16 + j];
+                                if (c32) C32[off] = v;
+                                else C64[off] = (double)hi[c16 * 16 + j] + (double)lo[c16 * 16 + j];
+                            }
+                        }
+                    }
+                }
+            } else {
+                // rows i lie O.si apart in memory and columns are contiguous: pass each
+                // 32 x 16 block through shared memory so that 16 lanes store one row run
+#pragma unroll
+                for (int c16 = 0; c16 < 4; ++c16) {
+                    if (c16 * 16 < ncw) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) stg[lane * TI_EPI_LD + j] = hi[c16 * 16 + j] + lo[c16 * 16 + j];
+                        __syncwarp();
+                        const int jj = lane & 15;
+                        const int col = U.n0 + h * 64 + c16 * 16 + jj;
+                        for (int rr = lane >> 4; rr < 32; rr += 2) {
+                            const int i = i0 + rr;
+                            if (i < O.mrows && col < O.ncols) {
+                                const int64_t off = (int64_t)i * O.si + col;
+                                const float v = stg[rr * TI_EPI_LD + jj];
+                                if (c32) C32[off] = v;
+                                else C64[off] = (double)v;
+                            }
+                        }
+                        __syncwarp();
+                    }
+                }
+            }
+        }
+        if (!ok && lane == 0) { *abort_flag = 1; atomicExch(&g_tc_status, 2); }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        __syncwarp();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(256u));
+    }
+}
+
+static int sm_count_of_current_device() {
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (cached[dev] == 0) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
+int tc_img_launch(const Stage& st, double* const* bufs, uint32_t f32mask, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    const ImgTables& t = st.img;
+    if (t.units.empty()) return QCM_OK;
+    if (!st.d_iunit || !bufs[QCM_BUF_IMG]) { set_error("image executor: tables or image buffer missing"); return QCM_E_STATE; }
+    TcBufs tb;
+    for (int i = 0; i < QCM_NBUF; ++i) tb.p[i] = bufs[i];
+    tb.f32mask = f32mask;
+    uint8_t* img = (uint8_t*)bufs[QCM_BUF_IMG];
+    const size_t n_build = t.build.size() / 2;
+    if (n_build > 0)
+        build_images_kernel<<<(unsigned)n_build, 256, 0, s>>>((const ImgPanel*)st.d_ipanel, (const int32_t*)st.d_ibuild,
+                                                              img, tb);
+    cudaError_t e = cudaFuncSetAttribute(tc_img_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TI_SMEM);
+    if (e != cudaSuccess) { set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e)); return QCM_E_CUDA; }
+    TiArgs a;
+    a.units = (const ImgUnit*)st.d_iunit;
+    a.segs = (const ImgSeg*)st.d_iseg;
+    a.outs = (const ImgOut*)st.d_iout;
+    a.img = img;
+    for (int i = 0; i < QCM_NBUF; ++i) a.p[i] = bufs[i];
+    a.f32mask = f32mask;
+    a.n_units = (int32_t)t.units.size();
+    const int grid = (int)std::min<size_t>(t.units.size(), (size_t)sm_count_of_current_device());
+    tc_img_kernel<<<grid, TI_THREADS, TI_SMEM, s>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) { set_error(std::string("tc_img launch: ") + cudaGetErrorString(e)); return QCM_E_CUDA; }
     return QCM_OK;
 }
 

@@ -81,11 +81,11 @@ def _ptr(t: Optional[torch.Tensor]) -> int:
 
 
 class Workspace:
-    """Grow-only scratch buffers for the three plan scratch slots."""
+    """Grow-only scratch buffers: the three plan scratch slots and the operand-image slot."""
 
     def __init__(self, device):
         self.device = device
-        self.bufs = [None, None, None]
+        self.bufs = [None, None, None, None]
 
     def get(self, sizes):
         out = []
@@ -103,12 +103,15 @@ class Workspace:
 class Engine:
     """Plan cache + execution of the SU2U1 contractions on one GPU."""
 
-    def __init__(self, device="cuda", precision: int = N.PREC_FP64, hermitian: bool = True):
+    def __init__(self, device="cuda", precision: int = N.PREC_FP64, hermitian: bool = True,
+                 use_images: bool = True):
         _require_cuda()
         N.lib()
         self.device = torch.device(device)
         self.precision = precision
         self.hermitian = hermitian
+        # BF16x3 form: feed the tensor cores from pre-split operand images
+        self.use_images = use_images
         self.ws = Workspace(self.device)
         self._plans: Dict[tuple, N.Plan] = {}
         self._mpo_cache: Dict[int, N.FMpo] = {}
@@ -143,7 +146,8 @@ class Engine:
         """Run a plan.  ``left`` / ``right`` are DeviceBoundary objects or raw FP64 tensors;
         the mixed forms read FP32 boundary shadows and keep every intermediate in FP32."""
         prec = self.precision if precision is None else precision
-        s0, s1, s2 = self.ws.get(plan.scratch)
+        img_elems = (plan.image_bytes + 7) // 8 if (prec == N.PREC_BF16X3 and self.use_images) else 0
+        s0, s1, s2, img = self.ws.get(list(plan.scratch) + [img_elems])
         mask = 0
         lt = left.data if isinstance(left, DeviceBoundary) else left
         rt = right.data if isinstance(right, DeviceBoundary) else right
@@ -155,8 +159,8 @@ class Engine:
             if isinstance(right, DeviceBoundary):
                 rt = right.f32()
                 mask |= 1 << N.QCM_BUF_RIGHT
-        plan.run_typed([_ptr(ket), _ptr(lt), _ptr(rt), _ptr(out), _ptr(s0), _ptr(s1), _ptr(s2)], mask, prec,
-                       self._stream(), first, last)
+        plan.run_typed([_ptr(ket), _ptr(lt), _ptr(rt), _ptr(out), _ptr(s0), _ptr(s1), _ptr(s2),
+                        _ptr(img) if img_elems else 0], mask, prec, self._stream(), first, last)
         if first == 0 and last == -1:
             self.launches += plan.launches
 

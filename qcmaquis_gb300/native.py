@@ -18,8 +18,8 @@ from .symmetry import Index
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libqcm_gb300.so")
 
-QCM_BUF_KET, QCM_BUF_LEFT, QCM_BUF_RIGHT, QCM_BUF_OUT, QCM_BUF_S0, QCM_BUF_S1, QCM_BUF_S2 = range(7)
-QCM_NBUF = 7
+QCM_BUF_KET, QCM_BUF_LEFT, QCM_BUF_RIGHT, QCM_BUF_OUT, QCM_BUF_S0, QCM_BUF_S1, QCM_BUF_S2, QCM_BUF_IMG = range(8)
+QCM_NBUF = 8
 PREC_FP64, PREC_TF32, PREC_BF16X3 = 0, 1, 2
 
 i32p = C.POINTER(C.c_int32)
@@ -68,6 +68,8 @@ def lib():
         getattr(L, name).argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks), C.POINTER(CBoundary),
                                                                C.POINTER(CMpo), C.c_int32, C.POINTER(C.c_void_p)]
     L.qcm_plan_sizes.argtypes = [C.c_void_p, i64p, i64p]
+    L.qcm_plan_image_bytes.argtypes = [C.c_void_p, i64p]
+    L.qcm_plan_stage_images.argtypes = [C.c_void_p, C.c_int32, i64p, i64p, i64p, i64p, f64p, i64p]
     L.qcm_plan_work.argtypes = [C.c_void_p, f64p, f64p, f64p, i32p]
     L.qcm_plan_out_layout.argtypes = [C.c_void_p, i32p, i32p, i32p, i32p, i64p, i64p, i64p]
     L.qcm_plan_num_stages.argtypes = [C.c_void_p, i32p]
@@ -288,6 +290,9 @@ class Plan:
         check(lib().qcm_plan_sizes(self.h, C.byref(out), sc), "qcm_plan_sizes")
         self.out_elems = out.value
         self.scratch = [sc[0], sc[1], sc[2]]
+        ib = C.c_int64()
+        check(lib().qcm_plan_image_bytes(self.h, C.byref(ib)), "qcm_plan_image_bytes")
+        self.image_bytes = ib.value
         gf, af, ab, nl = C.c_double(), C.c_double(), C.c_double(), C.c_int32()
         check(lib().qcm_plan_work(self.h, C.byref(gf), C.byref(af), C.byref(ab), C.byref(nl)), "qcm_plan_work")
         self.gemm_flops, self.axpy_flops, self.axpy_bytes, self.launches = gf.value, af.value, ab.value, nl.value
@@ -338,6 +343,21 @@ class Plan:
             else:
                 out.append(("zero", int(no.value), int(nt.value)))
         return out
+
+    def stage_images(self, stage: int):
+        """Export the BF16x3 image-executor tables of a GEMM stage (host-side inspection and tests)."""
+        cnt = np.zeros(4, dtype=np.int64)
+        check(lib().qcm_plan_stage_images(self.h, stage, _p(cnt, i64p), None, None, None, None, None),
+              "qcm_plan_stage_images")
+        npn, no, ns, nu = [int(x) for x in cnt]
+        pd = np.zeros((max(npn, 1), 8), dtype=np.int64)
+        od = np.zeros((max(no, 1), 6), dtype=np.int64)
+        sd = np.zeros((max(ns, 1), 5), dtype=np.int64)
+        sa = np.zeros(max(ns, 1))
+        td = np.zeros((max(nu, 1), 6), dtype=np.int64)
+        check(lib().qcm_plan_stage_images(self.h, stage, _p(cnt, i64p), _p(pd, i64p), _p(od, i64p), _p(sd, i64p),
+                                          _p(sa, f64p), _p(td, i64p)), "qcm_plan_stage_images")
+        return {"panels": pd[:npn], "outs": od[:no], "segs": sd[:ns], "alpha": sa[:ns], "tiles": td[:nu]}
 
     def upload(self):
         if not self.uploaded:

@@ -12,8 +12,14 @@ def _view(buf, off, ld, rows, cols):
     return np.lib.stride_tricks.as_strided(buf[off:], shape=(rows, cols), strides=(8, 8 * ld))
 
 
-def run_plan(plan, bufs):
-    for st in plan.stages():
+def run_plan(plan, bufs, images=False):
+    """images=True runs the GEMM stages through the BF16x3 image-executor tables."""
+    for si, st in enumerate(plan.stages()):
+        if images and st[0] == "gemm":
+            tab = plan.stage_images(si)
+            if len(tab["tiles"]):
+                run_gemm_images(tab, bufs, plan.image_bytes)
+                continue
         if st[0] == "zero":
             zbuf, zlen = st[1], st[2]
             bufs[zbuf][:zlen] = 0.0
@@ -37,3 +43,55 @@ def run_plan(plan, bufs):
                     B = _view(bufs[bb], bo, ldb, N, K).T if tb else _view(bufs[bb], bo, ldb, K, N)
                     acc += sa[s] * (A @ B)
                 _view(bufs[cb], co, ldc, M, N)[:, :] = acc
+
+
+def run_gemm_images(tab, bufs, image_bytes):
+    """Execute one GEMM stage the way the BF16x3 image executor addresses it,
+    with FP64 values in slice 0 and zero slices 1 and 2: build every panel
+    image, then for every output tile copy each K-chunk's row groups into a
+    128-row "shared memory" tile (rows the copy does not reach are NaN, as a
+    stale shared-memory row would be garbage), multiply, scale by the
+    segment's coefficient and store the tile's valid region.  A check of the
+    tables and of the kernel's index arithmetic, not an execution path."""
+    img = np.zeros(image_bytes // 2)   # one slot per 2-byte element position
+
+    def slot(img_off, G, c, s, r, k):
+        return (img_off + ((c * 3 + s) * G + r // 8) * 512 + ((k % 32) // 8) * 128 + (r % 8) * 16 + (k % 8) * 2) // 2
+
+    for (src_off, img_off, src_buf, ld, R, K, kcontig, G) in tab["panels"]:
+        kc = (K + 31) // 32
+        r = np.arange(G * 8)[:, None]
+        k = np.arange(kc * 32)[None, :]
+        ok = (r < R) & (k < K)
+        ix = np.where(kcontig, r * ld + k, r + k * ld)
+        vals = np.where(ok, bufs[src_buf][src_off + np.where(ok, ix, 0)], 0.0)
+        assert img_off % 512 == 0 and img_off + kc * 3 * G * 512 <= image_bytes
+        for s in range(3):
+            sl = slot(img_off, G, k // 32, s, r, k)
+            img[sl] = vals if s == 0 else 0.0
+    outs, segs, alpha = tab["outs"], tab["segs"], tab["alpha"]
+    for (out, m0, n0, nt, sb, se) in tab["tiles"]:
+        c_off, si, sj, c_buf, mrows, ncols = [int(x) for x in outs[out]]
+        assert nt % 16 == 0 and 16 <= nt <= 128 and m0 % 128 == 0 and n0 % 128 == 0
+        acc = np.zeros((128, nt))
+        for s in range(sb, se):
+            a_img, b_img, a_G, b_G, kc = [int(x) for x in segs[s]]
+            ngA, ngB = min(16, a_G - m0 // 8), min(nt // 8, b_G - n0 // 8)
+            assert ngA > 0 and ngB > 0
+            D = np.zeros((128, nt))
+            for c in range(kc):
+                A = np.full((128, 32), np.nan)
+                B = np.full((nt, 32), np.nan)
+                kk = np.arange(32)[None, :]
+                ra = np.arange(ngA * 8)[:, None]
+                rb = np.arange(ngB * 8)[:, None]
+                A[:ngA * 8] = img[slot(a_img, a_G, c, 0, m0 + ra, kk)]
+                B[:ngB * 8] = img[slot(b_img, b_G, c, 0, n0 + rb, kk)]
+                D += A @ B.T
+            acc += alpha[s] * D
+        i = np.arange(128)[:, None]
+        j = np.arange(nt)[None, :]
+        valid = (m0 + i < mrows) & (n0 + j < ncols)
+        assert np.all(np.isfinite(acc[valid]))
+        dst = c_off + (m0 + i) * si + (n0 + j) * sj
+        bufs[c_buf][dst[valid]] = acc[valid]

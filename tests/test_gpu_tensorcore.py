@@ -58,3 +58,29 @@ def test_tensorcore_sigma_multi_tile():
         err = (torch.linalg.norm(o[prec] - ref) / torch.linalg.norm(ref)).item()
         assert err < tol, (prec, err)
     assert _status() == 0
+
+
+@pytest.mark.parametrize("L,m", [(12, 256), (16, 512)])
+def test_image_executor_matches_in_kernel_split(L, m):
+    """The BF16x3 image executor (bulk-copied pre-split operands, persistent
+    warp-specialised kernel) and the in-kernel-split executor both stay within
+    2e-5 of the FP64 sigma and agree with each other to the same order; the
+    image executor is deterministic across calls."""
+    from qcmaquis_gb300.engine import Engine
+    from qcmaquis_gb300.workloads import build_sigma_host, upload_sigma_workload
+    w = build_sigma_host(L=L, nelec=L, m=m)
+    eng = Engine("cuda:0")
+    upload_sigma_workload(w, eng)
+    ref = eng.site_hamil2(w.psi, w.left, w.right, w.ts_mpo, precision=N.PREC_FP64).data.clone()
+    eng.use_images = True
+    a1 = eng.site_hamil2(w.psi, w.left, w.right, w.ts_mpo, precision=N.PREC_BF16X3).data.clone()
+    a2 = eng.site_hamil2(w.psi, w.left, w.right, w.ts_mpo, precision=N.PREC_BF16X3).data.clone()
+    eng.use_images = False
+    b = eng.site_hamil2(w.psi, w.left, w.right, w.ts_mpo, precision=N.PREC_BF16X3).data.clone()
+    torch.cuda.synchronize()
+    nr = torch.linalg.norm(ref)
+    assert (torch.linalg.norm(a1 - ref) / nr).item() < 2e-5
+    assert (torch.linalg.norm(b - ref) / nr).item() < 2e-5
+    assert (torch.linalg.norm(a1 - b) / nr).item() < 2e-5
+    assert torch.equal(a1, a2)
+    assert _status() == 0

@@ -54,6 +54,27 @@ def test_sigma_plan_matches_oracle(herm, site, m):
     assert np.linalg.norm(bufs[3] - ref) <= 1e-13 * np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("L,m,site,herm", [(12, 400, 5, True), (8, 200, 3, False)])
+def test_sigma_image_tables_match_oracle(L, m, site, herm):
+    """The BF16x3 image executor's tables and addressing (emulated in FP64,
+    stale shared-memory rows as NaN) reproduce the oracle's sigma; at L=12,
+    m=400 blocks span several 128-row tiles and 32-wide K-chunks.  The
+    executor keeps segment coefficients in FP32, hence the 1e-7 bound."""
+    psi, left, right, ts = _random_site_problem(L=L, N=L, m=m, site=site, herm=herm)
+    psi = psi.copy().make_left_paired()
+    lay = N.Layout.of(psi.data)
+    Ll, Rl = N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
+    p = N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, N.FMpo(ts), herm)
+    assert p.image_bytes > 0
+    tiles = [len(p.stage_images(i)["tiles"]) for i, k in enumerate(p.stage_kinds()) if k == "gemm"]
+    assert all(t > 0 for t in tiles)
+    bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.zeros(p.out_elems)] + \
+        [np.zeros(max(s, 1)) for s in p.scratch]
+    run_plan(p, bufs, images=True)
+    ref = lay.pack(R.site_hamil2(psi, left, right, ts, is_hermitian=herm).data)
+    assert np.linalg.norm(bufs[3] - ref) <= 1e-7 * np.linalg.norm(ref)
+
+
 @pytest.mark.parametrize("herm", [True, False])
 def test_boundary_plans_match_oracle_layout_and_values(herm):
     L, Ne = 6, 6
