@@ -173,14 +173,20 @@ int qcm_plan_stage_axpy(const qcm_plan* plan, int32_t stage, int64_t* out_desc /
 int qcm_plan_stage_gemm(const qcm_plan* plan, int32_t stage, int64_t* out_desc /*7*n_out*/,
                         int64_t* seg_desc /*9*n_terms*/, double* seg_alpha);
 
-/* Export the BF16x3 image-executor tables of a GEMM stage (host-side
- * inspection and tests).  counts4 = (panels, outputs, segments, tiles); call
- * with NULL arrays first.  panel: (src_off, img_off, src_buf, ld, R, K, kcontig, G);
- * output: (c_off, si, sj, c_buf, mrows, ncols); segment: (a_img, b_img, a_G, b_G, kc)
- * with seg_alpha; tile: (out, m0, n0, nt, s_begin, s_end). */
+/* Export the BF16x3 image-executor tables of a stage (host-side inspection
+ * and tests): the block products of a GEMM stage, or the dense groups of a
+ * gather-axpy stage.  counts4 = (panels, outputs, segments, tiles); call with
+ * NULL arrays first.  panel: (src_off, img_off, src_buf, ld, R, K, kcontig, G);
+ * output: (c_off, si, sj, c_buf, mrows, ncols, mode, rows, ctab); segment:
+ * (a_img, b_img, a_G, b_G, kc, flags) with seg_alpha; tile: (out, m0, n0, nt,
+ * s_begin, s_end). */
 int qcm_plan_stage_images(const qcm_plan* plan, int32_t stage, int64_t* counts4, int64_t* panel_desc /*8*n*/,
-                          int64_t* out_desc /*6*n*/, int64_t* seg_desc /*5*n*/, double* seg_alpha,
+                          int64_t* out_desc /*9*n*/, int64_t* seg_desc /*6*n*/, double* seg_alpha,
                           int64_t* tile_desc /*6*n*/);
+/* Auxiliary tables of the same: counts3 = (gather offsets, output-tile
+ * offsets, constant-image bytes). */
+int qcm_plan_stage_image_aux(const qcm_plan* plan, int32_t stage, int64_t* counts3, int64_t* gather,
+                             int64_t* coltab, uint8_t* const_images);
 
 /* Copy the plan's task tables to the current device (once per plan). */
 int qcm_plan_upload(qcm_plan* plan);

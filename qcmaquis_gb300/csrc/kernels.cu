@@ -409,12 +409,14 @@ void free_stage_device(Stage& st) {
     if (st.d_c) cudaFree(st.d_c);
     if (st.d_tcw) cudaFree(st.d_tcw);
     if (st.d_cw) cudaFree(st.d_cw);
-    for (void** d : {&st.d_ipanel, &st.d_ibuild, &st.d_iout, &st.d_iseg, &st.d_iunit}) {
+    for (void** d : {&st.d_ipanel, &st.d_ibuild, &st.d_iout, &st.d_iseg, &st.d_iunit, &st.d_igather, &st.d_icoltab,
+                     &st.d_icimg, &st.d_cw_light}) {
         if (*d) cudaFree(*d);
         *d = nullptr;
     }
     st.d_a = st.d_b = st.d_c = st.d_tcw = st.d_cw = nullptr;
     st.n_cw = 0;
+    st.n_cw_light = 0;
 }
 
 template <class T>
@@ -423,6 +425,20 @@ static int upload_vec(const std::vector<T>& v, void** d) {
     cudaError_t e = cudaMalloc(d, bytes);
     if (e != cudaSuccess) { set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e)); return QCM_E_NOMEM; }
     if (!v.empty()) QCM_CUDA(cudaMemcpy(*d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return QCM_OK;
+}
+
+static int upload_images(Stage& st) {
+    int rc = QCM_OK;
+    if (st.img.units.empty()) return QCM_OK;
+    if ((rc = upload_vec(st.img.panels, &st.d_ipanel))) return rc;
+    if ((rc = upload_vec(st.img.build, &st.d_ibuild))) return rc;
+    if ((rc = upload_vec(st.img.outs, &st.d_iout))) return rc;
+    if ((rc = upload_vec(st.img.segs, &st.d_iseg))) return rc;
+    if ((rc = upload_vec(st.img.units, &st.d_iunit))) return rc;
+    if ((rc = upload_vec(st.img.gather, &st.d_igather))) return rc;
+    if ((rc = upload_vec(st.img.coltab, &st.d_icoltab))) return rc;
+    if ((rc = upload_vec(st.img.cimg, &st.d_icimg))) return rc;
     return QCM_OK;
 }
 
@@ -454,6 +470,15 @@ static int upload_stage(Stage& st) {
         if (st.src_buf >= 0 && build_chunk_work(st, cw) && !cw.empty() && cw.size() < 0x7fffffffULL) {
             if ((rc = upload_vec(cw, &st.d_cw))) return rc;
             st.n_cw = (int64_t)cw.size();
+            if (!st.img.units.empty() && st.heavy.size() == st.aout.size()) {
+                // the outputs the dense groups do not compute, in the same order
+                std::vector<DevAxpyChunk> lw;
+                for (const DevAxpyChunk& c : cw)
+                    if (!st.heavy[c.out]) lw.push_back(c);
+                if (!lw.empty() && (rc = upload_vec(lw, &st.d_cw_light))) return rc;
+                st.n_cw_light = (int64_t)lw.size();
+                if ((rc = upload_images(st))) return rc;
+            }
         }
     } else if (st.kind == ST_GEMM) {
         std::vector<DevGemmOut> o(st.gout.size());
@@ -477,13 +502,7 @@ static int upload_stage(Stage& st) {
         tc_build_work(st, tw);
         if ((rc = upload_vec(tw, &st.d_tcw))) return rc;
         st.n_tcw = (int64_t)tw.size() / 3;
-        if (!st.img.units.empty()) {
-            if ((rc = upload_vec(st.img.panels, &st.d_ipanel))) return rc;
-            if ((rc = upload_vec(st.img.build, &st.d_ibuild))) return rc;
-            if ((rc = upload_vec(st.img.outs, &st.d_iout))) return rc;
-            if ((rc = upload_vec(st.img.segs, &st.d_iseg))) return rc;
-            if ((rc = upload_vec(st.img.units, &st.d_iunit))) return rc;
-        }
+        if ((rc = upload_images(st))) return rc;
     }
     return QCM_OK;
 }
@@ -500,7 +519,15 @@ static int launch_axpy(const Stage& st, const BufTable& bt, int precision, cudaS
     if (st.src_buf >= 0 && st.n_cw > 0 && precision != QCM_PREC_FP64) {
         const bool src32 = (bt.f32mask >> st.src_buf) & 1u;
         const auto* CW = (const DevAxpyChunk*)st.d_cw;
-        const unsigned gc = (unsigned)st.n_cw;
+        unsigned gc = (unsigned)st.n_cw;
+        if (precision == QCM_PREC_BF16X3 && bt.p[QCM_BUF_IMG] && st.d_iunit) {
+            // BF16x3 with images: the dense groups on the tensor cores, the rest gathered
+            int rc = tc_img_launch(st, bt.p, bt.f32mask, (void*)s);
+            if (rc) return rc;
+            CW = (const DevAxpyChunk*)st.d_cw_light;
+            gc = (unsigned)st.n_cw_light;
+            if (gc == 0) return QCM_OK;
+        }
         if (src32) {
             gather_axpy_contig<float, float><<<gc, CG_THREADS, 0, s>>>(bt, O, T, CW);
         } else {

@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <stdexcept>
 #include <thread>
@@ -679,7 +680,8 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
     P->scratch[2] = c_end;
     build_image_tables(s1, s1.img);
     build_image_tables(s3, s3.img);
-    P->image_bytes = std::max(s1.img.bytes, s3.img.bytes);
+    build_dense_groups(s2, 64, s2.img, s2.heavy);
+    P->image_bytes = std::max(std::max(s1.img.bytes, s3.img.bytes), s2.img.bytes);
     P->stages.push_back(std::move(z0));
     P->stages.push_back(std::move(s0));
     P->stages.push_back(std::move(s1));
@@ -1029,6 +1031,9 @@ void build_image_tables(const Stage& st, ImgTables& t) {
         io.sj = tr ? 1 : o.ldc;
         io.mrows = (int32_t)(tr ? o.N : o.M);
         io.ncols = (int32_t)(tr ? o.M : o.N);
+        io.ctab = 0;
+        io.mode = 0;
+        io.rows = 0;
         io.pad = 0;
         const int32_t oid = (int32_t)t.outs.size();
         t.outs.push_back(io);
@@ -1051,6 +1056,8 @@ void build_image_tables(const Stage& st, ImgTables& t) {
             s.b_G = B.G;
             s.kc = (int32_t)((g.K + 31) / 32);
             s.alpha = (float)g.alpha;
+            s.flags = 0;
+            s.pad = 0;
             t.segs.push_back(s);
         }
         const int32_t s_end = (int32_t)t.segs.size();
@@ -1068,6 +1075,168 @@ void build_image_tables(const Stage& st, ImgTables& t) {
     }
     if (t.build.size() / 2 > 0x7fffffffULL || t.units.size() > 0x7fffffffULL || t.segs.size() > 0x7fffffffULL)
         throw std::runtime_error("image executor: tables too large");
+}
+
+// Round-to-nearest-even FP32 -> BF16 (finite inputs) and back.
+static uint16_t bf16_rne(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+static float bf16_to_float(uint16_t h) {
+    const uint32_t u = (uint32_t)h << 16;
+    float x;
+    std::memcpy(&x, &u, 4);
+    return x;
+}
+
+void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::vector<char>& heavy) {
+    t = ImgTables();
+    const size_t nO = st.aout.size();
+    heavy.assign(nO, 0);
+    if (nO == 0) return;
+    // connected components of the output/source graph
+    std::vector<int32_t> parent(nO);
+    for (size_t i = 0; i < nO; ++i) parent[i] = (int32_t)i;
+    auto find = [&](int32_t x) {
+        while (parent[x] != x) { parent[x] = parent[parent[x]]; x = parent[x]; }
+        return x;
+    };
+    std::unordered_map<int64_t, int32_t> first_user;
+    first_user.reserve(st.aterm.size() / 4 + 16);
+    for (size_t i = 0; i < nO; ++i) {
+        const AxpyOut& a = st.aout[i];
+        for (int64_t k = a.t_begin; k < a.t_end; ++k) {
+            const AxpyTerm& x = st.aterm[k];
+            if (x.lds != a.rows && a.cols > 1) return;  // sources must be contiguous tiles
+            const int64_t key = ((int64_t)x.src_buf << 56) ^ x.src_off;
+            auto it = first_user.emplace(key, (int32_t)i);
+            if (!it.second) {
+                const int32_t r1 = find((int32_t)i), r2 = find(it.first->second);
+                if (r1 != r2) parent[std::max(r1, r2)] = std::min(r1, r2);
+            }
+        }
+    }
+    // candidate groups: (component, rows, cols, ldd, dst_buf, src_buf) over heavy outputs
+    std::map<std::tuple<int32_t, int64_t, int64_t, int64_t, int32_t, int32_t>, std::vector<int32_t>> groups;
+    for (size_t i = 0; i < nO; ++i) {
+        const AxpyOut& a = st.aout[i];
+        if (a.t_end - a.t_begin < min_terms || a.rows * a.cols <= 0) continue;
+        const int32_t sb = st.aterm[a.t_begin].src_buf;
+        bool uniform = true;
+        for (int64_t k = a.t_begin; k < a.t_end; ++k) uniform &= st.aterm[k].src_buf == sb;
+        if (!uniform) continue;
+        groups[std::make_tuple(find((int32_t)i), a.rows, a.cols, a.ldd, a.dst_buf, sb)].push_back((int32_t)i);
+    }
+    for (auto& kv : groups) {
+        const std::vector<int32_t>& O = kv.second;
+        const int64_t rows = std::get<1>(kv.first), cols = std::get<2>(kv.first), ldd = std::get<3>(kv.first);
+        const int32_t dst_buf = std::get<4>(kv.first), src_buf = std::get<5>(kv.first);
+        const int64_t E = rows * cols;
+        if (E > 0x7fffffffLL || ldd > 0x7fffffffLL || O.size() < 8) continue;
+        std::unordered_map<int64_t, int32_t> sid;
+        std::vector<int64_t> srcs;
+        int64_t nterms = 0;
+        for (int32_t o : O)
+            for (int64_t k = st.aout[o].t_begin; k < st.aout[o].t_end; ++k, ++nterms)
+                if (sid.emplace(st.aterm[k].src_off, (int32_t)srcs.size()).second) srcs.push_back(st.aterm[k].src_off);
+        const int64_t S = (int64_t)srcs.size();
+        // dense block products pay when a fair share of the (outputs x sources) block is populated
+        if ((double)nterms < 0.05 * (double)O.size() * (double)S) continue;
+        const int64_t KC = (S + 31) / 32;
+        const int32_t G = (int32_t)((E + 7) / 8);
+        const int32_t Gb = (int32_t)((O.size() + 7) / 8);
+        // A: gathered source tiles, rows e, K = source index
+        ImgPanel pa;
+        pa.src_off = (int64_t)t.gather.size();
+        pa.img_off = t.bytes;
+        pa.src_buf = src_buf;
+        pa.ld = 0;
+        pa.R = (int32_t)E;
+        pa.K = (int32_t)S;
+        pa.kcontig = 2;
+        pa.G = G;
+        t.gather.insert(t.gather.end(), srcs.begin(), srcs.end());
+        t.bytes += KC * 3 * (int64_t)G * 512;
+        const int32_t pid = (int32_t)t.panels.size();
+        for (int64_t c = 0; c < KC; ++c) { t.build.push_back(pid); t.build.push_back((int32_t)c); }
+        t.panels.push_back(pa);
+        // B: coefficient matrix W (rows = outputs, K = sources), split on the host
+        std::vector<float> W((size_t)O.size() * S, 0.0f);
+        {
+            std::vector<double> Wd((size_t)O.size() * S, 0.0);
+            for (size_t j = 0; j < O.size(); ++j)
+                for (int64_t k = st.aout[O[j]].t_begin; k < st.aout[O[j]].t_end; ++k)
+                    Wd[j * S + sid[st.aterm[k].src_off]] += st.aterm[k].alpha;
+            for (size_t x = 0; x < W.size(); ++x) W[x] = (float)Wd[x];
+        }
+        const int64_t b_off = (int64_t)t.cimg.size();
+        t.cimg.resize(t.cimg.size() + (size_t)(KC * 3 * (int64_t)Gb * 512), 0);
+        for (size_t j = 0; j < O.size(); ++j)
+            for (int64_t k = 0; k < S; ++k) {
+                const float x = W[j * S + k];
+                if (x == 0.0f) continue;
+                const uint16_t h0 = bf16_rne(x);
+                const float r1 = x - bf16_to_float(h0);
+                const uint16_t h1 = bf16_rne(r1);
+                const float r2 = r1 - bf16_to_float(h1);
+                const uint16_t h2 = bf16_rne(r2);
+                const uint16_t h[3] = {h0, h1, h2};
+                const int64_t c = k / 32, q = (k % 32) / 8;
+                for (int sl = 0; sl < 3; ++sl) {
+                    const int64_t byte = b_off + ((c * 3 + sl) * Gb + (int64_t)(j / 8)) * 512 + q * 128 +
+                                         (int64_t)(j % 8) * 16 + (k % 8) * 2;
+                    std::memcpy(&t.cimg[(size_t)byte], &h[sl], 2);
+                }
+            }
+        // output: column j is output tile O[j]
+        ImgOut io;
+        io.c_off = 0;
+        io.si = ldd;
+        io.sj = 0;
+        io.ctab = (int64_t)t.coltab.size();
+        io.c_buf = dst_buf;
+        io.mrows = (int32_t)E;
+        io.ncols = (int32_t)O.size();
+        io.mode = 1;
+        io.rows = (int32_t)rows;
+        io.pad = 0;
+        for (int32_t o : O) t.coltab.push_back(st.aout[o].dst_off);
+        const int32_t oid = (int32_t)t.outs.size();
+        t.outs.push_back(io);
+        // segments: 4 K-chunks (128 sources) per drain of the accumulator
+        const int32_t s_begin = (int32_t)t.segs.size();
+        for (int64_t c0 = 0; c0 < KC; c0 += 4) {
+            ImgSeg sg;
+            sg.a_img = pa.img_off + c0 * 3 * (int64_t)G * 512;
+            sg.b_img = b_off + c0 * 3 * (int64_t)Gb * 512;
+            sg.a_G = G;
+            sg.b_G = Gb;
+            sg.kc = (int32_t)std::min<int64_t>(4, KC - c0);
+            sg.alpha = 1.0f;
+            sg.flags = IMG_B_CONST;
+            sg.pad = 0;
+            t.segs.push_back(sg);
+        }
+        const int32_t s_end = (int32_t)t.segs.size();
+        const int32_t nnt = (int32_t)((O.size() + 127) / 128);
+        const int32_t per = (int32_t)(((O.size() + nnt - 1) / nnt + 15) / 16 * 16);
+        for (int32_t m0 = 0; m0 < (int32_t)E; m0 += 128)
+            for (int32_t n0 = 0; n0 < (int32_t)O.size(); n0 += per) {
+                ImgUnit u;
+                u.out = oid;
+                u.m0 = m0;
+                u.n0 = n0;
+                u.nt = std::min(per, ((int32_t)O.size() - n0 + 15) / 16 * 16);
+                u.s_begin = s_begin;
+                u.s_end = s_end;
+                t.units.push_back(u);
+            }
+        for (int32_t o : O) heavy[o] = 1;
+    }
+    if (t.build.size() / 2 > 0x7fffffffULL || t.units.size() > 0x7fffffffULL)
+        throw std::runtime_error("dense groups: tables too large");
 }
 
 }  // namespace qcm
@@ -1153,14 +1322,14 @@ int qcm_plan_stage_images(const qcm_plan* p, int32_t stage, int64_t* counts, int
     if (od)
         for (size_t i = 0; i < t.outs.size(); ++i) {
             const ImgOut& x = t.outs[i];
-            const int64_t v[6] = {x.c_off, x.si, x.sj, x.c_buf, x.mrows, x.ncols};
-            for (int j = 0; j < 6; ++j) od[6 * i + j] = v[j];
+            const int64_t v[9] = {x.c_off, x.si, x.sj, x.c_buf, x.mrows, x.ncols, x.mode, x.rows, x.ctab};
+            for (int j = 0; j < 9; ++j) od[9 * i + j] = v[j];
         }
     if (sd)
         for (size_t i = 0; i < t.segs.size(); ++i) {
             const ImgSeg& x = t.segs[i];
-            const int64_t v[5] = {x.a_img, x.b_img, x.a_G, x.b_G, x.kc};
-            for (int j = 0; j < 5; ++j) sd[5 * i + j] = v[j];
+            const int64_t v[6] = {x.a_img, x.b_img, x.a_G, x.b_G, x.kc, x.flags};
+            for (int j = 0; j < 6; ++j) sd[6 * i + j] = v[j];
             if (sa) sa[i] = x.alpha;
         }
     if (td)
@@ -1169,6 +1338,20 @@ int qcm_plan_stage_images(const qcm_plan* p, int32_t stage, int64_t* counts, int
             const int64_t v[6] = {x.out, x.m0, x.n0, x.nt, x.s_begin, x.s_end};
             for (int j = 0; j < 6; ++j) td[6 * i + j] = v[j];
         }
+    return QCM_OK;
+}
+
+int qcm_plan_stage_image_aux(const qcm_plan* p, int32_t stage, int64_t* counts, int64_t* gather, int64_t* coltab,
+                             uint8_t* cimg) {
+    if (!p || !counts) { set_error("null argument"); return QCM_E_INVALID; }
+    if (stage < 0 || stage >= (int32_t)p->stages.size()) { set_error("stage out of range"); return QCM_E_RANGE; }
+    const ImgTables& t = p->stages[stage].img;
+    counts[0] = (int64_t)t.gather.size();
+    counts[1] = (int64_t)t.coltab.size();
+    counts[2] = (int64_t)t.cimg.size();
+    if (gather && !t.gather.empty()) std::memcpy(gather, t.gather.data(), t.gather.size() * 8);
+    if (coltab && !t.coltab.empty()) std::memcpy(coltab, t.coltab.data(), t.coltab.size() * 8);
+    if (cimg && !t.cimg.empty()) std::memcpy(cimg, t.cimg.data(), t.cimg.size());
     return QCM_OK;
 }
 

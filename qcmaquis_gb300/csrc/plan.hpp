@@ -103,20 +103,25 @@ enum StageKind { ST_AXPY = 0, ST_GEMM = 1, ST_ZERO = 2 };
 // at q*128, row r%8 at 16-byte steps.  Rows are padded to G*8, K to the chunk
 // size, with zeros.
 struct ImgPanel {
-    int64_t src_off;   // element offset of the source block in its buffer
+    int64_t src_off;   // element offset of the source block (kcontig 2: offset into the gather table)
     int64_t img_off;   // byte offset of the image in the image buffer (multiple of 512)
-    int32_t src_buf, ld, R, K, kcontig, G;  // kcontig: element (r,k) at r*ld+k, else r+k*ld
+    int32_t src_buf, ld, R, K, kcontig, G;
+    // kcontig 0: element (r,k) at src_off + r + k*ld; 1: at src_off + r*ld + k;
+    // 2: at gather[src_off + k] + r (column k is a contiguous source tile)
 };
-// One output of the image executor: tile element (i, j) (i along the MMA M
-// side, j along N) goes to c_off + i*si + j*sj.
+// One output of the image executor, tile element (i, j) with i along the MMA
+// M side and j along N: mode 0 writes c_off + i*si + j*sj; mode 1 writes
+// coltab[ctab + j] + (i % rows) + (i / rows)*si (column j is one output tile).
 struct ImgOut {
-    int64_t c_off, si, sj;
-    int32_t c_buf, mrows, ncols, pad;
+    int64_t c_off, si, sj, ctab;
+    int32_t c_buf, mrows, ncols, mode, rows, pad;
 };
+enum { IMG_B_CONST = 2 };   // ImgSeg.flags: the B image lives in the plan's constant images
 struct ImgSeg {
-    int64_t a_img, b_img;   // byte offsets of the A and B panel images
+    int64_t a_img, b_img;   // byte offsets of the A and B panel images (at the chunk range start)
     int32_t a_G, b_G, kc;   // row groups of the panels, K-chunks
     float alpha;
+    int32_t flags, pad;
 };
 struct ImgUnit {
     int32_t out, m0, n0, nt, s_begin, s_end;  // nt: MMA N (multiple of 16, <= 128)
@@ -127,9 +132,18 @@ struct ImgTables {
     std::vector<ImgOut> outs;
     std::vector<ImgSeg> segs;
     std::vector<ImgUnit> units;
-    int64_t bytes = 0;
+    std::vector<int64_t> gather;  // source offsets of gathered panels (kcontig 2)
+    std::vector<int64_t> coltab;  // output-tile offsets of mode-1 outputs
+    std::vector<uint8_t> cimg;    // constant images (coefficient matrices), built by the plan
+    int64_t bytes = 0;            // per-call image bytes
 };
 void build_image_tables(const struct Stage& st, ImgTables& t);
+// Dense groups of a gather-axpy stage: output tiles that share their sources
+// (a connected component of the output/source graph), have at least
+// min_terms terms and one tile shape become one block product
+// contr[:, group] = T_gathered . W^T on the tensor cores.  heavy[o] marks the
+// outputs taken.
+void build_dense_groups(const struct Stage& st, int64_t min_terms, ImgTables& t, std::vector<char>& heavy);
 
 struct Stage {
     int kind;
@@ -152,8 +166,14 @@ struct Stage {
     int32_t src_buf = -1;   // AXPY: the one buffer all terms read (-2: several)
     void* d_cw = nullptr;   // AXPY: chunk work list of the contiguous-source executor
     int64_t n_cw = 0;       // 0: some term's source is not contiguous (generic executor)
-    // GEMM: tables of the BF16x3 image executor (host copies until upload)
+    // GEMM: tables of the BF16x3 image executor; AXPY: its dense groups
     ImgTables img;
+    std::vector<char> heavy;     // AXPY: outputs computed by the dense groups
+    void* d_igather = nullptr;
+    void* d_icoltab = nullptr;
+    void* d_icimg = nullptr;
+    void* d_cw_light = nullptr;  // AXPY: chunk work list of the outputs outside the dense groups
+    int64_t n_cw_light = 0;
     void* d_ipanel = nullptr;
     void* d_ibuild = nullptr;
     void* d_iout = nullptr;

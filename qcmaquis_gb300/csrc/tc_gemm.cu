@@ -416,6 +416,8 @@ struct TiArgs {
     const ImgSeg* segs;
     const ImgOut* outs;
     const uint8_t* img;
+    const uint8_t* cimg;      // constant images of the plan (coefficient matrices)
+    const int64_t* coltab;    // output-tile offsets of mode-1 outputs
     double* p[QCM_NBUF];
     uint32_t f32mask;
     int32_t n_units;
@@ -477,12 +479,13 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
 // one 16-byte vector per slice.
 __global__ void __launch_bounds__(256)
 build_images_kernel(const ImgPanel* __restrict__ panels, const int32_t* __restrict__ items,
-                    uint8_t* __restrict__ img, TcBufs bufs) {
+                    const int64_t* __restrict__ gather, uint8_t* __restrict__ img, TcBufs bufs) {
     const ImgPanel P = panels[items[2 * blockIdx.x]];
     const int c = items[2 * blockIdx.x + 1];
     const bool f32 = (bufs.f32mask >> P.src_buf) & 1u;
-    const float* __restrict__ S32 = (const float*)bufs.p[P.src_buf] + P.src_off;
-    const double* __restrict__ S64 = bufs.p[P.src_buf] + P.src_off;
+    const int64_t so = P.kcontig == 2 ? 0 : P.src_off;
+    const float* __restrict__ S32 = (const float*)bufs.p[P.src_buf] + so;
+    const double* __restrict__ S64 = bufs.p[P.src_buf] + so;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rr = lane & 7, q = lane >> 3;
     const int k0 = c * 32 + q * 8;
@@ -496,8 +499,13 @@ build_images_kernel(const ImgPanel* __restrict__ panels, const int32_t* __restri
             const int k = k0 + j;
             float x = 0.0f;
             if (r < P.R && k < P.K) {
-                const int ix = P.kcontig ? r * P.ld + k : r + k * P.ld;
-                x = f32 ? __ldg(S32 + ix) : (float)__ldg(S64 + ix);
+                if (P.kcontig == 2) {   // column k = one contiguous source tile
+                    const int64_t ix = __ldg(gather + P.src_off + k) + r;
+                    x = f32 ? __ldg((const float*)bufs.p[P.src_buf] + ix) : (float)__ldg(bufs.p[P.src_buf] + ix);
+                } else {
+                    const int ix = P.kcontig ? r * P.ld + k : r + k * P.ld;
+                    x = f32 ? __ldg(S32 + ix) : (float)__ldg(S64 + ix);
+                }
             }
             v[j] = x;
         }
@@ -548,6 +556,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                 const int gA0 = U.m0 >> 3, gB0 = U.n0 >> 3;
                 for (int s = U.s_begin; s < U.s_end && ok; ++s) {
                     const ImgSeg S = a.segs[s];
+                    const uint8_t* bbase = (S.flags & IMG_B_CONST) ? a.cimg : a.img;
                     const uint32_t bA = (uint32_t)min(16, S.a_G - gA0) * 512u;
                     const uint32_t bB = (uint32_t)min(U.nt >> 3, S.b_G - gB0) * 512u;
                     for (int c = 0; c < S.kc; ++c, ++it) {
@@ -561,7 +570,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                             bulk_g2s(dst + sl * TI_SLICE,
                                      a.img + S.a_img + ((int64_t)(c * 3 + sl) * S.a_G + gA0) * 512, bA, fb);
                             bulk_g2s(dst + (3 + sl) * TI_SLICE,
-                                     a.img + S.b_img + ((int64_t)(c * 3 + sl) * S.b_G + gB0) * 512, bB, fb);
+                                     bbase + S.b_img + ((int64_t)(c * 3 + sl) * S.b_G + gB0) * 512, bB, fb);
                         }
                     }
                 }
@@ -671,7 +680,25 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
             float* __restrict__ C32 = (float*)a.p[O.c_buf] + O.c_off;
             double* __restrict__ C64 = a.p[O.c_buf] + O.c_off;
             const int i0 = U.m0 + q * 32;
-            if (O.si == 1) {
+            if (O.mode == 1) {
+                // column j is one output tile: element i at (i % rows) + (i / rows)*si of it
+                const int i = i0 + lane;
+                const int64_t ib = (int64_t)(i % O.rows) + (int64_t)(i / O.rows) * O.si;
+#pragma unroll
+                for (int c16 = 0; c16 < 4; ++c16) {
+                    if (c16 * 16 < ncw) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const int col = U.n0 + h * 64 + c16 * 16 + j;
+                            if (i < O.mrows && col < O.ncols) {
+                                const int64_t off = __ldg(a.coltab + O.ctab + col) + ib;
+                                if (c32) ((float*)a.p[O.c_buf])[off] = hi[c16 * 16 + j] + lo[c16 * 16 + j];
+                                else a.p[O.c_buf][off] = (double)hi[c16 * 16 + j] + (double)lo[c16 * 16 + j];
+                            }
+                        }
+                    }
+                }
+            } else if (O.si == 1) {
                 // lanes hold consecutive rows i: each column store is coalesced
                 const int i = i0 + lane;
 #pragma unroll
@@ -749,7 +776,7 @@ int tc_img_launch(const Stage& st, double* const* bufs, uint32_t f32mask, void* 
     const size_t n_build = t.build.size() / 2;
     if (n_build > 0)
         build_images_kernel<<<(unsigned)n_build, 256, 0, s>>>((const ImgPanel*)st.d_ipanel, (const int32_t*)st.d_ibuild,
-                                                              img, tb);
+                                                              (const int64_t*)st.d_igather, img, tb);
     cudaError_t e = cudaFuncSetAttribute(tc_img_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TI_SMEM);
     if (e != cudaSuccess) { set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e)); return QCM_E_CUDA; }
     TiArgs a;
@@ -757,6 +784,8 @@ int tc_img_launch(const Stage& st, double* const* bufs, uint32_t f32mask, void* 
     a.segs = (const ImgSeg*)st.d_iseg;
     a.outs = (const ImgOut*)st.d_iout;
     a.img = img;
+    a.cimg = (const uint8_t*)st.d_icimg;
+    a.coltab = (const int64_t*)st.d_icoltab;
     for (int i = 0; i < QCM_NBUF; ++i) a.p[i] = bufs[i];
     a.f32mask = f32mask;
     a.n_units = (int32_t)t.units.size();

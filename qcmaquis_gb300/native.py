@@ -70,6 +70,7 @@ def lib():
     L.qcm_plan_sizes.argtypes = [C.c_void_p, i64p, i64p]
     L.qcm_plan_image_bytes.argtypes = [C.c_void_p, i64p]
     L.qcm_plan_stage_images.argtypes = [C.c_void_p, C.c_int32, i64p, i64p, i64p, i64p, f64p, i64p]
+    L.qcm_plan_stage_image_aux.argtypes = [C.c_void_p, C.c_int32, i64p, i64p, i64p, C.POINTER(C.c_uint8)]
     L.qcm_plan_work.argtypes = [C.c_void_p, f64p, f64p, f64p, i32p]
     L.qcm_plan_out_layout.argtypes = [C.c_void_p, i32p, i32p, i32p, i32p, i64p, i64p, i64p]
     L.qcm_plan_num_stages.argtypes = [C.c_void_p, i32p]
@@ -351,13 +352,21 @@ class Plan:
               "qcm_plan_stage_images")
         npn, no, ns, nu = [int(x) for x in cnt]
         pd = np.zeros((max(npn, 1), 8), dtype=np.int64)
-        od = np.zeros((max(no, 1), 6), dtype=np.int64)
-        sd = np.zeros((max(ns, 1), 5), dtype=np.int64)
+        od = np.zeros((max(no, 1), 9), dtype=np.int64)
+        sd = np.zeros((max(ns, 1), 6), dtype=np.int64)
         sa = np.zeros(max(ns, 1))
         td = np.zeros((max(nu, 1), 6), dtype=np.int64)
         check(lib().qcm_plan_stage_images(self.h, stage, _p(cnt, i64p), _p(pd, i64p), _p(od, i64p), _p(sd, i64p),
                                           _p(sa, f64p), _p(td, i64p)), "qcm_plan_stage_images")
-        return {"panels": pd[:npn], "outs": od[:no], "segs": sd[:ns], "alpha": sa[:ns], "tiles": td[:nu]}
+        ac = np.zeros(3, dtype=np.int64)
+        check(lib().qcm_plan_stage_image_aux(self.h, stage, _p(ac, i64p), None, None, None), "qcm_plan_stage_image_aux")
+        gat = np.zeros(max(int(ac[0]), 1), dtype=np.int64)
+        col = np.zeros(max(int(ac[1]), 1), dtype=np.int64)
+        cim = np.zeros(max(int(ac[2]), 1), dtype=np.uint8)
+        check(lib().qcm_plan_stage_image_aux(self.h, stage, _p(ac, i64p), _p(gat, i64p), _p(col, i64p),
+                                             cim.ctypes.data_as(C.POINTER(C.c_uint8))), "qcm_plan_stage_image_aux")
+        return {"panels": pd[:npn], "outs": od[:no], "segs": sd[:ns], "alpha": sa[:ns], "tiles": td[:nu],
+                "gather": gat[:int(ac[0])], "coltab": col[:int(ac[1])], "cimg": cim[:int(ac[2])]}
 
     def upload(self):
         if not self.uploaded:

@@ -15,11 +15,14 @@ def _view(buf, off, ld, rows, cols):
 def run_plan(plan, bufs, images=False):
     """images=True runs the GEMM stages through the BF16x3 image-executor tables."""
     for si, st in enumerate(plan.stages()):
-        if images and st[0] == "gemm":
+        heavy = set()
+        if images and st[0] in ("gemm", "axpy"):
             tab = plan.stage_images(si)
             if len(tab["tiles"]):
                 run_gemm_images(tab, bufs, plan.image_bytes)
-                continue
+                if st[0] == "gemm":
+                    continue
+                heavy = set(int(x) for x in tab["coltab"])   # outputs the dense groups wrote
         if st[0] == "zero":
             zbuf, zlen = st[1], st[2]
             bufs[zbuf][:zlen] = 0.0
@@ -27,6 +30,8 @@ def run_plan(plan, bufs, images=False):
             od, td, ta = st[1], st[2], st[3]
             for o in od:
                 dst_buf, dst_off, ldd, rows, cols, tb, te = [int(x) for x in o]
+                if dst_off in heavy:
+                    continue
                 acc = np.zeros((rows, cols))
                 for t in range(tb, te):
                     sb, so, lds = [int(x) for x in td[t]]
@@ -45,15 +50,27 @@ def run_plan(plan, bufs, images=False):
                 _view(bufs[cb], co, ldc, M, N)[:, :] = acc
 
 
+def _bf16_slots(raw):
+    """Decode an image byte array into one float per 2-byte BF16 slot."""
+    u = np.frombuffer(raw.tobytes(), dtype=np.uint16).astype(np.uint32) << 16
+    return u.view(np.float32).astype(np.float64)
+
+
+PAIRS = [(0, 0), (0, 1), (1, 0), (0, 2), (1, 1), (2, 0)]   # the six BF16 slice products
+
+
 def run_gemm_images(tab, bufs, image_bytes):
-    """Execute one GEMM stage the way the BF16x3 image executor addresses it,
-    with FP64 values in slice 0 and zero slices 1 and 2: build every panel
-    image, then for every output tile copy each K-chunk's row groups into a
-    128-row "shared memory" tile (rows the copy does not reach are NaN, as a
-    stale shared-memory row would be garbage), multiply, scale by the
-    segment's coefficient and store the tile's valid region.  A check of the
-    tables and of the kernel's index arithmetic, not an execution path."""
+    """Execute the image-executor tables of one stage the way the kernels
+    address them.  Per-call images are built with the FP64 value in slice 0
+    and zero slices 1 and 2; constant images (coefficient matrices) hold the
+    plan's real BF16 slices.  For every output tile each K-chunk's row groups
+    are copied into a 128-row "shared memory" tile (rows the copy does not
+    reach are NaN, as a stale shared-memory row would be garbage), the six
+    slice products are summed, the segment is scaled by its coefficient and
+    the tile's valid region is stored.  A check of the tables and of the
+    kernels' index arithmetic, not an execution path."""
     img = np.zeros(image_bytes // 2)   # one slot per 2-byte element position
+    cimg = _bf16_slots(tab["cimg"]) if len(tab["cimg"]) else np.zeros(1)
 
     def slot(img_off, G, c, s, r, k):
         return (img_off + ((c * 3 + s) * G + r // 8) * 512 + ((k % 32) // 8) * 128 + (r % 8) * 16 + (k % 8) * 2) // 2
@@ -63,35 +80,45 @@ def run_gemm_images(tab, bufs, image_bytes):
         r = np.arange(G * 8)[:, None]
         k = np.arange(kc * 32)[None, :]
         ok = (r < R) & (k < K)
-        ix = np.where(kcontig, r * ld + k, r + k * ld)
-        vals = np.where(ok, bufs[src_buf][src_off + np.where(ok, ix, 0)], 0.0)
+        if kcontig == 2:
+            col = tab["gather"][src_off + np.minimum(k, K - 1)]
+            ix = col + r
+        else:
+            ix = src_off + np.where(kcontig, r * ld + k, r + k * ld)
+        vals = np.where(ok, bufs[src_buf][np.where(ok, ix, 0)], 0.0)
         assert img_off % 512 == 0 and img_off + kc * 3 * G * 512 <= image_bytes
         for s in range(3):
-            sl = slot(img_off, G, k // 32, s, r, k)
-            img[sl] = vals if s == 0 else 0.0
+            img[slot(img_off, G, k // 32, s, r, k)] = vals if s == 0 else 0.0
     outs, segs, alpha = tab["outs"], tab["segs"], tab["alpha"]
     for (out, m0, n0, nt, sb, se) in tab["tiles"]:
-        c_off, si, sj, c_buf, mrows, ncols = [int(x) for x in outs[out]]
-        assert nt % 16 == 0 and 16 <= nt <= 128 and m0 % 128 == 0 and n0 % 128 == 0
+        c_off, si, sj, c_buf, mrows, ncols, mode, rows, ctab = [int(x) for x in outs[out]]
+        assert nt % 16 == 0 and 16 <= nt <= 128 and m0 % 128 == 0 and n0 % 8 == 0
         acc = np.zeros((128, nt))
         for s in range(sb, se):
-            a_img, b_img, a_G, b_G, kc = [int(x) for x in segs[s]]
+            a_img, b_img, a_G, b_G, kc, flags = [int(x) for x in segs[s]]
+            bsrc = cimg if flags & 2 else img
             ngA, ngB = min(16, a_G - m0 // 8), min(nt // 8, b_G - n0 // 8)
             assert ngA > 0 and ngB > 0
             D = np.zeros((128, nt))
+            kk = np.arange(32)[None, :]
+            ra = np.arange(ngA * 8)[:, None]
+            rb = np.arange(ngB * 8)[:, None]
             for c in range(kc):
-                A = np.full((128, 32), np.nan)
-                B = np.full((nt, 32), np.nan)
-                kk = np.arange(32)[None, :]
-                ra = np.arange(ngA * 8)[:, None]
-                rb = np.arange(ngB * 8)[:, None]
-                A[:ngA * 8] = img[slot(a_img, a_G, c, 0, m0 + ra, kk)]
-                B[:ngB * 8] = img[slot(b_img, b_G, c, 0, n0 + rb, kk)]
-                D += A @ B.T
+                A = np.full((3, 128, 32), np.nan)
+                B = np.full((3, nt, 32), np.nan)
+                for sl in range(3):
+                    A[sl, :ngA * 8] = img[slot(a_img, a_G, c, sl, m0 + ra, kk)]
+                    B[sl, :ngB * 8] = bsrc[slot(b_img, b_G, c, sl, n0 + rb, kk)]
+                for ia, ib in PAIRS:
+                    D += A[ia] @ B[ib].T
             acc += alpha[s] * D
         i = np.arange(128)[:, None]
         j = np.arange(nt)[None, :]
         valid = (m0 + i < mrows) & (n0 + j < ncols)
         assert np.all(np.isfinite(acc[valid]))
-        dst = c_off + (m0 + i) * si + (n0 + j) * sj
+        if mode == 0:
+            dst = c_off + (m0 + i) * si + (n0 + j) * sj
+        else:
+            e = m0 + i
+            dst = tab["coltab"][ctab + np.minimum(n0 + j, ncols - 1)] + (e % rows) + (e // rows) * si
         bufs[c_buf][dst[valid]] = acc[valid]
