@@ -133,54 +133,41 @@ def dgemm_peak_tflops():
     return 2.0 * n ** 3 / best / 1e12
 
 
-def cpu_oracle_sample(L: int, budget_s: float = 20.0):
-    """Oracle sigma on the host cores: same Hamiltonian family, bond dimension
-    reduced until the boundaries can be built in the time budget."""
-    import numpy as np
-    from oracle import dmrg_ref as R
-    from qcmaquis_gb300.workloads import build_sigma_host
-    m = 96
-    w = build_sigma_host(L=L, m=m)
-    t0 = time.time()
-    left = [R.BlockMatrix.from_indices(R.Index([((0, 0), 1)]), R.Index([((0, 0), 1)]), fill=1.0)]
-    for i, t in enumerate(w.left_sites):
-        ot = R.MPSTensor(t.phys_i, t.left_i, t.right_i, t.data.copy(), R.LEFT_PAIRED)
-        left = R.overlap_mpo_left_step(ot, ot, left, w.mpo[i])
-    right = [R.BlockMatrix.from_indices(R.Index([((w.nelec, 0), 1)]), R.Index([((w.nelec, 0), 1)]), fill=1.0)]
-    for k in range(len(w.right_sites) - 1, -1, -1):
-        i = w.site + 2 + k
-        t = w.right_sites[k]
-        ot = R.MPSTensor(t.phys_i, t.left_i, t.right_i, t.data.copy(), R.LEFT_PAIRED)
-        right = R.overlap_mpo_right_step(ot, ot, right, w.mpo[i])
-    tb = time.time() - t0
-    p = w.psi_host
-    psi = R.MPSTensor(p.phys_i, p.left_i, p.right_i, p.data.copy(), R.LEFT_PAIRED)
-    calls, flops, tt = 0, 0.0, 0.0
-    while tt < budget_s and calls < 50:
-        R.FLOPS.reset()
-        t1 = time.time()
-        R.site_hamil2(psi, left, right, w.ts_mpo)
-        tt += time.time() - t1
-        flops += R.FLOPS.gemm_flops + R.FLOPS.axpy_flops
-        calls += 1
-    return {"value": flops / tt / 1e12, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-            "sample": f"numpy oracle sigma, L={L} N={w.nelec} middle sites, bond dimension m={m} (m=1024 "
-                      f"boundaries do not build in a bounded CPU time); {calls} calls in {tt:.1f}s, "
-                      f"boundaries {tb:.1f}s; BLAS threads = host cores"}
+def cpu_oracle_sample(L: int, m: int, budget_s: float = 20.0):
+    """The oracle's sigma on the host cores, a bounded sample of the same workload."""
+    from oracle.cpu_sample import sigma_sample
+    return sigma_sample(L, m, budget_s=budget_s)
 
 
 def run_reference(args):
+    """CPU arm: the oracle port of the reference's sigma on the host cores
+    (the reference itself does not build here), on this workload; each step is
+    a bounded sample of one sigma."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    cpu = cpu_oracle_sample(args.L, budget_s=max(5.0, 3.0 * args.steps))
-    line = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "sigma vector, L=24 N=24 S=0 SU2U1 middle sites (bounded CPU sample)",
-                       "L": args.L, "m": args.m},
+    from oracle.cpu_sample import SigmaSample
+    smp = SigmaSample(args.L, args.m)
+    budget = 12.0
+    for _ in range(args.warmup):
+        smp.step(0.0)
+    flops = dt = 0.0
+    done = 0
+    for _ in range(args.steps):
+        f, t, done = smp.step(budget)
+        flops += f
+        dt += t
+    value = flops / dt / 1e12
+    cpu = {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+           "sample": smp.describe(flops, dt, done, args.steps)}
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded workload layouts, random boundary values)",
+            "config": {"workload": f"sigma vector H_eff.psi, L={args.L} N={args.L} S=0 SU2U1, middle sites, "
+                                   f"m={args.m} (bounded CPU sample per step)", "L": args.L, "m": args.m},
             "cpu_baseline": cpu,
-            "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
@@ -314,7 +301,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_oracle_sample(args.L, budget_s=15.0)
+            cpu = cpu_oracle_sample(args.L, args.m, budget_s=15.0)
         except Exception as e:  # the baseline must not hide the GPU line
             cpu = {"error": str(e)}
 

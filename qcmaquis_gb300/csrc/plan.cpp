@@ -29,6 +29,11 @@
 
 namespace qcm {
 
+// Whether the K2 dense groups and K3 read their A operands directly from the
+// FP32 sources and split them inside the block-product kernel (true), or from
+// images built by a separate pass (false).
+static constexpr bool kSplitA = false;
+
 static thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
 
@@ -678,9 +683,9 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
     P->scratch[0] = rp_end;
     P->scratch[1] = std::max(t_end, part_end);
     P->scratch[2] = c_end;
-    build_image_tables(s1, s1.img);
-    build_image_tables(s3, s3.img);
-    build_dense_groups(s2, 64, s2.img, s2.heavy);
+    build_image_tables(s1, s1.img, false);
+    build_image_tables(s3, s3.img, kSplitA);
+    build_dense_groups(s2, 64, s2.img, s2.heavy, kSplitA);
     P->image_bytes = std::max(std::max(s1.img.bytes, s3.img.bytes), s2.img.bytes);
     P->stages.push_back(std::move(z0));
     P->stages.push_back(std::move(s0));
@@ -981,7 +986,7 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
 // the MMA with the larger of (M, N) on the 128-row MMA side: when N > M the
 // stage's C = op(A) op(B) is computed as C^T = op(B)^T op(A)^T.  Panels that
 // several segments read with the same orientation share one image.
-void build_image_tables(const Stage& st, ImgTables& t) {
+void build_image_tables(const Stage& st, ImgTables& t, bool split_a) {
     t = ImgTables();
     struct Key {
         int32_t buf, ld, R, K, kc;
@@ -999,10 +1004,22 @@ void build_image_tables(const Stage& st, ImgTables& t) {
         }
     };
     std::unordered_map<Key, int32_t, KeyHash> ids;
-    auto panel = [&](int32_t buf, int64_t off, int64_t ld, int kcontig, int64_t R, int64_t K) -> int32_t {
+    // a panel gets an image (and image-builder work) the first time a segment reads it from one
+    auto give_image = [&](int32_t id) {
+        ImgPanel& p = t.panels[id];
+        if (p.img_off >= 0) return;
+        p.img_off = t.bytes;
+        const int64_t kc = (p.K + 31) / 32;
+        t.bytes += kc * 3 * (int64_t)p.G * 512;
+        for (int64_t c = 0; c < kc; ++c) { t.build.push_back(id); t.build.push_back((int32_t)c); }
+    };
+    auto panel = [&](int32_t buf, int64_t off, int64_t ld, int kcontig, int64_t R, int64_t K, bool image) -> int32_t {
         Key k{buf, (int32_t)ld, (int32_t)R, (int32_t)K, kcontig, off};
         auto it = ids.find(k);
-        if (it != ids.end()) return it->second;
+        if (it != ids.end()) {
+            if (image) give_image(it->second);
+            return it->second;
+        }
         ImgPanel p;
         p.src_off = off;
         p.src_buf = buf;
@@ -1011,13 +1028,11 @@ void build_image_tables(const Stage& st, ImgTables& t) {
         p.K = (int32_t)K;
         p.kcontig = kcontig;
         p.G = (int32_t)((R + 7) / 8);
-        p.img_off = t.bytes;
-        const int64_t kc = (K + 31) / 32;
-        t.bytes += kc * 3 * (int64_t)p.G * 512;
+        p.img_off = -1;
         const int32_t id = (int32_t)t.panels.size();
-        for (int64_t c = 0; c < kc; ++c) { t.build.push_back(id); t.build.push_back((int32_t)c); }
         t.panels.push_back(p);
         ids.emplace(k, id);
+        if (image) give_image(id);
         return id;
     };
     for (const GemmOut& o : st.gout) {
@@ -1044,19 +1059,22 @@ void build_image_tables(const Stage& st, ImgTables& t) {
             if (g.lda > 0x7fffffff || g.ldb > 0x7fffffff || g.K > 0x7fffffff)
                 throw std::runtime_error("image executor: block too large");
             // op(A): rows m, element (m,k) at ta ? k + m*lda : m + k*lda
-            const int32_t pa = panel(g.a_buf, g.a_off, g.lda, g.ta ? 1 : 0, o.M, g.K);
             // op(B)^T: rows n, element (n,k) = op(B)(k,n) at tb ? n + k*ldb : k + n*ldb
-            const int32_t pb = panel(g.b_buf, g.b_off, g.ldb, g.tb ? 0 : 1, o.N, g.K);
-            const ImgPanel& A = t.panels[tr ? pb : pa];
-            const ImgPanel& B = t.panels[tr ? pa : pb];
+            const int32_t pa = panel(g.a_buf, g.a_off, g.lda, g.ta ? 1 : 0, o.M, g.K, tr || !split_a);
+            const int32_t pb = panel(g.b_buf, g.b_off, g.ldb, g.tb ? 0 : 1, o.N, g.K, !tr || !split_a);
+            const int32_t ia = tr ? pb : pa, ib = tr ? pa : pb;
+            const ImgPanel& A = t.panels[ia];
+            const ImgPanel& B = t.panels[ib];
             ImgSeg s;
-            s.a_img = A.img_off;
+            s.a_img = split_a ? 0 : A.img_off;
             s.b_img = B.img_off;
             s.a_G = A.G;
             s.b_G = B.G;
             s.kc = (int32_t)((g.K + 31) / 32);
             s.alpha = (float)g.alpha;
-            s.flags = 0;
+            s.flags = split_a ? IMG_A_SPLIT : 0;
+            s.a_panel = ia;
+            s.a_c0 = 0;
             s.pad = 0;
             t.segs.push_back(s);
         }
@@ -1091,7 +1109,7 @@ static float bf16_to_float(uint16_t h) {
     return x;
 }
 
-void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::vector<char>& heavy) {
+void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::vector<char>& heavy, bool split_a) {
     t = ImgTables();
     const size_t nO = st.aout.size();
     heavy.assign(nO, 0);
@@ -1118,8 +1136,8 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
             }
         }
     }
-    // candidate groups: (component, rows, cols, ldd, dst_buf, src_buf) over heavy outputs
-    std::map<std::tuple<int32_t, int64_t, int64_t, int64_t, int32_t, int32_t>, std::vector<int32_t>> groups;
+    // candidate groups: (component, rows, cols, dst_buf, src_buf) over heavy outputs
+    std::map<std::tuple<int32_t, int64_t, int64_t, int32_t, int32_t>, std::vector<int32_t>> groups;
     for (size_t i = 0; i < nO; ++i) {
         const AxpyOut& a = st.aout[i];
         if (a.t_end - a.t_begin < min_terms || a.rows * a.cols <= 0) continue;
@@ -1127,14 +1145,15 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         bool uniform = true;
         for (int64_t k = a.t_begin; k < a.t_end; ++k) uniform &= st.aterm[k].src_buf == sb;
         if (!uniform) continue;
-        groups[std::make_tuple(find((int32_t)i), a.rows, a.cols, a.ldd, a.dst_buf, sb)].push_back((int32_t)i);
+        if (a.ldd > 0x7fffffffLL) continue;
+        groups[std::make_tuple(find((int32_t)i), a.rows, a.cols, a.dst_buf, sb)].push_back((int32_t)i);
     }
     for (auto& kv : groups) {
         const std::vector<int32_t>& O = kv.second;
-        const int64_t rows = std::get<1>(kv.first), cols = std::get<2>(kv.first), ldd = std::get<3>(kv.first);
-        const int32_t dst_buf = std::get<4>(kv.first), src_buf = std::get<5>(kv.first);
+        const int64_t rows = std::get<1>(kv.first), cols = std::get<2>(kv.first);
+        const int32_t dst_buf = std::get<3>(kv.first), src_buf = std::get<4>(kv.first);
         const int64_t E = rows * cols;
-        if (E > 0x7fffffffLL || ldd > 0x7fffffffLL || O.size() < 8) continue;
+        if (E > 0x7fffffffLL || O.size() < 8) continue;
         std::unordered_map<int64_t, int32_t> sid;
         std::vector<int64_t> srcs;
         int64_t nterms = 0;
@@ -1150,7 +1169,7 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         // A: gathered source tiles, rows e, K = source index
         ImgPanel pa;
         pa.src_off = (int64_t)t.gather.size();
-        pa.img_off = t.bytes;
+        pa.img_off = split_a ? -1 : t.bytes;
         pa.src_buf = src_buf;
         pa.ld = 0;
         pa.R = (int32_t)E;
@@ -1158,9 +1177,11 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         pa.kcontig = 2;
         pa.G = G;
         t.gather.insert(t.gather.end(), srcs.begin(), srcs.end());
-        t.bytes += KC * 3 * (int64_t)G * 512;
         const int32_t pid = (int32_t)t.panels.size();
-        for (int64_t c = 0; c < KC; ++c) { t.build.push_back(pid); t.build.push_back((int32_t)c); }
+        if (!split_a) {
+            t.bytes += KC * 3 * (int64_t)G * 512;
+            for (int64_t c = 0; c < KC; ++c) { t.build.push_back(pid); t.build.push_back((int32_t)c); }
+        }
         t.panels.push_back(pa);
         // B: coefficient matrix W (rows = outputs, K = sources), split on the host
         std::vector<float> W((size_t)O.size() * S, 0.0f);
@@ -1193,29 +1214,34 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         // output: column j is output tile O[j]
         ImgOut io;
         io.c_off = 0;
-        io.si = ldd;
+        io.si = 0;
         io.sj = 0;
-        io.ctab = (int64_t)t.coltab.size();
+        io.ctab = (int64_t)t.coltab.size() / 2;
         io.c_buf = dst_buf;
         io.mrows = (int32_t)E;
         io.ncols = (int32_t)O.size();
         io.mode = 1;
         io.rows = (int32_t)rows;
         io.pad = 0;
-        for (int32_t o : O) t.coltab.push_back(st.aout[o].dst_off);
+        for (int32_t o : O) {
+            t.coltab.push_back(st.aout[o].dst_off);
+            t.coltab.push_back(st.aout[o].ldd);
+        }
         const int32_t oid = (int32_t)t.outs.size();
         t.outs.push_back(io);
         // segments: 4 K-chunks (128 sources) per drain of the accumulator
         const int32_t s_begin = (int32_t)t.segs.size();
         for (int64_t c0 = 0; c0 < KC; c0 += 4) {
             ImgSeg sg;
-            sg.a_img = pa.img_off + c0 * 3 * (int64_t)G * 512;
+            sg.a_img = split_a ? 0 : pa.img_off + c0 * 3 * (int64_t)G * 512;
             sg.b_img = b_off + c0 * 3 * (int64_t)Gb * 512;
             sg.a_G = G;
             sg.b_G = Gb;
             sg.kc = (int32_t)std::min<int64_t>(4, KC - c0);
             sg.alpha = 1.0f;
-            sg.flags = IMG_B_CONST;
+            sg.flags = (split_a ? IMG_A_SPLIT : 0) | IMG_B_CONST;
+            sg.a_panel = pid;
+            sg.a_c0 = (int32_t)c0;
             sg.pad = 0;
             t.segs.push_back(sg);
         }
@@ -1328,8 +1354,8 @@ int qcm_plan_stage_images(const qcm_plan* p, int32_t stage, int64_t* counts, int
     if (sd)
         for (size_t i = 0; i < t.segs.size(); ++i) {
             const ImgSeg& x = t.segs[i];
-            const int64_t v[6] = {x.a_img, x.b_img, x.a_G, x.b_G, x.kc, x.flags};
-            for (int j = 0; j < 6; ++j) sd[6 * i + j] = v[j];
+            const int64_t v[8] = {x.a_img, x.b_img, x.a_G, x.b_G, x.kc, x.flags, x.a_panel, x.a_c0};
+            for (int j = 0; j < 8; ++j) sd[8 * i + j] = v[j];
             if (sa) sa[i] = x.alpha;
         }
     if (td)

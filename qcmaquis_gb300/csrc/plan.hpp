@@ -111,17 +111,21 @@ struct ImgPanel {
 };
 // One output of the image executor, tile element (i, j) with i along the MMA
 // M side and j along N: mode 0 writes c_off + i*si + j*sj; mode 1 writes
-// coltab[ctab + j] + (i % rows) + (i / rows)*si (column j is one output tile).
+// off_j + (i % rows) + (i / rows)*ld_j with (off_j, ld_j) = coltab pair
+// ctab + j (column j is one output tile).
 struct ImgOut {
     int64_t c_off, si, sj, ctab;
     int32_t c_buf, mrows, ncols, mode, rows, pad;
 };
-enum { IMG_B_CONST = 2 };   // ImgSeg.flags: the B image lives in the plan's constant images
+// ImgSeg.flags: IMG_A_SPLIT -- the A operand is read from its source panel
+// (a_panel, chunks from a_c0) and split inside the block-product kernel;
+// IMG_B_CONST -- the B image lives in the plan's constant images.
+enum { IMG_A_SPLIT = 1, IMG_B_CONST = 2 };
 struct ImgSeg {
     int64_t a_img, b_img;   // byte offsets of the A and B panel images (at the chunk range start)
     int32_t a_G, b_G, kc;   // row groups of the panels, K-chunks
     float alpha;
-    int32_t flags, pad;
+    int32_t flags, a_panel, a_c0, pad;
 };
 struct ImgUnit {
     int32_t out, m0, n0, nt, s_begin, s_end;  // nt: MMA N (multiple of 16, <= 128)
@@ -133,17 +137,19 @@ struct ImgTables {
     std::vector<ImgSeg> segs;
     std::vector<ImgUnit> units;
     std::vector<int64_t> gather;  // source offsets of gathered panels (kcontig 2)
-    std::vector<int64_t> coltab;  // output-tile offsets of mode-1 outputs
+    std::vector<int64_t> coltab;  // (offset, ld) pairs of the output tiles of mode-1 outputs
     std::vector<uint8_t> cimg;    // constant images (coefficient matrices), built by the plan
     int64_t bytes = 0;            // per-call image bytes
 };
-void build_image_tables(const struct Stage& st, ImgTables& t);
+// split_a: A operands are split inside the block-product kernel (no A image)
+void build_image_tables(const struct Stage& st, ImgTables& t, bool split_a = false);
 // Dense groups of a gather-axpy stage: output tiles that share their sources
 // (a connected component of the output/source graph), have at least
 // min_terms terms and one tile shape become one block product
 // contr[:, group] = T_gathered . W^T on the tensor cores.  heavy[o] marks the
 // outputs taken.
-void build_dense_groups(const struct Stage& st, int64_t min_terms, ImgTables& t, std::vector<char>& heavy);
+void build_dense_groups(const struct Stage& st, int64_t min_terms, ImgTables& t, std::vector<char>& heavy,
+                        bool split_a);
 
 struct Stage {
     int kind;

@@ -108,22 +108,22 @@ __device__ __forceinline__ void put_vec(uint8_t* base, uint32_t off, uint32_t sl
         q.x = to_tf32(v[0]); q.y = to_tf32(v[1]); q.z = to_tf32(v[2]); q.w = to_tf32(v[3]);
         *reinterpret_cast<uint4*>(base + off) = q;
     } else {
+        // pairs of values are rounded together (one packed bf16x2 conversion);
+        // each slice takes the round-to-nearest BF16 of what the previous ones left
         uint32_t s0[4], s1[4], s2[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            __nv_bfloat16 h[3][2];
-#pragma unroll
-            for (int j = 0; j < 2; ++j) {
-                const float x = v[2 * i + j];
-                h[0][j] = __float2bfloat16_rn(x);
-                const float r1 = x - __bfloat162float(h[0][j]);
-                h[1][j] = __float2bfloat16_rn(r1);
-                const float r2 = r1 - __bfloat162float(h[1][j]);
-                h[2][j] = __float2bfloat16_rn(r2);
-            }
-            s0[i] = (uint32_t)__bfloat16_as_ushort(h[0][0]) | ((uint32_t)__bfloat16_as_ushort(h[0][1]) << 16);
-            s1[i] = (uint32_t)__bfloat16_as_ushort(h[1][0]) | ((uint32_t)__bfloat16_as_ushort(h[1][1]) << 16);
-            s2[i] = (uint32_t)__bfloat16_as_ushort(h[2][0]) | ((uint32_t)__bfloat16_as_ushort(h[2][1]) << 16);
+            const float2 x = make_float2(v[2 * i], v[2 * i + 1]);
+            const __nv_bfloat162 h0 = __float22bfloat162_rn(x);
+            const float2 f0 = __bfloat1622float2(h0);
+            const float2 r1 = make_float2(x.x - f0.x, x.y - f0.y);
+            const __nv_bfloat162 h1 = __float22bfloat162_rn(r1);
+            const float2 f1 = __bfloat1622float2(h1);
+            const float2 r2 = make_float2(r1.x - f1.x, r1.y - f1.y);
+            const __nv_bfloat162 h2 = __float22bfloat162_rn(r2);
+            s0[i] = *reinterpret_cast<const uint32_t*>(&h0);
+            s1[i] = *reinterpret_cast<const uint32_t*>(&h1);
+            s2[i] = *reinterpret_cast<const uint32_t*>(&h2);
         }
         *reinterpret_cast<uint4*>(base + off) = make_uint4(s0[0], s0[1], s0[2], s0[3]);
         *reinterpret_cast<uint4*>(base + slice_bytes + off) = make_uint4(s1[0], s1[1], s1[2], s1[3]);
@@ -403,21 +403,29 @@ int tc_launch(const void* d_out, const void* d_seg, const void* d_work, int64_t 
 // TMEM accumulators, and warps 2..9 drain each finished segment (one block
 // product of the split-K sum) into compensated FP32 register sums, scaled by
 // the segment's coefficient, and store the tile once.
-constexpr int TI_NS = 4;
-constexpr int TI_THREADS = 320;
+constexpr int TI_NS = 4;                        // shared-memory stages (at most)
+constexpr int TI_NS_SPLIT = 3;                  // stages when A operands are split in the kernel ...
+constexpr int TI_RS = 3;                        // ... which also use this many raw FP32 A chunks
+constexpr uint32_t TI_RAW = 128 * 32 * 4;       // one raw FP32 A chunk (128 rows x 32 K)
+constexpr int TI_AWARPS = 4;                    // A-split producer warps
+constexpr int TI_THREADS = (10 + TI_AWARPS) * 32;
 constexpr uint32_t TI_SLICE = 16 * 512;         // one slice of a 128-row x 64-byte chunk
 constexpr uint32_t TI_STAGE = 6 * TI_SLICE;     // A and B, three slices each
 constexpr int TI_EPI_LD = 17;                   // epilogue staging row stride (floats)
+static_assert(TI_NS_SPLIT * TI_STAGE + TI_RS * TI_RAW <= TI_NS * TI_STAGE, "raw ring must fit in the stage area");
 constexpr uint32_t TI_SMEM = TI_NS * TI_STAGE + 8 * 32 * TI_EPI_LD * 4 + 1024;
 constexpr uint64_t TI_WAIT_NS = 4000000000ull;  // a wait that lasts this long gives up
 
 struct TiArgs {
+    int32_t ns;               // shared-memory stages in use (TI_NS, or TI_NS_SPLIT with the raw ring)
     const ImgUnit* units;
     const ImgSeg* segs;
     const ImgOut* outs;
+    const ImgPanel* panels;   // A panels of split segments
+    const int64_t* gather;    // source offsets of gathered panels
     const uint8_t* img;
     const uint8_t* cimg;      // constant images of the plan (coefficient matrices)
-    const int64_t* coltab;    // output-tile offsets of mode-1 outputs
+    const int64_t* coltab;    // (offset, ld) pairs of the output tiles of mode-1 outputs
     double* p[QCM_NBUF];
     uint32_t f32mask;
     int32_t n_units;
@@ -513,10 +521,226 @@ build_images_kernel(const ImgPanel* __restrict__ panels, const int32_t* __restri
     }
 }
 
+// This CTA's tiles u = blockIdx.x, blockIdx.x + gridDim.x, ... with the
+// descriptors of the next two tiles and of the next tile's first segment
+// requested ahead of use, so that no role stalls on a chain of dependent
+// global loads at a tile boundary (most K1 tiles have a single short segment).
+struct TiCursor {
+    const ImgUnit* units;
+    const ImgSeg* segs;
+    int n, g, u;
+    ImgUnit cur, nxt, nn;
+    ImgSeg first_cur, first_nxt;
+
+    __device__ static ImgUnit no_unit() {
+        ImgUnit e;
+        e.out = 0; e.m0 = 0; e.n0 = 0; e.nt = 16; e.s_begin = 0; e.s_end = 0;
+        return e;
+    }
+    __device__ static ImgSeg no_seg() {
+        ImgSeg z;
+        z.a_img = 0; z.b_img = 0; z.a_G = 1; z.b_G = 1; z.kc = 0; z.alpha = 0.0f; z.flags = 0;
+        z.a_panel = 0; z.a_c0 = 0; z.pad = 0;
+        return z;
+    }
+    __device__ ImgUnit at(int x) const { return x < n ? units[x] : no_unit(); }
+    __device__ ImgSeg seg(int s, int e) const { return s < e ? segs[s] : no_seg(); }
+    __device__ void init(const TiArgs& a) {
+        units = a.units; segs = a.segs; n = a.n_units; g = gridDim.x; u = blockIdx.x;
+        cur = at(u);
+        nxt = at(u + g);
+        first_cur = seg(cur.s_begin, cur.s_end);
+    }
+    __device__ bool valid() const { return u < n; }
+    __device__ void prefetch() {
+        nn = at(u + 2 * g);
+        first_nxt = seg(nxt.s_begin, nxt.s_end);
+    }
+    __device__ void advance() {
+        u += g; cur = nxt; nxt = nn; first_cur = first_nxt;
+    }
+};
+
+// TMEM columns of one CTA: two accumulators (segments alternate), then the
+// compensated running sum (hi, lo) of the tile.
+constexpr uint32_t TI_TMEM_COLS = 512;
+constexpr uint32_t TI_COL_HI = 256, TI_COL_LO = 384;
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+        :: "r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+           "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+        : "memory");
+}
+
+// Store 16 finished columns (c0 .. c0+15 of the tile) of this lane's row.
+__device__ __forceinline__ void ti_store16(const TiArgs& a, const ImgOut& O, const ImgUnit& U, int i0, int lane,
+                                           int cbase, const float (&hi)[16], const float (&lo)[16], float* stg) {
+    const bool c32 = (a.f32mask >> O.c_buf) & 1u;
+    float* __restrict__ C32 = (float*)a.p[O.c_buf] + O.c_off;
+    double* __restrict__ C64 = a.p[O.c_buf] + O.c_off;
+    if (O.mode == 1) {
+        // column j is one output tile: element i at (i % rows) + (i / rows)*ld_j of it
+        const int i = i0 + lane;
+        const int64_t ir = i % O.rows, ic = i / O.rows;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int col = U.n0 + cbase + j;
+            if (i < O.mrows && col < O.ncols) {
+                const int64_t off = __ldg(a.coltab + 2 * (O.ctab + col)) + ir + ic * __ldg(a.coltab + 2 * (O.ctab + col) + 1);
+                if (c32) ((float*)a.p[O.c_buf])[off] = hi[j] + lo[j];
+                else a.p[O.c_buf][off] = (double)hi[j] + (double)lo[j];
+            }
+        }
+    } else if (O.si == 1) {
+        // lanes hold consecutive rows i: each column store is coalesced
+        const int i = i0 + lane;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int col = U.n0 + cbase + j;
+            if (i < O.mrows && col < O.ncols) {
+                const int64_t off = (int64_t)i + (int64_t)col * O.sj;
+                if (c32) C32[off] = hi[j] + lo[j];
+                else C64[off] = (double)hi[j] + (double)lo[j];
+            }
+        }
+    } else {
+        // rows i lie O.si apart in memory and columns are contiguous: pass the
+        // 32 x 16 block through shared memory so that 16 lanes store one row run
+#pragma unroll
+        for (int j = 0; j < 16; ++j) stg[lane * TI_EPI_LD + j] = hi[j] + lo[j];
+        __syncwarp();
+        const int jj = lane & 15;
+        const int col = U.n0 + cbase + jj;
+        for (int rr = lane >> 4; rr < 32; rr += 2) {
+            const int i = i0 + rr;
+            if (i < O.mrows && col < O.ncols) {
+                const int64_t off = (int64_t)i * O.si + col;
+                const float v = stg[rr * TI_EPI_LD + jj];
+                if (c32) C32[off] = v;
+                else C64[off] = (double)v;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Element (r, k) of an operand panel (FP32 or FP64 source), 0 outside it.
+__device__ __forceinline__ float panel_elem(const TiArgs& a, const ImgPanel& P, bool f32, int r, int k) {
+    if (r >= P.R || k >= P.K) return 0.0f;
+    int64_t ix;
+    if (P.kcontig == 2) ix = __ldg(a.gather + P.src_off + k) + r;
+    else ix = P.src_off + (P.kcontig ? (int64_t)r * P.ld + k : (int64_t)r + (int64_t)k * P.ld);
+    return f32 ? __ldg((const float*)a.p[P.src_buf] + ix) : (float)__ldg(a.p[P.src_buf] + ix);
+}
+
+// Position in this CTA's chunk sequence (tile u, segment s, K-chunk c) with
+// the descriptors the A-split producers need.
+struct ChunkIt {
+    int u, s, c;
+    ImgUnit U;
+    ImgSeg S;
+    ImgPanel P;
+    bool valid;
+
+    __device__ void load_seg(const TiArgs& a) {
+        S = a.segs[s];
+        if (S.flags & IMG_A_SPLIT) P = a.panels[S.a_panel];
+    }
+    // move to the first chunk at or after (u, s, c)
+    __device__ void settle(const TiArgs& a) {
+        for (;;) {
+            if (s < U.s_end) {
+                if (c < S.kc) { valid = true; return; }
+                ++s;
+                c = 0;
+                if (s < U.s_end) load_seg(a);
+                continue;
+            }
+            u += gridDim.x;
+            if (u >= a.n_units) { valid = false; return; }
+            U = a.units[u];
+            s = U.s_begin;
+            c = 0;
+            if (s < U.s_end) load_seg(a);
+        }
+    }
+    __device__ void init(const TiArgs& a) {
+        u = blockIdx.x;
+        valid = u < a.n_units;
+        if (!valid) return;
+        U = a.units[u];
+        s = U.s_begin;
+        c = 0;
+        if (s < U.s_end) load_seg(a);
+        settle(a);
+    }
+    __device__ void next(const TiArgs& a) {
+        ++c;
+        settle(a);
+    }
+};
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" :: "r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+// Request row r of the split A chunk at `it` into a raw ring slot ([k][128]
+// floats): asynchronous copies of the FP32 source, plain stores of zeros
+// outside the panel (FP64 sources are converted with plain loads).
+__device__ __forceinline__ void ti_request_raw(const TiArgs& a, const ChunkIt& it, int r, float* raw) {
+    if (!(it.S.flags & IMG_A_SPLIT)) return;
+    const ImgPanel& P = it.P;
+    const int row = it.U.m0 + r;
+    const int kb = (it.S.a_c0 + it.c) * 32;
+    const bool f32 = (a.f32mask >> P.src_buf) & 1u;
+    const float* S32 = (const float*)a.p[P.src_buf];
+    const double* S64 = a.p[P.src_buf];
+    if (row >= P.R) {
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) raw[k * 128 + r] = 0.0f;
+        return;
+    }
+    if (P.kcontig == 2) {
+#pragma unroll
+        for (int k0 = 0; k0 < 32; k0 += 8) {
+            int64_t g[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) g[j] = (kb + k0 + j < P.K) ? __ldg(a.gather + P.src_off + kb + k0 + j) : -1;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                float* d = raw + (k0 + j) * 128 + r;
+                if (g[j] < 0) *d = 0.0f;
+                else if (f32) cp_async4(d, S32 + g[j] + row);
+                else *d = (float)__ldg(S64 + g[j] + row);
+            }
+        }
+    } else {
+        const int64_t base = P.src_off + (P.kcontig ? (int64_t)row * P.ld : (int64_t)row);
+        const int64_t step = P.kcontig ? 1 : P.ld;
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) {
+            float* d = raw + k * 128 + r;
+            if (kb + k >= P.K) *d = 0.0f;
+            else if (f32) cp_async4(d, S32 + base + (int64_t)(kb + k) * step);
+            else *d = (float)__ldg(S64 + base + (int64_t)(kb + k) * step);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
     extern __shared__ uint8_t ti_smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)ti_smem_raw + 1023) & ~(uintptr_t)1023);
-    float* epi = (float*)(smem + TI_NS * TI_STAGE);
+    float* epi = (float*)(smem + TI_NS * TI_STAGE);   // after the stages (and the raw ring)
     __shared__ __align__(8) uint64_t bar_full[TI_NS], bar_empty[TI_NS], bar_accf[2], bar_acce[2], bar_fin;
     __shared__ uint32_t tmem_sh;
     __shared__ int abort_sh;
@@ -525,12 +749,13 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     :: "r"(smem_u32(&tmem_sh)), "r"(256u));
+                     :: "r"(smem_u32(&tmem_sh)), "r"(TI_TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 32) {
         for (int i = 0; i < TI_NS; ++i) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bar_full[i])));
+            // full: the bulk-copy producer's arrive (with its transaction bytes) + the A-split warps
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_full[i])), "r"(1 + TI_AWARPS));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bar_empty[i])));
         }
         for (int i = 0; i < 2; ++i) {
@@ -548,27 +773,34 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
 
     if (warp == 0) {
         if (lane == 0) {
-            // ---------------- producer
+            // ---------------- bulk-copy producer: B always, A when it comes from an image
             uint32_t it = 0;
             bool ok = true;
-            for (int u = blockIdx.x; u < a.n_units && ok; u += gridDim.x) {
-                const ImgUnit U = a.units[u];
+            TiCursor cu;
+            cu.init(a);
+            for (; cu.valid() && ok; cu.advance()) {
+                cu.prefetch();
+                const ImgUnit U = cu.cur;
                 const int gA0 = U.m0 >> 3, gB0 = U.n0 >> 3;
+                ImgSeg Sn = cu.first_cur;
                 for (int s = U.s_begin; s < U.s_end && ok; ++s) {
-                    const ImgSeg S = a.segs[s];
+                    const ImgSeg S = Sn;
+                    if (s + 1 < U.s_end) Sn = a.segs[s + 1];
+                    const bool a_img = !(S.flags & IMG_A_SPLIT);
                     const uint8_t* bbase = (S.flags & IMG_B_CONST) ? a.cimg : a.img;
-                    const uint32_t bA = (uint32_t)min(16, S.a_G - gA0) * 512u;
+                    const uint32_t bA = a_img ? (uint32_t)min(16, S.a_G - gA0) * 512u : 0u;
                     const uint32_t bB = (uint32_t)min(U.nt >> 3, S.b_G - gB0) * 512u;
                     for (int c = 0; c < S.kc; ++c, ++it) {
-                        const uint32_t st = it % TI_NS, ph = (it / TI_NS) & 1u;
+                        const uint32_t st = it % (uint32_t)a.ns, ph = (it / (uint32_t)a.ns) & 1u;
                         if (!ti_wait(smem_u32(&bar_empty[st]), ph ^ 1u, abort_flag)) { ok = false; break; }
                         const uint32_t fb = smem_u32(&bar_full[st]);
                         mbar_expect_tx(fb, 3u * (bA + bB));
                         const uint32_t dst = smem_u32(smem + st * TI_STAGE);
 #pragma unroll
                         for (int sl = 0; sl < 3; ++sl) {
-                            bulk_g2s(dst + sl * TI_SLICE,
-                                     a.img + S.a_img + ((int64_t)(c * 3 + sl) * S.a_G + gA0) * 512, bA, fb);
+                            if (a_img)
+                                bulk_g2s(dst + sl * TI_SLICE,
+                                         a.img + S.a_img + ((int64_t)(c * 3 + sl) * S.a_G + gA0) * 512, bA, fb);
                             bulk_g2s(dst + (3 + sl) * TI_SLICE,
                                      bbase + S.b_img + ((int64_t)(c * 3 + sl) * S.b_G + gB0) * 512, bB, fb);
                         }
@@ -577,9 +809,10 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
             }
             if (!ok) { *abort_flag = 1; atomicExch(&g_tc_status, 2); }
             // the copies of every stage's latest round must have landed before the CTA exits
-            for (uint32_t k = 0; k < (uint32_t)TI_NS && k < it; ++k) {
+            for (uint32_t k = 0; k < (uint32_t)a.ns && k < it; ++k) {
                 const uint32_t j = it - 1 - k;
-                if (!ti_wait(smem_u32(&bar_full[j % TI_NS]), (j / TI_NS) & 1u, nullptr)) atomicExch(&g_tc_status, 2);
+                if (!ti_wait(smem_u32(&bar_full[j % (uint32_t)a.ns]), (j / (uint32_t)a.ns) & 1u, nullptr))
+                    atomicExch(&g_tc_status, 2);
             }
         }
     } else if (warp == 1) {
@@ -587,17 +820,22 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
             // ---------------- MMA issuer
             uint32_t it = 0, sc = 0;
             bool ok = true;
-            for (int u = blockIdx.x; u < a.n_units && ok; u += gridDim.x) {
-                const ImgUnit U = a.units[u];
+            TiCursor cu;
+            cu.init(a);
+            for (; cu.valid() && ok; cu.advance()) {
+                cu.prefetch();
+                const ImgUnit U = cu.cur;
                 const uint32_t idesc = make_idesc(1u, TC_BM, U.nt);
+                int kcn = cu.first_cur.kc;
                 for (int s = U.s_begin; s < U.s_end && ok; ++s) {
-                    const int kc = a.segs[s].kc;
+                    const int kc = kcn;
+                    if (s + 1 < U.s_end) kcn = a.segs[s + 1].kc;
                     const uint32_t b = sc & 1u;
                     if (!ti_wait(smem_u32(&bar_acce[b]), ((sc >> 1) & 1u) ^ 1u, abort_flag)) { ok = false; break; }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t d = tmem + b * 128u;
                     for (int c = 0; c < kc; ++c, ++it) {
-                        const uint32_t st = it % TI_NS, ph = (it / TI_NS) & 1u;
+                        const uint32_t st = it % (uint32_t)a.ns, ph = (it / (uint32_t)a.ns) & 1u;
                         if (!ti_wait(smem_u32(&bar_full[st]), ph, abort_flag)) { ok = false; break; }
                         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                         const uint32_t a0 = smem_u32(smem + st * TI_STAGE), b0 = a0 + 3 * TI_SLICE;
@@ -628,119 +866,137 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
             mma_commit(smem_u32(&bar_fin));
             if (!ti_wait(smem_u32(&bar_fin), 0u, nullptr)) atomicExch(&g_tc_status, 2);
         }
-    } else {
+    } else if (warp < 10) {
         // ---------------- epilogue: warps 2..9; TMEM lanes 32*(warp%4).., columns 64*h..
+        // Each finished segment is scaled by its coefficient and added into the
+        // tile's compensated FP32 sum (Knuth two-sum; hi and lo kept in TMEM).
         const int e = warp - 2, q = warp & 3, h = e >> 2;
         float* stg = epi + e * 32 * TI_EPI_LD;
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 64);
         uint32_t sc = 0;
         bool ok = true;
-        for (int u = blockIdx.x; u < a.n_units && ok; u += gridDim.x) {
-            const ImgUnit U = a.units[u];
-            const ImgOut O = a.outs[U.out];
+        TiCursor cu;
+        cu.init(a);
+        ImgOut On = a.outs[cu.cur.out];
+        for (; cu.valid() && ok; cu.advance()) {
+            cu.prefetch();
+            const ImgUnit U = cu.cur;
+            const ImgOut O = On;
+            On = a.outs[cu.nxt.out];   // the next tile's output descriptor, ahead of use
             const int ncw = max(0, min(64, U.nt - h * 64));
-            float hi[64], lo[64];
+            const int i0 = U.m0 + q * 32;
+            float alpha_n = cu.first_cur.alpha;
+            if (U.s_begin == U.s_end) {
+                // no segment: the tile is zero
+                float z[16];
 #pragma unroll
-            for (int j = 0; j < 64; ++j) { hi[j] = 0.0f; lo[j] = 0.0f; }
+                for (int j = 0; j < 16; ++j) z[j] = 0.0f;
+                for (int c16 = 0; c16 < 4; ++c16)
+                    if (c16 * 16 < ncw) ti_store16(a, O, U, i0, lane, h * 64 + c16 * 16, z, z, stg);
+                continue;
+            }
             for (int s = U.s_begin; s < U.s_end; ++s) {
-                const float alpha = a.segs[s].alpha;
+                const float alpha = alpha_n;
+                if (s + 1 < U.s_end) alpha_n = a.segs[s + 1].alpha;
+                const bool first = s == U.s_begin, last = s + 1 == U.s_end;
                 const uint32_t b = sc & 1u;
                 ok = __all_sync(0xffffffffu, ti_wait(smem_u32(&bar_accf[b]), (sc >> 1) & 1u, abort_flag));
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * 128u + (uint32_t)(h * 64);
-#pragma unroll
+#pragma unroll 1
                 for (int c16 = 0; c16 < 4; ++c16) {
-                    if (c16 * 16 < ncw) {
-                        uint32_t r[16];
-                        asm volatile(
-                            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                              "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                              "=r"(r[14]), "=r"(r[15])
-                            : "r"(taddr + (uint32_t)(c16 * 16)));
+                    if (c16 * 16 >= ncw) break;
+                    const uint32_t col = (uint32_t)(c16 * 16);
+                    uint32_t r[16];
+                    tmem_ld16(lane_base + b * 128u + col, r);
+                    float hi[16], lo[16];
+                    if (first) {
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) { hi[j] = alpha * __uint_as_float(r[j]); lo[j] = 0.0f; }
+                    } else {
+                        uint32_t rh[16], rl[16];
+                        tmem_ld16(lane_base + TI_COL_HI + col, rh);
+                        tmem_ld16(lane_base + TI_COL_LO + col, rl);
                         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
                         for (int j = 0; j < 16; ++j) {
                             const float x = alpha * __uint_as_float(r[j]);
-                            const float t = hi[c16 * 16 + j] + x;  // Knuth two-sum
-                            const float bp = t - hi[c16 * 16 + j];
-                            const float err = (hi[c16 * 16 + j] - (t - bp)) + (x - bp);
-                            hi[c16 * 16 + j] = t;
-                            lo[c16 * 16 + j] += err;
+                            const float hh = __uint_as_float(rh[j]);
+                            const float t = hh + x;  // Knuth two-sum
+                            const float bp = t - hh;
+                            const float err = (hh - (t - bp)) + (x - bp);
+                            hi[j] = t;
+                            lo[j] = __uint_as_float(rl[j]) + err;
                         }
                     }
+                    if (last) {
+                        ti_store16(a, O, U, i0, lane, h * 64 + c16 * 16, hi, lo, stg);
+                    } else {
+                        uint32_t wh[16], wl[16];
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) { wh[j] = __float_as_uint(hi[j]); wl[j] = __float_as_uint(lo[j]); }
+                        tmem_st16(lane_base + TI_COL_HI + col, wh);
+                        tmem_st16(lane_base + TI_COL_LO + col, wl);
+                    }
                 }
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(&bar_acce[b]));
                 ++sc;
             }
-            if (!ok) break;
-            const bool c32 = (a.f32mask >> O.c_buf) & 1u;
-            float* __restrict__ C32 = (float*)a.p[O.c_buf] + O.c_off;
-            double* __restrict__ C64 = a.p[O.c_buf] + O.c_off;
-            const int i0 = U.m0 + q * 32;
-            if (O.mode == 1) {
-                // column j is one output tile: element i at (i % rows) + (i / rows)*si of it
-                const int i = i0 + lane;
-                const int64_t ib = (int64_t)(i % O.rows) + (int64_t)(i / O.rows) * O.si;
-#pragma unroll
-                for (int c16 = 0; c16 < 4; ++c16) {
-                    if (c16 * 16 < ncw) {
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) {
-                            const int col = U.n0 + h * 64 + c16 * 16 + j;
-                            if (i < O.mrows && col < O.ncols) {
-                                const int64_t off = __ldg(a.coltab + O.ctab + col) + ib;
-                                if (c32) ((float*)a.p[O.c_buf])[off] = hi[c16 * 16 + j] + lo[c16 * 16 + j];
-                                else a.p[O.c_buf][off] = (double)hi[c16 * 16 + j] + (double)lo[c16 * 16 + j];
-                            }
-                        }
-                    }
-                }
-            } else if (O.si == 1) {
-                // lanes hold consecutive rows i: each column store is coalesced
-                const int i = i0 + lane;
-#pragma unroll
-                for (int c16 = 0; c16 < 4; ++c16) {
-                    if (c16 * 16 < ncw) {
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) {
-                            const int col = U.n0 + h * 64 + c16 * 16 + j;
-                            if (i < O.mrows && col < O.ncols) {
-                                const int64_t off = (int64_t)i + (int64_t)col * O.sj;
-                                const float v = hi[c16 * 16 + j] + lo[c16 * 16 + j];
-                                if (c32) C32[off] = v;
-                                else C64[off] = (double)hi[c16 * 16 + j] + (double)lo[c16 * 16 + j];
-                            }
-                        }
-                    }
-                }
-            } else {
-                // rows i lie O.si apart in memory and columns are contiguous: pass each
-                // 32 x 16 block through shared memory so that 16 lanes store one row run
-#pragma unroll
-                for (int c16 = 0; c16 < 4; ++c16) {
-                    if (c16 * 16 < ncw) {
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) stg[lane * TI_EPI_LD + j] = hi[c16 * 16 + j] + lo[c16 * 16 + j];
-                        __syncwarp();
-                        const int jj = lane & 15;
-                        const int col = U.n0 + h * 64 + c16 * 16 + jj;
-                        for (int rr = lane >> 4; rr < 32; rr += 2) {
-                            const int i = i0 + rr;
-                            if (i < O.mrows && col < O.ncols) {
-                                const int64_t off = (int64_t)i * O.si + col;
-                                const float v = stg[rr * TI_EPI_LD + jj];
-                                if (c32) C32[off] = v;
-                                else C64[off] = (double)v;
-                            }
-                        }
-                        __syncwarp();
-                    }
-                }
-            }
         }
+        if (!ok && lane == 0) { *abort_flag = 1; atomicExch(&g_tc_status, 2); }
+    } else {
+        // ---------------- A-split producers: warps 10..13.  Thread r (0..127)
+        // owns row m0 + r of every split A chunk.  A loader position runs
+        // TI_RS - 1 chunks ahead of the splitter: it requests the chunk's 32
+        // values of row r with asynchronous 4-byte copies into a raw FP32 ring
+        // in shared memory (no registers held while they are in flight); the
+        // splitter waits for its own copies, splits the row into three BF16
+        // slices and stores them in the stage in the canonical K-major layout.
+        // Each thread reads back only what it copied itself.
+        const int r = tid - 10 * 32;
+        float* rawbase = (float*)(smem + a.ns * TI_STAGE);
+        uint32_t it = 0;
+        bool ok = true;
+        ChunkIt ld, sp;
+        ld.init(a);
+        sp.init(a);
+        uint32_t li = 0;  // chunks requested by the loader
+        for (; li < (uint32_t)(TI_RS - 1) && ld.valid; ++li) {
+            ti_request_raw(a, ld, r, rawbase + (li % TI_RS) * (TI_RAW / 4));
+            asm volatile("cp.async.commit_group;" ::: "memory");
+            ld.next(a);
+        }
+        for (; li < (uint32_t)(TI_RS - 1); ++li) asm volatile("cp.async.commit_group;" ::: "memory");
+        for (; sp.valid && ok; ++it) {
+            if (ld.valid) {
+                ti_request_raw(a, ld, r, rawbase + (li % TI_RS) * (TI_RAW / 4));
+                ld.next(a);
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+            ++li;
+            asm volatile("cp.async.wait_group %0;" :: "n"(TI_RS - 1) : "memory");
+            const uint32_t st = it % (uint32_t)a.ns, ph = (it / (uint32_t)a.ns) & 1u;
+            ok = __all_sync(0xffffffffu, ti_wait(smem_u32(&bar_empty[st]), ph ^ 1u, abort_flag));
+            if (!ok) break;
+            if (sp.S.flags & IMG_A_SPLIT) {
+                const float* raw = rawbase + (it % TI_RS) * (TI_RAW / 4);
+                float v[32];
+#pragma unroll
+                for (int k = 0; k < 32; ++k) v[k] = raw[k * 128 + r];
+                uint8_t* sa = smem + st * TI_STAGE + (r >> 3) * 512 + (r & 7) * 16;
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) put_vec<QCM_PREC_BF16X3>(sa + qq * 128, 0, TI_SLICE, v + 8 * qq);
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&bar_full[st]));
+            sp.next(a);
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
         if (!ok && lane == 0) { *abort_flag = 1; atomicExch(&g_tc_status, 2); }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -748,7 +1004,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
     if (warp == 0) {
         __syncwarp();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(256u));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(TI_TMEM_COLS));
     }
 }
 
@@ -785,10 +1041,15 @@ int tc_img_launch(const Stage& st, double* const* bufs, uint32_t f32mask, void* 
     a.outs = (const ImgOut*)st.d_iout;
     a.img = img;
     a.cimg = (const uint8_t*)st.d_icimg;
+    a.panels = (const ImgPanel*)st.d_ipanel;
+    a.gather = (const int64_t*)st.d_igather;
     a.coltab = (const int64_t*)st.d_icoltab;
     for (int i = 0; i < QCM_NBUF; ++i) a.p[i] = bufs[i];
     a.f32mask = f32mask;
     a.n_units = (int32_t)t.units.size();
+    bool any_split = false;
+    for (const ImgSeg& sg : t.segs) any_split |= (sg.flags & IMG_A_SPLIT) != 0;
+    a.ns = any_split ? TI_NS_SPLIT : TI_NS;
     const int grid = (int)std::min<size_t>(t.units.size(), (size_t)sm_count_of_current_device());
     tc_img_kernel<<<grid, TI_THREADS, TI_SMEM, s>>>(a);
     e = cudaGetLastError();

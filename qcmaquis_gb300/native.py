@@ -353,7 +353,7 @@ class Plan:
         npn, no, ns, nu = [int(x) for x in cnt]
         pd = np.zeros((max(npn, 1), 8), dtype=np.int64)
         od = np.zeros((max(no, 1), 9), dtype=np.int64)
-        sd = np.zeros((max(ns, 1), 6), dtype=np.int64)
+        sd = np.zeros((max(ns, 1), 8), dtype=np.int64)
         sa = np.zeros(max(ns, 1))
         td = np.zeros((max(nu, 1), 6), dtype=np.int64)
         check(lib().qcm_plan_stage_images(self.h, stage, _p(cnt, i64p), _p(pd, i64p), _p(od, i64p), _p(sd, i64p),

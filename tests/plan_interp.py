@@ -22,7 +22,7 @@ def run_plan(plan, bufs, images=False):
                 run_gemm_images(tab, bufs, plan.image_bytes)
                 if st[0] == "gemm":
                     continue
-                heavy = set(int(x) for x in tab["coltab"])   # outputs the dense groups wrote
+                heavy = set(int(x) for x in tab["coltab"][0::2])   # outputs the dense groups wrote
         if st[0] == "zero":
             zbuf, zlen = st[1], st[2]
             bufs[zbuf][:zlen] = 0.0
@@ -75,17 +75,23 @@ def run_gemm_images(tab, bufs, image_bytes):
     def slot(img_off, G, c, s, r, k):
         return (img_off + ((c * 3 + s) * G + r // 8) * 512 + ((k % 32) // 8) * 128 + (r % 8) * 16 + (k % 8) * 2) // 2
 
-    for (src_off, img_off, src_buf, ld, R, K, kcontig, G) in tab["panels"]:
+    def panel_values(pn, r, k):
+        src_off, img_off, src_buf, ld, R, K, kcontig, G = [int(x) for x in pn]
+        ok = (r < R) & (k < K)
+        if kcontig == 2:
+            ix = tab["gather"][src_off + np.clip(k, 0, K - 1)] + r
+        else:
+            ix = src_off + np.where(kcontig, r * ld + k, r + k * ld)
+        return np.where(ok, bufs[src_buf][np.where(ok, ix, 0)], 0.0)
+
+    for pn in tab["panels"]:
+        src_off, img_off, src_buf, ld, R, K, kcontig, G = [int(x) for x in pn]
+        if img_off < 0:
+            continue   # read and split inside the block-product kernel
         kc = (K + 31) // 32
         r = np.arange(G * 8)[:, None]
         k = np.arange(kc * 32)[None, :]
-        ok = (r < R) & (k < K)
-        if kcontig == 2:
-            col = tab["gather"][src_off + np.minimum(k, K - 1)]
-            ix = col + r
-        else:
-            ix = src_off + np.where(kcontig, r * ld + k, r + k * ld)
-        vals = np.where(ok, bufs[src_buf][np.where(ok, ix, 0)], 0.0)
+        vals = panel_values(pn, r, k)
         assert img_off % 512 == 0 and img_off + kc * 3 * G * 512 <= image_bytes
         for s in range(3):
             img[slot(img_off, G, k // 32, s, r, k)] = vals if s == 0 else 0.0
@@ -95,7 +101,7 @@ def run_gemm_images(tab, bufs, image_bytes):
         assert nt % 16 == 0 and 16 <= nt <= 128 and m0 % 128 == 0 and n0 % 8 == 0
         acc = np.zeros((128, nt))
         for s in range(sb, se):
-            a_img, b_img, a_G, b_G, kc, flags = [int(x) for x in segs[s]]
+            a_img, b_img, a_G, b_G, kc, flags, a_panel, a_c0 = [int(x) for x in segs[s]]
             bsrc = cimg if flags & 2 else img
             ngA, ngB = min(16, a_G - m0 // 8), min(nt // 8, b_G - n0 // 8)
             assert ngA > 0 and ngB > 0
@@ -107,7 +113,11 @@ def run_gemm_images(tab, bufs, image_bytes):
                 A = np.full((3, 128, 32), np.nan)
                 B = np.full((3, nt, 32), np.nan)
                 for sl in range(3):
-                    A[sl, :ngA * 8] = img[slot(a_img, a_G, c, sl, m0 + ra, kk)]
+                    if flags & 1:   # A split in the kernel: all 128 rows from the source panel
+                        A[sl] = panel_values(tab["panels"][a_panel], m0 + np.arange(128)[:, None],
+                                             (a_c0 + c) * 32 + kk) if sl == 0 else 0.0
+                    else:
+                        A[sl, :ngA * 8] = img[slot(a_img, a_G, c, sl, m0 + ra, kk)]
                     B[sl, :ngB * 8] = bsrc[slot(b_img, b_G, c, sl, n0 + rb, kk)]
                 for ia, ib in PAIRS:
                     D += A[ia] @ B[ib].T
@@ -120,5 +130,6 @@ def run_gemm_images(tab, bufs, image_bytes):
             dst = c_off + (m0 + i) * si + (n0 + j) * sj
         else:
             e = m0 + i
-            dst = tab["coltab"][ctab + np.minimum(n0 + j, ncols - 1)] + (e % rows) + (e // rows) * si
+            jj = ctab + np.minimum(n0 + j, ncols - 1)
+            dst = tab["coltab"][2 * jj] + (e % rows) + (e // rows) * tab["coltab"][2 * jj + 1]
         bufs[c_buf][dst[valid]] = acc[valid]
