@@ -286,72 +286,6 @@ gather_axpy_contig(BufTable bufs, const DevAxpyOut* __restrict__ outs, const Dev
     }
 }
 
-// Warp-granular contiguous-source executor for small output tiles (the
-// outputs the dense groups leave, mostly a few terms over a few hundred
-// elements).  A work item is at most CW_ITEM elements of one tile; each warp
-// of a CTA owns one item, its lanes hold CW_PER accumulators at stride 32, and
-// the term descriptors are read by the lanes and broadcast with shuffles, so
-// an item costs no block-wide barrier.
-constexpr int CW_PER = 8;
-constexpr int CW_ITEM = 32 * CW_PER;
-constexpr int CW_WARPS = 8;
-
-template <class ACC, class SRC>
-__global__ void __launch_bounds__(32 * CW_WARPS)
-gather_axpy_warp(BufTable bufs, const DevAxpyOut* __restrict__ outs, const DevAxpyTerm* __restrict__ terms,
-                 const DevAxpyChunk* __restrict__ work, int64_t n_work) {
-    const int lane = threadIdx.x & 31;
-    const int64_t wi = (int64_t)blockIdx.x * CW_WARPS + (threadIdx.x >> 5);
-    if (wi >= n_work) return;
-    const DevAxpyChunk w = work[wi];
-    const DevAxpyOut o = outs[w.out];
-    const int n = w.n;
-    ACC acc[CW_PER];
-#pragma unroll
-    for (int u = 0; u < CW_PER; ++u) acc[u] = ACC(0);
-    const int64_t nterm = o.t_end - o.t_begin;
-    for (int64_t t0 = 0; t0 < nterm; t0 += 32) {
-        const int tn = (int)min((int64_t)32, nterm - t0);
-        const SRC* my_ptr = nullptr;
-        ACC my_alpha = ACC(0);
-        if (lane < tn) {
-            const DevAxpyTerm tt = terms[o.t_begin + t0 + lane];
-            my_ptr = (const SRC*)bufs.p[tt.src_buf] + tt.src_off + w.e0;
-            my_alpha = (ACC)tt.alpha;
-        }
-        for (int t = 0; t < tn; ++t) {
-            const SRC* __restrict__ p = (const SRC*)__shfl_sync(0xffffffffu, (unsigned long long)my_ptr, t) + lane;
-            const ACC al = __shfl_sync(0xffffffffu, my_alpha, t);
-            if (n == CW_ITEM) {
-#pragma unroll
-                for (int u = 0; u < CW_PER; ++u) acc[u] = fma(al, (ACC)__ldg(p + 32 * u), acc[u]);
-            } else {
-#pragma unroll
-                for (int u = 0; u < CW_PER; ++u)
-                    if (lane + 32 * u < n) acc[u] = fma(al, (ACC)__ldg(p + 32 * u), acc[u]);
-            }
-        }
-    }
-    const bool dst32 = slot_f32(bufs, o.dst_buf);
-    const int rows = (int)o.rows;
-    const int e_first = w.e0 + lane;
-    int rr = e_first % rows, cc = e_first / rows;
-    const int dr = 32 % rows, dc = 32 / rows;
-    float* __restrict__ D32 = (float*)bufs.p[o.dst_buf] + o.dst_off;
-    double* __restrict__ D64 = bufs.p[o.dst_buf] + o.dst_off;
-#pragma unroll
-    for (int u = 0; u < CW_PER; ++u) {
-        if (lane + 32 * u < n) {
-            const int64_t d = rr + (int64_t)cc * o.ldd;
-            if (dst32) D32[d] = (float)acc[u];
-            else D64[d] = (double)acc[u];
-        }
-        rr += dr;
-        cc += dc;
-        if (rr >= rows) { rr -= rows; ++cc; }
-    }
-}
-
 // Work list of the contiguous-source executor, ordered so that CTAs running
 // at the same time read the same source chunks: output tiles that share a
 // source tile (transitively) form one group; groups run one after another,
@@ -484,13 +418,17 @@ void free_stage_device(Stage& st) {
     if (st.d_tcw) cudaFree(st.d_tcw);
     if (st.d_cw) cudaFree(st.d_cw);
     for (void** d : {&st.d_ipanel, &st.d_ibuild, &st.d_iout, &st.d_iseg, &st.d_iunit, &st.d_igather, &st.d_icoltab,
-                     &st.d_icimg, &st.d_cw_light}) {
+                     &st.d_icimg, &st.d_cw_light, &st.d_icost}) {
         if (*d) cudaFree(*d);
         *d = nullptr;
     }
     st.d_a = st.d_b = st.d_c = st.d_tcw = st.d_cw = nullptr;
     st.n_cw = 0;
     st.n_cw_light = 0;
+    if (st.ev_fork) cudaEventDestroy((cudaEvent_t)st.ev_fork);
+    if (st.ev_join) cudaEventDestroy((cudaEvent_t)st.ev_join);
+    if (st.side_stream) cudaStreamDestroy((cudaStream_t)st.side_stream);
+    st.ev_fork = st.ev_join = st.side_stream = nullptr;
 }
 
 template <class T>
@@ -513,6 +451,7 @@ static int upload_images(Stage& st) {
     if ((rc = upload_vec(st.img.gather, &st.d_igather))) return rc;
     if ((rc = upload_vec(st.img.coltab, &st.d_icoltab))) return rc;
     if ((rc = upload_vec(st.img.cimg, &st.d_icimg))) return rc;
+    if (st.img.ares && (rc = upload_vec(st.img.cost, &st.d_icost))) return rc;
     return QCM_OK;
 }
 
@@ -548,12 +487,18 @@ static int upload_stage(Stage& st) {
                 // the outputs the dense groups do not compute, in the same order
                 std::vector<DevAxpyChunk> lw;
                 for (const DevAxpyChunk& c : cw)
-                    if (!st.heavy[c.out])
-                        for (int32_t e = 0; e < c.n; e += CW_ITEM)
-                            lw.push_back({c.out, c.e0 + e, std::min<int32_t>(CW_ITEM, c.n - e), 0});
+                    if (!st.heavy[c.out]) lw.push_back(c);
                 if (!lw.empty() && (rc = upload_vec(lw, &st.d_cw_light))) return rc;
                 st.n_cw_light = (int64_t)lw.size();
                 if ((rc = upload_images(st))) return rc;
+                cudaStream_t ss;
+                cudaEvent_t e0, e1;
+                QCM_CUDA(cudaStreamCreateWithFlags(&ss, cudaStreamNonBlocking));
+                st.side_stream = ss;
+                QCM_CUDA(cudaEventCreateWithFlags(&e0, cudaEventDisableTiming));
+                st.ev_fork = e0;
+                QCM_CUDA(cudaEventCreateWithFlags(&e1, cudaEventDisableTiming));
+                st.ev_join = e1;
             }
         }
     } else if (st.kind == ST_GEMM) {
@@ -597,16 +542,30 @@ static int launch_axpy(const Stage& st, const BufTable& bt, int precision, cudaS
         const auto* CW = (const DevAxpyChunk*)st.d_cw;
         unsigned gc = (unsigned)st.n_cw;
         if (precision == QCM_PREC_BF16X3 && bt.p[QCM_BUF_IMG] && st.d_iunit) {
-            // BF16x3 with images: the dense groups on the tensor cores, the rest gathered by warps
+            // BF16x3 with images: the dense groups on the tensor cores (on the caller's
+            // stream) and the gather of the other outputs on the stage's side stream,
+            // forked from and joined back into the caller's stream (disjoint outputs)
+            cudaStream_t ss = (cudaStream_t)st.side_stream;
+            const bool fork = ss && st.n_cw_light > 0;
+            if (fork) {
+                QCM_CUDA(cudaEventRecord((cudaEvent_t)st.ev_fork, s));
+                QCM_CUDA(cudaStreamWaitEvent(ss, (cudaEvent_t)st.ev_fork, 0));
+                const auto* LW = (const DevAxpyChunk*)st.d_cw_light;
+                const unsigned gl = (unsigned)st.n_cw_light;
+                if (src32) gather_axpy_contig<float, float><<<gl, CG_THREADS, 0, ss>>>(bt, O, T, LW);
+                else gather_axpy_contig<float, double><<<gl, CG_THREADS, 0, ss>>>(bt, O, T, LW);
+                QCM_CUDA(cudaGetLastError());
+            }
             int rc = tc_img_launch(st, bt.p, bt.f32mask, (void*)s);
+            if (fork) {
+                QCM_CUDA(cudaEventRecord((cudaEvent_t)st.ev_join, ss));
+                QCM_CUDA(cudaStreamWaitEvent(s, (cudaEvent_t)st.ev_join, 0));
+            }
             if (rc) return rc;
-            if (st.n_cw_light == 0) return QCM_OK;
-            const auto* LW = (const DevAxpyChunk*)st.d_cw_light;
-            const unsigned gl = (unsigned)((st.n_cw_light + CW_WARPS - 1) / CW_WARPS);
-            if (src32) gather_axpy_warp<float, float><<<gl, 32 * CW_WARPS, 0, s>>>(bt, O, T, LW, st.n_cw_light);
-            else gather_axpy_warp<float, double><<<gl, 32 * CW_WARPS, 0, s>>>(bt, O, T, LW, st.n_cw_light);
-            QCM_CUDA(cudaGetLastError());
-            return QCM_OK;
+            if (fork) return QCM_OK;
+            CW = (const DevAxpyChunk*)st.d_cw_light;
+            gc = (unsigned)st.n_cw_light;
+            if (gc == 0) return QCM_OK;
         }
         if (src32) {
             gather_axpy_contig<float, float><<<gc, CG_THREADS, 0, s>>>(bt, O, T, CW);

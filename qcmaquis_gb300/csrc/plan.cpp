@@ -29,10 +29,10 @@
 
 namespace qcm {
 
-// Whether the K2 dense groups and K3 read their A operands directly from the
-// FP32 sources and split them inside the block-product kernel (true), or from
-// images built by a separate pass (false).
-static constexpr bool kSplitA = false;
+// A-resident mode for single-segment stages (K1).  Off: measured slower at the
+// benchmark size, because contiguous per-CTA tile ranges lose the L2 reuse of
+// the B operand across CTAs that the strided order has.
+static constexpr bool kAResident = false;
 
 static thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
@@ -599,6 +599,67 @@ static void finalize_boundary_layout(qcm_plan* P, std::vector<BM>& out) {
 }
 
 // ------------------------------------------------------------------ plan kinds
+// The parts of the contr blocks that K3 reads but no K2 tile writes must be
+// zero.  Instead of clearing the whole contr arena, append zero-term output
+// tiles (written as zeros by the gather executors) covering exactly those
+// parts: per block, between consecutive column breakpoints of its tiles, the
+// row ranges no tile covers.  Blocks K3 never reads are left unwritten.
+static void add_zero_tiles(Stage& k2, const Stage& k3, int32_t buf) {
+    struct B { int64_t off, ld, cols; };
+    std::vector<B> blocks;
+    for (const GemmSeg& g : k3.gseg)
+        if (g.a_buf == buf && g.ta == 0) blocks.push_back({g.a_off, g.lda, g.K});
+    std::sort(blocks.begin(), blocks.end(), [](const B& x, const B& y) { return x.off < y.off; });
+    blocks.erase(std::unique(blocks.begin(), blocks.end(), [](const B& x, const B& y) { return x.off == y.off; }),
+                 blocks.end());
+    struct T { int64_t r0, c0, rows, cols; };
+    std::vector<std::vector<T>> in(blocks.size());
+    for (const AxpyOut& a : k2.aout) {
+        if (a.dst_buf != buf) continue;
+        auto it = std::upper_bound(blocks.begin(), blocks.end(), a.dst_off,
+                                   [](int64_t o, const B& b) { return o < b.off; });
+        if (it == blocks.begin()) continue;
+        --it;
+        const int64_t rel = a.dst_off - it->off;
+        if (rel >= it->ld * it->cols) continue;  // a block K3 does not read
+        if (a.ldd != it->ld) throw std::runtime_error("contr tile does not match its block");
+        in[it - blocks.begin()].push_back({rel % it->ld, rel / it->ld, a.rows, a.cols});
+    }
+    const int64_t t_at = (int64_t)k2.aterm.size();
+    for (size_t bi = 0; bi < blocks.size(); ++bi) {
+        const B& b = blocks[bi];
+        std::vector<int64_t> cut{0, b.cols};
+        for (const T& t : in[bi]) { cut.push_back(t.c0); cut.push_back(t.c0 + t.cols); }
+        std::sort(cut.begin(), cut.end());
+        cut.erase(std::unique(cut.begin(), cut.end()), cut.end());
+        for (size_t k = 0; k + 1 < cut.size(); ++k) {
+            const int64_t ca = cut[k], cb = cut[k + 1];
+            if (ca >= b.cols) break;
+            std::vector<std::pair<int64_t, int64_t>> rr;
+            for (const T& t : in[bi])
+                if (t.c0 <= ca && cb <= t.c0 + t.cols) rr.push_back({t.r0, t.r0 + t.rows});
+            std::sort(rr.begin(), rr.end());
+            int64_t r = 0;
+            auto emit = [&](int64_t r_lo, int64_t r_hi) {
+                if (r_hi <= r_lo) return;
+                AxpyOut z;
+                z.dst_buf = buf;
+                z.dst_off = b.off + r_lo + ca * b.ld;
+                z.ldd = b.ld;
+                z.rows = r_hi - r_lo;
+                z.cols = cb - ca;
+                z.t_begin = z.t_end = t_at;
+                k2.aout.push_back(z);
+            };
+            for (const auto& iv : rr) {
+                emit(r, iv.first);
+                r = std::max(r, iv.second);
+            }
+            emit(r, b.ld);
+        }
+    }
+}
+
 static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& right_i, const BM& psi,
                              const std::vector<BM>& L, const std::vector<BM>& R, const MpoV& W, bool herm) {
     auto* P = new qcm_plan();
@@ -683,9 +744,11 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
     P->scratch[0] = rp_end;
     P->scratch[1] = std::max(t_end, part_end);
     P->scratch[2] = c_end;
-    build_image_tables(s1, s1.img, false);
-    build_image_tables(s3, s3.img, kSplitA);
-    build_dense_groups(s2, 64, s2.img, s2.heavy, kSplitA);
+    add_zero_tiles(s2, s3, QCM_BUF_S2);
+    z2.zlen = 0;  // the zero tiles of K2 clear what K3 reads; the rest of contr is never read
+    build_image_tables(s1, s1.img);
+    build_image_tables(s3, s3.img);
+    build_dense_groups(s2, 64, s2.img, s2.heavy);
     P->image_bytes = std::max(std::max(s1.img.bytes, s3.img.bytes), s2.img.bytes);
     P->stages.push_back(std::move(z0));
     P->stages.push_back(std::move(s0));
@@ -986,7 +1049,7 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
 // the MMA with the larger of (M, N) on the 128-row MMA side: when N > M the
 // stage's C = op(A) op(B) is computed as C^T = op(B)^T op(A)^T.  Panels that
 // several segments read with the same orientation share one image.
-void build_image_tables(const Stage& st, ImgTables& t, bool split_a) {
+void build_image_tables(const Stage& st, ImgTables& t) {
     t = ImgTables();
     struct Key {
         int32_t buf, ld, R, K, kc;
@@ -1060,19 +1123,19 @@ void build_image_tables(const Stage& st, ImgTables& t, bool split_a) {
                 throw std::runtime_error("image executor: block too large");
             // op(A): rows m, element (m,k) at ta ? k + m*lda : m + k*lda
             // op(B)^T: rows n, element (n,k) = op(B)(k,n) at tb ? n + k*ldb : k + n*ldb
-            const int32_t pa = panel(g.a_buf, g.a_off, g.lda, g.ta ? 1 : 0, o.M, g.K, tr || !split_a);
-            const int32_t pb = panel(g.b_buf, g.b_off, g.ldb, g.tb ? 0 : 1, o.N, g.K, !tr || !split_a);
+            const int32_t pa = panel(g.a_buf, g.a_off, g.lda, g.ta ? 1 : 0, o.M, g.K, true);
+            const int32_t pb = panel(g.b_buf, g.b_off, g.ldb, g.tb ? 0 : 1, o.N, g.K, true);
             const int32_t ia = tr ? pb : pa, ib = tr ? pa : pb;
             const ImgPanel& A = t.panels[ia];
             const ImgPanel& B = t.panels[ib];
             ImgSeg s;
-            s.a_img = split_a ? 0 : A.img_off;
+            s.a_img = A.img_off;
             s.b_img = B.img_off;
             s.a_G = A.G;
             s.b_G = B.G;
             s.kc = (int32_t)((g.K + 31) / 32);
             s.alpha = (float)g.alpha;
-            s.flags = split_a ? IMG_A_SPLIT : 0;
+            s.flags = 0;
             s.a_panel = ia;
             s.a_c0 = 0;
             s.pad = 0;
@@ -1093,6 +1156,21 @@ void build_image_tables(const Stage& st, ImgTables& t, bool split_a) {
     }
     if (t.build.size() / 2 > 0x7fffffffULL || t.units.size() > 0x7fffffffULL || t.segs.size() > 0x7fffffffULL)
         throw std::runtime_error("image executor: tables too large");
+    // A-resident mode when every tile is a single short segment (K1: each T tile is one
+    // block product; the same psi tile is the A operand of hundreds of products)
+    bool ares = kAResident && !t.units.empty();
+    for (const ImgUnit& u : t.units)
+        ares = ares && u.s_end - u.s_begin == 1 && t.segs[u.s_begin].kc <= IMG_ARES_MAX;
+    if (ares) {
+        std::stable_sort(t.units.begin(), t.units.end(), [&](const ImgUnit& x, const ImgUnit& y) {
+            const int64_t ax = t.segs[x.s_begin].a_img, ay = t.segs[y.s_begin].a_img;
+            return ax != ay ? ax < ay : x.m0 < y.m0;
+        });
+        t.ares = true;
+        t.cost.assign(t.units.size() + 1, 0);
+        for (size_t i = 0; i < t.units.size(); ++i)
+            t.cost[i + 1] = t.cost[i] + (int64_t)t.segs[t.units[i].s_begin].kc * (t.units[i].nt + 32) + 64;
+    }
 }
 
 // Round-to-nearest-even FP32 -> BF16 (finite inputs) and back.
@@ -1109,7 +1187,7 @@ static float bf16_to_float(uint16_t h) {
     return x;
 }
 
-void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::vector<char>& heavy, bool split_a) {
+void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::vector<char>& heavy) {
     t = ImgTables();
     const size_t nO = st.aout.size();
     heavy.assign(nO, 0);
@@ -1169,7 +1247,7 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         // A: gathered source tiles, rows e, K = source index
         ImgPanel pa;
         pa.src_off = (int64_t)t.gather.size();
-        pa.img_off = split_a ? -1 : t.bytes;
+        pa.img_off = t.bytes;
         pa.src_buf = src_buf;
         pa.ld = 0;
         pa.R = (int32_t)E;
@@ -1178,10 +1256,8 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         pa.G = G;
         t.gather.insert(t.gather.end(), srcs.begin(), srcs.end());
         const int32_t pid = (int32_t)t.panels.size();
-        if (!split_a) {
-            t.bytes += KC * 3 * (int64_t)G * 512;
-            for (int64_t c = 0; c < KC; ++c) { t.build.push_back(pid); t.build.push_back((int32_t)c); }
-        }
+        t.bytes += KC * 3 * (int64_t)G * 512;
+        for (int64_t c = 0; c < KC; ++c) { t.build.push_back(pid); t.build.push_back((int32_t)c); }
         t.panels.push_back(pa);
         // B: coefficient matrix W (rows = outputs, K = sources), split on the host
         std::vector<float> W((size_t)O.size() * S, 0.0f);
@@ -1233,13 +1309,13 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         const int32_t s_begin = (int32_t)t.segs.size();
         for (int64_t c0 = 0; c0 < KC; c0 += 4) {
             ImgSeg sg;
-            sg.a_img = split_a ? 0 : pa.img_off + c0 * 3 * (int64_t)G * 512;
+            sg.a_img = pa.img_off + c0 * 3 * (int64_t)G * 512;
             sg.b_img = b_off + c0 * 3 * (int64_t)Gb * 512;
             sg.a_G = G;
             sg.b_G = Gb;
             sg.kc = (int32_t)std::min<int64_t>(4, KC - c0);
             sg.alpha = 1.0f;
-            sg.flags = (split_a ? IMG_A_SPLIT : 0) | IMG_B_CONST;
+            sg.flags = IMG_B_CONST;
             sg.a_panel = pid;
             sg.a_c0 = (int32_t)c0;
             sg.pad = 0;

@@ -117,15 +117,13 @@ struct ImgOut {
     int64_t c_off, si, sj, ctab;
     int32_t c_buf, mrows, ncols, mode, rows, pad;
 };
-// ImgSeg.flags: IMG_A_SPLIT -- the A operand is read from its source panel
-// (a_panel, chunks from a_c0) and split inside the block-product kernel;
-// IMG_B_CONST -- the B image lives in the plan's constant images.
-enum { IMG_A_SPLIT = 1, IMG_B_CONST = 2 };
+// ImgSeg.flags: IMG_B_CONST -- the B image lives in the plan's constant images.
+enum { IMG_B_CONST = 2 };
 struct ImgSeg {
     int64_t a_img, b_img;   // byte offsets of the A and B panel images (at the chunk range start)
     int32_t a_G, b_G, kc;   // row groups of the panels, K-chunks
     float alpha;
-    int32_t flags, a_panel, a_c0, pad;
+    int32_t flags, a_panel, a_c0, pad;   // a_panel / a_c0: the A panel and its first chunk (inspection)
 };
 struct ImgUnit {
     int32_t out, m0, n0, nt, s_begin, s_end;  // nt: MMA N (multiple of 16, <= 128)
@@ -140,16 +138,21 @@ struct ImgTables {
     std::vector<int64_t> coltab;  // (offset, ld) pairs of the output tiles of mode-1 outputs
     std::vector<uint8_t> cimg;    // constant images (coefficient matrices), built by the plan
     int64_t bytes = 0;            // per-call image bytes
+    // A-resident mode: every tile is one segment of at most IMG_ARES_MAX K-chunks,
+    // tiles are ordered by their A tile (image, m0), and each CTA takes a
+    // contiguous cost-balanced range of them, so that a run of tiles sharing one
+    // A tile loads it into shared memory once and streams only B.
+    bool ares = false;
+    std::vector<int64_t> cost;    // prefix sums of the tile costs (size tiles + 1)
 };
-// split_a: A operands are split inside the block-product kernel (no A image)
-void build_image_tables(const struct Stage& st, ImgTables& t, bool split_a = false);
+constexpr int IMG_ARES_MAX = 5;
+void build_image_tables(const struct Stage& st, ImgTables& t);
 // Dense groups of a gather-axpy stage: output tiles that share their sources
 // (a connected component of the output/source graph), have at least
 // min_terms terms and one tile shape become one block product
 // contr[:, group] = T_gathered . W^T on the tensor cores.  heavy[o] marks the
 // outputs taken.
-void build_dense_groups(const struct Stage& st, int64_t min_terms, ImgTables& t, std::vector<char>& heavy,
-                        bool split_a);
+void build_dense_groups(const struct Stage& st, int64_t min_terms, ImgTables& t, std::vector<char>& heavy);
 
 struct Stage {
     int kind;
@@ -180,11 +183,17 @@ struct Stage {
     void* d_icimg = nullptr;
     void* d_cw_light = nullptr;  // AXPY: chunk work list of the outputs outside the dense groups
     int64_t n_cw_light = 0;
+    // AXPY with dense groups: side stream and fork/join events, so that the gather of
+    // the other outputs runs alongside the dense groups' block products
+    void* side_stream = nullptr;
+    void* ev_fork = nullptr;
+    void* ev_join = nullptr;
     void* d_ipanel = nullptr;
     void* d_ibuild = nullptr;
     void* d_iout = nullptr;
     void* d_iseg = nullptr;
     void* d_iunit = nullptr;
+    void* d_icost = nullptr;
 };
 
 enum PlanKind { PK_SIGMA = 0, PK_BLEFT = 1, PK_BRIGHT = 2 };

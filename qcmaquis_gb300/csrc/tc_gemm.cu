@@ -403,26 +403,25 @@ int tc_launch(const void* d_out, const void* d_seg, const void* d_work, int64_t 
 // TMEM accumulators, and warps 2..9 drain each finished segment (one block
 // product of the split-K sum) into compensated FP32 register sums, scaled by
 // the segment's coefficient, and store the tile once.
-constexpr int TI_NS = 4;                        // shared-memory stages (at most)
-constexpr int TI_NS_SPLIT = 3;                  // stages when A operands are split in the kernel ...
-constexpr int TI_RS = 3;                        // ... which also use this many raw FP32 A chunks
-constexpr uint32_t TI_RAW = 128 * 32 * 4;       // one raw FP32 A chunk (128 rows x 32 K)
-constexpr int TI_AWARPS = 4;                    // A-split producer warps
-constexpr int TI_THREADS = (10 + TI_AWARPS) * 32;
+constexpr int TI_NS = 4;                        // shared-memory stages
+constexpr int TI_THREADS = 10 * 32;
 constexpr uint32_t TI_SLICE = 16 * 512;         // one slice of a 128-row x 64-byte chunk
 constexpr uint32_t TI_STAGE = 6 * TI_SLICE;     // A and B, three slices each
 constexpr int TI_EPI_LD = 17;                   // epilogue staging row stride (floats)
-static_assert(TI_NS_SPLIT * TI_STAGE + TI_RS * TI_RAW <= TI_NS * TI_STAGE, "raw ring must fit in the stage area");
+// A-resident mode: IMG_ARES_MAX A chunks (three slices each) stay in shared
+// memory, followed by TI_NSB stages of B chunks; same footprint as TI_NS stages.
+constexpr int TI_NSB = 3;
+constexpr uint32_t TI_ACHUNK = 3 * TI_SLICE;
+static_assert(IMG_ARES_MAX * TI_ACHUNK + TI_NSB * TI_ACHUNK <= TI_NS * TI_STAGE, "A-resident layout must fit");
 constexpr uint32_t TI_SMEM = TI_NS * TI_STAGE + 8 * 32 * TI_EPI_LD * 4 + 1024;
 constexpr uint64_t TI_WAIT_NS = 4000000000ull;  // a wait that lasts this long gives up
 
 struct TiArgs {
-    int32_t ns;               // shared-memory stages in use (TI_NS, or TI_NS_SPLIT with the raw ring)
+    int32_t ares;             // A-resident mode (ImgTables::ares)
+    const int64_t* cost;      // A-resident mode: prefix sums of the tile costs
     const ImgUnit* units;
     const ImgSeg* segs;
     const ImgOut* outs;
-    const ImgPanel* panels;   // A panels of split segments
-    const int64_t* gather;    // source offsets of gathered panels
     const uint8_t* img;
     const uint8_t* cimg;      // constant images of the plan (coefficient matrices)
     const int64_t* coltab;    // (offset, ld) pairs of the output tiles of mode-1 outputs
@@ -528,7 +527,7 @@ build_images_kernel(const ImgPanel* __restrict__ panels, const int32_t* __restri
 struct TiCursor {
     const ImgUnit* units;
     const ImgSeg* segs;
-    int n, g, u;
+    int n, g, u;   // tiles u, u+g, ... below n
     ImgUnit cur, nxt, nn;
     ImgSeg first_cur, first_nxt;
 
@@ -545,13 +544,15 @@ struct TiCursor {
     }
     __device__ ImgUnit at(int x) const { return x < n ? units[x] : no_unit(); }
     __device__ ImgSeg seg(int s, int e) const { return s < e ? segs[s] : no_seg(); }
-    __device__ void init(const TiArgs& a) {
-        units = a.units; segs = a.segs; n = a.n_units; g = gridDim.x; u = blockIdx.x;
+    // strided (u0 = blockIdx.x, step gridDim.x) or contiguous ([u0, end), step 1) tiles
+    __device__ void init(const TiArgs& a, int u0, int end, int step) {
+        units = a.units; segs = a.segs; n = end; g = step; u = u0;
         cur = at(u);
         nxt = at(u + g);
         first_cur = seg(cur.s_begin, cur.s_end);
     }
     __device__ bool valid() const { return u < n; }
+    __device__ bool has_next() const { return u + g < n; }
     __device__ void prefetch() {
         nn = at(u + 2 * g);
         first_nxt = seg(nxt.s_begin, nxt.s_end);
@@ -634,116 +635,15 @@ __device__ __forceinline__ void ti_store16(const TiArgs& a, const ImgOut& O, con
     }
 }
 
-// Element (r, k) of an operand panel (FP32 or FP64 source), 0 outside it.
-__device__ __forceinline__ float panel_elem(const TiArgs& a, const ImgPanel& P, bool f32, int r, int k) {
-    if (r >= P.R || k >= P.K) return 0.0f;
-    int64_t ix;
-    if (P.kcontig == 2) ix = __ldg(a.gather + P.src_off + k) + r;
-    else ix = P.src_off + (P.kcontig ? (int64_t)r * P.ld + k : (int64_t)r + (int64_t)k * P.ld);
-    return f32 ? __ldg((const float*)a.p[P.src_buf] + ix) : (float)__ldg(a.p[P.src_buf] + ix);
-}
-
-// Position in this CTA's chunk sequence (tile u, segment s, K-chunk c) with
-// the descriptors the A-split producers need.
-struct ChunkIt {
-    int u, s, c;
-    ImgUnit U;
-    ImgSeg S;
-    ImgPanel P;
-    bool valid;
-
-    __device__ void load_seg(const TiArgs& a) {
-        S = a.segs[s];
-        if (S.flags & IMG_A_SPLIT) P = a.panels[S.a_panel];
-    }
-    // move to the first chunk at or after (u, s, c)
-    __device__ void settle(const TiArgs& a) {
-        for (;;) {
-            if (s < U.s_end) {
-                if (c < S.kc) { valid = true; return; }
-                ++s;
-                c = 0;
-                if (s < U.s_end) load_seg(a);
-                continue;
-            }
-            u += gridDim.x;
-            if (u >= a.n_units) { valid = false; return; }
-            U = a.units[u];
-            s = U.s_begin;
-            c = 0;
-            if (s < U.s_end) load_seg(a);
-        }
-    }
-    __device__ void init(const TiArgs& a) {
-        u = blockIdx.x;
-        valid = u < a.n_units;
-        if (!valid) return;
-        U = a.units[u];
-        s = U.s_begin;
-        c = 0;
-        if (s < U.s_end) load_seg(a);
-        settle(a);
-    }
-    __device__ void next(const TiArgs& a) {
-        ++c;
-        settle(a);
-    }
-};
-
-__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" :: "r"(smem_u32(dst)), "l"(src) : "memory");
-}
-
-// Request row r of the split A chunk at `it` into a raw ring slot ([k][128]
-// floats): asynchronous copies of the FP32 source, plain stores of zeros
-// outside the panel (FP64 sources are converted with plain loads).
-__device__ __forceinline__ void ti_request_raw(const TiArgs& a, const ChunkIt& it, int r, float* raw) {
-    if (!(it.S.flags & IMG_A_SPLIT)) return;
-    const ImgPanel& P = it.P;
-    const int row = it.U.m0 + r;
-    const int kb = (it.S.a_c0 + it.c) * 32;
-    const bool f32 = (a.f32mask >> P.src_buf) & 1u;
-    const float* S32 = (const float*)a.p[P.src_buf];
-    const double* S64 = a.p[P.src_buf];
-    if (row >= P.R) {
-#pragma unroll 8
-        for (int k = 0; k < 32; ++k) raw[k * 128 + r] = 0.0f;
-        return;
-    }
-    if (P.kcontig == 2) {
-#pragma unroll
-        for (int k0 = 0; k0 < 32; k0 += 8) {
-            int64_t g[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) g[j] = (kb + k0 + j < P.K) ? __ldg(a.gather + P.src_off + kb + k0 + j) : -1;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                float* d = raw + (k0 + j) * 128 + r;
-                if (g[j] < 0) *d = 0.0f;
-                else if (f32) cp_async4(d, S32 + g[j] + row);
-                else *d = (float)__ldg(S64 + g[j] + row);
-            }
-        }
-    } else {
-        const int64_t base = P.src_off + (P.kcontig ? (int64_t)row * P.ld : (int64_t)row);
-        const int64_t step = P.kcontig ? 1 : P.ld;
-#pragma unroll 8
-        for (int k = 0; k < 32; ++k) {
-            float* d = raw + k * 128 + r;
-            if (kb + k >= P.K) *d = 0.0f;
-            else if (f32) cp_async4(d, S32 + base + (int64_t)(kb + k) * step);
-            else *d = (float)__ldg(S64 + base + (int64_t)(kb + k) * step);
-        }
-    }
-}
-
 __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
     extern __shared__ uint8_t ti_smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)ti_smem_raw + 1023) & ~(uintptr_t)1023);
-    float* epi = (float*)(smem + TI_NS * TI_STAGE);   // after the stages (and the raw ring)
+    float* epi = (float*)(smem + TI_NS * TI_STAGE);
     __shared__ __align__(8) uint64_t bar_full[TI_NS], bar_empty[TI_NS], bar_accf[2], bar_acce[2], bar_fin;
+    __shared__ __align__(8) uint64_t bar_ares_full, bar_ares_empty;
     __shared__ uint32_t tmem_sh;
     __shared__ int abort_sh;
+    __shared__ int range_sh[2];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     volatile int* abort_flag = &abort_sh;
 
@@ -754,8 +654,8 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
     }
     if (tid == 32) {
         for (int i = 0; i < TI_NS; ++i) {
-            // full: the bulk-copy producer's arrive (with its transaction bytes) + the A-split warps
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&bar_full[i])), "r"(1 + TI_AWARPS));
+            // full: the bulk-copy producer's arrive, completed by its transaction bytes
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bar_full[i])));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bar_empty[i])));
         }
         for (int i = 0; i < 2; ++i) {
@@ -763,22 +663,96 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;" :: "r"(smem_u32(&bar_acce[i])));
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bar_fin)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bar_ares_full)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bar_ares_empty)));
         abort_sh = 0;
+        // this CTA's tiles: a contiguous cost-balanced range (A-resident mode), else strided
+        if (a.ares) {
+            const int64_t total = a.cost[a.n_units];
+            int r2[2];
+            for (int side = 0; side < 2; ++side) {
+                const int64_t target = total * (int64_t)(blockIdx.x + side) / (int64_t)gridDim.x;
+                int lo = 0, hi = a.n_units;   // first tile whose cost prefix reaches the target
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (a.cost[mid] < target) lo = mid + 1; else hi = mid;
+                }
+                r2[side] = lo;
+            }
+            range_sh[0] = r2[0];
+            range_sh[1] = blockIdx.x + 1 == gridDim.x ? a.n_units : r2[1];
+        } else {
+            range_sh[0] = blockIdx.x;
+            range_sh[1] = a.n_units;
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_sh;
+    const int u_begin = range_sh[0], u_end = range_sh[1];
+    const int u_step = a.ares ? 1 : (int)gridDim.x;
+    uint8_t* ares_base = smem;                                  // A-resident mode: A chunks ...
+    uint8_t* bst_base = smem + IMG_ARES_MAX * TI_ACHUNK;        // ... then the B stages
 
     if (warp == 0) {
         if (lane == 0) {
-            // ---------------- bulk-copy producer: B always, A when it comes from an image
+            // ---------------- bulk-copy producer
             uint32_t it = 0;
             bool ok = true;
             TiCursor cu;
-            cu.init(a);
-            for (; cu.valid() && ok; cu.advance()) {
+            cu.init(a, u_begin, u_end, u_step);
+            if (a.ares) {
+                // A-resident: load a run's A chunks once, then stream the B chunks of its tiles
+                int run = -1;
+                int64_t key_img = -1;
+                int key_m0 = -1;
+                for (; cu.valid() && ok; cu.advance()) {
+                    cu.prefetch();
+                    const ImgUnit U = cu.cur;
+                    const ImgSeg S = cu.first_cur;
+                    const int gA0 = U.m0 >> 3, gB0 = U.n0 >> 3;
+                    if (S.a_img != key_img || U.m0 != key_m0) {
+                        if (run >= 0 && !ti_wait(smem_u32(&bar_ares_empty), (uint32_t)run & 1u, abort_flag)) {
+                            ok = false;
+                            break;
+                        }
+                        ++run;
+                        key_img = S.a_img;
+                        key_m0 = U.m0;
+                        const uint32_t bA = (uint32_t)min(16, S.a_G - gA0) * 512u;
+                        const uint32_t fa = smem_u32(&bar_ares_full);
+                        mbar_expect_tx(fa, 3u * bA * (uint32_t)S.kc);
+                        for (int c = 0; c < S.kc; ++c)
+#pragma unroll
+                            for (int sl = 0; sl < 3; ++sl)
+                                bulk_g2s(smem_u32(ares_base + c * TI_ACHUNK + sl * TI_SLICE),
+                                         a.img + S.a_img + ((int64_t)(c * 3 + sl) * S.a_G + gA0) * 512, bA, fa);
+                    }
+                    const uint8_t* bbase = (S.flags & IMG_B_CONST) ? a.cimg : a.img;
+                    const uint32_t bB = (uint32_t)min(U.nt >> 3, S.b_G - gB0) * 512u;
+                    for (int c = 0; c < S.kc; ++c, ++it) {
+                        const uint32_t st = it % (uint32_t)TI_NSB, ph = (it / (uint32_t)TI_NSB) & 1u;
+                        if (!ti_wait(smem_u32(&bar_empty[st]), ph ^ 1u, abort_flag)) { ok = false; break; }
+                        const uint32_t fb = smem_u32(&bar_full[st]);
+                        mbar_expect_tx(fb, 3u * bB);
+#pragma unroll
+                        for (int sl = 0; sl < 3; ++sl)
+                            bulk_g2s(smem_u32(bst_base + st * TI_ACHUNK + sl * TI_SLICE),
+                                     bbase + S.b_img + ((int64_t)(c * 3 + sl) * S.b_G + gB0) * 512, bB, fb);
+                    }
+                }
+                if (!ok) { *abort_flag = 1; atomicExch(&g_tc_status, 2); }
+                // the latest copies of every stage and of the resident A must have landed
+                for (uint32_t k = 0; k < (uint32_t)TI_NSB && k < it; ++k) {
+                    const uint32_t j = it - 1 - k;
+                    if (!ti_wait(smem_u32(&bar_full[j % TI_NSB]), (j / TI_NSB) & 1u, nullptr)) atomicExch(&g_tc_status, 2);
+                }
+                if (run >= 0 && !ti_wait(smem_u32(&bar_ares_full), (uint32_t)run & 1u, nullptr))
+                    atomicExch(&g_tc_status, 2);
+            }
+            for (; !a.ares && cu.valid() && ok; cu.advance()) {
                 cu.prefetch();
                 const ImgUnit U = cu.cur;
                 const int gA0 = U.m0 >> 3, gB0 = U.n0 >> 3;
@@ -786,33 +760,32 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                 for (int s = U.s_begin; s < U.s_end && ok; ++s) {
                     const ImgSeg S = Sn;
                     if (s + 1 < U.s_end) Sn = a.segs[s + 1];
-                    const bool a_img = !(S.flags & IMG_A_SPLIT);
                     const uint8_t* bbase = (S.flags & IMG_B_CONST) ? a.cimg : a.img;
-                    const uint32_t bA = a_img ? (uint32_t)min(16, S.a_G - gA0) * 512u : 0u;
+                    const uint32_t bA = (uint32_t)min(16, S.a_G - gA0) * 512u;
                     const uint32_t bB = (uint32_t)min(U.nt >> 3, S.b_G - gB0) * 512u;
                     for (int c = 0; c < S.kc; ++c, ++it) {
-                        const uint32_t st = it % (uint32_t)a.ns, ph = (it / (uint32_t)a.ns) & 1u;
+                        const uint32_t st = it % (uint32_t)TI_NS, ph = (it / (uint32_t)TI_NS) & 1u;
                         if (!ti_wait(smem_u32(&bar_empty[st]), ph ^ 1u, abort_flag)) { ok = false; break; }
                         const uint32_t fb = smem_u32(&bar_full[st]);
                         mbar_expect_tx(fb, 3u * (bA + bB));
                         const uint32_t dst = smem_u32(smem + st * TI_STAGE);
 #pragma unroll
                         for (int sl = 0; sl < 3; ++sl) {
-                            if (a_img)
-                                bulk_g2s(dst + sl * TI_SLICE,
-                                         a.img + S.a_img + ((int64_t)(c * 3 + sl) * S.a_G + gA0) * 512, bA, fb);
+                            bulk_g2s(dst + sl * TI_SLICE,
+                                     a.img + S.a_img + ((int64_t)(c * 3 + sl) * S.a_G + gA0) * 512, bA, fb);
                             bulk_g2s(dst + (3 + sl) * TI_SLICE,
                                      bbase + S.b_img + ((int64_t)(c * 3 + sl) * S.b_G + gB0) * 512, bB, fb);
                         }
                     }
                 }
             }
-            if (!ok) { *abort_flag = 1; atomicExch(&g_tc_status, 2); }
-            // the copies of every stage's latest round must have landed before the CTA exits
-            for (uint32_t k = 0; k < (uint32_t)a.ns && k < it; ++k) {
-                const uint32_t j = it - 1 - k;
-                if (!ti_wait(smem_u32(&bar_full[j % (uint32_t)a.ns]), (j / (uint32_t)a.ns) & 1u, nullptr))
-                    atomicExch(&g_tc_status, 2);
+            if (!a.ares) {
+                if (!ok) { *abort_flag = 1; atomicExch(&g_tc_status, 2); }
+                // the copies of every stage's latest round must have landed before the CTA exits
+                for (uint32_t k = 0; k < (uint32_t)TI_NS && k < it; ++k) {
+                    const uint32_t j = it - 1 - k;
+                    if (!ti_wait(smem_u32(&bar_full[j % TI_NS]), (j / TI_NS) & 1u, nullptr)) atomicExch(&g_tc_status, 2);
+                }
             }
         }
     } else if (warp == 1) {
@@ -821,8 +794,57 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
             uint32_t it = 0, sc = 0;
             bool ok = true;
             TiCursor cu;
-            cu.init(a);
-            for (; cu.valid() && ok; cu.advance()) {
+            cu.init(a, u_begin, u_end, u_step);
+            if (a.ares) {
+                int run = -1;
+                int64_t key_img = -1;
+                int key_m0 = -1;
+                for (; cu.valid() && ok; cu.advance()) {
+                    cu.prefetch();
+                    const ImgUnit U = cu.cur;
+                    const ImgSeg S = cu.first_cur;
+                    const uint32_t idesc = make_idesc(1u, TC_BM, U.nt);
+                    if (S.a_img != key_img || U.m0 != key_m0) {
+                        ++run;
+                        key_img = S.a_img;
+                        key_m0 = U.m0;
+                        if (!ti_wait(smem_u32(&bar_ares_full), (uint32_t)run & 1u, abort_flag)) { ok = false; break; }
+                    }
+                    const uint32_t b = sc & 1u;
+                    if (!ti_wait(smem_u32(&bar_acce[b]), ((sc >> 1) & 1u) ^ 1u, abort_flag)) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t d = tmem + b * 128u;
+                    for (int c = 0; c < S.kc; ++c, ++it) {
+                        const uint32_t st = it % (uint32_t)TI_NSB, ph = (it / (uint32_t)TI_NSB) & 1u;
+                        if (!ti_wait(smem_u32(&bar_full[st]), ph, abort_flag)) { ok = false; break; }
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        const uint32_t a0 = smem_u32(ares_base + c * TI_ACHUNK), b0 = smem_u32(bst_base + st * TI_ACHUNK);
+#pragma unroll
+                        for (int kk = 0; kk < 2; ++kk) {
+#pragma unroll
+                            for (int p = 0; p < 6; ++p) {
+                                const int ia = p == 2 ? 1 : p == 4 ? 1 : p == 5 ? 2 : 0;
+                                const int ib = p == 1 ? 1 : p == 3 ? 2 : p == 4 ? 1 : 0;
+                                const uint64_t da = make_sdesc(a0 + ia * TI_SLICE + kk * 256, 128, 512);
+                                const uint64_t db = make_sdesc(b0 + ib * TI_SLICE + kk * 256, 128, 512);
+                                const uint32_t accum = (c == 0 && kk == 0 && p == 0) ? 0u : 1u;
+                                asm volatile(
+                                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+                                    :: "r"(d), "l"(da), "l"(db), "r"(idesc), "r"(accum));
+                            }
+                        }
+                        mma_commit(smem_u32(&bar_empty[st]));
+                    }
+                    if (!ok) break;
+                    mma_commit(smem_u32(&bar_accf[b]));
+                    ++sc;
+                    // the run ends here when the next tile reads another A tile: release the resident A
+                    if (!cu.has_next() || cu.first_nxt.a_img != key_img || cu.nxt.m0 != key_m0)
+                        mma_commit(smem_u32(&bar_ares_empty));
+                }
+            }
+            for (; !a.ares && cu.valid() && ok; cu.advance()) {
                 cu.prefetch();
                 const ImgUnit U = cu.cur;
                 const uint32_t idesc = make_idesc(1u, TC_BM, U.nt);
@@ -835,7 +857,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t d = tmem + b * 128u;
                     for (int c = 0; c < kc; ++c, ++it) {
-                        const uint32_t st = it % (uint32_t)a.ns, ph = (it / (uint32_t)a.ns) & 1u;
+                        const uint32_t st = it % (uint32_t)TI_NS, ph = (it / (uint32_t)TI_NS) & 1u;
                         if (!ti_wait(smem_u32(&bar_full[st]), ph, abort_flag)) { ok = false; break; }
                         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                         const uint32_t a0 = smem_u32(smem + st * TI_STAGE), b0 = a0 + 3 * TI_SLICE;
@@ -866,7 +888,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
             mma_commit(smem_u32(&bar_fin));
             if (!ti_wait(smem_u32(&bar_fin), 0u, nullptr)) atomicExch(&g_tc_status, 2);
         }
-    } else if (warp < 10) {
+    } else {
         // ---------------- epilogue: warps 2..9; TMEM lanes 32*(warp%4).., columns 64*h..
         // Each finished segment is scaled by its coefficient and added into the
         // tile's compensated FP32 sum (Knuth two-sum; hi and lo kept in TMEM).
@@ -876,7 +898,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
         uint32_t sc = 0;
         bool ok = true;
         TiCursor cu;
-        cu.init(a);
+        cu.init(a, u_begin, u_end, u_step);
         ImgOut On = a.outs[cu.cur.out];
         for (; cu.valid() && ok; cu.advance()) {
             cu.prefetch();
@@ -893,6 +915,37 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                 for (int j = 0; j < 16; ++j) z[j] = 0.0f;
                 for (int c16 = 0; c16 < 4; ++c16)
                     if (c16 * 16 < ncw) ti_store16(a, O, U, i0, lane, h * 64 + c16 * 16, z, z, stg);
+                continue;
+            }
+            if (U.s_end - U.s_begin == 1) {
+                // one segment: no running sum; TMEM loads are issued two at a time
+                const float alpha = alpha_n;
+                const uint32_t b = sc & 1u;
+                ok = __all_sync(0xffffffffu, ti_wait(smem_u32(&bar_accf[b]), (sc >> 1) & 1u, abort_flag));
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+                for (int c32 = 0; c32 < 4; c32 += 2) {
+                    if (c32 * 16 >= ncw) break;
+                    uint32_t r2[2][16];
+#pragma unroll
+                    for (int q2 = 0; q2 < 2; ++q2)
+                        if ((c32 + q2) * 16 < ncw) tmem_ld16(lane_base + b * 128u + (uint32_t)((c32 + q2) * 16), r2[q2]);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                    for (int q2 = 0; q2 < 2; ++q2) {
+                        if ((c32 + q2) * 16 < ncw) {
+                            float hi[16], lo[16];
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) { hi[j] = alpha * __uint_as_float(r2[q2][j]); lo[j] = 0.0f; }
+                            ti_store16(a, O, U, i0, lane, h * 64 + (c32 + q2) * 16, hi, lo, stg);
+                        }
+                    }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&bar_acce[b]));
+                ++sc;
                 continue;
             }
             for (int s = U.s_begin; s < U.s_end; ++s) {
@@ -948,56 +1001,6 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
             }
         }
         if (!ok && lane == 0) { *abort_flag = 1; atomicExch(&g_tc_status, 2); }
-    } else {
-        // ---------------- A-split producers: warps 10..13.  Thread r (0..127)
-        // owns row m0 + r of every split A chunk.  A loader position runs
-        // TI_RS - 1 chunks ahead of the splitter: it requests the chunk's 32
-        // values of row r with asynchronous 4-byte copies into a raw FP32 ring
-        // in shared memory (no registers held while they are in flight); the
-        // splitter waits for its own copies, splits the row into three BF16
-        // slices and stores them in the stage in the canonical K-major layout.
-        // Each thread reads back only what it copied itself.
-        const int r = tid - 10 * 32;
-        float* rawbase = (float*)(smem + a.ns * TI_STAGE);
-        uint32_t it = 0;
-        bool ok = true;
-        ChunkIt ld, sp;
-        ld.init(a);
-        sp.init(a);
-        uint32_t li = 0;  // chunks requested by the loader
-        for (; li < (uint32_t)(TI_RS - 1) && ld.valid; ++li) {
-            ti_request_raw(a, ld, r, rawbase + (li % TI_RS) * (TI_RAW / 4));
-            asm volatile("cp.async.commit_group;" ::: "memory");
-            ld.next(a);
-        }
-        for (; li < (uint32_t)(TI_RS - 1); ++li) asm volatile("cp.async.commit_group;" ::: "memory");
-        for (; sp.valid && ok; ++it) {
-            if (ld.valid) {
-                ti_request_raw(a, ld, r, rawbase + (li % TI_RS) * (TI_RAW / 4));
-                ld.next(a);
-            }
-            asm volatile("cp.async.commit_group;" ::: "memory");
-            ++li;
-            asm volatile("cp.async.wait_group %0;" :: "n"(TI_RS - 1) : "memory");
-            const uint32_t st = it % (uint32_t)a.ns, ph = (it / (uint32_t)a.ns) & 1u;
-            ok = __all_sync(0xffffffffu, ti_wait(smem_u32(&bar_empty[st]), ph ^ 1u, abort_flag));
-            if (!ok) break;
-            if (sp.S.flags & IMG_A_SPLIT) {
-                const float* raw = rawbase + (it % TI_RS) * (TI_RAW / 4);
-                float v[32];
-#pragma unroll
-                for (int k = 0; k < 32; ++k) v[k] = raw[k * 128 + r];
-                uint8_t* sa = smem + st * TI_STAGE + (r >> 3) * 512 + (r & 7) * 16;
-#pragma unroll
-                for (int qq = 0; qq < 4; ++qq) put_vec<QCM_PREC_BF16X3>(sa + qq * 128, 0, TI_SLICE, v + 8 * qq);
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(smem_u32(&bar_full[st]));
-            sp.next(a);
-        }
-        asm volatile("cp.async.wait_all;" ::: "memory");
-        if (!ok && lane == 0) { *abort_flag = 1; atomicExch(&g_tc_status, 2); }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -1041,15 +1044,12 @@ int tc_img_launch(const Stage& st, double* const* bufs, uint32_t f32mask, void* 
     a.outs = (const ImgOut*)st.d_iout;
     a.img = img;
     a.cimg = (const uint8_t*)st.d_icimg;
-    a.panels = (const ImgPanel*)st.d_ipanel;
-    a.gather = (const int64_t*)st.d_igather;
+    a.ares = t.ares ? 1 : 0;
+    a.cost = (const int64_t*)st.d_icost;
     a.coltab = (const int64_t*)st.d_icoltab;
     for (int i = 0; i < QCM_NBUF; ++i) a.p[i] = bufs[i];
     a.f32mask = f32mask;
     a.n_units = (int32_t)t.units.size();
-    bool any_split = false;
-    for (const ImgSeg& sg : t.segs) any_split |= (sg.flags & IMG_A_SPLIT) != 0;
-    a.ns = any_split ? TI_NS_SPLIT : TI_NS;
     const int grid = (int)std::min<size_t>(t.units.size(), (size_t)sm_count_of_current_device());
     tc_img_kernel<<<grid, TI_THREADS, TI_SMEM, s>>>(a);
     e = cudaGetLastError();

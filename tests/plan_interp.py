@@ -87,7 +87,7 @@ def run_gemm_images(tab, bufs, image_bytes):
     for pn in tab["panels"]:
         src_off, img_off, src_buf, ld, R, K, kcontig, G = [int(x) for x in pn]
         if img_off < 0:
-            continue   # read and split inside the block-product kernel
+            continue   # a panel no segment reads from an image
         kc = (K + 31) // 32
         r = np.arange(G * 8)[:, None]
         k = np.arange(kc * 32)[None, :]
@@ -113,11 +113,7 @@ def run_gemm_images(tab, bufs, image_bytes):
                 A = np.full((3, 128, 32), np.nan)
                 B = np.full((3, nt, 32), np.nan)
                 for sl in range(3):
-                    if flags & 1:   # A split in the kernel: all 128 rows from the source panel
-                        A[sl] = panel_values(tab["panels"][a_panel], m0 + np.arange(128)[:, None],
-                                             (a_c0 + c) * 32 + kk) if sl == 0 else 0.0
-                    else:
-                        A[sl, :ngA * 8] = img[slot(a_img, a_G, c, sl, m0 + ra, kk)]
+                    A[sl, :ngA * 8] = img[slot(a_img, a_G, c, sl, m0 + ra, kk)]
                     B[sl, :ngB * 8] = bsrc[slot(b_img, b_G, c, sl, n0 + rb, kk)]
                 for ia, ib in PAIRS:
                     D += A[ia] @ B[ib].T

@@ -1,0 +1,106 @@
+"""Edge cases of the plan builder and executors: the smallest problems (one
+orbital pair, 1x1 blocks), sigma of a zero vector, oversized blocks, null and
+out-of-range arguments, and a problem run through every precision form.
+
+The CPU cases check the plan builder and the C ABI's argument checks; the GPU
+cases (marked) run the executors on the same inputs."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from qcmaquis_gb300 import native as N
+
+from oracle import dmrg_ref as R
+from plan_interp import run_plan
+from test_oracle import _random_site_problem
+
+
+def _plan(psi, left, right, ts, herm=True):
+    psi = psi.copy().make_left_paired()
+    lay = N.Layout.of(psi.data)
+    Ll, Rl = N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
+    return psi, lay, Ll, Rl, N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, N.FMpo(ts), herm)
+
+
+def test_smallest_problem_plan_matches_oracle():
+    """L=2, N=2 (the H2 case of the reference's tests): every block is tiny."""
+    psi, left, right, ts = _random_site_problem(L=2, N=2, m=4, site=0)
+    psi, lay, Ll, Rl, p = _plan(psi, left, right, ts)
+    bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.zeros(p.out_elems)] + \
+        [np.full(max(s, 1), np.nan) for s in p.scratch]
+    run_plan(p, bufs, images=True)
+    ref = lay.pack(R.site_hamil2(psi, left, right, ts).data)
+    assert np.linalg.norm(bufs[3] - ref) <= 1e-7 * np.linalg.norm(ref)
+
+
+def test_sigma_of_zero_vector_is_zero():
+    psi, left, right, ts = _random_site_problem(m=16)
+    psi, lay, Ll, Rl, p = _plan(psi, left, right, ts)
+    bufs = [np.zeros(lay.size), Ll.pack(left), Rl.pack(right), np.full(p.out_elems, np.nan)] + \
+        [np.full(max(s, 1), np.nan) for s in p.scratch]
+    run_plan(p, bufs)
+    assert np.all(bufs[3] == 0.0)
+
+
+def test_oversized_block_is_rejected():
+    """Blocks of 2^31 elements or more are refused (the executors use 32-bit in-block offsets)."""
+    psi, left, right, ts = _random_site_problem(m=8)
+    psi = psi.copy().make_left_paired()
+    lay = N.Layout.of(psi.data)
+    shapes = list(lay.shapes)
+    shapes[0] = (1 << 16, 1 << 15)
+    big = N.Layout(lay.keys, shapes)
+    with pytest.raises(RuntimeError):
+        N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, big, N.BoundaryLayout.of(left),
+                     N.BoundaryLayout.of(right), N.FMpo(ts))
+
+
+def test_null_and_out_of_range_arguments_are_rejected():
+    lib = N.lib()
+    assert lib.qcm_plan_sigma(None, None, None, None, None, None, None, 1, None) == -1
+    assert lib.qcm_plan_sizes(None, None, None) == -1
+    psi, left, right, ts = _random_site_problem(m=8)
+    _, _, _, _, p = _plan(psi, left, right, ts)
+    cnt = np.zeros(4, dtype=np.int64)
+    rc = lib.qcm_plan_stage_images(p.h, 99, cnt.ctypes.data_as(C.POINTER(C.c_int64)), None, None, None, None, None)
+    assert rc == -5
+    assert "range" in lib.qcm_last_error().decode()
+    # more vectors than the allocation-free dot product holds
+    out = C.c_double()
+    rc = lib.qcm_multi_dot_noalloc(None, 33, None, 0, C.byref(out), None)
+    assert rc in (-1, -5)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,N_,m,site", [(2, 2, 4, 0), (6, 6, 16, 2)])
+def test_small_problems_every_precision_on_gpu(L, N_, m, site):
+    """Tiny blocks through the FP64, TF32, BF16x3 (images) and BF16x3 (in-kernel split) executors."""
+    import torch
+    from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
+    psi, left, right, ts = _random_site_problem(L=L, N=N_, m=m, site=site)
+    psi = psi.copy().make_left_paired()
+    ref = N.Layout.of(psi.data).pack(R.site_hamil2(psi, left, right, ts).data)
+    eng = Engine("cuda:0")
+    x, Lb, Rb = DeviceMPSTensor.from_host(psi), DeviceBoundary.from_host(left), DeviceBoundary.from_host(right)
+    nref = np.linalg.norm(ref)
+    for prec, images, tol in [(N.PREC_FP64, True, 1e-12), (N.PREC_TF32, True, 5e-3),
+                              (N.PREC_BF16X3, True, 2e-5), (N.PREC_BF16X3, False, 2e-5)]:
+        eng.use_images = images
+        got = eng.site_hamil2(x, Lb, Rb, ts, precision=prec).data.cpu().numpy()
+        assert np.linalg.norm(got - ref) <= tol * nref, (prec, images)
+
+
+@pytest.mark.gpu
+def test_zero_vector_on_gpu():
+    import torch
+    from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
+    psi, left, right, ts = _random_site_problem(m=16)
+    psi = psi.copy().make_left_paired()
+    x = DeviceMPSTensor.from_host(psi)
+    x.data.zero_()
+    eng = Engine("cuda:0")
+    for prec in (N.PREC_FP64, N.PREC_BF16X3):
+        got = eng.site_hamil2(x, DeviceBoundary.from_host(left), DeviceBoundary.from_host(right), ts,
+                              precision=prec).data
+        assert torch.count_nonzero(got).item() == 0

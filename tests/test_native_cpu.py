@@ -47,8 +47,9 @@ def test_sigma_plan_matches_oracle(herm, site, m):
     lay = N.Layout.of(psi.data)
     Ll, Rl = N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
     p = N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, N.FMpo(ts), herm)
+    # scratch starts as NaN: a read of scratch that no stage wrote shows in sigma
     bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.zeros(p.out_elems)] + \
-        [np.zeros(max(s, 1)) for s in p.scratch]
+        [np.full(max(s, 1), np.nan) for s in p.scratch]
     run_plan(p, bufs)
     ref = lay.pack(R.site_hamil2(psi, left, right, ts, is_hermitian=herm).data)
     assert np.linalg.norm(bufs[3] - ref) <= 1e-13 * np.linalg.norm(ref)
@@ -69,7 +70,7 @@ def test_sigma_image_tables_match_oracle(L, m, site, herm):
     tiles = [len(p.stage_images(i)["tiles"]) for i, k in enumerate(p.stage_kinds()) if k == "gemm"]
     assert all(t > 0 for t in tiles)
     bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.zeros(p.out_elems)] + \
-        [np.zeros(max(s, 1)) for s in p.scratch]
+        [np.full(max(s, 1), np.nan) for s in p.scratch]
     run_plan(p, bufs, images=True)
     ref = lay.pack(R.site_hamil2(psi, left, right, ts, is_hermitian=herm).data)
     assert np.linalg.norm(bufs[3] - ref) <= 1e-7 * np.linalg.norm(ref)
