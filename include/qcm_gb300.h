@@ -155,6 +155,10 @@ int qcm_plan_sizes(const qcm_plan* plan, int64_t* out_elems, int64_t* scratch_el
  * kernel instead (same results, slower). */
 int qcm_plan_image_bytes(const qcm_plan* plan, int64_t* bytes);
 
+/* Number of kernels the plan's last run launched (memsets excluded): the
+ * executors chosen depend on the precision and on the image buffer. */
+int qcm_plan_last_kernels(const qcm_plan* plan, int32_t* n);
+
 /* Work counters: algorithmic FLOPs of the block products, FLOPs and bytes of the
  * gather/axpy stages, and the number of kernel launches of one run. */
 int qcm_plan_work(const qcm_plan* plan, double* gemm_flops, double* axpy_flops, double* axpy_bytes,

@@ -605,6 +605,22 @@ static int launch_gemm(const Stage& st, const BufTable& bt, int precision, cudaS
     return QCM_OK;
 }
 
+// Kernels one stage launches on the path launch_axpy / launch_gemm take.
+static int stage_kernels(const Stage& st, const BufTable& bt, int precision) {
+    const bool images = precision == QCM_PREC_BF16X3 && bt.p[QCM_BUF_IMG] && st.d_iunit;
+    if (st.kind == ST_AXPY) {
+        if (st.n_work == 0) return 0;
+        if (images && st.src_buf >= 0 && st.n_cw > 0)
+            return (st.n_cw_light > 0 ? 1 : 0) + (st.img.build.empty() ? 0 : 1) + 1;
+        return 1;
+    }
+    if (st.kind == ST_GEMM) {
+        if (st.n_work == 0) return 0;
+        return images ? (st.img.build.empty() ? 0 : 1) + 1 : 1;
+    }
+    return 0;
+}
+
 // ------------------------------------------------------------------ vector kernels
 constexpr int RED_THREADS = 256;
 constexpr int RED_BLOCKS = 304;  // 2 x 152 SMs
@@ -790,9 +806,11 @@ int qcm_plan_run_typed(qcm_plan* p, double* const* bufs, uint32_t f32mask, int32
     for (int i = 0; i < QCM_NBUF; ++i) bt.p[i] = bufs[i];
     bt.f32mask = f32mask;
     cudaStream_t s = (cudaStream_t)stream;
+    p->last_kernels = 0;
     for (int32_t si = first; si <= last; ++si) {
         Stage& st = p->stages[si];
         int rc = QCM_OK;
+        p->last_kernels += stage_kernels(st, bt, precision);
         if (st.kind == ST_ZERO) {
             if (st.zlen > 0) {
                 if (!bufs[st.zbuf]) { set_error("missing scratch buffer"); return QCM_E_INVALID; }

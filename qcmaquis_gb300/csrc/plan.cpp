@@ -1047,8 +1047,9 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
 
 // Image tables of one GEMM stage.  Each output is computed as a D tile of
 // the MMA with the larger of (M, N) on the 128-row MMA side: when N > M the
-// stage's C = op(A) op(B) is computed as C^T = op(B)^T op(A)^T.  Panels that
-// several segments read with the same orientation share one image.
+// stage's C = op(A) op(B) is computed as C^T = op(B)^T op(A)^T (less padding;
+// the other choice, with coalesced column stores, was measured slower for K1).
+// Panels that several segments read with the same orientation share one image.
 void build_image_tables(const Stage& st, ImgTables& t) {
     t = ImgTables();
     struct Key {
@@ -1142,13 +1143,16 @@ void build_image_tables(const Stage& st, ImgTables& t) {
             t.segs.push_back(s);
         }
         const int32_t s_end = (int32_t)t.segs.size();
+        // N tiles of balanced width (multiples of 16, at most 128): e.g. 160 = 80 + 80
+        const int32_t nnt = (io.ncols + 127) / 128;
+        const int32_t per = ((io.ncols + nnt - 1) / nnt + 15) / 16 * 16;
         for (int32_t m0 = 0; m0 < io.mrows; m0 += 128)
-            for (int32_t n0 = 0; n0 < io.ncols; n0 += 128) {
+            for (int32_t n0 = 0; n0 < io.ncols; n0 += per) {
                 ImgUnit u;
                 u.out = oid;
                 u.m0 = m0;
                 u.n0 = n0;
-                u.nt = std::min(128, (io.ncols - n0 + 15) / 16 * 16);
+                u.nt = std::min(per, (io.ncols - n0 + 15) / 16 * 16);
                 u.s_begin = s_begin;
                 u.s_end = s_end;
                 t.units.push_back(u);
@@ -1454,6 +1458,12 @@ int qcm_plan_stage_image_aux(const qcm_plan* p, int32_t stage, int64_t* counts, 
     if (gather && !t.gather.empty()) std::memcpy(gather, t.gather.data(), t.gather.size() * 8);
     if (coltab && !t.coltab.empty()) std::memcpy(coltab, t.coltab.data(), t.coltab.size() * 8);
     if (cimg && !t.cimg.empty()) std::memcpy(cimg, t.cimg.data(), t.cimg.size());
+    return QCM_OK;
+}
+
+int qcm_plan_last_kernels(const qcm_plan* p, int32_t* n) {
+    if (!p || !n) { set_error("null argument"); return QCM_E_INVALID; }
+    *n = p->last_kernels;
     return QCM_OK;
 }
 

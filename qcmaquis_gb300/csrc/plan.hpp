@@ -206,6 +206,7 @@ struct qcm_plan {
     int64_t out_elems = 0;
     int64_t scratch[3] = {0, 0, 0};
     int64_t image_bytes = 0;  // image buffer of the BF16x3 image executor
+    int32_t last_kernels = 0; // kernels the last run launched (memsets excluded)
     // output boundary layout (boundary plans)
     std::vector<int32_t> out_blk_ptr;
     std::vector<qcm::Blk> out_blocks;

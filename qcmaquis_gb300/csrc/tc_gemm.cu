@@ -466,6 +466,14 @@ __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(mbar) : "memory");
 }
 
+// Arrive without release semantics.  The epilogue signals with it that its TMEM
+// reads of an accumulator are complete (tcgen05.wait::ld / wait::st precede
+// it); a release arrive would also wait until all of the warp's earlier global
+// stores of output tiles are acknowledged, which serialised the epilogue.
+__device__ __forceinline__ void mbar_arrive_relaxed(uint32_t mbar) {
+    asm volatile("mbarrier.arrive.relaxed.cta.shared::cta.b64 _, [%0];" :: "r"(mbar) : "memory");
+}
+
 __device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(mbar), "r"(bytes) : "memory");
 }
@@ -617,21 +625,34 @@ __device__ __forceinline__ void ti_store16(const TiArgs& a, const ImgOut& O, con
     } else {
         // rows i lie O.si apart in memory and columns are contiguous: pass the
         // 32 x 16 block through shared memory so that 16 lanes store one row run
+        // explicit shared-space accesses (ld/st.shared), so that they need no
+        // ordering against the warp's outstanding global stores
+        const uint32_t sbase = smem_u32(stg);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) stg[lane * TI_EPI_LD + j] = hi[j] + lo[j];
+        for (int j = 0; j < 16; ++j)
+            asm volatile("st.shared.f32 [%0], %1;" :: "r"(sbase + (uint32_t)((lane * TI_EPI_LD + j) * 4)),
+                         "f"(hi[j] + lo[j]) : "memory");
         __syncwarp();
-        const int jj = lane & 15;
+        const int jj = lane & 15, r0 = lane >> 4;
         const int col = U.n0 + cbase + jj;
-        for (int rr = lane >> 4; rr < 32; rr += 2) {
-            const int i = i0 + rr;
-            if (i < O.mrows && col < O.ncols) {
-                const int64_t off = (int64_t)i * O.si + col;
-                const float v = stg[rr * TI_EPI_LD + jj];
-                if (c32) C32[off] = v;
-                else C64[off] = (double)v;
+        // all 16 shared-memory reads first, then 16 independent stores
+        float vv[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+            asm volatile("ld.shared.f32 %0, [%1];" : "=f"(vv[k])
+                         : "r"(sbase + (uint32_t)(((2 * k + r0) * TI_EPI_LD + jj) * 4)) : "memory");
+        __syncwarp();
+        if (col < O.ncols) {
+            const int64_t base = (int64_t)(i0 + r0) * O.si + col;
+            const int64_t step = 2 * O.si;
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+                if (i0 + r0 + 2 * k < O.mrows) {
+                    if (c32) C32[base + k * step] = vv[k];
+                    else C64[base + k * step] = (double)vv[k];
+                }
             }
         }
-        __syncwarp();
     }
 }
 
@@ -819,14 +840,16 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                         if (!ti_wait(smem_u32(&bar_full[st]), ph, abort_flag)) { ok = false; break; }
                         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                         const uint32_t a0 = smem_u32(ares_base + c * TI_ACHUNK), b0 = smem_u32(bst_base + st * TI_ACHUNK);
+                        const uint64_t da0 = make_sdesc(a0, 128, 512), db0 = make_sdesc(b0, 128, 512);
 #pragma unroll
                         for (int kk = 0; kk < 2; ++kk) {
 #pragma unroll
                             for (int p = 0; p < 6; ++p) {
                                 const int ia = p == 2 ? 1 : p == 4 ? 1 : p == 5 ? 2 : 0;
                                 const int ib = p == 1 ? 1 : p == 3 ? 2 : p == 4 ? 1 : 0;
-                                const uint64_t da = make_sdesc(a0 + ia * TI_SLICE + kk * 256, 128, 512);
-                                const uint64_t db = make_sdesc(b0 + ib * TI_SLICE + kk * 256, 128, 512);
+                                // start-address field (bits 0-13, address >> 4) advanced by the offset
+                                const uint64_t da = da0 + (uint64_t)((ia * TI_SLICE + kk * 256) >> 4);
+                                const uint64_t db = db0 + (uint64_t)((ib * TI_SLICE + kk * 256) >> 4);
                                 const uint32_t accum = (c == 0 && kk == 0 && p == 0) ? 0u : 1u;
                                 asm volatile(
                                     "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -861,14 +884,16 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                         if (!ti_wait(smem_u32(&bar_full[st]), ph, abort_flag)) { ok = false; break; }
                         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                         const uint32_t a0 = smem_u32(smem + st * TI_STAGE), b0 = a0 + 3 * TI_SLICE;
+                        const uint64_t da0 = make_sdesc(a0, 128, 512), db0 = make_sdesc(b0, 128, 512);
 #pragma unroll
                         for (int kk = 0; kk < 2; ++kk) {
 #pragma unroll
                             for (int p = 0; p < 6; ++p) {
                                 const int ia = p == 2 ? 1 : p == 4 ? 1 : p == 5 ? 2 : 0;
                                 const int ib = p == 1 ? 1 : p == 3 ? 2 : p == 4 ? 1 : 0;
-                                const uint64_t da = make_sdesc(a0 + ia * TI_SLICE + kk * 256, 128, 512);
-                                const uint64_t db = make_sdesc(b0 + ib * TI_SLICE + kk * 256, 128, 512);
+                                // start-address field (bits 0-13, address >> 4) advanced by the offset
+                                const uint64_t da = da0 + (uint64_t)((ia * TI_SLICE + kk * 256) >> 4);
+                                const uint64_t db = db0 + (uint64_t)((ib * TI_SLICE + kk * 256) >> 4);
                                 const uint32_t accum = (c == 0 && kk == 0 && p == 0) ? 0u : 1u;
                                 asm volatile(
                                     "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -944,7 +969,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                 }
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                 __syncwarp();
-                if (lane == 0) mbar_arrive(smem_u32(&bar_acce[b]));
+                if (lane == 0) mbar_arrive_relaxed(smem_u32(&bar_acce[b]));
                 ++sc;
                 continue;
             }
@@ -996,7 +1021,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                 asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                 __syncwarp();
-                if (lane == 0) mbar_arrive(smem_u32(&bar_acce[b]));
+                if (lane == 0) mbar_arrive_relaxed(smem_u32(&bar_acce[b]));
                 ++sc;
             }
         }

@@ -162,7 +162,7 @@ class Engine:
         plan.run_typed([_ptr(ket), _ptr(lt), _ptr(rt), _ptr(out), _ptr(s0), _ptr(s1), _ptr(s2),
                         _ptr(img) if img_elems else 0], mask, prec, self._stream(), first, last)
         if first == 0 and last == -1:
-            self.launches += plan.launches
+            self.launches += plan.last_kernels()
 
     # -- Engine surface ----------------------------------------------------
     def site_hamil2(self, ket: DeviceMPSTensor, L: DeviceBoundary, R: DeviceBoundary, mpo,

@@ -69,6 +69,7 @@ def lib():
                                                                C.POINTER(CMpo), C.c_int32, C.POINTER(C.c_void_p)]
     L.qcm_plan_sizes.argtypes = [C.c_void_p, i64p, i64p]
     L.qcm_plan_image_bytes.argtypes = [C.c_void_p, i64p]
+    L.qcm_plan_last_kernels.argtypes = [C.c_void_p, i32p]
     L.qcm_plan_stage_images.argtypes = [C.c_void_p, C.c_int32, i64p, i64p, i64p, i64p, f64p, i64p]
     L.qcm_plan_stage_image_aux.argtypes = [C.c_void_p, C.c_int32, i64p, i64p, i64p, C.POINTER(C.c_uint8)]
     L.qcm_plan_work.argtypes = [C.c_void_p, f64p, f64p, f64p, i32p]
@@ -344,6 +345,12 @@ class Plan:
             else:
                 out.append(("zero", int(no.value), int(nt.value)))
         return out
+
+    def last_kernels(self) -> int:
+        """Kernels the last run of this plan launched."""
+        n = C.c_int32()
+        check(lib().qcm_plan_last_kernels(self.h, C.byref(n)), "qcm_plan_last_kernels")
+        return n.value
 
     def stage_images(self, stage: int):
         """Export the BF16x3 image-executor tables of a GEMM stage (host-side inspection and tests)."""
