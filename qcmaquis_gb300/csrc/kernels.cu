@@ -299,30 +299,16 @@ static bool build_chunk_work(const Stage& st, std::vector<DevAxpyChunk>& w) {
         for (int64_t t = a.t_begin; t < a.t_end; ++t)
             if (st.aterm[t].lds != a.rows && a.cols > 1) return false;
     }
-    std::vector<int32_t> parent(nO);
-    std::iota(parent.begin(), parent.end(), 0);
-    auto find = [&](int32_t x) {
-        while (parent[x] != x) { parent[x] = parent[parent[x]]; x = parent[x]; }
-        return x;
-    };
-    std::unordered_map<int64_t, int32_t> first_user;
-    first_user.reserve(st.aterm.size() / 4 + 16);
-    for (size_t i = 0; i < nO; ++i) {
-        const AxpyOut& a = st.aout[i];
-        for (int64_t t = a.t_begin; t < a.t_end; ++t) {
-            const int64_t key = ((int64_t)st.aterm[t].src_buf << 56) ^ st.aterm[t].src_off;
-            auto it = first_user.emplace(key, (int32_t)i);
-            if (!it.second) {
-                const int32_t r1 = find((int32_t)i), r2 = find(it.first->second);
-                if (r1 != r2) parent[std::max(r1, r2)] = std::min(r1, r2);
-            }
-        }
+    std::vector<int32_t> rootv;
+    const std::vector<int32_t>* roots = &st.comp_root;
+    if (st.comp_root.size() != nO) {
+        if (!axpy_components(st, rootv)) return false;
+        roots = &rootv;
     }
     // groups in order of their first output; members in output order
     std::vector<int32_t> order(nO);
     std::iota(order.begin(), order.end(), 0);
-    std::vector<int32_t> root(nO);
-    for (size_t i = 0; i < nO; ++i) root[i] = find((int32_t)i);
+    const std::vector<int32_t>& root = *roots;
     std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return root[x] < root[y]; });
     w.clear();
     for (size_t g0 = 0; g0 < nO;) {

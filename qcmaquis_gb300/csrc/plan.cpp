@@ -16,6 +16,7 @@
 // by the output tile it writes, so the device executes every output exactly
 // once without atomics.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -462,22 +463,26 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
                                const PB& out_left_pb, int t_buf, int c_buf, Stage& st, qcm_plan* P, int64_t& end) {
     const qcm_mpo_t* m = W.m;
     std::vector<BM> C(m->col_dim);
-    using TileKey = std::tuple<int, Q, Q, int64_t>;  // b2, out_l, out_r, row offset
+    // tiles of one b2, keyed (out_l, out_r, row offset) in the reference's block order
+    using TileKey = std::tuple<Q, Q, int64_t>;
     struct TileKeyLess {
         bool operator()(const TileKey& a, const TileKey& b) const {
-            if (std::get<0>(a) != std::get<0>(b)) return std::get<0>(a) < std::get<0>(b);
+            if (std::get<0>(a) != std::get<0>(b)) return std::get<0>(a) > std::get<0>(b);
             if (std::get<1>(a) != std::get<1>(b)) return std::get<1>(a) > std::get<1>(b);
-            if (std::get<2>(a) != std::get<2>(b)) return std::get<2>(a) > std::get<2>(b);
-            return std::get<3>(a) < std::get<3>(b);
+            return std::get<2>(a) < std::get<2>(b);
         }
     };
     struct TileVal { int64_t rows, cols; std::vector<AxpyTerm> terms; };
-    std::map<TileKey, TileVal, TileKeyLess> tiles;
-    for (int b2 : b2list) {
+    using TileMap = std::map<TileKey, TileVal, TileKeyLess>;
+    for (int b2 : b2list)
+        if (b2 < 0 || b2 >= m->col_dim) throw std::runtime_error("b2 out of range");
+    for (int e = 0; e < m->col_ptr[m->col_dim]; ++e)
+        if (m->row_of[e] >= (int)T.size()) throw std::runtime_error("mpo row beyond boundary aux dimension");
+    // one b2 column: its contr blocks C[b2] and its tiles (independent of every other b2)
+    auto column = [&](int b2, TileMap& tiles, double& flops) {
         int ap = W.rspin(b2);
         for (int e = m->col_ptr[b2]; e < m->col_ptr[b2 + 1]; ++e) {
             int b1 = m->row_of[e];
-            if (b1 >= (int)T.size()) throw std::runtime_error("mpo row beyond boundary aux dimension");
             int a = W.lspin(b1);
             for (int tt = m->term_ptr[e]; tt < m->term_ptr[e + 1]; ++tt) {
                 int op = m->term_op[tt];
@@ -511,37 +516,67 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
                             int ss1 = m->ent[4 * en], ss2 = m->ent[4 * en + 1];
                             double alfa = m->ent_coeff[en] * cpl[spin_case(m->ent[4 * en + 2], m->ent[4 * en + 3])];
                             if (alfa == 0.0) continue;
-                            TileKey key(b2, out_l, out_r, olo + ss2 * l_size);
-                            auto& tv = tiles[key];
+                            auto& tv = tiles[TileKey(out_l, out_r, olo + ss2 * l_size)];
                             tv.rows = l_size;
                             tv.cols = r_size;
                             tv.terms.push_back({t_buf, tb.off + (iro + (int64_t)ss1 * r_size) * l_size, l_size, alfa});
-                            P->axpy_flops += 2.0 * l_size * r_size;
+                            flops += 2.0 * l_size * r_size;
                         }
                     }
                 }
             }
         }
+    };
+    // the columns are planned by all host threads (dynamic assignment), then
+    // concatenated in b2 order: the result does not depend on the thread count
+    std::vector<TileMap> per(b2list.size());
+    std::vector<double> fl(b2list.size(), 0.0);
+    {
+        std::atomic<size_t> next{0};
+        std::mutex err_mu;
+        std::string err;
+        auto worker = [&]() {
+            for (;;) {
+                const size_t i = next.fetch_add(1);
+                if (i >= b2list.size()) return;
+                try {
+                    column(b2list[i], per[i], fl[i]);
+                } catch (const std::exception& ex) {
+                    std::lock_guard<std::mutex> g(err_mu);
+                    if (err.empty()) err = ex.what();
+                }
+            }
+        };
+        const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        for (unsigned t = 1; t < nt; ++t) pool.emplace_back(worker);
+        worker();
+        for (auto& th : pool) th.join();
+        if (!err.empty()) throw std::runtime_error(err);
     }
     int64_t base = 0;
     for (auto& c : C) base = c.assign_offsets(base);
     end = base;
     st.kind = ST_AXPY;
-    for (auto& kv : tiles) {
-        int b2 = std::get<0>(kv.first);
+    for (size_t i = 0; i < b2list.size(); ++i) {
+        const int b2 = b2list[i];
+        P->axpy_flops += fl[i];
         const BM& cb = C[b2];
-        const Blk& d = cb.b[cb.find(std::get<1>(kv.first), std::get<2>(kv.first))];
-        AxpyOut o;
-        o.dst_buf = c_buf;
-        o.dst_off = d.off + std::get<3>(kv.first);
-        o.ldd = d.rows;
-        o.rows = kv.second.rows;
-        o.cols = kv.second.cols;
-        o.t_begin = (int64_t)st.aterm.size();
-        for (auto& t : kv.second.terms) st.aterm.push_back(t);
-        o.t_end = (int64_t)st.aterm.size();
-        st.aout.push_back(o);
-        P->axpy_bytes += 8.0 * o.rows * o.cols * (double)(kv.second.terms.size() + 1);
+        for (auto& kv : per[i]) {
+            const Blk& d = cb.b[cb.find(std::get<0>(kv.first), std::get<1>(kv.first))];
+            AxpyOut o;
+            o.dst_buf = c_buf;
+            o.dst_off = d.off + std::get<2>(kv.first);
+            o.ldd = d.rows;
+            o.rows = kv.second.rows;
+            o.cols = kv.second.cols;
+            o.t_begin = (int64_t)st.aterm.size();
+            st.aterm.insert(st.aterm.end(), kv.second.terms.begin(), kv.second.terms.end());
+            o.t_end = (int64_t)st.aterm.size();
+            st.aout.push_back(o);
+            P->axpy_bytes += 8.0 * o.rows * o.cols * (double)(kv.second.terms.size() + 1);
+        }
+        per[i].clear();
     }
     return C;
 }
@@ -748,6 +783,7 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
     z2.zlen = 0;  // the zero tiles of K2 clear what K3 reads; the rest of contr is never read
     build_image_tables(s1, s1.img);
     build_image_tables(s3, s3.img);
+    axpy_components(s2, s2.comp_root);
     build_dense_groups(s2, 64, s2.img, s2.heavy);
     P->image_bytes = std::max(std::max(s1.img.bytes, s3.img.bytes), s2.img.bytes);
     P->stages.push_back(std::move(z0));
@@ -1191,33 +1227,75 @@ static float bf16_to_float(uint16_t h) {
     return x;
 }
 
-void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::vector<char>& heavy) {
-    t = ImgTables();
+bool axpy_components(const Stage& st, std::vector<int32_t>& root) {
     const size_t nO = st.aout.size();
-    heavy.assign(nO, 0);
-    if (nO == 0) return;
-    // connected components of the output/source graph
+    for (size_t i = 0; i < nO; ++i) {
+        const AxpyOut& a = st.aout[i];
+        for (int64_t k = a.t_begin; k < a.t_end; ++k)
+            if (st.aterm[k].lds != a.rows && a.cols > 1) return false;
+    }
     std::vector<int32_t> parent(nO);
     for (size_t i = 0; i < nO; ++i) parent[i] = (int32_t)i;
     auto find = [&](int32_t x) {
         while (parent[x] != x) { parent[x] = parent[parent[x]]; x = parent[x]; }
         return x;
     };
-    std::unordered_map<int64_t, int32_t> first_user;
-    first_user.reserve(st.aterm.size() / 4 + 16);
+    // source tile -> first output that reads it: open addressing, linear probing
+    std::vector<int64_t> keys(1u << 16, -1);
+    std::vector<int32_t> vals(1u << 16, 0);
+    size_t used = 0;
+    auto slot = [&](int64_t key) {
+        const size_t mask = keys.size() - 1;
+        size_t h = (size_t)((uint64_t)key * 0x9E3779B97F4A7C15ull >> 17) & mask;
+        while (keys[h] != -1 && keys[h] != key) h = (h + 1) & mask;
+        return h;
+    };
     for (size_t i = 0; i < nO; ++i) {
         const AxpyOut& a = st.aout[i];
         for (int64_t k = a.t_begin; k < a.t_end; ++k) {
-            const AxpyTerm& x = st.aterm[k];
-            if (x.lds != a.rows && a.cols > 1) return;  // sources must be contiguous tiles
-            const int64_t key = ((int64_t)x.src_buf << 56) ^ x.src_off;
-            auto it = first_user.emplace(key, (int32_t)i);
-            if (!it.second) {
-                const int32_t r1 = find((int32_t)i), r2 = find(it.first->second);
+            const int64_t key = ((int64_t)st.aterm[k].src_buf << 56) ^ st.aterm[k].src_off;
+            size_t h = slot(key);
+            if (keys[h] == -1) {
+                keys[h] = key;
+                vals[h] = (int32_t)i;
+                if (2 * ++used > keys.size()) {  // grow and rehash
+                    std::vector<int64_t> ok;
+                    std::vector<int32_t> ov;
+                    ok.swap(keys);
+                    ov.swap(vals);
+                    keys.assign(ok.size() * 2, -1);
+                    vals.assign(ok.size() * 2, 0);
+                    for (size_t q = 0; q < ok.size(); ++q)
+                        if (ok[q] != -1) {
+                            const size_t g = slot(ok[q]);
+                            keys[g] = ok[q];
+                            vals[g] = ov[q];
+                        }
+                }
+            } else {
+                const int32_t r1 = find((int32_t)i), r2 = find(vals[h]);
                 if (r1 != r2) parent[std::max(r1, r2)] = std::min(r1, r2);
             }
         }
     }
+    root.resize(nO);
+    for (size_t i = 0; i < nO; ++i) root[i] = find((int32_t)i);
+    return true;
+}
+
+void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::vector<char>& heavy) {
+    t = ImgTables();
+    const size_t nO = st.aout.size();
+    heavy.assign(nO, 0);
+    if (nO == 0) return;
+    // connected components of the output/source graph
+    std::vector<int32_t> rootv;
+    const std::vector<int32_t>* roots = &st.comp_root;
+    if (st.comp_root.size() != nO) {
+        if (!axpy_components(st, rootv)) return;  // sources must be contiguous tiles
+        roots = &rootv;
+    }
+    auto find = [&](int32_t x) { return (*roots)[x]; };
     // candidate groups: (component, rows, cols, dst_buf, src_buf) over heavy outputs
     std::map<std::tuple<int32_t, int64_t, int64_t, int32_t, int32_t>, std::vector<int32_t>> groups;
     for (size_t i = 0; i < nO; ++i) {

@@ -153,6 +153,10 @@ void build_image_tables(const struct Stage& st, ImgTables& t);
 // contr[:, group] = T_gathered . W^T on the tensor cores.  heavy[o] marks the
 // outputs taken.
 void build_dense_groups(const struct Stage& st, int64_t min_terms, ImgTables& t, std::vector<char>& heavy);
+// Connected components of a gather-axpy stage's output/source graph (outputs
+// that share a source tile, transitively): root[i] = smallest output of i's
+// component.  Returns false when some term's source is not a contiguous tile.
+bool axpy_components(const struct Stage& st, std::vector<int32_t>& root);
 
 struct Stage {
     int kind;
@@ -178,6 +182,7 @@ struct Stage {
     // GEMM: tables of the BF16x3 image executor; AXPY: its dense groups
     ImgTables img;
     std::vector<char> heavy;     // AXPY: outputs computed by the dense groups
+    std::vector<int32_t> comp_root;  // AXPY: connected components (axpy_components), when computed
     void* d_igather = nullptr;
     void* d_icoltab = nullptr;
     void* d_icimg = nullptr;
