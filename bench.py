@@ -34,6 +34,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="bf16x3", choices=["fp64", "tf32", "bf16x3"])
+    ap.add_argument("--sweep", action="store_true",
+                    help="time one full two-site sweep (FP64 and BF16x3 sigma forms) instead of sigma calls")
+    ap.add_argument("--jd-maxiter", type=int, default=10)
+    ap.add_argument("--nsweeps", type=int, default=1, help="--sweep: number of sweeps")
+    ap.add_argument("--ramp", default="", help="--sweep: bond dimension per sweep, e.g. 256,256,512,512,1024,1024")
     ap.add_argument("--no-images", action="store_true",
                     help="BF16x3: split operands inside the block-product kernel instead of pre-split images")
     ap.add_argument("--compare-steps", type=int, default=2, help="FP64 sigma calls timed for the comparison")
@@ -171,10 +176,68 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_sweep(args):
+    """One full two-site sweep (2(L-2) microiterations: eigensolver, truncation,
+    boundary update) at bond dimension m from the same random right-normalised
+    MPS, in the FP64 form and in the BF16x3 sigma form; prints one JSON line."""
+    import numpy as np
+    import torch
+    from qcmaquis_gb300.engine import DeviceMPSTensor
+    from qcmaquis_gb300.integrals import synthetic_integral_map
+    from qcmaquis_gb300.model import QCModel
+    from qcmaquis_gb300.mpo import make_mpo, make_ts_cache_mpo
+    from qcmaquis_gb300.mps import bond_indices, right_canonical_chain
+    from qcmaquis_gb300.sweep import SweepParams, run_dmrg
+    L, nelec = args.L, args.L
+    t0 = time.time()
+    model = QCModel(L, synthetic_integral_map(L, seed=1, diag_range=(-3.0, -0.3)), nelec)
+    mpo = make_mpo(model)
+    ts = make_ts_cache_mpo(mpo, model.phys, workers=os.cpu_count() or 1)
+    bonds = bond_indices(L, model.phys, (nelec, 0), args.m)
+    sites, _ = right_canonical_chain(model.phys, bonds, L, 0, np.random.default_rng(7))
+    setup = time.time() - t0
+    out = {}
+    ramp = [int(x) for x in args.ramp.split(",")] if args.ramp else None
+    nsweeps = len(ramp) if ramp else args.nsweeps
+    variants = (("fp64", 0, 0), ("bf16x3", 2, 2)) if nsweeps > 1 else \
+        (("fp64", 0, 0), ("bf16x3", 2, 2), ("bf16x3_sigma_only", 2, 0))
+    for name, prec, bprec in variants:
+        mps = [DeviceMPSTensor.from_host(t) for t in sites]
+        p = SweepParams(nsweeps=nsweeps, max_bond_dimension=args.m, sweep_bond_dimensions=ramp,
+                        truncation_initial=1e-16, truncation_final=1e-16, ietl_jcd_tol=1e-7,
+                        ietl_jcd_maxiter=args.jd_maxiter)
+        torch.cuda.synchronize()
+        t1 = time.time()
+        rec, _ = run_dmrg(model, mpo, p, nelec, mps=mps, precision=prec, ts_mpo=ts, boundary_precision=bprec)
+        torch.cuda.synchronize()
+        out[name] = {"sweep_s": rec.sweep_seconds[-1], "sweep_seconds": rec.sweep_seconds, "wall_s": time.time() - t1,
+                     "energy": rec.sweep_energy[-1], "sweep_energies": rec.sweep_energy,
+                     "last_micro_energy": rec.energies[-1], "sigma_calls": rec.sigma_calls,
+                     "max_bond": max(rec.bond_dimension), "truncated_weight": rec.sweep_truncated_weight[-1],
+                     "seconds_by_part": rec.seconds}
+        del mps
+        torch.cuda.empty_cache()
+    f, b = out["fp64"], out["bf16x3"]
+    line = {"metric": f"sweep s (two-site sweep, L={L} N={nelec} S=0 SU2U1, m={args.m})", "value": b["sweep_s"],
+            "unit": "s", "higher_is_better": False, "n_gpus": 1,
+            "dtype": "bf16x3 sigma and boundary products; fp64 eigensolver algebra, SVD, storage",
+            "data": "synthetic (seeded integrals, random right-normalised MPS)",
+            "config": {"workload": (f"{nsweeps} sweep(s) from a random MPS at m={args.m}"
+                                    + (f", bond dimensions per sweep {ramp}" if ramp else f", Mmax {args.m}")
+                                    + f", Davidson tol 1e-7, maxiter {args.jd_maxiter}, cutoff 1e-16; value = "
+                                    "last sweep"), "L": L, "m": args.m},
+            "fp64_sweep_s": f["sweep_s"], "speedup_vs_fp64_gpu": f["sweep_s"] / b["sweep_s"],
+            "energy_fp64": f["energy"], "energy_bf16x3": b["energy"], "delta_energy_eh": abs(b["energy"] - f["energy"]),
+            "runs": out, "setup_s": setup}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.sweep:
+        return run_sweep(args)
     import numpy as np
     import torch
     from qcmaquis_gb300 import native as N
@@ -314,7 +377,7 @@ def main():
         "data": "synthetic (seeded integrals and random MPS; no dataset)",
         "config": {"workload": "sigma vector H_eff.psi, L=24 N=24 S=0 SU2U1, middle sites (11,12), m=1024",
                    **w.describe(), "precision": args.precision,
-                   "l2": "inputs (boundaries, several GB) larger than L2; no flush",
+                   "l2": "working set of one sigma (boundaries, T, contr, operand images: about 16 GB) far above L2; no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "setup_s": round(setup_s, 1)},
         "e2e": {"value": flops / t_e2e / 1e12 * world, "unit": UNIT,

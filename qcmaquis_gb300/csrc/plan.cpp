@@ -19,6 +19,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <stdexcept>
@@ -463,25 +464,25 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
                                const PB& out_left_pb, int t_buf, int c_buf, Stage& st, qcm_plan* P, int64_t& end) {
     const qcm_mpo_t* m = W.m;
     std::vector<BM> C(m->col_dim);
-    // tiles of one b2, keyed (out_l, out_r, row offset) in the reference's block order
-    using TileKey = std::tuple<Q, Q, int64_t>;
-    struct TileKeyLess {
-        bool operator()(const TileKey& a, const TileKey& b) const {
-            if (std::get<0>(a) != std::get<0>(b)) return std::get<0>(a) > std::get<0>(b);
-            if (std::get<1>(a) != std::get<1>(b)) return std::get<1>(a) > std::get<1>(b);
-            return std::get<2>(a) < std::get<2>(b);
-        }
-    };
-    struct TileVal { int64_t rows, cols; std::vector<AxpyTerm> terms; };
-    using TileMap = std::map<TileKey, TileVal, TileKeyLess>;
+    // the terms of one b2 column with their tile keys, sorted (stably) by key
+    // afterwards.  key = position of out_l in out_left_i (16 bits), of out_r in
+    // right_i (16 bits), row offset (32 bits): ascending keys are the reference's
+    // block order (both indices descend) with row offsets ascending.
+    struct KeyedTerm { uint64_t key; int64_t src_off; double alpha; int32_t rows, cols; };
+    using TileMap = std::vector<KeyedTerm>;
+    if (out_left_i.size() >= (1u << 16) || right_i.size() >= (1u << 16))
+        throw std::runtime_error("too many sectors for the K2 planner");
     for (int b2 : b2list)
         if (b2 < 0 || b2 >= m->col_dim) throw std::runtime_error("b2 out of range");
     for (int e = 0; e < m->col_ptr[m->col_dim]; ++e)
         if (m->row_of[e] >= (int)T.size()) throw std::runtime_error("mpo row beyond boundary aux dimension");
-    // one b2 column: its contr blocks C[b2] and its tiles (independent of every other b2)
-    auto column = [&](int b2, TileMap& tiles, double& flops) {
+    // The MPO elements of one b2 column, [e0, e1): the contr blocks they need and
+    // their keyed terms (independent of every other task).
+    struct BlkNeed { Q lc, rc; int64_t rows, cols; };
+    struct TaskOut { std::vector<KeyedTerm> terms; std::vector<BlkNeed> blocks; double flops = 0.0; };
+    auto column = [&](int b2, int e0, int e1, TaskOut& out) {
         int ap = W.rspin(b2);
-        for (int e = m->col_ptr[b2]; e < m->col_ptr[b2 + 1]; ++e) {
+        for (int e = e0; e < e1; ++e) {
             int b1 = m->row_of[e];
             int a = W.lspin(b1);
             for (int tt = m->term_ptr[e]; tt < m->term_ptr[e + 1]; ++tt) {
@@ -498,16 +499,12 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
                         if (rb == right_i.size()) continue;
                         Q out_l = fuse(lc, pout);
                         if (!triangle(out_r.s, ap, out_l.s)) continue;
-                        if (!out_left_i.has(out_l)) continue;
+                        const size_t pl = out_left_i.position(out_l);
+                        if (pl == out_left_i.size()) continue;
                         int64_t r_size = right_i.d[rb].second;
-                        if (C[b2].find(out_l, out_r) == C[b2].b.size()) {
-                            Blk nb;
-                            nb.lc = out_l;
-                            nb.rc = out_r;
-                            nb.rows = out_left_i.size_of(out_l);
-                            nb.cols = r_size;
-                            C[b2].insert(nb);
-                        }
+                        if (l_size >= (int64_t(1) << 31) || r_size >= (int64_t(1) << 31))
+                            throw std::runtime_error("block larger than 2^31 elements");
+                        out.blocks.push_back({out_l, out_r, out_left_i.d[pl].second, r_size});
                         int i = lc.s, ip = out_l.s, j = mc.s, jp = out_r.s;
                         double cpl[4];
                         set_coupling(j, std::abs(j - jp), jp, a, k, ap, i, std::abs(i - ip), ip, scale, cpl);
@@ -516,31 +513,42 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
                             int ss1 = m->ent[4 * en], ss2 = m->ent[4 * en + 1];
                             double alfa = m->ent_coeff[en] * cpl[spin_case(m->ent[4 * en + 2], m->ent[4 * en + 3])];
                             if (alfa == 0.0) continue;
-                            auto& tv = tiles[TileKey(out_l, out_r, olo + ss2 * l_size)];
-                            tv.rows = l_size;
-                            tv.cols = r_size;
-                            tv.terms.push_back({t_buf, tb.off + (iro + (int64_t)ss1 * r_size) * l_size, l_size, alfa});
-                            flops += 2.0 * l_size * r_size;
+                            const uint64_t key = ((uint64_t)pl << 48) | ((uint64_t)rb << 32) |
+                                                 (uint64_t)(uint32_t)(olo + ss2 * l_size);
+                            out.terms.push_back({key, tb.off + (iro + (int64_t)ss1 * r_size) * l_size, alfa,
+                                                 (int32_t)l_size, (int32_t)r_size});
+                            out.flops += 2.0 * l_size * r_size;
                         }
                     }
                 }
             }
         }
     };
-    // the columns are planned by all host threads (dynamic assignment), then
-    // concatenated in b2 order: the result does not depend on the thread count
+    // tasks: each b2 column cut into runs of at most 8 MPO elements (the Hamiltonian's
+    // complementary-operator columns hold hundreds), planned by all host threads
+    struct Task { size_t col; int e0, e1; };
+    std::vector<Task> tasks;
+    std::vector<size_t> task_begin(b2list.size() + 1, 0);
+    for (size_t i = 0; i < b2list.size(); ++i) {
+        task_begin[i] = tasks.size();
+        const int b2 = b2list[i];
+        for (int e = m->col_ptr[b2]; e < m->col_ptr[b2 + 1]; e += 8)
+            tasks.push_back({i, e, std::min(e + 8, m->col_ptr[b2 + 1])});
+    }
+    task_begin[b2list.size()] = tasks.size();
+    std::vector<TaskOut> tout(tasks.size());
     std::vector<TileMap> per(b2list.size());
     std::vector<double> fl(b2list.size(), 0.0);
-    {
+    auto parallel = [&](size_t n, const std::function<void(size_t)>& f) {
         std::atomic<size_t> next{0};
         std::mutex err_mu;
         std::string err;
         auto worker = [&]() {
             for (;;) {
                 const size_t i = next.fetch_add(1);
-                if (i >= b2list.size()) return;
+                if (i >= n) return;
                 try {
-                    column(b2list[i], per[i], fl[i]);
+                    f(i);
                 } catch (const std::exception& ex) {
                     std::lock_guard<std::mutex> g(err_mu);
                     if (err.empty()) err = ex.what();
@@ -553,30 +561,80 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
         worker();
         for (auto& th : pool) th.join();
         if (!err.empty()) throw std::runtime_error(err);
-    }
+    };
+    parallel(tasks.size(), [&](size_t ti) { column(b2list[tasks[ti].col], tasks[ti].e0, tasks[ti].e1, tout[ti]); });
+    // per column: its tasks' terms in task order, stably sorted by tile key; its blocks
+    parallel(b2list.size(), [&](size_t i) {
+        const int b2 = b2list[i];
+        size_t n = 0;
+        for (size_t ti = task_begin[i]; ti < task_begin[i + 1]; ++ti) n += tout[ti].terms.size();
+        per[i].reserve(n);
+        for (size_t ti = task_begin[i]; ti < task_begin[i + 1]; ++ti) {
+            per[i].insert(per[i].end(), tout[ti].terms.begin(), tout[ti].terms.end());
+            std::vector<KeyedTerm>().swap(tout[ti].terms);
+            fl[i] += tout[ti].flops;
+            for (const BlkNeed& bn : tout[ti].blocks)
+                if (C[b2].find(bn.lc, bn.rc) == C[b2].b.size()) {
+                    Blk nb;
+                    nb.lc = bn.lc;
+                    nb.rc = bn.rc;
+                    nb.rows = bn.rows;
+                    nb.cols = bn.cols;
+                    C[b2].insert(nb);
+                }
+        }
+        std::stable_sort(per[i].begin(), per[i].end(),
+                         [](const KeyedTerm& x, const KeyedTerm& y) { return x.key < y.key; });
+    });
     int64_t base = 0;
     for (auto& c : C) base = c.assign_offsets(base);
     end = base;
     st.kind = ST_AXPY;
+    // emit in b2 order: count each column's tiles, then every column fills its own
+    // precomputed range of the output and term tables (in parallel)
+    std::vector<size_t> ntile(b2list.size(), 0);
+    parallel(b2list.size(), [&](size_t i) {
+        const TileMap& v = per[i];
+        size_t n = 0;
+        for (size_t a = 0; a < v.size(); ++a)
+            if (a == 0 || v[a].key != v[a - 1].key) ++n;
+        ntile[i] = n;
+    });
+    std::vector<size_t> obase(b2list.size() + 1, st.aout.size()), tbase(b2list.size() + 1, st.aterm.size());
     for (size_t i = 0; i < b2list.size(); ++i) {
+        obase[i + 1] = obase[i] + ntile[i];
+        tbase[i + 1] = tbase[i] + per[i].size();
+    }
+    st.aout.resize(obase[b2list.size()]);
+    st.aterm.resize(tbase[b2list.size()]);
+    std::vector<double> bytes(b2list.size(), 0.0);
+    parallel(b2list.size(), [&](size_t i) {
         const int b2 = b2list[i];
-        P->axpy_flops += fl[i];
         const BM& cb = C[b2];
-        for (auto& kv : per[i]) {
-            const Blk& d = cb.b[cb.find(std::get<0>(kv.first), std::get<1>(kv.first))];
-            AxpyOut o;
+        TileMap& v = per[i];
+        size_t oi = obase[i], ti = tbase[i];
+        for (size_t a = 0; a < v.size();) {
+            size_t b = a + 1;
+            while (b < v.size() && v[b].key == v[a].key) ++b;   // equal keys: one tile
+            const Q out_l = out_left_i.d[v[a].key >> 48].first, out_r = right_i.d[(v[a].key >> 32) & 0xFFFFu].first;
+            const Blk& d = cb.b[cb.find(out_l, out_r)];
+            AxpyOut& o = st.aout[oi++];
             o.dst_buf = c_buf;
-            o.dst_off = d.off + std::get<2>(kv.first);
+            o.dst_off = d.off + (int64_t)(uint32_t)(v[a].key & 0xFFFFFFFFu);
             o.ldd = d.rows;
-            o.rows = kv.second.rows;
-            o.cols = kv.second.cols;
-            o.t_begin = (int64_t)st.aterm.size();
-            st.aterm.insert(st.aterm.end(), kv.second.terms.begin(), kv.second.terms.end());
-            o.t_end = (int64_t)st.aterm.size();
-            st.aout.push_back(o);
-            P->axpy_bytes += 8.0 * o.rows * o.cols * (double)(kv.second.terms.size() + 1);
+            o.rows = v[b - 1].rows;
+            o.cols = v[b - 1].cols;
+            o.t_begin = (int64_t)ti;
+            for (size_t k = a; k < b; ++k) st.aterm[ti++] = {t_buf, v[k].src_off, v[k].rows, v[k].alpha};
+            o.t_end = (int64_t)ti;
+            bytes[i] += 8.0 * o.rows * o.cols * (double)(b - a + 1);
+            a = b;
         }
-        per[i].clear();
+        TileMap().swap(v);
+    });
+    for (size_t i = 0; i < b2list.size(); ++i) {
+        P->axpy_flops += fl[i];
+        P->axpy_bytes += bytes[i];
     }
     return C;
 }
@@ -869,6 +927,11 @@ static qcm_plan* build_bleft(const Idx& phys, const Idx& left_i, const Idx& righ
     P->scratch[0] = rp_end;
     P->scratch[1] = t_end;
     P->scratch[2] = c_end;
+    build_image_tables(s1, s1.img);
+    build_image_tables(s3, s3.img);
+    axpy_components(s2, s2.comp_root);
+    build_dense_groups(s2, 64, s2.img, s2.heavy);
+    P->image_bytes = std::max(std::max(s1.img.bytes, s3.img.bytes), s2.img.bytes);
     P->stages.push_back(std::move(z0));
     P->stages.push_back(std::move(s0));
     P->stages.push_back(std::move(s1));
@@ -1072,6 +1135,11 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
     P->scratch[0] = rp_end;
     P->scratch[1] = t_end;
     P->scratch[2] = b_end;
+    build_image_tables(s1, s1.img);
+    build_image_tables(s3, s3.img);
+    axpy_components(s2, s2.comp_root);
+    build_dense_groups(s2, 64, s2.img, s2.heavy);
+    P->image_bytes = std::max(std::max(s1.img.bytes, s3.img.bytes), s2.img.bytes);
     P->stages.push_back(std::move(s1));
     P->stages.push_back(std::move(z2));
     P->stages.push_back(std::move(s2));
@@ -1308,53 +1376,46 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         if (a.ldd > 0x7fffffffLL) continue;
         groups[std::make_tuple(find((int32_t)i), a.rows, a.cols, a.dst_buf, sb)].push_back((int32_t)i);
     }
-    for (auto& kv : groups) {
-        const std::vector<int32_t>& O = kv.second;
-        const int64_t rows = std::get<1>(kv.first), cols = std::get<2>(kv.first);
-        const int32_t dst_buf = std::get<3>(kv.first), src_buf = std::get<4>(kv.first);
-        const int64_t E = rows * cols;
-        if (E > 0x7fffffffLL || O.size() < 8) continue;
-        std::unordered_map<int64_t, int32_t> sid;
+    // per group (in parallel): its source list and the BF16 slices of its
+    // coefficient matrix; then (in group order) the tables are appended
+    struct Prep {
+        bool keep = false;
         std::vector<int64_t> srcs;
+        std::vector<uint8_t> wimg;   // constant image, offsets relative to its own start
+        int64_t S = 0, KC = 0;
+        int32_t G = 0, Gb = 0;
+    };
+    std::vector<const std::pair<const std::tuple<int32_t, int64_t, int64_t, int32_t, int32_t>, std::vector<int32_t>>*> glist;
+    for (auto& kv : groups) glist.push_back(&kv);
+    std::vector<Prep> prep(glist.size());
+    auto prepare = [&](size_t gi) {
+        const std::vector<int32_t>& O = glist[gi]->second;
+        const int64_t rows = std::get<1>(glist[gi]->first), cols = std::get<2>(glist[gi]->first);
+        const int64_t E = rows * cols;
+        if (E > 0x7fffffffLL || O.size() < 8) return;
+        Prep& pr = prep[gi];
+        std::unordered_map<int64_t, int32_t> sid;
         int64_t nterms = 0;
         for (int32_t o : O)
             for (int64_t k = st.aout[o].t_begin; k < st.aout[o].t_end; ++k, ++nterms)
-                if (sid.emplace(st.aterm[k].src_off, (int32_t)srcs.size()).second) srcs.push_back(st.aterm[k].src_off);
-        const int64_t S = (int64_t)srcs.size();
+                if (sid.emplace(st.aterm[k].src_off, (int32_t)pr.srcs.size()).second) pr.srcs.push_back(st.aterm[k].src_off);
+        const int64_t S = (int64_t)pr.srcs.size();
         // dense block products pay when a fair share of the (outputs x sources) block is populated
-        if ((double)nterms < 0.05 * (double)O.size() * (double)S) continue;
-        const int64_t KC = (S + 31) / 32;
-        const int32_t G = (int32_t)((E + 7) / 8);
-        const int32_t Gb = (int32_t)((O.size() + 7) / 8);
-        // A: gathered source tiles, rows e, K = source index
-        ImgPanel pa;
-        pa.src_off = (int64_t)t.gather.size();
-        pa.img_off = t.bytes;
-        pa.src_buf = src_buf;
-        pa.ld = 0;
-        pa.R = (int32_t)E;
-        pa.K = (int32_t)S;
-        pa.kcontig = 2;
-        pa.G = G;
-        t.gather.insert(t.gather.end(), srcs.begin(), srcs.end());
-        const int32_t pid = (int32_t)t.panels.size();
-        t.bytes += KC * 3 * (int64_t)G * 512;
-        for (int64_t c = 0; c < KC; ++c) { t.build.push_back(pid); t.build.push_back((int32_t)c); }
-        t.panels.push_back(pa);
-        // B: coefficient matrix W (rows = outputs, K = sources), split on the host
-        std::vector<float> W((size_t)O.size() * S, 0.0f);
-        {
-            std::vector<double> Wd((size_t)O.size() * S, 0.0);
-            for (size_t j = 0; j < O.size(); ++j)
-                for (int64_t k = st.aout[O[j]].t_begin; k < st.aout[O[j]].t_end; ++k)
-                    Wd[j * S + sid[st.aterm[k].src_off]] += st.aterm[k].alpha;
-            for (size_t x = 0; x < W.size(); ++x) W[x] = (float)Wd[x];
-        }
-        const int64_t b_off = (int64_t)t.cimg.size();
-        t.cimg.resize(t.cimg.size() + (size_t)(KC * 3 * (int64_t)Gb * 512), 0);
+        if ((double)nterms < 0.05 * (double)O.size() * (double)S) return;
+        pr.keep = true;
+        pr.S = S;
+        pr.KC = (S + 31) / 32;
+        pr.G = (int32_t)((E + 7) / 8);
+        pr.Gb = (int32_t)((O.size() + 7) / 8);
+        // coefficient matrix W (rows = outputs, K = sources), split into BF16 slices
+        std::vector<double> Wd((size_t)O.size() * S, 0.0);
+        for (size_t j = 0; j < O.size(); ++j)
+            for (int64_t k = st.aout[O[j]].t_begin; k < st.aout[O[j]].t_end; ++k)
+                Wd[j * S + sid[st.aterm[k].src_off]] += st.aterm[k].alpha;
+        pr.wimg.assign((size_t)(pr.KC * 3 * (int64_t)pr.Gb * 512), 0);
         for (size_t j = 0; j < O.size(); ++j)
             for (int64_t k = 0; k < S; ++k) {
-                const float x = W[j * S + k];
+                const float x = (float)Wd[j * S + k];
                 if (x == 0.0f) continue;
                 const uint16_t h0 = bf16_rne(x);
                 const float r1 = x - bf16_to_float(h0);
@@ -1364,11 +1425,55 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
                 const uint16_t h[3] = {h0, h1, h2};
                 const int64_t c = k / 32, q = (k % 32) / 8;
                 for (int sl = 0; sl < 3; ++sl) {
-                    const int64_t byte = b_off + ((c * 3 + sl) * Gb + (int64_t)(j / 8)) * 512 + q * 128 +
+                    const int64_t byte = ((c * 3 + sl) * pr.Gb + (int64_t)(j / 8)) * 512 + q * 128 +
                                          (int64_t)(j % 8) * 16 + (k % 8) * 2;
-                    std::memcpy(&t.cimg[(size_t)byte], &h[sl], 2);
+                    std::memcpy(&pr.wimg[(size_t)byte], &h[sl], 2);
                 }
             }
+    };
+    {
+        std::atomic<size_t> next{0};
+        auto worker = [&]() {
+            for (;;) {
+                const size_t gi = next.fetch_add(1);
+                if (gi >= glist.size()) return;
+                prepare(gi);
+            }
+        };
+        const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        for (unsigned k = 1; k < nt; ++k) pool.emplace_back(worker);
+        worker();
+        for (auto& th : pool) th.join();
+    }
+    for (size_t gi = 0; gi < glist.size(); ++gi) {
+        if (!prep[gi].keep) continue;
+        const std::vector<int32_t>& O = glist[gi]->second;
+        const int64_t rows = std::get<1>(glist[gi]->first), cols = std::get<2>(glist[gi]->first);
+        const int32_t dst_buf = std::get<3>(glist[gi]->first), src_buf = std::get<4>(glist[gi]->first);
+        const int64_t E = rows * cols;
+        Prep& pr = prep[gi];
+        const int64_t KC = pr.KC;
+        const int32_t G = pr.G, Gb = pr.Gb;
+        // A: gathered source tiles, rows e, K = source index
+        ImgPanel pa;
+        pa.src_off = (int64_t)t.gather.size();
+        pa.img_off = t.bytes;
+        pa.src_buf = src_buf;
+        pa.ld = 0;
+        pa.R = (int32_t)E;
+        pa.K = (int32_t)pr.S;
+        pa.kcontig = 2;
+        pa.G = G;
+        t.gather.insert(t.gather.end(), pr.srcs.begin(), pr.srcs.end());
+        const int32_t pid = (int32_t)t.panels.size();
+        t.bytes += KC * 3 * (int64_t)G * 512;
+        for (int64_t c = 0; c < KC; ++c) { t.build.push_back(pid); t.build.push_back((int32_t)c); }
+        t.panels.push_back(pa);
+        // B: the group's constant image
+        const int64_t b_off = (int64_t)t.cimg.size();
+        t.cimg.insert(t.cimg.end(), pr.wimg.begin(), pr.wimg.end());
+        std::vector<uint8_t>().swap(pr.wimg);
         // output: column j is output tile O[j]
         ImgOut io;
         io.c_off = 0;

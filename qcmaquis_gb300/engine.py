@@ -14,6 +14,8 @@ from dataclasses import dataclass
 from typing import Dict, List, Optional, Tuple
 
 import numpy as np
+import time
+
 import torch
 
 from . import native as N
@@ -113,6 +115,7 @@ class Engine:
         # BF16x3 form: feed the tensor cores from pre-split operand images
         self.use_images = use_images
         self.ws = Workspace(self.device)
+        self.plan_seconds = 0.0   # host time spent building and uploading plans
         self._plans: Dict[tuple, N.Plan] = {}
         self._mpo_cache: Dict[int, N.FMpo] = {}
         self.launches = 0
@@ -132,9 +135,11 @@ class Engine:
         key = ("s", id(ket.layout), id(L.layout), id(R.layout), id(mpo), self.hermitian)
         p = self._plans.get(key)
         if p is None:
+            t0 = time.time()
             p = N.plan_sigma(ket.phys_i, ket.left_i, ket.right_i, ket.layout, L.layout, R.layout, self.fmpo(mpo),
                              self.hermitian)
             p.upload()
+            self.plan_seconds += time.time() - t0
             p._keep = (ket.layout, L.layout, R.layout)
             # keep the two most recent sigma plans (a plan's task tables can be hundreds of MB)
             while len(self._plans) >= 2:
@@ -174,24 +179,33 @@ class Engine:
         self.run(p, ket=ket.data, left=L, right=R, out=out, precision=precision)
         return ket.like(out)
 
-    def overlap_mpo_left_step(self, mps: DeviceMPSTensor, L: DeviceBoundary, mpo) -> DeviceBoundary:
-        """L[i+1] from L[i], A[i], W[i] (``Engine::overlap_mpo_left_step``, bra = ket)."""
+    def overlap_mpo_left_step(self, mps: DeviceMPSTensor, L: DeviceBoundary, mpo,
+                              precision: int = N.PREC_FP64) -> DeviceBoundary:
+        """L[i+1] from L[i], A[i], W[i] (``Engine::overlap_mpo_left_step``, bra = ket).
+        The boundary is stored in FP64; ``precision`` selects the arithmetic of its
+        block products (the mixed forms: FP32 intermediates, tensor-core products)."""
+        t0 = time.time()
         p = N.plan_boundary_left(mps.phys_i, mps.left_i, mps.right_i, mps.layout, L.layout, self.fmpo(mpo),
                                  self.hermitian)
         p.upload()
+        self.plan_seconds += time.time() - t0
         lay = p.out_layout()
         out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=self.device)
-        self.run(p, ket=mps.data, left=L, out=out, precision=N.PREC_FP64)
+        self.run(p, ket=mps.data, left=L, out=out, precision=precision)
         return DeviceBoundary(lay, out)
 
-    def overlap_mpo_right_step(self, mps: DeviceMPSTensor, R: DeviceBoundary, mpo) -> DeviceBoundary:
-        """R[i] from R[i+1], B[i], W[i] (``Engine::overlap_mpo_right_step``, bra = ket)."""
+    def overlap_mpo_right_step(self, mps: DeviceMPSTensor, R: DeviceBoundary, mpo,
+                               precision: int = N.PREC_FP64) -> DeviceBoundary:
+        """R[i] from R[i+1], B[i], W[i] (``Engine::overlap_mpo_right_step``, bra = ket);
+        ``precision`` as for ``overlap_mpo_left_step``."""
+        t0 = time.time()
         p = N.plan_boundary_right(mps.phys_i, mps.left_i, mps.right_i, mps.layout, R.layout, self.fmpo(mpo),
                                   self.hermitian)
         p.upload()
+        self.plan_seconds += time.time() - t0
         lay = p.out_layout()
         out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=self.device)
-        self.run(p, ket=mps.data, right=R, out=out, precision=N.PREC_FP64)
+        self.run(p, ket=mps.data, right=R, out=out, precision=precision)
         return DeviceBoundary(lay, out)
 
 

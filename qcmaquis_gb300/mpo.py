@@ -399,8 +399,22 @@ def make_twosite_mpo(mpo1: MPOTensor, mpo2: MPOTensor, phys1: Index, phys2: Inde
                      mpo1.left_spins, mpo2.right_spins)
 
 
-def make_ts_cache_mpo(mpo: MPO, phys: Index) -> List[MPOTensor]:
-    return [make_twosite_mpo(mpo[p], mpo[p + 1], phys, phys) for p in range(len(mpo) - 1)]
+def _twosite_job(args):
+    a, b, phys = args
+    return make_twosite_mpo(a, b, phys, phys)
+
+
+def make_ts_cache_mpo(mpo: MPO, phys: Index, workers: int = 1) -> List[MPOTensor]:
+    """Two-site MPO tensors of every site pair (``make_ts_cache_mpo``,
+    ``mp_tensors/ts_ops.h``).  ``workers`` > 1 builds them in that many spawned
+    processes (host work only; spawn, so it is safe after CUDA is initialised)."""
+    jobs = [(mpo[p], mpo[p + 1], phys) for p in range(len(mpo) - 1)]
+    if workers <= 1 or len(jobs) < 2:
+        return [_twosite_job(j) for j in jobs]
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    with ProcessPoolExecutor(max_workers=min(workers, len(jobs)), mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_twosite_job, jobs))
 
 
 __all__ = ["MPOTensor", "MPO", "Hermitian", "TaggedMPOMaker", "make_mpo", "make_twosite_mpo",

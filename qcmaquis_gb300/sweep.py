@@ -15,7 +15,7 @@ from __future__ import annotations
 import math
 import time
 from dataclasses import dataclass, field
-from typing import List, Optional
+from typing import Dict, List, Optional
 
 import numpy as np
 import torch
@@ -74,6 +74,9 @@ class SweepRecord:
     sweep_truncated_weight: List[float] = field(default_factory=list)
     sweep_seconds: List[float] = field(default_factory=list)
     sigma_calls: int = 0
+    # wall time per part of the sweeps (host clock, device synchronised at each part's end)
+    seconds: Dict[str, float] = field(default_factory=lambda: {"eigensolver": 0.0, "truncation": 0.0,
+                                                               "boundary": 0.0, "plans": 0.0})
 
 
 def default_mps_init(L, phys, right_end, init_bond_dimension, seed, device="cuda") -> List[DeviceMPSTensor]:
@@ -144,26 +147,32 @@ def expval(mps: List[DeviceMPSTensor], mpo, engine_full: Engine, right_end) -> f
 
 
 def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optional[List[DeviceMPSTensor]] = None,
-             engine: Optional[Engine] = None, device="cuda", callback=None, precision: int = 0):
+             engine: Optional[Engine] = None, device="cuda", callback=None, precision: int = 0, ts_mpo=None,
+             boundary_precision: Optional[int] = None):
     """Two-site sweeps.  ``precision`` selects the sigma-vector form (0 = FP64,
     1 = TF32, 2 = BF16x3 tensor cores); boundary updates, the eigensolver's
     vector algebra, the subspace problem, the SVD truncation and the per-sweep
-    energy stay FP64."""
+    energy stay FP64.  ``boundary_precision`` (default: FP64) selects the form
+    of the boundary updates' block products (the boundaries are stored in FP64
+    either way).  ``mps`` (right-normalised) replaces the default initial
+    state; ``ts_mpo`` is a prebuilt two-site MPO cache (``make_ts_cache_mpo``)."""
     L = model.L
     phys = model.phys
     engine = engine or Engine(device, precision=precision)
     engine_full = Engine(device, hermitian=False)
+    bprec = 0 if boundary_precision is None else boundary_precision
     right_end = (nelec, twoS)
     if mps is None:
         mps = default_mps_init(L, phys, right_end, p.init_bond_dimension, p.seed, device)
         normalize_right(mps)
-    ts_mpo = make_ts_cache_mpo(mpo, phys)
+    if ts_mpo is None:
+        ts_mpo = make_ts_cache_mpo(mpo, phys)
     left: List = [None] * (L + 1)
     right: List = [None] * (L + 1)
     left[0] = _ones_boundary((0, 0), engine.device)
     right[L] = _ones_boundary(right_end, engine.device)
     for i in range(L - 1, 0, -1):
-        right[i] = engine.overlap_mpo_right_step(mps[i], right[i + 1], mpo[i])
+        right[i] = engine.overlap_mpo_right_step(mps[i], right[i + 1], mpo[i], precision=bprec)
     rec = SweepRecord()
     nmicro = 2 * (L - 2) if L > 2 else 1
     for sweep in range(p.nsweeps):
@@ -175,30 +184,43 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
             forward = mi < L - 1
             change = (mi == L - 2) or (mi == nmicro - 1)
             l2r = forward and not change
+            tp0 = engine.plan_seconds
+            t_a = time.time()
             psi = O.make_two_site_mps(mps[site], mps[site + 1])
             sp = SiteProblem(engine, left[site], right[site + 2], ts_mpo[site])
             theta, u, iters = solve_ietl_jcd(sp, psi, p.ietl_jcd_tol, p.ietl_jcd_maxiter)
+            torch.cuda.synchronize()
+            t_b = time.time()
             rec.energies.append(theta + mpo.core_energy)
             rec.jd_iterations.append(iters)
             rec.sigma_calls += iters
             A, B, tr = O.split(u, mps[site], mps[site + 1], Mmax, cutoff, l2r)
             mps[site], mps[site + 1] = A, B
+            torch.cuda.synchronize()
+            t_c = time.time()
             rec.truncated_weight.append(tr.truncated_weight)
             rec.bond_dimension.append(tr.bond_dimension)
             if l2r:
-                left[site + 1] = engine.overlap_mpo_left_step(mps[site], left[site], mpo[site])
+                left[site + 1] = engine.overlap_mpo_left_step(mps[site], left[site], mpo[site], precision=bprec)
                 if site + 2 < L:
                     mps[site + 1], t = O.left_normalize_and_return(mps[site + 1])
                     mps[site + 2] = O.multiply_from_left(mps[site + 2], t)
                 else:
                     mps[site + 1], _ = O.left_normalize_and_return(mps[site + 1])
             else:
-                right[site + 1] = engine.overlap_mpo_right_step(mps[site + 1], right[site + 2], mpo[site + 1])
+                right[site + 1] = engine.overlap_mpo_right_step(mps[site + 1], right[site + 2], mpo[site + 1],
+                                                                precision=bprec)
                 if site > 0:
                     mps[site], t = O.right_normalize_and_return(mps[site])
                     mps[site - 1] = O.multiply_from_right(mps[site - 1], t)
                 else:
                     mps[site], _ = O.right_normalize_and_return(mps[site])
+            torch.cuda.synchronize()
+            t_d = time.time()
+            rec.seconds["eigensolver"] += t_b - t_a
+            rec.seconds["truncation"] += t_c - t_b
+            rec.seconds["boundary"] += t_d - t_c
+            rec.seconds["plans"] += engine.plan_seconds - tp0
             if callback:
                 callback(sweep, mi, rec)
         torch.cuda.synchronize()

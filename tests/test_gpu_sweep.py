@@ -73,3 +73,15 @@ def test_mixed_precision_sweep_energy_close_to_fp64():
     gpu, _ = G.run_dmrg(model, make_mpo(model), G.SweepParams(nsweeps=6, max_bond_dimension=64), nelec=8,
                         precision=2)
     assert abs(gpu.sweep_energy[-1] - ref["sweep_energy"][-1]) < 1e-6
+
+
+def test_mixed_precision_boundaries_sweep_energy_close_to_fp64():
+    """BF16x3 sigma vectors and BF16x3 boundary updates (boundaries stored in
+    FP64): final energy within 1e-6 Eh of the FP64 sweep (L=8, N=8, m=64, 6 sweeps)."""
+    from qcmaquis_gb300 import sweep as G
+    with open(os.path.join(HERE, "golden", "oracle_L8_m64.json")) as f:
+        ref = json.load(f)
+    model = QCModel(8, synthetic_integral_map(8, seed=0, diag_range=(-2.0, -0.5)), 8)
+    gpu, _ = G.run_dmrg(model, make_mpo(model), G.SweepParams(nsweeps=6, max_bond_dimension=64), nelec=8,
+                        precision=2, boundary_precision=2)
+    assert abs(gpu.sweep_energy[-1] - ref["sweep_energy"][-1]) < 1e-6

@@ -84,3 +84,34 @@ def test_image_executor_matches_in_kernel_split(L, m):
     assert (torch.linalg.norm(a1 - b) / nr).item() < 2e-5
     assert torch.equal(a1, a2)
     assert _status() == 0
+
+
+def test_mixed_precision_boundary_steps_match_fp64():
+    """Left and right boundary updates with BF16x3 block products (FP64 storage)
+    within 2e-5 of the FP64 updates, L=12 m=256 middle sites."""
+    from qcmaquis_gb300.engine import DeviceMPSTensor, Engine
+    from qcmaquis_gb300.workloads import build_sigma_host, upload_sigma_workload
+    w = build_sigma_host(L=12, nelec=12, m=256)
+    eng = Engine("cuda:0")
+    upload_sigma_workload(w, eng)
+    A = DeviceMPSTensor.from_host(w.left_sites[-1])
+    i = len(w.left_sites) - 1
+    # the left boundary before site i: rebuild it from the start
+    from qcmaquis_gb300.block_matrix import BlockMatrix
+    from qcmaquis_gb300.engine import DeviceBoundary
+    from qcmaquis_gb300.symmetry import Index
+    one = lambda c: BlockMatrix.from_indices(Index([(c, 1)]), Index([(c, 1)]), fill=1.0)
+    left = DeviceBoundary.from_host([one((0, 0))])
+    for k in range(i):
+        left = eng.overlap_mpo_left_step(DeviceMPSTensor.from_host(w.left_sites[k]), left, w.mpo[k])
+    ref = eng.overlap_mpo_left_step(A, left, w.mpo[i]).data
+    mix = eng.overlap_mpo_left_step(A, left, w.mpo[i], precision=N.PREC_BF16X3).data
+    assert (torch.linalg.norm(mix - ref) / torch.linalg.norm(ref)).item() < 2e-5
+    B = DeviceMPSTensor.from_host(w.right_sites[0])
+    right = DeviceBoundary.from_host([one((w.nelec, 0))])
+    for k in range(len(w.right_sites) - 1, 0, -1):
+        right = eng.overlap_mpo_right_step(DeviceMPSTensor.from_host(w.right_sites[k]), right, w.mpo[w.site + 2 + k])
+    ref = eng.overlap_mpo_right_step(B, right, w.mpo[w.site + 2]).data
+    mix = eng.overlap_mpo_right_step(B, right, w.mpo[w.site + 2], precision=N.PREC_BF16X3).data
+    assert (torch.linalg.norm(mix - ref) / torch.linalg.norm(ref)).item() < 2e-5
+    assert _status() == 0

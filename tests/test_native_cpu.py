@@ -77,6 +77,40 @@ def test_sigma_image_tables_match_oracle(L, m, site, herm):
 
 
 @pytest.mark.parametrize("herm", [True, False])
+def test_boundary_image_tables_match_oracle(herm):
+    """The BF16x3 image tables of the boundary-update plans (emulated in FP64,
+    scratch starting as NaN) reproduce the oracle's boundaries."""
+    L, Ne = 8, 8
+    m = QCModel(L, synthetic_integral_map(L, seed=3), Ne)
+    mpo = make_mpo(m)
+    mps = initial_state(m, mpo, SweepParams(init_bond_dimension=64, seed=11), Ne, 0)
+    left = R.left_boundary(mps[0])
+    for i in range(4):
+        A = mps[i].copy().make_left_paired()
+        lay, Ll = N.Layout.of(A.data), N.BoundaryLayout.of(left)
+        p = N.plan_boundary_left(A.phys_i, A.left_i, A.right_i, lay, Ll, N.FMpo(mpo[i]), herm)
+        ol = p.out_layout()
+        bufs = [lay.pack(A.data), Ll.pack(left), None, np.zeros(max(p.out_elems, 1))] + \
+            [np.full(max(s, 1), np.nan) for s in p.scratch]
+        run_plan(p, bufs, images=True)
+        ref = ol.pack(R.overlap_mpo_left_step(mps[i], mps[i], left, mpo[i], herm))
+        assert np.linalg.norm(bufs[3][:ol.size] - ref) <= 1e-7 * max(np.linalg.norm(ref), 1e-300)
+        left = R.overlap_mpo_left_step(mps[i], mps[i], left, mpo[i], herm)
+    right = R.right_boundary(mps[L - 1])
+    for i in range(L - 1, 3, -1):
+        A = mps[i].copy().make_left_paired()
+        lay, Rl = N.Layout.of(A.data), N.BoundaryLayout.of(right)
+        p = N.plan_boundary_right(A.phys_i, A.left_i, A.right_i, lay, Rl, N.FMpo(mpo[i]), herm)
+        ol = p.out_layout()
+        bufs = [lay.pack(A.data), None, Rl.pack(right), np.zeros(max(p.out_elems, 1))] + \
+            [np.full(max(s, 1), np.nan) for s in p.scratch]
+        run_plan(p, bufs, images=True)
+        ref = ol.pack(R.overlap_mpo_right_step(mps[i], mps[i], right, mpo[i], herm))
+        assert np.linalg.norm(bufs[3][:ol.size] - ref) <= 1e-7 * max(np.linalg.norm(ref), 1e-300)
+        right = R.overlap_mpo_right_step(mps[i], mps[i], right, mpo[i], herm)
+
+
+@pytest.mark.parametrize("herm", [True, False])
 def test_boundary_plans_match_oracle_layout_and_values(herm):
     L, Ne = 6, 6
     m = QCModel(L, synthetic_integral_map(L, seed=3), Ne)
