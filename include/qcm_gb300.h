@@ -17,6 +17,8 @@
  *       .../non-abelian/engine.hpp:104-113 -> qcm_plan_boundary_left + qcm_plan_run
  *   contraction::Engine<..., SU2>::overlap_mpo_right_step
  *       .../non-abelian/engine.hpp:115-124 -> qcm_plan_boundary_right + qcm_plan_run
+ *   contraction::Engine<..., SU2>::left/right_boundary_tensor_mpo
+ *       .../non-abelian/engine.hpp:84-102 -> qcm_plan_boundary_tensor_mpo + qcm_plan_run
  *   ietl::dot / ietl::two_norm on MPSTensor (scalar_overlap, norm)
  *       dmrg/framework/dmrg/mp_tensors/mpstensor.hpp:365-380 -> qcm_dot, qcm_nrm2
  *   vector updates inside jacobi_davidson::calculate_eigenvalue
@@ -145,6 +147,21 @@ int qcm_plan_boundary_left(const qcm_index_t* phys, const qcm_index_t* left_i, c
 int qcm_plan_boundary_right(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
                             const qcm_blocks_t* mps, const qcm_boundary_t* right, const qcm_mpo_t* mpo,
                             int32_t hermitian, qcm_plan** plan);
+
+/* The boundary x MPS x MPO contraction without the bra, one block matrix per
+ * MPO bond on the open side (side 0: Engine::left_boundary_tensor_mpo, a
+ * block matrix per right bond b2; side 1: right_boundary_tensor_mpo, one per
+ * left bond b1; dmrg/framework/dmrg/mp_tensors/contractions/common/
+ * move_boundary.hpp:66-126).  Every bond is computed; hermitian != 0 lets the
+ * boundary product read the Hermitian partners, as the reference's default.
+ * Output layout through qcm_plan_out_layout.  Its use in the reference is the
+ * density-matrix perturbation of the heev truncation
+ * (mp_tensors/twositetensor.hpp:184-297), with the two-site tensor seen as
+ * one site (side 0: physical index of site 1, right index adjoin(phys2) x
+ * right; side 1: physical index of site 2, left index phys1 x left). */
+int qcm_plan_boundary_tensor_mpo(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                                 const qcm_blocks_t* mps, const qcm_boundary_t* boundary, const qcm_mpo_t* mpo,
+                                 int32_t side, int32_t hermitian, qcm_plan** plan);
 
 /* Sizes (elements) of the output and of the three scratch slots. */
 int qcm_plan_sizes(const qcm_plan* plan, int64_t* out_elems, int64_t* scratch_elems3);

@@ -997,6 +997,118 @@ def split_mps(tst_lp: BlockMatrix, p1, p2, left_i, right_i, Mmax, cutoff, l2r: b
     return A, Bt, trunc
 
 
+def left_boundary_tensor_mpo(mps: MPSTensor, left: List[BlockMatrix], mpo) -> List[BlockMatrix]:
+    """``left_boundary_tensor_mpo`` (``ct/common/move_boundary.hpp:66-97``): the left
+    boundary x MPS x MPO contraction without the bra, one block matrix per right
+    MPO bond.  The boundary product is trimmed to the ket's left index, every b2
+    is computed and the output rows are phys x left (no restriction)."""
+    mps = mps.copy()
+    phys, left_i, right_i = mps.phys_i, mps.left_i, mps.right_i
+    out_left_i = index_product(phys, left_i)
+    mps.make_right_paired()
+    T = boundary_mps_product(mps.data, left, mpo, left_i, True)
+    out_left_pb = ProductBasis(phys, left_i)
+    in_right_pb = ProductBasis(phys, right_i, fuse_neg_first)
+    return [lbtm_kernel(b2, T, mpo, right_i, out_left_i, in_right_pb, out_left_pb) for b2 in range(mpo.col_dim)]
+
+
+def right_boundary_tensor_mpo(mps: MPSTensor, right: List[BlockMatrix], mpo) -> List[BlockMatrix]:
+    """``right_boundary_tensor_mpo`` (``ct/common/move_boundary.hpp:99-126``), one block
+    matrix per left MPO bond.  ``MPSBoundaryProduct(mps, right, mpo)`` trims its
+    products to the ket's *left* index (``boundary_times_mps.hpp:258-261``); the
+    output columns are adjoin(phys) x right (no restriction)."""
+    mps = mps.copy()
+    phys, left_i, right_i = mps.phys_i, mps.left_i, mps.right_i
+    mps.make_left_paired()
+    t = mps_boundary_product(mps.data, right, mpo, left_i, True)
+    out_right_i = index_product(adjoin(phys), right_i)
+    in_left_pb = ProductBasis(phys, left_i)
+    out_right_pb = ProductBasis(phys, right_i, fuse_neg_first)
+    ret = []
+    for b1 in range(mpo.row_dim):
+        bufs = rbtm_tasks_apply(b1, t, mpo, left_i, out_right_i, in_left_pb, out_right_pb)
+        blk = BlockMatrix()
+        for key in bufs:
+            blk.insert_block(bufs[key], *key)
+        ret.append(blk)
+    return ret
+
+
+def heev_truncate(M: BlockMatrix, cutoff: float, Mmax: int):
+    """``heev_truncate`` + ``estimate_truncation`` (``block_matrix_algorithms.h:188-200,
+    211-251, 388-440``): per-block eigendecomposition, eigenvalues reordered
+    descending with their vectors (``algorithms.hpp:402-421``), one global cut on
+    the eigenvalues.  The result carries the truncated fraction in both weight
+    fields, as the reference returns it (``block_matrix_algorithms.h:439``)."""
+    U, evs = BlockMatrix(), []
+    for (lc, rc), b in zip(M.keys, M.blocks):
+        w, v = np.linalg.eigh(b)
+        U.insert_block(v[:, ::-1].copy(), lc, rc)
+        evs.append(w[::-1].copy())
+    allevals = np.sort(np.concatenate(evs))[::-1]
+    evalscut = cutoff * allevals[0]
+    if allevals.size > Mmax:
+        evalscut = max(evalscut, allevals[Mmax])
+    smallest_ev = evalscut / allevals[0]
+    disc = allevals[allevals < evalscut]
+    truncated_fraction = float(disc.sum() / allevals.sum())
+    keeps = [int(np.argmax(e < evalscut)) if np.any(e < evalscut) else e.size for e in evs]
+    Ut, St = BlockMatrix(), []
+    for k, kk in enumerate(keeps):
+        if kk == 0:
+            continue
+        lc, rc = U.keys[k]
+        Ut.insert_block(U.blocks[k][:, :kk].copy(), lc, rc)
+        St.append((rc, evs[k][:kk]))
+    return Ut, St, TruncationResults(sum(keeps), truncated_fraction, truncated_fraction, smallest_ev)
+
+
+def predict_split_mps(tst_lp: BlockMatrix, p1, p2, left_i, right_i, Mmax, cutoff, l2r: bool,
+                      alpha: float = 0.0, boundary=None, mpo=None, perturb: bool = True):
+    """``TwoSiteTensor::predict_split_l2r/r2l`` (``twositetensor.hpp:184-297``).
+
+    l2r: rho = theta theta^T (+ alpha sum_b h_b h_b^T, h = left_boundary_tensor_mpo of
+    theta seen as one site with right index adjoin(p2) x right, ``boundary`` =
+    left boundary of the pair, ``mpo`` = MPO tensor of the left site); the kept
+    eigenvectors U give A = U and B = U^T theta.
+    r2l: rho = theta^T theta (+ alpha sum_b h_b^T h_b from right_boundary_tensor_mpo
+    with left index p1 x left, the right boundary and the right site's MPO
+    tensor); B = U^T and A = theta U.  Only perturbation blocks whose charges
+    theta holds are added (``twositetensor.hpp:207-221``)."""
+    both = _reshape_left_to_both(p1, p2, left_i, right_i, tst_lp)
+    bt = both.transpose()
+    dm = bm_gemm(both, bt) if l2r else bm_gemm(bt, both)
+    if perturb and boundary is not None:
+        if l2r:
+            tmp = MPSTensor.from_block(p1, left_i, index_product(adjoin(p2), right_i), both, LEFT_PAIRED)
+            half = left_boundary_tensor_mpo(tmp, boundary, mpo)
+        else:
+            tmp = MPSTensor.from_block(p2, index_product(p1, left_i), right_i, both, RIGHT_PAIRED)
+            half = right_boundary_tensor_mpo(tmp, boundary, mpo)
+        for h in half:
+            ht = h.transpose()
+            tdm = bm_gemm(h, ht) if l2r else bm_gemm(ht, h)
+            for (lc, rc), b in zip(tdm.keys, tdm.blocks):
+                if both.find_block(lc, rc) == both.n_blocks():
+                    continue
+                p = dm.find_block(lc, rc)
+                if p == dm.n_blocks():
+                    dm.insert_block(alpha * b, lc, rc)
+                else:
+                    dm.blocks[p] = dm.blocks[p] + alpha * b
+    U, S, trunc = heev_truncate(dm, cutoff, Mmax)
+    if l2r:
+        A = MPSTensor.from_block(p1, left_i, U.right_basis(), U, LEFT_PAIRED)
+        V = bm_gemm(U.transpose(), both)
+        Bt = MPSTensor.from_block(p2, V.left_basis(), right_i, V, RIGHT_PAIRED)
+    else:
+        Ut = U.transpose()
+        Bt = MPSTensor.from_block(p2, Ut.left_basis(), right_i, Ut, RIGHT_PAIRED)
+        V = bm_gemm(both, U)
+        A = MPSTensor.from_block(p1, left_i, V.right_basis(), V, LEFT_PAIRED)
+    return A, Bt, trunc
+
+
 # --------------------------------------------------------------------------- Jacobi-Davidson
 def jcd_solve(apply_h, init: MPSTensor, tol: float, maxiter: int):
     """``solve_ietl_jcd`` -> ``jacobi_davidson::calculate_eigenvalue`` with zero GMRES

@@ -35,6 +35,21 @@ class SweepParams:
     ietl_jcd_tol: float = 1e-8
     ietl_jcd_maxiter: int = 10
     seed: int = 42
+    # truncation mode and noise schedule (``fw/utils/DmrgParameters.h:45-59``)
+    twosite_truncation: str = "svd"
+    alpha_initial: float = 1e-2
+    alpha_main: float = 1e-4
+    alpha_final: float = 1e-8
+    nmainsweeps: int = 5
+
+
+def get_alpha(p: SweepParams, sweep: int) -> float:
+    """``getAlpha`` (``sba/GenericSweepSimulation.h:242-253``)."""
+    if sweep < p.ngrowsweeps:
+        return p.alpha_initial
+    if sweep < p.ngrowsweeps + p.nmainsweeps:
+        return p.alpha_main
+    return p.alpha_final
 
 
 def log_interpolate(y0, y1, N, i):
@@ -129,7 +144,14 @@ def run_dmrg(model, mpo: MPO, p: SweepParams, nelec: int, twoS: int = 0, mps=Non
             u.make_left_paired()
             A0, B0 = mps[site], mps[site + 1]
             _, tst = R.unreduce_left(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, u.data)
-            A, B, trunc = R.split_mps(tst, A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, Mmax, cutoff, l2r)
+            if p.twosite_truncation == "svd":
+                A, B, trunc = R.split_mps(tst, A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, Mmax, cutoff, l2r)
+            else:
+                # sba/SweepMPSUpdater.h:192-203: left boundary of the pair and the left
+                # site's MPO tensor going right; right boundary and right site going left
+                bnd, w = (left[site], mpo[site]) if l2r else (right[site + 2], mpo[site + 1])
+                A, B, trunc = R.predict_split_mps(tst, A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, Mmax, cutoff,
+                                                  l2r, get_alpha(p, sweep), bnd, w)
             mps[site], mps[site + 1] = A, B
             rec.truncated_weight.append(trunc.truncated_weight)
             rec.bond_dimension.append(trunc.bond_dimension)

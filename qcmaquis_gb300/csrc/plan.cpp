@@ -854,31 +854,59 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
     return P;
 }
 
+// tensor_mpo: the plan stops after the operator application and writes it to
+// OUT as a boundary with one block matrix per right MPO bond -- every bond,
+// as left_boundary_tensor_mpo computes them (move_boundary.hpp:66-97): the
+// boundary x MPS product is trimmed to the ket's left index and the output
+// rows are not restricted to the right index.
 static qcm_plan* build_bleft(const Idx& phys, const Idx& left_i, const Idx& right_i, const BM& mps,
-                             const std::vector<BM>& L, const MpoV& W, bool herm) {
+                             const std::vector<BM>& L, const MpoV& W, bool herm, bool tensor_mpo = false) {
     auto* P = new qcm_plan();
     P->kind = PK_BLEFT;
     const qcm_mpo_t* m = W.m;
     if ((int)L.size() != m->row_dim) throw std::runtime_error("left boundary aux dimension does not match the MPO");
     Idx out_left_i = index_product(phys, left_i);
     Idx rib = right_i;
-    common_subset(out_left_i, rib);
+    if (!tensor_mpo) common_subset(out_left_i, rib);
     PB out_left_pb(phys, left_i, false), in_right_pb(phys, right_i, true);
     Stage z0; z0.kind = ST_ZERO; z0.zbuf = QCM_BUF_S0;
     Stage s0; int64_t rp_end = 0;
     BM rp = plan_reshape_l2r(phys, left_i, right_i, mps, QCM_BUF_KET, QCM_BUF_S0, s0, P, rp_end);
     z0.zlen = rp_end;
     Idx ref;
-    for (auto& b : rp.b) ref.d.push_back({b.lc, b.rows});
+    if (tensor_mpo) ref = left_i;
+    else for (auto& b : rp.b) ref.d.push_back({b.lc, b.rows});
     Stage s1; int64_t t_end = 0;
     std::vector<BM> T = plan_k1(L, W, herm, rp, QCM_BUF_S0, ref, QCM_BUF_S1, s1, P, t_end);
     std::vector<int> b2list;
     for (int b2 = 0; b2 < m->col_dim; ++b2)
-        if (!(herm && W.rskip(b2))) b2list.push_back(b2);
+        if (tensor_mpo || !(herm && W.rskip(b2))) b2list.push_back(b2);
     Stage s2; int64_t c_end = 0;
+    const int32_t c_buf = tensor_mpo ? QCM_BUF_OUT : QCM_BUF_S2;
     std::vector<BM> C = plan_k2(T, W, b2list, right_i, out_left_i, in_right_pb, out_left_pb, QCM_BUF_S1,
-                                QCM_BUF_S2, s2, P, c_end);
-    Stage z2; z2.kind = ST_ZERO; z2.zbuf = QCM_BUF_S2; z2.zlen = c_end;
+                                c_buf, s2, P, c_end);
+    Stage z2; z2.kind = ST_ZERO; z2.zbuf = c_buf; z2.zlen = c_end;
+    if (tensor_mpo) {
+        // C already carries its offsets in OUT, bond after bond
+        P->out_blk_ptr.assign(1, 0);
+        for (auto& bm : C) {
+            for (auto& b : bm.b) P->out_blocks.push_back(b);
+            P->out_blk_ptr.push_back((int32_t)P->out_blocks.size());
+        }
+        P->out_elems = c_end;
+        P->scratch[0] = rp_end;
+        P->scratch[1] = t_end;
+        build_image_tables(s1, s1.img);
+        axpy_components(s2, s2.comp_root);
+        build_dense_groups(s2, 64, s2.img, s2.heavy);
+        P->image_bytes = std::max(s1.img.bytes, s2.img.bytes);
+        P->stages.push_back(std::move(z0));
+        P->stages.push_back(std::move(s0));
+        P->stages.push_back(std::move(s1));
+        P->stages.push_back(std::move(z2));
+        P->stages.push_back(std::move(s2));
+        return P;
+    }
     // ret[b2] = SU2::gemm(transpose(contr[b2]), bra_lp, right_spin(b2))
     std::vector<BM> out(m->col_dim);
     struct Job { int b2; Q lc, rc; int64_t a_off, a_rows, a_cols; size_t bk; };
@@ -941,18 +969,26 @@ static qcm_plan* build_bleft(const Idx& phys, const Idx& left_i, const Idx& righ
     return P;
 }
 
+// tensor_mpo: as for build_bleft, the plan ends after the operator application
+// and writes every left MPO bond's block matrix to OUT, as
+// right_boundary_tensor_mpo computes them (move_boundary.hpp:99-126): the
+// MPS x boundary product is trimmed to the ket's *left* index (the index
+// MPSBoundaryProduct's three-argument constructor passes,
+// boundary_times_mps.hpp:258-261) and the output columns are not restricted
+// to the left index.
 static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& right_i, const BM& mps,
-                              const std::vector<BM>& R, const MpoV& W, bool herm) {
+                              const std::vector<BM>& R, const MpoV& W, bool herm, bool tensor_mpo = false) {
     auto* P = new qcm_plan();
     P->kind = PK_BRIGHT;
     const qcm_mpo_t* m = W.m;
     if ((int)R.size() != m->col_dim) throw std::runtime_error("right boundary aux dimension does not match the MPO");
     Idx out_right_i = index_product(adjoin(phys), right_i);
     Idx bli = left_i;
-    common_subset(out_right_i, bli);
+    if (!tensor_mpo) common_subset(out_right_i, bli);
     PB in_left_pb(phys, left_i, false), out_right_pb(phys, right_i, true);
     Idx ref;  // bra (left-paired) right basis
-    for (auto& b : mps.b) ref.d.push_back({b.rc, b.cols});
+    if (tensor_mpo) ref = left_i;
+    else for (auto& b : mps.b) ref.d.push_back({b.rc, b.cols});
     // t[b2] = mps_lp . R'[b2]  (gemm_trim_right)
     std::vector<BM> t(m->col_dim);
     struct Job { int b2; Q lc, rc; size_t ak; int64_t b_off, ldb; int tb; double sc; int64_t N; };
@@ -1027,7 +1063,7 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
     std::vector<BM> buf(m->row_dim);
     MpoV const& Wv = W;
     for (int b1 = 0; b1 < m->row_dim; ++b1) {
-        if (herm && Wv.lskip(b1)) continue;
+        if (herm && !tensor_mpo && Wv.lskip(b1)) continue;
         int a = Wv.lspin(b1);
         for (size_t r = 0; r < Wv.row_b2[b1].size(); ++r) {
             int b2 = Wv.row_b2[b1][r];
@@ -1076,13 +1112,14 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
     }
     int64_t b_end = 0;
     for (auto& x : buf) b_end = x.assign_offsets(b_end);
-    Stage z2; z2.kind = ST_ZERO; z2.zbuf = QCM_BUF_S2; z2.zlen = b_end;
+    const int32_t buf_slot = tensor_mpo ? QCM_BUF_OUT : QCM_BUF_S2;
+    Stage z2; z2.kind = ST_ZERO; z2.zbuf = buf_slot; z2.zlen = b_end;
     Stage s2; s2.kind = ST_AXPY;
     for (auto& kv : tiles) {
         int b1 = std::get<0>(kv.first);
         const Blk& d = buf[b1].b[buf[b1].find(std::get<1>(kv.first), std::get<2>(kv.first))];
         AxpyOut o;
-        o.dst_buf = QCM_BUF_S2;
+        o.dst_buf = buf_slot;
         o.dst_off = d.off + std::get<3>(kv.first) * d.rows;
         o.ldd = d.rows;
         o.rows = kv.second.rows;
@@ -1092,6 +1129,23 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
         o.t_end = (int64_t)s2.aterm.size();
         s2.aout.push_back(o);
         P->axpy_bytes += 8.0 * o.rows * o.cols * (double)(kv.second.terms.size() + 1);
+    }
+    if (tensor_mpo) {
+        P->out_blk_ptr.assign(1, 0);
+        for (auto& bm : buf) {
+            for (auto& b : bm.b) P->out_blocks.push_back(b);
+            P->out_blk_ptr.push_back((int32_t)P->out_blocks.size());
+        }
+        P->out_elems = b_end;
+        P->scratch[1] = t_end;
+        build_image_tables(s1, s1.img);
+        axpy_components(s2, s2.comp_root);
+        build_dense_groups(s2, 64, s2.img, s2.heavy);
+        P->image_bytes = std::max(s1.img.bytes, s2.img.bytes);
+        P->stages.push_back(std::move(s1));
+        P->stages.push_back(std::move(z2));
+        P->stages.push_back(std::move(s2));
+        return P;
     }
     // bra right-paired copy for the final product
     Stage z0; z0.kind = ST_ZERO; z0.zbuf = QCM_BUF_S0;
@@ -1565,6 +1619,27 @@ int qcm_plan_boundary_left(const qcm_index_t* phys, const qcm_index_t* left_i, c
         return QCM_OK;
     } catch (const std::exception& e) {
         set_error(std::string("qcm_plan_boundary_left: ") + e.what());
+        *plan = nullptr;
+        return QCM_E_INVALID;
+    }
+}
+
+int qcm_plan_boundary_tensor_mpo(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                                 const qcm_blocks_t* mps, const qcm_boundary_t* boundary, const qcm_mpo_t* mpo,
+                                 int32_t side, int32_t hermitian, qcm_plan** plan) {
+    if (!plan) { set_error("null plan pointer"); return QCM_E_INVALID; }
+    if (side != 0 && side != 1) { set_error("qcm_plan_boundary_tensor_mpo: side must be 0 (left) or 1 (right)"); return QCM_E_INVALID; }
+    try {
+        MpoV W(mpo);
+        if (side == 0)
+            *plan = build_bleft(read_index(phys), read_index(left_i), read_index(right_i), read_blocks(mps),
+                                read_boundary(boundary), W, hermitian != 0, true);
+        else
+            *plan = build_bright(read_index(phys), read_index(left_i), read_index(right_i), read_blocks(mps),
+                                 read_boundary(boundary), W, hermitian != 0, true);
+        return QCM_OK;
+    } catch (const std::exception& e) {
+        set_error(std::string("qcm_plan_boundary_tensor_mpo: ") + e.what());
         *plan = nullptr;
         return QCM_E_INVALID;
     }

@@ -208,6 +208,24 @@ class Engine:
         self.run(p, ket=mps.data, right=R, out=out, precision=precision)
         return DeviceBoundary(lay, out)
 
+    def boundary_tensor_mpo(self, mps: DeviceMPSTensor, B: DeviceBoundary, mpo, side: str) -> DeviceBoundary:
+        """``Engine::left_boundary_tensor_mpo`` (side "left", B = left boundary) or
+        ``right_boundary_tensor_mpo`` (side "right", B = right boundary),
+        ``non-abelian/engine.hpp:84-102``: the bra-free contraction, one block
+        matrix per open MPO bond, in FP64."""
+        t0 = time.time()
+        p = N.plan_boundary_tensor_mpo(mps.phys_i, mps.left_i, mps.right_i, mps.layout, B.layout, self.fmpo(mpo),
+                                       side, self.hermitian)
+        p.upload()
+        self.plan_seconds += time.time() - t0
+        lay = p.out_layout()
+        out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=self.device)
+        if side == "left":
+            self.run(p, ket=mps.data, left=B, out=out, precision=N.PREC_FP64)
+        else:
+            self.run(p, ket=mps.data, right=B, out=out, precision=N.PREC_FP64)
+        return DeviceBoundary(lay, out)
+
 
 class SiteProblem:
     """``SiteProblem{left, right, mpo}`` with ``ietl::mult`` = ``apply``."""

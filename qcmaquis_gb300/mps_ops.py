@@ -371,24 +371,164 @@ def svd_truncate(M: DBM, rel_tol: float, Mmax: int):
     return U, S, V, Trunc(sum(keeps), tw, tfrac, smallest_ev)
 
 
-def split(u: DeviceMPSTensor, A0: DeviceMPSTensor, B0: DeviceMPSTensor, Mmax: int, cutoff: float, l2r: bool):
-    """``tst << u`` then ``split_mps_l2r/r2l``; returns new (A, B, truncation)."""
+def heev_truncate(dm: DBM, cutoff: float, Mmax: int):
+    """``heev_truncate`` + ``estimate_truncation`` (``block_matrix_algorithms.h:188-200,
+    211-251, 388-440``): per-block eigendecomposition on the GPU (cuSOLVER, FP64),
+    eigenpairs in descending order (``algorithms.hpp:402-421``), the global cut on
+    the eigenvalues on the host.  The truncated fraction is returned in both
+    weight fields, as the reference does."""
+    Us, evs = [], []
+    for b in dm.blocks:
+        w, v = torch.linalg.eigh(b)
+        evs.append(torch.flip(w, [0]))
+        Us.append(torch.flip(v, [1]))
+    sizes = [int(e.numel()) for e in evs]
+    host = torch.cat(evs).cpu().numpy() if evs else np.zeros(0)
+    evals = np.split(host, np.cumsum(sizes)[:-1]) if sizes else []
+    allv = np.sort(host)[::-1]
+    evalscut = cutoff * allv[0]
+    if allv.size > Mmax:
+        evalscut = max(evalscut, allv[Mmax])
+    smallest_ev = evalscut / allv[0]
+    disc = allv[allv < evalscut]
+    tfrac = float(disc.sum() / allv.sum())
+    keeps = [int(np.argmax(e < evalscut)) if np.any(e < evalscut) else e.size for e in evals]
+    U = DBM()
+    S: Dict = {}
+    for k, (key, kk) in enumerate(zip(dm.keys, keeps)):
+        if kk == 0:
+            continue
+        lc, rc = key
+        U.insert(Us[k][:, :kk], lc, rc)
+        S[rc] = evs[k][:kk]
+    return U, S, Trunc(sum(keeps), tfrac, tfrac, smallest_ev)
+
+
+def _transpose(M: DBM) -> DBM:
+    T = DBM()
+    for (lc, rc), b in zip(M.keys, M.blocks):
+        T.insert(b.t(), rc, lc)
+    return T
+
+
+# concatenated operand size of one perturbation product (elements)
+_PERTURB_CHUNK = 1 << 26
+
+
+def add_perturbation(dm: DBM, both: DBM, half, alpha: float, l2r: bool):
+    """dm += alpha sum_b h_b h_b^T (l2r) or alpha sum_b h_b^T h_b (r2l) on the blocks
+    whose charges theta holds (``twositetensor.hpp:195-221, 255-281``).  ``half`` is
+    the device boundary of ``left/right_boundary_tensor_mpo``.  Products that land
+    on one dm block are summed as one GEMM over the concatenated h blocks."""
+    keys = set(both.keys)
+    diag: Dict = {}
+    cross: List = []
+    lay = half.layout
+    for b in range(lay.aux):
+        groups: Dict = {}
+        for k in range(lay.blk_ptr[b], lay.blk_ptr[b + 1]):
+            (lc, rc), (r, c), o = lay.keys[k], lay.shapes[k], lay.offsets[k]
+            v = half.data[o:o + r * c].view(c, r).t()
+            # l2r pairs blocks of one column charge; r2l blocks of one row charge
+            groups.setdefault(rc if l2r else lc, []).append((lc if l2r else rc, v))
+        for g in groups.values():
+            for i, (ci, vi) in enumerate(g):
+                for cj, vj in g:
+                    if (ci, cj) not in keys:
+                        continue
+                    if vi is vj:
+                        diag.setdefault(ci, []).append(vi)
+                    else:
+                        cross.append((ci, cj, vi, vj))
+    for c, vs in diag.items():
+        p = dm.find(c, c)
+        if p == len(dm.keys):
+            n = vs[0].shape[0] if l2r else vs[0].shape[1]
+            p = dm.insert(torch.zeros((n, n), dtype=torch.float64, device=vs[0].device), c, c)
+        dst = dm.blocks[p]
+        i = 0
+        while i < len(vs):
+            j, n = i, 0
+            while j < len(vs) and (j == i or n + vs[j].numel() <= _PERTURB_CHUNK):
+                n += vs[j].numel()
+                j += 1
+            X = torch.cat(vs[i:j], dim=1 if l2r else 0)
+            if l2r:
+                dst.addmm_(X, X.t(), alpha=alpha)
+            else:
+                dst.addmm_(X.t(), X, alpha=alpha)
+            i = j
+    for ci, cj, vi, vj in cross:
+        p = dm.find(ci, cj)
+        if p == len(dm.keys):
+            r = vi.shape[0] if l2r else vi.shape[1]
+            cdim = vj.shape[0] if l2r else vj.shape[1]
+            p = dm.insert(torch.zeros((r, cdim), dtype=torch.float64, device=vi.device), ci, cj)
+        if l2r:
+            dm.blocks[p].addmm_(vi, vj.t(), alpha=alpha)
+        else:
+            dm.blocks[p].addmm_(vi.t(), vj, alpha=alpha)
+
+
+def split(u: DeviceMPSTensor, A0: DeviceMPSTensor, B0: DeviceMPSTensor, Mmax: int, cutoff: float, l2r: bool,
+          truncation: str = "svd", alpha: float = 0.0, engine=None, boundary=None, mpo=None):
+    """``tst << u`` then the truncation of ``SweepMPSUpdater`` (``sba/SweepMPSUpdater.h:186-203``):
+    ``split_mps_l2r/r2l`` (``truncation="svd"``, the reference's default) or
+    ``predict_split_l2r/r2l`` (``"heev"``, ``twositetensor.hpp:184-297``), whose
+    density matrix carries the perturbation alpha sum_b h_b h_b^T when ``boundary``
+    (left boundary of the pair going right, right boundary going left) and ``mpo``
+    (the left / right site's MPO tensor) are given and alpha != 0.  (The
+    reference computes the alpha = 0 perturbation and adds zeros; skipping it
+    gives the same matrix.)  Returns new (A, B, truncation results)."""
     _, tst = unreduce_left(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, as_dbm(u))
     both = _left_to_both(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, tst)
-    U, S, V, tr = svd_truncate(both, cutoff, Mmax)
     p1, p2 = A0.phys_i, B0.phys_i
-    if l2r:
-        SV = DBM()
-        for (lc, rc), b in zip(V.keys, V.blocks):
-            SV.insert(S[lc][:, None] * b, lc, rc)
-        A_lp = U
-        B_rp = SV
+    if truncation == "svd":
+        U, S, V, tr = svd_truncate(both, cutoff, Mmax)
+        if l2r:
+            SV = DBM()
+            for (lc, rc), b in zip(V.keys, V.blocks):
+                SV.insert(S[lc][:, None] * b, lc, rc)
+            A_lp = U
+            B_rp = SV
+        else:
+            US = DBM()
+            for (lc, rc), b in zip(U.keys, U.blocks):
+                US.insert(b * S[rc][None, :], lc, rc)
+            A_lp = US
+            B_rp = V
+    elif truncation in ("heev", "heev_truncation"):
+        bt = _transpose(both)
+        dm = gemm(both, bt) if l2r else gemm(bt, both)
+        if alpha != 0.0 and boundary is not None:
+            if engine is None or mpo is None:
+                raise ValueError("the heev perturbation needs the engine and the site's MPO tensor")
+            if l2r:
+                # theta as one site: phys p1, right index adjoin(p2) x right (from its blocks)
+                t_right = both.right_basis()
+                t_left = A0.left_i.copy()
+                common_subset(t_left, index_product(adjoin(p1), t_right))
+                tmp = from_dbm(p1, t_left, t_right, both)
+                half = engine.boundary_tensor_mpo(tmp, boundary, mpo, "left")
+            else:
+                # theta as one site: phys p2, left index p1 x left (from its blocks)
+                t_left = both.left_basis()
+                t_right = B0.right_i.copy()
+                common_subset(t_right, index_product(p2, t_left))
+                tmp = from_dbm(p2, t_left, t_right, reshape_r2l(p2, t_left, t_right, both))
+                half = engine.boundary_tensor_mpo(tmp, boundary, mpo, "right")
+            add_perturbation(dm, both, half, alpha, l2r)
+            del half
+        U, _, tr = heev_truncate(dm, cutoff, Mmax)
+        del dm
+        if l2r:
+            A_lp = U
+            B_rp = gemm(_transpose(U), both)
+        else:
+            B_rp = _transpose(U)
+            A_lp = gemm(both, U)
     else:
-        US = DBM()
-        for (lc, rc), b in zip(U.keys, U.blocks):
-            US.insert(b * S[rc][None, :], lc, rc)
-        A_lp = US
-        B_rp = V
+        raise ValueError(f"unknown twosite_truncation {truncation!r} (svd or heev)")
     # A: MPSTensor(p1, left, A_lp.right_basis(), A_lp, LeftPaired)
     a_right = A_lp.right_basis()
     a_left = A0.left_i.copy()
@@ -440,5 +580,5 @@ def multiply_from_right(t: DeviceMPSTensor, Nm: DBM) -> DeviceMPSTensor:
     return from_dbm(t.phys_i, left, new_right, tmp)
 
 
-__all__ = ["DBM", "block_views", "make_two_site_mps", "split", "svd_truncate", "left_normalize_and_return",
-           "right_normalize_and_return", "multiply_from_left", "multiply_from_right", "reshape_l2r", "reshape_r2l"]
+__all__ = ["DBM", "block_views", "make_two_site_mps", "split", "svd_truncate", "heev_truncate", "add_perturbation",
+           "left_normalize_and_return", "right_normalize_and_return", "multiply_from_left", "multiply_from_right", "reshape_l2r", "reshape_r2l"]

@@ -67,6 +67,9 @@ def lib():
     for name in ("qcm_plan_boundary_left", "qcm_plan_boundary_right"):
         getattr(L, name).argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks), C.POINTER(CBoundary),
                                                                C.POINTER(CMpo), C.c_int32, C.POINTER(C.c_void_p)]
+    L.qcm_plan_boundary_tensor_mpo.argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks), C.POINTER(CBoundary),
+                                                                      C.POINTER(CMpo), C.c_int32, C.c_int32,
+                                                                      C.POINTER(C.c_void_p)]
     L.qcm_plan_sizes.argtypes = [C.c_void_p, i64p, i64p]
     L.qcm_plan_image_bytes.argtypes = [C.c_void_p, i64p]
     L.qcm_plan_last_kernels.argtypes = [C.c_void_p, i32p]
@@ -428,5 +431,20 @@ def plan_boundary_right(phys, left_i, right_i, mps: Layout, R: BoundaryLayout, m
     return Plan(h, "bright")
 
 
+def plan_boundary_tensor_mpo(phys, left_i, right_i, mps: Layout, B: BoundaryLayout, mpo: FMpo, side: str,
+                             hermitian=True) -> Plan:
+    """``left_boundary_tensor_mpo`` (side "left") / ``right_boundary_tensor_mpo`` (side "right"):
+    the plan's output is the bra-free boundary, layout through ``out_layout``."""
+    if side not in ("left", "right"):
+        raise ValueError("side must be 'left' or 'right'")
+    fp, fl, fr = FIndex(phys), FIndex(left_i), FIndex(right_i)
+    h = C.c_void_p()
+    check(lib().qcm_plan_boundary_tensor_mpo(C.byref(fp.c), C.byref(fl.c), C.byref(fr.c), C.byref(mps.c),
+                                             C.byref(B.c), C.byref(mpo.c), 0 if side == "left" else 1,
+                                             1 if hermitian else 0, C.byref(h)), "qcm_plan_boundary_tensor_mpo")
+    return Plan(h, "btm_" + side)
+
+
 __all__ = ["lib", "check", "Layout", "BoundaryLayout", "FMpo", "FIndex", "Plan", "plan_sigma",
-           "plan_boundary_left", "plan_boundary_right", "PREC_FP64", "PREC_TF32", "PREC_BF16X3"]
+           "plan_boundary_left", "plan_boundary_right", "plan_boundary_tensor_mpo", "PREC_FP64", "PREC_TF32",
+           "PREC_BF16X3"]

@@ -42,6 +42,21 @@ class SweepParams:
     ietl_jcd_tol: float = 1e-8
     ietl_jcd_maxiter: int = 10
     seed: int = 42
+    # "svd" (default) or "heev" with the noise schedule below (DmrgParameters.h:45-59)
+    twosite_truncation: str = "svd"
+    alpha_initial: float = 1e-2
+    alpha_main: float = 1e-4
+    alpha_final: float = 1e-8
+    nmainsweeps: int = 5
+
+
+def get_alpha(p: SweepParams, sweep: int) -> float:
+    """``getAlpha`` (``sba/GenericSweepSimulation.h:242-253``)."""
+    if sweep < p.ngrowsweeps:
+        return p.alpha_initial
+    if sweep < p.ngrowsweeps + p.nmainsweeps:
+        return p.alpha_main
+    return p.alpha_final
 
 
 def _log_interpolate(y0, y1, N, i):
@@ -151,8 +166,9 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
              boundary_precision: Optional[int] = None):
     """Two-site sweeps.  ``precision`` selects the sigma-vector form (0 = FP64,
     1 = TF32, 2 = BF16x3 tensor cores); boundary updates, the eigensolver's
-    vector algebra, the subspace problem, the SVD truncation and the per-sweep
-    energy stay FP64.  ``boundary_precision`` (default: FP64) selects the form
+    vector algebra, the subspace problem, the truncation (SVD, or the
+    density-matrix eigendecomposition with ``twosite_truncation="heev"``) and the
+    per-sweep energy stay FP64.  ``boundary_precision`` (default: FP64) selects the form
     of the boundary updates' block products (the boundaries are stored in FP64
     either way).  ``mps`` (right-normalised) replaces the default initial
     state; ``ts_mpo`` is a prebuilt two-site MPO cache (``make_ts_cache_mpo``)."""
@@ -194,7 +210,14 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
             rec.energies.append(theta + mpo.core_energy)
             rec.jd_iterations.append(iters)
             rec.sigma_calls += iters
-            A, B, tr = O.split(u, mps[site], mps[site + 1], Mmax, cutoff, l2r)
+            if p.twosite_truncation == "svd":
+                A, B, tr = O.split(u, mps[site], mps[site + 1], Mmax, cutoff, l2r)
+            else:
+                # SweepMPSUpdater.h:192-203: the pair's left boundary and left site's MPO
+                # tensor going right, the right boundary and right site's tensor going left
+                bnd, w = (left[site], mpo[site]) if l2r else (right[site + 2], mpo[site + 1])
+                A, B, tr = O.split(u, mps[site], mps[site + 1], Mmax, cutoff, l2r, truncation=p.twosite_truncation,
+                                   alpha=get_alpha(p, sweep), engine=engine, boundary=bnd, mpo=w)
             mps[site], mps[site + 1] = A, B
             torch.cuda.synchronize()
             t_c = time.time()
@@ -231,4 +254,4 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
     return rec, mps
 
 
-__all__ = ["SweepParams", "SweepRecord", "run_dmrg", "default_mps_init", "normalize_right", "expval", "overlap"]
+__all__ = ["SweepParams", "SweepRecord", "run_dmrg", "get_alpha", "default_mps_init", "normalize_right", "expval", "overlap"]

@@ -1,0 +1,241 @@
+"""The density-matrix (heev) truncation of the two-site step
+(``TwoSiteTensor::predict_split_l2r/r2l``, ``twositetensor.hpp:184-297``;
+``heev_truncate``, ``block_matrix_algorithms.h:388-440``) and the bra-free
+boundary contractions that feed its perturbation
+(``left/right_boundary_tensor_mpo``, ``move_boundary.hpp:66-126``).
+
+The reference's tests hold no golden vectors for this path, so the oracle is
+pinned through its relations to the pinned paths: without noise the eigenvector
+cut keeps the same subspace as the SVD cut (eigenvalues = squared singular
+values, truncated fraction = SVD truncated weight), and contracting the
+bra-free boundary with the bra gives the boundary step.  The plan builder's
+tensor-MPO plans are checked against the oracle through the task-table
+interpreter; the GPU cases (marked) check the device path against the oracle."""
+import numpy as np
+import pytest
+
+from qcmaquis_gb300 import native as N
+from qcmaquis_gb300.block_matrix import BlockMatrix
+from qcmaquis_gb300.integrals import synthetic_integral_map
+from qcmaquis_gb300.model import QCModel
+from qcmaquis_gb300.mpo import make_mpo
+from qcmaquis_gb300.symmetry import adjoin, index_product
+
+from oracle import dmrg_ref as R
+from oracle.sweep import SweepParams, initial_state
+from plan_interp import run_plan
+
+
+def _pair_problem(L=6, Ne=6, m=16, site=2, seed=3):
+    """Two-site problem at (site, site+1) with the single-site MPO tensors:
+    (two-site tensor, A0, B0, left boundary, right boundary, mpo)."""
+    model = QCModel(L, synthetic_integral_map(L, seed=seed), Ne)
+    mpo = make_mpo(model)
+    mps = initial_state(model, mpo, SweepParams(init_bond_dimension=m, seed=11), Ne, 0)
+    left = R.left_boundary(mps[0])
+    for i in range(site):
+        t = R.left_normalize_and_return(mps[i])
+        R.multiply_from_left(mps[i + 1], t)
+        left = R.overlap_mpo_left_step(mps[i], mps[i], left, mpo[i])
+    right = R.right_boundary(mps[L - 1])
+    for i in range(L - 1, site + 1, -1):
+        right = R.overlap_mpo_right_step(mps[i], mps[i], right, mpo[i])
+    psi = R.make_two_site_mps(mps[site], mps[site + 1])
+    return model, mpo, mps, psi, left, right
+
+
+def _tst(psi, A0, B0):
+    u = psi.copy().make_left_paired()
+    _, tst = R.unreduce_left(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, u.data)
+    return tst
+
+
+def _theta(A, B):
+    return R.two_site_theta(A, B)
+
+
+def _block_pairs(a: BlockMatrix, b: BlockMatrix):
+    """(key, block of a, block of b) over the union of keys; a missing block is zeros."""
+    for k in sorted(set(a.keys) | set(b.keys), reverse=True):
+        pa, pb = a.find_block(*k), b.find_block(*k)
+        xa = a.blocks[pa] if pa < a.n_blocks() else None
+        xb = b.blocks[pb] if pb < b.n_blocks() else None
+        yield k, (np.zeros_like(xb) if xa is None else xa), (np.zeros_like(xa) if xb is None else xb)
+
+
+def _bm_close(a: BlockMatrix, b: BlockMatrix, tol):
+    """Same blocks (missing blocks count as zeros) within tol * max norm."""
+    scale = max(a.norm(), b.norm(), 1e-300)
+    for k, xa, xb in _block_pairs(a, b):
+        assert xa.shape == xb.shape, k
+        assert np.linalg.norm(xa - xb) <= tol * scale, k
+
+
+@pytest.mark.parametrize("l2r", [True, False])
+def test_oracle_heev_without_noise_keeps_the_svd_subspace(l2r):
+    model, mpo, mps, psi, left, right = _pair_problem()
+    A0, B0 = mps[2], mps[3]
+    tst = _tst(psi, A0, B0)
+    Mmax = 10
+    As, Bs, ts = R.split_mps(tst, A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, Mmax, 1e-16, l2r)
+    Ah, Bh, th = R.predict_split_mps(tst, A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, Mmax, 1e-16, l2r,
+                                     alpha=0.0, boundary=None)
+    assert th.bond_dimension == ts.bond_dimension
+    # the eigenvalue cut: fraction of discarded eigenvalues = SVD truncated weight
+    assert abs(th.truncated_fraction - ts.truncated_weight) <= 1e-9 * ts.truncated_weight + 1e-15
+    assert th.truncated_weight == th.truncated_fraction
+    _bm_close(_theta(Ah, Bh), _theta(As, Bs), 1e-10)
+
+
+def test_oracle_boundary_tensor_mpo_contracts_to_the_boundary_steps():
+    """sum over the bra of left/right_boundary_tensor_mpo = overlap_mpo_left/right_step."""
+    model, mpo, mps, psi, left, right = _pair_problem()
+    A = mps[2].copy().make_left_paired()
+    half = R.left_boundary_tensor_mpo(A, left, mpo[2])
+    # the boundaries hold no blocks at the Hermitian-skipped bonds: compare the others
+    ref = R.overlap_mpo_left_step(A, A, left, mpo[2])
+    assert len(half) == mpo[2].col_dim
+    for b2 in range(mpo[2].col_dim):
+        if mpo[2].herm.right_skip(b2):
+            continue
+        got = R.su2_gemm(half[b2].transpose(), A.data, mpo[2].right_spin(b2).get())
+        _bm_close(got, ref[b2], 1e-12)
+    B = mps[3].copy()
+    half = R.right_boundary_tensor_mpo(B, right, mpo[3])
+    refr = R.overlap_mpo_right_step(B, B, right, mpo[3])
+    Brp = B.copy().make_right_paired()
+    assert len(half) == mpo[3].row_dim
+    for b1 in range(mpo[3].row_dim):
+        if mpo[3].herm.left_skip(b1):
+            continue
+        got = R.su2_gemm(half[b1], Brp.data.transpose(), mpo[3].left_spin(b1).get())
+        _bm_close(got, refr[b1], 1e-12)
+
+
+@pytest.mark.parametrize("l2r", [True, False])
+def test_oracle_heev_with_noise_is_an_orthonormal_projection(l2r):
+    model, mpo, mps, psi, left, right = _pair_problem()
+    A0, B0 = mps[2], mps[3]
+    tst = _tst(psi, A0, B0)
+    both = R._reshape_left_to_both(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, tst)
+    bnd, w = (left, mpo[2]) if l2r else (right, mpo[3])
+    A, B, tr = R.predict_split_mps(tst, A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, 10, 1e-16, l2r,
+                                   alpha=1e-2, boundary=bnd, mpo=w)
+    An, Bn, _ = R.predict_split_mps(tst, A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, 10, 1e-16, l2r,
+                                    alpha=0.0, boundary=None)
+    # the kept factor is orthonormal (left-normalised A going right, right-normalised B going left)
+    iso = A.copy().make_left_paired().data if l2r else B.copy().make_right_paired().data
+    for b in iso.blocks:
+        g = b.T @ b if l2r else b @ b.T
+        assert np.allclose(g, np.eye(g.shape[0]), atol=1e-12)
+    # the kept two-site state is theta's orthogonal projection onto the kept subspace
+    kept = _theta(A, B)
+    cross = sum(float(np.vdot(xk, xt - xk)) for _, xk, xt in _block_pairs(kept, both))
+    assert abs(cross) <= 1e-12 * both.norm() ** 2
+    assert 0 < tr.bond_dimension <= 11
+    # the noise moves the kept subspace away from the noiseless one
+    diff = np.sqrt(sum(np.linalg.norm(x - y) ** 2 for _, x, y in _block_pairs(kept, _theta(An, Bn))))
+    assert diff > 1e-8 * both.norm()
+
+
+@pytest.mark.parametrize("side", ["left", "right"])
+def test_tensor_mpo_plans_match_oracle(side):
+    """qcm_plan_boundary_tensor_mpo on the two-site tensor seen as one site, as the
+    heev perturbation uses it, through the task-table interpreter."""
+    model, mpo, mps, psi, left, right = _pair_problem()
+    A0, B0 = mps[2], mps[3]
+    tst = _tst(psi, A0, B0)
+    both = R._reshape_left_to_both(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, tst)
+    if side == "left":
+        tmp = R.MPSTensor.from_block(A0.phys_i, A0.left_i, index_product(adjoin(B0.phys_i), B0.right_i), both,
+                                     R.LEFT_PAIRED)
+        ref = R.left_boundary_tensor_mpo(tmp, left, mpo[2])
+        bnd, w = left, mpo[2]
+    else:
+        tmp = R.MPSTensor.from_block(B0.phys_i, index_product(A0.phys_i, A0.left_i), B0.right_i, both,
+                                     R.RIGHT_PAIRED)
+        ref = R.right_boundary_tensor_mpo(tmp, right, mpo[3])
+        bnd, w = right, mpo[3]
+    t = tmp.copy().make_left_paired()
+    lay, Bl = N.Layout.of(t.data), N.BoundaryLayout.of(bnd)
+    p = N.plan_boundary_tensor_mpo(t.phys_i, t.left_i, t.right_i, lay, Bl, N.FMpo(w), side, True)
+    ol = p.out_layout()
+    assert ol.aux == len(ref)
+    bufs = [lay.pack(t.data), Bl.pack(bnd) if side == "left" else None, Bl.pack(bnd) if side == "right" else None,
+            np.full(max(p.out_elems, 1), np.nan)] + [np.full(max(s, 1), np.nan) for s in p.scratch]
+    run_plan(p, bufs)
+    got = ol.unpack(bufs[3])
+    assert [g.keys for g in got] == [r.keys for r in ref]
+    assert np.allclose(ol.pack(ref), bufs[3][:ol.size], rtol=0, atol=1e-13)
+
+
+def test_tensor_mpo_plan_rejects_a_bad_side():
+    lib = N.lib()
+    import ctypes as C
+    h = C.c_void_p()
+    assert lib.qcm_plan_boundary_tensor_mpo(None, None, None, None, None, None, 2, 1, C.byref(h)) != 0
+    assert "side" in lib.qcm_last_error().decode()
+
+
+# ------------------------------------------------------------------ GPU
+def _host_theta(A, B):
+    """Two-site product of device tensors, on the host."""
+    a = R.MPSTensor(A.phys_i, A.left_i, A.right_i, A.to_block_matrix(), R.LEFT_PAIRED)
+    b = R.MPSTensor(B.phys_i, B.left_i, B.right_i, B.to_block_matrix(), R.LEFT_PAIRED)
+    return R.two_site_theta(a, b)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("l2r", [True, False])
+@pytest.mark.parametrize("alpha", [0.0, 1e-2])
+def test_gpu_heev_split_matches_oracle(l2r, alpha):
+    from qcmaquis_gb300 import mps_ops as O
+    from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
+    model, mpo, mps, psi, left, right = _pair_problem(m=24)
+    A0, B0 = mps[2], mps[3]
+    tst = _tst(psi, A0, B0)
+    bnd, w = (left, mpo[2]) if l2r else (right, mpo[3])
+    Ar, Br, tr = R.predict_split_mps(tst, A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, 12, 1e-16, l2r,
+                                     alpha=alpha, boundary=bnd, mpo=w)
+    eng = Engine("cuda:0")
+    dA0 = DeviceMPSTensor.from_host(A0.copy().make_left_paired())
+    dB0 = DeviceMPSTensor.from_host(B0.copy().make_left_paired())
+    u = DeviceMPSTensor.from_host(psi.copy().make_left_paired())
+    A, B, tg = O.split(u, dA0, dB0, 12, 1e-16, l2r, truncation="heev", alpha=alpha, engine=eng,
+                       boundary=DeviceBoundary.from_host(bnd), mpo=w)
+    assert tg.bond_dimension == tr.bond_dimension
+    assert abs(tg.truncated_fraction - tr.truncated_fraction) <= 1e-8 * tr.truncated_fraction + 1e-14
+    assert abs(tg.smallest_ev - tr.smallest_ev) <= 1e-8 * tr.smallest_ev + 1e-16
+    _bm_close(_host_theta(A, B), R.two_site_theta(Ar, Br), 1e-10)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("side", ["left", "right"])
+def test_gpu_boundary_tensor_mpo_matches_oracle(side):
+    from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
+    model, mpo, mps, psi, left, right = _pair_problem()
+    t = mps[2] if side == "left" else mps[3]
+    bnd, w = (left, mpo[2]) if side == "left" else (right, mpo[3])
+    ref = (R.left_boundary_tensor_mpo if side == "left" else R.right_boundary_tensor_mpo)(t, bnd, w)
+    eng = Engine("cuda:0")
+    got = eng.boundary_tensor_mpo(DeviceMPSTensor.from_host(t.copy().make_left_paired()),
+                                  DeviceBoundary.from_host(bnd), w, side)
+    lay = got.layout
+    assert np.allclose(lay.pack(ref), got.data.cpu().numpy()[:lay.size], rtol=0, atol=1e-13)
+
+
+@pytest.mark.gpu
+def test_gpu_heev_sweep_matches_oracle():
+    """Two heev sweeps with the reference's noise schedule (alpha 1e-2 in the
+    growth sweeps): per-sweep energies to 1e-10 Eh of the oracle's."""
+    from qcmaquis_gb300 import sweep as G
+    from oracle.sweep import SweepParams as OP, run_dmrg as oracle_dmrg
+    L, Ne, m = 6, 6, 24
+    model = QCModel(L, synthetic_integral_map(L, seed=3), Ne)
+    mpo = make_mpo(model)
+    gpu, _ = G.run_dmrg(model, mpo, G.SweepParams(nsweeps=2, max_bond_dimension=m, twosite_truncation="heev"),
+                        nelec=Ne)
+    ref, _ = oracle_dmrg(model, mpo, OP(nsweeps=2, max_bond_dimension=m, twosite_truncation="heev"), nelec=Ne)
+    assert np.max(np.abs(np.array(gpu.energies) - np.array(ref.energies))) < 1e-10
+    assert np.max(np.abs(np.array(gpu.sweep_energy) - np.array(ref.sweep_energy))) < 1e-10
+    assert gpu.bond_dimension == ref.bond_dimension
