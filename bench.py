@@ -118,6 +118,19 @@ def measured_peaks():
     return {}
 
 
+def captured_traffic(L: int, m: int):
+    """DRAM bytes per sigma of the roofline kernel (K1 + K3 stages) from the committed
+    summary of one ncu capture of this workload, or None for another size."""
+    path = os.path.join(ROOT, "profiles", f"sigma_bf16x3_L{L}_m{m}_traffic.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_k1_k3 ="):
+                return int(line.split("=")[1])
+    return None
+
+
 def dgemm_peak_tflops():
     """cuBLAS FP64 GEMM rate on this GPU, measured live (4096^3, best of 3)."""
     import torch
@@ -361,8 +374,13 @@ def main():
         peak = peaks.get("bf16_tflops", 1900.0)
         nprod = 6 if prec == N.PREC_BF16X3 else 1
         ach = plan.gemm_flops * nprod / gemm_t / 1e12
+        traffic = captured_traffic(args.L, args.m) if (prec == N.PREC_BF16X3 and not args.no_images) else None
         roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                "traffic": None,
+                "traffic": traffic,
+                "traffic_source": (f"profiles/sigma_bf16x3_L{args.L}_m{args.m}_traffic.md (ncu dram__bytes_read.sum "
+                                   "+ dram__bytes_write.sum over the K1 and K3 launches of one sigma)")
+                if traffic else None,
+                "traffic_gbs": traffic / gemm_t / 1e9 if traffic else None,
                 "kernel": ("tc_img_kernel + build_images_kernel (tcgen05 K1 + K3 block products from "
                            "bulk-copied BF16 slice images)" if (prec == N.PREC_BF16X3 and not args.no_images)
                            else "tc_gemm_kernel (tcgen05 K1 + K3 grouped block products)"),

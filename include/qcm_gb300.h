@@ -163,6 +163,22 @@ int qcm_plan_boundary_tensor_mpo(const qcm_index_t* phys, const qcm_index_t* lef
                                  const qcm_blocks_t* mps, const qcm_boundary_t* boundary, const qcm_mpo_t* mpo,
                                  int32_t side, int32_t hermitian, qcm_plan** plan);
 
+/* Gradient of the local energy E = <psi| H_eff psi> (the contraction of
+ * qcm_plan_sigma, same arguments) with respect to every term scale of the MPO
+ * tensor: OUT[t] = dE/d term_scale[t], t indexing the flattened term arrays of
+ * qcm_mpo_t (out_elems = their length).  With left = L[j], right = R[j+1] and
+ * psi = the site tensor of a single-site problem at j, E is <Psi|H|Psi> of the
+ * whole MPS, so OUT is the derivative of the energy expectation value with
+ * respect to the site-j MPO coefficients -- the adjoint behind dE/d(t_pq),
+ * dE/d(V_pqrs) and the RDMs.  Stages: K1, the adjoint of K3 (Y = dE/dcontr,
+ * grouped GEMM), per-term dots of the K2 tables against Y and their sums per
+ * term scale.  FP64 form only (other precisions: QCM_E_INVALID).  Not a
+ * reference entry point: the reference obtains RDMs by separate expectation
+ * values (dmrg/framework/dmrg/models/measurements/tagged_nrankrdm_su2u1.h). */
+int qcm_plan_energy_gradient(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                             const qcm_blocks_t* psi, const qcm_boundary_t* left, const qcm_boundary_t* right,
+                             const qcm_mpo_t* mpo, int32_t hermitian, qcm_plan** plan);
+
 /* Sizes (elements) of the output and of the three scratch slots. */
 int qcm_plan_sizes(const qcm_plan* plan, int64_t* out_elems, int64_t* scratch_elems3);
 
@@ -186,13 +202,19 @@ int qcm_plan_work(const qcm_plan* plan, double* gemm_flops, double* axpy_flops, 
 int qcm_plan_out_layout(const qcm_plan* plan, int32_t* aux, int32_t* nblocks, int32_t* blk_ptr,
                         int32_t* q, int64_t* rows, int64_t* cols, int64_t* off);
 
-/* Stage export for host-side inspection: kind 0 = gather-axpy, 1 = grouped GEMM. */
+/* Stage export for host-side inspection: kind 0 = gather-axpy, 1 = grouped GEMM,
+ * 2 = clear (n_out = slot, n_terms = length), 3 = per-term dots of an energy-gradient plan. */
 int qcm_plan_num_stages(const qcm_plan* plan, int32_t* n);
 int qcm_plan_stage_info(const qcm_plan* plan, int32_t stage, int32_t* kind, int64_t* n_out, int64_t* n_terms);
 int qcm_plan_stage_axpy(const qcm_plan* plan, int32_t stage, int64_t* out_desc /*7*n_out*/,
                         int64_t* term_desc /*3*n_terms*/, double* term_alpha);
 int qcm_plan_stage_gemm(const qcm_plan* plan, int32_t stage, int64_t* out_desc /*7*n_out*/,
                         int64_t* seg_desc /*9*n_terms*/, double* seg_alpha);
+/* Dot stage: output-adjoint tiles (7 per tile, as qcm_plan_stage_axpy), terms
+ * (3 each), per-term weight and MPO term index; meta = {dot buffer slot, number
+ * of MPO terms}. */
+int qcm_plan_stage_dot(const qcm_plan* plan, int32_t stage, int64_t* out_desc, int64_t* term_desc, double* weight,
+                       int32_t* term_index, int32_t* meta);
 
 /* Export the BF16x3 image-executor tables of a stage (host-side inspection
  * and tests): the block products of a GEMM stage, or the dense groups of a

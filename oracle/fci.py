@@ -48,6 +48,51 @@ def _apply_cre(det, p):
 
 def fci_energies(L, ints, nelec, twoS=0, nroots=1):
     """Lowest eigenvalues with total spin S = twoS/2 (Sz = S sector filtered by S^2)."""
+    return [e for e, _ in fci_states(L, ints, nelec, twoS, nroots)[0]]
+
+
+def fci_rdms(L, dets, vec):
+    """Spin-summed RDMs of a CI vector: gamma_pq = sum_s <a+_ps a_qs> and the
+    chemist-ordered Gamma_pqrs = sum_st <a+_ps a+_rt a_st a_qs>, so that
+    E = core + sum t_pq gamma_pq + 1/2 sum (pq|rs) Gamma_pqrs."""
+    index = {d: i for i, d in enumerate(dets)}
+    g1 = np.zeros((L, L))
+    g2 = np.zeros((L, L, L, L))
+    for col, d in enumerate(dets):
+        c = vec[col]
+        if c == 0.0:
+            continue
+        for p in range(L):
+            for q in range(L):
+                for s in (0, 1):
+                    d1, s1 = _apply_ann(d, 2 * q + s)
+                    if d1 is None:
+                        continue
+                    d2, s2 = _apply_cre(d1, 2 * p + s)
+                    if d2 is None or d2 not in index:
+                        continue
+                    g1[p, q] += vec[index[d2]] * c * s1 * s2
+        for p, q, r, s_ in itertools.product(range(L), repeat=4):
+            for sa in (0, 1):
+                for sb in (0, 1):
+                    d1, h1 = _apply_ann(d, 2 * q + sa)
+                    if d1 is None:
+                        continue
+                    d2, h2 = _apply_ann(d1, 2 * s_ + sb)
+                    if d2 is None:
+                        continue
+                    d3, h3 = _apply_cre(d2, 2 * r + sb)
+                    if d3 is None:
+                        continue
+                    d4, h4 = _apply_cre(d3, 2 * p + sa)
+                    if d4 is None or d4 not in index:
+                        continue
+                    g2[p, q, r, s_] += vec[index[d4]] * c * h1 * h2 * h3 * h4
+    return g1, g2
+
+
+def fci_states(L, ints, nelec, twoS=0, nroots=1):
+    """([(energy, CI vector)], determinants) of the lowest states with total spin twoS/2."""
     t, V, core = expand_integrals(L, ints)
     nalpha = (nelec + twoS) // 2
     nbeta = nelec - nalpha
@@ -125,7 +170,7 @@ def fci_energies(L, ints, nelec, twoS=0, nroots=1):
     for k in range(n):
         s2 = float(U[:, k] @ S2 @ U[:, k])
         if abs(s2 - target) < 1e-6:
-            out.append(float(w[k]))
+            out.append((float(w[k]), U[:, k].copy()))
             if len(out) == nroots:
                 break
-    return out
+    return out, dets

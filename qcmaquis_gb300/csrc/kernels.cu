@@ -291,6 +291,65 @@ gather_axpy_contig(BufTable bufs, const DevAxpyOut* __restrict__ outs, const Dev
 // source tile (transitively) form one group; groups run one after another,
 // and inside a group all tiles' chunk 0 runs before any chunk 1, and so on.
 // Returns false (and no list) when some term's source is not contiguous.
+// ------------------------------------------------------------------ adjoint (energy gradient)
+// One term of a DOT stage: a source tile and the output-adjoint tile it pairs with.
+struct DevDotTerm {
+    int64_t src_off, lds, dst_off, ldd;
+    int32_t rows, cols, src_buf, dst_buf;
+};
+constexpr int DOT_THREADS = 256;
+
+// g[k] = sum over the tile of src_k * dst_k (FP64), one CTA per term at a time; the
+// element order and the reduction tree are fixed, so the result is deterministic.
+__global__ void __launch_bounds__(DOT_THREADS) dot_terms_kernel(BufTable bt, const DevDotTerm* __restrict__ terms,
+                                                                int64_t n, double* __restrict__ g) {
+    __shared__ double red[DOT_THREADS / 32];
+    for (int64_t k = blockIdx.x; k < n; k += gridDim.x) {
+        const DevDotTerm t = terms[k];
+        const double* __restrict__ src = bt.p[t.src_buf] + t.src_off;
+        const double* __restrict__ dst = bt.p[t.dst_buf] + t.dst_off;
+        double acc = 0.0;
+        if (t.rows >= 32) {
+            // warps over columns, lanes down the column
+            const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            for (int c = warp; c < t.cols; c += DOT_THREADS / 32) {
+                const double* sc = src + (int64_t)c * t.lds;
+                const double* dc = dst + (int64_t)c * t.ldd;
+                for (int r = lane; r < t.rows; r += 32) acc = fma(sc[r], dc[r], acc);
+            }
+        } else {
+            const int64_t ne = (int64_t)t.rows * t.cols;
+            for (int64_t e = threadIdx.x; e < ne; e += DOT_THREADS) {
+                const int64_t c = e / t.rows, r = e - c * t.rows;
+                acc = fma(src[r + c * t.lds], dst[r + c * t.ldd], acc);
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double v = 0.0;
+            for (int w = 0; w < DOT_THREADS / 32; ++w) v += red[w];
+            g[k] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// out[tt] = sum over the terms of tt (ascending term index) of w[k] g[k]
+__global__ void dot_reduce_kernel(const int64_t* __restrict__ ptr, const int64_t* __restrict__ idx,
+                                  const double* __restrict__ w, const double* __restrict__ g, int32_t n_tt,
+                                  double* __restrict__ out) {
+    const int32_t tt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tt >= n_tt) return;
+    double acc = 0.0;
+    for (int64_t q = ptr[tt]; q < ptr[tt + 1]; ++q) {
+        const int64_t k = idx[q];
+        acc = fma(w[k], g[k], acc);
+    }
+    out[tt] = acc;
+}
+
 static bool build_chunk_work(const Stage& st, std::vector<DevAxpyChunk>& w) {
     const size_t nO = st.aout.size();
     for (size_t i = 0; i < nO; ++i) {
@@ -404,7 +463,7 @@ void free_stage_device(Stage& st) {
     if (st.d_tcw) cudaFree(st.d_tcw);
     if (st.d_cw) cudaFree(st.d_cw);
     for (void** d : {&st.d_ipanel, &st.d_ibuild, &st.d_iout, &st.d_iseg, &st.d_iunit, &st.d_igather, &st.d_icoltab,
-                     &st.d_icimg, &st.d_cw_light, &st.d_icost}) {
+                     &st.d_icimg, &st.d_cw_light, &st.d_icost, &st.d_dterm, &st.d_dptr, &st.d_didx, &st.d_dw}) {
         if (*d) cudaFree(*d);
         *d = nullptr;
     }
@@ -443,6 +502,34 @@ static int upload_images(Stage& st) {
 
 static int upload_stage(Stage& st) {
     int rc = QCM_OK;
+    if (st.kind == ST_DOT) {
+        std::vector<DevDotTerm> t(st.aterm.size());
+        for (const AxpyOut& o : st.aout) {
+            if (o.rows >= (int64_t(1) << 31) || o.cols >= (int64_t(1) << 31)) {
+                set_error("dot tile too large");
+                return QCM_E_RANGE;
+            }
+            for (int64_t k = o.t_begin; k < o.t_end; ++k) {
+                const AxpyTerm& a = st.aterm[k];
+                t[k] = {a.src_off, a.lds, o.dst_off, o.ldd, (int32_t)o.rows, (int32_t)o.cols, a.src_buf, o.dst_buf};
+            }
+        }
+        // terms of each parameter in ascending term order (counting sort)
+        std::vector<int64_t> ptr(st.n_tt + 1, 0), idx(st.dot_tt.size());
+        for (int32_t tt : st.dot_tt) {
+            if (tt < 0 || tt >= st.n_tt) { set_error("dot parameter index out of range"); return QCM_E_RANGE; }
+            ++ptr[tt + 1];
+        }
+        for (int32_t i = 0; i < st.n_tt; ++i) ptr[i + 1] += ptr[i];
+        std::vector<int64_t> fill(ptr.begin(), ptr.end() - 1);
+        for (size_t k = 0; k < st.dot_tt.size(); ++k) idx[fill[st.dot_tt[k]]++] = (int64_t)k;
+        if ((rc = upload_vec(t, &st.d_dterm))) return rc;
+        if ((rc = upload_vec(ptr, &st.d_dptr))) return rc;
+        if ((rc = upload_vec(idx, &st.d_didx))) return rc;
+        if ((rc = upload_vec(st.dot_w, &st.d_dw))) return rc;
+        st.n_work = (int64_t)t.size();
+        return QCM_OK;
+    }
     if (st.kind == ST_AXPY) {
         std::vector<DevAxpyOut> o(st.aout.size());
         std::vector<DevAxpyTerm> t(st.aterm.size());
@@ -604,7 +691,25 @@ static int stage_kernels(const Stage& st, const BufTable& bt, int precision) {
         if (st.n_work == 0) return 0;
         return images ? (st.img.build.empty() ? 0 : 1) + 1 : 1;
     }
+    if (st.kind == ST_DOT) return (st.n_work > 0 ? 1 : 0) + (st.n_tt > 0 ? 1 : 0);
     return 0;
+}
+
+static int launch_dot(const Stage& st, const BufTable& bt, cudaStream_t s) {
+    double* g = bt.p[st.dot_buf];
+    double* out = bt.p[QCM_BUF_OUT];
+    if (!out || (st.n_work > 0 && !g)) { set_error("missing buffer for the gradient stage"); return QCM_E_INVALID; }
+    if (st.n_work > 0) {
+        const unsigned grid = (unsigned)std::min<int64_t>(st.n_work, 152 * 16);
+        dot_terms_kernel<<<grid, DOT_THREADS, 0, s>>>(bt, (const DevDotTerm*)st.d_dterm, st.n_work, g);
+        QCM_CUDA(cudaGetLastError());
+    }
+    if (st.n_tt > 0) {
+        dot_reduce_kernel<<<(st.n_tt + 127) / 128, 128, 0, s>>>((const int64_t*)st.d_dptr, (const int64_t*)st.d_didx,
+                                                              (const double*)st.d_dw, g, st.n_tt, out);
+        QCM_CUDA(cudaGetLastError());
+    }
+    return QCM_OK;
 }
 
 // ------------------------------------------------------------------ vector kernels
@@ -788,6 +893,10 @@ int qcm_plan_run_typed(qcm_plan* p, double* const* bufs, uint32_t f32mask, int32
         set_error("unknown precision");
         return QCM_E_INVALID;
     }
+    if (p->kind == PK_GRAD && (precision != QCM_PREC_FP64 || f32mask != 0)) {
+        set_error("energy-gradient plans run in the FP64 form only");
+        return QCM_E_INVALID;
+    }
     BufTable bt;
     for (int i = 0; i < QCM_NBUF; ++i) bt.p[i] = bufs[i];
     bt.f32mask = f32mask;
@@ -805,6 +914,8 @@ int qcm_plan_run_typed(qcm_plan* p, double* const* bufs, uint32_t f32mask, int32
             }
         } else if (st.kind == ST_AXPY) {
             rc = launch_axpy(st, bt, precision, s);
+        } else if (st.kind == ST_DOT) {
+            rc = launch_dot(st, bt, s);
         } else {
             rc = launch_gemm(st, bt, precision, s);
         }

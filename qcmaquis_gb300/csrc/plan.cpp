@@ -459,16 +459,19 @@ static std::vector<BM> plan_k1(const std::vector<BM>& L, const MpoV& W, bool her
 }
 
 // K2: contr[b2] = sum_{b1,op} couplings x stripes of T[b1]  (lbtm_kernel).
+// prov (optional): per emitted term, in aterm order, the MPO term it comes from
+// (index into term_op/term_scale) and its coefficient per unit of that term's scale.
 static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const std::vector<int>& b2list,
                                const Idx& right_i, const Idx& out_left_i, const PB& in_right_pb,
-                               const PB& out_left_pb, int t_buf, int c_buf, Stage& st, qcm_plan* P, int64_t& end) {
+                               const PB& out_left_pb, int t_buf, int c_buf, Stage& st, qcm_plan* P, int64_t& end,
+                               std::vector<std::pair<int32_t, double>>* prov = nullptr) {
     const qcm_mpo_t* m = W.m;
     std::vector<BM> C(m->col_dim);
     // the terms of one b2 column with their tile keys, sorted (stably) by key
     // afterwards.  key = position of out_l in out_left_i (16 bits), of out_r in
     // right_i (16 bits), row offset (32 bits): ascending keys are the reference's
     // block order (both indices descend) with row offsets ascending.
-    struct KeyedTerm { uint64_t key; int64_t src_off; double alpha; int32_t rows, cols; };
+    struct KeyedTerm { uint64_t key; int64_t src_off; double alpha; int32_t rows, cols, tt; };
     using TileMap = std::vector<KeyedTerm>;
     if (out_left_i.size() >= (1u << 16) || right_i.size() >= (1u << 16))
         throw std::runtime_error("too many sectors for the K2 planner");
@@ -516,7 +519,7 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
                             const uint64_t key = ((uint64_t)pl << 48) | ((uint64_t)rb << 32) |
                                                  (uint64_t)(uint32_t)(olo + ss2 * l_size);
                             out.terms.push_back({key, tb.off + (iro + (int64_t)ss1 * r_size) * l_size, alfa,
-                                                 (int32_t)l_size, (int32_t)r_size});
+                                                 (int32_t)l_size, (int32_t)r_size, tt});
                             out.flops += 2.0 * l_size * r_size;
                         }
                     }
@@ -607,6 +610,7 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
     }
     st.aout.resize(obase[b2list.size()]);
     st.aterm.resize(tbase[b2list.size()]);
+    if (prov) prov->assign(st.aterm.size(), {0, 0.0});
     std::vector<double> bytes(b2list.size(), 0.0);
     parallel(b2list.size(), [&](size_t i) {
         const int b2 = b2list[i];
@@ -625,7 +629,10 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
             o.rows = v[b - 1].rows;
             o.cols = v[b - 1].cols;
             o.t_begin = (int64_t)ti;
-            for (size_t k = a; k < b; ++k) st.aterm[ti++] = {t_buf, v[k].src_off, v[k].rows, v[k].alpha};
+            for (size_t k = a; k < b; ++k) {
+                if (prov) (*prov)[ti] = {v[k].tt, v[k].alpha / m->term_scale[v[k].tt]};
+                st.aterm[ti++] = {t_buf, v[k].src_off, v[k].rows, v[k].alpha};
+            }
             o.t_end = (int64_t)ti;
             bytes[i] += 8.0 * o.rows * o.cols * (double)(b - a + 1);
             a = b;
@@ -851,6 +858,110 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
     P->stages.push_back(std::move(s2));
     P->stages.push_back(std::move(s3));
     if (!s4.aout.empty()) P->stages.push_back(std::move(s4));
+    return P;
+}
+
+// Gradient of the local energy E = <psi| H_eff psi> (the sigma plan's
+// contraction, E = sum over psi blocks of <psi, sigma>) with respect to every
+// MPO term scale w: E is linear in each K2 coefficient alpha_k = w_tt a_k, so
+//   dE/dw_tt = sum over the K2 terms k of tt of a_k <T[src_k], Y[dst_k]>,
+// with Y = dE/dcontr the adjoint of K3: for the K3 segment
+// sigma_ob += alpha contr_a op(R), Y_a = alpha psi_ob op(R)^T.  Stages: psi
+// right-paired (S0), K1 (T in S1), Y (grouped GEMM into S2, contr's layout),
+// then the per-term dots (into S0) and the per-term-scale sums (into OUT).
+static qcm_plan* build_grad(const Idx& phys, const Idx& left_i, const Idx& right_i, const BM& psi,
+                            const std::vector<BM>& L, const std::vector<BM>& R, const MpoV& W, bool herm) {
+    auto* P = new qcm_plan();
+    P->kind = PK_GRAD;
+    const qcm_mpo_t* m = W.m;
+    if ((int)L.size() != m->row_dim || (int)R.size() != m->col_dim)
+        throw std::runtime_error("boundary aux dimensions do not match the MPO");
+    Idx out_left_i = index_product(phys, left_i);
+    Idx rib = right_i;
+    common_subset(out_left_i, rib);
+    PB out_left_pb(phys, left_i, false), in_right_pb(phys, right_i, true);
+    Stage z0; z0.kind = ST_ZERO; z0.zbuf = QCM_BUF_S0;
+    Stage s0; int64_t rp_end = 0;
+    BM rp = plan_reshape_l2r(phys, left_i, right_i, psi, QCM_BUF_KET, QCM_BUF_S0, s0, P, rp_end);
+    z0.zlen = rp_end;
+    Idx ref;
+    for (auto& b : rp.b) ref.d.push_back({b.lc, b.rows});
+    Stage s1; int64_t t_end = 0;
+    std::vector<BM> T = plan_k1(L, W, herm, rp, QCM_BUF_S0, ref, QCM_BUF_S1, s1, P, t_end);
+    std::vector<int> b2list;
+    for (int b2 = 0; b2 < m->col_dim; ++b2) b2list.push_back(b2);
+    Stage k2; int64_t c_end = 0;
+    std::vector<std::pair<int32_t, double>> prov;
+    std::vector<BM> C = plan_k2(T, W, b2list, right_i, out_left_i, in_right_pb, out_left_pb, QCM_BUF_S1,
+                                QCM_BUF_S2, k2, P, c_end, &prov);
+    // Y = dE/dcontr in S2 (blocks no K3 segment reads stay zero)
+    Stage zy; zy.kind = ST_ZERO; zy.zbuf = QCM_BUF_S2; zy.zlen = c_end;
+    Stage sy; sy.kind = ST_GEMM;
+    for (auto& ob : psi.b) {
+        if (!(ob.lc == ob.rc)) throw std::runtime_error("psi layout is not block diagonal (left-paired)");
+        Q al = ob.lc;
+        for (int b2 = 0; b2 < m->col_dim; ++b2) {
+            const BM& cb = C[b2];
+            size_t it = cb.left_lower_bound(al);
+            for (; it < cb.b.size() && cb.b[it].lc == al; ++it) {
+                const Blk& a = cb.b[it];
+                Q ar = a.rc;
+                GemmSeg s;
+                s.a_buf = QCM_BUF_KET; s.ta = 0; s.a_off = ob.off; s.lda = ob.rows; s.K = ob.cols;
+                if (herm && W.rskip(b2)) {
+                    // K3 read R_conj (al, ar) transposed: Y_a = alpha psi_ob R_conj
+                    const BM& rs = R[W.rconj(b2)];
+                    size_t k = rs.find(al, ar);
+                    if (k == rs.b.size()) continue;
+                    s.b_buf = QCM_BUF_RIGHT; s.tb = 0; s.b_off = rs.b[k].off; s.ldb = rs.b[k].rows;
+                    s.alpha = conjugate_correction(ar.s, al.s, W.rspin(b2)) * W.rphase(W.rconj(b2));
+                    if (rs.b[k].cols != a.cols || rs.b[k].rows != ob.cols)
+                        throw std::runtime_error("gradient: K3 dimension mismatch (adjoint)");
+                } else {
+                    // K3 read R (ar, al): Y_a = psi_ob R^T
+                    const BM& rs = R[b2];
+                    size_t k = rs.find(ar, al);
+                    if (k == rs.b.size()) continue;
+                    s.b_buf = QCM_BUF_RIGHT; s.tb = 1; s.b_off = rs.b[k].off; s.ldb = rs.b[k].rows;
+                    s.alpha = 1.0;
+                    if (rs.b[k].rows != a.cols || rs.b[k].cols != ob.cols)
+                        throw std::runtime_error("gradient: K3 dimension mismatch");
+                }
+                if (a.rows != ob.rows) throw std::runtime_error("gradient: K3 row mismatch");
+                GemmOut o;
+                o.c_buf = QCM_BUF_S2; o.c_off = a.off; o.ldc = a.rows; o.M = a.rows; o.N = a.cols;
+                o.s_begin = (int64_t)sy.gseg.size();
+                sy.gseg.push_back(s);
+                o.s_end = (int64_t)sy.gseg.size();
+                sy.gout.push_back(o);
+                P->gemm_flops += 2.0 * a.rows * a.cols * ob.cols;
+            }
+        }
+    }
+    // the per-term dots of K2's tables against Y, and the sums per MPO term scale
+    Stage sd; sd.kind = ST_DOT;
+    sd.aout = std::move(k2.aout);
+    sd.aterm = std::move(k2.aterm);
+    sd.dot_w.resize(prov.size());
+    sd.dot_tt.resize(prov.size());
+    for (size_t k = 0; k < prov.size(); ++k) {
+        sd.dot_tt[k] = prov[k].first;
+        sd.dot_w[k] = prov[k].second;
+    }
+    // the output tiles already point into S2, where Y has contr's layout
+    for (const AxpyOut& o : sd.aout) P->axpy_flops += 2.0 * o.rows * o.cols * (double)(o.t_end - o.t_begin);
+    sd.dot_buf = QCM_BUF_S0;
+    sd.n_tt = m->term_ptr[m->col_ptr[m->col_dim]];
+    P->out_elems = sd.n_tt;
+    P->scratch[0] = std::max(rp_end, (int64_t)sd.aterm.size());
+    P->scratch[1] = t_end;
+    P->scratch[2] = c_end;
+    P->stages.push_back(std::move(z0));
+    P->stages.push_back(std::move(s0));
+    P->stages.push_back(std::move(s1));
+    P->stages.push_back(std::move(zy));
+    P->stages.push_back(std::move(sy));
+    P->stages.push_back(std::move(sd));
     return P;
 }
 
@@ -1624,6 +1735,22 @@ int qcm_plan_boundary_left(const qcm_index_t* phys, const qcm_index_t* left_i, c
     }
 }
 
+int qcm_plan_energy_gradient(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                             const qcm_blocks_t* psi, const qcm_boundary_t* left, const qcm_boundary_t* right,
+                             const qcm_mpo_t* mpo, int32_t hermitian, qcm_plan** plan) {
+    if (!plan) { set_error("null plan pointer"); return QCM_E_INVALID; }
+    try {
+        MpoV W(mpo);
+        *plan = build_grad(read_index(phys), read_index(left_i), read_index(right_i), read_blocks(psi),
+                           read_boundary(left), read_boundary(right), W, hermitian != 0);
+        return QCM_OK;
+    } catch (const std::exception& e) {
+        set_error(std::string("qcm_plan_energy_gradient: ") + e.what());
+        *plan = nullptr;
+        return QCM_E_INVALID;
+    }
+}
+
 int qcm_plan_boundary_tensor_mpo(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
                                  const qcm_blocks_t* mps, const qcm_boundary_t* boundary, const qcm_mpo_t* mpo,
                                  int32_t side, int32_t hermitian, qcm_plan** plan) {
@@ -1780,9 +1907,35 @@ int qcm_plan_stage_info(const qcm_plan* p, int32_t s, int32_t* kind, int64_t* n_
     } else if (st.kind == ST_GEMM) {
         if (n_out) *n_out = (int64_t)st.gout.size();
         if (n_terms) *n_terms = (int64_t)st.gseg.size();
+    } else if (st.kind == ST_DOT) {
+        if (n_out) *n_out = (int64_t)st.aout.size();
+        if (n_terms) *n_terms = (int64_t)st.aterm.size();
     } else {
         if (n_out) *n_out = st.zbuf;
         if (n_terms) *n_terms = st.zlen;
+    }
+    return QCM_OK;
+}
+
+int qcm_plan_stage_dot(const qcm_plan* p, int32_t s, int64_t* od, int64_t* td, double* w, int32_t* tt,
+                       int32_t* meta) {
+    if (!p || s < 0 || s >= (int32_t)p->stages.size() || p->stages[s].kind != ST_DOT) {
+        set_error("not a dot stage");
+        return QCM_E_INVALID;
+    }
+    const Stage& st = p->stages[s];
+    if (meta) { meta[0] = st.dot_buf; meta[1] = st.n_tt; }
+    for (size_t i = 0; i < st.aout.size(); ++i) {
+        const AxpyOut& o = st.aout[i];
+        int64_t* d = od + 7 * i;
+        d[0] = o.dst_buf; d[1] = o.dst_off; d[2] = o.ldd; d[3] = o.rows; d[4] = o.cols; d[5] = o.t_begin; d[6] = o.t_end;
+    }
+    for (size_t i = 0; i < st.aterm.size(); ++i) {
+        td[3 * i] = st.aterm[i].src_buf;
+        td[3 * i + 1] = st.aterm[i].src_off;
+        td[3 * i + 2] = st.aterm[i].lds;
+        w[i] = st.dot_w[i];
+        tt[i] = st.dot_tt[i];
     }
     return QCM_OK;
 }

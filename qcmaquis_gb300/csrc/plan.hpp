@@ -92,7 +92,10 @@ struct GemmSeg {
     double alpha;
 };
 
-enum StageKind { ST_AXPY = 0, ST_GEMM = 1, ST_ZERO = 2 };
+// ST_DOT: the adjoint of a gather-axpy stage -- for every term k of the axpy
+// tables (aout/aterm), g[k] = <source tile, output-adjoint tile>, written to
+// dot_buf; then OUT[tt] = sum over the terms of parameter tt of dot_w[k] g[k]
+enum StageKind { ST_AXPY = 0, ST_GEMM = 1, ST_ZERO = 2, ST_DOT = 3 };
 
 // ---- operand images of the BF16x3 tensor-core executor
 // An image holds one operand panel (R rows x K, K-major as the MMA reads it)
@@ -199,9 +202,20 @@ struct Stage {
     void* d_iseg = nullptr;
     void* d_iunit = nullptr;
     void* d_icost = nullptr;
+    // DOT: per-term weight and parameter index, the buffer of the per-term dots,
+    // the number of parameters; device: terms, parameter-sorted term lists, weights
+    std::vector<double> dot_w;
+    std::vector<int32_t> dot_tt;
+    int32_t dot_buf = 0;
+    int32_t n_tt = 0;
+    void* d_dterm = nullptr;
+    void* d_dptr = nullptr;
+    void* d_didx = nullptr;
+    void* d_dw = nullptr;
 };
 
-enum PlanKind { PK_SIGMA = 0, PK_BLEFT = 1, PK_BRIGHT = 2 };
+// PK_GRAD: gradient of <psi| H_eff |psi> with respect to every MPO term scale
+enum PlanKind { PK_SIGMA = 0, PK_BLEFT = 1, PK_BRIGHT = 2, PK_GRAD = 3 };
 
 }  // namespace qcm
 

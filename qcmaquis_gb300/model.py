@@ -196,13 +196,16 @@ def construct_collection(t: Operators):
 
 
 class Term:
-    """``term_descriptor``: list of (position, tag) with a coefficient."""
-    __slots__ = ("ops", "coeff", "is_fermionic")
+    """``term_descriptor``: list of (position, tag) with a coefficient.  ``src`` records
+    the coefficient as a linear combination of integral values,
+    coeff = sum_u src[u] * integral[u] (keys of the integral map)."""
+    __slots__ = ("ops", "coeff", "is_fermionic", "src")
 
     def __init__(self, coeff=1.0, fermionic=False):
         self.ops: List[Tuple[int, int]] = []
         self.coeff = coeff
         self.is_fermionic = fermionic
+        self.src: Dict = {}
 
     def push(self, pos, tag):
         self.ops.append((pos, tag))
@@ -448,7 +451,7 @@ class QCModel:
         for key, val in self.integrals.items():
             if abs(val) > self.integral_cutoff:
                 i, j, k, l = [x - 1 for x in key]
-                out.append((align(i, j, k, l), float(val)))
+                out.append((align(i, j, k, l), float(val), key))
         return out
 
     def _create_terms(self):
@@ -462,6 +465,8 @@ class QCModel:
         def add(store, key, term):
             if key in store:
                 store[key].coeff += term.coeff
+                for u, f in term.src.items():
+                    store[key].src[u] = store[key].src.get(u, 0.0) + f
             else:
                 store[key] = term
 
@@ -475,71 +480,17 @@ class QCModel:
         def add4(term):
             add(four_terms, tuple(term.position(x) for x in range(4)) + tuple(term.tag(x) for x in range(4)), term)
 
-        for (i, j, k, l), me in self._parsed():
-            if i == -1 and j == -1 and k == -1 and l == -1:
-                t = Term(me)
-                t.push(0, self.ops.ident)
-                self.terms.append(t)
-            elif i == j and k == -1 and l == -1:
-                t = Term(me)
-                t.push(i, self.ops.count)
-                self.terms.append(t)
-            elif k == -1 and l == -1:
-                if N == 1:
-                    raise NotImplementedError("one-electron systems are not supported")
-                f = me * (1.0 / (N - 1))
-                terms = []
-                for kk in range(self.L):
-                    if kk == j or kk == i:
-                        continue
-                    terms += ss.three_term(f, i, kk, kk, j)
-                    terms += ss.three_term(f, j, kk, kk, i)
-                for t in terms:
-                    add3(t)
-                terms = []
-                terms += ss.V_term(f, i, i, i, j)
-                terms += ss.V_term(f, j, i, i, i)
-                terms += ss.V_term(f, i, j, j, j)
-                terms += ss.V_term(f, j, j, j, i)
-                for t in terms:
+        for (i, j, k, l), me, ukey in self._parsed():
+            for kind, t in self._integral_terms(i, j, k, l, me, ss, N):
+                # the coefficient per unit of this integral, before terms are merged
+                t.src = {ukey: t.coeff / me}
+                if kind == 1:
+                    self.terms.append(t)
+                elif kind == 2:
                     add2(t)
-            elif i == j == k == l:
-                t = Term(me)
-                t.push(i, self.ops.docc)
-                self.terms.append(t)
-            elif (i == j and j == k and k != l) or (i != j and j == k and k == l):
-                if i == j:
-                    s, p = i, l
-                elif k == l:
-                    s, p = l, i
+                elif kind == 3:
+                    add3(t)
                 else:
-                    raise RuntimeError("V_ijjj")
-                for t in ss.two_term(me, s, s, s, p) + ss.two_term(me, s, p, s, s):
-                    add2(t)
-            elif i == j and k == l and j != k:
-                for t in ss.two_term(me, i, k, k, i):
-                    add2(t)
-            elif i == k and j == l and i != j:
-                terms = ss.two_term(0.5 * me, i, i, j, j) + ss.two_term(0.5 * me, j, j, i, i) + \
-                    ss.two_term(me, i, j, i, j)
-                for t in terms:
-                    add2(t)
-            elif (i == j and j != k and k != l) or (k == l and i != j and j != k):
-                if i == j:
-                    terms = ss.three_term(me, i, k, l, i) + ss.three_term(me, i, l, k, i)
-                else:
-                    terms = ss.three_term(me, i, k, k, j) + ss.three_term(me, j, k, k, i)
-                for t in terms:
-                    add3(t)
-            elif ((i == k and j != l) or j == k or (j == l and i != k)) and (i != j and k != l):
-                terms = (ss.three_term(me, i, k, l, j) + ss.three_term(me, i, l, k, j)
-                         + ss.three_term(me, j, k, l, i) + ss.three_term(me, j, l, k, i))
-                for t in terms:
-                    add3(t)
-            elif i != j and j != k and k != l and i != k and j != l:
-                terms = (ss.four_term(me, i, k, l, j) + ss.four_term(me, i, l, k, j)
-                         + ss.four_term(me, j, k, l, i) + ss.four_term(me, j, l, k, i))
-                for t in terms:
                     add4(t)
         for key in sorted(two_terms):
             self.terms.append(two_terms[key])
@@ -547,6 +498,69 @@ class QCModel:
             self.terms.append(three_terms[key])
         for key in sorted(four_terms):
             self.terms.append(four_terms[key])
+
+    def _integral_terms(self, i, j, k, l, me, ss, N):
+        """The terms of one integral as (kind, term): kind 1 = kept as is, 2/3/4 =
+        merged with equal two-/three-/four-operator terms (``model.hpp:96-139``)."""
+        out = []
+        if i == -1 and j == -1 and k == -1 and l == -1:
+            t = Term(me)
+            t.push(0, self.ops.ident)
+            out.append((1, t))
+        elif i == j and k == -1 and l == -1:
+            t = Term(me)
+            t.push(i, self.ops.count)
+            out.append((1, t))
+        elif k == -1 and l == -1:
+            if N == 1:
+                raise NotImplementedError("one-electron systems are not supported")
+            f = me * (1.0 / (N - 1))
+            terms = []
+            for kk in range(self.L):
+                if kk == j or kk == i:
+                    continue
+                terms += ss.three_term(f, i, kk, kk, j)
+                terms += ss.three_term(f, j, kk, kk, i)
+            out += [(3, t) for t in terms]
+            terms = []
+            terms += ss.V_term(f, i, i, i, j)
+            terms += ss.V_term(f, j, i, i, i)
+            terms += ss.V_term(f, i, j, j, j)
+            terms += ss.V_term(f, j, j, j, i)
+            out += [(2, t) for t in terms]
+        elif i == j == k == l:
+            t = Term(me)
+            t.push(i, self.ops.docc)
+            out.append((1, t))
+        elif (i == j and j == k and k != l) or (i != j and j == k and k == l):
+            if i == j:
+                s, p = i, l
+            elif k == l:
+                s, p = l, i
+            else:
+                raise RuntimeError("V_ijjj")
+            out += [(2, t) for t in ss.two_term(me, s, s, s, p) + ss.two_term(me, s, p, s, s)]
+        elif i == j and k == l and j != k:
+            out += [(2, t) for t in ss.two_term(me, i, k, k, i)]
+        elif i == k and j == l and i != j:
+            terms = ss.two_term(0.5 * me, i, i, j, j) + ss.two_term(0.5 * me, j, j, i, i) + \
+                ss.two_term(me, i, j, i, j)
+            out += [(2, t) for t in terms]
+        elif (i == j and j != k and k != l) or (k == l and i != j and j != k):
+            if i == j:
+                terms = ss.three_term(me, i, k, l, i) + ss.three_term(me, i, l, k, i)
+            else:
+                terms = ss.three_term(me, i, k, k, j) + ss.three_term(me, j, k, k, i)
+            out += [(3, t) for t in terms]
+        elif ((i == k and j != l) or j == k or (j == l and i != k)) and (i != j and k != l):
+            terms = (ss.three_term(me, i, k, l, j) + ss.three_term(me, i, l, k, j)
+                     + ss.three_term(me, j, k, l, i) + ss.three_term(me, j, l, k, i))
+            out += [(3, t) for t in terms]
+        elif i != j and j != k and k != l and i != k and j != l:
+            terms = (ss.four_term(me, i, k, l, j) + ss.four_term(me, i, l, k, j)
+                     + ss.four_term(me, j, k, l, i) + ss.four_term(me, j, l, k, i))
+            out += [(4, t) for t in terms]
+        return out
 
 
 __all__ = ["QCModel", "TagHandler", "phys_index", "align", "Term"]

@@ -74,16 +74,23 @@ class MPOTensor:
         self.left_spins = list(left_spins)
         self.right_spins = list(right_spins)
         # element lists: later entries (in column-major order) are prepended
+        # entries (b1, b2, tag, scale[, label]); a label names the model term whose
+        # coefficient the scale is (kept parallel to the element lists in ``labels``)
         entries = sorted(prempo, key=lambda t: (t[1], t[0]))
         self.elements: Dict[Tuple[int, int], List[Tuple[int, float]]] = {}
+        self.labels: Dict[Tuple[int, int], List] = {}
         self.row_index: List[set] = [set() for _ in range(ld)]
-        for b1, b2, tag, scale in entries:
+        for ent in entries:
+            b1, b2, tag, scale = ent[:4]
+            label = ent[4] if len(ent) > 4 else None
             key = (b1, b2)
             if key not in self.elements:
                 self.elements[key] = [(tag, scale)]
+                self.labels[key] = [label]
                 self.row_index[b1].add(b2)
             else:
                 self.elements[key].insert(0, (tag, scale))
+                self.labels[key].insert(0, label)
         self.cols: List[List[int]] = [[] for _ in range(rd)]
         for (b1, b2) in sorted(self.elements, key=lambda k: (k[1], k[0])):
             self.cols[b2].append(b1)
@@ -105,6 +112,9 @@ class MPOTensor:
 
     def at(self, b1, b2) -> List[Tuple[int, float]]:
         return self.elements[(b1, b2)]
+
+    def labels_at(self, b1, b2) -> List:
+        return self.labels.get((b1, b2), [None] * len(self.elements[(b1, b2)]))
 
     def column(self, b2) -> List[int]:
         return self.cols[b2]
@@ -131,10 +141,16 @@ class MPOTensor:
 
 class MPO(list):
     core_energy: float = 0.0
+    core_labels: list = []   # model terms folded into core_energy
 
 
 class TaggedMPOMaker:
-    def __init__(self, model: QCModel):
+    """``merge_site_terms=False`` keeps every one-site term as its own (tag, scale)
+    entry instead of one summed operator per site (the same operator; used where
+    each term's coefficient must stay a separate MPO scale, as for gradients).
+    Every coefficient-carrying scale is labelled with its model term's index."""
+
+    def __init__(self, model: QCModel, merge_site_terms: bool = True):
         self.L = model.L
         self.th: TagHandler = model.tag_handler
         self.identity = model.ops.ident
@@ -146,8 +162,14 @@ class TaggedMPOMaker:
         self.rightmost_left = 0
         self.core_energy = 0.0
         self.finalized = False
-        for t in model.terms:
+        self.merge_site_terms = merge_site_terms
+        self.site_term_lists: Dict[int, list] = {}
+        self.core_labels: List[int] = []
+        self._label = None
+        for idx, t in enumerate(model.terms):
+            self._label = idx
             self.add_term(t)
+        self._label = None
 
     # -- prempo helpers ------------------------------------------------------
     def _insert(self, p, kk, val, attach):
@@ -166,8 +188,8 @@ class TaggedMPOMaker:
             d = self.prempo[s]
             kk = (k, k)
             if kk not in d:
-                d[kk] = [(op, 1.0)]
-            elif d[kk][0] != (op, 1.0):
+                d[kk] = [(op, 1.0, None)]
+            elif d[kk][0][:2] != (op, 1.0):
                 raise RuntimeError(f"Pre-existing term at site {s}")
 
     def add_term(self, term: Term):
@@ -185,6 +207,9 @@ class TaggedMPOMaker:
     def _add_1term(self, term):
         if term.tag(0) == self.identity:
             self.core_energy += term.coeff
+            self.core_labels.append(self._label)
+        elif not self.merge_site_terms:
+            self.site_term_lists.setdefault(term.position(0), []).append((term.tag(0), term.coeff, self._label))
         else:
             op = self.th.get_op(term.tag(0)).scaled(term.coeff)
             p = term.position(0)
@@ -202,13 +227,13 @@ class TaggedMPOMaker:
         k1 = KEY_TL
         mpo_spin = mpo_spin.couple(th.get_op(term.tag(0)).spin)
         k2 = bulk_key([term.ops[1]])
-        k1 = self._insert(term.position(0), (k1, k2), (term.tag(0), term.coeff), attach=False)
+        k1 = self._insert(term.position(0), (k1, k2), (term.tag(0), term.coeff, self._label), attach=False)
         if th.is_fermionic(term.tag(0)):
             nferm -= 1
         trivial = (nferm % 2 == 0)
         self._insert_filling(term.position(0) + 1, term.position(1), k1, trivial, mpo_spin.get() > 1)
         mpo_spin = mpo_spin.couple(th.get_op(term.tag(1)).spin)
-        self._insert(term.position(1), (k1, KEY_TR), (term.tag(1), 1.0), attach=True)
+        self._insert(term.position(1), (k1, KEY_TR), (term.tag(1), 1.0, None), attach=True)
         assert mpo_spin.get() == 0
 
     def _add_generic_term(self, term):
@@ -223,14 +248,14 @@ class TaggedMPOMaker:
             mpo_spin = mpo_spin.couple(th.get_op(term.tag(i)).spin)
             ops_left.append(term.ops[i])
             k2 = bulk_key(ops_left)
-            k1 = self._insert(term.position(i), (k1, k2), (term.tag(i), 1.0), attach=True)
+            k1 = self._insert(term.position(i), (k1, k2), (term.tag(i), 1.0, None), attach=True)
             if th.is_fermionic(term.tag(i)):
                 nferm -= 1
             self._insert_filling(term.position(i) + 1, term.position(i + 1), k1, nferm % 2 == 0, mpo_spin.get() > 1)
         ops_right = [term.ops[j] for j in range(thresh + 1, nops)]
         k2 = bulk_key(ops_right)
         mpo_spin = mpo_spin.couple(th.get_op(term.tag(thresh)).spin)
-        k1 = self._insert(term.position(thresh), (k1, k2), (term.tag(thresh), term.coeff), attach=False)
+        k1 = self._insert(term.position(thresh), (k1, k2), (term.tag(thresh), term.coeff, self._label), attach=False)
         if th.is_fermionic(term.tag(thresh)):
             nferm -= 1
         self._insert_filling(term.position(thresh) + 1, term.position(thresh + 1), k1, nferm % 2 == 0,
@@ -241,7 +266,7 @@ class TaggedMPOMaker:
             else:
                 k2 = bulk_key([term.ops[j] for j in range(i + 1, nops)])
             mpo_spin = mpo_spin.couple(th.get_op(term.tag(i)).spin)
-            k1 = self._insert(term.position(i), (k1, k2), (term.tag(i), 1.0), attach=True)
+            k1 = self._insert(term.position(i), (k1, k2), (term.tag(i), 1.0, None), attach=True)
             if th.is_fermionic(term.tag(i)):
                 nferm -= 1
             if i != nops - 1:
@@ -256,13 +281,18 @@ class TaggedMPOMaker:
             d = self.prempo[p]
             if kk in d:
                 raise RuntimeError("another site term already existing!")
-            d[kk] = [(tag, 1.0)]
+            d[kk] = [(tag, 1.0, None)]
+        for p in sorted(self.site_term_lists):
+            d = self.prempo[p]
+            if kk in d:
+                raise RuntimeError("another site term already existing!")
+            d[kk] = list(self.site_term_lists[p])
         for p in range(self.rightmost_left):
             d = self.prempo[p]
-            d.setdefault((KEY_TL, KEY_TL), []).append((self.identity, 1.0))
+            d.setdefault((KEY_TL, KEY_TL), []).append((self.identity, 1.0, None))
         for p in range(self.leftmost_right + 1, self.L):
             d = self.prempo[p]
-            d.setdefault((KEY_TR, KEY_TR), []).append((self.identity, 1.0))
+            d.setdefault((KEY_TR, KEY_TR), []).append((self.identity, 1.0, None))
         self.finalized = True
 
     def _conjugate_key(self, k, p):
@@ -323,7 +353,7 @@ class TaggedMPOMaker:
                             right[k2] = r
                             r += 1
                     rr_dim = 0 if p == L - 1 else right[k2]
-                    pre.append((ll, rr_dim, val[0], val[1]))
+                    pre.append((ll, rr_dim, val[0], val[1], val[2]))
                     ck2, phase = self._conjugate_key(k2, p)
                     if k2 != ck2:
                         herm_pairs[k2] = ck2
@@ -331,7 +361,7 @@ class TaggedMPOMaker:
             ldim = max(x[0] for x in pre) + 1
             rdim = max(x[1] for x in pre) + 1
             right_spins = [SpinDescriptor() for _ in range(rdim)]
-            for (b1, b2, tag, _) in pre:
+            for (b1, b2, tag, _, _) in pre:
                 out_spin = left_spins[b1].couple(table[tag].spin)
                 assert right_spins[b2].get() == 0 or right_spins[b2].get() == out_spin.get()
                 right_spins[b2] = out_spin
@@ -357,6 +387,7 @@ class TaggedMPOMaker:
             LeftHerm = RightHerm
             LeftPhase = RightPhase
         mpo.core_energy = self.core_energy
+        mpo.core_labels = list(self.core_labels)
         return mpo
 
 

@@ -81,6 +81,10 @@ def lib():
     L.qcm_plan_stage_info.argtypes = [C.c_void_p, C.c_int32, i32p, i64p, i64p]
     L.qcm_plan_stage_axpy.argtypes = [C.c_void_p, C.c_int32, i64p, i64p, f64p]
     L.qcm_plan_stage_gemm.argtypes = [C.c_void_p, C.c_int32, i64p, i64p, f64p]
+    L.qcm_plan_stage_dot.argtypes = [C.c_void_p, C.c_int32, i64p, i64p, f64p, i32p, i32p]
+    L.qcm_plan_energy_gradient.argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks), C.POINTER(CBoundary),
+                                                                  C.POINTER(CBoundary), C.POINTER(CMpo), C.c_int32,
+                                                                  C.POINTER(C.c_void_p)]
     L.qcm_plan_upload.argtypes = [C.c_void_p]
     L.qcm_plan_run.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.c_int32, C.c_void_p]
     L.qcm_plan_run_stages.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.c_int32, C.c_void_p, C.c_int32,
@@ -240,15 +244,21 @@ class FMpo:
         self.left_phase = np.array(mpo.herm.LeftPhase, dtype=np.int32)
         self.right_phase = np.array(mpo.herm.RightPhase, dtype=np.int32)
         col_ptr, row_of, term_ptr, term_op, term_scale = [0], [], [0], [], []
+        # per flattened term: (b1, b2, position in the element list) and the model-term label
+        self.term_key, self.term_label = [], []
         used_ops = {}
+        labels_at = getattr(mpo, "labels_at", None)
         for b2 in range(mpo.col_dim):
             for b1 in mpo.column(b2):
                 row_of.append(b1)
-                for tag, scale in mpo.at(b1, b2):
+                labs = labels_at(b1, b2) if labels_at else [None] * len(mpo.at(b1, b2))
+                for pos, ((tag, scale), lab) in enumerate(zip(mpo.at(b1, b2), labs)):
                     if tag not in used_ops:
                         used_ops[tag] = len(used_ops)
                     term_op.append(used_ops[tag])
                     term_scale.append(scale)
+                    self.term_key.append((b1, b2, pos))
+                    self.term_label.append(lab)
                 term_ptr.append(len(term_op))
             col_ptr.append(len(row_of))
         op_spin, op_blk_ptr, blk_q, blk_ent_ptr, ent, ent_coeff = [], [0], [], [0], [], []
@@ -275,12 +285,31 @@ class FMpo:
         self.blk_ent_ptr = a32(blk_ent_ptr)
         self.ent = a32(ent)
         self.ent_coeff = np.array(ent_coeff or [0.0], dtype=np.float64)
+        self.n_ops = len(op_spin)
+        self._make_c()
+
+    def _make_c(self):
+        mpo = self.mpo
         self.c = CMpo(mpo.row_dim, mpo.col_dim, _p(self.left_spin, i32p), _p(self.right_spin, i32p),
                       _p(self.left_herm, i32p), _p(self.right_herm, i32p), _p(self.left_phase, i32p),
                       _p(self.right_phase, i32p), _p(self.col_ptr, i32p), _p(self.row_of, i32p),
                       _p(self.term_ptr, i32p), _p(self.term_op, i32p), _p(self.term_scale, f64p),
-                      len(op_spin), _p(self.op_spin, i32p), _p(self.op_blk_ptr, i32p), _p(self.blk_q, i32p),
+                      self.n_ops, _p(self.op_spin, i32p), _p(self.op_blk_ptr, i32p), _p(self.blk_q, i32p),
                       _p(self.blk_ent_ptr, i32p), _p(self.ent, i32p), _p(self.ent_coeff, f64p))
+
+    @property
+    def n_terms(self) -> int:
+        return len(self.term_key)
+
+    def with_scales(self, scales) -> "FMpo":
+        """The same tensor with its term scales replaced (flattened term order)."""
+        import copy
+        f = copy.copy(self)
+        f.term_scale = np.array(scales, dtype=np.float64).reshape(-1)
+        if f.term_scale.size != max(self.n_terms, 1):
+            raise ValueError("one scale per flattened term")
+        f._make_c()
+        return f
 
 
 # ------------------------------------------------------------------ plans
@@ -345,6 +374,16 @@ class Plan:
                 sa = np.zeros(max(nt.value, 1))
                 check(lib().qcm_plan_stage_gemm(self.h, s, _p(od, i64p), _p(sd, i64p), _p(sa, f64p)), "stage_gemm")
                 out.append(("gemm", od[:no.value], sd[:nt.value], sa[:nt.value]))
+            elif kind.value == 3:
+                od = np.zeros((max(no.value, 1), 7), dtype=np.int64)
+                td = np.zeros((max(nt.value, 1), 3), dtype=np.int64)
+                w = np.zeros(max(nt.value, 1))
+                tt = np.zeros(max(nt.value, 1), dtype=np.int32)
+                meta = np.zeros(2, dtype=np.int32)
+                check(lib().qcm_plan_stage_dot(self.h, s, _p(od, i64p), _p(td, i64p), _p(w, f64p), _p(tt, i32p),
+                                               _p(meta, i32p)), "stage_dot")
+                out.append(("dot", od[:no.value], td[:nt.value], w[:nt.value], tt[:nt.value], int(meta[0]),
+                            int(meta[1])))
             else:
                 out.append(("zero", int(no.value), int(nt.value)))
         return out
@@ -431,6 +470,18 @@ def plan_boundary_right(phys, left_i, right_i, mps: Layout, R: BoundaryLayout, m
     return Plan(h, "bright")
 
 
+def plan_energy_gradient(phys: Index, left_i: Index, right_i: Index, psi: Layout, L: BoundaryLayout,
+                         R: BoundaryLayout, mpo: FMpo, hermitian: bool = True) -> Plan:
+    """Gradient of <psi|H_eff psi> with respect to every term scale of ``mpo`` (flattened
+    term order of ``FMpo``); run in the FP64 form, output length = number of terms."""
+    fp, fl, fr = FIndex(phys), FIndex(left_i), FIndex(right_i)
+    h = C.c_void_p()
+    check(lib().qcm_plan_energy_gradient(C.byref(fp.c), C.byref(fl.c), C.byref(fr.c), C.byref(psi.c), C.byref(L.c),
+                                         C.byref(R.c), C.byref(mpo.c), 1 if hermitian else 0, C.byref(h)),
+          "qcm_plan_energy_gradient")
+    return Plan(h, "grad")
+
+
 def plan_boundary_tensor_mpo(phys, left_i, right_i, mps: Layout, B: BoundaryLayout, mpo: FMpo, side: str,
                              hermitian=True) -> Plan:
     """``left_boundary_tensor_mpo`` (side "left") / ``right_boundary_tensor_mpo`` (side "right"):
@@ -446,5 +497,5 @@ def plan_boundary_tensor_mpo(phys, left_i, right_i, mps: Layout, B: BoundaryLayo
 
 
 __all__ = ["lib", "check", "Layout", "BoundaryLayout", "FMpo", "FIndex", "Plan", "plan_sigma",
-           "plan_boundary_left", "plan_boundary_right", "plan_boundary_tensor_mpo", "PREC_FP64", "PREC_TF32",
+           "plan_boundary_left", "plan_boundary_right", "plan_boundary_tensor_mpo", "plan_energy_gradient", "PREC_FP64", "PREC_TF32",
            "PREC_BF16X3"]

@@ -6,7 +6,9 @@ Reads, as text, the reference test sources:
   and ``:112`` reference energy;
 * ``dmrg/tests/Fixtures/H2Fixture.h:26-35`` -- H2 integrals (L=2, N=2);
 * ``dmrg/tests/test1.cpp:93`` -- H2 ground-state energy;
-* ``dmrg/tests/test_wigner.cpp:21-45`` -- 24 Wigner 9j values.
+* ``dmrg/tests/test_wigner.cpp:21-45`` -- 24 Wigner 9j values;
+* ``dmrg/tests/test2.cpp:60-120`` -- the LiH (SU2U1) ground-state 2-RDM
+  (measurement ``twoptdm``): index quadruples and values.
 
 Run from the repository root with the reference mounted at REFERENCE (default
 ``/root/reference``); the JSON it writes is committed so tests never need the
@@ -35,6 +37,7 @@ def main():
     h2 = open(os.path.join(REF, "dmrg/tests/Fixtures/H2Fixture.h")).read()
     t1 = open(os.path.join(REF, "dmrg/tests/test1.cpp")).read()
     tw = open(os.path.join(REF, "dmrg/tests/test_wigner.cpp")).read()
+    t2 = open(os.path.join(REF, "dmrg/tests/test2.cpp")).read()
 
     lih_ints = parse_integral_map(lih)
     lih_e = float(re.search(r"referenceEnergy\s*=\s*(" + NUM + ")", lih).group(1))
@@ -46,6 +49,16 @@ def main():
         if len(args) == 9:
             wig.append([args, float(m.group(2))])
 
+    # test2.cpp: const rdm_measurement ref_2rdm = { { {i,j,k,l}, ... }, std::vector<double> { ... } };
+    blk = t2[t2.index("ref_2rdm"):]
+    blk = blk[:blk.index("check_measurement_mat")]
+    idx_part, val_part = blk.split("std::vector<double>")
+    rdm_idx = [[int(x) for x in m.groups()] for m in
+               re.finditer(r"\{\s*(\d+)\s*,\s*(\d+)\s*,\s*(\d+)\s*,\s*(\d+)\s*\}", idx_part)]
+    rdm_val = [float(x) for x in re.findall(NUM, val_part[val_part.index("{"):])]
+    if len(rdm_idx) != len(rdm_val):
+        raise SystemExit(f"2-RDM parse mismatch: {len(rdm_idx)} indices, {len(rdm_val)} values")
+
     data = {
         "source": "values read from the reference test sources by tests/golden/make_golden.py",
         "lih": {"L": 4, "nelec": 2, "spin": 0, "integrals": lih_ints, "energy": lih_e,
@@ -53,10 +66,12 @@ def main():
         "h2": {"L": 2, "nelec": 2, "spin": 0, "integrals": h2_ints, "energy": h2_e,
                "cite": "dmrg/tests/Fixtures/H2Fixture.h:26-35; dmrg/tests/test1.cpp:93"},
         "wigner9j": {"cases": wig, "rel_tol_percent": 1e-6, "cite": "dmrg/tests/test_wigner.cpp:21-45"},
+        "lih_2rdm": {"index": rdm_idx, "value": rdm_val, "cite": "dmrg/tests/test2.cpp:60-120 (twoptdm)"},
     }
     with open(os.path.join(HERE, "reference_fixtures.json"), "w") as f:
         json.dump(data, f, indent=1)
-    print(f"LiH {len(lih_ints)} integrals E={lih_e}; H2 {len(h2_ints)} integrals E={h2_e}; {len(wig)} 9j cases")
+    print(f"LiH {len(lih_ints)} integrals E={lih_e}; H2 {len(h2_ints)} integrals E={h2_e}; {len(wig)} 9j cases; "
+          f"LiH 2-RDM {len(rdm_val)} elements")
 
 
 if __name__ == "__main__":

@@ -1,6 +1,6 @@
 """Host-side interpreter of exported plan task tables (test infrastructure).
 
-Executes the ZERO / AXPY / GEMM stages of a native plan with numpy so the
+Executes the ZERO / AXPY / GEMM / DOT stages of a native plan with numpy so the
 plan builder can be checked against the oracle without a GPU.  It is a
 checker of the task tables, not an execution path of the library.
 """
@@ -26,6 +26,20 @@ def run_plan(plan, bufs, images=False):
         if st[0] == "zero":
             zbuf, zlen = st[1], st[2]
             bufs[zbuf][:zlen] = 0.0
+        elif st[0] == "dot":
+            # per-term dots against the output-adjoint tiles, then sums per MPO term
+            od, td, w, tt, gbuf, ntt = st[1:]
+            g = np.zeros(len(td))
+            for o in od:
+                dst_buf, dst_off, ldd, rows, cols, tb, te = [int(x) for x in o]
+                Y = _view(bufs[dst_buf], dst_off, ldd, rows, cols)
+                for t in range(tb, te):
+                    sb, so, lds = [int(x) for x in td[t]]
+                    g[t] = float(np.sum(_view(bufs[sb], so, lds, rows, cols) * Y))
+            bufs[gbuf][:len(g)] = g
+            out = np.zeros(ntt)
+            np.add.at(out, tt, w * g)
+            bufs[3][:ntt] = out
         elif st[0] == "axpy":
             od, td, ta = st[1], st[2], st[3]
             for o in od:

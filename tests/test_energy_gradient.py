@@ -1,0 +1,249 @@
+"""The adjoint of the local energy: dE/d(MPO term scale) from the energy-gradient
+plan (K1, the adjoint of K3, per-term dots of the K2 tables), and through the MPO
+builder's term labels and the model's integral provenance dE/d(t_pq),
+dE/d(V_pqrs).
+
+E = <psi| H_eff psi> is linear in every MPO term scale, so the gradient is
+checked exactly through the pinned sigma path: for any direction d of the
+scales, <grad, d> = <psi, H_eff(d) psi>, the sigma with the scales replaced by
+d (the oracle's sigma, pinned against the reference's golden values).  The
+integral gradient is checked against central differences of the energy of a
+fixed MPS (exact up to rounding: the energy is linear in the integrals) and,
+at the converged LiH ground state, against the 2-RDM of exact
+diagonalisation."""
+import numpy as np
+import pytest
+
+from qcmaquis_gb300 import native as N
+from qcmaquis_gb300.integrals import synthetic_integral_map
+from qcmaquis_gb300.model import QCModel
+from qcmaquis_gb300.mpo import TaggedMPOMaker
+
+from oracle import dmrg_ref as R
+from oracle.sweep import SweepParams, initial_state
+from plan_interp import run_plan
+
+
+def _single_site_problem(L=6, Ne=6, m=16, site=2, seed=3, merge=False):
+    """Site tensor j with the full environments L[j], R[j+1] of a random MPS."""
+    model = QCModel(L, synthetic_integral_map(L, seed=seed), Ne)
+    mpo = TaggedMPOMaker(model, merge_site_terms=merge).create_mpo()
+    mps = initial_state(model, mpo, SweepParams(init_bond_dimension=m, seed=11), Ne, 0)
+    left = R.left_boundary(mps[0])
+    for i in range(site):
+        left = R.overlap_mpo_left_step(mps[i], mps[i], left, mpo[i])
+    right = R.right_boundary(mps[L - 1])
+    for i in range(L - 1, site, -1):
+        right = R.overlap_mpo_right_step(mps[i], mps[i], right, mpo[i])
+    return model, mpo, mps, left, right
+
+
+def _with_scales(t, scales, f):
+    """A copy of MPO tensor t whose term scales are ``scales`` (FMpo's flattened order)."""
+    import copy
+    c = copy.copy(t)
+    c.elements = {k: list(v) for k, v in t.elements.items()}
+    for (b1, b2, pos), s in zip(f.term_key, scales):
+        tag, _ = c.elements[(b1, b2)][pos]
+        c.elements[(b1, b2)][pos] = (tag, float(s))
+    return c
+
+
+def _interp_gradient(psi, left, right, w):
+    lay = N.Layout.of(psi.data)
+    Ll, Rl = N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
+    f = N.FMpo(w)
+    p = N.plan_energy_gradient(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, f, True)
+    assert p.out_elems == f.n_terms
+    bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.full(p.out_elems, np.nan)] + \
+        [np.full(max(s, 1), np.nan) for s in p.scratch]
+    run_plan(p, bufs)
+    return bufs[3][:p.out_elems].copy(), f
+
+
+@pytest.mark.parametrize("site", [0, 2, 5])
+def test_gradient_plan_gives_every_directional_derivative(site):
+    model, mpo, mps, left, right = _single_site_problem(site=site)
+    psi = mps[site].copy().make_left_paired()
+    g, f = _interp_gradient(psi, left, right, mpo[site])
+    # Euler: E is linear in the scales
+    e = psi.dot(R.site_hamil2(psi.copy(), left, right, mpo[site]))
+    assert abs(float(np.dot(f.term_scale, g)) - e) <= 1e-11 * abs(e)
+    rng = np.random.default_rng(site)
+    for _ in range(3):
+        d = rng.standard_normal(f.n_terms)
+        ed = psi.dot(R.site_hamil2(psi.copy(), left, right, _with_scales(mpo[site], d, f)))
+        assert abs(float(np.dot(d, g)) - ed) <= 1e-11 * max(1.0, abs(ed), np.abs(d).sum() * np.abs(g).max())
+
+
+def test_local_energy_is_the_expectation_value():
+    """With full environments, <psi_j| H_eff psi_j> is <Psi|H|Psi> of the whole MPS at every j."""
+    from oracle.sweep import expval
+    model, mpo, mps, left, right = _single_site_problem(site=3)
+    psi = mps[3].copy().make_left_paired()
+    e = psi.dot(R.site_hamil2(psi.copy(), left, right, mpo[3]))
+    assert abs(e - expval(mps, mpo)) <= 1e-11 * abs(e)
+
+
+def test_every_model_term_is_a_labelled_mpo_scale():
+    model = QCModel(6, synthetic_integral_map(6, seed=3), 6)
+    mpo = TaggedMPOMaker(model, merge_site_terms=False).create_mpo()
+    seen = {}
+    for j, t in enumerate(mpo):
+        for key, labs in t.labels.items():
+            for pos, lab in enumerate(labs):
+                if lab is not None:
+                    assert lab not in seen
+                    seen[lab] = (j, key, pos)
+                    assert t.elements[key][pos][1] == model.terms[lab].coeff
+    assert set(seen) | set(mpo.core_labels) == set(range(len(model.terms)))
+    # the coefficients are the recorded linear combinations of the integrals
+    for term in model.terms:
+        assert abs(sum(f * model.integrals[u] for u, f in term.src.items()) - term.coeff) <= 1e-14 * max(
+            1.0, abs(term.coeff))
+
+
+def test_unmerged_site_terms_give_the_same_energy():
+    from oracle.sweep import expval
+    model = QCModel(6, synthetic_integral_map(6, seed=3), 6)
+    a = TaggedMPOMaker(model).create_mpo()
+    b = TaggedMPOMaker(model, merge_site_terms=False).create_mpo()
+    mps = initial_state(model, a, SweepParams(init_bond_dimension=12, seed=11), 6, 0)
+    assert abs(expval(mps, a) - expval(mps, b)) <= 1e-12 * abs(expval(mps, a))
+
+
+# ------------------------------------------------------------------ integrals
+def _oracle_integral_gradient(model, mps, nelec):
+    """The gradient driver's chain on the CPU: oracle environments, the plans run by the
+    task-table interpreter, then chain_to_integrals."""
+    from qcmaquis_gb300.gradient import chain_to_integrals
+    from oracle.sweep import overlap
+    mpo = TaggedMPOMaker(model, merge_site_terms=False).create_mpo()
+    L = model.L
+    right = [None] * (L + 1)
+    right[L] = R.right_boundary(mps[L - 1])
+    for j in range(L - 1, 0, -1):
+        right[j] = R.overlap_mpo_right_step(mps[j], mps[j], right[j + 1], mpo[j])
+    left = R.left_boundary(mps[0])
+    grads, fmpos = [], []
+    for j in range(L):
+        psi = mps[j].copy().make_left_paired()
+        g, f = _interp_gradient(psi, left, right[j + 1], mpo[j])
+        grads.append(g)
+        fmpos.append(f)
+        left = R.overlap_mpo_left_step(mps[j], mps[j], left, mpo[j])
+    return chain_to_integrals(model, mpo, grads, fmpos, overlap(mps))
+
+
+def _energy(model_ints, L, nelec, mps):
+    from oracle.sweep import expval, overlap
+    m = QCModel(L, model_ints, nelec)
+    mpo = TaggedMPOMaker(m).create_mpo()
+    return expval(mps, mpo) / overlap(mps) + mpo.core_energy
+
+
+def test_integral_gradient_matches_central_differences():
+    """20 random integrals of an L=6 problem at a random MPS: the energy is linear in
+    each integral, so central differences (step 1e-5) are exact up to rounding."""
+    L, Ne = 6, 6
+    ints = synthetic_integral_map(L, seed=3)
+    model = QCModel(L, ints, Ne)
+    mps = initial_state(model, TaggedMPOMaker(model).create_mpo(), SweepParams(init_bond_dimension=12, seed=5),
+                        Ne, 0)
+    _, d_int = _oracle_integral_gradient(model, mps, Ne)
+    keys = sorted(ints)
+    rng = np.random.default_rng(7)
+    h = 1e-5
+    for u in [keys[i] for i in rng.choice(len(keys), 20, replace=False)]:
+        up, dn = dict(ints), dict(ints)
+        up[u] += h
+        dn[u] -= h
+        fd = (_energy(up, L, Ne, mps) - _energy(dn, L, Ne, mps)) / (2 * h)
+        assert abs(fd - d_int[u]) <= 1e-7 * max(1.0, abs(fd)), (u, fd, d_int[u])
+
+
+def test_integral_gradient_at_the_lih_ground_state_is_the_reference_rdm(golden):
+    """LiH (L=4, N=2): the converged oracle DMRG state's integral gradient equals the RDM
+    sums of exact diagonalisation, and the exact 2-RDM equals the reference's own
+    golden 2-RDM (test2.cpp:60-120), whose element (i,j,k,l) is the chemist-ordered
+    Gamma[i,k,j,l] = sum_st <a+_is a+_jt a_lt a_ks>."""
+    from conftest import integral_map
+    from oracle.fci import fci_rdms, fci_states
+    from oracle.sweep import SweepParams as OP, run_dmrg
+    from qcmaquis_gb300.gradient import rdm_sums_from_gamma
+    g = golden["lih"]
+    ints = integral_map(g["integrals"])
+    L, Ne = g["L"], g["nelec"]
+    model = QCModel(L, ints, Ne)
+    rec, mps = run_dmrg(model, TaggedMPOMaker(model).create_mpo(),
+                        OP(nsweeps=6, max_bond_dimension=32, ietl_jcd_tol=1e-13, ietl_jcd_maxiter=20), nelec=Ne)
+    assert abs(rec.sweep_energy[-1] - g["energy"]) < 1e-9
+    _, d_int = _oracle_integral_gradient(model, mps, Ne)
+    (st,), dets = fci_states(L, ints, Ne, 0, 1)
+    g1, g2 = fci_rdms(L, dets, st[1])
+    want = rdm_sums_from_gamma(L, list(d_int), g1, g2)
+    err = max(abs(d_int[u] - want[u]) for u in d_int)
+    assert err < 1e-8, err
+    ref = golden["lih_2rdm"]
+    got = np.array([g2[i, k, j, l] for (i, j, k, l) in ref["index"]])
+    assert np.max(np.abs(got - np.array(ref["value"]))) < 1e-8
+
+
+# ------------------------------------------------------------------ GPU
+@pytest.mark.gpu
+@pytest.mark.parametrize("site", [0, 3])
+def test_gpu_gradient_plan_matches_interpreter(site):
+    import torch
+    from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
+    model, mpo, mps, left, right = _single_site_problem(site=site, m=24)
+    psi = mps[site].copy().make_left_paired()
+    want, f = _interp_gradient(psi, left, right, mpo[site])
+    eng = Engine("cuda:0")
+    x, Lb, Rb = DeviceMPSTensor.from_host(psi), DeviceBoundary.from_host(left), DeviceBoundary.from_host(right)
+    p = N.plan_energy_gradient(psi.phys_i, psi.left_i, psi.right_i, x.layout, Lb.layout, Rb.layout, f, True)
+    p.upload()
+    out = torch.empty(p.out_elems, dtype=torch.float64, device="cuda:0")
+    eng.run(p, ket=x.data, left=Lb, right=Rb, out=out, precision=N.PREC_FP64)
+    got = out.cpu().numpy()
+    assert np.max(np.abs(got - want)) <= 1e-12 * max(1.0, np.abs(want).max())
+    with pytest.raises(RuntimeError):
+        eng.run(p, ket=x.data, left=Lb, right=Rb, out=out, precision=N.PREC_BF16X3)
+
+
+@pytest.mark.gpu
+def test_gpu_integral_gradient_matches_the_cpu_chain():
+    from qcmaquis_gb300.engine import DeviceMPSTensor
+    from qcmaquis_gb300.gradient import energy_gradient
+    L, Ne = 6, 6
+    ints = synthetic_integral_map(L, seed=3)
+    model = QCModel(L, ints, Ne)
+    mps = initial_state(model, TaggedMPOMaker(model).create_mpo(), SweepParams(init_bond_dimension=16, seed=5),
+                        Ne, 0)
+    _, want = _oracle_integral_gradient(model, mps, Ne)
+    res = energy_gradient(model, [DeviceMPSTensor.from_host(t.copy().make_left_paired()) for t in mps], Ne)
+    assert abs(res.energy - _energy(ints, L, Ne, mps)) <= 1e-11 * abs(res.energy)
+    err = max(abs(res.d_integrals[u] - want[u]) for u in want)
+    assert err <= 1e-11 * max(1.0, max(abs(v) for v in want.values()))
+
+
+@pytest.mark.gpu
+def test_gpu_lih_ground_state_gradient_is_the_rdm(golden):
+    """GPU sweeps to the LiH ground state, the GPU gradient, and the RDM sums of exact
+    diagonalisation (pinned to the reference's golden 2-RDM by the CPU test)."""
+    from conftest import integral_map
+    from oracle.fci import fci_rdms, fci_states
+    from qcmaquis_gb300 import sweep as G
+    from qcmaquis_gb300.gradient import energy_gradient, rdm_sums_from_gamma
+    g = golden["lih"]
+    ints = integral_map(g["integrals"])
+    L, Ne = g["L"], g["nelec"]
+    model = QCModel(L, ints, Ne)
+    rec, mps = G.run_dmrg(model, TaggedMPOMaker(model).create_mpo(),
+                          G.SweepParams(nsweeps=6, max_bond_dimension=32, ietl_jcd_tol=1e-13, ietl_jcd_maxiter=20),
+                          nelec=Ne)
+    assert abs(rec.sweep_energy[-1] - g["energy"]) < 1e-9
+    res = energy_gradient(model, mps, Ne)
+    (st,), dets = fci_states(L, ints, Ne, 0, 1)
+    g1, g2 = fci_rdms(L, dets, st[1])
+    want = rdm_sums_from_gamma(L, list(res.d_integrals), g1, g2)
+    assert max(abs(res.d_integrals[u] - want[u]) for u in want) < 1e-8
