@@ -166,7 +166,7 @@ int qcm_plan_boundary_tensor_mpo(const qcm_index_t* phys, const qcm_index_t* lef
 /* Gradient of the local energy E = <psi| H_eff psi> (the contraction of
  * qcm_plan_sigma, same arguments) with respect to every term scale of the MPO
  * tensor: OUT[t] = dE/d term_scale[t], t indexing the flattened term arrays of
- * qcm_mpo_t (out_elems = their length).  With left = L[j], right = R[j+1] and
+ * qcm_mpo_t; out_elems is their length.  With left = L[j], right = R[j+1] and
  * psi = the site tensor of a single-site problem at j, E is <Psi|H|Psi> of the
  * whole MPS, so OUT is the derivative of the energy expectation value with
  * respect to the site-j MPO coefficients -- the adjoint behind dE/d(t_pq),
