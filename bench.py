@@ -38,6 +38,8 @@ def parse():
                     help="time one full two-site sweep (FP64 and BF16x3 sigma forms) instead of sigma calls")
     ap.add_argument("--jd-maxiter", type=int, default=10)
     ap.add_argument("--nsweeps", type=int, default=1, help="--sweep: number of sweeps")
+    ap.add_argument("--overlap-host", action="store_true",
+                    help="--sweep: also time the forms without per-part synchronisation")
     ap.add_argument("--ramp", default="", help="--sweep: bond dimension per sweep, e.g. 256,256,512,512,1024,1024")
     ap.add_argument("--no-images", action="store_true",
                     help="BF16x3: split operands inside the block-product kernel instead of pre-split images")
@@ -222,7 +224,13 @@ def run_sweep(args):
     variants = (("fp64", 0, 0, "svd"), ("mixed", 2, 0, "heev"))
     if nsweeps == 1:
         variants += (("bf16x3_sigma_svd", 2, 0, "svd"),)
-    for name, prec, bprec, trunc in variants:
+    variants = tuple(v + (True,) for v in variants)
+    if args.overlap_host:
+        # both forms with the device left running while the host builds the next plan (the
+        # headline), and the mixed form once more synchronised per part for its breakdown
+        variants = (("fp64", 0, 0, "svd", False), ("mixed", 2, 0, "heev", False),
+                    ("mixed_timed_parts", 2, 0, "heev", True))
+    for name, prec, bprec, trunc, time_parts in variants:
         mps = [DeviceMPSTensor.from_host(t) for t in sites]
         p = SweepParams(nsweeps=nsweeps, max_bond_dimension=args.m, sweep_bond_dimensions=ramp,
                         truncation_initial=1e-16, truncation_final=1e-16, ietl_jcd_tol=1e-7,
@@ -230,7 +238,8 @@ def run_sweep(args):
                         alpha_initial=0.0, alpha_main=0.0, alpha_final=0.0)
         torch.cuda.synchronize()
         t1 = time.time()
-        rec, _ = run_dmrg(model, mpo, p, nelec, mps=mps, precision=prec, ts_mpo=ts, boundary_precision=bprec)
+        rec, _ = run_dmrg(model, mpo, p, nelec, mps=mps, precision=prec, ts_mpo=ts, boundary_precision=bprec,
+                          time_parts=time_parts)
         torch.cuda.synchronize()
         out[name] = {"sweep_s": rec.sweep_seconds[-1], "sweep_seconds": rec.sweep_seconds, "wall_s": time.time() - t1,
                      "energy": rec.sweep_energy[-1], "sweep_energies": rec.sweep_energy,

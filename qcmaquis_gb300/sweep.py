@@ -163,7 +163,7 @@ def expval(mps: List[DeviceMPSTensor], mpo, engine_full: Engine, right_end) -> f
 
 def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optional[List[DeviceMPSTensor]] = None,
              engine: Optional[Engine] = None, device="cuda", callback=None, precision: int = 0, ts_mpo=None,
-             boundary_precision: Optional[int] = None):
+             boundary_precision: Optional[int] = None, time_parts: bool = True):
     """Two-site sweeps.  ``precision`` selects the sigma-vector form (0 = FP64,
     1 = TF32, 2 = BF16x3 tensor cores); boundary updates, the eigensolver's
     vector algebra, the subspace problem, the truncation (SVD, or the
@@ -171,7 +171,10 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
     per-sweep energy stay FP64.  ``boundary_precision`` (default: FP64) selects the form
     of the boundary updates' block products (the boundaries are stored in FP64
     either way).  ``mps`` (right-normalised) replaces the default initial
-    state; ``ts_mpo`` is a prebuilt two-site MPO cache (``make_ts_cache_mpo``)."""
+    state; ``ts_mpo`` is a prebuilt two-site MPO cache (``make_ts_cache_mpo``).
+    ``time_parts`` synchronises the device after each part of a microiteration to
+    time it (``SweepRecord.seconds``); without it the device finishes one
+    microiteration's boundary update while the host builds the next sigma plan."""
     L = model.L
     phys = model.phys
     engine = engine or Engine(device, precision=precision)
@@ -205,7 +208,8 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
             psi = O.make_two_site_mps(mps[site], mps[site + 1])
             sp = SiteProblem(engine, left[site], right[site + 2], ts_mpo[site])
             theta, u, iters = solve_ietl_jcd(sp, psi, p.ietl_jcd_tol, p.ietl_jcd_maxiter)
-            torch.cuda.synchronize()
+            if time_parts:
+                torch.cuda.synchronize()
             t_b = time.time()
             rec.energies.append(theta + mpo.core_energy)
             rec.jd_iterations.append(iters)
@@ -219,7 +223,8 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
                 A, B, tr = O.split(u, mps[site], mps[site + 1], Mmax, cutoff, l2r, truncation=p.twosite_truncation,
                                    alpha=get_alpha(p, sweep), engine=engine, boundary=bnd, mpo=w)
             mps[site], mps[site + 1] = A, B
-            torch.cuda.synchronize()
+            if time_parts:
+                torch.cuda.synchronize()
             t_c = time.time()
             rec.truncated_weight.append(tr.truncated_weight)
             rec.bond_dimension.append(tr.bond_dimension)
@@ -238,7 +243,8 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
                     mps[site - 1] = O.multiply_from_right(mps[site - 1], t)
                 else:
                     mps[site], _ = O.right_normalize_and_return(mps[site])
-            torch.cuda.synchronize()
+            if time_parts:
+                torch.cuda.synchronize()
             t_d = time.time()
             rec.seconds["eigensolver"] += t_b - t_a
             rec.seconds["truncation"] += t_c - t_b
