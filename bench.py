@@ -38,6 +38,7 @@ def parse():
                     help="time one full two-site sweep (FP64 and BF16x3 sigma forms) instead of sigma calls")
     ap.add_argument("--jd-maxiter", type=int, default=10)
     ap.add_argument("--nsweeps", type=int, default=1, help="--sweep: number of sweeps")
+    ap.add_argument("--forms", default="", help="--sweep: comma-separated subset of the forms to run")
     ap.add_argument("--overlap-host", action="store_true",
                     help="--sweep: also time the forms without per-part synchronisation")
     ap.add_argument("--ramp", default="", help="--sweep: bond dimension per sweep, e.g. 256,256,512,512,1024,1024")
@@ -230,6 +231,9 @@ def run_sweep(args):
         # headline), and the mixed form once more synchronised per part for its breakdown
         variants = (("fp64", 0, 0, "svd", False), ("mixed", 2, 0, "heev", False),
                     ("mixed_timed_parts", 2, 0, "heev", True))
+    if args.forms:
+        keep = set(args.forms.split(","))
+        variants = tuple(v for v in variants if v[0] in keep)
     for name, prec, bprec, trunc, time_parts in variants:
         mps = [DeviceMPSTensor.from_host(t) for t in sites]
         p = SweepParams(nsweeps=nsweeps, max_bond_dimension=args.m, sweep_bond_dimensions=ramp,
@@ -245,9 +249,14 @@ def run_sweep(args):
                      "energy": rec.sweep_energy[-1], "sweep_energies": rec.sweep_energy,
                      "last_micro_energy": rec.energies[-1], "sigma_calls": rec.sigma_calls,
                      "max_bond": max(rec.bond_dimension), "truncated_weight": rec.sweep_truncated_weight[-1],
-                     "truncation": trunc, "seconds_by_part": rec.seconds}
+                     "truncation": trunc, "seconds_by_part": rec.seconds,
+                     "repeated_layouts": len(rec.layout_digests) - len(set(rec.layout_digests)),
+                     "microiterations": len(rec.layout_digests)}
         del mps
         torch.cuda.empty_cache()
+    if "fp64" not in out or "mixed" not in out:
+        print(json.dumps({"metric": "sweep s (subset of forms)", "runs": out, "setup_s": setup}))
+        return
     f, b = out["fp64"], out["mixed"]
     dsweep = [abs(x - y) for x, y in zip(b["sweep_energies"], f["sweep_energies"])]
     line = {"metric": f"sweep s (two-site sweep, L={L} N={nelec} S=0 SU2U1, m={args.m})", "value": b["sweep_s"],

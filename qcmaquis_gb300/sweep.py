@@ -89,6 +89,9 @@ class SweepRecord:
     sweep_truncated_weight: List[float] = field(default_factory=list)
     sweep_seconds: List[float] = field(default_factory=list)
     sigma_calls: int = 0
+    # per microiteration: a digest of the sigma problem's layouts (psi, L, R) -- equal
+    # digests at the same site in different sweeps could share one plan
+    layout_digests: List[int] = field(default_factory=list)
     # wall time per part of the sweeps (host clock, device synchronised at each part's end)
     seconds: Dict[str, float] = field(default_factory=lambda: {"eigensolver": 0.0, "truncation": 0.0,
                                                                "boundary": 0.0, "plans": 0.0})
@@ -163,7 +166,8 @@ def expval(mps: List[DeviceMPSTensor], mpo, engine_full: Engine, right_end) -> f
 
 def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optional[List[DeviceMPSTensor]] = None,
              engine: Optional[Engine] = None, device="cuda", callback=None, precision: int = 0, ts_mpo=None,
-             boundary_precision: Optional[int] = None, time_parts: bool = True):
+             boundary_precision: Optional[int] = None, time_parts: bool = True, checkpoint: Optional[str] = None,
+             start_sweep: int = 0):
     """Two-site sweeps.  ``precision`` selects the sigma-vector form (0 = FP64,
     1 = TF32, 2 = BF16x3 tensor cores); boundary updates, the eigensolver's
     vector algebra, the subspace problem, the truncation (SVD, or the
@@ -174,7 +178,10 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
     state; ``ts_mpo`` is a prebuilt two-site MPO cache (``make_ts_cache_mpo``).
     ``time_parts`` synchronises the device after each part of a microiteration to
     time it (``SweepRecord.seconds``); without it the device finishes one
-    microiteration's boundary update while the host builds the next sigma plan."""
+    microiteration's boundary update while the host builds the next sigma plan.
+    ``checkpoint`` (a directory) saves the MPS and the sweep status after every
+    sweep (``sim.hpp:197-211``); ``start_sweep`` resumes a run at that sweep of
+    its schedule (``mps`` from ``checkpoint.load``, sweeps start_sweep..nsweeps-1)."""
     L = model.L
     phys = model.phys
     engine = engine or Engine(device, precision=precision)
@@ -194,7 +201,7 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
         right[i] = engine.overlap_mpo_right_step(mps[i], right[i + 1], mpo[i], precision=bprec)
     rec = SweepRecord()
     nmicro = 2 * (L - 2) if L > 2 else 1
-    for sweep in range(p.nsweeps):
+    for sweep in range(start_sweep, p.nsweeps):
         t0 = time.time()
         Mmax = get_Mmax(p, sweep)
         cutoff = get_cutoff(p, sweep)
@@ -206,6 +213,9 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
             tp0 = engine.plan_seconds
             t_a = time.time()
             psi = O.make_two_site_mps(mps[site], mps[site + 1])
+            rec.layout_digests.append(hash((site, tuple(psi.layout.keys), tuple(psi.layout.shapes),
+                                            tuple(left[site].layout.keys), tuple(left[site].layout.shapes),
+                                            tuple(right[site + 2].layout.keys), tuple(right[site + 2].layout.shapes))))
             sp = SiteProblem(engine, left[site], right[site + 2], ts_mpo[site])
             theta, u, iters = solve_ietl_jcd(sp, psi, p.ietl_jcd_tol, p.ietl_jcd_maxiter)
             if time_parts:
@@ -257,6 +267,11 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
         e = expval(mps, mpo, engine_full, right_end) / overlap(mps) + mpo.core_energy
         rec.sweep_energy.append(e)
         rec.sweep_truncated_weight.append(max(rec.truncated_weight[-nmicro:]))
+        if checkpoint:
+            from .checkpoint import save
+            save(checkpoint, mps, status={"sweep": sweep + 1, "energy": e,
+                                          "truncated_weight": rec.sweep_truncated_weight[-1]},
+                 parameters={k: v for k, v in vars(p).items()})
     return rec, mps
 
 
