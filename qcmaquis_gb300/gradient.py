@@ -60,15 +60,16 @@ def chain_to_integrals(model, mpo, site_grads: List[np.ndarray], fmpos: List[N.F
     return d_coeff, d_int
 
 
-def energy_gradient(model, mps: List[DeviceMPSTensor], nelec: int, twoS: int = 0,
-                    engine: Optional[Engine] = None, device="cuda") -> EnergyGradient:
-    """dE/d(integral) for every integral of ``model`` at the MPS ``mps`` (left-paired
-    device tensors)."""
+def term_gradients(mpo, mps: List[DeviceMPSTensor], nelec: int, twoS: int = 0, engine: Optional[Engine] = None,
+                   device="cuda"):
+    """d<Psi|H|Psi>/d(term scale) of every term of every site tensor of ``mpo`` (one
+    energy-gradient plan per site with the full environments L[j], R[j+1]).
+    Returns (per-site gradients, per-site FMpo, <Psi|H|Psi> per site, seconds of the
+    site plans)."""
     import time
-    from .sweep import _ones_boundary, overlap
+    from .sweep import _ones_boundary
     engine = engine or Engine(device)
-    mpo = TaggedMPOMaker(model, merge_site_terms=False).create_mpo()
-    L = model.L
+    L = len(mpo)
     right_end = (nelec, twoS)
     right: List[Optional[DeviceBoundary]] = [None] * (L + 1)
     right[L] = _ones_boundary(right_end, engine.device)
@@ -93,7 +94,17 @@ def energy_gradient(model, mps: List[DeviceMPSTensor], nelec: int, twoS: int = 0
             left = engine.overlap_mpo_left_step(t, left, mpo[j])
         right[j + 1] = None
     torch.cuda.synchronize()
-    site_s = time.time() - t0
+    return grads, fmpos, e_sites, time.time() - t0
+
+
+def energy_gradient(model, mps: List[DeviceMPSTensor], nelec: int, twoS: int = 0,
+                    engine: Optional[Engine] = None, device="cuda") -> EnergyGradient:
+    """dE/d(integral) for every integral of ``model`` at the MPS ``mps`` (left-paired
+    device tensors)."""
+    from .sweep import overlap
+    engine = engine or Engine(device)
+    mpo = TaggedMPOMaker(model, merge_site_terms=False).create_mpo()
+    grads, fmpos, e_sites, site_s = term_gradients(mpo, mps, nelec, twoS, engine)
     nrm = overlap(mps)
     e_raw = float(np.mean(e_sites))
     d_coeff, d_int = chain_to_integrals(model, mpo, grads, fmpos, nrm)
@@ -121,4 +132,4 @@ def rdm_sums_from_gamma(L: int, keys, g1: np.ndarray, g2: np.ndarray) -> Dict[tu
     return out
 
 
-__all__ = ["EnergyGradient", "energy_gradient", "chain_to_integrals", "rdm_sums_from_gamma"]
+__all__ = ["EnergyGradient", "energy_gradient", "term_gradients", "chain_to_integrals", "rdm_sums_from_gamma"]

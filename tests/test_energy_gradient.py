@@ -247,3 +247,77 @@ def test_gpu_lih_ground_state_gradient_is_the_rdm(golden):
     g1, g2 = fci_rdms(L, dets, st[1])
     want = rdm_sums_from_gamma(L, list(res.d_integrals), g1, g2)
     assert max(abs(res.d_integrals[u] - want[u]) for u in want) < 1e-8
+
+
+# ------------------------------------------------------------------ RDMs
+def _oracle_term_gradients(mpo, mps):
+    """Per-site term gradients of <Psi|O|Psi> on the CPU (oracle environments, plans run
+    by the task-table interpreter)."""
+    L = len(mpo)
+    right = [None] * (L + 1)
+    right[L] = R.right_boundary(mps[L - 1])
+    for j in range(L - 1, 0, -1):
+        right[j] = R.overlap_mpo_right_step(mps[j], mps[j], right[j + 1], mpo[j])
+    left = R.left_boundary(mps[0])
+    grads, fmpos = [], []
+    for j in range(L):
+        g, f = _interp_gradient(mps[j].copy().make_left_paired(), left, right[j + 1], mpo[j])
+        grads.append(g)
+        fmpos.append(f)
+        left = R.overlap_mpo_left_step(mps[j], mps[j], left, mpo[j])
+    return grads, fmpos
+
+
+def _lih_ground_state(golden):
+    from conftest import integral_map
+    from oracle.sweep import SweepParams as OP, run_dmrg
+    g = golden["lih"]
+    ints = integral_map(g["integrals"])
+    model = QCModel(g["L"], ints, g["nelec"])
+    rec, mps = run_dmrg(model, TaggedMPOMaker(model).create_mpo(),
+                        OP(nsweeps=6, max_bond_dimension=32, ietl_jcd_tol=1e-13, ietl_jcd_maxiter=20),
+                        nelec=g["nelec"])
+    assert abs(rec.sweep_energy[-1] - g["energy"]) < 1e-9
+    return g, ints, model, mps
+
+
+def test_rdm_measurement_reproduces_the_reference_lih_2rdm(golden):
+    """One adjoint pass over a measurement MPO that holds every element's terms gives
+    the reference's spin-free 2-RDM (twoptdm of dmrg/tests/test2.cpp:60-120), element
+    for element and in the reference's element order; and the 1-RDM equals exact
+    diagonalisation's spin-summed gamma_pq."""
+    from oracle.fci import fci_rdms, fci_states
+    from oracle.sweep import overlap
+    from qcmaquis_gb300 import rdm as RD
+    g, ints, model, mps = _lih_ground_state(golden)
+    elems, terms, owner = RD.rdm_terms(model, 2)
+    mpo = RD.measurement_mpo(model, terms)
+    grads, fmpos = _oracle_term_gradients(mpo, mps)
+    vals = RD.elements_from_term_gradients(mpo, terms, owner, len(elems), grads, fmpos, overlap(mps))
+    ref = golden["lih_2rdm"]
+    assert [tuple(x) for x in ref["index"]] == elems
+    assert np.max(np.abs(vals - np.array(ref["value"]))) < 1e-8
+    (st,), dets = fci_states(g["L"], ints, g["nelec"], 0, 1)
+    g1, _ = fci_rdms(g["L"], dets, st[1])
+    elems1, terms1, owner1 = RD.rdm_terms(model, 1)
+    mpo1 = RD.measurement_mpo(model, terms1)
+    grads1, fmpos1 = _oracle_term_gradients(mpo1, mps)
+    v1 = RD.elements_from_term_gradients(mpo1, terms1, owner1, len(elems1), grads1, fmpos1, overlap(mps))
+    for (p, q), v in zip(elems1, v1):
+        assert abs(v - g1[p, q]) < 1e-8, ((p, q), v, g1[p, q])
+
+
+@pytest.mark.gpu
+def test_gpu_rdm_measurement_reproduces_the_reference_lih_2rdm(golden):
+    from conftest import integral_map
+    from qcmaquis_gb300 import sweep as G
+    from qcmaquis_gb300.rdm import measure_rdm
+    g = golden["lih"]
+    model = QCModel(g["L"], integral_map(g["integrals"]), g["nelec"])
+    rec, mps = G.run_dmrg(model, TaggedMPOMaker(model).create_mpo(),
+                          G.SweepParams(nsweeps=6, max_bond_dimension=32, ietl_jcd_tol=1e-13, ietl_jcd_maxiter=20),
+                          nelec=g["nelec"])
+    rdm2 = measure_rdm(model, mps, g["nelec"], rank=2)
+    ref = golden["lih_2rdm"]
+    assert list(rdm2) == [tuple(x) for x in ref["index"]]
+    assert np.max(np.abs(np.array(list(rdm2.values())) - np.array(ref["value"]))) < 1e-8
