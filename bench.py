@@ -332,6 +332,25 @@ def run_adjoint(args):
         fd = (energy(up) - energy(dn)) / (2 * h)
         fd_err = max(fd_err, abs(fd - res.d_integrals[u]) / max(1.0, abs(fd)))
         fd_rows.append([list(u), fd, res.d_integrals[u]])
+    # the spin-free RDMs through the same plans, and the energy they imply
+    from qcmaquis_gb300.integrals import synthetic_integrals
+    from qcmaquis_gb300.rdm import measure_rdm
+    torch.cuda.synchronize()
+    t2 = time.time()
+    rdm1 = measure_rdm(model, mps, nelec, rank=1, engine=eng)
+    rdm2 = measure_rdm(model, mps, nelec, rank=2, engine=eng)
+    torch.cuda.synchronize()
+    t_rdm = time.time() - t2
+    tmat, V, core = synthetic_integrals(L, 4, (-2.0, -0.5))
+    g1 = np.zeros((L, L))
+    for (p_, q_), v in rdm1.items():
+        g1[p_, q_] = g1[q_, p_] = v
+    G = np.zeros((L, L, L, L))
+    for (i, j, k, l_), v in rdm2.items():
+        # element (i,j,k,l) = sum_st <a+_is a+_jt a_lt a_ks>; images pqrs = rspq = qpsr = srqp
+        for a, b, c, d in ((i, j, k, l_), (k, l_, i, j), (j, i, l_, k), (l_, k, j, i)):
+            G[a, c, b, d] = v
+    e_rdm = core + float(np.sum(tmat * g1)) + 0.5 * float(np.sum(V * G))
     line = {"metric": f"adjoint dE/d(integrals) s (L={L} N={nelec} S=0 SU2U1, m={m}, all unique integrals)",
             "value": t_grad, "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": "f64",
             "data": "synthetic integrals (seeded), converged from a random MPS",
@@ -341,6 +360,8 @@ def run_adjoint(args):
             "energy_consistency_eh": abs(res.energy - rec.sweep_energy[-1]),
             "converge_s": t_conv, "gradient_site_s": res.site_seconds,
             "fd_max_rel_err_20_integrals": fd_err, "fd_samples": fd_rows,
+            "rdm_s": t_rdm, "rdm1_elements": len(rdm1), "rdm2_elements": len(rdm2),
+            "energy_from_rdms": e_rdm, "energy_from_rdms_err_eh": abs(e_rdm - res.energy),
             "rdm_check": ("tests/test_energy_gradient.py: LiH gradient vs exact-diagonalisation RDM sums and the "
                           "exact 2-RDM vs the reference's golden 2-RDM (dmrg/tests/test2.cpp:60-120)")}
     print(json.dumps(line))

@@ -1109,6 +1109,47 @@ def predict_split_mps(tst_lp: BlockMatrix, p1, p2, left_i, right_i, Mmax, cutoff
     return A, Bt, trunc
 
 
+def predict_new_state(mps: MPSTensor, mpo, left, right, alpha: float, cutoff: float, Mmax: int, l2r: bool):
+    """``predict_new_state_l2r_sweep`` / ``predict_new_state_r2l_sweep`` with the
+    density-matrix perturbation (``ct/common/prediction.hpp:19-125``) and the zero-site
+    factor of ``getZeroSiteTensorL2R/R2L`` (``prediction.hpp:62-73, 126-136``).
+
+    l2r: rho = M M^T + alpha sum_b h_b h_b^T (M left-paired, h = left_boundary_tensor_mpo),
+    the kept eigenvectors U are the new left-normalised site, the zero-site factor is
+    U^T M.  r2l: rho = M^T M + alpha sum_b h_b^T h_b (M right-paired,
+    h = right_boundary_tensor_mpo), the new site is U^T (right-paired), the factor M U.
+    Returns (new site tensor, zero-site factor, truncation results)."""
+    mps = mps.copy()
+    if l2r:
+        mps.make_left_paired()
+    else:
+        mps.make_right_paired()
+    M = mps.data
+    Mt = M.transpose()
+    dm = bm_gemm(M, Mt) if l2r else bm_gemm(Mt, M)
+    half = left_boundary_tensor_mpo(mps, left, mpo) if l2r else right_boundary_tensor_mpo(mps, right, mpo)
+    for h in half:
+        ht = h.transpose()
+        tdm = bm_gemm(h, ht) if l2r else bm_gemm(ht, h)
+        for (lc, rc), b in zip(tdm.keys, tdm.blocks):
+            if M.find_block(lc, rc) == M.n_blocks():
+                continue
+            p = dm.find_block(lc, rc)
+            if p == dm.n_blocks():
+                dm.insert_block(alpha * b, lc, rc)
+            else:
+                dm.blocks[p] = dm.blocks[p] + alpha * b
+    U, S, trunc = heev_truncate(dm, cutoff, Mmax)
+    if l2r:
+        new = MPSTensor.from_block(mps.phys_i, mps.left_i, U.right_basis(), U, LEFT_PAIRED)
+        zero = bm_gemm(U.transpose(), M)
+    else:
+        Ut = U.transpose()
+        new = MPSTensor.from_block(mps.phys_i, Ut.left_basis(), mps.right_i, Ut, RIGHT_PAIRED)
+        zero = bm_gemm(M, U)
+    return new, zero, trunc
+
+
 # --------------------------------------------------------------------------- Jacobi-Davidson
 def jcd_solve(apply_h, init: MPSTensor, tol: float, maxiter: int):
     """``solve_ietl_jcd`` -> ``jacobi_davidson::calculate_eigenvalue`` with zero GMRES

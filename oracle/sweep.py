@@ -178,3 +178,64 @@ def run_dmrg(model, mpo: MPO, p: SweepParams, nelec: int, twoS: int = 0, mps=Non
         rec.sweep_energy.append(e)
         rec.sweep_truncated_weight.append(max(rec.truncated_weight[-nmicro:]))
     return rec, mps
+
+
+def run_dmrg_single_site(model, mpo: MPO, p: SweepParams, nelec: int, twoS: int = 0, mps=None,
+                         callback=None) -> (SweepRecord, List[R.MPSTensor]):
+    """Single-site sweeps: ``SweepOptimizationTypeTrait<SingleSite>``
+    (``sba/SweepOptimizationTypeTrait.h:23-84``: 2(L-1) microiterations, site i going
+    right and 2L-2-i going left) with ``SweepMPSUpdater<SingleSite>``
+    (``sba/SweepMPSUpdater.h:32-155``): the local problem on one site with L[i],
+    R[i+1] and the site's MPO tensor, the density-matrix prediction with the
+    sweep's noise alpha (``R.predict_new_state``), the boundary update, and the
+    zero-site factor merged into the neighbour."""
+    L = model.L
+    if mps is None:
+        mps = initial_state(model, mpo, p, nelec, twoS)
+    left: List = [None] * (L + 1)
+    right: List = [None] * (L + 1)
+    left[0] = R.left_boundary(mps[0])
+    right[L] = R.right_boundary(mps[L - 1])
+    for i in range(L - 1, 0, -1):
+        right[i] = R.overlap_mpo_right_step(mps[i], mps[i], right[i + 1], mpo[i])
+    rec = SweepRecord()
+    nmicro = 1 if L == 1 else (2 if L == 2 else 2 * (L - 1))
+    for sweep in range(p.nsweeps):
+        Mmax = get_Mmax(p, sweep)
+        cutoff = get_cutoff(p, sweep)
+        alpha = get_alpha(p, sweep)
+        for mi in range(nmicro):
+            site = mi if mi < L else 2 * L - 2 - mi
+            forward = mi < L
+            change = (mi == L - 1) or (mi == nmicro - 1)
+            l2r = forward and not change
+
+            def apply_h(x, _l=left[site], _r=right[site + 1], _w=mpo[site]):
+                return R.site_hamil2(x, _l, _r, _w)
+
+            theta, u, iters = R.jcd_solve(apply_h, mps[site], p.ietl_jcd_tol, p.ietl_jcd_maxiter)
+            rec.energies.append(theta + mpo.core_energy)
+            mps[site] = u
+            if l2r and site < L - 1:
+                new, zero, trunc = R.predict_new_state(u, mpo[site], left[site], right[site + 1], alpha, cutoff,
+                                                       Mmax, True)
+                mps[site] = new
+                left[site + 1] = R.overlap_mpo_left_step(mps[site], mps[site], left[site], mpo[site])
+                R.multiply_from_left(mps[site + 1], zero)
+            elif not l2r and site > 0:
+                new, zero, trunc = R.predict_new_state(u, mpo[site], left[site], right[site + 1], alpha, cutoff,
+                                                       Mmax, False)
+                mps[site] = new
+                right[site] = R.overlap_mpo_right_step(mps[site], mps[site], right[site + 1], mpo[site])
+                R.multiply_from_right(mps[site - 1], zero)
+            else:
+                trunc = None
+            if trunc is not None:
+                rec.truncated_weight.append(trunc.truncated_weight)
+                rec.bond_dimension.append(trunc.bond_dimension)
+            if callback:
+                callback(sweep, mi, rec)
+        e = expval(mps, mpo) / overlap(mps) + mpo.core_energy
+        rec.sweep_energy.append(e)
+        rec.sweep_truncated_weight.append(max(rec.truncated_weight[-(nmicro - 1):] or [0.0]))
+    return rec, mps

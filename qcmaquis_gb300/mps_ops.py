@@ -542,6 +542,36 @@ def split(u: DeviceMPSTensor, A0: DeviceMPSTensor, B0: DeviceMPSTensor, Mmax: in
     return A, B, tr
 
 
+def predict_new_state(u: DeviceMPSTensor, mpo, left, right, alpha: float, cutoff: float, Mmax: int, l2r: bool,
+                      engine):
+    """``predict_new_state_l2r_sweep`` / ``_r2l_sweep`` (``ct/common/prediction.hpp:19-125``)
+    of a single-site tensor and the zero-site factor of ``getZeroSiteTensorL2R/R2L``:
+    rho = M M^T (l2r, M left-paired) or M^T M (r2l, M right-paired) plus the noise term
+    alpha sum_b h_b h_b^T from ``left/right_boundary_tensor_mpo``, the FP64
+    eigendecomposition cut, the new site U (l2r) or U^T (r2l) and the factor U^T M
+    (l2r) or M U (r2l).  Returns (new site, factor, truncation results)."""
+    M = as_dbm(u) if l2r else reshape_l2r(u.phys_i, u.left_i, u.right_i, as_dbm(u))
+    Mt = _transpose(M)
+    dm = gemm(M, Mt) if l2r else gemm(Mt, M)
+    if alpha != 0.0:
+        half = engine.boundary_tensor_mpo(u, left if l2r else right, mpo, "left" if l2r else "right")
+        add_perturbation(dm, M, half, alpha, l2r)
+        del half
+    U, _, tr = heev_truncate(dm, cutoff, Mmax)
+    del dm
+    phys = u.phys_i
+    if l2r:
+        new_right = U.right_basis()
+        new_left = u.left_i.copy()
+        common_subset(new_left, index_product(adjoin(phys), new_right))
+        return from_dbm(phys, new_left, new_right, U), gemm(_transpose(U), M), tr
+    Ut = _transpose(U)
+    new_left = Ut.left_basis()
+    new_right = u.right_i.copy()
+    common_subset(new_right, index_product(phys, new_left))
+    return from_dbm(phys, new_left, new_right, reshape_r2l(phys, new_left, new_right, Ut)), gemm(M, U), tr
+
+
 def left_normalize_and_return(t: DeviceMPSTensor) -> Tuple[DeviceMPSTensor, DBM]:
     Q, R = DBM(), DBM()
     for (lc, rc), b in zip(t.layout.keys, as_dbm(t).blocks):
@@ -581,4 +611,5 @@ def multiply_from_right(t: DeviceMPSTensor, Nm: DBM) -> DeviceMPSTensor:
 
 
 __all__ = ["DBM", "block_views", "make_two_site_mps", "split", "svd_truncate", "heev_truncate", "add_perturbation",
+           "predict_new_state",
            "left_normalize_and_return", "right_normalize_and_return", "multiply_from_left", "multiply_from_right", "reshape_l2r", "reshape_r2l"]

@@ -275,4 +275,70 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
     return rec, mps
 
 
-__all__ = ["SweepParams", "SweepRecord", "run_dmrg", "get_alpha", "default_mps_init", "normalize_right", "expval", "overlap"]
+def run_dmrg_single_site(model, mpo, p: SweepParams, nelec: int, twoS: int = 0,
+                         mps: Optional[List[DeviceMPSTensor]] = None, engine: Optional[Engine] = None, device="cuda",
+                         precision: int = 0, callback=None):
+    """Single-site sweeps on the GPU: ``SweepOptimizationTypeTrait<SingleSite>``
+    (``sba/SweepOptimizationTypeTrait.h:23-84``) with ``SweepMPSUpdater<SingleSite>``
+    (``sba/SweepMPSUpdater.h:32-155``): 2(L-1) microiterations, the local problem on
+    one site with L[i], R[i+1] and the single-site MPO tensor (a sigma plan of its
+    own), the density-matrix prediction with the sweep's noise alpha
+    (``mps_ops.predict_new_state``), the boundary update and the zero-site factor
+    merged into the neighbour.  ``precision`` as for ``run_dmrg``."""
+    L = model.L
+    phys = model.phys
+    engine = engine or Engine(device, precision=precision)
+    engine_full = Engine(device, hermitian=False)
+    right_end = (nelec, twoS)
+    if mps is None:
+        mps = default_mps_init(L, phys, right_end, p.init_bond_dimension, p.seed, device)
+        normalize_right(mps)
+    left: List = [None] * (L + 1)
+    right: List = [None] * (L + 1)
+    left[0] = _ones_boundary((0, 0), engine.device)
+    right[L] = _ones_boundary(right_end, engine.device)
+    for i in range(L - 1, 0, -1):
+        right[i] = engine.overlap_mpo_right_step(mps[i], right[i + 1], mpo[i])
+    rec = SweepRecord()
+    nmicro = 1 if L == 1 else (2 if L == 2 else 2 * (L - 1))
+    for sweep in range(p.nsweeps):
+        t0 = time.time()
+        Mmax = get_Mmax(p, sweep)
+        cutoff = get_cutoff(p, sweep)
+        alpha = get_alpha(p, sweep)
+        for mi in range(nmicro):
+            site = mi if mi < L else 2 * L - 2 - mi
+            forward = mi < L
+            change = (mi == L - 1) or (mi == nmicro - 1)
+            l2r = forward and not change
+            sp = SiteProblem(engine, left[site], right[site + 1], mpo[site])
+            theta, u, iters = solve_ietl_jcd(sp, mps[site], p.ietl_jcd_tol, p.ietl_jcd_maxiter)
+            rec.energies.append(theta + mpo.core_energy)
+            rec.jd_iterations.append(iters)
+            rec.sigma_calls += iters
+            mps[site] = u
+            tr = None
+            if l2r and site < L - 1:
+                mps[site], zero, tr = O.predict_new_state(u, mpo[site], left[site], right[site + 1], alpha, cutoff,
+                                                          Mmax, True, engine)
+                left[site + 1] = engine.overlap_mpo_left_step(mps[site], left[site], mpo[site])
+                mps[site + 1] = O.multiply_from_left(mps[site + 1], zero)
+            elif not l2r and site > 0:
+                mps[site], zero, tr = O.predict_new_state(u, mpo[site], left[site], right[site + 1], alpha, cutoff,
+                                                          Mmax, False, engine)
+                right[site] = engine.overlap_mpo_right_step(mps[site], right[site + 1], mpo[site])
+                mps[site - 1] = O.multiply_from_right(mps[site - 1], zero)
+            if tr is not None:
+                rec.truncated_weight.append(tr.truncated_weight)
+                rec.bond_dimension.append(tr.bond_dimension)
+            if callback:
+                callback(sweep, mi, rec)
+        torch.cuda.synchronize()
+        rec.sweep_seconds.append(time.time() - t0)
+        e = expval(mps, mpo, engine_full, right_end) / overlap(mps) + mpo.core_energy
+        rec.sweep_energy.append(e)
+        rec.sweep_truncated_weight.append(max(rec.truncated_weight[-(nmicro - 1):] or [0.0]))
+    return rec, mps
+
+
+__all__ = ["SweepParams", "SweepRecord", "run_dmrg", "run_dmrg_single_site", "get_alpha", "default_mps_init", "normalize_right", "expval", "overlap"]

@@ -85,3 +85,18 @@ def test_mixed_precision_boundaries_sweep_energy_close_to_fp64():
     gpu, _ = G.run_dmrg(model, make_mpo(model), G.SweepParams(nsweeps=6, max_bond_dimension=64), nelec=8,
                         precision=2, boundary_precision=2)
     assert abs(gpu.sweep_energy[-1] - ref["sweep_energy"][-1]) < 1e-6
+
+
+def test_gpu_single_site_sweep_matches_oracle():
+    """Single-site sweeps (density-matrix prediction with the reference's noise
+    schedule): per-microiteration and per-sweep energies to 1e-10 Eh of the oracle's."""
+    from oracle.sweep import SweepParams as OP, run_dmrg_single_site as oracle_ss
+    from qcmaquis_gb300 import sweep as G
+    L, N, m = 6, 6, 24
+    model = QCModel(L, synthetic_integral_map(L, seed=3), N)
+    mpo = make_mpo(model)
+    gpu, _ = G.run_dmrg_single_site(model, mpo, G.SweepParams(nsweeps=3, max_bond_dimension=m), nelec=N)
+    ref, _ = oracle_ss(model, mpo, OP(nsweeps=3, max_bond_dimension=m), nelec=N)
+    assert np.max(np.abs(np.array(gpu.energies) - np.array(ref.energies))) < E_TOL
+    assert np.max(np.abs(np.array(gpu.sweep_energy) - np.array(ref.sweep_energy))) < E_TOL
+    assert gpu.bond_dimension == ref.bond_dimension

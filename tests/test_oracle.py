@@ -111,3 +111,16 @@ def test_hermitian_skip_matches_full_boundary():
     a = R.site_hamil_lbtm(psi, left, right, ts, is_hermitian=True)
     b = R.site_hamil_lbtm(psi2, left2, right2, ts2, is_hermitian=False)
     assert a.copy().axpy(-1.0, b).norm() <= 1e-12 * a.norm()
+
+
+def test_single_site_sweeps_reach_exact_diagonalisation():
+    """The oracle's single-site sweeps (noise-driven bond growth from m=5) reach the
+    exact ground state of an L=6, N=6 singlet."""
+    from oracle.fci import fci_energies
+    from oracle.sweep import SweepParams as OP, run_dmrg_single_site
+    L, N = 6, 6
+    ints = synthetic_integral_map(L, seed=3)
+    model = QCModel(L, ints, N)
+    rec, _ = run_dmrg_single_site(model, make_mpo(model), OP(nsweeps=5, max_bond_dimension=64,
+                                                             alpha_main=0.0, alpha_final=0.0), nelec=N)
+    assert abs(rec.sweep_energy[-1] - fci_energies(L, ints, N, 0, 1)[0]) < 1e-9
