@@ -39,6 +39,8 @@ def parse():
     ap.add_argument("--jd-maxiter", type=int, default=10)
     ap.add_argument("--nsweeps", type=int, default=1, help="--sweep: number of sweeps")
     ap.add_argument("--forms", default="", help="--sweep: comma-separated subset of the forms to run")
+    ap.add_argument("--plan-cache", type=int, default=0,
+                    help="--sweep: sigma plans kept, keyed by layouts (0: the engine default of 2)")
     ap.add_argument("--overlap-host", action="store_true",
                     help="--sweep: also time the forms without per-part synchronisation")
     ap.add_argument("--ramp", default="", help="--sweep: bond dimension per sweep, e.g. 256,256,512,512,1024,1024")
@@ -243,7 +245,7 @@ def run_sweep(args):
         torch.cuda.synchronize()
         t1 = time.time()
         rec, _ = run_dmrg(model, mpo, p, nelec, mps=mps, precision=prec, ts_mpo=ts, boundary_precision=bprec,
-                          time_parts=time_parts)
+                          time_parts=time_parts, plan_cache=args.plan_cache)
         torch.cuda.synchronize()
         out[name] = {"sweep_s": rec.sweep_seconds[-1], "sweep_seconds": rec.sweep_seconds, "wall_s": time.time() - t1,
                      "energy": rec.sweep_energy[-1], "sweep_energies": rec.sweep_energy,
@@ -251,6 +253,7 @@ def run_sweep(args):
                      "max_bond": max(rec.bond_dimension), "truncated_weight": rec.sweep_truncated_weight[-1],
                      "truncation": trunc, "seconds_by_part": rec.seconds,
                      "repeated_layouts": len(rec.layout_digests) - len(set(rec.layout_digests)),
+                     "plan_hits": rec.plan_hits,
                      "microiterations": len(rec.layout_digests)}
         del mps
         torch.cuda.empty_cache()

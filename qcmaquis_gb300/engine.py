@@ -78,6 +78,30 @@ class DeviceBoundary:
         return sh
 
 
+def _digest(*parts) -> bytes:
+    """Content digest of indices and layouts (cached on layout objects)."""
+    import hashlib
+    h = hashlib.blake2b(digest_size=20)
+    for x in parts:
+        d = getattr(x, "_qcm_digest", None)
+        if d is None:
+            g = hashlib.blake2b(digest_size=20)
+            if isinstance(x, Index):
+                g.update(repr(x.data).encode())
+            else:
+                for a in (x.q, x.rows, x.cols, x.off, getattr(x, "ptr", None)):
+                    if a is not None:
+                        g.update(np.ascontiguousarray(a).tobytes())
+                        g.update(b"|")
+            d = g.digest()
+            try:
+                x._qcm_digest = d
+            except AttributeError:   # Index has __slots__
+                pass
+        h.update(d)
+    return h.digest()
+
+
 def _ptr(t: Optional[torch.Tensor]) -> int:
     return 0 if t is None else int(t.data_ptr())
 
@@ -117,6 +141,8 @@ class Engine:
         self.ws = Workspace(self.device)
         self.plan_seconds = 0.0   # host time spent building and uploading plans
         self._plans: Dict[tuple, N.Plan] = {}
+        self.plan_cache_size = 2     # sigma plans kept (least recently used dropped first)
+        self.plan_hits = 0
         self._mpo_cache: Dict[int, N.FMpo] = {}
         self.launches = 0
 
@@ -132,17 +158,23 @@ class Engine:
         return int(torch.cuda.current_stream(self.device).cuda_stream)
 
     def sigma_plan(self, ket: DeviceMPSTensor, L: DeviceBoundary, R: DeviceBoundary, mpo) -> N.Plan:
-        key = ("s", id(ket.layout), id(L.layout), id(R.layout), id(mpo), self.hermitian)
+        # keyed by content: a later site problem with the same indices, layouts and MPO
+        # tensor (frequent once the bond dimensions have settled) reuses the plan
+        key = ("s", _digest(ket.phys_i, ket.left_i, ket.right_i, ket.layout), _digest(L.layout), _digest(R.layout),
+               id(mpo), self.hermitian)
         p = self._plans.get(key)
+        if p is not None:
+            self._plans[key] = self._plans.pop(key)   # most recently used last
+            self.plan_hits += 1
         if p is None:
             t0 = time.time()
             p = N.plan_sigma(ket.phys_i, ket.left_i, ket.right_i, ket.layout, L.layout, R.layout, self.fmpo(mpo),
                              self.hermitian)
             p.upload()
             self.plan_seconds += time.time() - t0
-            p._keep = (ket.layout, L.layout, R.layout)
-            # keep the two most recent sigma plans (a plan's task tables can be hundreds of MB)
-            while len(self._plans) >= 2:
+            p._keep = (mpo,)
+            # keep the most recently used sigma plans (a plan's task tables can be hundreds of MB)
+            while self._plans and len(self._plans) >= max(1, self.plan_cache_size):
                 self._plans.pop(next(iter(self._plans)))
             self._plans[key] = p
         return p

@@ -89,6 +89,7 @@ class SweepRecord:
     sweep_truncated_weight: List[float] = field(default_factory=list)
     sweep_seconds: List[float] = field(default_factory=list)
     sigma_calls: int = 0
+    plan_hits: int = 0
     # per microiteration: a digest of the sigma problem's layouts (psi, L, R) -- equal
     # digests at the same site in different sweeps could share one plan
     layout_digests: List[int] = field(default_factory=list)
@@ -167,7 +168,7 @@ def expval(mps: List[DeviceMPSTensor], mpo, engine_full: Engine, right_end) -> f
 def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optional[List[DeviceMPSTensor]] = None,
              engine: Optional[Engine] = None, device="cuda", callback=None, precision: int = 0, ts_mpo=None,
              boundary_precision: Optional[int] = None, time_parts: bool = True, checkpoint: Optional[str] = None,
-             start_sweep: int = 0):
+             start_sweep: int = 0, plan_cache: int = 0):
     """Two-site sweeps.  ``precision`` selects the sigma-vector form (0 = FP64,
     1 = TF32, 2 = BF16x3 tensor cores); boundary updates, the eigensolver's
     vector algebra, the subspace problem, the truncation (SVD, or the
@@ -181,10 +182,14 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
     microiteration's boundary update while the host builds the next sigma plan.
     ``checkpoint`` (a directory) saves the MPS and the sweep status after every
     sweep (``sim.hpp:197-211``); ``start_sweep`` resumes a run at that sweep of
-    its schedule (``mps`` from ``checkpoint.load``, sweeps start_sweep..nsweeps-1)."""
+    its schedule (``mps`` from ``checkpoint.load``, sweeps start_sweep..nsweeps-1).
+    ``plan_cache`` > 0 keeps that many sigma plans, keyed by their layouts, so a
+    site problem whose layouts recur in a later sweep reuses its plan."""
     L = model.L
     phys = model.phys
     engine = engine or Engine(device, precision=precision)
+    if plan_cache > 0:
+        engine.plan_cache_size = plan_cache
     engine_full = Engine(device, hermitian=False)
     bprec = 0 if boundary_precision is None else boundary_precision
     right_end = (nelec, twoS)
@@ -264,6 +269,7 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
                 callback(sweep, mi, rec)
         torch.cuda.synchronize()
         rec.sweep_seconds.append(time.time() - t0)
+        rec.plan_hits = engine.plan_hits
         e = expval(mps, mpo, engine_full, right_end) / overlap(mps) + mpo.core_energy
         rec.sweep_energy.append(e)
         rec.sweep_truncated_weight.append(max(rec.truncated_weight[-nmicro:]))

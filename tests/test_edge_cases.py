@@ -104,3 +104,18 @@ def test_zero_vector_on_gpu():
         got = eng.site_hamil2(x, DeviceBoundary.from_host(left), DeviceBoundary.from_host(right), ts,
                               precision=prec).data
         assert torch.count_nonzero(got).item() == 0
+
+
+def test_plan_cache_key_is_the_layout_content():
+    """Sigma plans are cached by the content of their indices and layouts: equal
+    content gives one key, any change of a block gives another."""
+    from qcmaquis_gb300.engine import _digest
+    psi, left, right, ts = _random_site_problem(m=8)
+    psi = psi.copy().make_left_paired()
+    a, b = N.Layout.of(psi.data), N.Layout.of(psi.data)
+    assert a is not b and _digest(psi.phys_i, a) == _digest(psi.phys_i, b)
+    shapes = list(a.shapes)
+    shapes[0] = (shapes[0][0] + 1, shapes[0][1])
+    assert _digest(psi.phys_i, a) != _digest(psi.phys_i, N.Layout(a.keys, shapes))
+    La, Lb = N.BoundaryLayout.of(left), N.BoundaryLayout.of(left)
+    assert _digest(La) == _digest(Lb) != _digest(N.BoundaryLayout.of(right))
