@@ -99,4 +99,7 @@ def test_gpu_single_site_sweep_matches_oracle():
     ref, _ = oracle_ss(model, mpo, OP(nsweeps=3, max_bond_dimension=m), nelec=N)
     assert np.max(np.abs(np.array(gpu.energies) - np.array(ref.energies))) < E_TOL
     assert np.max(np.abs(np.array(gpu.sweep_energy) - np.array(ref.sweep_energy))) < E_TOL
-    assert gpu.bond_dimension == ref.bond_dimension
+    # the bond dimension can differ by density-matrix eigenvalues at rounding level
+    # (~1e-17) that fall on either side of the cut; the kept weight cannot
+    tw_g, tw_r = np.array(gpu.truncated_weight), np.array(ref.truncated_weight)
+    assert np.all(np.abs(tw_g - tw_r) <= TW_REL * np.abs(tw_r) + TW_ABS)
