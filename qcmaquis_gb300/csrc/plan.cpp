@@ -541,6 +541,7 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
     task_begin[b2list.size()] = tasks.size();
     std::vector<TaskOut> tout(tasks.size());
     std::vector<TileMap> per(b2list.size());
+    std::vector<std::vector<std::pair<uint64_t, uint32_t>>> ord(b2list.size());
     std::vector<double> fl(b2list.size(), 0.0);
     auto parallel = [&](size_t n, const std::function<void(size_t)>& f) {
         std::atomic<size_t> next{0};
@@ -586,8 +587,11 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
                     C[b2].insert(nb);
                 }
         }
-        std::stable_sort(per[i].begin(), per[i].end(),
-                         [](const KeyedTerm& x, const KeyedTerm& y) { return x.key < y.key; });
+        // stable order by key: sort (key, position) pairs, not the records
+        std::vector<std::pair<uint64_t, uint32_t>>& o = ord[i];
+        o.resize(per[i].size());
+        for (size_t k = 0; k < o.size(); ++k) o[k] = {per[i][k].key, (uint32_t)k};
+        std::sort(o.begin(), o.end());
     });
     int64_t base = 0;
     for (auto& c : C) base = c.assign_offsets(base);
@@ -597,10 +601,10 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
     // precomputed range of the output and term tables (in parallel)
     std::vector<size_t> ntile(b2list.size(), 0);
     parallel(b2list.size(), [&](size_t i) {
-        const TileMap& v = per[i];
+        const std::vector<std::pair<uint64_t, uint32_t>>& o = ord[i];
         size_t n = 0;
-        for (size_t a = 0; a < v.size(); ++a)
-            if (a == 0 || v[a].key != v[a - 1].key) ++n;
+        for (size_t a = 0; a < o.size(); ++a)
+            if (a == 0 || o[a].first != o[a - 1].first) ++n;
         ntile[i] = n;
     });
     std::vector<size_t> obase(b2list.size() + 1, st.aout.size()), tbase(b2list.size() + 1, st.aterm.size());
@@ -616,28 +620,33 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
         const int b2 = b2list[i];
         const BM& cb = C[b2];
         TileMap& v = per[i];
+        std::vector<std::pair<uint64_t, uint32_t>>& ov = ord[i];
         size_t oi = obase[i], ti = tbase[i];
-        for (size_t a = 0; a < v.size();) {
+        for (size_t a = 0; a < ov.size();) {
             size_t b = a + 1;
-            while (b < v.size() && v[b].key == v[a].key) ++b;   // equal keys: one tile
-            const Q out_l = out_left_i.d[v[a].key >> 48].first, out_r = right_i.d[(v[a].key >> 32) & 0xFFFFu].first;
+            while (b < ov.size() && ov[b].first == ov[a].first) ++b;   // equal keys: one tile
+            const uint64_t key = ov[a].first;
+            const Q out_l = out_left_i.d[key >> 48].first, out_r = right_i.d[(key >> 32) & 0xFFFFu].first;
             const Blk& d = cb.b[cb.find(out_l, out_r)];
+            const KeyedTerm& last = v[ov[b - 1].second];
             AxpyOut& o = st.aout[oi++];
             o.dst_buf = c_buf;
-            o.dst_off = d.off + (int64_t)(uint32_t)(v[a].key & 0xFFFFFFFFu);
+            o.dst_off = d.off + (int64_t)(uint32_t)(key & 0xFFFFFFFFu);
             o.ldd = d.rows;
-            o.rows = v[b - 1].rows;
-            o.cols = v[b - 1].cols;
+            o.rows = last.rows;
+            o.cols = last.cols;
             o.t_begin = (int64_t)ti;
             for (size_t k = a; k < b; ++k) {
-                if (prov) (*prov)[ti] = {v[k].tt, v[k].alpha / m->term_scale[v[k].tt]};
-                st.aterm[ti++] = {t_buf, v[k].src_off, v[k].rows, v[k].alpha};
+                const KeyedTerm& x = v[ov[k].second];
+                if (prov) (*prov)[ti] = {x.tt, x.alpha / m->term_scale[x.tt]};
+                st.aterm[ti++] = {t_buf, x.src_off, x.rows, x.alpha};
             }
             o.t_end = (int64_t)ti;
             bytes[i] += 8.0 * o.rows * o.cols * (double)(b - a + 1);
             a = b;
         }
         TileMap().swap(v);
+        std::vector<std::pair<uint64_t, uint32_t>>().swap(ov);
     });
     for (size_t i = 0; i < b2list.size(); ++i) {
         P->axpy_flops += fl[i];
@@ -1462,55 +1471,85 @@ static float bf16_to_float(uint16_t h) {
 
 bool axpy_components(const Stage& st, std::vector<int32_t>& root) {
     const size_t nO = st.aout.size();
-    for (size_t i = 0; i < nO; ++i) {
-        const AxpyOut& a = st.aout[i];
-        for (int64_t k = a.t_begin; k < a.t_end; ++k)
-            if (st.aterm[k].lds != a.rows && a.cols > 1) return false;
-    }
-    std::vector<int32_t> parent(nO);
-    for (size_t i = 0; i < nO; ++i) parent[i] = (int32_t)i;
+    const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    auto run = [&](const std::function<void(unsigned)>& f) {
+        std::vector<std::thread> pool;
+        for (unsigned t = 1; t < nt; ++t) pool.emplace_back(f, t);
+        f(0);
+        for (auto& th : pool) th.join();
+    };
+    std::atomic<bool> contiguous{true};
+    run([&](unsigned t) {
+        for (size_t i = t; i < nO && contiguous.load(std::memory_order_relaxed); i += nt) {
+            const AxpyOut& a = st.aout[i];
+            for (int64_t k = a.t_begin; k < a.t_end; ++k)
+                if (st.aterm[k].lds != a.rows && a.cols > 1) { contiguous = false; break; }
+        }
+    });
+    if (!contiguous) return false;
+    // lock-free union-find: a root is only ever linked under a smaller root (CAS on
+    // the root's own entry), so every component ends with its smallest output as root
+    std::vector<std::atomic<int32_t>> parent(nO);
+    for (size_t i = 0; i < nO; ++i) parent[i].store((int32_t)i, std::memory_order_relaxed);
     auto find = [&](int32_t x) {
-        while (parent[x] != x) { parent[x] = parent[parent[x]]; x = parent[x]; }
-        return x;
+        for (;;) {
+            const int32_t p = parent[x].load(std::memory_order_relaxed);
+            if (p == x) return x;
+            x = p;
+        }
     };
-    // source tile -> first output that reads it: open addressing, linear probing
-    std::vector<int64_t> keys(1u << 16, -1);
-    std::vector<int32_t> vals(1u << 16, 0);
-    size_t used = 0;
-    auto slot = [&](int64_t key) {
-        const size_t mask = keys.size() - 1;
-        size_t h = (size_t)((uint64_t)key * 0x9E3779B97F4A7C15ull >> 17) & mask;
-        while (keys[h] != -1 && keys[h] != key) h = (h + 1) & mask;
-        return h;
+    auto unite = [&](int32_t a, int32_t b) {
+        for (;;) {
+            a = find(a);
+            b = find(b);
+            if (a == b) return;
+            if (a > b) std::swap(a, b);
+            int32_t expect = b;
+            if (parent[b].compare_exchange_strong(expect, a)) return;
+        }
     };
-    for (size_t i = 0; i < nO; ++i) {
-        const AxpyOut& a = st.aout[i];
-        for (int64_t k = a.t_begin; k < a.t_end; ++k) {
-            const int64_t key = ((int64_t)st.aterm[k].src_buf << 56) ^ st.aterm[k].src_off;
-            size_t h = slot(key);
-            if (keys[h] == -1) {
-                keys[h] = key;
-                vals[h] = (int32_t)i;
-                if (2 * ++used > keys.size()) {  // grow and rehash
-                    std::vector<int64_t> ok;
-                    std::vector<int32_t> ov;
-                    ok.swap(keys);
-                    ov.swap(vals);
-                    keys.assign(ok.size() * 2, -1);
-                    vals.assign(ok.size() * 2, 0);
-                    for (size_t q = 0; q < ok.size(); ++q)
-                        if (ok[q] != -1) {
-                            const size_t g = slot(ok[q]);
-                            keys[g] = ok[q];
-                            vals[g] = ov[q];
-                        }
+    // every thread owns the source keys of one hash class: it keeps their first output
+    // in a private open-addressing table and unites later readers with it
+    auto mix = [](int64_t key) { return (uint64_t)key * 0x9E3779B97F4A7C15ull; };
+    run([&](unsigned t) {
+        std::vector<int64_t> keys(1u << 12, -1);
+        std::vector<int32_t> vals(1u << 12, 0);
+        size_t used = 0;
+        auto slot = [&](int64_t key) {
+            const size_t mask = keys.size() - 1;
+            size_t h = (size_t)(mix(key) >> 24) & mask;
+            while (keys[h] != -1 && keys[h] != key) h = (h + 1) & mask;
+            return h;
+        };
+        for (size_t i = 0; i < nO; ++i) {
+            const AxpyOut& a = st.aout[i];
+            for (int64_t k = a.t_begin; k < a.t_end; ++k) {
+                const int64_t key = ((int64_t)st.aterm[k].src_buf << 56) ^ st.aterm[k].src_off;
+                if ((mix(key) >> 58) % nt != t) continue;
+                size_t h = slot(key);
+                if (keys[h] == -1) {
+                    keys[h] = key;
+                    vals[h] = (int32_t)i;
+                    if (2 * ++used > keys.size()) {  // grow and rehash
+                        std::vector<int64_t> ok;
+                        std::vector<int32_t> ov;
+                        ok.swap(keys);
+                        ov.swap(vals);
+                        keys.assign(ok.size() * 2, -1);
+                        vals.assign(ok.size() * 2, 0);
+                        for (size_t q = 0; q < ok.size(); ++q)
+                            if (ok[q] != -1) {
+                                const size_t g = slot(ok[q]);
+                                keys[g] = ok[q];
+                                vals[g] = ov[q];
+                            }
+                    }
+                } else if (vals[h] != (int32_t)i) {
+                    unite((int32_t)i, vals[h]);
                 }
-            } else {
-                const int32_t r1 = find((int32_t)i), r2 = find(vals[h]);
-                if (r1 != r2) parent[std::max(r1, r2)] = std::min(r1, r2);
             }
         }
-    }
+    });
     root.resize(nO);
     for (size_t i = 0; i < nO; ++i) root[i] = find((int32_t)i);
     return true;

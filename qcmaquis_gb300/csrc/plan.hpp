@@ -11,6 +11,7 @@
 
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <string>
 #include <utility>
 #include <vector>
@@ -66,6 +67,17 @@ struct BM {
     size_t left_lower_bound(Q lc) const;
     size_t insert(Blk x);  // returns position
     int64_t assign_offsets(int64_t base);  // sequential offsets, returns end
+};
+
+// Allocator that default-initialises (no zero fill when a table of PODs is resized
+// before every element is written in parallel).
+template <class T>
+struct DefaultInitAlloc : std::allocator<T> {
+    template <class U> struct rebind { using other = DefaultInitAlloc<U>; };
+    DefaultInitAlloc() = default;
+    template <class U> DefaultInitAlloc(const DefaultInitAlloc<U>&) noexcept {}
+    template <class U> void construct(U* p) noexcept { ::new ((void*)p) U; }
+    template <class U, class... A> void construct(U* p, A&&... a) { ::new ((void*)p) U(std::forward<A>(a)...); }
 };
 
 struct AxpyOut {
@@ -167,8 +179,8 @@ struct Stage {
     int32_t zbuf = 0;
     int64_t zoff = 0, zlen = 0;
     // AXPY
-    std::vector<AxpyOut> aout;
-    std::vector<AxpyTerm> aterm;
+    std::vector<AxpyOut, DefaultInitAlloc<AxpyOut>> aout;
+    std::vector<AxpyTerm, DefaultInitAlloc<AxpyTerm>> aterm;
     // GEMM
     std::vector<GemmOut> gout;
     std::vector<GemmSeg> gseg;
