@@ -476,8 +476,8 @@ void free_stage_device(Stage& st) {
     st.ev_fork = st.ev_join = st.side_stream = nullptr;
 }
 
-template <class T>
-static int upload_vec(const std::vector<T>& v, void** d) {
+template <class T, class A>
+static int upload_vec(const std::vector<T, A>& v, void** d) {
     size_t bytes = std::max<size_t>(v.size(), 1) * sizeof(T);
     cudaError_t e = cudaMalloc(d, bytes);
     if (e != cudaSuccess) { set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e)); return QCM_E_NOMEM; }

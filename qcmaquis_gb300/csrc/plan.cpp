@@ -1650,6 +1650,29 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         worker();
         for (auto& th : pool) th.join();
     }
+    // the groups' constant images go to their final offsets, copied in parallel
+    std::vector<int64_t> cim_off(glist.size(), 0);
+    {
+        int64_t c = (int64_t)t.cimg.size();
+        for (size_t gi = 0; gi < glist.size(); ++gi)
+            if (prep[gi].keep) { cim_off[gi] = c; c += (int64_t)prep[gi].wimg.size(); }
+        t.cimg.resize((size_t)c);
+        std::atomic<size_t> next{0};
+        auto copier = [&]() {
+            for (;;) {
+                const size_t gi = next.fetch_add(1);
+                if (gi >= glist.size()) return;
+                if (!prep[gi].keep) continue;
+                std::memcpy(t.cimg.data() + cim_off[gi], prep[gi].wimg.data(), prep[gi].wimg.size());
+                std::vector<uint8_t>().swap(prep[gi].wimg);
+            }
+        };
+        const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        for (unsigned k = 1; k < nt; ++k) pool.emplace_back(copier);
+        copier();
+        for (auto& th : pool) th.join();
+    }
     for (size_t gi = 0; gi < glist.size(); ++gi) {
         if (!prep[gi].keep) continue;
         const std::vector<int32_t>& O = glist[gi]->second;
@@ -1674,10 +1697,8 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         t.bytes += KC * 3 * (int64_t)G * 512;
         for (int64_t c = 0; c < KC; ++c) { t.build.push_back(pid); t.build.push_back((int32_t)c); }
         t.panels.push_back(pa);
-        // B: the group's constant image
-        const int64_t b_off = (int64_t)t.cimg.size();
-        t.cimg.insert(t.cimg.end(), pr.wimg.begin(), pr.wimg.end());
-        std::vector<uint8_t>().swap(pr.wimg);
+        // B: the group's constant image (copied above)
+        const int64_t b_off = cim_off[gi];
         // output: column j is output tile O[j]
         ImgOut io;
         io.c_off = 0;

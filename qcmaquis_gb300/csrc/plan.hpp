@@ -151,7 +151,7 @@ struct ImgTables {
     std::vector<ImgUnit> units;
     std::vector<int64_t> gather;  // source offsets of gathered panels (kcontig 2)
     std::vector<int64_t> coltab;  // (offset, ld) pairs of the output tiles of mode-1 outputs
-    std::vector<uint8_t> cimg;    // constant images (coefficient matrices), built by the plan
+    std::vector<uint8_t, DefaultInitAlloc<uint8_t>> cimg;  // constant images (coefficient matrices), built by the plan
     int64_t bytes = 0;            // per-call image bytes
     // A-resident mode: every tile is one segment of at most IMG_ARES_MAX K-chunks,
     // tiles are ordered by their A tile (image, m0), and each CTA takes a
