@@ -350,9 +350,10 @@ def run_adjoint(args):
         g1[p_, q_] = g1[q_, p_] = v
     G = np.zeros((L, L, L, L))
     for (i, j, k, l_), v in rdm2.items():
-        # element (i,j,k,l) = sum_st <a+_is a+_jt a_lt a_ks>; images pqrs = rspq = qpsr = srqp
+        # element (a,b,c,d) = chemist Gamma[b,c,a,d] = sum_st <a+_bs a+_at a_dt a_cs>;
+        # the element's index images pqrs = rspq = qpsr = srqp fill the rest
         for a, b, c, d in ((i, j, k, l_), (k, l_, i, j), (j, i, l_, k), (l_, k, j, i)):
-            G[a, c, b, d] = v
+            G[b, c, a, d] = v
     e_rdm = core + float(np.sum(tmat * g1)) + 0.5 * float(np.sum(V * G))
     line = {"metric": f"adjoint dE/d(integrals) s (L={L} N={nelec} S=0 SU2U1, m={m}, all unique integrals)",
             "value": t_grad, "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": "f64",

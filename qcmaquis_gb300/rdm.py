@@ -12,7 +12,8 @@ Here all elements' terms go into ONE MPO, every term its own labelled scale, and
 one pass of energy-gradient plans along the chain gives d<Psi|O|Psi>/d(scale)
 for every term at once; an element is the sum of its terms' coefficients times
 those derivatives (the expectation value is linear in each scale), divided by
-<Psi|Psi>.
+<Psi|Psi>.  The measurement MPO is not Hermitian, so its boundaries and plans
+contract every MPO bond (no Hermitian-partner shortcut).
 """
 from __future__ import annotations
 
@@ -98,6 +99,10 @@ def measure_rdm(model, mps, nelec: int, rank: int = 2, twoS: int = 0, engine: Op
     from .sweep import overlap
     elems, terms, owner = rdm_terms(model, rank)
     mpo = measurement_mpo(model, terms)
+    # a measurement MPO is not Hermitian (an element's terms come without their
+    # conjugates), so every MPO bond is contracted: no Hermitian-partner shortcut
+    if engine is None or engine.hermitian:
+        engine = Engine(mps[0].data.device, hermitian=False)
     grads, fmpos, _, _ = term_gradients(mpo, mps, nelec, twoS, engine)
     vals = elements_from_term_gradients(mpo, terms, owner, len(elems), grads, fmpos, overlap(mps))
     return dict(zip(elems, vals.tolist()))

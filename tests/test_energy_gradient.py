@@ -49,11 +49,11 @@ def _with_scales(t, scales, f):
     return c
 
 
-def _interp_gradient(psi, left, right, w):
+def _interp_gradient(psi, left, right, w, herm=True):
     lay = N.Layout.of(psi.data)
     Ll, Rl = N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
     f = N.FMpo(w)
-    p = N.plan_energy_gradient(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, f, True)
+    p = N.plan_energy_gradient(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, f, herm)
     assert p.out_elems == f.n_terms
     bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.full(p.out_elems, np.nan)] + \
         [np.full(max(s, 1), np.nan) for s in p.scratch]
@@ -166,7 +166,7 @@ def test_integral_gradient_at_the_lih_ground_state_is_the_reference_rdm(golden):
     """LiH (L=4, N=2): the converged oracle DMRG state's integral gradient equals the RDM
     sums of exact diagonalisation, and the exact 2-RDM equals the reference's own
     golden 2-RDM (test2.cpp:60-120), whose element (i,j,k,l) is the chemist-ordered
-    Gamma[i,k,j,l] = sum_st <a+_is a+_jt a_lt a_ks>."""
+    Gamma[j,k,i,l] = sum_st <a+_js a+_it a_lt a_ks>."""
     from conftest import integral_map
     from oracle.fci import fci_rdms, fci_states
     from oracle.sweep import SweepParams as OP, run_dmrg
@@ -185,7 +185,7 @@ def test_integral_gradient_at_the_lih_ground_state_is_the_reference_rdm(golden):
     err = max(abs(d_int[u] - want[u]) for u in d_int)
     assert err < 1e-8, err
     ref = golden["lih_2rdm"]
-    got = np.array([g2[i, k, j, l] for (i, j, k, l) in ref["index"]])
+    got = np.array([g2[j, k, i, l] for (i, j, k, l) in ref["index"]])
     assert np.max(np.abs(got - np.array(ref["value"]))) < 1e-8
 
 
@@ -250,21 +250,22 @@ def test_gpu_lih_ground_state_gradient_is_the_rdm(golden):
 
 
 # ------------------------------------------------------------------ RDMs
-def _oracle_term_gradients(mpo, mps):
+def _oracle_term_gradients(mpo, mps, herm=False):
     """Per-site term gradients of <Psi|O|Psi> on the CPU (oracle environments, plans run
-    by the task-table interpreter)."""
+    by the task-table interpreter); a measurement MPO is not Hermitian, so every bond
+    is contracted."""
     L = len(mpo)
     right = [None] * (L + 1)
     right[L] = R.right_boundary(mps[L - 1])
     for j in range(L - 1, 0, -1):
-        right[j] = R.overlap_mpo_right_step(mps[j], mps[j], right[j + 1], mpo[j])
+        right[j] = R.overlap_mpo_right_step(mps[j], mps[j], right[j + 1], mpo[j], is_hermitian=herm)
     left = R.left_boundary(mps[0])
     grads, fmpos = [], []
     for j in range(L):
-        g, f = _interp_gradient(mps[j].copy().make_left_paired(), left, right[j + 1], mpo[j])
+        g, f = _interp_gradient(mps[j].copy().make_left_paired(), left, right[j + 1], mpo[j], herm)
         grads.append(g)
         fmpos.append(f)
-        left = R.overlap_mpo_left_step(mps[j], mps[j], left, mpo[j])
+        left = R.overlap_mpo_left_step(mps[j], mps[j], left, mpo[j], is_hermitian=herm)
     return grads, fmpos
 
 
@@ -321,3 +322,65 @@ def test_gpu_rdm_measurement_reproduces_the_reference_lih_2rdm(golden):
     ref = golden["lih_2rdm"]
     assert list(rdm2) == [tuple(x) for x in ref["index"]]
     assert np.max(np.abs(np.array(list(rdm2.values())) - np.array(ref["value"]))) < 1e-8
+
+
+def _energy_from_rdms(L, ints, rdm1, rdm2):
+    """core + sum t gamma + 1/2 sum (pq|rs) Gamma from the measured elements (their
+    index symmetry pqrs = rspq = qpsr = srqp fills the rest)."""
+    from oracle.fci import expand_integrals
+    t, V, core = expand_integrals(L, ints)
+    g1 = np.zeros((L, L))
+    for (p, q), v in rdm1.items():
+        g1[p, q] = g1[q, p] = v
+    G = np.zeros((L, L, L, L))
+    for (i, j, k, l), v in rdm2.items():
+        # element (a,b,c,d) = chemist Gamma[b,c,a,d]
+        for a, b, c, d in ((i, j, k, l), (k, l, i, j), (j, i, l, k), (l, k, j, i)):
+            G[b, c, a, d] = v
+    return core + float(np.sum(t * g1)) + 0.5 * float(np.sum(V * G))
+
+
+def test_rdms_of_a_random_state_give_its_energy():
+    """E = core + sum t gamma + 1/2 sum (pq|rs) Gamma holds for any state: the measured
+    RDMs of a random L=6, N=6 MPS reproduce its expectation value."""
+    from oracle.sweep import expval, overlap
+    from qcmaquis_gb300 import rdm as RD
+    L, Ne = 6, 6
+    ints = synthetic_integral_map(L, seed=3)
+    model = QCModel(L, ints, Ne)
+    mpo = TaggedMPOMaker(model).create_mpo()
+    mps = initial_state(model, mpo, SweepParams(init_bond_dimension=12, seed=5), Ne, 0)
+    nrm = overlap(mps)
+    out = []
+    for rank in (1, 2):
+        elems, terms, owner = RD.rdm_terms(model, rank)
+        m = RD.measurement_mpo(model, terms)
+        grads, fmpos = _oracle_term_gradients(m, mps)
+        out.append(dict(zip(elems, RD.elements_from_term_gradients(m, terms, owner, len(elems), grads, fmpos, nrm))))
+    e = expval(mps, mpo) / nrm + mpo.core_energy
+    assert abs(_energy_from_rdms(L, ints, *out) - e) < 1e-10 * max(1.0, abs(e))
+
+
+def test_measured_2rdm_is_the_exact_2rdm_at_l6():
+    """At the L=6, N=6 ground state, the measured elements and their index images fill
+    the whole chemist-ordered Gamma, equal to exact diagonalisation's."""
+    from oracle.fci import fci_rdms, fci_states
+    from oracle.sweep import SweepParams as OP, overlap, run_dmrg
+    from qcmaquis_gb300 import rdm as RD
+    L, Ne = 6, 6
+    ints = synthetic_integral_map(L, seed=3)
+    model = QCModel(L, ints, Ne)
+    rec, mps = run_dmrg(model, TaggedMPOMaker(model).create_mpo(),
+                        OP(nsweeps=6, max_bond_dimension=64, ietl_jcd_tol=1e-13, ietl_jcd_maxiter=20), nelec=Ne)
+    (st,), dets = fci_states(L, ints, Ne, 0, 1)
+    _, g2 = fci_rdms(L, dets, st[1])
+    elems, terms, owner = RD.rdm_terms(model, 2)
+    m = RD.measurement_mpo(model, terms)
+    grads, fmpos = _oracle_term_gradients(m, mps)
+    vals = RD.elements_from_term_gradients(m, terms, owner, len(elems), grads, fmpos, overlap(mps))
+    G = np.full((L,) * 4, np.nan)
+    for (i, j, k, l), v in zip(elems, vals):
+        for a, b, c, d in ((i, j, k, l), (k, l, i, j), (j, i, l, k), (l, k, j, i)):
+            G[b, c, a, d] = v
+    assert not np.isnan(G).any()
+    assert np.max(np.abs(G - g2)) < 1e-9
