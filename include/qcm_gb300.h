@@ -179,6 +179,15 @@ int qcm_plan_energy_gradient(const qcm_index_t* phys, const qcm_index_t* left_i,
                              const qcm_blocks_t* psi, const qcm_boundary_t* left, const qcm_boundary_t* right,
                              const qcm_mpo_t* mpo, int32_t hermitian, qcm_plan** plan);
 
+/* Batching: one plan for n independent sigma problems (plans of qcm_plan_sigma).
+ * caller_off holds, per problem, the element offsets of its KET, LEFT, RIGHT and
+ * OUT data inside the buffers passed to qcm_plan_run (4 per problem); the scratch
+ * slots and the operand images of the problems are laid out back to back by the
+ * merged plan (qcm_plan_sizes, qcm_plan_image_bytes).  Each stage of the merged
+ * plan runs every problem's work in one launch: one persistent grouped block-
+ * product launch per stage for all problems.  The sub-plans stay valid. */
+int qcm_plan_merge(qcm_plan* const* plans, int32_t n, const int64_t* caller_off, qcm_plan** out);
+
 /* Sizes (elements) of the output and of the three scratch slots. */
 int qcm_plan_sizes(const qcm_plan* plan, int64_t* out_elems, int64_t* scratch_elems3);
 

@@ -16,6 +16,7 @@
 // by the output tile it writes, so the device executes every output exactly
 // once without atomics.
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -1807,6 +1808,169 @@ int qcm_plan_energy_gradient(const qcm_index_t* phys, const qcm_index_t* left_i,
     } catch (const std::exception& e) {
         set_error(std::string("qcm_plan_energy_gradient: ") + e.what());
         *plan = nullptr;
+        return QCM_E_INVALID;
+    }
+}
+
+// ------------------------------------------------------------------ batching
+// One plan for many independent sigma problems: every stage's task tables are the
+// concatenation of the problems' tables with their offsets moved to each problem's
+// slice of shared buffers -- the caller's KET/LEFT/RIGHT/OUT slices (given), the
+// scratch slots and the per-stage image bytes (back to back, in problem order),
+// the plans' constant images (appended).  Each stage then runs every problem's
+// work in one launch.
+static qcm_plan* merge_sigma_plans(qcm_plan* const* plans, int32_t n, const int64_t* caller_off) {
+    if (n < 1) throw std::runtime_error("no plans to merge");
+    size_t nst = 0;
+    for (int32_t k = 0; k < n; ++k) {
+        if (!plans[k]) throw std::runtime_error("null plan");
+        if (plans[k]->kind != PK_SIGMA) throw std::runtime_error("only sigma plans can be merged");
+        nst = std::max(nst, plans[k]->stages.size());
+    }
+    auto* P = new qcm_plan();
+    P->kind = PK_SIGMA;
+    // element offsets of problem k in every slot
+    std::vector<std::array<int64_t, QCM_NBUF>> base(n);
+    int64_t sc[3] = {0, 0, 0};
+    for (int32_t k = 0; k < n; ++k) {
+        base[k].fill(0);
+        for (int q = 0; q < 4; ++q) base[k][q] = caller_off[4 * k + q];
+        for (int q = 0; q < 3; ++q) {
+            base[k][QCM_BUF_S0 + q] = sc[q];
+            sc[q] += plans[k]->scratch[q];
+        }
+        P->out_elems = std::max(P->out_elems, base[k][QCM_BUF_OUT] + plans[k]->out_elems);
+        P->gemm_flops += plans[k]->gemm_flops;
+        P->axpy_flops += plans[k]->axpy_flops;
+        P->axpy_bytes += plans[k]->axpy_bytes;
+    }
+    for (int q = 0; q < 3; ++q) P->scratch[q] = sc[q];
+    for (size_t si = 0; si < nst; ++si) {
+        int kind = -1;
+        for (int32_t k = 0; k < n; ++k)
+            if (si < plans[k]->stages.size()) {
+                const int kk = plans[k]->stages[si].kind;
+                if (kind >= 0 && kk != kind) throw std::runtime_error("plans to merge differ in their stages");
+                kind = kk;
+            }
+        Stage m;
+        m.kind = kind;
+        if (kind == ST_ZERO) {
+            int64_t any = 0;
+            for (int32_t k = 0; k < n; ++k)
+                if (si < plans[k]->stages.size()) {
+                    const Stage& st = plans[k]->stages[si];
+                    if (m.zlen == 0) m.zbuf = st.zbuf;
+                    if (st.zbuf != m.zbuf || st.zoff != 0 || st.zbuf < QCM_BUF_S0 || st.zbuf > QCM_BUF_S2)
+                        throw std::runtime_error("merge: unsupported clear stage");
+                    any = std::max(any, st.zlen);
+                }
+            // clear the whole merged slot when any problem clears its slot
+            m.zlen = any > 0 ? sc[m.zbuf - QCM_BUF_S0] : 0;
+        } else if (kind == ST_AXPY || kind == ST_GEMM) {
+            int64_t img_off = 0;
+            for (int32_t k = 0; k < n; ++k) {
+                if (si >= plans[k]->stages.size()) continue;
+                const Stage& st = plans[k]->stages[si];
+                const auto& b = base[k];
+                if (st.img.ares) throw std::runtime_error("merge: A-resident image tables are not supported");
+                const int64_t o0 = kind == ST_AXPY ? (int64_t)m.aout.size() : (int64_t)m.gout.size();
+                if (kind == ST_AXPY) {
+                    const int64_t t0 = (int64_t)m.aterm.size();
+                    for (AxpyOut o : st.aout) {
+                        o.dst_off += b[o.dst_buf];
+                        o.t_begin += t0;
+                        o.t_end += t0;
+                        m.aout.push_back(o);
+                    }
+                    for (AxpyTerm t : st.aterm) {
+                        t.src_off += b[t.src_buf];
+                        m.aterm.push_back(t);
+                    }
+                    if (st.comp_root.size() == st.aout.size())
+                        for (int32_t r : st.comp_root) m.comp_root.push_back(r + (int32_t)o0);
+                    if (st.heavy.size() == st.aout.size()) m.heavy.insert(m.heavy.end(), st.heavy.begin(), st.heavy.end());
+                    else m.heavy.insert(m.heavy.end(), st.aout.size(), 0);
+                } else {
+                    const int64_t g0 = (int64_t)m.gseg.size();
+                    for (GemmOut o : st.gout) {
+                        o.c_off += b[o.c_buf];
+                        o.s_begin += g0;
+                        o.s_end += g0;
+                        m.gout.push_back(o);
+                    }
+                    for (GemmSeg g : st.gseg) {
+                        g.a_off += b[g.a_buf];
+                        g.b_off += b[g.b_buf];
+                        m.gseg.push_back(g);
+                    }
+                }
+                // image tables
+                const ImgTables& it = st.img;
+                ImgTables& mt = m.img;
+                const int32_t p0 = (int32_t)mt.panels.size(), u0 = (int32_t)mt.outs.size();
+                const int32_t s0 = (int32_t)mt.segs.size();
+                const int64_t ci0 = (int64_t)mt.cimg.size();
+                for (ImgPanel pa : it.panels) {
+                    if (pa.kcontig == 2) {
+                        for (int32_t q = 0; q < pa.K; ++q) mt.gather.push_back(it.gather[pa.src_off + q] + b[pa.src_buf]);
+                        pa.src_off = (int64_t)mt.gather.size() - pa.K;
+                    } else {
+                        pa.src_off += b[pa.src_buf];
+                    }
+                    pa.img_off += img_off;
+                    mt.panels.push_back(pa);
+                }
+                for (size_t q = 0; q < it.build.size(); q += 2) {
+                    mt.build.push_back(it.build[q] + p0);
+                    mt.build.push_back(it.build[q + 1]);
+                }
+                for (ImgOut o : it.outs) {
+                    if (o.mode == 1) {
+                        for (int32_t j = 0; j < o.ncols; ++j) {
+                            mt.coltab.push_back(it.coltab[2 * (o.ctab + j)] + b[o.c_buf]);
+                            mt.coltab.push_back(it.coltab[2 * (o.ctab + j) + 1]);
+                        }
+                        o.ctab = (int64_t)mt.coltab.size() / 2 - o.ncols;
+                    } else {
+                        o.c_off += b[o.c_buf];
+                    }
+                    mt.outs.push_back(o);
+                }
+                for (ImgSeg sg : it.segs) {
+                    sg.a_img += img_off;
+                    sg.b_img += (sg.flags & IMG_B_CONST) ? ci0 : img_off;
+                    sg.a_panel += p0;
+                    mt.segs.push_back(sg);
+                }
+                for (ImgUnit u : it.units) {
+                    u.out += u0;
+                    u.s_begin += s0;
+                    u.s_end += s0;
+                    mt.units.push_back(u);
+                }
+                mt.cimg.insert(mt.cimg.end(), it.cimg.begin(), it.cimg.end());
+                img_off += it.bytes;
+            }
+            m.img.bytes = img_off;
+            P->image_bytes = std::max(P->image_bytes, img_off);
+            if (kind == ST_AXPY && m.comp_root.size() != m.aout.size()) m.comp_root.clear();
+        } else {
+            throw std::runtime_error("merge: unsupported stage kind");
+        }
+        P->stages.push_back(std::move(m));
+    }
+    return P;
+}
+
+int qcm_plan_merge(qcm_plan* const* plans, int32_t n, const int64_t* caller_off, qcm_plan** out) {
+    if (!out || !plans || !caller_off) { set_error("null argument"); return QCM_E_INVALID; }
+    try {
+        *out = merge_sigma_plans(plans, n, caller_off);
+        return QCM_OK;
+    } catch (const std::exception& e) {
+        set_error(std::string("qcm_plan_merge: ") + e.what());
+        *out = nullptr;
         return QCM_E_INVALID;
     }
 }

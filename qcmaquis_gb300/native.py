@@ -70,6 +70,7 @@ def lib():
     L.qcm_plan_boundary_tensor_mpo.argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks), C.POINTER(CBoundary),
                                                                       C.POINTER(CMpo), C.c_int32, C.c_int32,
                                                                       C.POINTER(C.c_void_p)]
+    L.qcm_plan_merge.argtypes = [C.POINTER(C.c_void_p), C.c_int32, i64p, C.POINTER(C.c_void_p)]
     L.qcm_plan_sizes.argtypes = [C.c_void_p, i64p, i64p]
     L.qcm_plan_image_bytes.argtypes = [C.c_void_p, i64p]
     L.qcm_plan_last_kernels.argtypes = [C.c_void_p, i32p]
@@ -482,6 +483,19 @@ def plan_energy_gradient(phys: Index, left_i: Index, right_i: Index, psi: Layout
     return Plan(h, "grad")
 
 
+def plan_merge(plans, caller_offsets) -> Plan:
+    """One plan for several sigma problems (``qcm_plan_merge``); ``caller_offsets`` is a
+    sequence of (KET, LEFT, RIGHT, OUT) element offsets, one per plan."""
+    n = len(plans)
+    arr = (C.c_void_p * n)(*[p.h for p in plans])
+    off = np.ascontiguousarray(np.array(caller_offsets, dtype=np.int64).reshape(n, 4))
+    h = C.c_void_p()
+    check(lib().qcm_plan_merge(arr, n, _p(off, i64p), C.byref(h)), "qcm_plan_merge")
+    p = Plan(h, "sigma")
+    p._parts = list(plans)
+    return p
+
+
 def plan_boundary_tensor_mpo(phys, left_i, right_i, mps: Layout, B: BoundaryLayout, mpo: FMpo, side: str,
                              hermitian=True) -> Plan:
     """``left_boundary_tensor_mpo`` (side "left") / ``right_boundary_tensor_mpo`` (side "right"):
@@ -497,5 +511,5 @@ def plan_boundary_tensor_mpo(phys, left_i, right_i, mps: Layout, B: BoundaryLayo
 
 
 __all__ = ["lib", "check", "Layout", "BoundaryLayout", "FMpo", "FIndex", "Plan", "plan_sigma",
-           "plan_boundary_left", "plan_boundary_right", "plan_boundary_tensor_mpo", "plan_energy_gradient", "PREC_FP64", "PREC_TF32",
+           "plan_boundary_left", "plan_boundary_right", "plan_boundary_tensor_mpo", "plan_energy_gradient", "plan_merge", "PREC_FP64", "PREC_TF32",
            "PREC_BF16X3"]
