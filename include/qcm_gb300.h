@@ -296,6 +296,14 @@ int qcm_multi_dot(const double* const* v_dev_ptrs, int32_t nvec, const double* y
 int qcm_multi_dot_noalloc(const double* const* v_dev_ptrs, int32_t nvec, const double* y, int64_t n,
                           double* out_dev, void* stream);
 
+/* Segmented dots for eigensolvers that run several problems in lockstep on
+ * concatenated vectors: out_dev[j * nseg + k] = sum over i in [seg_off[k],
+ * seg_off[k+1]) of V_j[i] * y[i], for j < nvec (<= 32) and k < nseg.  seg_off is a
+ * device array of nseg + 1 element offsets; v_dev_ptrs is a host array of device
+ * pointers.  Fixed reduction order; allocates nothing. */
+int qcm_seg_multi_dot(const double* const* v_dev_ptrs, int32_t nvec, const double* y, const int64_t* seg_off_dev,
+                      int32_t nseg, double* out_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -800,6 +800,21 @@ multi_dot_partial_byval(DotPtrs v, int nvec, const double* __restrict__ y, int64
     }
 }
 
+// Segmented dots for batched eigensolvers: out[j * nseg + k] = sum over segment k
+// ([seg[k], seg[k+1]) of the concatenated vectors) of V_j[i] * y[i]; one block per
+// (segment, vector), fixed reduction order.
+__global__ void __launch_bounds__(RED_THREADS)
+seg_multi_dot_kernel(DotPtrs v, const double* __restrict__ y, const int64_t* __restrict__ seg, int nseg,
+                     double* __restrict__ out) {
+    const int k = blockIdx.x, j = blockIdx.y;
+    const double* __restrict__ x = v.x[j];
+    const int64_t e = seg[k + 1];
+    double s = 0.0;
+    for (int64_t i = seg[k] + threadIdx.x; i < e; i += RED_THREADS) s = fma(x[i], y[i], s);
+    s = block_sum(s);
+    if (threadIdx.x == 0) out[(int64_t)j * nseg + k] = s;
+}
+
 // Device address of g_noalloc_partial per device, looked up once (set-up of the
 // first call on that device).
 static std::mutex g_noalloc_mu;
@@ -935,6 +950,26 @@ int qcm_multi_dot(const double* const* v, int32_t nvec, const double* y, int64_t
     multi_dot_partial<<<RED_BLOCKS, RED_THREADS, 0, s>>>(ws->ptrs, nvec, y, n, ws->partial);
     QCM_CUDA(cudaGetLastError());
     multi_dot_final<<<1, RED_THREADS, 0, s>>>(ws->partial, RED_BLOCKS, nvec, out, 0);
+    QCM_CUDA(cudaGetLastError());
+    return QCM_OK;
+}
+
+int qcm_seg_multi_dot(const double* const* v, int32_t nvec, const double* y, const int64_t* seg_off, int32_t nseg,
+                      double* out, void* stream) {
+    if (nvec < 0 || nvec > NOALLOC_MAX_VEC) {
+        set_error("qcm_seg_multi_dot: nvec " + std::to_string(nvec) + " out of range (at most " +
+                  std::to_string(NOALLOC_MAX_VEC) + ")");
+        return QCM_E_RANGE;
+    }
+    if (nseg < 0 || nseg > 65535) { set_error("qcm_seg_multi_dot: nseg out of range"); return QCM_E_RANGE; }
+    if (nvec == 0 || nseg == 0) return QCM_OK;
+    if (!v || !y || !seg_off || !out) { set_error("qcm_seg_multi_dot: null pointer"); return QCM_E_INVALID; }
+    DotPtrs args;
+    for (int k = 0; k < NOALLOC_MAX_VEC; ++k) args.x[k] = (k < nvec) ? v[k] : nullptr;
+    for (int k = 0; k < nvec; ++k)
+        if (!args.x[k]) { set_error("qcm_seg_multi_dot: null vector pointer"); return QCM_E_INVALID; }
+    seg_multi_dot_kernel<<<dim3((unsigned)nseg, (unsigned)nvec), RED_THREADS, 0, (cudaStream_t)stream>>>(
+        args, y, seg_off, nseg, out);
     QCM_CUDA(cudaGetLastError());
     return QCM_OK;
 }

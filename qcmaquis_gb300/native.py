@@ -102,6 +102,8 @@ def lib():
     L.qcm_device_status.argtypes = [C.POINTER(C.c_int32)]
     L.qcm_multi_dot_noalloc.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.c_void_p, C.c_int64, C.c_void_p,
                                         C.c_void_p]
+    L.qcm_seg_multi_dot.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                                    C.c_void_p, C.c_void_p]
     _lib = L
     return L
 
