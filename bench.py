@@ -384,10 +384,12 @@ def run_batch(args):
     from qcmaquis_gb300.engine import Engine, SiteProblem
     from qcmaquis_gb300.jd import solve_ietl_jcd
     from qcmaquis_gb300.workloads import build_sigma_host, upload_sigma_workload
+    from qcmaquis_gb300 import native as N
     nprob, L = 32, 12
     ms = np.random.default_rng(0).choice([64, 128, 256, 512], size=nprob)
     t0 = time.time()
-    eng = Engine("cuda:0")
+    prec = {"fp64": N.PREC_FP64, "tf32": N.PREC_TF32, "bf16x3": N.PREC_BF16X3}[args.precision]
+    eng = Engine("cuda:0", precision=prec)
     probs = []
     for k in range(nprob):
         w = upload_sigma_workload(build_sigma_host(L=L, nelec=L, m=int(ms[k]), seed=k + 1,
@@ -433,7 +435,7 @@ def run_batch(args):
     torch.cuda.synchronize()
     sig_s = e0.elapsed_time(e1) / reps
     line = {"metric": "batched Davidson solve s (32 independent L=12 N=12 S=0 SU2U1 problems)",
-            "value": t_batched, "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": "f64",
+            "value": t_batched, "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": args.precision,
             "data": "synthetic integrals (seeds 1..32), random MPS",
             "config": {"workload": "middle two-site problem of each of 32 systems, m drawn from {64,128,256,512}",
                        "m": [int(x) for x in ms], "tol": tol, "maxiter": maxiter},
