@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--no-images", action="store_true",
                     help="BF16x3: split operands inside the block-product kernel instead of pre-split images")
     ap.add_argument("--compare-steps", type=int, default=2, help="FP64 sigma calls timed for the comparison")
+    ap.add_argument("--autotune", action="store_true",
+                    help="time every sigma plan-shape candidate on the workload and report the choice")
     ap.add_argument("--batch", action="store_true",
                     help="32 independent L=12 problems: batched Davidson against separate solves")
     ap.add_argument("--adjoint", action="store_true",
@@ -446,6 +448,34 @@ def run_batch(args):
     print(json.dumps(line))
 
 
+def run_autotune(args):
+    """The plan-shape autotuner on the sigma workload: every candidate
+    (split_k_segs, dense_min_terms) timed, the choice against the defaults (32, 64)."""
+    import torch
+    from qcmaquis_gb300 import native as N
+    from qcmaquis_gb300.autotune import Autotuner, shape_key
+    from qcmaquis_gb300.engine import Engine
+    from qcmaquis_gb300.workloads import build_sigma_host, upload_sigma_workload
+    prec = {"fp64": N.PREC_FP64, "tf32": N.PREC_TF32, "bf16x3": N.PREC_BF16X3}[args.precision]
+    w = build_sigma_host(L=args.L, m=args.m, seed=1)
+    eng = Engine("cuda:0", precision=prec)
+    upload_sigma_workload(w, eng)
+    tuner = Autotuner(reps=5)
+    t0 = time.time()
+    sk, dm = tuner.choice(eng, w.psi, w.left, w.right, w.ts_mpo)
+    t_tune = time.time() - t0
+    key = shape_key(w.psi.layout, w.left.layout, w.right.layout, w.ts_mpo, prec)
+    ms = tuner.table[key]["ms"]
+    line = {"metric": f"autotuned sigma ms (L={args.L} N={args.L} S=0 SU2U1, m={args.m}, middle sites)",
+            "value": ms[f"{sk},{dm}"], "unit": "ms", "higher_is_better": False, "n_gpus": 1,
+            "dtype": args.precision, "data": "synthetic", "config": {"workload": "sigma vector, plan-shape autotuning",
+                                                                      "L": args.L, "m": args.m},
+            "choice": {"split_k_segs": sk, "dense_min_terms": dm}, "default_ms": ms["32,64"],
+            "speedup_vs_default": ms["32,64"] / ms[f"{sk},{dm}"], "candidates_ms": ms,
+            "plan_build_s": tuner.table[key]["plan_s"], "tuning_s": t_tune}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -456,6 +486,8 @@ def main():
         return run_adjoint(args)
     if args.batch:
         return run_batch(args)
+    if args.autotune:
+        return run_autotune(args)
     import numpy as np
     import torch
     from qcmaquis_gb300 import native as N

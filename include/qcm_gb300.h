@@ -138,6 +138,22 @@ int qcm_plan_sigma(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm
                    const qcm_blocks_t* psi, const qcm_boundary_t* left, const qcm_boundary_t* right,
                    const qcm_mpo_t* mpo, int32_t hermitian, qcm_plan** plan);
 
+/* Plan-shape options of a sigma plan (0 = default).  split_k_segs: the largest
+ * number of block products summed into one K3 output before it is split into
+ * partial tiles (default 32); dense_min_terms: the fewest K2 terms an output tile
+ * needs to join a dense tensor-core group (default 64).  Chosen per problem shape
+ * by the autotuner of the Python layer (qcmaquis_gb300/autotune.py). */
+typedef struct {
+    int32_t split_k_segs;
+    int32_t dense_min_terms;
+    int32_t reserved[6];
+} qcm_plan_opts_t;
+
+/* qcm_plan_sigma with plan-shape options (NULL: the defaults). */
+int qcm_plan_sigma_opts(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                        const qcm_blocks_t* psi, const qcm_boundary_t* left, const qcm_boundary_t* right,
+                        const qcm_mpo_t* mpo, int32_t hermitian, const qcm_plan_opts_t* opts, qcm_plan** plan);
+
 /* New left boundary L[i+1] from L[i], site tensor (bra = ket, left-paired) and W[i]. */
 int qcm_plan_boundary_left(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
                            const qcm_blocks_t* mps, const qcm_boundary_t* left, const qcm_mpo_t* mpo,

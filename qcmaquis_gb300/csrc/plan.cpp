@@ -771,7 +771,8 @@ static void add_zero_tiles(Stage& k2, const Stage& k3, int32_t buf) {
 }
 
 static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& right_i, const BM& psi,
-                             const std::vector<BM>& L, const std::vector<BM>& R, const MpoV& W, bool herm) {
+                             const std::vector<BM>& L, const std::vector<BM>& R, const MpoV& W, bool herm,
+                             int64_t split_k_segs = 32, int64_t dense_min_terms = 64) {
     auto* P = new qcm_plan();
     P->kind = PK_SIGMA;
     const qcm_mpo_t* m = W.m;
@@ -849,7 +850,7 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
     // split-K over the MPO bond sum: partial tiles in scratch 1 (T is dead after K2)
     Stage s4;
     int64_t part_end = 0;
-    split_k(s3, QCM_BUF_S1, 0, 32, s4, part_end);
+    split_k(s3, QCM_BUF_S1, 0, split_k_segs, s4, part_end);
     for (auto& a : s4.aout) P->axpy_bytes += 8.0 * a.rows * a.cols * (double)(a.t_end - a.t_begin + 1);
     P->scratch[0] = rp_end;
     P->scratch[1] = std::max(t_end, part_end);
@@ -859,7 +860,7 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
     build_image_tables(s1, s1.img);
     build_image_tables(s3, s3.img);
     axpy_components(s2, s2.comp_root);
-    build_dense_groups(s2, 64, s2.img, s2.heavy);
+    build_dense_groups(s2, dense_min_terms, s2.img, s2.heavy);
     P->image_bytes = std::max(std::max(s1.img.bytes, s3.img.bytes), s2.img.bytes);
     P->stages.push_back(std::move(z0));
     P->stages.push_back(std::move(s0));
@@ -1775,6 +1776,32 @@ int qcm_plan_sigma(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm
         return QCM_OK;
     } catch (const std::exception& e) {
         set_error(std::string("qcm_plan_sigma: ") + e.what());
+        *plan = nullptr;
+        return QCM_E_INVALID;
+    }
+}
+
+int qcm_plan_sigma_opts(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                        const qcm_blocks_t* psi, const qcm_boundary_t* left, const qcm_boundary_t* right,
+                        const qcm_mpo_t* mpo, int32_t hermitian, const qcm_plan_opts_t* opts, qcm_plan** plan) {
+    if (!plan) { set_error("null plan pointer"); return QCM_E_INVALID; }
+    int64_t sk = 32, dm = 64;
+    if (opts) {
+        if (opts->split_k_segs > 0) sk = opts->split_k_segs;
+        if (opts->dense_min_terms > 0) dm = opts->dense_min_terms;
+    }
+    if (sk < 2 || sk > (1 << 20) || dm < 8) {
+        set_error("qcm_plan_sigma_opts: split_k_segs must be in [2, 2^20], dense_min_terms >= 8");
+        *plan = nullptr;
+        return QCM_E_INVALID;
+    }
+    try {
+        MpoV W(mpo);
+        *plan = build_sigma(read_index(phys), read_index(left_i), read_index(right_i), read_blocks(psi),
+                            read_boundary(left), read_boundary(right), W, hermitian != 0, sk, dm);
+        return QCM_OK;
+    } catch (const std::exception& e) {
+        set_error(std::string("qcm_plan_sigma_opts: ") + e.what());
         *plan = nullptr;
         return QCM_E_INVALID;
     }

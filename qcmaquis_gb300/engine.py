@@ -142,6 +142,7 @@ class Engine:
         self.plan_seconds = 0.0   # host time spent building and uploading plans
         self._plans: Dict[tuple, N.Plan] = {}
         self.plan_cache_size = 2     # sigma plans kept (least recently used dropped first)
+        self.autotuner = None        # autotune.Autotuner: measured plan shapes per problem shape
         self.plan_hits = 0
         self._mpo_cache: Dict[int, N.FMpo] = {}
         self.launches = 0
@@ -167,9 +168,12 @@ class Engine:
             self._plans[key] = self._plans.pop(key)   # most recently used last
             self.plan_hits += 1
         if p is None:
+            sk = dm = 0
+            if self.autotuner is not None:
+                sk, dm = self.autotuner.choice(self, ket, L, R, mpo)
             t0 = time.time()
             p = N.plan_sigma(ket.phys_i, ket.left_i, ket.right_i, ket.layout, L.layout, R.layout, self.fmpo(mpo),
-                             self.hermitian)
+                             self.hermitian, split_k_segs=sk, dense_min_terms=dm)
             p.upload()
             self.plan_seconds += time.time() - t0
             p._keep = (mpo,)

@@ -70,6 +70,9 @@ def lib():
     L.qcm_plan_boundary_tensor_mpo.argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks), C.POINTER(CBoundary),
                                                                       C.POINTER(CMpo), C.c_int32, C.c_int32,
                                                                       C.POINTER(C.c_void_p)]
+    L.qcm_plan_sigma_opts.argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks), C.POINTER(CBoundary),
+                                                              C.POINTER(CBoundary), C.POINTER(CMpo), C.c_int32,
+                                                              C.c_void_p, C.POINTER(C.c_void_p)]
     L.qcm_plan_merge.argtypes = [C.POINTER(C.c_void_p), C.c_int32, i64p, C.POINTER(C.c_void_p)]
     L.qcm_plan_sizes.argtypes = [C.c_void_p, i64p, i64p]
     L.qcm_plan_image_bytes.argtypes = [C.c_void_p, i64p]
@@ -448,12 +451,24 @@ class Plan:
         return kinds
 
 
+class CPlanOpts(C.Structure):
+    _fields_ = [("split_k_segs", C.c_int32), ("dense_min_terms", C.c_int32), ("reserved", C.c_int32 * 6)]
+
+
 def plan_sigma(phys: Index, left_i: Index, right_i: Index, psi: Layout, L: BoundaryLayout, R: BoundaryLayout,
-               mpo: FMpo, hermitian: bool = True) -> Plan:
+               mpo: FMpo, hermitian: bool = True, split_k_segs: int = 0, dense_min_terms: int = 0) -> Plan:
+    """``qcm_plan_sigma`` (``qcm_plan_sigma_opts`` when a plan-shape option is given)."""
     fp, fl, fr = FIndex(phys), FIndex(left_i), FIndex(right_i)
     h = C.c_void_p()
-    check(lib().qcm_plan_sigma(C.byref(fp.c), C.byref(fl.c), C.byref(fr.c), C.byref(psi.c), C.byref(L.c),
-                               C.byref(R.c), C.byref(mpo.c), 1 if hermitian else 0, C.byref(h)), "qcm_plan_sigma")
+    if split_k_segs or dense_min_terms:
+        o = CPlanOpts(int(split_k_segs), int(dense_min_terms))
+        check(lib().qcm_plan_sigma_opts(C.byref(fp.c), C.byref(fl.c), C.byref(fr.c), C.byref(psi.c), C.byref(L.c),
+                                        C.byref(R.c), C.byref(mpo.c), 1 if hermitian else 0, C.byref(o),
+                                        C.byref(h)), "qcm_plan_sigma_opts")
+    else:
+        check(lib().qcm_plan_sigma(C.byref(fp.c), C.byref(fl.c), C.byref(fr.c), C.byref(psi.c), C.byref(L.c),
+                                   C.byref(R.c), C.byref(mpo.c), 1 if hermitian else 0, C.byref(h)),
+              "qcm_plan_sigma")
     return Plan(h, "sigma")
 
 

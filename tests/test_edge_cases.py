@@ -119,3 +119,46 @@ def test_plan_cache_key_is_the_layout_content():
     assert _digest(psi.phys_i, a) != _digest(psi.phys_i, N.Layout(a.keys, shapes))
     La, Lb = N.BoundaryLayout.of(left), N.BoundaryLayout.of(left)
     assert _digest(La) == _digest(Lb) != _digest(N.BoundaryLayout.of(right))
+
+
+def test_plan_shape_options_keep_sigma_and_change_the_plan():
+    """Plan-shape options (the autotuner's knobs) change the split-K and dense-group
+    tables, never the sigma; the shape key ignores block values and offsets."""
+    from qcmaquis_gb300.autotune import shape_key
+    psi, left, right, ts = _random_site_problem(L=6, N=6, m=24, site=2)
+    psi = psi.copy().make_left_paired()
+    lay, Ll, Rl = N.Layout.of(psi.data), N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
+    ref = lay.pack(R.site_hamil2(psi, left, right, ts).data)
+    outs = []
+    for sk, dm in [(0, 0), (2, 8), (4, 16)]:
+        p = N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, N.FMpo(ts), True,
+                         split_k_segs=sk, dense_min_terms=dm)
+        bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.full(p.out_elems, np.nan)] + \
+            [np.full(max(s, 1), np.nan) for s in p.scratch]
+        run_plan(p, bufs, images=True)
+        assert np.linalg.norm(bufs[3] - ref) <= 1e-7 * np.linalg.norm(ref)
+        st = p.stages()
+        outs.append((len(p.stage_images(4)["tiles"]), len(st[6][1]) if len(st) > 6 else 0))
+    # lower thresholds: more dense-group tiles and more split-K outputs
+    assert outs[1][0] > outs[0][0] and outs[1][1] > outs[0][1]
+    with pytest.raises(RuntimeError):
+        N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, N.FMpo(ts), True, split_k_segs=1)
+    assert shape_key(lay, Ll, Rl, ts, 2) == shape_key(N.Layout.of(psi.data), Ll, Rl, ts, 2)
+    assert shape_key(lay, Ll, Rl, ts, 2) != shape_key(lay, Ll, Rl, ts, 0)
+
+
+@pytest.mark.gpu
+def test_autotuned_engine_gives_the_same_sigma(tmp_path):
+    import torch
+    from qcmaquis_gb300.autotune import Autotuner
+    from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
+    psi, left, right, ts = _random_site_problem(L=6, N=6, m=24, site=2)
+    psi = psi.copy().make_left_paired()
+    x, Lb, Rb = DeviceMPSTensor.from_host(psi), DeviceBoundary.from_host(left), DeviceBoundary.from_host(right)
+    a = Engine("cuda:0", precision=N.PREC_BF16X3)
+    b = Engine("cuda:0", precision=N.PREC_BF16X3)
+    b.autotuner = Autotuner(path=str(tmp_path / "tune.json"), candidates=[(4, 16), (32, 64)], reps=2)
+    sa = a.site_hamil2(x, Lb, Rb, ts).data
+    sb = b.site_hamil2(x, Lb, Rb, ts).data
+    assert torch.linalg.norm(sa - sb).item() <= 1e-5 * torch.linalg.norm(sa).item()
+    assert len(Autotuner(path=str(tmp_path / "tune.json")).table) == 1
