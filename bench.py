@@ -33,7 +33,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="bf16x3", choices=["fp64", "tf32", "bf16x3"])
+    ap.add_argument("--precision", default="bf16x3", choices=["fp64", "tf32", "bf16x3", "bf16x2"])
     ap.add_argument("--sweep", action="store_true",
                     help="time one full two-site sweep (FP64 and BF16x3 sigma forms) instead of sigma calls")
     ap.add_argument("--jd-maxiter", type=int, default=10)
@@ -390,7 +390,7 @@ def run_batch(args):
     nprob, L = 32, 12
     ms = np.random.default_rng(0).choice([64, 128, 256, 512], size=nprob)
     t0 = time.time()
-    prec = {"fp64": N.PREC_FP64, "tf32": N.PREC_TF32, "bf16x3": N.PREC_BF16X3}[args.precision]
+    prec = {"fp64": N.PREC_FP64, "tf32": N.PREC_TF32, "bf16x3": N.PREC_BF16X3, "bf16x2": N.PREC_BF16X2}[args.precision]
     eng = Engine("cuda:0", precision=prec)
     probs = []
     for k in range(nprob):
@@ -456,7 +456,7 @@ def run_autotune(args):
     from qcmaquis_gb300.autotune import Autotuner, shape_key
     from qcmaquis_gb300.engine import Engine
     from qcmaquis_gb300.workloads import build_sigma_host, upload_sigma_workload
-    prec = {"fp64": N.PREC_FP64, "tf32": N.PREC_TF32, "bf16x3": N.PREC_BF16X3}[args.precision]
+    prec = {"fp64": N.PREC_FP64, "tf32": N.PREC_TF32, "bf16x3": N.PREC_BF16X3, "bf16x2": N.PREC_BF16X2}[args.precision]
     w = build_sigma_host(L=args.L, m=args.m, seed=1)
     eng = Engine("cuda:0", precision=prec)
     upload_sigma_workload(w, eng)
@@ -501,7 +501,7 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    prec = {"fp64": N.PREC_FP64, "tf32": N.PREC_TF32, "bf16x3": N.PREC_BF16X3}[args.precision]
+    prec = {"fp64": N.PREC_FP64, "tf32": N.PREC_TF32, "bf16x3": N.PREC_BF16X3, "bf16x2": N.PREC_BF16X2}[args.precision]
 
     t0 = time.time()
     w = build_sigma_host(L=args.L, m=args.m, seed=1 + rank * 0)
@@ -600,7 +600,7 @@ def main():
                 "peak_source": "cuBLAS FP64 DGEMM 4096^3 measured in this run (no FP64 entry in MEASURED_PEAKS.json)"}
     else:
         peak = peaks.get("bf16_tflops", 1900.0)
-        nprod = 6 if prec == N.PREC_BF16X3 else 1
+        nprod = 6 if prec == N.PREC_BF16X3 else (3 if prec == N.PREC_BF16X2 else 1)
         ach = plan.gemm_flops * nprod / gemm_t / 1e12
         traffic = captured_traffic(args.L, args.m) if (prec == N.PREC_BF16X3 and not args.no_images) else None
         roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
@@ -610,7 +610,8 @@ def main():
                 if traffic else None,
                 "traffic_gbs": traffic / gemm_t / 1e9 if traffic else None,
                 "kernel": ("tc_img_kernel + build_images_kernel (tcgen05 K1 + K3 block products from "
-                           "bulk-copied BF16 slice images)" if (prec == N.PREC_BF16X3 and not args.no_images)
+                           "bulk-copied BF16 slice images)" if (prec in (N.PREC_BF16X3, N.PREC_BF16X2)
+                                                                 and not args.no_images)
                            else "tc_gemm_kernel (tcgen05 K1 + K3 grouped block products)"),
                 "achieved_counts": f"{nprod} tensor-core products per FP64-equivalent product",
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"}
@@ -628,7 +629,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak" if world > 1 else "weak", "vs_baseline": None,
-        "dtype": {"fp64": "f64", "tf32": "tf32", "bf16x3": "bf16x3"}[args.precision],
+        "dtype": {"fp64": "f64", "tf32": "tf32", "bf16x3": "bf16x3", "bf16x2": "bf16x2"}[args.precision],
         "data": "synthetic (seeded integrals and random MPS; no dataset)",
         "config": {"workload": "sigma vector H_eff.psi, L=24 N=24 S=0 SU2U1, middle sites (11,12), m=1024",
                    **w.describe(), "precision": args.precision,

@@ -125,7 +125,9 @@ enum {
 enum {
     QCM_PREC_FP64 = 0,      /* all arithmetic FP64 */
     QCM_PREC_TF32 = 1,      /* tcgen05 kind::tf32 products, FP32 accumulation */
-    QCM_PREC_BF16X3 = 2     /* 3-slice BF16 split products, FP32 accumulation */
+    QCM_PREC_BF16X3 = 2,    /* 3-slice BF16 split products, FP32 accumulation */
+    QCM_PREC_BF16X2 = 3     /* the same images, the 3 products a_i b_j with i + j <= 1 (2-slice
+                               accuracy, half the tensor-core work); image slot required */
 };
 
 const char* qcm_last_error(void);

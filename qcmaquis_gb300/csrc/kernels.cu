@@ -601,6 +601,12 @@ static int upload_stage(Stage& st) {
     return QCM_OK;
 }
 
+// The image-executor forms: BF16x3 (6 slice products per K-step) and BF16x2 (3).
+static inline bool img_form(int precision) {
+    return precision == QCM_PREC_BF16X3 || precision == QCM_PREC_BF16X2;
+}
+static inline int img_products(int precision) { return precision == QCM_PREC_BF16X2 ? 3 : 6; }
+
 static int launch_axpy(const Stage& st, const BufTable& bt, int precision, cudaStream_t s) {
     if (st.n_work == 0) return QCM_OK;
     if (st.n_work > 0x7fffffffLL) { set_error("axpy work list too large"); return QCM_E_RANGE; }
@@ -614,8 +620,8 @@ static int launch_axpy(const Stage& st, const BufTable& bt, int precision, cudaS
         const bool src32 = (bt.f32mask >> st.src_buf) & 1u;
         const auto* CW = (const DevAxpyChunk*)st.d_cw;
         unsigned gc = (unsigned)st.n_cw;
-        if (precision == QCM_PREC_BF16X3 && bt.p[QCM_BUF_IMG] && st.d_iunit) {
-            // BF16x3 with images: the dense groups on the tensor cores (on the caller's
+        if (img_form(precision) && bt.p[QCM_BUF_IMG] && st.d_iunit) {
+            // BF16x3 / BF16x2 with images: the dense groups on the tensor cores (on the caller's
             // stream) and the gather of the other outputs on the stage's side stream,
             // forked from and joined back into the caller's stream (disjoint outputs)
             cudaStream_t ss = (cudaStream_t)st.side_stream;
@@ -629,7 +635,7 @@ static int launch_axpy(const Stage& st, const BufTable& bt, int precision, cudaS
                 else gather_axpy_contig<float, double><<<gl, CG_THREADS, 0, ss>>>(bt, O, T, LW);
                 QCM_CUDA(cudaGetLastError());
             }
-            int rc = tc_img_launch(st, bt.p, bt.f32mask, (void*)s);
+            int rc = tc_img_launch(st, bt.p, bt.f32mask, (void*)s, img_products(precision));
             if (fork) {
                 QCM_CUDA(cudaEventRecord((cudaEvent_t)st.ev_join, ss));
                 QCM_CUDA(cudaStreamWaitEvent(s, (cudaEvent_t)st.ev_join, 0));
@@ -667,8 +673,12 @@ static int launch_axpy(const Stage& st, const BufTable& bt, int precision, cudaS
 static int launch_gemm(const Stage& st, const BufTable& bt, int precision, cudaStream_t s) {
     if (st.n_work == 0) return QCM_OK;
     if (st.n_work > 0x7fffffffLL) { set_error("gemm work list too large"); return QCM_E_RANGE; }
-    if (precision == QCM_PREC_BF16X3 && bt.p[QCM_BUF_IMG] && st.d_iunit)
-        return tc_img_launch(st, bt.p, bt.f32mask, (void*)s);
+    if (img_form(precision) && bt.p[QCM_BUF_IMG] && st.d_iunit)
+        return tc_img_launch(st, bt.p, bt.f32mask, (void*)s, img_products(precision));
+    if (precision == QCM_PREC_BF16X2) {
+        set_error("the BF16x2 form runs on the image executor only: pass the operand-image slot");
+        return QCM_E_INVALID;
+    }
     if (precision != QCM_PREC_FP64)
         return tc_launch(st.d_a, st.d_b, st.d_tcw, st.n_tcw, bt.p, bt.f32mask, precision, (void*)s);
     if (bt.f32mask) { set_error("the FP64 form takes FP64 buffers only"); return QCM_E_INVALID; }
@@ -680,7 +690,7 @@ static int launch_gemm(const Stage& st, const BufTable& bt, int precision, cudaS
 
 // Kernels one stage launches on the path launch_axpy / launch_gemm take.
 static int stage_kernels(const Stage& st, const BufTable& bt, int precision) {
-    const bool images = precision == QCM_PREC_BF16X3 && bt.p[QCM_BUF_IMG] && st.d_iunit;
+    const bool images = img_form(precision) && bt.p[QCM_BUF_IMG] && st.d_iunit;
     if (st.kind == ST_AXPY) {
         if (st.n_work == 0) return 0;
         if (images && st.src_buf >= 0 && st.n_cw > 0)
@@ -904,7 +914,8 @@ int qcm_plan_run_typed(qcm_plan* p, double* const* bufs, uint32_t f32mask, int32
     int dev = 0;
     QCM_CUDA(cudaGetDevice(&dev));
     if (dev != p->device) { set_error("plan was uploaded to another device"); return QCM_E_STATE; }
-    if (precision != QCM_PREC_FP64 && precision != QCM_PREC_TF32 && precision != QCM_PREC_BF16X3) {
+    if (precision != QCM_PREC_FP64 && precision != QCM_PREC_TF32 && precision != QCM_PREC_BF16X3 &&
+        precision != QCM_PREC_BF16X2) {
         set_error("unknown precision");
         return QCM_E_INVALID;
     }

@@ -254,7 +254,7 @@ void set_coupling(int a, int b, int c, int d, int e, int f, int g, int h, int i,
 double conjugate_correction(int lc_spin, int rc_spin, int tensor_spin);
 void free_stage_device(Stage& st);
 int tc_build_work(const Stage& st, std::vector<int64_t>& w);
-int tc_img_launch(const Stage& st, double* const* bufs, uint32_t f32mask, void* stream);
+int tc_img_launch(const Stage& st, double* const* bufs, uint32_t f32mask, void* stream, int nprod = 6);
 int tc_launch(const void* d_out, const void* d_seg, const void* d_work, int64_t n_work, double* const* bufs,
               uint32_t f32mask, int precision, void* stream);
 }  // namespace qcm

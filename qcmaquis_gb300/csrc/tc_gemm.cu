@@ -428,6 +428,7 @@ struct TiArgs {
     double* p[QCM_NBUF];
     uint32_t f32mask;
     int32_t n_units;
+    int32_t nprod;            // slice products per K-step: 6 (BF16x3) or 3 (BF16x2)
 };
 
 __device__ __forceinline__ uint64_t global_ns() {
@@ -657,6 +658,7 @@ __device__ __forceinline__ void ti_store16(const TiArgs& a, const ImgOut& O, con
 }
 
 __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
+    const int nprod = a.nprod;
     extern __shared__ uint8_t ti_smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)ti_smem_raw + 1023) & ~(uintptr_t)1023);
     float* epi = (float*)(smem + TI_NS * TI_STAGE);
@@ -845,6 +847,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                         for (int kk = 0; kk < 2; ++kk) {
 #pragma unroll
                             for (int p = 0; p < 6; ++p) {
+                                if (p >= nprod) break;   // BF16x2 form: the slice pairs with i + j <= 1
                                 const int ia = p == 2 ? 1 : p == 4 ? 1 : p == 5 ? 2 : 0;
                                 const int ib = p == 1 ? 1 : p == 3 ? 2 : p == 4 ? 1 : 0;
                                 // start-address field (bits 0-13, address >> 4) advanced by the offset
@@ -889,6 +892,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                         for (int kk = 0; kk < 2; ++kk) {
 #pragma unroll
                             for (int p = 0; p < 6; ++p) {
+                                if (p >= nprod) break;   // BF16x2 form: the slice pairs with i + j <= 1
                                 const int ia = p == 2 ? 1 : p == 4 ? 1 : p == 5 ? 2 : 0;
                                 const int ib = p == 1 ? 1 : p == 3 ? 2 : p == 4 ? 1 : 0;
                                 // start-address field (bits 0-13, address >> 4) advanced by the offset
@@ -1048,7 +1052,8 @@ static int sm_count_of_current_device() {
     return cached[dev];
 }
 
-int tc_img_launch(const Stage& st, double* const* bufs, uint32_t f32mask, void* stream) {
+int tc_img_launch(const Stage& st, double* const* bufs, uint32_t f32mask, void* stream, int nprod) {
+    if (nprod != 3 && nprod != 6) { set_error("image executor: 3 or 6 slice products"); return QCM_E_INVALID; }
     cudaStream_t s = (cudaStream_t)stream;
     const ImgTables& t = st.img;
     if (t.units.empty()) return QCM_OK;
@@ -1075,6 +1080,7 @@ int tc_img_launch(const Stage& st, double* const* bufs, uint32_t f32mask, void* 
     for (int i = 0; i < QCM_NBUF; ++i) a.p[i] = bufs[i];
     a.f32mask = f32mask;
     a.n_units = (int32_t)t.units.size();
+    a.nprod = nprod;
     const int grid = (int)std::min<size_t>(t.units.size(), (size_t)sm_count_of_current_device());
     tc_img_kernel<<<grid, TI_THREADS, TI_SMEM, s>>>(a);
     e = cudaGetLastError();

@@ -187,7 +187,8 @@ class Engine:
         """Run a plan.  ``left`` / ``right`` are DeviceBoundary objects or raw FP64 tensors;
         the mixed forms read FP32 boundary shadows and keep every intermediate in FP32."""
         prec = self.precision if precision is None else precision
-        img_elems = (plan.image_bytes + 7) // 8 if (prec == N.PREC_BF16X3 and self.use_images) else 0
+        img_form = prec == N.PREC_BF16X3 or prec == N.PREC_BF16X2
+        img_elems = (plan.image_bytes + 7) // 8 if (img_form and (self.use_images or prec == N.PREC_BF16X2)) else 0
         s0, s1, s2, img = self.ws.get(list(plan.scratch) + [img_elems])
         mask = 0
         lt = left.data if isinstance(left, DeviceBoundary) else left

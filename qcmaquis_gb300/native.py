@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(HERE, "libqcm_gb300.so")
 
 QCM_BUF_KET, QCM_BUF_LEFT, QCM_BUF_RIGHT, QCM_BUF_OUT, QCM_BUF_S0, QCM_BUF_S1, QCM_BUF_S2, QCM_BUF_IMG = range(8)
 QCM_NBUF = 8
-PREC_FP64, PREC_TF32, PREC_BF16X3 = 0, 1, 2
+PREC_FP64, PREC_TF32, PREC_BF16X3, PREC_BF16X2 = 0, 1, 2, 3
 
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
@@ -528,5 +528,5 @@ def plan_boundary_tensor_mpo(phys, left_i, right_i, mps: Layout, B: BoundaryLayo
 
 
 __all__ = ["lib", "check", "Layout", "BoundaryLayout", "FMpo", "FIndex", "Plan", "plan_sigma",
-           "plan_boundary_left", "plan_boundary_right", "plan_boundary_tensor_mpo", "plan_energy_gradient", "plan_merge", "PREC_FP64", "PREC_TF32",
+           "plan_boundary_left", "plan_boundary_right", "plan_boundary_tensor_mpo", "plan_energy_gradient", "plan_merge", "PREC_BF16X2", "PREC_FP64", "PREC_TF32",
            "PREC_BF16X3"]

@@ -12,14 +12,15 @@ def _view(buf, off, ld, rows, cols):
     return np.lib.stride_tricks.as_strided(buf[off:], shape=(rows, cols), strides=(8, 8 * ld))
 
 
-def run_plan(plan, bufs, images=False):
-    """images=True runs the GEMM stages through the BF16x3 image-executor tables."""
+def run_plan(plan, bufs, images=False, nprod=6):
+    """images=True runs the GEMM stages through the BF16x3 image-executor tables
+    (nprod=3: the BF16x2 form's three slice products)."""
     for si, st in enumerate(plan.stages()):
         heavy = set()
         if images and st[0] in ("gemm", "axpy"):
             tab = plan.stage_images(si)
             if len(tab["tiles"]):
-                run_gemm_images(tab, bufs, plan.image_bytes)
+                run_gemm_images(tab, bufs, plan.image_bytes, nprod)
                 if st[0] == "gemm":
                     continue
                 heavy = set(int(x) for x in tab["coltab"][0::2])   # outputs the dense groups wrote
@@ -73,7 +74,7 @@ def _bf16_slots(raw):
 PAIRS = [(0, 0), (0, 1), (1, 0), (0, 2), (1, 1), (2, 0)]   # the six BF16 slice products
 
 
-def run_gemm_images(tab, bufs, image_bytes):
+def run_gemm_images(tab, bufs, image_bytes, nprod=6):
     """Execute the image-executor tables of one stage the way the kernels
     address them.  Per-call images are built with the FP64 value in slice 0
     and zero slices 1 and 2; constant images (coefficient matrices) hold the
@@ -129,7 +130,7 @@ def run_gemm_images(tab, bufs, image_bytes):
                 for sl in range(3):
                     A[sl, :ngA * 8] = img[slot(a_img, a_G, c, sl, m0 + ra, kk)]
                     B[sl, :ngB * 8] = bsrc[slot(b_img, b_G, c, sl, n0 + rb, kk)]
-                for ia, ib in PAIRS:
+                for ia, ib in PAIRS[:nprod]:
                     D += A[ia] @ B[ib].T
             acc += alpha[s] * D
         i = np.arange(128)[:, None]

@@ -162,3 +162,19 @@ def test_autotuned_engine_gives_the_same_sigma(tmp_path):
     sb = b.site_hamil2(x, Lb, Rb, ts).data
     assert torch.linalg.norm(sa - sb).item() <= 1e-5 * torch.linalg.norm(sa).item()
     assert len(Autotuner(path=str(tmp_path / "tune.json")).table) == 1
+
+
+@pytest.mark.gpu
+def test_bf16x2_form_on_gpu():
+    import torch
+    from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
+    psi, left, right, ts = _random_site_problem(L=6, N=6, m=24, site=2)
+    psi = psi.copy().make_left_paired()
+    ref = N.Layout.of(psi.data).pack(R.site_hamil2(psi, left, right, ts).data)
+    x, Lb, Rb = DeviceMPSTensor.from_host(psi), DeviceBoundary.from_host(left), DeviceBoundary.from_host(right)
+    err = {}
+    for prec in (N.PREC_BF16X2, N.PREC_BF16X3):
+        got = Engine("cuda:0", precision=prec).site_hamil2(x, Lb, Rb, ts).data.cpu().numpy()
+        err[prec] = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    # the three products with i + j <= 1: two-slice accuracy, looser than BF16x3
+    assert err[N.PREC_BF16X2] < 1e-4 and err[N.PREC_BF16X2] > err[N.PREC_BF16X3]
