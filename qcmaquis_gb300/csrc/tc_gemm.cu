@@ -659,6 +659,7 @@ __device__ __forceinline__ void ti_store16(const TiArgs& a, const ImgOut& O, con
 
 __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
     const int nprod = a.nprod;
+    const int nsl = nprod == 3 ? 2 : 3;   // image slices the products read (BF16x2: slices 0 and 1)
     extern __shared__ uint8_t ti_smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)ti_smem_raw + 1023) & ~(uintptr_t)1023);
     float* epi = (float*)(smem + TI_NS * TI_STAGE);
@@ -746,10 +747,9 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                         key_m0 = U.m0;
                         const uint32_t bA = (uint32_t)min(16, S.a_G - gA0) * 512u;
                         const uint32_t fa = smem_u32(&bar_ares_full);
-                        mbar_expect_tx(fa, 3u * bA * (uint32_t)S.kc);
+                        mbar_expect_tx(fa, (uint32_t)nsl * bA * (uint32_t)S.kc);
                         for (int c = 0; c < S.kc; ++c)
-#pragma unroll
-                            for (int sl = 0; sl < 3; ++sl)
+                            for (int sl = 0; sl < nsl; ++sl)
                                 bulk_g2s(smem_u32(ares_base + c * TI_ACHUNK + sl * TI_SLICE),
                                          a.img + S.a_img + ((int64_t)(c * 3 + sl) * S.a_G + gA0) * 512, bA, fa);
                     }
@@ -759,9 +759,8 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                         const uint32_t st = it % (uint32_t)TI_NSB, ph = (it / (uint32_t)TI_NSB) & 1u;
                         if (!ti_wait(smem_u32(&bar_empty[st]), ph ^ 1u, abort_flag)) { ok = false; break; }
                         const uint32_t fb = smem_u32(&bar_full[st]);
-                        mbar_expect_tx(fb, 3u * bB);
-#pragma unroll
-                        for (int sl = 0; sl < 3; ++sl)
+                        mbar_expect_tx(fb, (uint32_t)nsl * bB);
+                        for (int sl = 0; sl < nsl; ++sl)
                             bulk_g2s(smem_u32(bst_base + st * TI_ACHUNK + sl * TI_SLICE),
                                      bbase + S.b_img + ((int64_t)(c * 3 + sl) * S.b_G + gB0) * 512, bB, fb);
                     }
@@ -790,10 +789,9 @@ __global__ void __launch_bounds__(TI_THREADS, 1) tc_img_kernel(TiArgs a) {
                         const uint32_t st = it % (uint32_t)TI_NS, ph = (it / (uint32_t)TI_NS) & 1u;
                         if (!ti_wait(smem_u32(&bar_empty[st]), ph ^ 1u, abort_flag)) { ok = false; break; }
                         const uint32_t fb = smem_u32(&bar_full[st]);
-                        mbar_expect_tx(fb, 3u * (bA + bB));
+                        mbar_expect_tx(fb, (uint32_t)nsl * (bA + bB));
                         const uint32_t dst = smem_u32(smem + st * TI_STAGE);
-#pragma unroll
-                        for (int sl = 0; sl < 3; ++sl) {
+                        for (int sl = 0; sl < nsl; ++sl) {
                             bulk_g2s(dst + sl * TI_SLICE,
                                      a.img + S.a_img + ((int64_t)(c * 3 + sl) * S.a_G + gA0) * 512, bA, fb);
                             bulk_g2s(dst + (3 + sl) * TI_SLICE,
