@@ -102,7 +102,8 @@ struct TcCfg<QCM_PREC_BF16X3> {
 // the FP64 pipe of this part is far narrower than the FP32 one, and three BF16
 // slices carry the 24 bits an FP32 value has.
 template <int PREC>
-__device__ __forceinline__ void put_vec(uint8_t* base, uint32_t off, uint32_t slice_bytes, const float* v) {
+__device__ __forceinline__ void put_vec(uint8_t* base, uint32_t off, uint32_t slice_bytes, const float* v,
+                                        int nsl = 3) {
     if constexpr (PREC == QCM_PREC_TF32) {
         uint4 q;
         q.x = to_tf32(v[0]); q.y = to_tf32(v[1]); q.z = to_tf32(v[2]); q.w = to_tf32(v[3]);
@@ -127,7 +128,8 @@ __device__ __forceinline__ void put_vec(uint8_t* base, uint32_t off, uint32_t sl
         }
         *reinterpret_cast<uint4*>(base + off) = make_uint4(s0[0], s0[1], s0[2], s0[3]);
         *reinterpret_cast<uint4*>(base + slice_bytes + off) = make_uint4(s1[0], s1[1], s1[2], s1[3]);
-        *reinterpret_cast<uint4*>(base + 2 * slice_bytes + off) = make_uint4(s2[0], s2[1], s2[2], s2[3]);
+        if (nsl > 2)   // the BF16x2 form reads slices 0 and 1 only
+            *reinterpret_cast<uint4*>(base + 2 * slice_bytes + off) = make_uint4(s2[0], s2[1], s2[2], s2[3]);
     }
 }
 
@@ -495,7 +497,7 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
 // one 16-byte vector per slice.
 __global__ void __launch_bounds__(256)
 build_images_kernel(const ImgPanel* __restrict__ panels, const int32_t* __restrict__ items,
-                    const int64_t* __restrict__ gather, uint8_t* __restrict__ img, TcBufs bufs) {
+                    const int64_t* __restrict__ gather, uint8_t* __restrict__ img, TcBufs bufs, int nsl) {
     const ImgPanel P = panels[items[2 * blockIdx.x]];
     const int c = items[2 * blockIdx.x + 1];
     const bool f32 = (bufs.f32mask >> P.src_buf) & 1u;
@@ -525,7 +527,7 @@ build_images_kernel(const ImgPanel* __restrict__ panels, const int32_t* __restri
             }
             v[j] = x;
         }
-        put_vec<QCM_PREC_BF16X3>(base + (size_t)g * 512, 0, sstride, v);
+        put_vec<QCM_PREC_BF16X3>(base + (size_t)g * 512, 0, sstride, v, nsl);
     }
 }
 
@@ -1063,7 +1065,8 @@ int tc_img_launch(const Stage& st, double* const* bufs, uint32_t f32mask, void* 
     const size_t n_build = t.build.size() / 2;
     if (n_build > 0)
         build_images_kernel<<<(unsigned)n_build, 256, 0, s>>>((const ImgPanel*)st.d_ipanel, (const int32_t*)st.d_ibuild,
-                                                              (const int64_t*)st.d_igather, img, tb);
+                                                              (const int64_t*)st.d_igather, img, tb,
+                                                              nprod == 3 ? 2 : 3);
     cudaError_t e = cudaFuncSetAttribute(tc_img_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TI_SMEM);
     if (e != cudaSuccess) { set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e)); return QCM_E_CUDA; }
     TiArgs a;
