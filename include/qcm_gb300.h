@@ -181,6 +181,17 @@ int qcm_plan_boundary_tensor_mpo(const qcm_index_t* phys, const qcm_index_t* lef
                                  const qcm_blocks_t* mps, const qcm_boundary_t* boundary, const qcm_mpo_t* mpo,
                                  int32_t side, int32_t hermitian, qcm_plan** plan);
 
+/* Zero-site problem (ZeroSiteProblem::apply, dmrg/framework/dmrg/mp_tensors/
+ * zerositeproblem.h:40-42 -> zerosite_hamil_lbtm_kernel, dmrg/framework/dmrg/
+ * mp_tensors/contractions/non-abelian/zero_site_hamil.hpp:44-79): sigma =
+ * H_eff C for the bond matrix C between sites i and i+1 (block diagonal in the
+ * bond's charges), with left = L[i+1], right = R[i+1], mpo_left = W[i] (its
+ * columns are the bond) and mpo_right = W[i+1] (its rows are the bond).  sigma
+ * has C's layout; the plan's KET buffer is C.  hermitian != 0 uses the bond's
+ * Hermitian partners, without phases, as the reference does. */
+int qcm_plan_zerosite(const qcm_blocks_t* bond, const qcm_boundary_t* left, const qcm_boundary_t* right,
+                      const qcm_mpo_t* mpo_left, const qcm_mpo_t* mpo_right, int32_t hermitian, qcm_plan** plan);
+
 /* Gradient of the local energy E = <psi| H_eff psi> (the contraction of
  * qcm_plan_sigma, same arguments) with respect to every term scale of the MPO
  * tensor: OUT[t] = dE/d term_scale[t], t indexing the flattened term arrays of

@@ -662,6 +662,34 @@ def site_hamil2(ket: MPSTensor, left, right, mpo, is_hermitian=True, force=None)
     return site_hamil_rbtm(ket, left, right, mpo, is_hermitian)
 
 
+def zerosite_hamil(bond: BlockMatrix, left: List[BlockMatrix], right: List[BlockMatrix], mpo_left, mpo_right,
+                   is_hermitian=True) -> BlockMatrix:
+    """``zerosite_hamil_lbtm_kernel`` (``ct/non-abelian/zero_site_hamil.hpp:44-79``), bra = ket.
+
+    ``bond`` is the bond matrix C between sites i and i+1, ``left`` = L[i+1],
+    ``right`` = R[i+1], ``mpo_left`` = W[i], ``mpo_right`` = W[i+1].  For every bond
+    index b: T[b] = L[b]^T C (``BoundaryMPSProduct`` over C with
+    ``correctConjugate = false``: a Hermitian partner enters as L[conj b] with no
+    phase), then sigma += T[b] R[b] (``gemm_trim`` with unit scales; a partner as
+    R[conj b]^T, again with no phase).  The skip test is W[i+1]'s left one, the
+    right partner index W[i]'s right one, as in the reference."""
+    ref = bond.left_basis()
+    hr, hl = mpo_right.herm, mpo_left.herm
+    out = BlockMatrix()
+    for b in range(mpo_right.row_dim):
+        conj = is_hermitian and hr.left_skip(b)
+        if conj:
+            T = gemm_trim_left(left[hr.left_conj(b)], bond, ref)
+            Radj = right[hl.right_conj(b)].transpose()
+            tmp = gemm_trim(T, Radj, [1.0] * Radj.n_blocks(), False)
+        else:
+            T = gemm_trim_left(left[b].transpose(), bond, ref)
+            tmp = gemm_trim(T, right[b], [1.0] * T.n_blocks(), True)
+        for k in range(tmp.n_blocks()):
+            out.match_and_add_block(tmp.blocks[k], *tmp.keys[k])
+    return out
+
+
 # --------------------------------------------------------------------------- boundary steps
 def overlap_mpo_left_step(bra: MPSTensor, ket: MPSTensor, left: List[BlockMatrix], mpo,
                           is_hermitian=True) -> List[BlockMatrix]:

@@ -388,8 +388,12 @@ static BM plan_reshape_l2r(const Idx& phys, const Idx& left_i, const Idx& right_
 }
 
 // K1: T[b1] = A(b1) . rp (BoundaryMPSProduct with gemm_trim_left).
+// phases = false: the Hermitian partner L[conj(b1)] is used without the SU(2)
+// conjugate correction and bond phase (BoundaryMPSProduct with
+// correctConjugate = false, as the zero-site problem builds it).
 static std::vector<BM> plan_k1(const std::vector<BM>& L, const MpoV& W, bool herm, const BM& rp, int rp_buf,
-                               const Idx& ref, int t_buf, Stage& st, qcm_plan* P, int64_t& end) {
+                               const Idx& ref, int t_buf, Stage& st, qcm_plan* P, int64_t& end,
+                               bool phases = true) {
     std::vector<BM> T(L.size());
     struct Job { int b1; Q a, l; int64_t a_off, lda; int ta; double scale; int64_t M, K; size_t rpk; };
     std::vector<Job> jobs;
@@ -399,7 +403,8 @@ static std::vector<BM> plan_k1(const std::vector<BM>& L, const MpoV& W, bool her
         if (use_conj) {
             const BM& src = L[W.lconj((int)b1)];
             for (auto& x : src.b) {
-                double sc = conjugate_correction(x.lc.s, x.rc.s, W.lspin((int)b1)) * W.lphase((int)b1);
+                double sc = phases ? conjugate_correction(x.lc.s, x.rc.s, W.lspin((int)b1)) * W.lphase((int)b1)
+                                   : 1.0;
                 Ab.push_back({(int)b1, x.lc, x.rc, x.off, x.rows, 0, sc, x.rows, x.cols, 0});
             }
         } else {
@@ -867,6 +872,90 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
     P->stages.push_back(std::move(s1));
     P->stages.push_back(std::move(z2));
     P->stages.push_back(std::move(s2));
+    P->stages.push_back(std::move(s3));
+    if (!s4.aout.empty()) P->stages.push_back(std::move(s4));
+    return P;
+}
+
+// Zero-site problem (zerosite_hamil_lbtm_kernel, ct/non-abelian/zero_site_hamil.hpp:44-79):
+// the bond matrix C between two sites, the left boundary L and the right boundary R
+// of that bond, the MPO tensors either side of it (Wl: its columns are the bond,
+// Wr: its rows are the bond).  sigma(al,al) = sum_b op(L[b])^T C (al,ar) . R'[b](ar,al)
+// with, for the bonds Wr marks as Hermitian partners, L[conj b] and R[conj b]^T in
+// place of L[b]^T and R[b], both without phases (the reference passes
+// correctConjugate = false and unit scales).  Stages: K1 (T[b] = op(L[b]) C into
+// S1), K3 (sigma into OUT, split-K partials in S0), the split-K sum.
+static qcm_plan* build_zerosite(const BM& bond, const std::vector<BM>& L, const std::vector<BM>& R,
+                                const MpoV& Wl, const MpoV& Wr, bool herm, int64_t split_k_segs = 32) {
+    auto* P = new qcm_plan();
+    P->kind = PK_SIGMA;
+    const int nb = Wr.m->row_dim;
+    if (Wl.m->col_dim != nb) throw std::runtime_error("MPO tensors do not share the bond");
+    if ((int)L.size() != nb || (int)R.size() != nb)
+        throw std::runtime_error("boundary aux dimensions do not match the bond");
+    int64_t c_end = 0;
+    for (auto& b : bond.b) {
+        if (!(b.lc == b.rc)) throw std::runtime_error("bond matrix is not block diagonal");
+        c_end = std::max(c_end, b.off + b.rows * b.cols);
+    }
+    P->out_elems = c_end;
+    Idx ref;
+    for (auto& b : bond.b) ref.d.push_back({b.lc, b.rows});
+    Stage s1; int64_t t_end = 0;
+    std::vector<BM> T = plan_k1(L, Wr, herm, bond, QCM_BUF_KET, ref, QCM_BUF_S1, s1, P, t_end, false);
+    Stage s3; s3.kind = ST_GEMM;
+    for (auto& ob : bond.b) {
+        Q al = ob.lc;
+        GemmOut o;
+        o.c_buf = QCM_BUF_OUT;
+        o.c_off = ob.off;
+        o.ldc = ob.rows;
+        o.M = ob.rows;
+        o.N = ob.cols;
+        o.s_begin = (int64_t)s3.gseg.size();
+        for (int b = 0; b < nb; ++b) {
+            const BM& tb = T[b];
+            size_t it = tb.left_lower_bound(al);
+            for (; it < tb.b.size() && tb.b[it].lc == al; ++it) {
+                const Blk& a = tb.b[it];
+                Q ar = a.rc;
+                GemmSeg g;
+                g.a_buf = QCM_BUF_S1; g.ta = 0; g.a_off = a.off; g.lda = a.rows; g.K = a.cols;
+                g.alpha = 1.0;
+                if (herm && Wr.lskip(b)) {
+                    const BM& rs = R[Wl.rconj(b)];
+                    size_t k = rs.find(al, ar);
+                    if (k == rs.b.size()) continue;
+                    g.b_buf = QCM_BUF_RIGHT; g.tb = 1; g.b_off = rs.b[k].off; g.ldb = rs.b[k].rows;
+                    if (rs.b[k].cols != a.cols || rs.b[k].rows != ob.cols)
+                        throw std::runtime_error("zero-site dimension mismatch (adjoint)");
+                } else {
+                    const BM& rs = R[b];
+                    size_t k = rs.find(ar, al);
+                    if (k == rs.b.size()) continue;
+                    g.b_buf = QCM_BUF_RIGHT; g.tb = 0; g.b_off = rs.b[k].off; g.ldb = rs.b[k].rows;
+                    if (rs.b[k].rows != a.cols || rs.b[k].cols != ob.cols)
+                        throw std::runtime_error("zero-site dimension mismatch");
+                }
+                if (a.rows != ob.rows) throw std::runtime_error("zero-site row mismatch");
+                s3.gseg.push_back(g);
+                P->gemm_flops += 2.0 * ob.rows * ob.cols * a.cols;
+            }
+        }
+        o.s_end = (int64_t)s3.gseg.size();
+        s3.gout.push_back(o);
+    }
+    Stage s4;
+    int64_t part_end = 0;
+    split_k(s3, QCM_BUF_S0, 0, split_k_segs, s4, part_end);
+    for (auto& a : s4.aout) P->axpy_bytes += 8.0 * a.rows * a.cols * (double)(a.t_end - a.t_begin + 1);
+    P->scratch[0] = part_end;
+    P->scratch[1] = t_end;
+    P->scratch[2] = 0;
+    build_image_tables(s1, s1.img);
+    build_image_tables(s3, s3.img);
+    P->image_bytes = std::max(s1.img.bytes, s3.img.bytes);
+    P->stages.push_back(std::move(s1));
     P->stages.push_back(std::move(s3));
     if (!s4.aout.empty()) P->stages.push_back(std::move(s4));
     return P;
@@ -1818,6 +1907,20 @@ int qcm_plan_boundary_left(const qcm_index_t* phys, const qcm_index_t* left_i, c
         return QCM_OK;
     } catch (const std::exception& e) {
         set_error(std::string("qcm_plan_boundary_left: ") + e.what());
+        *plan = nullptr;
+        return QCM_E_INVALID;
+    }
+}
+
+int qcm_plan_zerosite(const qcm_blocks_t* bond, const qcm_boundary_t* left, const qcm_boundary_t* right,
+                      const qcm_mpo_t* mpo_left, const qcm_mpo_t* mpo_right, int32_t hermitian, qcm_plan** plan) {
+    if (!plan) { set_error("null plan pointer"); return QCM_E_INVALID; }
+    try {
+        MpoV Wl(mpo_left), Wr(mpo_right);
+        *plan = build_zerosite(read_blocks(bond), read_boundary(left), read_boundary(right), Wl, Wr, hermitian != 0);
+        return QCM_OK;
+    } catch (const std::exception& e) {
+        set_error(std::string("qcm_plan_zerosite: ") + e.what());
         *plan = nullptr;
         return QCM_E_INVALID;
     }

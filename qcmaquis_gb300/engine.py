@@ -55,6 +55,28 @@ class DeviceMPSTensor:
 
 
 @dataclass
+class DeviceBlockMatrix:
+    """A block matrix (the bond matrix of a zero-site problem) in one device arena."""
+    layout: N.Layout
+    data: torch.Tensor  # float64, flat
+
+    @classmethod
+    def from_host(cls, bm, device="cuda"):
+        lay = N.Layout.of(bm)
+        return cls(lay, torch.from_numpy(lay.pack(bm)).to(device))
+
+    def to_host(self):
+        return self.layout.unpack(self.data.detach().cpu().numpy())
+
+    def like(self, data: torch.Tensor) -> "DeviceBlockMatrix":
+        return DeviceBlockMatrix(self.layout, data)
+
+    @property
+    def n(self) -> int:
+        return int(self.data.numel())
+
+
+@dataclass
 class DeviceBoundary:
     """A boundary (one block matrix per MPO bond index) in one device arena."""
     layout: N.BoundaryLayout
@@ -216,6 +238,31 @@ class Engine:
         self.run(p, ket=ket.data, left=L, right=R, out=out, precision=precision)
         return ket.like(out)
 
+    def zerosite_hamil2(self, bond: DeviceBlockMatrix, L: DeviceBoundary, R: DeviceBoundary, mpo_left, mpo_right,
+                        out: Optional[torch.Tensor] = None, precision=None) -> DeviceBlockMatrix:
+        """sigma = H_eff C for the bond matrix C between sites i and i+1
+        (``Engine::zerosite_hamil2``, ``non-abelian/zero_site_hamil.hpp:36-79``);
+        L = L[i+1], R = R[i+1], mpo_left = W[i], mpo_right = W[i+1]."""
+        key = ("z", _digest(bond.layout), _digest(L.layout), _digest(R.layout), id(mpo_left), id(mpo_right),
+               self.hermitian)
+        p = self._plans.get(key)
+        if p is None:
+            t0 = time.time()
+            p = N.plan_zerosite(bond.layout, L.layout, R.layout, self.fmpo(mpo_left), self.fmpo(mpo_right),
+                                self.hermitian)
+            p.upload()
+            self.plan_seconds += time.time() - t0
+            p._keep = (mpo_left, mpo_right)
+            while self._plans and len(self._plans) >= max(1, self.plan_cache_size):
+                self._plans.pop(next(iter(self._plans)))
+            self._plans[key] = p
+        else:
+            self.plan_hits += 1
+        if out is None:
+            out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=self.device)
+        self.run(p, ket=bond.data, left=L, right=R, out=out, precision=precision)
+        return bond.like(out)
+
     def overlap_mpo_left_step(self, mps: DeviceMPSTensor, L: DeviceBoundary, mpo,
                               precision: int = N.PREC_FP64) -> DeviceBoundary:
         """L[i+1] from L[i], A[i], W[i] (``Engine::overlap_mpo_left_step``, bra = ket).
@@ -277,4 +324,26 @@ class SiteProblem:
         return self.engine.site_hamil2(x, self.left, self.right, self.mpo, out=out)
 
 
-__all__ = ["Engine", "SiteProblem", "DeviceMPSTensor", "DeviceBoundary"]
+class ZeroSiteProblem:
+    """``ZeroSiteProblem{mpo_left, mpo_right, left, right}`` (``mp_tensors/zerositeproblem.h:25-56``):
+    ``apply`` = ``zerosite_hamil2``, ``get_energy`` = <x|H x> / <x|x>."""
+
+    def __init__(self, engine: Engine, mpo_left, mpo_right, left: DeviceBoundary, right: DeviceBoundary):
+        self.engine = engine
+        self.mpo_left = mpo_left
+        self.mpo_right = mpo_right
+        self.left = left
+        self.right = right
+
+    def apply(self, x: DeviceBlockMatrix, out: Optional[torch.Tensor] = None) -> DeviceBlockMatrix:
+        return self.engine.zerosite_hamil2(x, self.left, self.right, self.mpo_left, self.mpo_right, out=out)
+
+    def get_energy(self, x: DeviceBlockMatrix) -> float:
+        from .jd import VecOps
+        ops = getattr(self, "_ops", None) or VecOps(self.engine.device)
+        self._ops = ops
+        y = self.apply(x)
+        return ops.dot(x.data, y.data) / ops.dot(x.data, x.data)
+
+
+__all__ = ["Engine", "SiteProblem", "ZeroSiteProblem", "DeviceMPSTensor", "DeviceBlockMatrix", "DeviceBoundary"]

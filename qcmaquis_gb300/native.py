@@ -73,6 +73,8 @@ def lib():
     L.qcm_plan_sigma_opts.argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks), C.POINTER(CBoundary),
                                                               C.POINTER(CBoundary), C.POINTER(CMpo), C.c_int32,
                                                               C.c_void_p, C.POINTER(C.c_void_p)]
+    L.qcm_plan_zerosite.argtypes = [C.POINTER(CBlocks), C.POINTER(CBoundary), C.POINTER(CBoundary),
+                                    C.POINTER(CMpo), C.POINTER(CMpo), C.c_int32, C.POINTER(C.c_void_p)]
     L.qcm_plan_merge.argtypes = [C.POINTER(C.c_void_p), C.c_int32, i64p, C.POINTER(C.c_void_p)]
     L.qcm_plan_sizes.argtypes = [C.c_void_p, i64p, i64p]
     L.qcm_plan_image_bytes.argtypes = [C.c_void_p, i64p]
@@ -527,6 +529,16 @@ def plan_boundary_tensor_mpo(phys, left_i, right_i, mps: Layout, B: BoundaryLayo
     return Plan(h, "btm_" + side)
 
 
+def plan_zerosite(bond: Layout, L: BoundaryLayout, R: BoundaryLayout, mpo_left: FMpo, mpo_right: FMpo,
+                  hermitian=True) -> Plan:
+    """``zerosite_hamil2``: sigma = H_eff C for the bond matrix C (layout ``bond``), the
+    boundaries L = L[i+1], R = R[i+1] of that bond and the MPO tensors W[i], W[i+1]."""
+    h = C.c_void_p()
+    check(lib().qcm_plan_zerosite(C.byref(bond.c), C.byref(L.c), C.byref(R.c), C.byref(mpo_left.c),
+                                  C.byref(mpo_right.c), 1 if hermitian else 0, C.byref(h)), "qcm_plan_zerosite")
+    return Plan(h, "sigma")
+
+
 __all__ = ["lib", "check", "Layout", "BoundaryLayout", "FMpo", "FIndex", "Plan", "plan_sigma",
-           "plan_boundary_left", "plan_boundary_right", "plan_boundary_tensor_mpo", "plan_energy_gradient", "plan_merge", "PREC_BF16X2", "PREC_FP64", "PREC_TF32",
-           "PREC_BF16X3"]
+           "plan_boundary_left", "plan_boundary_right", "plan_boundary_tensor_mpo", "plan_energy_gradient",
+           "plan_merge", "plan_zerosite", "PREC_BF16X2", "PREC_FP64", "PREC_TF32", "PREC_BF16X3"]

@@ -15,7 +15,7 @@ from qcmaquis_gb300.mpo import make_mpo
 from oracle import dmrg_ref as R
 from oracle.sweep import SweepParams, initial_state
 from plan_interp import run_plan
-from test_oracle import _random_site_problem
+from test_oracle import _random_site_problem, _zero_site_problem
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -144,6 +144,30 @@ def test_boundary_plans_match_oracle_layout_and_values(herm):
         assert [g.keys for g in got] == [r.keys for r in ref]
         assert np.allclose(ol.pack(ref), bufs[3][:ol.size], rtol=0, atol=1e-13)
         right = ref
+
+
+@pytest.mark.parametrize("herm", [True, False])
+@pytest.mark.parametrize("bond", [0, 2, 4])
+@pytest.mark.parametrize("images", [False, True])
+def test_zero_site_plan_matches_oracle(herm, bond, images):
+    """qcm_plan_zerosite against the oracle's zerosite_hamil; images=True runs the
+    BF16x3 image tables (FP64 values in slice 0)."""
+    _, Cm, left, right, mpo = _zero_site_problem(bond=bond, herm=herm)
+    lay, Ll, Rl = N.Layout.of(Cm), N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
+    p = N.plan_zerosite(lay, Ll, Rl, N.FMpo(mpo[bond]), N.FMpo(mpo[bond + 1]), herm)
+    assert [st[0] for st in p.stages()][:2] == ["gemm", "gemm"]
+    bufs = [lay.pack(Cm), Ll.pack(left), Rl.pack(right), np.full(p.out_elems, np.nan)] + \
+        [np.full(max(s, 1), np.nan) for s in p.scratch]
+    run_plan(p, bufs, images=images)
+    ref = lay.pack(R.zerosite_hamil(Cm, left, right, mpo[bond], mpo[bond + 1], is_hermitian=herm))
+    assert np.linalg.norm(bufs[3] - ref) <= (1e-7 if images else 1e-13) * np.linalg.norm(ref)
+
+
+def test_zero_site_plan_rejects_mismatched_bond():
+    _, Cm, left, right, mpo = _zero_site_problem(bond=2)
+    lay, Ll, Rl = N.Layout.of(Cm), N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
+    with pytest.raises(RuntimeError, match="qcm_plan_zerosite"):
+        N.plan_zerosite(lay, Ll, Rl, N.FMpo(mpo[1]), N.FMpo(mpo[3]))
 
 
 def test_plan_work_counters_match_oracle():

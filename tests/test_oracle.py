@@ -124,3 +124,58 @@ def test_single_site_sweeps_reach_exact_diagonalisation():
     rec, _ = run_dmrg_single_site(model, make_mpo(model), OP(nsweeps=5, max_bond_dimension=64,
                                                              alpha_main=0.0, alpha_final=0.0), nelec=N)
     assert abs(rec.sweep_energy[-1] - fci_energies(L, ints, N, 0, 1)[0]) < 1e-9
+
+
+def _zero_site_problem(L=6, N=6, seed=3, m=16, bond=2, herm=True):
+    """State, bond matrix C between sites ``bond`` and ``bond + 1``, L[bond+1], R[bond+1]
+    and the MPO, as ``test_siteproblem.cpp:97-154`` prepares them: the sites left of
+    the bond left-normalised, C the R factor of the QR of site ``bond``."""
+    ints = synthetic_integral_map(L, seed=seed)
+    model = QCModel(L, ints, N)
+    mpo = make_mpo(model)
+    mps = initial_state(model, mpo, SweepParams(init_bond_dimension=m, seed=11), N, 0)
+    full = [t.copy() for t in mps]
+    left = R.left_boundary(mps[0])
+    for i in range(bond):
+        t = R.left_normalize_and_return(mps[i])
+        R.multiply_from_left(mps[i + 1], t)
+        left = R.overlap_mpo_left_step(mps[i], mps[i], left, mpo[i], is_hermitian=herm)
+    C = R.left_normalize_and_return(mps[bond])
+    left = R.overlap_mpo_left_step(mps[bond], mps[bond], left, mpo[bond], is_hermitian=herm)
+    right = R.right_boundary(mps[L - 1])
+    for i in range(L - 1, bond, -1):
+        right = R.overlap_mpo_right_step(mps[i], mps[i], right, mpo[i], is_hermitian=herm)
+    return full, C, left, right, mpo
+
+
+def _bm_dot(a, b) -> float:
+    s = 0.0
+    for key, blk in zip(a.keys, a.blocks):
+        k = b.find_block(*key)
+        if k < b.n_blocks():
+            s += float(np.sum(blk * b.blocks[k]))
+    return s
+
+
+@pytest.mark.parametrize("herm", [True, False])
+@pytest.mark.parametrize("bond", [0, 2, 4])
+def test_zero_site_energy_equals_expval(herm, bond):
+    """``test_siteproblem.cpp:97-154``: <C|H_0 C> / <C|C> is the energy of the state."""
+    from oracle.sweep import expval, overlap
+    full, C, left, right, mpo = _zero_site_problem(bond=bond, herm=herm)
+    sig = R.zerosite_hamil(C, left, right, mpo[bond], mpo[bond + 1], is_hermitian=herm)
+    e0 = _bm_dot(C, sig) / _bm_dot(C, C)
+    e = expval(full, mpo) / overlap(full)
+    assert abs(e0 - e) < 1e-10 * max(1.0, abs(e))
+
+
+def test_zero_site_hermitian_partners_match_full_boundary():
+    """The zero-site sigma with Hermitian partners (no phases, as the reference
+    contracts them) equals the one over all bond indices."""
+    _, C, left, right, mpo = _zero_site_problem(bond=2, herm=True)
+    _, C2, left2, right2, _ = _zero_site_problem(bond=2, herm=False)
+    a = R.zerosite_hamil(C, left, right, mpo[2], mpo[3], is_hermitian=True)
+    b = R.zerosite_hamil(C2, left2, right2, mpo[2], mpo[3], is_hermitian=False)
+    assert a.keys == b.keys
+    diff = max(float(np.abs(x - y).max()) for x, y in zip(a.blocks, b.blocks))
+    assert diff <= 1e-12 * a.norm()
