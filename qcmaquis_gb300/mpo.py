@@ -396,10 +396,15 @@ def make_mpo(model: QCModel) -> MPO:
 
 
 def make_twosite_mpo(mpo1: MPOTensor, mpo2: MPOTensor, phys1: Index, phys2: Index) -> MPOTensor:
-    """Two-site MPO tensor W(b1,b3) = sum_b2 W1(b1,b2) (x) W2(b2,b3) per operator spin."""
+    """Two-site MPO tensor W(b1,b3) = sum_b2 W1(b1,b2) (x) W2(b2,b3) per operator spin
+    (``make_twosite_mpo``, ``mp_tensors/ts_ops.h:78-152``).  The spin-coupled
+    Kronecker product depends only on the two operators and the three bond spins,
+    so each distinct (op1, op2, spins, product spin) is formed once and reused
+    scaled; the sums are those of the reference, term for term."""
     assert mpo1.col_dim == mpo2.row_dim
     table: List[SiteOperator] = []
     prempo = []
+    kron: Dict[tuple, SiteOperator] = {}
     for b1 in range(mpo1.row_dim):
         row1 = mpo1.row(b1)
         for b3 in range(mpo2.col_dim):
@@ -415,10 +420,15 @@ def make_twosite_mpo(mpo1: MPOTensor, mpo2: MPOTensor, phys1: Index, phys2: Inde
                         spins = allowed_spins(mpo1.left_spin(b1).get(), mpo2.right_spin(b3).get(),
                                               op1.spin.get(), op2.spin.get())
                         for s in spins:
-                            prod_spin = SpinDescriptor(s, mpo1.left_spin(b1).get(), mpo2.right_spin(b3).get())
-                            prod = op_kron_su2(phys1, phys2, op1, op2, mpo1.left_spin(b1), mpo1.right_spin(b2),
-                                               mpo2.right_spin(b3), prod_spin)
-                            prod.remove_empty_blocks()
+                            key = (tag1, tag2, mpo1.left_spin(b1).get(), mpo1.right_spin(b2).get(),
+                                   mpo2.right_spin(b3).get(), s)
+                            prod = kron.get(key)
+                            if prod is None:
+                                prod_spin = SpinDescriptor(s, mpo1.left_spin(b1).get(), mpo2.right_spin(b3).get())
+                                prod = op_kron_su2(phys1, phys2, op1, op2, mpo1.left_spin(b1),
+                                                   mpo1.right_spin(b2), mpo2.right_spin(b3), prod_spin)
+                                prod.remove_empty_blocks()
+                                kron[key] = prod
                             prod = prod.scaled(s1 * s2)
                             if s not in ret:
                                 ret[s] = SiteOperator()
