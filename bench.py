@@ -209,14 +209,15 @@ def run_sweep(args):
     from qcmaquis_gb300.engine import DeviceMPSTensor
     from qcmaquis_gb300.integrals import synthetic_integral_map
     from qcmaquis_gb300.model import QCModel
-    from qcmaquis_gb300.mpo import make_mpo, make_ts_cache_mpo
+    from qcmaquis_gb300.mpo import make_mpo
+    from qcmaquis_gb300.native import make_ts_cache_fmpo
     from qcmaquis_gb300.mps import bond_indices, right_canonical_chain
     from qcmaquis_gb300.sweep import SweepParams, run_dmrg
     L, nelec = args.L, args.L
     t0 = time.time()
     model = QCModel(L, synthetic_integral_map(L, seed=1, diag_range=(-3.0, -0.3)), nelec)
     mpo = make_mpo(model)
-    ts = make_ts_cache_mpo(mpo, model.phys, workers=os.cpu_count() or 1)
+    ts = make_ts_cache_fmpo(mpo, model.phys)
     bonds = bond_indices(L, model.phys, (nelec, 0), args.m)
     sites, _ = right_canonical_chain(model.phys, bonds, L, 0, np.random.default_rng(7))
     setup = time.time() - t0
@@ -293,7 +294,8 @@ def run_adjoint(args):
     from qcmaquis_gb300.gradient import energy_gradient
     from qcmaquis_gb300.integrals import synthetic_integral_map
     from qcmaquis_gb300.model import QCModel
-    from qcmaquis_gb300.mpo import make_mpo, make_ts_cache_mpo
+    from qcmaquis_gb300.mpo import make_mpo
+    from qcmaquis_gb300.native import make_ts_cache_fmpo
     from qcmaquis_gb300.mps import bond_indices, right_canonical_chain
     from qcmaquis_gb300.sweep import SweepParams, expval, overlap, run_dmrg
     L = 16 if args.L == 24 else args.L
@@ -303,7 +305,7 @@ def run_adjoint(args):
     ints = synthetic_integral_map(L, seed=4, diag_range=(-2.0, -0.5))
     model = QCModel(L, ints, nelec)
     mpo = make_mpo(model)
-    ts = make_ts_cache_mpo(mpo, model.phys, workers=os.cpu_count() or 1)
+    ts = make_ts_cache_fmpo(mpo, model.phys)
     bonds = bond_indices(L, model.phys, (nelec, 0), m)
     sites, _ = right_canonical_chain(model.phys, bonds, L, 0, np.random.default_rng(7))
     mps = [DeviceMPSTensor.from_host(t) for t in sites]

@@ -181,6 +181,30 @@ int qcm_plan_boundary_tensor_mpo(const qcm_index_t* phys, const qcm_index_t* lef
                                  const qcm_blocks_t* mps, const qcm_boundary_t* boundary, const qcm_mpo_t* mpo,
                                  int32_t side, int32_t hermitian, qcm_plan** plan);
 
+/* Two-site MPO tensor on the host (make_twosite_mpo, dmrg/framework/dmrg/
+ * mp_tensors/ts_ops.h:78-152): W(b1,b3) = sum_b2 W1(b1,b2) (x) W2(b2,b3), one
+ * operator per allowed product spin s, flattened as qcm_mpo_t.  Three steps:
+ * qcm_mpo_twosite_begin walks the non-zero (b1, b2, b3) chains and returns the
+ * number of distinct spin-coupled Kronecker products they need;
+ * qcm_mpo_twosite_keys lists them, 6 int32 each: (operator of W1, operator of
+ * W2, spin of b1, spin of b2, spin of b3, s); the caller forms each product
+ * (SU(2) op_kron, site_operator_algorithms.h) and passes them, in key order, as
+ * the operators of a qcm_mpo_t -- n_ops, op_spin, op_blk_ptr, blk_q, blk_ent_ptr,
+ * ent, ent_coeff; the other fields are not read -- to qcm_mpo_twosite_finish,
+ * which sums the scaled products of every (b1, b3, s) in the reference's order.
+ * qcm_mpo_buf_view points a qcm_mpo_t at the result (valid until
+ * qcm_mpo_buf_destroy); sizes[4] = elements, terms, operator blocks, entries.
+ * Terms are listed element by element, column-major; an element's operators
+ * with s descending; qcm_mpo_buf_term_pos gives each term's position in its
+ * element.  Every term has scale 1 and its own operator. */
+typedef struct qcm_mpo_buf qcm_mpo_buf;
+int qcm_mpo_twosite_begin(const qcm_mpo_t* w1, const qcm_mpo_t* w2, qcm_mpo_buf** out, int32_t* n_keys);
+int qcm_mpo_twosite_keys(const qcm_mpo_buf* buf, int32_t* keys);
+int qcm_mpo_twosite_finish(qcm_mpo_buf* buf, const qcm_mpo_t* products);
+int qcm_mpo_buf_view(const qcm_mpo_buf* buf, qcm_mpo_t* view, int64_t* sizes);
+int qcm_mpo_buf_term_pos(const qcm_mpo_buf* buf, int32_t* pos);
+void qcm_mpo_buf_destroy(qcm_mpo_buf* buf);
+
 /* Zero-site problem (ZeroSiteProblem::apply, dmrg/framework/dmrg/mp_tensors/
  * zerositeproblem.h:40-42 -> zerosite_hamil_lbtm_kernel, dmrg/framework/dmrg/
  * mp_tensors/contractions/non-abelian/zero_site_hamil.hpp:44-79): sigma =

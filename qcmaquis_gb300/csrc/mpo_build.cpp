@@ -1,0 +1,302 @@
+// Two-site MPO tensors on the host, in native code (make_twosite_mpo,
+// dmrg/framework/dmrg/mp_tensors/ts_ops.h:78-152).
+//
+// W(b1,b3) = sum over b2 of W1(b1,b2) (x) W2(b2,b3), one operator per product
+// spin s allowed by the bond spins (ts_ops.h:21-35).  The spin-coupled
+// Kronecker product of two site operators depends only on the two operators,
+// the three bond spins and s, so a tensor needs few distinct products: phase 1
+// walks the non-zero (b1, b2, b3) chains and lists them, the caller forms each
+// once (the SU(2) op_kron), and phase 2 sums the scaled products of every
+// (b1, b3, s) in the reference's order and writes the flattened tensor
+// (qcm_mpo_t layout) that the plan builders read.
+#include <algorithm>
+#include <array>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "plan.hpp"
+
+using qcm::Q;
+using qcm::set_error;
+
+struct qcm_mpo_buf {
+    int32_t row_dim = 0, col_dim = 0;
+    std::vector<int32_t> left_spin, right_spin, left_herm, right_herm, left_phase, right_phase;
+    // phase 1: distinct products (op1, op2, j, jpp, jp, s) and, per output operator
+    // in the reference's table order (b1, b3 ascending, s ascending), its summands
+    std::vector<int32_t> keys;
+    struct Out { int32_t b1, b3, s; int64_t sb, se; };
+    std::vector<Out> outs;
+    std::vector<int32_t> sum_prod;
+    std::vector<double> sum_coeff;
+    // phase 2: the flattened tensor
+    bool built = false;
+    std::vector<int32_t> col_ptr, row_of, term_ptr, term_op, op_spin, op_blk_ptr, blk_q, blk_ent_ptr, ent, term_pos;
+    std::vector<double> term_scale, ent_coeff;
+};
+
+namespace {
+
+struct KeyHash {
+    size_t operator()(const std::array<int32_t, 6>& k) const {
+        uint64_t h = 1469598103934665603ull;
+        for (int32_t x : k) { h ^= (uint32_t)x; h *= 1099511628211ull; }
+        return (size_t)h;
+    }
+};
+
+void check_mpo(const qcm_mpo_t* w, const char* what) {
+    if (!w) throw std::runtime_error(std::string("null ") + what);
+    if (w->row_dim < 0 || w->col_dim < 0 || !w->col_ptr || !w->term_ptr || !w->left_spin || !w->right_spin)
+        throw std::runtime_error(std::string("malformed ") + what);
+    int64_t ne = w->col_ptr[w->col_dim];
+    for (int64_t e = 0; e < ne; ++e) {
+        if (w->row_of[e] < 0 || w->row_of[e] >= w->row_dim) throw std::runtime_error("mpo row index out of range");
+        for (int t = w->term_ptr[e]; t < w->term_ptr[e + 1]; ++t)
+            if (w->term_op[t] < 0 || w->term_op[t] >= w->n_ops) throw std::runtime_error("mpo operator out of range");
+    }
+}
+
+// rows of a CSC tensor: b1 -> [(b2, element)], b2 ascending
+std::vector<std::vector<std::pair<int32_t, int32_t>>> rows_of(const qcm_mpo_t* w) {
+    std::vector<std::vector<std::pair<int32_t, int32_t>>> r(w->row_dim);
+    for (int b2 = 0; b2 < w->col_dim; ++b2)
+        for (int e = w->col_ptr[b2]; e < w->col_ptr[b2 + 1]; ++e) r[w->row_of[e]].push_back({b2, e});
+    return r;
+}
+
+void phase1(qcm_mpo_buf& B, const qcm_mpo_t* w1, const qcm_mpo_t* w2) {
+    if (w1->col_dim != w2->row_dim) throw std::runtime_error("the MPO tensors do not share a bond");
+    B.row_dim = w1->row_dim;
+    B.col_dim = w2->col_dim;
+    B.left_spin.assign(w1->left_spin, w1->left_spin + w1->row_dim);
+    B.right_spin.assign(w2->right_spin, w2->right_spin + w2->col_dim);
+    auto copy_or_identity = [](const int32_t* p, int n, bool herm) {
+        std::vector<int32_t> v(n);
+        for (int i = 0; i < n; ++i) v[i] = p ? p[i] : (herm ? i : 1);
+        return v;
+    };
+    B.left_herm = copy_or_identity(w1->left_herm, w1->row_dim, true);
+    B.left_phase = copy_or_identity(w1->left_phase, w1->row_dim, false);
+    B.right_herm = copy_or_identity(w2->right_herm, w2->col_dim, true);
+    B.right_phase = copy_or_identity(w2->right_phase, w2->col_dim, false);
+    auto rows1 = rows_of(w1);
+    auto rows2 = rows_of(w2);
+    std::unordered_map<std::array<int32_t, 6>, int32_t, KeyHash> kid;
+    // b3 -> [(b2, element of W1, element of W2)] for the current b1
+    std::vector<std::vector<std::array<int32_t, 3>>> chains(w2->col_dim);
+    std::vector<int32_t> touched;
+    struct Acc { std::vector<int32_t> prod; std::vector<double> coeff; };
+    std::map<int, Acc> per_s;
+    for (int b1 = 0; b1 < w1->row_dim; ++b1) {
+        touched.clear();
+        for (auto& [b2, e1] : rows1[b1])
+            for (auto& [b3, e2] : rows2[b2]) {
+                if (chains[b3].empty()) touched.push_back(b3);
+                chains[b3].push_back({b2, e1, e2});
+            }
+        std::sort(touched.begin(), touched.end());
+        const int j = w1->left_spin[b1];
+        for (int b3 : touched) {
+            const int jp = w2->right_spin[b3];
+            per_s.clear();
+            for (auto& ch : chains[b3]) {
+                const int jpp = w1->right_spin[ch[0]];
+                for (int t1 = w1->term_ptr[ch[1]]; t1 < w1->term_ptr[ch[1] + 1]; ++t1) {
+                    const int o1 = w1->term_op[t1], k1 = w1->op_spin[o1];
+                    for (int t2 = w2->term_ptr[ch[2]]; t2 < w2->term_ptr[ch[2] + 1]; ++t2) {
+                        const int o2 = w2->term_op[t2], k2 = w2->op_spin[o2];
+                        for (int s = std::abs(k1 - k2); s <= std::abs(k1 + k2); s += 2) {
+                            if (!(std::abs(s - j) <= jp && jp <= std::abs(s + j))) continue;
+                            std::array<int32_t, 6> key{o1, o2, j, jpp, jp, s};
+                            auto it = kid.find(key);
+                            if (it == kid.end()) {
+                                it = kid.emplace(key, (int32_t)(B.keys.size() / 6)).first;
+                                B.keys.insert(B.keys.end(), key.begin(), key.end());
+                            }
+                            Acc& a = per_s[s];
+                            a.prod.push_back(it->second);
+                            a.coeff.push_back(w1->term_scale[t1] * w2->term_scale[t2]);
+                        }
+                    }
+                }
+            }
+            for (auto& [s, a] : per_s) {
+                qcm_mpo_buf::Out o{b1, b3, s, (int64_t)B.sum_prod.size(), 0};
+                B.sum_prod.insert(B.sum_prod.end(), a.prod.begin(), a.prod.end());
+                B.sum_coeff.insert(B.sum_coeff.end(), a.coeff.begin(), a.coeff.end());
+                o.se = (int64_t)B.sum_prod.size();
+                B.outs.push_back(o);
+            }
+            chains[b3].clear();
+        }
+    }
+}
+
+struct Entry { int32_t r, c, rs, cs; double v; };
+struct Block { Q lc, rc; std::vector<Entry> e; };
+
+void phase2(qcm_mpo_buf& B, const qcm_mpo_t* prods) {
+    const int64_t nkeys = (int64_t)B.keys.size() / 6;
+    if (!prods || prods->n_ops != nkeys || !prods->op_blk_ptr || !prods->blk_q || !prods->blk_ent_ptr)
+        throw std::runtime_error("one product operator per listed key expected");
+    // the output operators, grouped per element (b1, b3) in column-major order;
+    // an element lists its operators with s descending (later table entries first)
+    std::vector<int64_t> order(B.outs.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int64_t)i;
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+        const auto &x = B.outs[a], &y = B.outs[b];
+        if (x.b3 != y.b3) return x.b3 < y.b3;
+        return x.b1 < y.b1;
+    });
+    B.col_ptr.assign(1, 0);
+    B.term_ptr.assign(1, 0);
+    B.op_blk_ptr.assign(1, 0);
+    B.blk_ent_ptr.assign(1, 0);
+    std::vector<Block> blocks;
+    size_t i = 0;
+    for (int b3 = 0; b3 < B.col_dim; ++b3) {
+        while (i < order.size() && B.outs[order[i]].b3 == b3) {
+            size_t k = i;
+            const int b1 = B.outs[order[i]].b1;
+            while (k < order.size() && B.outs[order[k]].b3 == b3 && B.outs[order[k]].b1 == b1) ++k;
+            B.row_of.push_back(b1);
+            for (size_t q = k; q-- > i;) {   // s descending
+                const auto& o = B.outs[order[q]];
+                B.term_pos.push_back((int32_t)(k - 1 - q));
+                B.term_op.push_back((int32_t)B.op_spin.size());
+                B.term_scale.push_back(1.0);
+                B.op_spin.push_back(o.s);
+                // sum of the scaled products, summand by summand, entry by entry
+                blocks.clear();
+                for (int64_t t = o.sb; t < o.se; ++t) {
+                    const int p = B.sum_prod[t];
+                    const double c = B.sum_coeff[t];
+                    for (int kb = prods->op_blk_ptr[p]; kb < prods->op_blk_ptr[p + 1]; ++kb) {
+                        Q lc(prods->blk_q[4 * kb], prods->blk_q[4 * kb + 1]);
+                        Q rc(prods->blk_q[4 * kb + 2], prods->blk_q[4 * kb + 3]);
+                        Block* bl = nullptr;
+                        for (auto& x : blocks)
+                            if (x.lc == lc && x.rc == rc) { bl = &x; break; }
+                        if (!bl) { blocks.push_back({lc, rc, {}}); bl = &blocks.back(); }
+                        for (int en = prods->blk_ent_ptr[kb]; en < prods->blk_ent_ptr[kb + 1]; ++en) {
+                            const int32_t* x = prods->ent + 4 * en;
+                            const double v = prods->ent_coeff[en] * c;
+                            Entry* hit = nullptr;
+                            for (auto& y : bl->e)
+                                if (y.r == x[0] && y.c == x[1]) { hit = &y; break; }
+                            if (hit) hit->v = hit->v + v;
+                            else bl->e.push_back({x[0], x[1], x[2], x[3], v});
+                        }
+                    }
+                }
+                std::sort(blocks.begin(), blocks.end(), [](const Block& a, const Block& b) {
+                    return a.lc > b.lc || (a.lc == b.lc && a.rc > b.rc);
+                });
+                for (auto& bl : blocks) {
+                    B.blk_q.insert(B.blk_q.end(), {bl.lc.n, bl.lc.s, bl.rc.n, bl.rc.s});
+                    std::sort(bl.e.begin(), bl.e.end(), [](const Entry& a, const Entry& b) {
+                        return a.r < b.r || (a.r == b.r && a.c < b.c);
+                    });
+                    for (auto& y : bl.e) {
+                        if (y.v == 0.0) continue;
+                        B.ent.insert(B.ent.end(), {y.r, y.c, y.rs, y.cs});
+                        B.ent_coeff.push_back(y.v);
+                    }
+                    B.blk_ent_ptr.push_back((int32_t)B.ent_coeff.size());
+                }
+                B.op_blk_ptr.push_back((int32_t)B.blk_ent_ptr.size() - 1);
+            }
+            B.term_ptr.push_back((int32_t)B.term_op.size());
+            i = k;
+        }
+        B.col_ptr.push_back((int32_t)B.row_of.size());
+    }
+    if (B.ent_coeff.size() > (size_t)INT32_MAX || B.term_op.size() > (size_t)INT32_MAX)
+        throw std::runtime_error("two-site tensor too large for 32-bit offsets");
+    B.built = true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qcm_mpo_twosite_begin(const qcm_mpo_t* w1, const qcm_mpo_t* w2, qcm_mpo_buf** out, int32_t* n_keys) {
+    if (!out || !n_keys) { set_error("qcm_mpo_twosite_begin: null output"); return QCM_E_INVALID; }
+    *out = nullptr;
+    auto* B = new qcm_mpo_buf();
+    try {
+        check_mpo(w1, "left MPO tensor");
+        check_mpo(w2, "right MPO tensor");
+        phase1(*B, w1, w2);
+        *n_keys = (int32_t)(B->keys.size() / 6);
+        *out = B;
+        return QCM_OK;
+    } catch (const std::exception& e) {
+        delete B;
+        set_error(std::string("qcm_mpo_twosite_begin: ") + e.what());
+        return QCM_E_INVALID;
+    }
+}
+
+int qcm_mpo_twosite_keys(const qcm_mpo_buf* B, int32_t* keys) {
+    if (!B || !keys) { set_error("qcm_mpo_twosite_keys: null argument"); return QCM_E_INVALID; }
+    std::memcpy(keys, B->keys.data(), B->keys.size() * sizeof(int32_t));
+    return QCM_OK;
+}
+
+int qcm_mpo_twosite_finish(qcm_mpo_buf* B, const qcm_mpo_t* products) {
+    if (!B) { set_error("qcm_mpo_twosite_finish: null handle"); return QCM_E_INVALID; }
+    try {
+        phase2(*B, products);
+        return QCM_OK;
+    } catch (const std::exception& e) {
+        set_error(std::string("qcm_mpo_twosite_finish: ") + e.what());
+        return QCM_E_INVALID;
+    }
+}
+
+int qcm_mpo_buf_view(const qcm_mpo_buf* B, qcm_mpo_t* view, int64_t* sizes) {
+    if (!B || !view || !sizes) { set_error("qcm_mpo_buf_view: null argument"); return QCM_E_INVALID; }
+    if (!B->built) { set_error("qcm_mpo_buf_view: tensor not built (qcm_mpo_twosite_finish)"); return QCM_E_INVALID; }
+    view->row_dim = B->row_dim;
+    view->col_dim = B->col_dim;
+    view->left_spin = B->left_spin.data();
+    view->right_spin = B->right_spin.data();
+    view->left_herm = B->left_herm.data();
+    view->right_herm = B->right_herm.data();
+    view->left_phase = B->left_phase.data();
+    view->right_phase = B->right_phase.data();
+    view->col_ptr = B->col_ptr.data();
+    view->row_of = B->row_of.data();
+    view->term_ptr = B->term_ptr.data();
+    view->term_op = B->term_op.data();
+    view->term_scale = B->term_scale.data();
+    view->n_ops = (int32_t)B->op_spin.size();
+    view->op_spin = B->op_spin.data();
+    view->op_blk_ptr = B->op_blk_ptr.data();
+    view->blk_q = B->blk_q.data();
+    view->blk_ent_ptr = B->blk_ent_ptr.data();
+    view->ent = B->ent.data();
+    view->ent_coeff = B->ent_coeff.data();
+    sizes[0] = (int64_t)B->row_of.size();        // elements
+    sizes[1] = (int64_t)B->term_op.size();       // terms (= operators)
+    sizes[2] = (int64_t)B->blk_q.size() / 4;     // operator blocks
+    sizes[3] = (int64_t)B->ent_coeff.size();     // entries
+    return QCM_OK;
+}
+
+int qcm_mpo_buf_term_pos(const qcm_mpo_buf* B, int32_t* pos) {
+    if (!B || !pos || !B->built) { set_error("qcm_mpo_buf_term_pos: no built tensor"); return QCM_E_INVALID; }
+    std::memcpy(pos, B->term_pos.data(), B->term_pos.size() * sizeof(int32_t));
+    return QCM_OK;
+}
+
+void qcm_mpo_buf_destroy(qcm_mpo_buf* B) { delete B; }
+
+}  // extern "C"

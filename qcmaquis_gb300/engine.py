@@ -171,6 +171,8 @@ class Engine:
 
     # -- helpers ---------------------------------------------------------
     def fmpo(self, mpo) -> N.FMpo:
+        if isinstance(mpo, N.FMpo):     # already flattened (the native two-site builder)
+            return mpo
         f = self._mpo_cache.get(id(mpo))
         if f is None or f.mpo is not mpo:
             f = N.FMpo(mpo)

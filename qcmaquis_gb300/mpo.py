@@ -395,46 +395,83 @@ def make_mpo(model: QCModel) -> MPO:
     return TaggedMPOMaker(model).create_mpo()
 
 
+def _merge_spins(dst: List[int], src: List[int]):
+    """``extend_spin_basis``: grow ``dst`` to ``src``'s length, non-zero entries of src win."""
+    if len(dst) < len(src):
+        dst.extend([0] * (len(src) - len(dst)))
+    for i, v in enumerate(src):
+        if v != 0:
+            dst[i] = v
+
+
 def make_twosite_mpo(mpo1: MPOTensor, mpo2: MPOTensor, phys1: Index, phys2: Index) -> MPOTensor:
     """Two-site MPO tensor W(b1,b3) = sum_b2 W1(b1,b2) (x) W2(b2,b3) per operator spin
     (``make_twosite_mpo``, ``mp_tensors/ts_ops.h:78-152``).  The spin-coupled
     Kronecker product depends only on the two operators and the three bond spins,
     so each distinct (op1, op2, spins, product spin) is formed once and reused
-    scaled; the sums are those of the reference, term for term."""
+    scaled.  Only the non-zero (b1, b2, b3) chains are visited (b2 in row b1 of W1,
+    b3 in row b2 of W2), and every (b1, b3, spin) sum runs over its summands in the
+    reference's order, block by block, with the reference's additions."""
     assert mpo1.col_dim == mpo2.row_dim
     table: List[SiteOperator] = []
     prempo = []
     kron: Dict[tuple, SiteOperator] = {}
+    rows2 = [mpo2.row(b2) for b2 in range(mpo2.row_dim)]
     for b1 in range(mpo1.row_dim):
-        row1 = mpo1.row(b1)
-        for b3 in range(mpo2.col_dim):
-            summands = [b2 for b2 in row1 if mpo2.has(b2, b3)]
-            ret: Dict[int, SiteOperator] = {}
-            for b2 in summands:
-                p1 = mpo1.at(b1, b2)
-                p2 = mpo2.at(b2, b3)
-                for tag1, s1 in p1:
+        chains: Dict[int, List[int]] = {}
+        for b2 in mpo1.row(b1):
+            for b3 in rows2[b2]:
+                chains.setdefault(b3, []).append(b2)
+        j = mpo1.left_spin(b1).get()
+        for b3 in sorted(chains):
+            jp = mpo2.right_spin(b3).get()
+            # per product spin: block sums keyed (lc, rc), the spin basis, the first summand's spin
+            acc: Dict[int, list] = {}
+            for b2 in chains[b3]:
+                jpp = mpo1.right_spin(b2).get()
+                for tag1, s1 in mpo1.at(b1, b2):
                     op1 = mpo1.op(tag1)
-                    for tag2, s2 in p2:
+                    for tag2, s2 in mpo2.at(b2, b3):
                         op2 = mpo2.op(tag2)
-                        spins = allowed_spins(mpo1.left_spin(b1).get(), mpo2.right_spin(b3).get(),
-                                              op1.spin.get(), op2.spin.get())
-                        for s in spins:
-                            key = (tag1, tag2, mpo1.left_spin(b1).get(), mpo1.right_spin(b2).get(),
-                                   mpo2.right_spin(b3).get(), s)
+                        for sp in allowed_spins(j, jp, op1.spin.get(), op2.spin.get()):
+                            key = (tag1, tag2, j, jpp, jp, sp)
                             prod = kron.get(key)
                             if prod is None:
-                                prod_spin = SpinDescriptor(s, mpo1.left_spin(b1).get(), mpo2.right_spin(b3).get())
                                 prod = op_kron_su2(phys1, phys2, op1, op2, mpo1.left_spin(b1),
-                                                   mpo1.right_spin(b2), mpo2.right_spin(b3), prod_spin)
+                                                   mpo1.right_spin(b2), mpo2.right_spin(b3),
+                                                   SpinDescriptor(sp, j, jp))
                                 prod.remove_empty_blocks()
                                 kron[key] = prod
-                            prod = prod.scaled(s1 * s2)
-                            if s not in ret:
-                                ret[s] = SiteOperator()
-                            ret[s].iadd(prod)
-            for s in sorted(ret):
-                table.append(ret[s])
+                            c = s1 * s2
+                            a = acc.get(sp)
+                            if a is None:
+                                a = acc[sp] = [{}, {}, None, set()]
+                            blocks, basis = a[0], a[1]
+                            if not blocks:   # SiteOperator += takes the spin while empty
+                                a[2] = (prod.spin.twoS, prod.spin.diff)
+                            for bk, blk in zip(prod.bm.keys, prod.bm.blocks):
+                                cur = blocks.get(bk)
+                                blocks[bk] = blk * c if cur is None else cur + blk * c
+                            # a basis spin is a function of its position (the spin of that
+                            # product state), so merging one product's spin basis again
+                            # changes nothing: once per distinct product
+                            if key not in a[3]:
+                                a[3].add(key)
+                                for bk, (rr, cc) in prod.spin_basis.items():
+                                    d = basis.get(bk)
+                                    if d is None:
+                                        basis[bk] = (list(rr), list(cc))
+                                    else:
+                                        _merge_spins(d[0], rr)
+                                        _merge_spins(d[1], cc)
+            for sp in sorted(acc):
+                blocks, basis, spin_raw, _ = acc[sp]
+                op = SiteOperator(spin_basis=basis)
+                if spin_raw is not None:
+                    op.spin = SpinDescriptor.raw(*spin_raw)
+                for (lc, rc), blk in blocks.items():
+                    op.bm.insert_block(blk, lc, rc)
+                table.append(op)
                 prempo.append((b1, b3, len(table) - 1, 1.0))
     return MPOTensor(mpo1.row_dim, mpo2.col_dim, prempo, table, mpo1.herm * mpo2.herm,
                      mpo1.left_spins, mpo2.right_spins)

@@ -75,6 +75,13 @@ def lib():
                                                               C.c_void_p, C.POINTER(C.c_void_p)]
     L.qcm_plan_zerosite.argtypes = [C.POINTER(CBlocks), C.POINTER(CBoundary), C.POINTER(CBoundary),
                                     C.POINTER(CMpo), C.POINTER(CMpo), C.c_int32, C.POINTER(C.c_void_p)]
+    L.qcm_mpo_twosite_begin.argtypes = [C.POINTER(CMpo), C.POINTER(CMpo), C.POINTER(C.c_void_p), i32p]
+    L.qcm_mpo_twosite_keys.argtypes = [C.c_void_p, i32p]
+    L.qcm_mpo_twosite_finish.argtypes = [C.c_void_p, C.POINTER(CMpo)]
+    L.qcm_mpo_buf_view.argtypes = [C.c_void_p, C.POINTER(CMpo), i64p]
+    L.qcm_mpo_buf_term_pos.argtypes = [C.c_void_p, i32p]
+    L.qcm_mpo_buf_destroy.argtypes = [C.c_void_p]
+    L.qcm_mpo_buf_destroy.restype = None
     L.qcm_plan_merge.argtypes = [C.POINTER(C.c_void_p), C.c_int32, i64p, C.POINTER(C.c_void_p)]
     L.qcm_plan_sizes.argtypes = [C.c_void_p, i64p, i64p]
     L.qcm_plan_image_bytes.argtypes = [C.c_void_p, i64p]
@@ -270,6 +277,7 @@ class FMpo:
                 term_ptr.append(len(term_op))
             col_ptr.append(len(row_of))
         op_spin, op_blk_ptr, blk_q, blk_ent_ptr, ent, ent_coeff = [], [0], [], [0], [], []
+        self.op_tags = [tag for tag, _ in sorted(used_ops.items(), key=lambda kv: kv[1])]
         for tag, oid in sorted(used_ops.items(), key=lambda kv: kv[1]):
             op = mpo.op(tag)
             sp = mpo.sparse(tag)
@@ -318,6 +326,105 @@ class FMpo:
             raise ValueError("one scale per flattened term")
         f._make_c()
         return f
+
+
+class _FlatTensor:
+    """Shape of a tensor that exists only in flattened form."""
+
+    def __init__(self, row_dim: int, col_dim: int):
+        self.row_dim = row_dim
+        self.col_dim = col_dim
+
+
+def _copy(ptr, n, dtype):
+    if n <= 0:
+        return np.zeros(1, dtype=dtype)
+    return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+
+def make_twosite_fmpo(w1: FMpo, w2: FMpo, phys1: Index, phys2: Index = None) -> FMpo:
+    """The flattened two-site MPO tensor of W1 (x) W2 (``make_twosite_mpo``,
+    ``mp_tensors/ts_ops.h:78-152``) from the native builder: the distinct
+    spin-coupled Kronecker products are formed here by ``op_kron_su2``, the
+    chain walk and the sums run in ``qcm_mpo_twosite_*``.  Term for term the
+    result equals ``FMpo(make_twosite_mpo(...))``."""
+    from .site_operator import SpinDescriptor, op_kron_su2
+    phys2 = phys1 if phys2 is None else phys2
+    L = lib()
+    h = C.c_void_p()
+    nk = C.c_int32()
+    check(L.qcm_mpo_twosite_begin(C.byref(w1.c), C.byref(w2.c), C.byref(h), C.byref(nk)), "qcm_mpo_twosite_begin")
+    try:
+        keys = np.zeros(max(6 * nk.value, 1), dtype=np.int32)
+        check(L.qcm_mpo_twosite_keys(h, _p(keys, i32p)), "qcm_mpo_twosite_keys")
+        op_spin, op_blk_ptr, blk_q, blk_ent_ptr, ent, ent_coeff = [], [0], [], [0], [], []
+        for o1, o2, j, jpp, jp, sp in keys[:6 * nk.value].reshape(-1, 6).tolist():
+            op1 = w1.mpo.op(w1.op_tags[o1])
+            op2 = w2.mpo.op(w2.op_tags[o2])
+            prod = op_kron_su2(phys1, phys2, op1, op2, SpinDescriptor(j), SpinDescriptor(jpp), SpinDescriptor(jp),
+                               SpinDescriptor(sp, j, jp))
+            prod.remove_empty_blocks()
+            op_spin.append(sp)
+            for (pin, pout), ents in zip(prod.bm.keys, prod.sparse()):
+                blk_q += [pin[0], pin[1], pout[0], pout[1]]
+                for (r, c, rs, cs, v) in ents:
+                    ent += [r, c, rs, cs]
+                    ent_coeff.append(v)
+                blk_ent_ptr.append(len(ent_coeff))
+            op_blk_ptr.append(len(blk_ent_ptr) - 1)
+        a32 = lambda x: np.array(x or [0], dtype=np.int32)
+        arrs = dict(op_spin=a32(op_spin), op_blk_ptr=a32(op_blk_ptr), blk_q=a32(blk_q),
+                    blk_ent_ptr=a32(blk_ent_ptr), ent=a32(ent),
+                    ent_coeff=np.array(ent_coeff or [0.0], dtype=np.float64))
+        prods = CMpo()
+        prods.n_ops = len(op_spin)
+        for k in ("op_spin", "op_blk_ptr", "blk_q", "blk_ent_ptr", "ent"):
+            setattr(prods, k, _p(arrs[k], i32p))
+        prods.ent_coeff = _p(arrs["ent_coeff"], f64p)
+        check(L.qcm_mpo_twosite_finish(h, C.byref(prods)), "qcm_mpo_twosite_finish")
+        v = CMpo()
+        sz = (C.c_int64 * 4)()
+        check(L.qcm_mpo_buf_view(h, C.byref(v), sz), "qcm_mpo_buf_view")
+        ne, nt, nb, nent = sz[0], sz[1], sz[2], sz[3]
+        f = FMpo.__new__(FMpo)
+        f.mpo = _FlatTensor(v.row_dim, v.col_dim)
+        f.left_spin = _copy(v.left_spin, v.row_dim, np.int32)
+        f.right_spin = _copy(v.right_spin, v.col_dim, np.int32)
+        f.left_herm = _copy(v.left_herm, v.row_dim, np.int32)
+        f.right_herm = _copy(v.right_herm, v.col_dim, np.int32)
+        f.left_phase = _copy(v.left_phase, v.row_dim, np.int32)
+        f.right_phase = _copy(v.right_phase, v.col_dim, np.int32)
+        f.col_ptr = _copy(v.col_ptr, v.col_dim + 1, np.int32)
+        f.row_of = _copy(v.row_of, ne, np.int32)
+        f.term_ptr = _copy(v.term_ptr, ne + 1, np.int32)
+        f.term_op = _copy(v.term_op, nt, np.int32)
+        f.term_scale = _copy(v.term_scale, nt, np.float64)
+        f.n_ops = v.n_ops
+        f.op_spin = _copy(v.op_spin, nt, np.int32)
+        f.op_blk_ptr = _copy(v.op_blk_ptr, nt + 1, np.int32)
+        f.blk_q = _copy(v.blk_q, 4 * nb, np.int32)
+        f.blk_ent_ptr = _copy(v.blk_ent_ptr, nb + 1, np.int32)
+        f.ent = _copy(v.ent, 4 * nent, np.int32)
+        f.ent_coeff = _copy(v.ent_coeff, nent, np.float64)
+        pos = np.zeros(max(nt, 1), dtype=np.int32)
+        check(L.qcm_mpo_buf_term_pos(h, _p(pos, i32p)), "qcm_mpo_buf_term_pos")
+    finally:
+        L.qcm_mpo_buf_destroy(h)
+    b2 = np.repeat(np.arange(f.mpo.col_dim), np.diff(f.col_ptr[:f.mpo.col_dim + 1]))
+    tb1 = np.repeat(f.row_of[:ne], np.diff(f.term_ptr[:ne + 1])) if ne else np.zeros(0, dtype=np.int32)
+    tb2 = np.repeat(b2, np.diff(f.term_ptr[:ne + 1])) if ne else np.zeros(0, dtype=np.int64)
+    f.term_key = list(zip(tb1.tolist(), tb2.tolist(), pos[:nt].tolist()))
+    f.term_label = [None] * nt
+    f.op_tags = list(range(nt))
+    f._make_c()
+    return f
+
+
+def make_ts_cache_fmpo(mpo, phys: Index) -> List[FMpo]:
+    """Flattened two-site MPO tensors of every site pair (``make_ts_cache_mpo``,
+    ``mp_tensors/ts_ops.h:154-170``) from the native builder."""
+    flat = [FMpo(w) for w in mpo]
+    return [make_twosite_fmpo(flat[p], flat[p + 1], phys) for p in range(len(mpo) - 1)]
 
 
 # ------------------------------------------------------------------ plans
@@ -541,4 +648,4 @@ def plan_zerosite(bond: Layout, L: BoundaryLayout, R: BoundaryLayout, mpo_left: 
 
 __all__ = ["lib", "check", "Layout", "BoundaryLayout", "FMpo", "FIndex", "Plan", "plan_sigma",
            "plan_boundary_left", "plan_boundary_right", "plan_boundary_tensor_mpo", "plan_energy_gradient",
-           "plan_merge", "plan_zerosite", "PREC_BF16X2", "PREC_FP64", "PREC_TF32", "PREC_BF16X3"]
+           "plan_merge", "plan_zerosite", "make_twosite_fmpo", "make_ts_cache_fmpo", "PREC_BF16X2", "PREC_FP64", "PREC_TF32", "PREC_BF16X3"]

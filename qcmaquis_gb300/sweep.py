@@ -24,7 +24,7 @@ from . import mps_ops as O
 from .block_matrix import BlockMatrix
 from .engine import DeviceBoundary, DeviceMPSTensor, Engine, SiteProblem
 from .jd import solve_ietl_jcd
-from .mpo import make_ts_cache_mpo
+from . import native as N
 from .mps import allowed_sectors
 from .symmetry import Index, adjoin, common_subset, index_product
 
@@ -176,7 +176,8 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
     per-sweep energy stay FP64.  ``boundary_precision`` (default: FP64) selects the form
     of the boundary updates' block products (the boundaries are stored in FP64
     either way).  ``mps`` (right-normalised) replaces the default initial
-    state; ``ts_mpo`` is a prebuilt two-site MPO cache (``make_ts_cache_mpo``).
+    state; ``ts_mpo`` is a prebuilt two-site MPO cache (``native.make_ts_cache_fmpo``, or
+    ``mpo.make_ts_cache_mpo``); by default the native builder makes it.
     ``time_parts`` synchronises the device after each part of a microiteration to
     time it (``SweepRecord.seconds``); without it the device finishes one
     microiteration's boundary update while the host builds the next sigma plan.
@@ -197,7 +198,7 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
         mps = default_mps_init(L, phys, right_end, p.init_bond_dimension, p.seed, device)
         normalize_right(mps)
     if ts_mpo is None:
-        ts_mpo = make_ts_cache_mpo(mpo, phys)
+        ts_mpo = N.make_ts_cache_fmpo(mpo, phys)
     left: List = [None] * (L + 1)
     right: List = [None] * (L + 1)
     left[0] = _ones_boundary((0, 0), engine.device)

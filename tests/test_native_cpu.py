@@ -196,3 +196,32 @@ def test_cpp_layer_builds_a_plan(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "out=4" in out.stdout
+
+
+_FMPO_ARRAYS = ("left_spin", "right_spin", "left_herm", "right_herm", "left_phase", "right_phase", "col_ptr",
+                "row_of", "term_ptr", "term_op", "term_scale", "op_spin", "op_blk_ptr", "blk_q", "blk_ent_ptr",
+                "ent", "ent_coeff")
+
+
+@pytest.mark.parametrize("L,nelec,seed", [(6, 6, 3), (8, 6, 5)])
+def test_native_twosite_mpo_equals_python_builder(L, nelec, seed):
+    """qcm_mpo_twosite_* (the native two-site builder) reproduces the flattened
+    make_twosite_mpo tensor of every site pair array for array, bit for bit."""
+    from qcmaquis_gb300.mpo import make_twosite_mpo
+    model = QCModel(L, synthetic_integral_map(L, seed=seed), nelec)
+    mpo = make_mpo(model)
+    flat = [N.FMpo(w) for w in mpo]
+    for p in range(L - 1):
+        ref = N.FMpo(make_twosite_mpo(mpo[p], mpo[p + 1], model.phys, model.phys))
+        got = N.make_twosite_fmpo(flat[p], flat[p + 1], model.phys)
+        for k in _FMPO_ARRAYS:
+            a, b = getattr(ref, k), getattr(got, k)
+            assert a.shape == b.shape and np.array_equal(a, b), (p, k)
+        assert got.n_ops == ref.n_ops and got.term_key == ref.term_key
+
+
+def test_native_twosite_mpo_rejects_unshared_bond():
+    model = QCModel(6, synthetic_integral_map(6, seed=3), 6)
+    mpo = make_mpo(model)
+    with pytest.raises(RuntimeError, match="do not share a bond"):
+        N.make_twosite_fmpo(N.FMpo(mpo[0]), N.FMpo(mpo[2]), model.phys)
