@@ -751,6 +751,70 @@ def overlap_mpo_right_step(bra: MPSTensor, ket: MPSTensor, right: List[BlockMatr
     return ret
 
 
+# --------------------------------------------------------------------------- overlap boundaries
+def overlap_left_step(bra: MPSTensor, ket: MPSTensor, left: BlockMatrix) -> BlockMatrix:
+    """``common::overlap_left_step`` with ``SU2::gemm`` (``ct/common/move_boundary.hpp:20-40``):
+    the MPO-free left step of <bra|ket>; blocks keyed (bra charge, ket charge)."""
+    k = ket.copy().make_right_paired()
+    t1 = su2_gemm(left, k.data, -1)
+    t3 = reshape_right_to_left(k.phys_i, bra.left_i, k.right_i, t1)
+    b = bra.copy().make_left_paired()
+    return su2_gemm(b.data.transpose(), t3, -1)
+
+
+def overlap_right_step(bra: MPSTensor, ket: MPSTensor, right: BlockMatrix) -> BlockMatrix:
+    """``common::overlap_right_step`` (``ct/common/move_boundary.hpp:45-62``)."""
+    k = ket.copy().make_left_paired()
+    t1 = su2_gemm(k.data, right.transpose(), -1)
+    t3 = reshape_left_to_right(k.phys_i, k.left_i, bra.right_i, t1)
+    b = bra.copy().make_right_paired()
+    return su2_gemm(b.data, t3.transpose(), -1)
+
+
+def reshape_and_pad_left(phys: Index, in_left_i: Index, in_right_i: Index, out_left_i: Index,
+                         m1: BlockMatrix, m2: BlockMatrix) -> BlockMatrix:
+    """``reshape_and_pad_left`` (``mp_tensors/reshapes.h:228-278``): m2 zeroed, then every
+    (phys, left) stripe of m1 that m2's layout holds copied to its place in m2."""
+    out = BlockMatrix()
+    for key, blk in zip(m2.keys, m2.blocks):
+        out.insert_block(np.zeros_like(blk), *key)
+    in_left = ProductBasis(phys, in_left_i)
+    out_left = ProductBasis(phys, out_left_i)
+    for (lc, rc), blk in zip(m1.keys, m1.blocks):
+        for s in range(len(phys)):
+            pc, pd = phys[s]
+            if not in_right_i.has(rc):
+                continue
+            r = in_right_i.position(rc)
+            l_in = fuse(lc, neg(pc))
+            if not in_left_i.has(l_in):
+                continue
+            l = in_left_i.position(l_in)
+            ldim = in_left_i[l][1]
+            if not out_left_i.has(l_in):
+                continue
+            k2 = out.find_block(lc, rc)
+            if k2 == out.n_blocks():
+                continue
+            io, oo = in_left(pc, l_in), out_left(pc, l_in)
+            nr = in_right_i[r][1]
+            out.blocks[k2][oo:oo + pd * ldim, :nr] = blk[io:io + pd * ldim, :nr]
+    return out
+
+
+def site_ortho_boundaries(mps: MPSTensor, ortho: MPSTensor, o_left: BlockMatrix, o_right: BlockMatrix) -> MPSTensor:
+    """``site_ortho_boundaries`` (``ct/abelian/special.hpp:16-43``): the state ``ortho``
+    seen through the overlap boundaries of the sites around ``mps`` -- its
+    projection onto the variational space of ``mps``, in ``mps``'s left-paired layout."""
+    o = ortho.copy().make_right_paired()
+    t = bm_gemm(o_left, o.data)
+    t2 = reshape_right_to_left(mps.phys_i, o_left.left_basis(), o.right_i, t)
+    t3 = bm_gemm(t2, o_right.transpose())
+    m = mps.copy().make_left_paired()
+    data = reshape_and_pad_left(mps.phys_i, o_left.left_basis(), o_right.left_basis(), m.left_i, t3, m.data)
+    return MPSTensor(mps.phys_i, mps.left_i, mps.right_i, data, LEFT_PAIRED)
+
+
 # --------------------------------------------------------------------------- two-site tensor
 def two_site_theta(A: MPSTensor, B: MPSTensor) -> BlockMatrix:
     """``TwoSiteTensor(mps1, mps2)``: theta = A(lp) . B(rp) (``twositetensor.hpp:22-31``)."""
@@ -1179,19 +1243,47 @@ def predict_new_state(mps: MPSTensor, mpo, left, right, alpha: float, cutoff: fl
 
 
 # --------------------------------------------------------------------------- Jacobi-Davidson
-def jcd_solve(apply_h, init: MPSTensor, tol: float, maxiter: int):
+def _project(t: MPSTensor, ortho: List[MPSTensor]) -> MPSTensor:
+    """``SingleSiteVS::project`` (``fw/optimize/ietl_lanczos_solver.h:90-95``)."""
+    for o in ortho:
+        t.axpy(-o.dot(t) / o.dot(o), o)
+    return t
+
+
+def jcd_solve(apply_h, init: MPSTensor, tol: float, maxiter: int, ortho: Optional[List[MPSTensor]] = None,
+              completeness: float = 1e-10):
     """``solve_ietl_jcd`` -> ``jacobi_davidson::calculate_eigenvalue`` with zero GMRES
     steps (``fw/optimize/ietl_jacobi_davidson.h:16-77``, ``ietl/jacobi.h:99-138, 361-493``).
 
     ``basic_iteration(maxiter, tol, tol)`` stops when ||r|| < tol or
     ||r|| < tol*|theta| (``alps/src/ietl/iteration.h``), or after maxiter steps.
+    ``ortho``: vectors the solution is kept orthogonal to (excited states,
+    ``ietl_jacobi_davidson.h:28-49``): Gram-Schmidt among themselves (a vector
+    left with norm <= ``completeness`` is dropped), projected out of the start
+    vector, of every new basis vector and of A u before the residual
+    (``jacobi.h:378, 393, 432``).  If the start vector has nothing left after the
+    projection the solve is skipped and <init|A init> returned with ``init``.
     Returns (theta, u, iterations).
     """
     kappa = 0.25
+    local: List[MPSTensor] = []
+    for o in list(ortho or [])[:max(init.data.num_elements() - 1, 0)]:
+        v = o.copy().make_left_paired()
+        for q in local:
+            v.axpy(-q.dot(v), q)
+        if v.norm() > completeness:
+            local.append(v.scaled(1.0 / v.norm()))
+    if local:
+        tmp = init.copy().make_left_paired()
+        for q in local:
+            tmp.axpy(-tmp.dot(q), q)
+        if tmp.norm() < completeness:
+            x = init.copy().make_left_paired()
+            return x.dot(apply_h(x)), x, 0
     V: List[MPSTensor] = []
     VA: List[MPSTensor] = []
     M = np.zeros((maxiter, maxiter))
-    t = init.copy().make_left_paired()
+    t = _project(init.copy().make_left_paired(), local)
     it = 0
     while True:
         tau = t.norm()
@@ -1200,6 +1292,7 @@ def jcd_solve(apply_h, init: MPSTensor, tol: float, maxiter: int):
         if t.norm() < kappa * tau:
             for i in range(it):
                 t.axpy(-V[i].dot(t), V[i])
+        _project(t, local)
         t = t.scaled(1.0 / t.norm())
         V.append(t)
         VA.append(apply_h(t))
@@ -1216,6 +1309,7 @@ def jcd_solve(apply_h, init: MPSTensor, tol: float, maxiter: int):
         uA = VA[0].scaled(s[0])
         for j in range(1, n):
             uA.axpy(s[j], VA[j])
+        _project(uA, local)
         r = uA.axpy(-theta, u)
         it += 1
         rn = r.norm()

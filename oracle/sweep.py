@@ -110,13 +110,49 @@ def initial_state(model, mpo, p: SweepParams, nelec: int, twoS: int):
     return mps
 
 
+class OverlapBoundaries:
+    """``OverlapPropagator`` (``sba/OverlapPropagator.h``): per orthogonal state n the
+    MPO-free left and right overlap boundaries <psi|phi_n> of the current state
+    ``mps`` (bra) with phi_n (ket), started at site 0 (the right ones all built)."""
+
+    def __init__(self, mps: List[R.MPSTensor], others: List[List[R.MPSTensor]]):
+        L = len(mps)
+        self.mps, self.others = mps, others
+        self.left = [[None] * (L + 1) for _ in others]
+        self.right = [[None] * (L + 1) for _ in others]
+        for n in range(len(others)):
+            self.left[n][0] = R.left_boundary(mps[0])[0]
+            self.right[n][L] = R.right_boundary(mps[L - 1])[0]
+            for i in range(L - 1, 0, -1):
+                self.update_right(i, n)
+
+    def update_left(self, i: int, only=None):
+        for n in (range(len(self.others)) if only is None else [only]):
+            self.left[n][i] = R.overlap_left_step(self.mps[i - 1], self.others[n][i - 1], self.left[n][i - 1])
+
+    def update_right(self, i: int, only=None):
+        for n in (range(len(self.others)) if only is None else [only]):
+            self.right[n][i] = R.overlap_right_step(self.mps[i], self.others[n][i], self.right[n][i + 1])
+
+    def vectors(self, site: int, psi: R.MPSTensor) -> List[R.MPSTensor]:
+        """``getOrthogonalVector`` of every state for the two-site problem at (site, site + 1)."""
+        out = []
+        for n, phi in enumerate(self.others):
+            theta = R.make_two_site_mps(phi[site], phi[site + 1])
+            out.append(R.site_ortho_boundaries(psi, theta, self.left[n][site], self.right[n][site + 2]))
+        return out
+
+
 def run_dmrg(model, mpo: MPO, p: SweepParams, nelec: int, twoS: int = 0, mps=None,
-             callback=None) -> (SweepRecord, List[R.MPSTensor]):
+             callback=None, ortho_states=None) -> (SweepRecord, List[R.MPSTensor]):
+    """Two-site sweeps; ``ortho_states``: MPSs the state is optimised orthogonal to
+    (``n_ortho_states`` / ``ortho_states``, ``sba/SweepBasedEnergyMinimization.h:52-67``)."""
     L = model.L
     phys = model.phys
     if mps is None:
         mps = initial_state(model, mpo, p, nelec, twoS)
     ts_mpo = make_ts_cache_mpo(mpo, phys)
+    ovl = OverlapBoundaries(mps, list(ortho_states)) if ortho_states else None
     left: List = [None] * (L + 1)
     right: List = [None] * (L + 1)
     left[0] = R.left_boundary(mps[0])
@@ -139,7 +175,8 @@ def run_dmrg(model, mpo: MPO, p: SweepParams, nelec: int, twoS: int = 0, mps=Non
             def apply_h(x, _l=left[site], _r=right[site + 2], _w=ts):
                 return R.site_hamil2(x, _l, _r, _w)
 
-            theta, u, iters = R.jcd_solve(apply_h, psi, p.ietl_jcd_tol, p.ietl_jcd_maxiter)
+            ortho = ovl.vectors(site, psi) if ovl else None
+            theta, u, iters = R.jcd_solve(apply_h, psi, p.ietl_jcd_tol, p.ietl_jcd_maxiter, ortho)
             rec.energies.append(theta + mpo.core_energy)
             u.make_left_paired()
             A0, B0 = mps[site], mps[site + 1]
@@ -160,6 +197,12 @@ def run_dmrg(model, mpo: MPO, p: SweepParams, nelec: int, twoS: int = 0, mps=Non
             else:
                 right[site + 1] = R.overlap_mpo_right_step(mps[site + 1], mps[site + 1], right[site + 2],
                                                            mpo[site + 1])
+            if ovl:
+                # SweepBasedEnergyMinimization::propagateOtherTensors
+                if l2r:
+                    ovl.update_left(site + 1)
+                else:
+                    ovl.update_right(site + 1)
             if l2r:
                 if site + 2 < L:
                     t = R.left_normalize_and_return(mps[site + 1])

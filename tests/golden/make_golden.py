@@ -8,7 +8,9 @@ Reads, as text, the reference test sources:
 * ``dmrg/tests/test1.cpp:93`` -- H2 ground-state energy;
 * ``dmrg/tests/test_wigner.cpp:21-45`` -- 24 Wigner 9j values;
 * ``dmrg/tests/test2.cpp:60-120`` -- the LiH (SU2U1) ground-state 2-RDM
-  (measurement ``twoptdm``): index quadruples and values.
+  (measurement ``twoptdm``): index quadruples and values;
+* ``dmrg/tests/test2.cpp:138`` -- the LiH (SU2U1) first excited singlet energy,
+  optimised orthogonal to the ground state (``n_ortho_states = 1``).
 
 Run from the repository root with the reference mounted at REFERENCE (default
 ``/root/reference``); the JSON it writes is committed so tests never need the
@@ -59,6 +61,9 @@ def main():
     if len(rdm_idx) != len(rdm_val):
         raise SystemExit(f"2-RDM parse mismatch: {len(rdm_idx)} indices, {len(rdm_val)} values")
 
+    s1 = re.search(r"ref_energy_excited_state\s*=\s*su2\s*\?\s*(" + NUM + ")", t2)
+    lih_s1 = float(s1.group(1))
+
     data = {
         "source": "values read from the reference test sources by tests/golden/make_golden.py",
         "lih": {"L": 4, "nelec": 2, "spin": 0, "integrals": lih_ints, "energy": lih_e,
@@ -67,11 +72,13 @@ def main():
                "cite": "dmrg/tests/Fixtures/H2Fixture.h:26-35; dmrg/tests/test1.cpp:93"},
         "wigner9j": {"cases": wig, "rel_tol_percent": 1e-6, "cite": "dmrg/tests/test_wigner.cpp:21-45"},
         "lih_2rdm": {"index": rdm_idx, "value": rdm_val, "cite": "dmrg/tests/test2.cpp:60-120 (twoptdm)"},
+        "lih_s1": {"energy": lih_s1, "rel_tol_percent": 1e-7,
+                   "cite": "dmrg/tests/test2.cpp:122-139 (SU2U1 excited singlet, one orthogonal state)"},
     }
     with open(os.path.join(HERE, "reference_fixtures.json"), "w") as f:
         json.dump(data, f, indent=1)
     print(f"LiH {len(lih_ints)} integrals E={lih_e}; H2 {len(h2_ints)} integrals E={h2_e}; {len(wig)} 9j cases; "
-          f"LiH 2-RDM {len(rdm_val)} elements")
+          f"LiH 2-RDM {len(rdm_val)} elements; LiH S1 E={lih_s1}")
 
 
 if __name__ == "__main__":

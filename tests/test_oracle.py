@@ -179,3 +179,41 @@ def test_zero_site_hermitian_partners_match_full_boundary():
     assert a.keys == b.keys
     diff = max(float(np.abs(x - y).max()) for x, y in zip(a.blocks, b.blocks))
     assert diff <= 1e-12 * a.norm()
+
+
+def test_fci_pins_golden_excited_state(golden):
+    """The second singlet root of LiH is the reference's excited-state energy
+    (``dmrg/tests/test2.cpp:138``), independently of any DMRG code."""
+    g = golden["lih"]
+    e = fci_energies(g["L"], integral_map(g["integrals"]), g["nelec"], g["spin"], 2)[1]
+    assert abs(e - golden["lih_s1"]["energy"]) < 1e-9 * abs(e)
+
+
+def test_oracle_excited_state_golden_lih(golden):
+    """``dmrg/tests/test2.cpp:122-139``: optimised orthogonal to the ground state
+    (one orthogonal state), the LiH sweeps reach the reference's S1 energy
+    (BOOST_CHECK_CLOSE 1e-7 percent)."""
+    g = golden["lih"]
+    m = QCModel(g["L"], integral_map(g["integrals"]), g["nelec"])
+    mpo = make_mpo(m)
+    _, gs = run_dmrg(m, mpo, SweepParams(nsweeps=2, max_bond_dimension=100), nelec=g["nelec"])
+    rec, _ = run_dmrg(m, mpo, SweepParams(nsweeps=2, max_bond_dimension=100, seed=7), nelec=g["nelec"],
+                      ortho_states=[gs])
+    s1 = golden["lih_s1"]["energy"]
+    assert abs(rec.sweep_energy[-1] - s1) < 1e-9 * abs(s1)
+
+
+def test_oracle_excited_states_match_fci_L6():
+    """Sequential constrained sweeps: S1 orthogonal to S0, S2 orthogonal to both,
+    against exact diagonalisation (L=6, N=6 singlet)."""
+    L, N = 6, 6
+    ints = synthetic_integral_map(L, seed=3)
+    model = QCModel(L, ints, N)
+    mpo = make_mpo(model)
+    exact = fci_energies(L, ints, N, 0, 3)
+    _, s0 = run_dmrg(model, mpo, SweepParams(nsweeps=3, max_bond_dimension=64), nelec=N)
+    r1, s1 = run_dmrg(model, mpo, SweepParams(nsweeps=3, max_bond_dimension=64, seed=5), nelec=N, ortho_states=[s0])
+    r2, _ = run_dmrg(model, mpo, SweepParams(nsweeps=3, max_bond_dimension=64, seed=9), nelec=N,
+                     ortho_states=[s0, s1])
+    assert abs(r1.sweep_energy[-1] - exact[1]) < 1e-9
+    assert abs(r2.sweep_energy[-1] - exact[2]) < 1e-9
