@@ -17,7 +17,7 @@ host in FP64 (the reference uses LAPACK dsyevx there too).
 from __future__ import annotations
 
 import ctypes as C
-from typing import List
+from typing import List, Optional, Sequence
 
 import numpy as np
 import torch
@@ -56,16 +56,46 @@ class VecOps:
                                      self.stream()), "lincomb")
 
 
-def solve_ietl_jcd(sp: SiteProblem, init: DeviceMPSTensor, tol: float = 1e-8, maxiter: int = 10):
-    """Smallest eigenpair of H_eff; returns (theta, eigenvector tensor, iterations, sigma calls)."""
+def solve_ietl_jcd(sp: SiteProblem, init: DeviceMPSTensor, tol: float = 1e-8, maxiter: int = 10,
+                   ortho: Optional[Sequence[torch.Tensor]] = None, completeness: float = 1e-10):
+    """Smallest eigenpair of H_eff; returns (theta, eigenvector tensor, iterations).
+
+    ``ortho``: flat vectors in ``init``'s layout the solution is kept orthogonal
+    to (excited states, ``ietl_jacobi_davidson.h:28-49``): Gram-Schmidt among
+    themselves (dropped at norm <= ``completeness``), projected out of the start
+    vector, of every new basis vector and of A u before the residual
+    (``SingleSiteVS::project``, ``jacobi.h:378, 393, 432``).  With nothing left of
+    the start vector after the projection the solve is skipped: (<init|A init>,
+    init, 0)."""
     dev = init.data.device
     ops = VecOps(dev)
     n = init.n
+    local: List[torch.Tensor] = []
+    for o in list(ortho or [])[:max(n - 1, 0)]:
+        v = o.clone()
+        for q in local:
+            ops.axpby(-ops.dot(q, v), q, 1.0, v)
+        nv = ops.nrm2(v)
+        if nv > completeness:
+            ops.axpby(1.0 / nv, v, 0.0, v)
+            local.append(v)
+
+    def project(x: torch.Tensor):
+        for q in local:
+            ops.axpby(-ops.dot(q, x) / ops.dot(q, q), q, 1.0, x)
+
+    if local:
+        tmp = init.data.clone()
+        for q in local:
+            ops.axpby(-ops.dot(tmp, q), q, 1.0, tmp)
+        if ops.nrm2(tmp) < completeness:
+            return ops.dot(init.data, sp.apply(init).data), init, 0
     V: List[torch.Tensor] = []
     VA: List[torch.Tensor] = []
     M = np.zeros((maxiter, maxiter))
     kappa = 0.25
     t = init.data.clone()
+    project(t)
     it = 0
     while True:
         tau = ops.nrm2(t)
@@ -74,6 +104,7 @@ def solve_ietl_jcd(sp: SiteProblem, init: DeviceMPSTensor, tol: float = 1e-8, ma
         if ops.nrm2(t) < kappa * tau:
             for i in range(it):
                 ops.axpby(-ops.dot(V[i], t), V[i], 1.0, t)
+        project(t)
         nt = ops.nrm2(t)
         ops.axpby(1.0 / nt, t, 0.0, t)
         V.append(t)
@@ -90,6 +121,7 @@ def solve_ietl_jcd(sp: SiteProblem, init: DeviceMPSTensor, tol: float = 1e-8, ma
         uA = torch.empty(n, dtype=torch.float64, device=dev)
         ops.lincomb(V, s, u)
         ops.lincomb(VA, s, uA)
+        project(uA)
         ops.axpby(-theta, u, 1.0, uA)  # r = uA - theta u  (in uA)
         it += 1
         rn = ops.nrm2(uA)

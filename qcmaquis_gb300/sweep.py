@@ -23,6 +23,7 @@ import torch
 from . import mps_ops as O
 from .block_matrix import BlockMatrix
 from .engine import DeviceBoundary, DeviceMPSTensor, Engine, SiteProblem
+from .excited import OverlapBoundaries
 from .jd import solve_ietl_jcd
 from . import native as N
 from .mps import allowed_sectors
@@ -168,7 +169,7 @@ def expval(mps: List[DeviceMPSTensor], mpo, engine_full: Engine, right_end) -> f
 def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optional[List[DeviceMPSTensor]] = None,
              engine: Optional[Engine] = None, device="cuda", callback=None, precision: int = 0, ts_mpo=None,
              boundary_precision: Optional[int] = None, time_parts: bool = True, checkpoint: Optional[str] = None,
-             start_sweep: int = 0, plan_cache: int = 0):
+             start_sweep: int = 0, plan_cache: int = 0, ortho_states: Optional[List[List[DeviceMPSTensor]]] = None):
     """Two-site sweeps.  ``precision`` selects the sigma-vector form (0 = FP64,
     1 = TF32, 2 = BF16x3 tensor cores); boundary updates, the eigensolver's
     vector algebra, the subspace problem, the truncation (SVD, or the
@@ -185,7 +186,10 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
     sweep (``sim.hpp:197-211``); ``start_sweep`` resumes a run at that sweep of
     its schedule (``mps`` from ``checkpoint.load``, sweeps start_sweep..nsweeps-1).
     ``plan_cache`` > 0 keeps that many sigma plans, keyed by their layouts, so a
-    site problem whose layouts recur in a later sweep reuses its plan."""
+    site problem whose layouts recur in a later sweep reuses its plan.
+    ``ortho_states``: device MPSs the state is optimised orthogonal to (excited
+    states, ``n_ortho_states`` / ``ortho_states``,
+    ``sba/SweepBasedEnergyMinimization.h:52-67``; ``excited.OverlapBoundaries``)."""
     L = model.L
     phys = model.phys
     engine = engine or Engine(device, precision=precision)
@@ -205,6 +209,7 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
     right[L] = _ones_boundary(right_end, engine.device)
     for i in range(L - 1, 0, -1):
         right[i] = engine.overlap_mpo_right_step(mps[i], right[i + 1], mpo[i], precision=bprec)
+    ovl = OverlapBoundaries(mps, ortho_states, right_end) if ortho_states else None
     rec = SweepRecord()
     nmicro = 2 * (L - 2) if L > 2 else 1
     for sweep in range(start_sweep, p.nsweeps):
@@ -223,7 +228,8 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
                                             tuple(left[site].layout.keys), tuple(left[site].layout.shapes),
                                             tuple(right[site + 2].layout.keys), tuple(right[site + 2].layout.shapes))))
             sp = SiteProblem(engine, left[site], right[site + 2], ts_mpo[site])
-            theta, u, iters = solve_ietl_jcd(sp, psi, p.ietl_jcd_tol, p.ietl_jcd_maxiter)
+            ortho = ovl.vectors(site, psi) if ovl else None
+            theta, u, iters = solve_ietl_jcd(sp, psi, p.ietl_jcd_tol, p.ietl_jcd_maxiter, ortho)
             if time_parts:
                 torch.cuda.synchronize()
             t_b = time.time()
@@ -259,6 +265,12 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
                     mps[site - 1] = O.multiply_from_right(mps[site - 1], t)
                 else:
                     mps[site], _ = O.right_normalize_and_return(mps[site])
+            if ovl:
+                # SweepBasedEnergyMinimization::propagateOtherTensors
+                if l2r:
+                    ovl.update_left(site + 1)
+                else:
+                    ovl.update_right(site + 1)
             if time_parts:
                 torch.cuda.synchronize()
             t_d = time.time()
