@@ -478,7 +478,6 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
     // right_i (16 bits), row offset (32 bits): ascending keys are the reference's
     // block order (both indices descend) with row offsets ascending.
     struct KeyedTerm { uint64_t key; int64_t src_off; double alpha; int32_t rows, cols, tt; };
-    using TileMap = std::vector<KeyedTerm>;
     if (out_left_i.size() >= (1u << 16) || right_i.size() >= (1u << 16))
         throw std::runtime_error("too many sectors for the K2 planner");
     for (int b2 : b2list)
@@ -546,8 +545,9 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
     }
     task_begin[b2list.size()] = tasks.size();
     std::vector<TaskOut> tout(tasks.size());
-    std::vector<TileMap> per(b2list.size());
-    std::vector<std::vector<std::pair<uint64_t, uint32_t>>> ord(b2list.size());
+    // per column: pointers to its terms (in the tasks' own lists, task order),
+    // stably ordered by tile key
+    std::vector<std::vector<const KeyedTerm*>> ord(b2list.size());
     std::vector<double> fl(b2list.size(), 0.0);
     auto parallel = [&](size_t n, const std::function<void(size_t)>& f) {
         std::atomic<size_t> next{0};
@@ -573,15 +573,16 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
         if (!err.empty()) throw std::runtime_error(err);
     };
     parallel(tasks.size(), [&](size_t ti) { column(b2list[tasks[ti].col], tasks[ti].e0, tasks[ti].e1, tout[ti]); });
-    // per column: its tasks' terms in task order, stably sorted by tile key; its blocks
+    // per column: its blocks, and its terms stably ordered by key.  A column has few
+    // distinct keys (its output tiles) and many terms per key, so the terms are
+    // grouped by key through a hash table, the distinct keys sorted, and every group
+    // laid out in task and position order -- the order a stable sort of the
+    // concatenated task lists by key gives
     parallel(b2list.size(), [&](size_t i) {
         const int b2 = b2list[i];
-        size_t n = 0;
-        for (size_t ti = task_begin[i]; ti < task_begin[i + 1]; ++ti) n += tout[ti].terms.size();
-        per[i].reserve(n);
+        size_t nt = 0;
         for (size_t ti = task_begin[i]; ti < task_begin[i + 1]; ++ti) {
-            per[i].insert(per[i].end(), tout[ti].terms.begin(), tout[ti].terms.end());
-            std::vector<KeyedTerm>().swap(tout[ti].terms);
+            nt += tout[ti].terms.size();
             fl[i] += tout[ti].flops;
             for (const BlkNeed& bn : tout[ti].blocks)
                 if (C[b2].find(bn.lc, bn.rc) == C[b2].b.size()) {
@@ -592,12 +593,35 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
                     nb.cols = bn.cols;
                     C[b2].insert(nb);
                 }
+            std::vector<BlkNeed>().swap(tout[ti].blocks);
         }
-        // stable order by key: sort (key, position) pairs, not the records
-        std::vector<std::pair<uint64_t, uint32_t>>& o = ord[i];
-        o.resize(per[i].size());
-        for (size_t k = 0; k < o.size(); ++k) o[k] = {per[i][k].key, (uint32_t)k};
-        std::sort(o.begin(), o.end());
+        std::unordered_map<uint64_t, uint32_t> gid;
+        gid.reserve(1024);
+        std::vector<uint32_t> g(nt), cnt;
+        std::vector<uint64_t> gkey;
+        size_t k = 0;
+        for (size_t ti = task_begin[i]; ti < task_begin[i + 1]; ++ti)
+            for (const KeyedTerm& x : tout[ti].terms) {
+                auto it = gid.find(x.key);
+                if (it == gid.end()) {
+                    it = gid.emplace(x.key, (uint32_t)gkey.size()).first;
+                    gkey.push_back(x.key);
+                    cnt.push_back(0);
+                }
+                g[k++] = it->second;
+                ++cnt[it->second];
+            }
+        std::vector<uint32_t> rank(gkey.size());
+        for (size_t q = 0; q < rank.size(); ++q) rank[q] = (uint32_t)q;
+        std::sort(rank.begin(), rank.end(), [&](uint32_t a, uint32_t b) { return gkey[a] < gkey[b]; });
+        std::vector<size_t> pos(gkey.size());
+        size_t acc = 0;
+        for (uint32_t r : rank) { pos[r] = acc; acc += cnt[r]; }
+        std::vector<const KeyedTerm*>& o = ord[i];
+        o.resize(nt);
+        k = 0;
+        for (size_t ti = task_begin[i]; ti < task_begin[i + 1]; ++ti)
+            for (const KeyedTerm& x : tout[ti].terms) o[pos[g[k++]]++] = &x;
     });
     int64_t base = 0;
     for (auto& c : C) base = c.assign_offsets(base);
@@ -607,16 +631,16 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
     // precomputed range of the output and term tables (in parallel)
     std::vector<size_t> ntile(b2list.size(), 0);
     parallel(b2list.size(), [&](size_t i) {
-        const std::vector<std::pair<uint64_t, uint32_t>>& o = ord[i];
+        const std::vector<const KeyedTerm*>& o = ord[i];
         size_t n = 0;
         for (size_t a = 0; a < o.size(); ++a)
-            if (a == 0 || o[a].first != o[a - 1].first) ++n;
+            if (a == 0 || o[a]->key != o[a - 1]->key) ++n;
         ntile[i] = n;
     });
     std::vector<size_t> obase(b2list.size() + 1, st.aout.size()), tbase(b2list.size() + 1, st.aterm.size());
     for (size_t i = 0; i < b2list.size(); ++i) {
         obase[i + 1] = obase[i] + ntile[i];
-        tbase[i + 1] = tbase[i] + per[i].size();
+        tbase[i + 1] = tbase[i] + ord[i].size();
     }
     st.aout.resize(obase[b2list.size()]);
     st.aterm.resize(tbase[b2list.size()]);
@@ -625,16 +649,15 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
     parallel(b2list.size(), [&](size_t i) {
         const int b2 = b2list[i];
         const BM& cb = C[b2];
-        TileMap& v = per[i];
-        std::vector<std::pair<uint64_t, uint32_t>>& ov = ord[i];
+        std::vector<const KeyedTerm*>& ov = ord[i];
         size_t oi = obase[i], ti = tbase[i];
         for (size_t a = 0; a < ov.size();) {
             size_t b = a + 1;
-            while (b < ov.size() && ov[b].first == ov[a].first) ++b;   // equal keys: one tile
-            const uint64_t key = ov[a].first;
+            while (b < ov.size() && ov[b]->key == ov[a]->key) ++b;   // equal keys: one tile
+            const uint64_t key = ov[a]->key;
             const Q out_l = out_left_i.d[key >> 48].first, out_r = right_i.d[(key >> 32) & 0xFFFFu].first;
             const Blk& d = cb.b[cb.find(out_l, out_r)];
-            const KeyedTerm& last = v[ov[b - 1].second];
+            const KeyedTerm& last = *ov[b - 1];
             AxpyOut& o = st.aout[oi++];
             o.dst_buf = c_buf;
             o.dst_off = d.off + (int64_t)(uint32_t)(key & 0xFFFFFFFFu);
@@ -643,7 +666,7 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
             o.cols = last.cols;
             o.t_begin = (int64_t)ti;
             for (size_t k = a; k < b; ++k) {
-                const KeyedTerm& x = v[ov[k].second];
+                const KeyedTerm& x = *ov[k];
                 if (prov) (*prov)[ti] = {x.tt, x.alpha / m->term_scale[x.tt]};
                 st.aterm[ti++] = {t_buf, x.src_off, x.rows, x.alpha};
             }
@@ -651,8 +674,7 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
             bytes[i] += 8.0 * o.rows * o.cols * (double)(b - a + 1);
             a = b;
         }
-        TileMap().swap(v);
-        std::vector<std::pair<uint64_t, uint32_t>>().swap(ov);
+        std::vector<const KeyedTerm*>().swap(ov);
     });
     for (size_t i = 0; i < b2list.size(); ++i) {
         P->axpy_flops += fl[i];
