@@ -1622,8 +1622,32 @@ bool axpy_components(const Stage& st, std::vector<int32_t>& root) {
         }
     };
     // every thread owns the source keys of one hash class: it keeps their first output
-    // in a private open-addressing table and unites later readers with it
+    // in a private open-addressing table and unites later readers with it.  The terms
+    // are read once: each thread buckets the (key, output) pairs of its share of the
+    // outputs by class, then the owner of a class walks the buckets in output order.
+    // (The components, and so every root, do not depend on the walk order.)
     auto mix = [](int64_t key) { return (uint64_t)key * 0x9E3779B97F4A7C15ull; };
+    std::vector<std::vector<std::vector<std::pair<int64_t, int32_t>>>> bucket(
+        nt, std::vector<std::vector<std::pair<int64_t, int32_t>>>(nt));
+    run([&](unsigned t) {
+        const size_t i0 = nO * t / nt, i1 = nO * (t + 1) / nt;
+        std::vector<size_t> cnt(nt, 0);
+        for (size_t i = i0; i < i1; ++i) {
+            const AxpyOut& a = st.aout[i];
+            for (int64_t k = a.t_begin; k < a.t_end; ++k) {
+                const int64_t key = ((int64_t)st.aterm[k].src_buf << 56) ^ st.aterm[k].src_off;
+                ++cnt[(mix(key) >> 58) % nt];
+            }
+        }
+        for (unsigned c = 0; c < nt; ++c) bucket[t][c].reserve(cnt[c]);
+        for (size_t i = i0; i < i1; ++i) {
+            const AxpyOut& a = st.aout[i];
+            for (int64_t k = a.t_begin; k < a.t_end; ++k) {
+                const int64_t key = ((int64_t)st.aterm[k].src_buf << 56) ^ st.aterm[k].src_off;
+                bucket[t][(mix(key) >> 58) % nt].push_back({key, (int32_t)i});
+            }
+        }
+    });
     run([&](unsigned t) {
         std::vector<int64_t> keys(1u << 12, -1);
         std::vector<int32_t> vals(1u << 12, 0);
@@ -1634,11 +1658,10 @@ bool axpy_components(const Stage& st, std::vector<int32_t>& root) {
             while (keys[h] != -1 && keys[h] != key) h = (h + 1) & mask;
             return h;
         };
-        for (size_t i = 0; i < nO; ++i) {
-            const AxpyOut& a = st.aout[i];
-            for (int64_t k = a.t_begin; k < a.t_end; ++k) {
-                const int64_t key = ((int64_t)st.aterm[k].src_buf << 56) ^ st.aterm[k].src_off;
-                if ((mix(key) >> 58) % nt != t) continue;
+        for (unsigned src = 0; src < nt; ++src)
+            for (const auto& kv : bucket[src][t]) {
+                const int64_t key = kv.first;
+                const int32_t i = kv.second;
                 size_t h = slot(key);
                 if (keys[h] == -1) {
                     keys[h] = key;
@@ -1657,11 +1680,11 @@ bool axpy_components(const Stage& st, std::vector<int32_t>& root) {
                                 vals[g] = ov[q];
                             }
                     }
-                } else if (vals[h] != (int32_t)i) {
-                    unite((int32_t)i, vals[h]);
+                } else if (vals[h] != i) {
+                    unite(i, vals[h]);
                 }
             }
-        }
+        for (unsigned src = 0; src < nt; ++src) std::vector<std::pair<int64_t, int32_t>>().swap(bucket[src][t]);
     });
     root.resize(nO);
     for (size_t i = 0; i < nO; ++i) root[i] = find((int32_t)i);
