@@ -205,6 +205,16 @@ int qcm_mpo_buf_view(const qcm_mpo_buf* buf, qcm_mpo_t* view, int64_t* sizes);
 int qcm_mpo_buf_term_pos(const qcm_mpo_buf* buf, int32_t* pos);
 void qcm_mpo_buf_destroy(qcm_mpo_buf* buf);
 
+/* Diagonal of H_eff (Engine::diagonal_hamiltonian, dmrg/framework/dmrg/mp_tensors/
+ * contractions/non-abelian/engine.hpp:221-226 -> SU2::diagonal_hamiltonian,
+ * non-abelian/h_diag.hpp:118-158), the arguments of qcm_plan_sigma without
+ * hermitian: every L[b1] and R[b2] is read as given, so the boundaries must hold
+ * every bond index (built with hermitian = 0).  OUT has psi's layout.  FP64 form
+ * only (other precisions: QCM_E_INVALID). */
+int qcm_plan_diagonal(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                      const qcm_blocks_t* psi, const qcm_boundary_t* left, const qcm_boundary_t* right,
+                      const qcm_mpo_t* mpo, qcm_plan** plan);
+
 /* Zero-site problem (ZeroSiteProblem::apply, dmrg/framework/dmrg/mp_tensors/
  * zerositeproblem.h:40-42 -> zerosite_hamil_lbtm_kernel, dmrg/framework/dmrg/
  * mp_tensors/contractions/non-abelian/zero_site_hamil.hpp:44-79): sigma =

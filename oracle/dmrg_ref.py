@@ -16,7 +16,7 @@ import numpy as np
 from qcmaquis_gb300.block_matrix import BlockMatrix, gemm as bm_gemm
 from qcmaquis_gb300.symmetry import (Index, ProductBasis, adjoin, common_subset, fuse, fuse_neg_first,
                                      index_product, neg, spin, triangle)
-from qcmaquis_gb300.wigner import conjugate_correction, set_coupling, wigner6j
+from qcmaquis_gb300.wigner import conjugate_correction, mod_coupling, set_coupling, wigner6j
 
 LEFT_PAIRED, RIGHT_PAIRED = 0, 1
 
@@ -688,6 +688,69 @@ def zerosite_hamil(bond: BlockMatrix, left: List[BlockMatrix], right: List[Block
         for k in range(tmp.n_blocks()):
             out.match_and_add_block(tmp.blocks[k], *tmp.keys[k])
     return out
+
+
+def diagonal_hamiltonian(left: List[BlockMatrix], right: List[BlockMatrix], mpo, x: MPSTensor) -> BlockMatrix:
+    """``SU2::diagonal_hamiltonian`` + ``lbtm_diag_kernel`` (``ct/non-abelian/h_diag.hpp:13-158``):
+    the diagonal of H_eff in x's left-paired layout.  Reads L[b1] and R[b2] for
+    every bond index (no Hermitian partners), so the boundaries must hold every b.
+    Per b2 and every MPO term of its column, the diagonal entries (row == col) of
+    the operator add coeff * coupling * diag(L[b1](lc, lc)) to the rows of
+    (phys, lc) in every column of the output block; the per-b2 block is then
+    scaled column by column by diag(R[b2](rc, rc)) and added in, when R[b2]
+    has that block."""
+    phys = x.phys_i
+    xs = x.copy().make_left_paired()
+    right_i = xs.right_i.copy()
+    out_left_i = index_product(phys, xs.left_i)
+    common_subset(out_left_i, right_i)
+    left_pb = ProductBasis(phys, xs.left_i)
+    ret = BlockMatrix()
+    for b2 in range(len(right)):
+        lb2 = BlockMatrix()
+        ap = mpo.right_spin(b2).get()
+        for b1 in mpo.column(b2):
+            a = mpo.left_spin(b1).get()
+            for tag, scale in mpo.at(b1, b2):
+                W = mpo.op(tag)
+                wsparse = mpo.sparse(tag)
+                k = W.spin.get()
+                for blk in range(len(right_i)):
+                    in_charge = right_i[blk][0]
+                    o = lb2.find_block(in_charge, in_charge)
+                    if o == lb2.n_blocks():
+                        o = lb2.insert_block(np.zeros((out_left_i[blk][1], right_i[blk][1])), in_charge, in_charge)
+                    for pc, _pd in phys:
+                        lin = fuse(in_charge, neg(pc))
+                        if not xs.left_i.has(lin):
+                            continue
+                        l = xs.left_i.position(lin)
+                        lc, ld = xs.left_i[l]
+                        lk = left[b1].find_block(lc, lc)
+                        if lk == left[b1].n_blocks():
+                            continue
+                        ldiag = np.diagonal(left[b1].blocks[lk])[:ld]
+                        loff = left_pb(pc, lc)
+                        for wb in range(W.bm.n_blocks()):
+                            p_in, p_out = W.bm.keys[wb]
+                            if pc != p_in or p_in != p_out:
+                                continue
+                            i, ip, j, jp = spin(lc), spin(in_charge), spin(lc), spin(in_charge)
+                            pref = math.sqrt((ip + 1.0) * (j + 1.0) / ((i + 1.0) * (jp + 1.0))) * scale
+                            c0 = pref * mod_coupling(j, abs(j - jp), jp, a, k, ap, i, abs(i - ip), ip)
+                            c1 = pref * mod_coupling(j, 2, jp, a, k, ap, i, 2, ip)
+                            for (ss1, ss2, rspin, _cspin, coeff) in wsparse[wb]:
+                                if ss1 != ss2:
+                                    continue
+                                alfa = coeff * (c1 if rspin == 2 else c0)
+                                lb2.blocks[o][loff + ss1 * ld:loff + (ss1 + 1) * ld, :] += (alfa * ldiag)[:, None]
+        for (lc, rc), blk in zip(lb2.keys, lb2.blocks):
+            rk = right[b2].find_block(rc, rc)
+            if rk == right[b2].n_blocks():
+                continue
+            rdiag = np.diagonal(right[b2].blocks[rk])[:blk.shape[1]]
+            ret.match_and_add_block(blk * rdiag[None, :], rc, rc)
+    return ret
 
 
 # --------------------------------------------------------------------------- boundary steps

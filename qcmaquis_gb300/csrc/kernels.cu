@@ -919,8 +919,9 @@ int qcm_plan_run_typed(qcm_plan* p, double* const* bufs, uint32_t f32mask, int32
         set_error("unknown precision");
         return QCM_E_INVALID;
     }
-    if (p->kind == PK_GRAD && (precision != QCM_PREC_FP64 || f32mask != 0)) {
-        set_error("energy-gradient plans run in the FP64 form only");
+    if ((p->kind == PK_GRAD || p->kind == PK_DIAG) && (precision != QCM_PREC_FP64 || f32mask != 0)) {
+        set_error(p->kind == PK_GRAD ? "energy-gradient plans run in the FP64 form only"
+                                     : "diagonal plans run in the FP64 form only");
         return QCM_E_INVALID;
     }
     BufTable bt;

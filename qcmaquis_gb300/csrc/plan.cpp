@@ -983,6 +983,147 @@ static qcm_plan* build_zerosite(const BM& bond, const std::vector<BM>& L, const 
     return P;
 }
 
+// Diagonal of H_eff (SU2::diagonal_hamiltonian + lbtm_diag_kernel,
+// ct/non-abelian/h_diag.hpp:13-158) in the ket's left-paired layout.  Every L[b1]
+// and R[b2] is read as given (the reference uses no Hermitian partners here).  A
+// contribution -- b2, b1 of its column, a term, a phys charge p with lc = c - p,
+// a diagonal operator entry (ss, ss) -- adds alfa * diag(L[b1](lc,lc)) (x)
+// diag(R[b2](c,c)) to the ld rows of (p, ss, lc) in every column of block (c, c),
+// when R[b2] holds (c, c).  Stages: the diagonals of the boundary blocks as dense
+// vectors (one strided 1 x n tile per block: L into S0, R into S1), a clear of
+// OUT, then one K = 1 product per contribution, summed per (block, row stripe),
+// split-K partials in S2 and their sum.
+static qcm_plan* build_diag(const Idx& phys, const Idx& left_i, const Idx& right_i, const BM& psi,
+                            const std::vector<BM>& L, const std::vector<BM>& R, const MpoV& W,
+                            int64_t split_k_segs = 32) {
+    auto* P = new qcm_plan();
+    P->kind = PK_DIAG;
+    const qcm_mpo_t* m = W.m;
+    if ((int)L.size() != m->row_dim || (int)R.size() != m->col_dim)
+        throw std::runtime_error("boundary aux dimensions do not match the MPO");
+    int64_t psi_end = 0;
+    for (auto& b : psi.b) psi_end = std::max(psi_end, b.off + b.rows * b.cols);
+    P->out_elems = psi_end;
+    Idx out_left_i = index_product(phys, left_i);
+    Idx rib = right_i;
+    common_subset(out_left_i, rib);
+    PB left_pb(phys, left_i, false);
+    // diagonals of the square charge-diagonal boundary blocks
+    Stage sx; sx.kind = ST_AXPY;
+    // (bond index, charge) -> (offset, length) of the diagonal vector
+    std::vector<std::map<std::pair<int, int>, std::pair<int64_t, int64_t>>> dl(L.size()), dr(R.size());
+    int64_t l_end = 0, r_end = 0;
+    auto diag_tiles = [&](const std::vector<BM>& B, int src, int dst, int64_t& end,
+                          std::vector<std::map<std::pair<int, int>, std::pair<int64_t, int64_t>>>& where) {
+        for (size_t b = 0; b < B.size(); ++b)
+            for (const Blk& x : B[b].b) {
+                if (!(x.lc == x.rc) || x.rows != x.cols || x.rows == 0) continue;
+                AxpyOut o;
+                o.dst_buf = dst;
+                o.dst_off = end;
+                o.ldd = 1;
+                o.rows = 1;
+                o.cols = x.rows;
+                o.t_begin = (int64_t)sx.aterm.size();
+                sx.aterm.push_back({src, x.off, x.rows + 1, 1.0});
+                o.t_end = (int64_t)sx.aterm.size();
+                sx.aout.push_back(o);
+                where[b][{x.lc.n, x.lc.s}] = {end, x.rows};
+                end += x.rows;
+            }
+    };
+    diag_tiles(L, QCM_BUF_LEFT, QCM_BUF_S0, l_end, dl);
+    diag_tiles(R, QCM_BUF_RIGHT, QCM_BUF_S1, r_end, dr);
+    Stage z; z.kind = ST_ZERO; z.zbuf = QCM_BUF_OUT; z.zlen = psi_end;
+    // one output per (psi block, phys charge, diagonal entry row, lc) stripe
+    Stage sg; sg.kind = ST_GEMM;
+    struct Contrib { int b1, b2, tt, ss; double alfa; };
+    for (const Blk& ob : psi.b) {
+        if (!(ob.lc == ob.rc)) throw std::runtime_error("psi layout is not block diagonal (left-paired)");
+        const Q c = ob.lc;
+        if (!rib.has(c) || !out_left_i.has(c)) continue;
+        if (out_left_i.size_of(c) != ob.rows || rib.size_of(c) != ob.cols)
+            throw std::runtime_error("psi block does not match the product index");
+        const int jp = c.s, ip = c.s;
+        for (auto& pp : phys.d) {
+            const Q pc = pp.first;
+            const Q lin = fuse(c, neg(pc));
+            const size_t l = left_i.position(lin);
+            if (l == left_i.size()) continue;
+            const int64_t ld = left_i.d[l].second;
+            const int64_t loff = left_pb(pc, lin);
+            // contributions grouped by the operator entry's row ss
+            std::map<int, std::vector<Contrib>> per_ss;
+            for (int b2 = 0; b2 < m->col_dim; ++b2) {
+                auto rit = dr[b2].find({c.n, c.s});
+                if (rit == dr[b2].end()) continue;
+                if (rit->second.second < ob.cols) throw std::runtime_error("right boundary block smaller than psi's");
+                const int ap = W.rspin(b2);
+                for (int e = m->col_ptr[b2]; e < m->col_ptr[b2 + 1]; ++e) {
+                    const int b1 = m->row_of[e];
+                    auto lit = dl[b1].find({lin.n, lin.s});
+                    if (lit == dl[b1].end()) continue;
+                    if (lit->second.second < ld) throw std::runtime_error("left boundary block smaller than psi's");
+                    const int a = W.lspin(b1);
+                    const int i = lin.s, j = lin.s;
+                    for (int tt = m->term_ptr[e]; tt < m->term_ptr[e + 1]; ++tt) {
+                        const int op = m->term_op[tt];
+                        const int k = m->op_spin[op];
+                        const double pref = std::sqrt((ip + 1.0) * (j + 1.0) / ((i + 1.0) * (jp + 1.0))) *
+                                            m->term_scale[tt];
+                        const double c0 = pref * mod_coupling(j, std::abs(j - jp), jp, a, k, ap, i, std::abs(i - ip), ip);
+                        const double c1 = pref * mod_coupling(j, 2, jp, a, k, ap, i, 2, ip);
+                        for (int wb = m->op_blk_ptr[op]; wb < m->op_blk_ptr[op + 1]; ++wb) {
+                            Q pin(m->blk_q[4 * wb], m->blk_q[4 * wb + 1]), pout(m->blk_q[4 * wb + 2], m->blk_q[4 * wb + 3]);
+                            if (!(pin == pc) || !(pin == pout)) continue;
+                            for (int en = m->blk_ent_ptr[wb]; en < m->blk_ent_ptr[wb + 1]; ++en) {
+                                const int ss1 = m->ent[4 * en], ss2 = m->ent[4 * en + 1];
+                                if (ss1 != ss2) continue;
+                                const double alfa = m->ent_coeff[en] * (m->ent[4 * en + 2] == 2 ? c1 : c0);
+                                if ((int64_t)(ss1 + 1) * ld > pp.second * ld) throw std::runtime_error("operator entry beyond phys sector");
+                                per_ss[ss1].push_back({b1, b2, tt, ss1, alfa});
+                            }
+                        }
+                    }
+                }
+            }
+            for (auto& [ss, list] : per_ss) {
+                GemmOut o;
+                o.c_buf = QCM_BUF_OUT;
+                o.c_off = ob.off + loff + (int64_t)ss * ld;
+                o.ldc = ob.rows;
+                o.M = ld;
+                o.N = ob.cols;
+                if (loff + (int64_t)(ss + 1) * ld > ob.rows) throw std::runtime_error("diagonal stripe beyond psi block");
+                o.s_begin = (int64_t)sg.gseg.size();
+                for (const Contrib& q : list) {
+                    GemmSeg g;
+                    g.a_buf = QCM_BUF_S0; g.ta = 0; g.a_off = dl[q.b1][{lin.n, lin.s}].first; g.lda = ld;
+                    g.b_buf = QCM_BUF_S1; g.tb = 0; g.b_off = dr[q.b2][{c.n, c.s}].first; g.ldb = 1;
+                    g.K = 1;
+                    g.alpha = q.alfa;
+                    sg.gseg.push_back(g);
+                    P->gemm_flops += 2.0 * ld * ob.cols;
+                }
+                o.s_end = (int64_t)sg.gseg.size();
+                sg.gout.push_back(o);
+            }
+        }
+    }
+    Stage sr;
+    int64_t part_end = 0;
+    split_k(sg, QCM_BUF_S2, 0, split_k_segs, sr, part_end);
+    for (auto& a : sr.aout) P->axpy_bytes += 8.0 * a.rows * a.cols * (double)(a.t_end - a.t_begin + 1);
+    P->scratch[0] = l_end;
+    P->scratch[1] = r_end;
+    P->scratch[2] = part_end;
+    P->stages.push_back(std::move(sx));
+    P->stages.push_back(std::move(z));
+    P->stages.push_back(std::move(sg));
+    if (!sr.aout.empty()) P->stages.push_back(std::move(sr));
+    return P;
+}
+
 // Gradient of the local energy E = <psi| H_eff psi> (the sigma plan's
 // contraction, E = sum over psi blocks of <psi, sigma>) with respect to every
 // MPO term scale w: E is linear in each K2 coefficient alpha_k = w_tt a_k, so
@@ -1952,6 +2093,22 @@ int qcm_plan_boundary_left(const qcm_index_t* phys, const qcm_index_t* left_i, c
         return QCM_OK;
     } catch (const std::exception& e) {
         set_error(std::string("qcm_plan_boundary_left: ") + e.what());
+        *plan = nullptr;
+        return QCM_E_INVALID;
+    }
+}
+
+int qcm_plan_diagonal(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                      const qcm_blocks_t* psi, const qcm_boundary_t* left, const qcm_boundary_t* right,
+                      const qcm_mpo_t* mpo, qcm_plan** plan) {
+    if (!plan) { set_error("null plan pointer"); return QCM_E_INVALID; }
+    try {
+        MpoV W(mpo);
+        *plan = build_diag(read_index(phys), read_index(left_i), read_index(right_i), read_blocks(psi),
+                           read_boundary(left), read_boundary(right), W);
+        return QCM_OK;
+    } catch (const std::exception& e) {
+        set_error(std::string("qcm_plan_diagonal: ") + e.what());
         *plan = nullptr;
         return QCM_E_INVALID;
     }

@@ -227,7 +227,8 @@ struct Stage {
 };
 
 // PK_GRAD: gradient of <psi| H_eff |psi> with respect to every MPO term scale
-enum PlanKind { PK_SIGMA = 0, PK_BLEFT = 1, PK_BRIGHT = 2, PK_GRAD = 3 };
+// PK_DIAG: the diagonal of H_eff (FP64 only)
+enum PlanKind { PK_SIGMA = 0, PK_BLEFT = 1, PK_BRIGHT = 2, PK_GRAD = 3, PK_DIAG = 4 };
 
 }  // namespace qcm
 

@@ -240,6 +240,18 @@ class Engine:
         self.run(p, ket=ket.data, left=L, right=R, out=out, precision=precision)
         return ket.like(out)
 
+    def diagonal_hamiltonian(self, ket: DeviceMPSTensor, L: DeviceBoundary, R: DeviceBoundary, mpo) -> DeviceMPSTensor:
+        """The diagonal of H_eff in the ket's layout (``Engine::diagonal_hamiltonian``,
+        ``non-abelian/engine.hpp:221-226`` -> ``h_diag.hpp:118-158``), in FP64.  Reads
+        every L[b1] and R[b2]: the boundaries must be built with ``hermitian=False``."""
+        t0 = time.time()
+        p = N.plan_diagonal(ket.phys_i, ket.left_i, ket.right_i, ket.layout, L.layout, R.layout, self.fmpo(mpo))
+        p.upload()
+        self.plan_seconds += time.time() - t0
+        out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=self.device)
+        self.run(p, ket=ket.data, left=L, right=R, out=out, precision=N.PREC_FP64)
+        return ket.like(out)
+
     def zerosite_hamil2(self, bond: DeviceBlockMatrix, L: DeviceBoundary, R: DeviceBoundary, mpo_left, mpo_right,
                         out: Optional[torch.Tensor] = None, precision=None) -> DeviceBlockMatrix:
         """sigma = H_eff C for the bond matrix C between sites i and i+1

@@ -73,6 +73,9 @@ def lib():
     L.qcm_plan_sigma_opts.argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks), C.POINTER(CBoundary),
                                                               C.POINTER(CBoundary), C.POINTER(CMpo), C.c_int32,
                                                               C.c_void_p, C.POINTER(C.c_void_p)]
+    L.qcm_plan_diagonal.argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks), C.POINTER(CBoundary),
+                                                            C.POINTER(CBoundary), C.POINTER(CMpo),
+                                                            C.POINTER(C.c_void_p)]
     L.qcm_plan_zerosite.argtypes = [C.POINTER(CBlocks), C.POINTER(CBoundary), C.POINTER(CBoundary),
                                     C.POINTER(CMpo), C.POINTER(CMpo), C.c_int32, C.POINTER(C.c_void_p)]
     L.qcm_mpo_twosite_begin.argtypes = [C.POINTER(CMpo), C.POINTER(CMpo), C.POINTER(C.c_void_p), i32p]
@@ -636,6 +639,17 @@ def plan_boundary_tensor_mpo(phys, left_i, right_i, mps: Layout, B: BoundaryLayo
     return Plan(h, "btm_" + side)
 
 
+def plan_diagonal(phys: Index, left_i: Index, right_i: Index, psi: Layout, L: BoundaryLayout, R: BoundaryLayout,
+                  mpo: FMpo) -> Plan:
+    """``diagonal_hamiltonian``: the diagonal of H_eff in psi's layout (FP64; the
+    boundaries must hold every bond index)."""
+    fp, fl, fr = FIndex(phys), FIndex(left_i), FIndex(right_i)
+    h = C.c_void_p()
+    check(lib().qcm_plan_diagonal(C.byref(fp.c), C.byref(fl.c), C.byref(fr.c), C.byref(psi.c), C.byref(L.c),
+                                  C.byref(R.c), C.byref(mpo.c), C.byref(h)), "qcm_plan_diagonal")
+    return Plan(h, "diag")
+
+
 def plan_zerosite(bond: Layout, L: BoundaryLayout, R: BoundaryLayout, mpo_left: FMpo, mpo_right: FMpo,
                   hermitian=True) -> Plan:
     """``zerosite_hamil2``: sigma = H_eff C for the bond matrix C (layout ``bond``), the
@@ -648,4 +662,4 @@ def plan_zerosite(bond: Layout, L: BoundaryLayout, R: BoundaryLayout, mpo_left: 
 
 __all__ = ["lib", "check", "Layout", "BoundaryLayout", "FMpo", "FIndex", "Plan", "plan_sigma",
            "plan_boundary_left", "plan_boundary_right", "plan_boundary_tensor_mpo", "plan_energy_gradient",
-           "plan_merge", "plan_zerosite", "make_twosite_fmpo", "make_ts_cache_fmpo", "PREC_BF16X2", "PREC_FP64", "PREC_TF32", "PREC_BF16X3"]
+           "plan_merge", "plan_zerosite", "plan_diagonal", "make_twosite_fmpo", "make_ts_cache_fmpo", "PREC_BF16X2", "PREC_FP64", "PREC_TF32", "PREC_BF16X3"]

@@ -1,9 +1,11 @@
 """The zero-site problem on the GPU (``qcm_plan_zerosite`` through
 ``Engine.zerosite_hamil2`` / ``ZeroSiteProblem``) against the oracle's
 ``zerosite_hamil``: FP64 to 1e-12 relative, the tensor-core forms to their
-stated accuracy, and the energy identity of ``test_siteproblem.cpp:97-154``."""
+stated accuracy, and the energy identity of ``test_siteproblem.cpp:97-154``;
+and the diagonal of H_eff (``qcm_plan_diagonal``) against the oracle's."""
 import numpy as np
 import pytest
+import torch
 
 from oracle import dmrg_ref as R
 from oracle.sweep import expval, overlap
@@ -42,3 +44,26 @@ def test_zero_site_mixed_forms(prec, tol):
     got = eng.zerosite_hamil2(x, zsp.left, zsp.right, zsp.mpo_left, zsp.mpo_right,
                               precision=getattr(N, "PREC_" + prec)).data.cpu().numpy()
     assert np.linalg.norm(got - want) <= tol * np.linalg.norm(want)
+
+
+@pytest.mark.parametrize("site,m", [(2, 16), (3, 24)])
+def test_diagonal_hamiltonian_matches_oracle(site, m):
+    """``qcm_plan_diagonal`` through ``Engine.diagonal_hamiltonian`` (full boundaries)
+    against the oracle's ``diagonal_hamiltonian``, FP64 to 1e-12 relative; a mixed
+    form is refused."""
+    from qcmaquis_gb300 import native as N
+    from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
+    from test_oracle import _random_site_problem
+    psi, left, right, ts = _random_site_problem(site=site, m=m, herm=False)
+    psi = psi.copy().make_left_paired()
+    eng = Engine("cuda:0", hermitian=False)
+    x = DeviceMPSTensor.from_host(psi, "cuda:0")
+    Lb, Rb = DeviceBoundary.from_host(left, "cuda:0"), DeviceBoundary.from_host(right, "cuda:0")
+    got = eng.diagonal_hamiltonian(x, Lb, Rb, ts).data.cpu().numpy()
+    want = x.layout.pack(R.diagonal_hamiltonian(left, right, ts, psi))
+    assert np.linalg.norm(got - want) <= 1e-12 * np.linalg.norm(want)
+    p = N.plan_diagonal(psi.phys_i, psi.left_i, psi.right_i, x.layout, Lb.layout, Rb.layout, eng.fmpo(ts))
+    p.upload()
+    with pytest.raises(RuntimeError, match="FP64 form only"):
+        eng.run(p, ket=x.data, left=Lb, right=Rb, out=torch.empty(p.out_elems, dtype=torch.float64, device="cuda:0"),
+                precision=N.PREC_BF16X3)

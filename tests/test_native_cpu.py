@@ -163,6 +163,22 @@ def test_zero_site_plan_matches_oracle(herm, bond, images):
     assert np.linalg.norm(bufs[3] - ref) <= (1e-7 if images else 1e-13) * np.linalg.norm(ref)
 
 
+
+@pytest.mark.parametrize("site,m", [(2, 8), (3, 12)])
+def test_diagonal_plan_matches_oracle(site, m):
+    """qcm_plan_diagonal against the oracle's diagonal_hamiltonian (full boundaries)."""
+    psi, left, right, ts = _random_site_problem(site=site, m=m, herm=False)
+    psi = psi.copy().make_left_paired()
+    lay, Ll, Rl = N.Layout.of(psi.data), N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
+    p = N.plan_diagonal(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, N.FMpo(ts))
+    assert [st[0] for st in p.stages()][:3] == ["axpy", "zero", "gemm"]
+    bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.full(p.out_elems, np.nan)] + \
+        [np.full(max(s, 1), np.nan) for s in p.scratch]
+    run_plan(p, bufs)
+    ref = lay.pack(R.diagonal_hamiltonian(left, right, ts, psi))
+    assert np.linalg.norm(bufs[3] - ref) <= 1e-13 * np.linalg.norm(ref)
+
+
 def test_zero_site_plan_rejects_mismatched_bond():
     _, Cm, left, right, mpo = _zero_site_problem(bond=2)
     lay, Ll, Rl = N.Layout.of(Cm), N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)

@@ -217,3 +217,26 @@ def test_oracle_excited_states_match_fci_L6():
                      ortho_states=[s0, s1])
     assert abs(r1.sweep_energy[-1] - exact[1]) < 1e-9
     assert abs(r2.sweep_energy[-1] - exact[2]) < 1e-9
+
+
+@pytest.mark.parametrize("site,m", [(2, 8), (1, 12)])
+def test_diagonal_hamiltonian_is_the_diagonal_of_sigma(site, m):
+    """``ref_diag`` (``fw/optimize/ietl_davidson.h:25-58``): every element of
+    ``diagonal_hamiltonian`` equals (H e_ij)(i, j) for the unit tensor e_ij, to 1e-12
+    (full boundaries)."""
+    psi, left, right, ts = _random_site_problem(site=site, m=m, herm=False)
+    psi = psi.copy().make_left_paired()
+    d = R.diagonal_hamiltonian(left, right, ts, psi)
+    assert d.keys == psi.data.keys
+    rng = np.random.default_rng(site)
+    for key, blk in zip(psi.data.keys, psi.data.blocks):
+        r, c = blk.shape
+        for _ in range(3):
+            i, j = int(rng.integers(r)), int(rng.integers(c))
+            e = psi.copy()
+            for q in range(e.data.n_blocks()):
+                e.data.blocks[q] = np.zeros_like(e.data.blocks[q])
+            e.data.blocks[e.data.find_block(*key)][i, j] = 1.0
+            h = R.site_hamil2(e, left, right, ts, is_hermitian=False).make_left_paired()
+            want = h.data.blocks[h.data.find_block(*key)][i, j]
+            assert abs(d.blocks[d.find_block(*key)][i, j] - want) < 1e-12 * max(1.0, abs(want))
