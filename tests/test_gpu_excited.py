@@ -40,3 +40,23 @@ def test_gpu_excited_states_match_oracle_and_fci_L6():
     orec, _ = oracle_run(model, mpo, OP(nsweeps=3, max_bond_dimension=64, seed=5), nelec=Ne, ortho_states=[ogs])
     assert np.max(np.abs(np.array(rec.energies) - np.array(orec.energies))) < 1e-9
     assert abs(rec.sweep_energy[-1] - fci_energies(L, ints, Ne, 0, 2)[1]) < 1e-9
+
+
+def test_gpu_constrained_jcd_skip_and_empty_constraint():
+    """The device eigensolver's constraint handling: a start vector inside the
+    constraint span skips the solve (<init|H|init>, 0 iterations); a zero constraint
+    is dropped and leaves the solve unchanged."""
+    import torch
+    from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine, SiteProblem
+    from qcmaquis_gb300.jd import solve_ietl_jcd
+    from test_oracle import _random_site_problem
+    psi, left, right, ts = _random_site_problem()
+    x = DeviceMPSTensor.from_host(psi.copy().make_left_paired(), "cuda:0")
+    eng = Engine("cuda:0")
+    sp = SiteProblem(eng, DeviceBoundary.from_host(left, "cuda:0"), DeviceBoundary.from_host(right, "cuda:0"), ts)
+    th, _, it = solve_ietl_jcd(sp, x, 1e-8, 6, ortho=[2.0 * x.data])
+    ref = float(torch.dot(x.data, sp.apply(x).data))
+    assert it == 0 and abs(th - ref) < 1e-12 * max(1.0, abs(ref))
+    t1, _, i1 = solve_ietl_jcd(sp, x, 1e-8, 6)
+    t2, _, i2 = solve_ietl_jcd(sp, x, 1e-8, 6, ortho=[torch.zeros_like(x.data)])
+    assert i1 == i2 and abs(t1 - t2) < 1e-10 * abs(t1)

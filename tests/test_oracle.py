@@ -240,3 +240,18 @@ def test_diagonal_hamiltonian_is_the_diagonal_of_sigma(site, m):
             h = R.site_hamil2(e, left, right, ts, is_hermitian=False).make_left_paired()
             want = h.data.blocks[h.data.find_block(*key)][i, j]
             assert abs(d.blocks[d.find_block(*key)][i, j] - want) < 1e-12 * max(1.0, abs(want))
+
+
+def test_constrained_jcd_skips_a_fully_constrained_start():
+    """``ietl_jacobi_davidson.h:41-47, 58-64``: when the constraints remove the whole start
+    vector the solve is skipped and <init|H|init> returned with ``init``; a constraint
+    the start vector is orthogonal to leaves the solve unchanged."""
+    psi, left, right, ts = _random_site_problem()
+    apply_h = lambda x: R.site_hamil2(x, left, right, ts)
+    x0 = psi.copy().make_left_paired()
+    theta, u, it = R.jcd_solve(apply_h, x0, 1e-8, 6, ortho=[x0.scaled(2.0)])
+    assert it == 0 and abs(theta - x0.dot(apply_h(x0))) < 1e-12 * max(1.0, abs(theta))
+    zero = x0.scaled(0.0)
+    t1, _, i1 = R.jcd_solve(apply_h, x0, 1e-8, 6)
+    t2, _, i2 = R.jcd_solve(apply_h, x0, 1e-8, 6, ortho=[zero])
+    assert i1 == i2 and abs(t1 - t2) < 1e-12 * abs(t1)
