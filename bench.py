@@ -259,6 +259,7 @@ def run_sweep(args):
                      "truncation": trunc, "seconds_by_part": rec.seconds,
                      "repeated_layouts": len(rec.layout_digests) - len(set(rec.layout_digests)),
                      "plan_hits": rec.plan_hits,
+                     "boundary_plan_hits": rec.boundary_plan_hits,
                      "microiterations": len(rec.layout_digests)}
         del mps
         torch.cuda.empty_cache()

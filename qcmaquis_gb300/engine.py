@@ -166,6 +166,10 @@ class Engine:
         self.plan_cache_size = 2     # sigma plans kept (least recently used dropped first)
         self.autotuner = None        # autotune.Autotuner: measured plan shapes per problem shape
         self.plan_hits = 0
+        # boundary-step plans kept, keyed like the sigma plans (0: none, the default)
+        self.boundary_plan_cache_size = 0
+        self.boundary_plan_hits = 0
+        self._bplans: Dict[tuple, N.Plan] = {}
         self._mpo_cache: Dict[int, N.FMpo] = {}
         self.launches = 0
 
@@ -277,16 +281,34 @@ class Engine:
         self.run(p, ket=bond.data, left=L, right=R, out=out, precision=precision)
         return bond.like(out)
 
+    def _boundary_plan(self, side: str, mps: DeviceMPSTensor, B: DeviceBoundary, mpo) -> N.Plan:
+        """A boundary-step plan, from the cache when ``boundary_plan_cache_size`` > 0 and a
+        step with the same indices, layouts and MPO tensor was planned before."""
+        key = (side, _digest(mps.phys_i, mps.left_i, mps.right_i, mps.layout), _digest(B.layout), id(mpo),
+               self.hermitian)
+        p = self._bplans.get(key) if self.boundary_plan_cache_size > 0 else None
+        if p is not None:
+            self._bplans[key] = self._bplans.pop(key)   # most recently used last
+            self.boundary_plan_hits += 1
+            return p
+        t0 = time.time()
+        build = N.plan_boundary_left if side == "left" else N.plan_boundary_right
+        p = build(mps.phys_i, mps.left_i, mps.right_i, mps.layout, B.layout, self.fmpo(mpo), self.hermitian)
+        p.upload()
+        self.plan_seconds += time.time() - t0
+        if self.boundary_plan_cache_size > 0:
+            p._keep = (mpo,)
+            while self._bplans and len(self._bplans) >= self.boundary_plan_cache_size:
+                self._bplans.pop(next(iter(self._bplans)))
+            self._bplans[key] = p
+        return p
+
     def overlap_mpo_left_step(self, mps: DeviceMPSTensor, L: DeviceBoundary, mpo,
                               precision: int = N.PREC_FP64) -> DeviceBoundary:
         """L[i+1] from L[i], A[i], W[i] (``Engine::overlap_mpo_left_step``, bra = ket).
         The boundary is stored in FP64; ``precision`` selects the arithmetic of its
         block products (the mixed forms: FP32 intermediates, tensor-core products)."""
-        t0 = time.time()
-        p = N.plan_boundary_left(mps.phys_i, mps.left_i, mps.right_i, mps.layout, L.layout, self.fmpo(mpo),
-                                 self.hermitian)
-        p.upload()
-        self.plan_seconds += time.time() - t0
+        p = self._boundary_plan("left", mps, L, mpo)
         lay = p.out_layout()
         out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=self.device)
         self.run(p, ket=mps.data, left=L, out=out, precision=precision)
@@ -296,11 +318,7 @@ class Engine:
                                precision: int = N.PREC_FP64) -> DeviceBoundary:
         """R[i] from R[i+1], B[i], W[i] (``Engine::overlap_mpo_right_step``, bra = ket);
         ``precision`` as for ``overlap_mpo_left_step``."""
-        t0 = time.time()
-        p = N.plan_boundary_right(mps.phys_i, mps.left_i, mps.right_i, mps.layout, R.layout, self.fmpo(mpo),
-                                  self.hermitian)
-        p.upload()
-        self.plan_seconds += time.time() - t0
+        p = self._boundary_plan("right", mps, R, mpo)
         lay = p.out_layout()
         out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=self.device)
         self.run(p, ket=mps.data, right=R, out=out, precision=precision)

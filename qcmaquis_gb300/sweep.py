@@ -91,6 +91,7 @@ class SweepRecord:
     sweep_seconds: List[float] = field(default_factory=list)
     sigma_calls: int = 0
     plan_hits: int = 0
+    boundary_plan_hits: int = 0
     # per microiteration: a digest of the sigma problem's layouts (psi, L, R) -- equal
     # digests at the same site in different sweeps could share one plan
     layout_digests: List[int] = field(default_factory=list)
@@ -185,8 +186,9 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
     ``checkpoint`` (a directory) saves the MPS and the sweep status after every
     sweep (``sim.hpp:197-211``); ``start_sweep`` resumes a run at that sweep of
     its schedule (``mps`` from ``checkpoint.load``, sweeps start_sweep..nsweeps-1).
-    ``plan_cache`` > 0 keeps that many sigma plans, keyed by their layouts, so a
-    site problem whose layouts recur in a later sweep reuses its plan.
+    ``plan_cache`` > 0 keeps that many sigma plans and that many boundary-step plans,
+    keyed by their layouts, so a site problem or boundary step whose layouts recur
+    in a later sweep reuses its plan.
     ``ortho_states``: device MPSs the state is optimised orthogonal to (excited
     states, ``n_ortho_states`` / ``ortho_states``,
     ``sba/SweepBasedEnergyMinimization.h:52-67``; ``excited.OverlapBoundaries``)."""
@@ -195,6 +197,7 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
     engine = engine or Engine(device, precision=precision)
     if plan_cache > 0:
         engine.plan_cache_size = plan_cache
+        engine.boundary_plan_cache_size = plan_cache
     engine_full = Engine(device, hermitian=False)
     bprec = 0 if boundary_precision is None else boundary_precision
     right_end = (nelec, twoS)
@@ -283,6 +286,7 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
         torch.cuda.synchronize()
         rec.sweep_seconds.append(time.time() - t0)
         rec.plan_hits = engine.plan_hits
+        rec.boundary_plan_hits = engine.boundary_plan_hits
         e = expval(mps, mpo, engine_full, right_end) / overlap(mps) + mpo.core_energy
         rec.sweep_energy.append(e)
         rec.sweep_truncated_weight.append(max(rec.truncated_weight[-nmicro:]))

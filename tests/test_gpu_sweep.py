@@ -103,3 +103,18 @@ def test_gpu_single_site_sweep_matches_oracle():
     # (~1e-17) that fall on either side of the cut; the kept weight cannot
     tw_g, tw_r = np.array(gpu.truncated_weight), np.array(ref.truncated_weight)
     assert np.all(np.abs(tw_g - tw_r) <= TW_REL * np.abs(tw_r) + TW_ABS)
+
+
+def test_gpu_sweep_with_plan_caches_is_unchanged():
+    """``run_dmrg(plan_cache=n)`` reuses sigma and boundary-step plans whose layouts
+    recur; the plans are the same tables, so every energy equals the uncached one."""
+    from qcmaquis_gb300 import sweep as G
+    L, Ne = 6, 6
+    model = QCModel(L, synthetic_integral_map(L, seed=3), Ne)
+    mpo = make_mpo(model)
+    p = G.SweepParams(nsweeps=4, max_bond_dimension=24)
+    plain, _ = G.run_dmrg(model, mpo, p, nelec=Ne)
+    cached, _ = G.run_dmrg(model, mpo, p, nelec=Ne, plan_cache=64)
+    assert cached.boundary_plan_hits > 0 and cached.plan_hits > 0
+    assert np.max(np.abs(np.array(cached.energies) - np.array(plain.energies))) < 1e-12
+    assert np.max(np.abs(np.array(cached.sweep_energy) - np.array(plain.sweep_energy))) < 1e-12
