@@ -241,3 +241,19 @@ def test_native_twosite_mpo_rejects_unshared_bond():
     mpo = make_mpo(model)
     with pytest.raises(RuntimeError, match="do not share a bond"):
         N.make_twosite_fmpo(N.FMpo(mpo[0]), N.FMpo(mpo[2]), model.phys)
+
+
+@pytest.mark.parametrize("name", ["h2", "lih"])
+def test_native_twosite_mpo_on_the_golden_systems(golden, name):
+    """The native two-site builder on the reference's H2 (L=2, one pair) and LiH
+    (L=4) systems equals the Python builder array for array."""
+    from conftest import integral_map
+    from qcmaquis_gb300.mpo import make_twosite_mpo
+    g = golden[name]
+    model = QCModel(g["L"], integral_map(g["integrals"]), g["nelec"])
+    mpo = make_mpo(model)
+    for p in range(g["L"] - 1):
+        ref = N.FMpo(make_twosite_mpo(mpo[p], mpo[p + 1], model.phys, model.phys))
+        got = N.make_twosite_fmpo(N.FMpo(mpo[p]), N.FMpo(mpo[p + 1]), model.phys)
+        for k in _FMPO_ARRAYS:
+            assert np.array_equal(getattr(ref, k), getattr(got, k)), (p, k)
