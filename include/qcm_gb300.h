@@ -204,6 +204,12 @@ int qcm_mpo_twosite_finish(qcm_mpo_buf* buf, const qcm_mpo_t* products);
 int qcm_mpo_buf_view(const qcm_mpo_buf* buf, qcm_mpo_t* view, int64_t* sizes);
 int qcm_mpo_buf_term_pos(const qcm_mpo_buf* buf, int32_t* pos);
 void qcm_mpo_buf_destroy(qcm_mpo_buf* buf);
+/* The three steps in one call, the SU(2) op_kron (site_operator_algorithms.h) in
+ * native code too: phys1, phys2 are the two sites' local indices.  Its Wigner
+ * symbols are long-double Racah sums, so coefficients can differ from an
+ * exact-rational evaluation in the last bits.  View and destroy as above. */
+int qcm_mpo_twosite(const qcm_mpo_t* w1, const qcm_mpo_t* w2, const qcm_index_t* phys1, const qcm_index_t* phys2,
+                    qcm_mpo_buf** out);
 
 /* Diagonal of H_eff (Engine::diagonal_hamiltonian, dmrg/framework/dmrg/mp_tensors/
  * contractions/non-abelian/engine.hpp:221-226 -> SU2::diagonal_hamiltonian,

@@ -12,7 +12,9 @@
 #include <algorithm>
 #include <array>
 #include <cstdlib>
+#include <cmath>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -222,6 +224,137 @@ void phase2(qcm_mpo_buf& B, const qcm_mpo_t* prods) {
     B.built = true;
 }
 
+// The operators of a flattened tensor's products, in the qcm_mpo_t operator layout.
+struct ProdOps {
+    std::vector<int32_t> op_spin, op_blk_ptr{0}, blk_q, blk_ent_ptr{0}, ent;
+    std::vector<double> ent_coeff;
+    qcm_mpo_t view() const {
+        qcm_mpo_t v;
+        std::memset(&v, 0, sizeof(v));
+        v.n_ops = (int32_t)op_spin.size();
+        v.op_spin = op_spin.data();
+        v.op_blk_ptr = op_blk_ptr.data();
+        v.blk_q = blk_q.data();
+        v.blk_ent_ptr = blk_ent_ptr.data();
+        v.ent = ent.data();
+        v.ent_coeff = ent_coeff.data();
+        return v;
+    }
+};
+
+struct DenseBlock { Q in, out; int64_t rows, cols; std::vector<double> v; };  // row-major
+
+std::vector<DenseBlock> dense_op(const qcm_mpo_t* w, int o, const qcm::Idx& phys) {
+    std::vector<DenseBlock> r;
+    for (int kb = w->op_blk_ptr[o]; kb < w->op_blk_ptr[o + 1]; ++kb) {
+        DenseBlock b;
+        b.in = Q(w->blk_q[4 * kb], w->blk_q[4 * kb + 1]);
+        b.out = Q(w->blk_q[4 * kb + 2], w->blk_q[4 * kb + 3]);
+        b.rows = phys.size_of(b.in);
+        b.cols = phys.size_of(b.out);
+        b.v.assign((size_t)(b.rows * b.cols), 0.0);
+        for (int en = w->blk_ent_ptr[kb]; en < w->blk_ent_ptr[kb + 1]; ++en) {
+            const int r0 = w->ent[4 * en], c0 = w->ent[4 * en + 1];
+            if (r0 < 0 || r0 >= b.rows || c0 < 0 || c0 >= b.cols) throw std::runtime_error("operator entry outside its block");
+            b.v[(size_t)(r0 * b.cols + c0)] = w->ent_coeff[en];
+        }
+        r.push_back(std::move(b));
+    }
+    return r;
+}
+
+// The small identity of a spin-0 operator next to a spin > 0 one is extended by the
+// two off-diagonal unit entries between the second and third local charges
+// (site_operator_algorithms.h:238-256).
+void expand_identity(std::vector<DenseBlock>& op, const qcm::Idx& phys) {
+    if (phys.size() < 3) return;
+    const Q cb = phys.d[1].first, cc = phys.d[2].first;
+    for (auto& b : op)
+        if (b.in == cb && b.out == cc) return;
+    op.push_back({cb, cc, 1, 1, {1.0}});
+    op.push_back({cc, cb, 1, 1, {1.0}});
+}
+
+int product_spin(Q a, Q b) { return (a.s == -1 && b.s == 1) ? 2 : std::abs(a.s + b.s); }
+
+double mod_coupling9(int a, int b, int c, int d, int e, int f, int g, int h, int i) {
+    return std::sqrt((g + 1.0) * (h + 1.0) * (c + 1.0) * (f + 1.0)) * qcm::wigner9j(a, b, c, d, e, f, g, h, i);
+}
+
+// op_kron for SU(2) (site_operator_algorithms.h): the spin-coupled Kronecker product
+// of operator o1 of W1 and o2 of W2 for bond spins (j, jpp, jp) and product spin k.
+void op_kron(const qcm_mpo_t* w1, const qcm_mpo_t* w2, int o1, int o2, int j, int jpp, int jp, int k,
+             const qcm::Idx& p1, const qcm::Idx& p2, const qcm::PB& pb, ProdOps& out) {
+    std::vector<DenseBlock> A = dense_op(w1, o1, p1), Bo = dense_op(w2, o2, p2);
+    const int k1 = w1->op_spin[o1], k2 = w2->op_spin[o2];
+    if (k1 > 0 && k2 == 0) expand_identity(Bo, p2);
+    if (k1 == 0 && k2 > 0) expand_identity(A, p1);
+    struct Acc { int64_t rows, cols; std::vector<double> v; std::vector<int32_t> rs, cs; };
+    std::map<std::pair<Q, Q>, Acc, std::function<bool(const std::pair<Q, Q>&, const std::pair<Q, Q>&)>> blocks(
+        [](const std::pair<Q, Q>& x, const std::pair<Q, Q>& y) {
+            return x.first > y.first || (x.first == y.first && x.second > y.second);   // DualIndex order
+        });
+    for (const DenseBlock& a : A)
+        for (const DenseBlock& b : Bo) {
+            const Q nl = qcm::fuse(a.in, b.in), nr = qcm::fuse(a.out, b.out);
+            auto it = blocks.find({nl, nr});
+            if (it == blocks.end()) {
+                Acc z;
+                z.rows = pb.size(nl);
+                z.cols = pb.size(nr);
+                z.v.assign((size_t)(z.rows * z.cols), 0.0);
+                z.rs.assign((size_t)z.rows, 0);
+                z.cs.assign((size_t)z.cols, 0);
+                it = blocks.emplace(std::make_pair(nl, nr), std::move(z)).first;
+            }
+            Acc& t = it->second;
+            const int64_t io = pb(a.in, b.in), oo = pb(a.out, b.out);
+            const int J = product_spin(a.in, b.in), Jp = product_spin(a.out, b.out);
+            const double c9 = mod_coupling9(std::abs(a.in.s), std::abs(b.in.s), J, k1, k2, k, std::abs(a.out.s),
+                                            std::abs(b.out.s), Jp);
+            for (int64_t l1 = 0; l1 < a.rows; ++l1)
+                for (int64_t r1 = 0; r1 < a.cols; ++r1)
+                    for (int64_t l2 = 0; l2 < b.rows; ++l2)
+                        for (int64_t r2 = 0; r2 < b.cols; ++r2) {
+                            const int64_t row = io + l1 * b.rows + l2, col = oo + r1 * b.cols + r2;
+                            t.v[(size_t)(row * t.cols + col)] = (b.v[(size_t)(l2 * b.cols + r2)] *
+                                                                 a.v[(size_t)(l1 * a.cols + r1)]) * c9;
+                        }
+            t.rs[(size_t)io] = J;
+            t.cs[(size_t)oo] = Jp;
+        }
+    double c6 = std::sqrt((jpp + 1.0) * (k + 1.0)) * qcm::wigner6j(j, jp, k, k2, k1, jpp);
+    if (((j + jp + k1 + k2) / 2) % 2) c6 = -c6;
+    out.op_spin.push_back(k);
+    for (auto& [key, t] : blocks) {
+        bool any = false;
+        for (double& x : t.v) {
+            x = x * c6;
+            if (x != 0.0) any = true;
+        }
+        if (!any) continue;   // remove_empty_blocks
+        out.blk_q.insert(out.blk_q.end(), {key.first.n, key.first.s, key.second.n, key.second.s});
+        for (int64_t r0 = 0; r0 < t.rows; ++r0)
+            for (int64_t c0 = 0; c0 < t.cols; ++c0) {
+                const double x = t.v[(size_t)(r0 * t.cols + c0)];
+                if (x == 0.0) continue;
+                out.ent.insert(out.ent.end(), {(int32_t)r0, (int32_t)c0, t.rs[(size_t)r0], t.cs[(size_t)c0]});
+                out.ent_coeff.push_back(x);
+            }
+        out.blk_ent_ptr.push_back((int32_t)out.ent_coeff.size());
+    }
+    out.op_blk_ptr.push_back((int32_t)out.blk_ent_ptr.size() - 1);
+}
+
+qcm::Idx read_idx(const qcm_index_t* x) {
+    qcm::Idx r;
+    if (!x) throw std::runtime_error("null index");
+    for (int i = 0; i < x->n; ++i) r.d.push_back({Q(x->q[2 * i], x->q[2 * i + 1]), x->size[i]});
+    for (size_t i = 1; i < r.d.size(); ++i)
+        if (!(r.d[i - 1].first > r.d[i].first)) throw std::runtime_error("index not sorted descending");
+    return r;
+}
+
 }  // namespace
 
 extern "C" {
@@ -295,6 +428,33 @@ int qcm_mpo_buf_term_pos(const qcm_mpo_buf* B, int32_t* pos) {
     if (!B || !pos || !B->built) { set_error("qcm_mpo_buf_term_pos: no built tensor"); return QCM_E_INVALID; }
     std::memcpy(pos, B->term_pos.data(), B->term_pos.size() * sizeof(int32_t));
     return QCM_OK;
+}
+
+int qcm_mpo_twosite(const qcm_mpo_t* w1, const qcm_mpo_t* w2, const qcm_index_t* phys1, const qcm_index_t* phys2,
+                    qcm_mpo_buf** out) {
+    if (!out) { set_error("qcm_mpo_twosite: null output"); return QCM_E_INVALID; }
+    *out = nullptr;
+    auto* B = new qcm_mpo_buf();
+    try {
+        check_mpo(w1, "left MPO tensor");
+        check_mpo(w2, "right MPO tensor");
+        const qcm::Idx p1 = read_idx(phys1), p2 = read_idx(phys2);
+        const qcm::PB pb(p1, p2, false);
+        phase1(*B, w1, w2);
+        ProdOps prods;
+        for (size_t q = 0; q + 5 < B->keys.size(); q += 6) {
+            const int32_t* k = &B->keys[q];
+            op_kron(w1, w2, k[0], k[1], k[2], k[3], k[4], k[5], p1, p2, pb, prods);
+        }
+        const qcm_mpo_t v = prods.view();
+        phase2(*B, &v);
+        *out = B;
+        return QCM_OK;
+    } catch (const std::exception& e) {
+        delete B;
+        set_error(std::string("qcm_mpo_twosite: ") + e.what());
+        return QCM_E_INVALID;
+    }
 }
 
 void qcm_mpo_buf_destroy(qcm_mpo_buf* B) { delete B; }

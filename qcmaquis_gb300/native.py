@@ -83,6 +83,8 @@ def lib():
     L.qcm_mpo_twosite_finish.argtypes = [C.c_void_p, C.POINTER(CMpo)]
     L.qcm_mpo_buf_view.argtypes = [C.c_void_p, C.POINTER(CMpo), i64p]
     L.qcm_mpo_buf_term_pos.argtypes = [C.c_void_p, i32p]
+    L.qcm_mpo_twosite.argtypes = [C.POINTER(CMpo), C.POINTER(CMpo), C.POINTER(CIndex), C.POINTER(CIndex),
+                                  C.POINTER(C.c_void_p)]
     L.qcm_mpo_buf_destroy.argtypes = [C.c_void_p]
     L.qcm_mpo_buf_destroy.restype = None
     L.qcm_plan_merge.argtypes = [C.POINTER(C.c_void_p), C.c_int32, i64p, C.POINTER(C.c_void_p)]
@@ -345,16 +347,32 @@ def _copy(ptr, n, dtype):
     return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
 
 
-def make_twosite_fmpo(w1: FMpo, w2: FMpo, phys1: Index, phys2: Index = None) -> FMpo:
+def make_twosite_fmpo(w1: FMpo, w2: FMpo, phys1: Index, phys2: Index = None, native_kron: bool = False) -> FMpo:
     """The flattened two-site MPO tensor of W1 (x) W2 (``make_twosite_mpo``,
-    ``mp_tensors/ts_ops.h:78-152``) from the native builder: the distinct
-    spin-coupled Kronecker products are formed here by ``op_kron_su2``, the
-    chain walk and the sums run in ``qcm_mpo_twosite_*``.  Term for term the
-    result equals ``FMpo(make_twosite_mpo(...))``."""
-    from .site_operator import SpinDescriptor, op_kron_su2
+    ``mp_tensors/ts_ops.h:78-152``) from the native builder.  The chain walk and
+    the sums run in ``qcm_mpo_twosite_*``; the distinct spin-coupled Kronecker
+    products are formed here by ``op_kron_su2`` (term for term the result then
+    equals ``FMpo(make_twosite_mpo(...))``), or with ``native_kron`` in native
+    code too (``qcm_mpo_twosite``: its Wigner symbols are long-double sums, so
+    coefficients can differ from the exact-rational ones in the last bits)."""
     phys2 = phys1 if phys2 is None else phys2
     L = lib()
     h = C.c_void_p()
+    if native_kron:
+        f1, f2 = FIndex(phys1), FIndex(phys2)
+        check(L.qcm_mpo_twosite(C.byref(w1.c), C.byref(w2.c), C.byref(f1.c), C.byref(f2.c), C.byref(h)),
+              "qcm_mpo_twosite")
+    else:
+        _twosite_products(L, w1, w2, phys1, phys2, h)
+    try:
+        return _fmpo_from_buf(L, h)
+    finally:
+        L.qcm_mpo_buf_destroy(h)
+
+
+def _twosite_products(L, w1: FMpo, w2: FMpo, phys1: Index, phys2: Index, h):
+    """qcm_mpo_twosite_begin / _keys / _finish with the products formed by op_kron_su2."""
+    from .site_operator import SpinDescriptor, op_kron_su2
     nk = C.c_int32()
     check(L.qcm_mpo_twosite_begin(C.byref(w1.c), C.byref(w2.c), C.byref(h), C.byref(nk)), "qcm_mpo_twosite_begin")
     try:
@@ -385,34 +403,40 @@ def make_twosite_fmpo(w1: FMpo, w2: FMpo, phys1: Index, phys2: Index = None) -> 
             setattr(prods, k, _p(arrs[k], i32p))
         prods.ent_coeff = _p(arrs["ent_coeff"], f64p)
         check(L.qcm_mpo_twosite_finish(h, C.byref(prods)), "qcm_mpo_twosite_finish")
-        v = CMpo()
-        sz = (C.c_int64 * 4)()
-        check(L.qcm_mpo_buf_view(h, C.byref(v), sz), "qcm_mpo_buf_view")
-        ne, nt, nb, nent = sz[0], sz[1], sz[2], sz[3]
-        f = FMpo.__new__(FMpo)
-        f.mpo = _FlatTensor(v.row_dim, v.col_dim)
-        f.left_spin = _copy(v.left_spin, v.row_dim, np.int32)
-        f.right_spin = _copy(v.right_spin, v.col_dim, np.int32)
-        f.left_herm = _copy(v.left_herm, v.row_dim, np.int32)
-        f.right_herm = _copy(v.right_herm, v.col_dim, np.int32)
-        f.left_phase = _copy(v.left_phase, v.row_dim, np.int32)
-        f.right_phase = _copy(v.right_phase, v.col_dim, np.int32)
-        f.col_ptr = _copy(v.col_ptr, v.col_dim + 1, np.int32)
-        f.row_of = _copy(v.row_of, ne, np.int32)
-        f.term_ptr = _copy(v.term_ptr, ne + 1, np.int32)
-        f.term_op = _copy(v.term_op, nt, np.int32)
-        f.term_scale = _copy(v.term_scale, nt, np.float64)
-        f.n_ops = v.n_ops
-        f.op_spin = _copy(v.op_spin, nt, np.int32)
-        f.op_blk_ptr = _copy(v.op_blk_ptr, nt + 1, np.int32)
-        f.blk_q = _copy(v.blk_q, 4 * nb, np.int32)
-        f.blk_ent_ptr = _copy(v.blk_ent_ptr, nb + 1, np.int32)
-        f.ent = _copy(v.ent, 4 * nent, np.int32)
-        f.ent_coeff = _copy(v.ent_coeff, nent, np.float64)
-        pos = np.zeros(max(nt, 1), dtype=np.int32)
-        check(L.qcm_mpo_buf_term_pos(h, _p(pos, i32p)), "qcm_mpo_buf_term_pos")
-    finally:
+    except Exception:
         L.qcm_mpo_buf_destroy(h)
+        h.value = None
+        raise
+
+
+def _fmpo_from_buf(L, h) -> FMpo:
+    """Copy a built two-site tensor out of its native buffer into an FMpo."""
+    v = CMpo()
+    sz = (C.c_int64 * 4)()
+    check(L.qcm_mpo_buf_view(h, C.byref(v), sz), "qcm_mpo_buf_view")
+    ne, nt, nb, nent = sz[0], sz[1], sz[2], sz[3]
+    f = FMpo.__new__(FMpo)
+    f.mpo = _FlatTensor(v.row_dim, v.col_dim)
+    f.left_spin = _copy(v.left_spin, v.row_dim, np.int32)
+    f.right_spin = _copy(v.right_spin, v.col_dim, np.int32)
+    f.left_herm = _copy(v.left_herm, v.row_dim, np.int32)
+    f.right_herm = _copy(v.right_herm, v.col_dim, np.int32)
+    f.left_phase = _copy(v.left_phase, v.row_dim, np.int32)
+    f.right_phase = _copy(v.right_phase, v.col_dim, np.int32)
+    f.col_ptr = _copy(v.col_ptr, v.col_dim + 1, np.int32)
+    f.row_of = _copy(v.row_of, ne, np.int32)
+    f.term_ptr = _copy(v.term_ptr, ne + 1, np.int32)
+    f.term_op = _copy(v.term_op, nt, np.int32)
+    f.term_scale = _copy(v.term_scale, nt, np.float64)
+    f.n_ops = v.n_ops
+    f.op_spin = _copy(v.op_spin, nt, np.int32)
+    f.op_blk_ptr = _copy(v.op_blk_ptr, nt + 1, np.int32)
+    f.blk_q = _copy(v.blk_q, 4 * nb, np.int32)
+    f.blk_ent_ptr = _copy(v.blk_ent_ptr, nb + 1, np.int32)
+    f.ent = _copy(v.ent, 4 * nent, np.int32)
+    f.ent_coeff = _copy(v.ent_coeff, nent, np.float64)
+    pos = np.zeros(max(nt, 1), dtype=np.int32)
+    check(L.qcm_mpo_buf_term_pos(h, _p(pos, i32p)), "qcm_mpo_buf_term_pos")
     b2 = np.repeat(np.arange(f.mpo.col_dim), np.diff(f.col_ptr[:f.mpo.col_dim + 1]))
     tb1 = np.repeat(f.row_of[:ne], np.diff(f.term_ptr[:ne + 1])) if ne else np.zeros(0, dtype=np.int32)
     tb2 = np.repeat(b2, np.diff(f.term_ptr[:ne + 1])) if ne else np.zeros(0, dtype=np.int64)

@@ -257,3 +257,24 @@ def test_native_twosite_mpo_on_the_golden_systems(golden, name):
         got = N.make_twosite_fmpo(N.FMpo(mpo[p]), N.FMpo(mpo[p + 1]), model.phys)
         for k in _FMPO_ARRAYS:
             assert np.array_equal(getattr(ref, k), getattr(got, k)), (p, k)
+
+
+def test_native_twosite_mpo_with_native_kronecker_products():
+    """qcm_mpo_twosite (the SU(2) op_kron in native code as well): the same tensor
+    structure as the Python builder, coefficients equal to within 1e-15 of the
+    tensor's largest (the Wigner symbols are long-double sums there, exact
+    rationals in the Python restatement)."""
+    from qcmaquis_gb300.mpo import make_twosite_mpo
+    L, nelec = 8, 6
+    model = QCModel(L, synthetic_integral_map(L, seed=5), nelec)
+    mpo = make_mpo(model)
+    flat = [N.FMpo(w) for w in mpo]
+    for p in range(L - 1):
+        ref = N.FMpo(make_twosite_mpo(mpo[p], mpo[p + 1], model.phys, model.phys))
+        got = N.make_twosite_fmpo(flat[p], flat[p + 1], model.phys, native_kron=True)
+        for k in _FMPO_ARRAYS:
+            if k == "ent_coeff":
+                continue
+            assert np.array_equal(getattr(ref, k), getattr(got, k)), (p, k)
+        assert got.term_key == ref.term_key
+        assert np.max(np.abs(got.ent_coeff - ref.ent_coeff)) <= 1e-15 * np.max(np.abs(ref.ent_coeff))
