@@ -644,7 +644,10 @@ def main():
         "gpu_launches": int(gpu_launches),
         "roofline": roof,
         "stages_ms": {f"{i}:{k}": round(t * 1e3, 3) for i, (k, t) in enumerate(zip(kinds, stage_t))},
-        "axpy_gather_gbs": axpy_gbs,
+        # naive count: every axpy term reads its source and reads+writes its output
+        # in FP64 (3 x 8 B per element-term); sources are shared across terms and
+        # served from L2, so this is an element-term rate, not DRAM traffic
+        "axpy_element_term_rate_gbs_naive": axpy_gbs,
         "work": {"gemm_flops": plan.gemm_flops, "axpy_flops": plan.axpy_flops, "axpy_bytes": plan.axpy_bytes},
         "clocks": clk.summary(),
         "vs_fp64_gpu": compare,

@@ -336,7 +336,11 @@ void qcm_plan_destroy(qcm_plan* plan);
 int qcm_device_status(int32_t* status);
 
 /* FP64 vector kernels over n elements (deterministic reductions).
- * The result of qcm_dot / qcm_nrm2 is written to a device double. */
+ * The result of qcm_dot / qcm_nrm2 is written to a device double.
+ * qcm_dot, qcm_nrm2 and qcm_multi_dot share one library-owned workspace per
+ * device (partial sums and a vector-pointer table, allocated on first use):
+ * calls issued on streams with no ordering between them race on it, so issue
+ * them on one stream (or order the streams). */
 int qcm_dot(const double* x, const double* y, int64_t n, double* result_dev, void* stream);
 int qcm_nrm2(const double* x, int64_t n, double* result_dev, void* stream);
 /* y = a*x + b*y */
@@ -358,8 +362,11 @@ int qcm_multi_dot(const double* const* v_dev_ptrs, int32_t nvec, const double* y
  * instead of a workspace allocated on first use; every GPU that loads the
  * library holds that array until the process exits.
  * Limits: nvec <= 32, otherwise QCM_E_RANGE and nothing is launched.
- * The first call on each device looks up the array's device address; make
- * that first call before any stream capture.  All calls share the array:
+ * The first call on each device looks up the array's device address and,
+ * with CUDA's default lazy module loading, may load the library's device code,
+ * which takes device memory for the code and the array: make that first call
+ * before the host's pool reserves the device budget (or run with
+ * CUDA_MODULE_LOADING=EAGER) and before any stream capture.  All calls share the array:
  * calls that overlap on the GPU (different streams, no ordering between them)
  * race on it and must be serialised by the caller. */
 int qcm_multi_dot_noalloc(const double* const* v_dev_ptrs, int32_t nvec, const double* y, int64_t n,

@@ -52,16 +52,44 @@ struct KeyHash {
     }
 };
 
+// Operator tables of a flattened MPO (or of a product list): non-null arrays,
+// monotone block and entry pointers starting at 0.
+void check_ops(const qcm_mpo_t* w, const char* what) {
+    if (w->n_ops < 0 || (w->n_ops > 0 && (!w->op_blk_ptr || !w->blk_q || !w->blk_ent_ptr)))
+        throw std::runtime_error(std::string("malformed operator tables of ") + what);
+    if (w->n_ops == 0) return;
+    if (w->op_blk_ptr[0] != 0) throw std::runtime_error(std::string("op_blk_ptr[0] != 0 in ") + what);
+    for (int32_t o = 0; o < w->n_ops; ++o)
+        if (w->op_blk_ptr[o + 1] < w->op_blk_ptr[o])
+            throw std::runtime_error(std::string("op_blk_ptr not monotone in ") + what);
+    const int32_t nblk = w->op_blk_ptr[w->n_ops];
+    if (w->blk_ent_ptr[0] != 0) throw std::runtime_error(std::string("blk_ent_ptr[0] != 0 in ") + what);
+    for (int32_t k = 0; k < nblk; ++k)
+        if (w->blk_ent_ptr[k + 1] < w->blk_ent_ptr[k])
+            throw std::runtime_error(std::string("blk_ent_ptr not monotone in ") + what);
+    if (w->blk_ent_ptr[nblk] > 0 && (!w->ent || !w->ent_coeff))
+        throw std::runtime_error(std::string("null operator entries in ") + what);
+}
+
 void check_mpo(const qcm_mpo_t* w, const char* what) {
     if (!w) throw std::runtime_error(std::string("null ") + what);
     if (w->row_dim < 0 || w->col_dim < 0 || !w->col_ptr || !w->term_ptr || !w->left_spin || !w->right_spin)
         throw std::runtime_error(std::string("malformed ") + what);
+    if (w->col_ptr[0] != 0) throw std::runtime_error(std::string("col_ptr[0] != 0 in ") + what);
+    for (int32_t b = 0; b < w->col_dim; ++b)
+        if (w->col_ptr[b + 1] < w->col_ptr[b]) throw std::runtime_error(std::string("col_ptr not monotone in ") + what);
     int64_t ne = w->col_ptr[w->col_dim];
+    if (ne > 0 && (!w->row_of || !w->term_op || !w->term_scale))
+        throw std::runtime_error(std::string("null element arrays in ") + what);
+    if (w->term_ptr[0] != 0) throw std::runtime_error(std::string("term_ptr[0] != 0 in ") + what);
     for (int64_t e = 0; e < ne; ++e) {
         if (w->row_of[e] < 0 || w->row_of[e] >= w->row_dim) throw std::runtime_error("mpo row index out of range");
+        if (w->term_ptr[e + 1] < w->term_ptr[e]) throw std::runtime_error("mpo term_ptr not monotone");
         for (int t = w->term_ptr[e]; t < w->term_ptr[e + 1]; ++t)
             if (w->term_op[t] < 0 || w->term_op[t] >= w->n_ops) throw std::runtime_error("mpo operator out of range");
     }
+    if (w->n_ops > 0 && !w->op_spin) throw std::runtime_error(std::string("null op_spin in ") + what);
+    check_ops(w, what);
 }
 
 // rows of a CSC tensor: b1 -> [(b2, element)], b2 ascending
@@ -141,12 +169,25 @@ void phase1(qcm_mpo_buf& B, const qcm_mpo_t* w1, const qcm_mpo_t* w2) {
 }
 
 struct Entry { int32_t r, c, rs, cs; double v; };
-struct Block { Q lc, rc; std::vector<Entry> e; };
+// entries in first-occurrence order; pos maps (row, col) to the entry, so each
+// summand is found in constant time and the summation order is unchanged
+struct Block {
+    Q lc, rc;
+    std::vector<Entry> e;
+    std::unordered_map<uint64_t, int32_t> pos;
+};
+inline uint64_t rc_key(int32_t r, int32_t c) { return ((uint64_t)(uint32_t)r << 32) | (uint32_t)c; }
 
 void phase2(qcm_mpo_buf& B, const qcm_mpo_t* prods) {
     const int64_t nkeys = (int64_t)B.keys.size() / 6;
     if (!prods || prods->n_ops != nkeys || !prods->op_blk_ptr || !prods->blk_q || !prods->blk_ent_ptr)
         throw std::runtime_error("one product operator per listed key expected");
+    check_ops(prods, "the product operators");
+    // start from empty output tables, so a retry after a failed finish rebuilds cleanly
+    B.built = false;
+    B.col_ptr.clear(); B.row_of.clear(); B.term_ptr.clear(); B.term_op.clear(); B.op_spin.clear();
+    B.op_blk_ptr.clear(); B.blk_q.clear(); B.blk_ent_ptr.clear(); B.ent.clear(); B.term_pos.clear();
+    B.term_scale.clear(); B.ent_coeff.clear();
     // the output operators, grouped per element (b1, b3) in column-major order;
     // an element lists its operators with s descending (later table entries first)
     std::vector<int64_t> order(B.outs.size());
@@ -185,15 +226,18 @@ void phase2(qcm_mpo_buf& B, const qcm_mpo_t* prods) {
                         Block* bl = nullptr;
                         for (auto& x : blocks)
                             if (x.lc == lc && x.rc == rc) { bl = &x; break; }
-                        if (!bl) { blocks.push_back({lc, rc, {}}); bl = &blocks.back(); }
+                        if (!bl) { blocks.push_back({lc, rc, {}, {}}); bl = &blocks.back(); }
                         for (int en = prods->blk_ent_ptr[kb]; en < prods->blk_ent_ptr[kb + 1]; ++en) {
                             const int32_t* x = prods->ent + 4 * en;
                             const double v = prods->ent_coeff[en] * c;
-                            Entry* hit = nullptr;
-                            for (auto& y : bl->e)
-                                if (y.r == x[0] && y.c == x[1]) { hit = &y; break; }
-                            if (hit) hit->v = hit->v + v;
-                            else bl->e.push_back({x[0], x[1], x[2], x[3], v});
+                            auto it = bl->pos.find(rc_key(x[0], x[1]));
+                            if (it != bl->pos.end()) {
+                                Entry& y = bl->e[it->second];
+                                y.v = y.v + v;
+                            } else {
+                                bl->pos.emplace(rc_key(x[0], x[1]), (int32_t)bl->e.size());
+                                bl->e.push_back({x[0], x[1], x[2], x[3], v});
+                            }
                         }
                     }
                 }

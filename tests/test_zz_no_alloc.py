@@ -47,6 +47,35 @@ def test_noalloc_multi_dot_matches_allocating_entry_point_twice():
     assert torch.allclose(out2, exp, rtol=REL_TOL, atol=1e-12)
 
 
+def test_noalloc_multi_dot_allocates_no_device_memory():
+    """After a first call (which looks up the scratch array and may load the
+    library's device code), further calls of different sizes leave both torch's
+    allocator and the device's free memory unchanged."""
+    lib = N.lib()
+    g = torch.Generator(device="cuda").manual_seed(99)
+    sizes = [17, 4096, 1_000_003, 65_536]
+    vs = [torch.randn(max(sizes), dtype=torch.float64, device="cuda", generator=g) for _ in range(32)]
+    y = torch.randn(max(sizes), dtype=torch.float64, device="cuda", generator=g)
+    out = torch.zeros(32, dtype=torch.float64, device="cuda")
+    N.check(lib.qcm_multi_dot_noalloc(_ptrs(vs), 32, C.c_void_p(y.data_ptr()), 8, C.c_void_p(out.data_ptr()), None),
+            "qcm_multi_dot_noalloc")
+    torch.cuda.synchronize()
+    torch_before = torch.cuda.memory_allocated()
+    free_before, _ = torch.cuda.mem_get_info()
+    for k, n in enumerate(sizes):
+        nv = (5 * k + 3) % 32 + 1
+        N.check(lib.qcm_multi_dot_noalloc(_ptrs(vs[:nv]), nv, C.c_void_p(y.data_ptr()), n,
+                                          C.c_void_p(out.data_ptr()), None), "qcm_multi_dot_noalloc")
+        torch.cuda.synchronize()
+        exp = torch.stack([torch.dot(v[:n], y[:n]) for v in vs[:nv]])
+        assert torch.allclose(out[:nv], exp, rtol=1e-11, atol=1e-11 * float(exp.abs().max()))
+    del exp
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert torch.cuda.memory_allocated() == torch_before
+    assert free_after == free_before, (free_before, free_after)
+
+
 def test_noalloc_multi_dot_rejects_too_many_vectors():
     lib = N.lib()
     y = torch.zeros(16, dtype=torch.float64, device="cuda")
