@@ -1,8 +1,9 @@
 """Numpy restatement of QCMaquis's SU2U1 two-site DMRG step (oracle; tests only).
 
-Block-sparse tensors use ``qcmaquis_gb300.block_matrix.BlockMatrix`` as a plain
-container; every algorithm below is written against the reference files cited
-in its docstring.  Arithmetic is FP64 throughout.  Work counters (``FLOPS``)
+Block-sparse tensors, indices and couplings are the oracle's own
+(``oracle.qn``, ``oracle.su2``, ``oracle.ts_mpo``), written from the reference
+and not from the product package; every algorithm below is written against the
+reference files cited in its docstring.  Arithmetic is FP64 throughout.  Work counters (``FLOPS``)
 record the algorithmic floating-point work of each GEMM/axpy the reference
 algorithm issues, which the benchmark uses as the roofline numerator.
 """
@@ -13,10 +14,10 @@ from typing import Dict, List, Optional, Tuple
 
 import numpy as np
 
-from qcmaquis_gb300.block_matrix import BlockMatrix, gemm as bm_gemm
-from qcmaquis_gb300.symmetry import (Index, ProductBasis, adjoin, common_subset, fuse, fuse_neg_first,
-                                     index_product, neg, spin, triangle)
-from qcmaquis_gb300.wigner import conjugate_correction, mod_coupling, set_coupling, wigner6j
+from .qn import (BlockMatrix, Index, ProductBasis, adjoin, bm_gemm, common_subset, fuse, fuse_neg_first,
+                 index_product, neg, spin, triangle)
+from .su2 import conjugate_correction, mod_coupling, set_coupling, wigner6j
+from .ts_mpo import sparse_of
 
 LEFT_PAIRED, RIGHT_PAIRED = 0, 1
 
@@ -491,7 +492,7 @@ def lbtm_kernel(b2, T: List[BlockMatrix], mpo, right_i: Index, out_left_i: Index
         Tb = T[b1]
         for tag, scale in mpo.at(b1, b2):
             W = mpo.op(tag)
-            wsparse = mpo.sparse(tag)
+            wsparse = sparse_of(mpo.op(tag))
             a = mpo.left_spin(b1).get()
             k = W.spin.get()
             ap = mpo.right_spin(b2).get()
@@ -542,7 +543,7 @@ def rbtm_tasks_apply(b1, t: List[BlockMatrix], mpo, left_i: Index, out_right_i: 
         Tb = t[b2]
         for tag, scale in mpo.at(b1, b2):
             W = mpo.op(tag)
-            wsparse = mpo.sparse(tag)
+            wsparse = sparse_of(mpo.op(tag))
             a = mpo.left_spin(b1).get()
             k = W.spin.get()
             ap = mpo.right_spin(b2).get()
@@ -713,7 +714,7 @@ def diagonal_hamiltonian(left: List[BlockMatrix], right: List[BlockMatrix], mpo,
             a = mpo.left_spin(b1).get()
             for tag, scale in mpo.at(b1, b2):
                 W = mpo.op(tag)
-                wsparse = mpo.sparse(tag)
+                wsparse = sparse_of(mpo.op(tag))
                 k = W.spin.get()
                 for blk in range(len(right_i)):
                     in_charge = right_i[blk][0]

@@ -18,7 +18,7 @@ from typing import Dict, List, Optional
 
 import numpy as np
 
-from qcmaquis_gb300.mpo import MPO, make_ts_cache_mpo
+from .ts_mpo import make_ts_cache_mpo
 
 from . import dmrg_ref as R
 
@@ -82,7 +82,7 @@ class SweepRecord:
     sweep_truncated_weight: List[float] = field(default_factory=list)
 
 
-def expval(mps: List[R.MPSTensor], mpo: MPO) -> float:
+def expval(mps: List[R.MPSTensor], mpo) -> float:
     """``expval`` (``mp_tensors/mps_mpo_ops.h:57-68``) without the core energy."""
     left = R.left_boundary(mps[0])
     for i in range(len(mps)):
@@ -143,7 +143,7 @@ class OverlapBoundaries:
         return out
 
 
-def run_dmrg(model, mpo: MPO, p: SweepParams, nelec: int, twoS: int = 0, mps=None,
+def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps=None,
              callback=None, ortho_states=None) -> (SweepRecord, List[R.MPSTensor]):
     """Two-site sweeps; ``ortho_states``: MPSs the state is optimised orthogonal to
     (``n_ortho_states`` / ``ortho_states``, ``sba/SweepBasedEnergyMinimization.h:52-67``)."""
@@ -223,7 +223,7 @@ def run_dmrg(model, mpo: MPO, p: SweepParams, nelec: int, twoS: int = 0, mps=Non
     return rec, mps
 
 
-def run_dmrg_single_site(model, mpo: MPO, p: SweepParams, nelec: int, twoS: int = 0, mps=None,
+def run_dmrg_single_site(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps=None,
                          callback=None) -> (SweepRecord, List[R.MPSTensor]):
     """Single-site sweeps: ``SweepOptimizationTypeTrait<SingleSite>``
     (``sba/SweepOptimizationTypeTrait.h:23-84``: 2(L-1) microiterations, site i going

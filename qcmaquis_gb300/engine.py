@@ -108,7 +108,7 @@ def _digest(*parts) -> bytes:
         d = getattr(x, "_qcm_digest", None)
         if d is None:
             g = hashlib.blake2b(digest_size=20)
-            if isinstance(x, Index):
+            if not hasattr(x, "q"):   # a quantum-number index (list of [charge, size])
                 g.update(repr(x.data).encode())
             else:
                 for a in (x.q, x.rows, x.cols, x.off, getattr(x, "ptr", None)):

@@ -118,7 +118,9 @@ class Index:
         return iter(self.data)
 
     def __eq__(self, other):
-        return isinstance(other, Index) and [tuple(x) for x in self.data] == [tuple(x) for x in other.data]
+        if not isinstance(other, Index):
+            return NotImplemented
+        return [tuple(x) for x in self.data] == [tuple(x) for x in other.data]
 
     def __repr__(self):
         return "Index(" + ", ".join(f"{c}:{s}" for c, s in self.data) + ")"

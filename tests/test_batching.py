@@ -16,11 +16,11 @@ from test_oracle import _random_site_problem
 def _problems():
     out = []
     for (L, Ne, m, site, seed) in [(6, 6, 16, 2, 3), (6, 6, 12, 1, 4), (5, 4, 10, 1, 5)]:
-        psi, left, right, ts = _random_site_problem(L=L, N=Ne, m=m, site=site, seed=seed)
+        psi, left, right, ts, ots = _random_site_problem(L=L, N=Ne, m=m, site=site, seed=seed)
         psi = psi.copy().make_left_paired()
         lay, Ll, Rl = N.Layout.of(psi.data), N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
         p = N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, N.FMpo(ts), True)
-        out.append((psi, left, right, ts, lay, Ll, Rl, p))
+        out.append((psi, left, right, ots, lay, Ll, Rl, p))
     return out
 
 

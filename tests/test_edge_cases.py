@@ -25,17 +25,17 @@ def _plan(psi, left, right, ts, herm=True):
 
 def test_smallest_problem_plan_matches_oracle():
     """L=2, N=2 (the H2 case of the reference's tests): every block is tiny."""
-    psi, left, right, ts = _random_site_problem(L=2, N=2, m=4, site=0)
+    psi, left, right, ts, ots = _random_site_problem(L=2, N=2, m=4, site=0)
     psi, lay, Ll, Rl, p = _plan(psi, left, right, ts)
     bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.zeros(p.out_elems)] + \
         [np.full(max(s, 1), np.nan) for s in p.scratch]
     run_plan(p, bufs, images=True)
-    ref = lay.pack(R.site_hamil2(psi, left, right, ts).data)
+    ref = lay.pack(R.site_hamil2(psi, left, right, ots).data)
     assert np.linalg.norm(bufs[3] - ref) <= 1e-7 * np.linalg.norm(ref)
 
 
 def test_sigma_of_zero_vector_is_zero():
-    psi, left, right, ts = _random_site_problem(m=16)
+    psi, left, right, ts, ots = _random_site_problem(m=16)
     psi, lay, Ll, Rl, p = _plan(psi, left, right, ts)
     bufs = [np.zeros(lay.size), Ll.pack(left), Rl.pack(right), np.full(p.out_elems, np.nan)] + \
         [np.full(max(s, 1), np.nan) for s in p.scratch]
@@ -45,7 +45,7 @@ def test_sigma_of_zero_vector_is_zero():
 
 def test_oversized_block_is_rejected():
     """Blocks of 2^31 elements or more are refused (the executors use 32-bit in-block offsets)."""
-    psi, left, right, ts = _random_site_problem(m=8)
+    psi, left, right, ts, ots = _random_site_problem(m=8)
     psi = psi.copy().make_left_paired()
     lay = N.Layout.of(psi.data)
     shapes = list(lay.shapes)
@@ -60,7 +60,7 @@ def test_null_and_out_of_range_arguments_are_rejected():
     lib = N.lib()
     assert lib.qcm_plan_sigma(None, None, None, None, None, None, None, 1, None) == -1
     assert lib.qcm_plan_sizes(None, None, None) == -1
-    psi, left, right, ts = _random_site_problem(m=8)
+    psi, left, right, ts, ots = _random_site_problem(m=8)
     _, _, _, _, p = _plan(psi, left, right, ts)
     cnt = np.zeros(4, dtype=np.int64)
     rc = lib.qcm_plan_stage_images(p.h, 99, cnt.ctypes.data_as(C.POINTER(C.c_int64)), None, None, None, None, None)
@@ -78,9 +78,9 @@ def test_small_problems_every_precision_on_gpu(L, N_, m, site):
     """Tiny blocks through the FP64, TF32, BF16x3 (images) and BF16x3 (in-kernel split) executors."""
     import torch
     from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
-    psi, left, right, ts = _random_site_problem(L=L, N=N_, m=m, site=site)
+    psi, left, right, ts, ots = _random_site_problem(L=L, N=N_, m=m, site=site)
     psi = psi.copy().make_left_paired()
-    ref = N.Layout.of(psi.data).pack(R.site_hamil2(psi, left, right, ts).data)
+    ref = N.Layout.of(psi.data).pack(R.site_hamil2(psi, left, right, ots).data)
     eng = Engine("cuda:0")
     x, Lb, Rb = DeviceMPSTensor.from_host(psi), DeviceBoundary.from_host(left), DeviceBoundary.from_host(right)
     nref = np.linalg.norm(ref)
@@ -95,7 +95,7 @@ def test_small_problems_every_precision_on_gpu(L, N_, m, site):
 def test_zero_vector_on_gpu():
     import torch
     from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
-    psi, left, right, ts = _random_site_problem(m=16)
+    psi, left, right, ts, ots = _random_site_problem(m=16)
     psi = psi.copy().make_left_paired()
     x = DeviceMPSTensor.from_host(psi)
     x.data.zero_()
@@ -110,7 +110,7 @@ def test_plan_cache_key_is_the_layout_content():
     """Sigma plans are cached by the content of their indices and layouts: equal
     content gives one key, any change of a block gives another."""
     from qcmaquis_gb300.engine import _digest
-    psi, left, right, ts = _random_site_problem(m=8)
+    psi, left, right, ts, ots = _random_site_problem(m=8)
     psi = psi.copy().make_left_paired()
     a, b = N.Layout.of(psi.data), N.Layout.of(psi.data)
     assert a is not b and _digest(psi.phys_i, a) == _digest(psi.phys_i, b)
@@ -125,10 +125,10 @@ def test_plan_shape_options_keep_sigma_and_change_the_plan():
     """Plan-shape options (the autotuner's knobs) change the split-K and dense-group
     tables, never the sigma; the shape key ignores block values and offsets."""
     from qcmaquis_gb300.autotune import shape_key
-    psi, left, right, ts = _random_site_problem(L=6, N=6, m=24, site=2)
+    psi, left, right, ts, ots = _random_site_problem(L=6, N=6, m=24, site=2)
     psi = psi.copy().make_left_paired()
     lay, Ll, Rl = N.Layout.of(psi.data), N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
-    ref = lay.pack(R.site_hamil2(psi, left, right, ts).data)
+    ref = lay.pack(R.site_hamil2(psi, left, right, ots).data)
     outs = []
     for sk, dm in [(0, 0), (2, 8), (4, 16)]:
         p = N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, N.FMpo(ts), True,
@@ -152,7 +152,7 @@ def test_autotuned_engine_gives_the_same_sigma(tmp_path):
     import torch
     from qcmaquis_gb300.autotune import Autotuner
     from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
-    psi, left, right, ts = _random_site_problem(L=6, N=6, m=24, site=2)
+    psi, left, right, ts, ots = _random_site_problem(L=6, N=6, m=24, site=2)
     psi = psi.copy().make_left_paired()
     x, Lb, Rb = DeviceMPSTensor.from_host(psi), DeviceBoundary.from_host(left), DeviceBoundary.from_host(right)
     a = Engine("cuda:0", precision=N.PREC_BF16X3)
@@ -168,9 +168,9 @@ def test_autotuned_engine_gives_the_same_sigma(tmp_path):
 def test_bf16x2_form_on_gpu():
     import torch
     from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
-    psi, left, right, ts = _random_site_problem(L=6, N=6, m=24, site=2)
+    psi, left, right, ts, ots = _random_site_problem(L=6, N=6, m=24, site=2)
     psi = psi.copy().make_left_paired()
-    ref = N.Layout.of(psi.data).pack(R.site_hamil2(psi, left, right, ts).data)
+    ref = N.Layout.of(psi.data).pack(R.site_hamil2(psi, left, right, ots).data)
     x, Lb, Rb = DeviceMPSTensor.from_host(psi), DeviceBoundary.from_host(left), DeviceBoundary.from_host(right)
     err = {}
     for prec in (N.PREC_BF16X2, N.PREC_BF16X3):

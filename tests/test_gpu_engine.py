@@ -28,19 +28,19 @@ def engine():
 def test_sigma_matches_oracle(engine, herm, site, m):
     from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
     eng = engine if herm else Engine("cuda:0", hermitian=False)
-    psi, left, right, ts = _random_site_problem(site=site, m=m, herm=herm)
+    psi, left, right, ts, ots = _random_site_problem(site=site, m=m, herm=herm)
     psi = psi.copy().make_left_paired()
     dk = DeviceMPSTensor.from_host(psi)
     out = eng.site_hamil2(dk, DeviceBoundary.from_host(left), DeviceBoundary.from_host(right), ts)
     torch.cuda.synchronize()
-    ref = dk.layout.pack(R.site_hamil2(psi, left, right, ts, is_hermitian=herm).data)
+    ref = dk.layout.pack(R.site_hamil2(psi, left, right, ots, is_hermitian=herm).data)
     got = out.data.cpu().numpy()
     assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref)
 
 
 def test_sigma_repeated_calls_are_bitwise_identical(engine):
     from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor
-    psi, left, right, ts = _random_site_problem(site=2, m=24)
+    psi, left, right, ts, ots = _random_site_problem(site=2, m=24)
     psi = psi.copy().make_left_paired()
     dk = DeviceMPSTensor.from_host(psi)
     L, Rb = DeviceBoundary.from_host(left), DeviceBoundary.from_host(right)

@@ -50,7 +50,7 @@ def test_gpu_constrained_jcd_skip_and_empty_constraint():
     from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine, SiteProblem
     from qcmaquis_gb300.jd import solve_ietl_jcd
     from test_oracle import _random_site_problem
-    psi, left, right, ts = _random_site_problem()
+    psi, left, right, ts, ots = _random_site_problem()
     x = DeviceMPSTensor.from_host(psi.copy().make_left_paired(), "cuda:0")
     eng = Engine("cuda:0")
     sp = SiteProblem(eng, DeviceBoundary.from_host(left, "cuda:0"), DeviceBoundary.from_host(right, "cuda:0"), ts)

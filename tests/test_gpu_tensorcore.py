@@ -33,7 +33,7 @@ def _sigma_all_precisions(eng, psi, L, R, W):
 @pytest.mark.parametrize("site,m", [(2, 16), (2, 40)])
 def test_tensorcore_sigma_small(site, m):
     from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
-    psi, left, right, ts = _random_site_problem(site=site, m=m)
+    psi, left, right, ts, ots = _random_site_problem(site=site, m=m)
     psi = psi.copy().make_left_paired()
     eng = Engine("cuda:0")
     o = _sigma_all_precisions(eng, DeviceMPSTensor.from_host(psi), DeviceBoundary.from_host(left),

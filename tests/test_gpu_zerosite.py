@@ -54,13 +54,13 @@ def test_diagonal_hamiltonian_matches_oracle(site, m):
     from qcmaquis_gb300 import native as N
     from qcmaquis_gb300.engine import DeviceBoundary, DeviceMPSTensor, Engine
     from test_oracle import _random_site_problem
-    psi, left, right, ts = _random_site_problem(site=site, m=m, herm=False)
+    psi, left, right, ts, ots = _random_site_problem(site=site, m=m, herm=False)
     psi = psi.copy().make_left_paired()
     eng = Engine("cuda:0", hermitian=False)
     x = DeviceMPSTensor.from_host(psi, "cuda:0")
     Lb, Rb = DeviceBoundary.from_host(left, "cuda:0"), DeviceBoundary.from_host(right, "cuda:0")
     got = eng.diagonal_hamiltonian(x, Lb, Rb, ts).data.cpu().numpy()
-    want = x.layout.pack(R.diagonal_hamiltonian(left, right, ts, psi))
+    want = x.layout.pack(R.diagonal_hamiltonian(left, right, ots, psi))
     assert np.linalg.norm(got - want) <= 1e-12 * np.linalg.norm(want)
     p = N.plan_diagonal(psi.phys_i, psi.left_i, psi.right_i, x.layout, Lb.layout, Rb.layout, eng.fmpo(ts))
     p.upload()

@@ -30,7 +30,7 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_invalid_layout_is_rejected():
-    psi, left, right, ts = _random_site_problem()
+    psi, left, right, ts, ots = _random_site_problem()
     psi = psi.copy().make_left_paired()
     lay = N.Layout.of(psi.data)
     bad = N.Layout(list(reversed(lay.keys)), list(reversed(lay.shapes)))
@@ -42,7 +42,7 @@ def test_invalid_layout_is_rejected():
 @pytest.mark.parametrize("herm", [True, False])
 @pytest.mark.parametrize("site,m", [(1, 8), (2, 16), (3, 12)])
 def test_sigma_plan_matches_oracle(herm, site, m):
-    psi, left, right, ts = _random_site_problem(site=site, m=m, herm=herm)
+    psi, left, right, ts, ots = _random_site_problem(site=site, m=m, herm=herm)
     psi = psi.copy().make_left_paired()
     lay = N.Layout.of(psi.data)
     Ll, Rl = N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
@@ -51,7 +51,7 @@ def test_sigma_plan_matches_oracle(herm, site, m):
     bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.zeros(p.out_elems)] + \
         [np.full(max(s, 1), np.nan) for s in p.scratch]
     run_plan(p, bufs)
-    ref = lay.pack(R.site_hamil2(psi, left, right, ts, is_hermitian=herm).data)
+    ref = lay.pack(R.site_hamil2(psi, left, right, ots, is_hermitian=herm).data)
     assert np.linalg.norm(bufs[3] - ref) <= 1e-13 * np.linalg.norm(ref)
 
 
@@ -61,7 +61,7 @@ def test_sigma_image_tables_match_oracle(L, m, site, herm):
     stale shared-memory rows as NaN) reproduce the oracle's sigma; at L=12,
     m=400 blocks span several 128-row tiles and 32-wide K-chunks.  The
     executor keeps segment coefficients in FP32, hence the 1e-7 bound."""
-    psi, left, right, ts = _random_site_problem(L=L, N=L, m=m, site=site, herm=herm)
+    psi, left, right, ts, ots = _random_site_problem(L=L, N=L, m=m, site=site, herm=herm)
     psi = psi.copy().make_left_paired()
     lay = N.Layout.of(psi.data)
     Ll, Rl = N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
@@ -72,7 +72,7 @@ def test_sigma_image_tables_match_oracle(L, m, site, herm):
     bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.zeros(p.out_elems)] + \
         [np.full(max(s, 1), np.nan) for s in p.scratch]
     run_plan(p, bufs, images=True)
-    ref = lay.pack(R.site_hamil2(psi, left, right, ts, is_hermitian=herm).data)
+    ref = lay.pack(R.site_hamil2(psi, left, right, ots, is_hermitian=herm).data)
     assert np.linalg.norm(bufs[3] - ref) <= 1e-7 * np.linalg.norm(ref)
 
 
@@ -167,7 +167,7 @@ def test_zero_site_plan_matches_oracle(herm, bond, images):
 @pytest.mark.parametrize("site,m", [(2, 8), (3, 12)])
 def test_diagonal_plan_matches_oracle(site, m):
     """qcm_plan_diagonal against the oracle's diagonal_hamiltonian (full boundaries)."""
-    psi, left, right, ts = _random_site_problem(site=site, m=m, herm=False)
+    psi, left, right, ts, ots = _random_site_problem(site=site, m=m, herm=False)
     psi = psi.copy().make_left_paired()
     lay, Ll, Rl = N.Layout.of(psi.data), N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
     p = N.plan_diagonal(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, N.FMpo(ts))
@@ -175,7 +175,7 @@ def test_diagonal_plan_matches_oracle(site, m):
     bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.full(p.out_elems, np.nan)] + \
         [np.full(max(s, 1), np.nan) for s in p.scratch]
     run_plan(p, bufs)
-    ref = lay.pack(R.diagonal_hamiltonian(left, right, ts, psi))
+    ref = lay.pack(R.diagonal_hamiltonian(left, right, ots, psi))
     assert np.linalg.norm(bufs[3] - ref) <= 1e-13 * np.linalg.norm(ref)
 
 
@@ -187,13 +187,13 @@ def test_zero_site_plan_rejects_mismatched_bond():
 
 
 def test_plan_work_counters_match_oracle():
-    psi, left, right, ts = _random_site_problem()
+    psi, left, right, ts, ots = _random_site_problem()
     psi = psi.copy().make_left_paired()
     lay = N.Layout.of(psi.data)
     p = N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, lay, N.BoundaryLayout.of(left),
                      N.BoundaryLayout.of(right), N.FMpo(ts))
     R.FLOPS.reset()
-    R.site_hamil_lbtm(psi, left, right, ts)
+    R.site_hamil_lbtm(psi, left, right, ots)
     # the plan computes every T row eagerly, as the oracle does; the sums match
     assert p.gemm_flops == R.FLOPS.gemm_flops
     assert p.axpy_flops <= R.FLOPS.axpy_flops

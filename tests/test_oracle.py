@@ -6,6 +6,8 @@ from qcmaquis_gb300.integrals import synthetic_integral_map
 from qcmaquis_gb300.model import QCModel
 from qcmaquis_gb300.mpo import make_mpo, make_ts_cache_mpo
 from qcmaquis_gb300.wigner import wigner9j
+from oracle import ts_mpo as OTS
+from oracle import su2 as OSU2
 
 from oracle import dmrg_ref as R
 from oracle.fci import fci_energies
@@ -22,6 +24,68 @@ def test_wigner9j_reference_table(golden):
             assert abs(got) < 1e-12
         else:
             assert abs(got - val) <= 1e-8 * abs(val) + 5e-11, (args, got, val)
+
+
+def test_oracle_wigner_symbols_pinned(golden):
+    """The oracle's own 9j (oracle.su2) reproduces the reference's 9j table, and its
+    6j/9j equal an independent exact evaluation (sympy, where installed) on a
+    sweep of small doubled spins."""
+    for args, val in golden["wigner9j"]["cases"]:
+        got = OSU2.ninej(*args)
+        assert abs(got - val) <= 1e-8 * abs(val) + 5e-11, (args, got, val)
+    wig = pytest.importorskip("sympy.physics.wigner")
+    from sympy import Rational
+    rng = np.random.default_rng(5)
+    h = lambda x: Rational(int(x), 2)
+    from oracle.qn import triangle as tri
+    valid6, valid9 = [], []
+    while len(valid6) < 300:
+        a = [int(v) for v in rng.integers(0, 9, 6)]
+        if all(tri(*t) for t in ((a[0], a[1], a[2]), (a[0], a[4], a[5]), (a[3], a[1], a[5]), (a[3], a[4], a[2]))):
+            valid6.append(a)
+    while len(valid9) < 120:
+        a = [int(v) for v in rng.integers(0, 6, 9)]
+        rows = ((a[0], a[1], a[2]), (a[3], a[4], a[5]), (a[6], a[7], a[8]))
+        cols = ((a[0], a[3], a[6]), (a[1], a[4], a[7]), (a[2], a[5], a[8]))
+        if all(tri(*t) for t in rows + cols):
+            valid9.append(a)
+    for a in valid6:
+        exact = float(wig.wigner_6j(*map(h, a)))
+        assert abs(OSU2.sixj(*a) - exact) <= 1e-14 * max(1.0, abs(exact)), (a, exact)
+    for a in valid9:
+        exact = float(wig.wigner_9j(*map(h, a)))
+        assert abs(OSU2.ninej(*a) - exact) <= 1e-14 * max(1.0, abs(exact)), (a, exact)
+
+
+@pytest.mark.parametrize("L,N,site", [(6, 6, 0), (6, 6, 2), (6, 4, 4), (4, 2, 1)])
+def test_oracle_two_site_mpo_matches_product_builder(L, N, site):
+    """The oracle's two-site MPO tensor (oracle.ts_mpo, written from mt/ts_ops.h and the
+    SU(2) op_kron) and the product's (Python builder; the native builder equals it
+    array for array) give the same operator per (b1, b3, product spin), and the
+    oracle's sigma with either tensor agrees to 1e-13."""
+    ints = synthetic_integral_map(L, seed=L + site)
+    model = QCModel(L, ints, N)
+    mpo = make_mpo(model)
+    prod = make_ts_cache_mpo(mpo, model.phys)[site]
+    orc = OTS.make_twosite_mpo(mpo[site], mpo[site + 1], model.phys, model.phys)
+    assert (orc.row_dim, orc.col_dim) == (prod.row_dim, prod.col_dim)
+    assert set(orc.elements) == set(prod.elements)
+    for key in orc.elements:
+        a = {orc.op(t).spin.get(): orc.op(t) for t, _ in orc.at(*key)}
+        b = {prod.op(t).spin.get(): prod.op(t) for t, _ in prod.at(*key)}
+        assert sorted(a) == sorted(b), key
+        for s in a:
+            oa, ob = a[s], b[s]
+            sa = OTS.sparse_of(oa)
+            sb = prod.sparse(dict((prod.op(t).spin.get(), t) for t, _ in prod.at(*key))[s])
+            assert list(oa.bm.keys) == list(ob.bm.keys), key
+            for ea, eb in zip(sa, sb):
+                assert [e[:4] for e in ea] == [e[:4] for e in eb], key
+                assert np.allclose([e[4] for e in ea], [e[4] for e in eb], rtol=1e-14, atol=1e-15), key
+    psi, left, right, ts, ots = _random_site_problem(L=L, N=N, m=12, site=site, seed=L + site)
+    s1 = R.site_hamil2(psi.copy(), left, right, ots)
+    s2 = R.site_hamil2(psi.copy(), left, right, ts)
+    assert s1.copy().axpy(-1.0, s2).norm() <= 1e-13 * s1.norm()
 
 
 @pytest.mark.parametrize("name", ["lih", "h2"])
@@ -79,37 +143,39 @@ def _random_site_problem(L=6, N=6, seed=3, m=16, site=2, herm=True):
     for i in range(L - 1, site + 1, -1):
         right = R.overlap_mpo_right_step(mps[i], mps[i], right, mpo[i], is_hermitian=herm)
     ts = make_ts_cache_mpo(mpo, model.phys)[site]
+    # the oracle's own two-site tensor (oracle.ts_mpo), for the oracle's side of a comparison
+    ots = OTS.make_twosite_mpo(mpo[site], mpo[site + 1], model.phys, model.phys)
     psi = R.make_two_site_mps(mps[site], mps[site + 1])
-    return psi, left, right, ts
+    return psi, left, right, ts, ots
 
 
 def test_lbtm_equals_rbtm():
-    psi, left, right, ts = _random_site_problem()
-    a = R.site_hamil_lbtm(psi, left, right, ts)
-    b = R.site_hamil_rbtm(psi, left, right, ts)
+    psi, left, right, ts, ots = _random_site_problem()
+    a = R.site_hamil_lbtm(psi, left, right, ots)
+    b = R.site_hamil_rbtm(psi, left, right, ots)
     diff = a.copy().axpy(-1.0, b)
     assert diff.norm() <= 1e-12 * a.norm()
 
 
 def test_sigma_is_symmetric():
-    psi, left, right, ts = _random_site_problem()
+    psi, left, right, ts, ots = _random_site_problem()
     rng = np.random.default_rng(0)
     x = psi.copy().make_left_paired()
     y = psi.copy().make_left_paired()
     for k in range(y.data.n_blocks()):
         y.data.blocks[k] = rng.standard_normal(y.data.blocks[k].shape)
-    hx = R.site_hamil2(x, left, right, ts)
-    hy = R.site_hamil2(y, left, right, ts)
+    hx = R.site_hamil2(x, left, right, ots)
+    hy = R.site_hamil2(y, left, right, ots)
     assert abs(y.dot(hx) - x.dot(hy)) < 1e-12 * max(1.0, abs(y.dot(hx)))
 
 
 def test_hermitian_skip_matches_full_boundary():
     # dmrg/tests/test_mps_mpo_ops/test_mps_mpo_ops_electronic.cpp:39-99: skipping
     # Hermitian partners must not change sigma
-    psi, left, right, ts = _random_site_problem(herm=True)
-    psi2, left2, right2, ts2 = _random_site_problem(herm=False)
-    a = R.site_hamil_lbtm(psi, left, right, ts, is_hermitian=True)
-    b = R.site_hamil_lbtm(psi2, left2, right2, ts2, is_hermitian=False)
+    psi, left, right, ts, ots = _random_site_problem(herm=True)
+    psi2, left2, right2, ts2, ots2 = _random_site_problem(herm=False)
+    a = R.site_hamil_lbtm(psi, left, right, ots, is_hermitian=True)
+    b = R.site_hamil_lbtm(psi2, left2, right2, ots2, is_hermitian=False)
     assert a.copy().axpy(-1.0, b).norm() <= 1e-12 * a.norm()
 
 
@@ -224,9 +290,9 @@ def test_diagonal_hamiltonian_is_the_diagonal_of_sigma(site, m):
     """``ref_diag`` (``fw/optimize/ietl_davidson.h:25-58``): every element of
     ``diagonal_hamiltonian`` equals (H e_ij)(i, j) for the unit tensor e_ij, to 1e-12
     (full boundaries)."""
-    psi, left, right, ts = _random_site_problem(site=site, m=m, herm=False)
+    psi, left, right, ts, ots = _random_site_problem(site=site, m=m, herm=False)
     psi = psi.copy().make_left_paired()
-    d = R.diagonal_hamiltonian(left, right, ts, psi)
+    d = R.diagonal_hamiltonian(left, right, ots, psi)
     assert d.keys == psi.data.keys
     rng = np.random.default_rng(site)
     for key, blk in zip(psi.data.keys, psi.data.blocks):
@@ -237,7 +303,7 @@ def test_diagonal_hamiltonian_is_the_diagonal_of_sigma(site, m):
             for q in range(e.data.n_blocks()):
                 e.data.blocks[q] = np.zeros_like(e.data.blocks[q])
             e.data.blocks[e.data.find_block(*key)][i, j] = 1.0
-            h = R.site_hamil2(e, left, right, ts, is_hermitian=False).make_left_paired()
+            h = R.site_hamil2(e, left, right, ots, is_hermitian=False).make_left_paired()
             want = h.data.blocks[h.data.find_block(*key)][i, j]
             assert abs(d.blocks[d.find_block(*key)][i, j] - want) < 1e-12 * max(1.0, abs(want))
 
@@ -246,8 +312,8 @@ def test_constrained_jcd_skips_a_fully_constrained_start():
     """``ietl_jacobi_davidson.h:41-47, 58-64``: when the constraints remove the whole start
     vector the solve is skipped and <init|H|init> returned with ``init``; a constraint
     the start vector is orthogonal to leaves the solve unchanged."""
-    psi, left, right, ts = _random_site_problem()
-    apply_h = lambda x: R.site_hamil2(x, left, right, ts)
+    psi, left, right, ts, ots = _random_site_problem()
+    apply_h = lambda x: R.site_hamil2(x, left, right, ots)
     x0 = psi.copy().make_left_paired()
     theta, u, it = R.jcd_solve(apply_h, x0, 1e-8, 6, ortho=[x0.scaled(2.0)])
     assert it == 0 and abs(theta - x0.dot(apply_h(x0))) < 1e-12 * max(1.0, abs(theta))
