@@ -380,6 +380,94 @@ int qcm_multi_dot_noalloc(const double* const* v_dev_ptrs, int32_t nvec, const d
 int qcm_seg_multi_dot(const double* const* v_dev_ptrs, int32_t nvec, const double* y, const int64_t* seg_off_dev,
                       int32_t nseg, double* out_dev, void* stream);
 
+/* ---------------------------------------------------------------- MPS-level steps
+ * The linear maps around the eigensolver as plans (qcm_plan_upload /
+ * qcm_plan_run, FP64): every map is planned once as gather tiles with its
+ * couplings precomputed, and runs as one gather launch; nothing is done per
+ * block on the host.
+ *
+ * TwoSiteTensor(mps1, mps2) + make_mps (dmrg/framework/dmrg/mp_tensors/
+ * twositetensor.hpp:22-31, 132-139): theta = A . B, reshape_both_to_right,
+ * the SU(2) reduce_right 6j recoupling (mp_tensors/ts_reduction.h:42-141) and
+ * the reshape to left-paired.  Slots: KET = A (left-paired), LEFT = B
+ * (left-paired), OUT = the reduced two-site tensor; its layout and indices
+ * through qcm_plan_out_tensor. */
+int qcm_plan_two_site(const qcm_index_t* phys1, const qcm_index_t* a_left, const qcm_index_t* a_right,
+                      const qcm_blocks_t* a, const qcm_index_t* phys2, const qcm_index_t* b_left,
+                      const qcm_index_t* b_right, const qcm_blocks_t* b, qcm_plan** plan);
+
+/* The prologue of split_mps_l2r/r2l (twositetensor.hpp:141-180 with operator<<,
+ * :372-389): the SU(2) unreduce_left recoupling (ts_reduction.h:143-251) and
+ * reshape_left_to_both.  left_i / right_i are the outer indices of the pair
+ * (left of site i, right of site i+1).  Slots: KET = the reduced two-site
+ * tensor (left-paired), OUT = the both-paired matrix the truncation factorises
+ * (its blocks through qcm_plan_out_tensor; they are the qcm_svd batch). */
+int qcm_plan_split_theta(const qcm_index_t* phys1, const qcm_index_t* phys2, const qcm_index_t* left_i,
+                         const qcm_index_t* right_i, const qcm_blocks_t* u, qcm_plan** plan);
+
+/* The epilogue of split_mps_l2r (l2r != 0: A = U, B = S V) or split_mps_r2l
+ * (A = U S, B = V), after the truncation cut: from the qcm_svd of the split
+ * plan's output blocks (u_off, vt_off, s_off from qcm_svd_block_offsets; S on
+ * the host; keep[k] from qcm_truncation_cut).  Slots: KET = U, LEFT = Vt; OUT =
+ * the new site i (left-paired, qcm_plan_out_tensor which = 0), S2 = the new
+ * site i+1 (left-paired, which = 1); S0 is scratch. */
+int qcm_plan_split_assemble(const qcm_plan* split, const int64_t* u_off, const int64_t* vt_off, const int64_t* keep,
+                            const double* S_host, const int64_t* s_off, int32_t l2r, qcm_plan** plan);
+
+/* Output tensor of an MPS-level plan: block list (q: 4 per block, rows, cols,
+ * element offsets) and its three indices (physical, left, right) concatenated:
+ * n_idx3[i] sectors each, charges idx_q (2 per sector) and sizes idx_size.
+ * Call with NULL arrays first for the counts. */
+int qcm_plan_out_tensor(const qcm_plan* plan, int32_t which, int32_t* nblocks, int32_t* q, int64_t* rows,
+                        int64_t* cols, int64_t* off, int32_t* n_idx3, int32_t* idx_q, int64_t* idx_size);
+
+/* ---------------------------------------------------------------- factorisations
+ * Batched FP64 SVD of independent column-major blocks by one-sided Jacobi, on
+ * the GPU: replaces the per-block LAPACK calls of the truncation and
+ * canonicalisation steps -- gesvd in svd_truncate (dmrg/framework/dmrg/
+ * block_matrix/block_matrix_algorithms.h:163-333), heevd in heev_truncate
+ * (:387-440; for a symmetric positive semi-definite block the SVD is its
+ * eigendecomposition, eigenvalues descending), and the QR / LQ of
+ * leftNormalizeAndReturn / rightNormalizeAndReturn (:442-492, mp_tensors/
+ * mpstensor.hpp:219-258; U and S.Vt serve as the orthonormal factor and the
+ * remainder).  Block k is rows[k] x cols[k] at element src_off[k] of the
+ * source (ld = rows); it yields k_k = min(rows, cols) singular values,
+ * descending, U (rows x k_k, ld rows) and Vt (k_k x cols, ld k_k), packed
+ * block after block (qcm_svd_block_offsets).  The workspace holds the
+ * rotated block and the accumulated rotations (qcm_svd_sizes).  Rounds run
+ * until no pair of columns is rotated in a whole sweep (|a.b| <= 1e-15 |a||b|);
+ * a block still rotating after 40 sweeps makes qcm_svd_run return
+ * QCM_E_RANGE.  min(rows, cols) <= 4096 per block. */
+typedef struct qcm_svd qcm_svd;
+int qcm_svd_create(int32_t nblocks, const int64_t* rows, const int64_t* cols, const int64_t* src_off, qcm_svd** out);
+int qcm_svd_sizes(const qcm_svd* svd, int64_t* work_elems, int64_t* u_elems, int64_t* s_elems, int64_t* vt_elems);
+int qcm_svd_block_offsets(const qcm_svd* svd, int64_t* s_off, int64_t* u_off, int64_t* vt_off);
+int qcm_svd_run(qcm_svd* svd, const double* src, double* work, double* U, double* S, double* Vt, void* stream);
+/* Sweeps of the widest block in the last run (host polls once per such sweep). */
+int qcm_svd_last_sweeps(const qcm_svd* svd, int32_t* sweeps);
+void qcm_svd_destroy(qcm_svd* svd);
+
+/* Truncation results (truncation_results, dmrg/framework/dmrg/block_matrix/
+ * block_matrix_algorithms.h:211-333). */
+typedef struct {
+    int64_t bond_dimension;
+    double truncated_weight;
+    double truncated_fraction;
+    double smallest_ev;
+    double evalscut;
+} qcm_trunc_t;
+
+/* The global cut of estimate_truncation on the device: vals_dev holds each
+ * block's values in descending order, block k at [blk_off[k], blk_off[k+1])
+ * (host array).  evalscut = max(cutoff * s0, s[Mmax]); every value >= evalscut
+ * is kept (Mmax + 1 values when there is no tie, as the reference keeps them);
+ * keep[k] (host) = values kept of block k.  mode 0: singular values, weight =
+ * discarded sum of s^2 / sum of s^2; mode 1: density-matrix eigenvalues, both
+ * weight fields = the discarded fraction (as heev_truncate reports them).  At
+ * most 16384 values.  Synchronises the stream. */
+int qcm_truncation_cut(const double* vals_dev, int32_t nblocks, const int64_t* blk_off, int64_t Mmax, double cutoff,
+                       int32_t mode, int64_t* keep, qcm_trunc_t* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -256,7 +256,7 @@ double conjugate_correction(int lc, int rc, int S) {
 }
 
 // ------------------------------------------------------------------ views of the C-ABI inputs
-static Idx read_index(const qcm_index_t* x) {
+Idx read_index(const qcm_index_t* x) {
     Idx r;
     if (!x) throw std::runtime_error("null index");
     for (int i = 0; i < x->n; ++i) r.d.push_back({Q(x->q[2 * i], x->q[2 * i + 1]), x->size[i]});
@@ -264,7 +264,7 @@ static Idx read_index(const qcm_index_t* x) {
         if (!(r.d[i - 1].first > r.d[i].first)) throw std::runtime_error("index not sorted descending");
     return r;
 }
-static BM read_blocks(const qcm_blocks_t* x) {
+BM read_blocks(const qcm_blocks_t* x) {
     BM r;
     if (!x) throw std::runtime_error("null block list");
     for (int k = 0; k < x->n; ++k) {

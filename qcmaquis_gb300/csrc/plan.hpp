@@ -228,7 +228,10 @@ struct Stage {
 
 // PK_GRAD: gradient of <psi| H_eff |psi> with respect to every MPO term scale
 // PK_DIAG: the diagonal of H_eff (FP64 only)
-enum PlanKind { PK_SIGMA = 0, PK_BLEFT = 1, PK_BRIGHT = 2, PK_GRAD = 3, PK_DIAG = 4 };
+// PK_THETA: two-site tensor from two site tensors; PK_SPLIT: both-paired two-site
+// tensor from the reduced one; PK_ASSEMBLE: the site tensors of a truncated split
+enum PlanKind { PK_SIGMA = 0, PK_BLEFT = 1, PK_BRIGHT = 2, PK_GRAD = 3, PK_DIAG = 4, PK_THETA = 5, PK_SPLIT = 6,
+                PK_ASSEMBLE = 7 };
 
 }  // namespace qcm
 
@@ -243,12 +246,21 @@ struct qcm_plan {
     std::vector<int32_t> out_blk_ptr;
     std::vector<qcm::Blk> out_blocks;
     double gemm_flops = 0, axpy_flops = 0, axpy_bytes = 0;
+    // output tensor of an MPS-level plan (PK_THETA / PK_SPLIT / PK_ASSEMBLE): its block
+    // layout and its indices (physical, left, right); PK_ASSEMBLE has a second output
+    // (the right site, slot OUT2 = S2) in out2_*
+    std::vector<qcm::Blk> out_bm;
+    qcm::Idx out_phys, out_left, out_right;
+    std::vector<qcm::Blk> out2_bm;
+    qcm::Idx out2_phys, out2_left, out2_right;
     bool uploaded = false;
     int device = -1;
 };
 
 namespace qcm {
 void set_error(const std::string& msg);
+Idx read_index(const qcm_index_t* x);
+BM read_blocks(const qcm_blocks_t* x);
 double wigner6j(int, int, int, int, int, int);
 double wigner9j(int, int, int, int, int, int, int, int, int);
 void set_coupling(int a, int b, int c, int d, int e, int f, int g, int h, int i, double init, double out[4]);

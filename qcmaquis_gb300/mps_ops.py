@@ -14,9 +14,11 @@ column-major views into the buffer.  These operations restate:
 * ``leftNormalizeAndReturn`` / ``rightNormalizeAndReturn`` / ``multiply_from_*``:
   ``mp_tensors/mpstensor.hpp:219-330``.
 
-Dense factorisations (SVD, QR) run on the GPU through torch.linalg (cuSOLVER);
-block products through torch.matmul (cuBLAS).  Nothing here runs on the CPU
-except index bookkeeping and the truncation decision on the singular values.
+Dense factorisations (SVD, density-matrix eigendecomposition, the QR/LQ of the
+canonicalisation) run in the library's batched FP64 Jacobi SVD (``qcm_svd_*``)
+and the truncation cut in its device cut (``qcm_truncation_cut``); block
+products through torch.matmul.  Nothing here runs on the CPU except index
+bookkeeping.
 """
 from __future__ import annotations
 
@@ -341,67 +343,59 @@ class Trunc:
         self.smallest_ev = smallest_ev
 
 
+def _stream(dev) -> int:
+    return int(torch.cuda.current_stream(dev).cuda_stream)
+
+
+def batched_svd(M: DBM):
+    """FP64 SVD of every block of M in one batch on the GPU (``qcm_svd_*``, one-sided
+    Jacobi, hand-written; replaces the per-block LAPACK gesvd/heevd/geqrf of the
+    reference).  Returns the ``native.BatchedSVD`` with U, S (descending), Vt."""
+    lay, flat = M.to_flat()
+    svd = N.BatchedSVD([tuple(b.shape) for b in M.blocks], lay.offsets)
+    svd.run(flat, _stream(flat.device))
+    return svd
+
+
 def svd_truncate(M: DBM, rel_tol: float, Mmax: int):
-    """Per-block SVD on the GPU, global cut on the host (``block_matrix_algorithms.h:210-333``)."""
-    Us, Ss, Vs = [], [], []
-    for b in M.blocks:
-        u, s, vh = torch.linalg.svd(b, full_matrices=False)
-        Us.append(u)
-        Ss.append(s)
-        Vs.append(vh)
-    svals = [s.detach().cpu().numpy() for s in Ss]
-    allv = np.sort(np.concatenate(svals))[::-1]
-    evalscut = rel_tol * allv[0]
-    if allv.size > Mmax:
-        evalscut = max(evalscut, allv[Mmax])
-    smallest_ev = evalscut / allv[0]
-    disc = allv[allv < evalscut]
-    tfrac = float(disc.sum() / allv.sum())
-    tw = float((disc * disc).sum() / (allv * allv).sum())
-    keeps = [int(np.argmax(s < evalscut)) if np.any(s < evalscut) else s.size for s in svals]
+    """``svd_truncate`` + ``estimate_truncation`` (``block_matrix_algorithms.h:210-333``):
+    the batched device SVD of all blocks, then the global cut on the device
+    (``qcm_truncation_cut``: keep every s >= max(cutoff s0, s[Mmax]); weight and
+    fraction of the discarded values without multiplicity weighting)."""
+    svd = batched_svd(M)
+    keep, tr = svd.cut(Mmax, rel_tol, 0, _stream(svd.S.device))
     U, V = DBM(), DBM()
     S: Dict = {}
-    for k, (key, kk) in enumerate(zip(M.keys, keeps)):
+    for k, (key, kk) in enumerate(zip(M.keys, keep)):
+        kk = int(kk)
         if kk == 0:
             continue
         lc, rc = key
-        U.insert(Us[k][:, :kk], lc, rc)
-        V.insert(Vs[k][:kk, :], rc, rc)
-        S[rc] = Ss[k][:kk]
-    return U, S, V, Trunc(sum(keeps), tw, tfrac, smallest_ev)
+        U.insert(svd.u(k)[:, :kk], lc, rc)
+        V.insert(svd.vt(k)[:kk, :], rc, rc)
+        S[rc] = svd.s(k)[:kk]
+    return U, S, V, Trunc(int(tr.bond_dimension), tr.truncated_weight, tr.truncated_fraction, tr.smallest_ev)
 
 
 def heev_truncate(dm: DBM, cutoff: float, Mmax: int):
     """``heev_truncate`` + ``estimate_truncation`` (``block_matrix_algorithms.h:188-200,
-    211-251, 388-440``): per-block eigendecomposition on the GPU (cuSOLVER, FP64),
-    eigenpairs in descending order (``algorithms.hpp:402-421``), the global cut on
-    the eigenvalues on the host.  The truncated fraction is returned in both
-    weight fields, as the reference does."""
-    Us, evs = [], []
-    for b in dm.blocks:
-        w, v = torch.linalg.eigh(b)
-        evs.append(torch.flip(w, [0]))
-        Us.append(torch.flip(v, [1]))
-    sizes = [int(e.numel()) for e in evs]
-    host = torch.cat(evs).cpu().numpy() if evs else np.zeros(0)
-    evals = np.split(host, np.cumsum(sizes)[:-1]) if sizes else []
-    allv = np.sort(host)[::-1]
-    evalscut = cutoff * allv[0]
-    if allv.size > Mmax:
-        evalscut = max(evalscut, allv[Mmax])
-    smallest_ev = evalscut / allv[0]
-    disc = allv[allv < evalscut]
-    tfrac = float(disc.sum() / allv.sum())
-    keeps = [int(np.argmax(e < evalscut)) if np.any(e < evalscut) else e.size for e in evals]
+    211-251, 388-440``): the eigendecomposition of every (symmetric positive
+    semi-definite) density-matrix block in one batch on the GPU -- its SVD, which
+    gives the eigenpairs in descending order (``algorithms.hpp:402-421``) -- and the
+    global cut on the eigenvalues on the device.  The truncated fraction is
+    returned in both weight fields, as the reference does."""
+    svd = batched_svd(dm)
+    keep, tr = svd.cut(Mmax, cutoff, 1, _stream(svd.S.device))
     U = DBM()
     S: Dict = {}
-    for k, (key, kk) in enumerate(zip(dm.keys, keeps)):
+    for k, (key, kk) in enumerate(zip(dm.keys, keep)):
+        kk = int(kk)
         if kk == 0:
             continue
         lc, rc = key
-        U.insert(Us[k][:, :kk], lc, rc)
-        S[rc] = evs[k][:kk]
-    return U, S, Trunc(sum(keeps), tfrac, tfrac, smallest_ev)
+        U.insert(svd.u(k)[:, :kk], lc, rc)
+        S[rc] = svd.s(k)[:kk]
+    return U, S, Trunc(int(tr.bond_dimension), tr.truncated_fraction, tr.truncated_fraction, tr.smallest_ev)
 
 
 def _transpose(M: DBM) -> DBM:
@@ -573,22 +567,31 @@ def predict_new_state(u: DeviceMPSTensor, mpo, left, right, alpha: float, cutoff
 
 
 def left_normalize_and_return(t: DeviceMPSTensor) -> Tuple[DeviceMPSTensor, DBM]:
+    """``leftNormalizeAndReturn`` (``mp_tensors/mpstensor.hpp:219-236``): every left-paired
+    block M = Q R with Q having orthonormal columns.  The factorisation is the batched
+    device SVD, Q = U and R = S Vt: the same bond dimensions and the same product Q R
+    as the reference's QR, in a different (orthogonal) gauge of the new bond, which no
+    energy, overlap or truncation weight depends on."""
+    svd = N.BatchedSVD(t.layout.shapes, t.layout.offsets)
+    svd.run(t.data, _stream(t.data.device))
     Q, R = DBM(), DBM()
-    for (lc, rc), b in zip(t.layout.keys, as_dbm(t).blocks):
-        q, r = torch.linalg.qr(b, mode="reduced")
-        Q.insert(q, lc, rc)
-        R.insert(r, rc, rc)
+    for k, (lc, rc) in enumerate(t.layout.keys):
+        Q.insert(svd.u(k), lc, rc)
+        R.insert(svd.s(k)[:, None] * svd.vt(k), rc, rc)
     new_right = Q.right_basis()
     return from_dbm(t.phys_i, t.left_i, new_right, Q), R
 
 
 def right_normalize_and_return(t: DeviceMPSTensor) -> Tuple[DeviceMPSTensor, DBM]:
+    """``rightNormalizeAndReturn`` (``mp_tensors/mpstensor.hpp:238-258``): every
+    right-paired block M = L Q with Q having orthonormal rows, from the batched device
+    SVD (L = U S, Q = Vt; the gauge remark of ``left_normalize_and_return`` applies)."""
     rp = reshape_l2r(t.phys_i, t.left_i, t.right_i, as_dbm(t))
+    svd = batched_svd(rp)
     Lm, Q = DBM(), DBM()
-    for (lc, rc), b in zip(rp.keys, rp.blocks):
-        q, r = torch.linalg.qr(b.t(), mode="reduced")
-        Lm.insert(r.t(), lc, lc)
-        Q.insert(q.t(), lc, rc)
+    for k, (lc, rc) in enumerate(rp.keys):
+        Lm.insert(svd.u(k) * svd.s(k)[None, :], lc, lc)
+        Q.insert(svd.vt(k), lc, rc)
     new_left = Q.left_basis()
     return from_dbm(t.phys_i, new_left, t.right_i, reshape_r2l(t.phys_i, new_left, t.right_i, Q)), Lm
 

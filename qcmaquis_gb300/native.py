@@ -121,8 +121,115 @@ def lib():
                                         C.c_void_p]
     L.qcm_seg_multi_dot.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                     C.c_void_p, C.c_void_p]
+    L.qcm_plan_two_site.argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks)] + [C.POINTER(CIndex)] * 3 + \
+        [C.POINTER(CBlocks), C.POINTER(C.c_void_p)]
+    L.qcm_plan_split_theta.argtypes = [C.POINTER(CIndex)] * 4 + [C.POINTER(CBlocks), C.POINTER(C.c_void_p)]
+    L.qcm_plan_split_assemble.argtypes = [C.c_void_p, i64p, i64p, i64p, f64p, i64p, C.c_int32,
+                                          C.POINTER(C.c_void_p)]
+    L.qcm_plan_out_tensor.argtypes = [C.c_void_p, C.c_int32, i32p, i32p, i64p, i64p, i64p, i32p, i32p, i64p]
+    L.qcm_svd_create.argtypes = [C.c_int32, i64p, i64p, i64p, C.POINTER(C.c_void_p)]
+    L.qcm_svd_sizes.argtypes = [C.c_void_p, i64p, i64p, i64p, i64p]
+    L.qcm_svd_block_offsets.argtypes = [C.c_void_p, i64p, i64p, i64p]
+    L.qcm_svd_run.argtypes = [C.c_void_p] + [C.c_void_p] * 6
+    L.qcm_svd_last_sweeps.argtypes = [C.c_void_p, i32p]
+    L.qcm_svd_destroy.argtypes = [C.c_void_p]
+    L.qcm_svd_destroy.restype = None
+    L.qcm_truncation_cut.argtypes = [C.c_void_p, C.c_int32, i64p, C.c_int64, C.c_double, C.c_int32, i64p,
+                                     C.POINTER(CTrunc), C.c_void_p]
     _lib = L
     return L
+
+
+class CTrunc(C.Structure):
+    _fields_ = [("bond_dimension", C.c_int64), ("truncated_weight", C.c_double),
+                ("truncated_fraction", C.c_double), ("smallest_ev", C.c_double), ("evalscut", C.c_double)]
+
+
+class BatchedSVD:
+    """FP64 SVD of a batch of independent blocks on the GPU (``qcm_svd_*``: one-sided
+    Jacobi).  ``shapes`` = [(rows, cols)], ``offsets`` = element offsets of the
+    column-major blocks in the source buffer.  ``run`` returns flat device arrays
+    U, S, Vt packed block after block; ``u(k)``, ``s(k)``, ``vt(k)`` are views of block
+    k (U: rows x k_k, S: k_k descending, Vt: k_k x cols)."""
+
+    def __init__(self, shapes, offsets):
+        self.shapes = [(int(r), int(c)) for r, c in shapes]
+        n = len(self.shapes)
+        rows = np.array([r for r, _ in self.shapes] or [0], dtype=np.int64)
+        cols = np.array([c for _, c in self.shapes] or [0], dtype=np.int64)
+        offs = np.array(list(offsets) or [0], dtype=np.int64)
+        h = C.c_void_p()
+        check(lib().qcm_svd_create(n, _p(rows, i64p), _p(cols, i64p), _p(offs, i64p), C.byref(h)), "qcm_svd_create")
+        self.h = h
+        w, u, sv, vt = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        check(lib().qcm_svd_sizes(h, C.byref(w), C.byref(u), C.byref(sv), C.byref(vt)), "qcm_svd_sizes")
+        self.sizes = (w.value, u.value, sv.value, vt.value)
+        self.s_off = np.zeros(max(n, 1), dtype=np.int64)
+        self.u_off = np.zeros(max(n, 1), dtype=np.int64)
+        self.vt_off = np.zeros(max(n, 1), dtype=np.int64)
+        check(lib().qcm_svd_block_offsets(h, _p(self.s_off, i64p), _p(self.u_off, i64p), _p(self.vt_off, i64p)),
+              "qcm_svd_block_offsets")
+        self.U = self.S = self.Vt = None
+
+    def run(self, src, stream, work=None):
+        import torch
+        dev = src.device
+        w, u, sv, vt = self.sizes
+        work = torch.empty(max(w, 1), dtype=torch.float64, device=dev) if work is None else work
+        self.U = torch.empty(max(u, 1), dtype=torch.float64, device=dev)
+        self.S = torch.empty(max(sv, 1), dtype=torch.float64, device=dev)
+        self.Vt = torch.empty(max(vt, 1), dtype=torch.float64, device=dev)
+        check(lib().qcm_svd_run(self.h, C.c_void_p(src.data_ptr()), C.c_void_p(work.data_ptr()),
+                                C.c_void_p(self.U.data_ptr()), C.c_void_p(self.S.data_ptr()),
+                                C.c_void_p(self.Vt.data_ptr()), C.c_void_p(stream)), "qcm_svd_run")
+        return self.U, self.S, self.Vt
+
+    def k(self, i):
+        r, c = self.shapes[i]
+        return min(r, c)
+
+    def u(self, i):
+        r, c = self.shapes[i]
+        k = min(r, c)
+        o = int(self.u_off[i])
+        return self.U[o:o + r * k].view(k, r).t()
+
+    def s(self, i):
+        o = int(self.s_off[i])
+        return self.S[o:o + self.k(i)]
+
+    def vt(self, i):
+        r, c = self.shapes[i]
+        k = min(r, c)
+        o = int(self.vt_off[i])
+        return self.Vt[o:o + k * c].view(c, k).t()
+
+    def sweeps(self) -> int:
+        n = C.c_int32()
+        check(lib().qcm_svd_last_sweeps(self.h, C.byref(n)), "qcm_svd_last_sweeps")
+        return n.value
+
+    def cut(self, Mmax: int, cutoff: float, mode: int, stream):
+        """The device truncation cut over this batch's values (see ``qcm_truncation_cut``);
+        returns (keep per block, qcm_trunc_t)."""
+        n = len(self.shapes)
+        blk = np.zeros(n + 1, dtype=np.int64)
+        for i in range(n):
+            blk[i + 1] = blk[i] + self.k(i)
+        keep = np.zeros(max(n, 1), dtype=np.int64)
+        tr = CTrunc()
+        check(lib().qcm_truncation_cut(C.c_void_p(self.S.data_ptr()), n, _p(blk, i64p), int(Mmax), float(cutoff),
+                                       int(mode), _p(keep, i64p), C.byref(tr), C.c_void_p(stream)),
+              "qcm_truncation_cut")
+        return keep[:n], tr
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().qcm_svd_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
 
 
 def check(rc: int, what: str = ""):
@@ -585,6 +692,64 @@ class Plan:
             check(lib().qcm_plan_stage_info(self.h, s, C.byref(k), C.byref(a), C.byref(b)), "stage_info")
             kinds.append(("axpy", "gemm", "zero")[k.value])
         return kinds
+
+
+def out_tensor(plan: "Plan", which: int = 0):
+    """Output tensor of an MPS-level plan (``qcm_plan_out_tensor``): (phys, left, right,
+    Layout with the plan's offsets)."""
+    nb = C.c_int32()
+    n3 = (C.c_int32 * 3)()
+    check(lib().qcm_plan_out_tensor(plan.h, which, C.byref(nb), None, None, None, None, n3, None, None),
+          "qcm_plan_out_tensor")
+    n = max(nb.value, 1)
+    ni = max(n3[0] + n3[1] + n3[2], 1)
+    q = np.zeros(4 * n, dtype=np.int32)
+    rows, cols, off = (np.zeros(n, dtype=np.int64) for _ in range(3))
+    iq = np.zeros(2 * ni, dtype=np.int32)
+    isz = np.zeros(ni, dtype=np.int64)
+    check(lib().qcm_plan_out_tensor(plan.h, which, C.byref(nb), _p(q, i32p), _p(rows, i64p), _p(cols, i64p),
+                                    _p(off, i64p), n3, _p(iq, i32p), _p(isz, i64p)), "qcm_plan_out_tensor")
+    nb = nb.value
+    keys = [((int(q[4 * k]), int(q[4 * k + 1])), (int(q[4 * k + 2]), int(q[4 * k + 3]))) for k in range(nb)]
+    shapes = [(int(rows[k]), int(cols[k])) for k in range(nb)]
+    idx, base = [], 0
+    for i in range(3):
+        idx.append(Index.from_sorted([((int(iq[2 * (base + k)]), int(iq[2 * (base + k) + 1])), int(isz[base + k]))
+                                      for k in range(n3[i])]))
+        base += n3[i]
+    return idx[0], idx[1], idx[2], Layout(keys, shapes, [int(x) for x in off[:nb]])
+
+
+def plan_two_site(a_phys, a_left, a_right, a_lay: "Layout", b_phys, b_left, b_right, b_lay: "Layout") -> "Plan":
+    """``qcm_plan_two_site``: the reduced two-site tensor of sites (i, i+1) from their
+    left-paired tensors (slots KET = A, LEFT = B, OUT = the two-site tensor)."""
+    f = [FIndex(x) for x in (a_phys, a_left, a_right, b_phys, b_left, b_right)]
+    h = C.c_void_p()
+    check(lib().qcm_plan_two_site(C.byref(f[0].c), C.byref(f[1].c), C.byref(f[2].c), C.byref(a_lay.c),
+                                  C.byref(f[3].c), C.byref(f[4].c), C.byref(f[5].c), C.byref(b_lay.c), C.byref(h)),
+          "qcm_plan_two_site")
+    return Plan(h, "theta")
+
+
+def plan_split_theta(p1, p2, left_i, right_i, u_lay: "Layout") -> "Plan":
+    """``qcm_plan_split_theta``: the both-paired two-site tensor (slot OUT) from the
+    reduced left-paired one (slot KET)."""
+    f = [FIndex(x) for x in (p1, p2, left_i, right_i)]
+    h = C.c_void_p()
+    check(lib().qcm_plan_split_theta(C.byref(f[0].c), C.byref(f[1].c), C.byref(f[2].c), C.byref(f[3].c),
+                                     C.byref(u_lay.c), C.byref(h)), "qcm_plan_split_theta")
+    return Plan(h, "split")
+
+
+def plan_split_assemble(split: "Plan", u_off, vt_off, keep, S_host, s_off, l2r: bool) -> "Plan":
+    """``qcm_plan_split_assemble``: the two new site tensors of a truncated SVD split
+    (slots KET = U, LEFT = Vt; OUT = site i left-paired, S2 = site i+1 left-paired)."""
+    a = [np.ascontiguousarray(x, dtype=np.int64) for x in (u_off, vt_off, keep, s_off)]
+    sv = np.ascontiguousarray(S_host, dtype=np.float64)
+    h = C.c_void_p()
+    check(lib().qcm_plan_split_assemble(split.h, _p(a[0], i64p), _p(a[1], i64p), _p(a[2], i64p), _p(sv, f64p),
+                                        _p(a[3], i64p), 1 if l2r else 0, C.byref(h)), "qcm_plan_split_assemble")
+    return Plan(h, "assemble")
 
 
 class CPlanOpts(C.Structure):
