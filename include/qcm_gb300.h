@@ -380,6 +380,83 @@ int qcm_multi_dot_noalloc(const double* const* v_dev_ptrs, int32_t nvec, const d
 int qcm_seg_multi_dot(const double* const* v_dev_ptrs, int32_t nvec, const double* y, const int64_t* seg_off_dev,
                       int32_t nseg, double* out_dev, void* stream);
 
+/* Truncation results (truncation_results, dmrg/framework/dmrg/block_matrix/
+ * block_matrix_algorithms.h:211-333). */
+typedef struct {
+    int64_t bond_dimension;
+    double truncated_weight;
+    double truncated_fraction;
+    double smallest_ev;
+    double evalscut;
+} qcm_trunc_t;
+
+/* ---------------------------------------------------------------- execution context
+ * A context owns what plan runs need besides the caller's tensors: its CUDA
+ * stream, the plans' scratch slots and operand-image buffer, FP32 shadows of
+ * the boundaries for the mixed forms, and the eigensolver's basis vectors and
+ * reduction workspace (SURVEY's proposed qcm_ctx; the reference has no
+ * counterpart -- its Engine calls allocate per call).  Its device buffers grow
+ * on demand and are freed by qcm_ctx_destroy.  Calls on one context run in
+ * order on its stream and are not reentrant; different contexts share nothing.
+ * Created on the current device. */
+typedef struct qcm_ctx qcm_ctx;
+int qcm_ctx_create(void* stream, qcm_ctx** ctx);
+int qcm_ctx_set_stream(qcm_ctx* ctx, void* stream);
+void qcm_ctx_destroy(qcm_ctx* ctx);
+
+/* Run any plan with the context's scratch: ket/left/right/out fill the KET,
+ * LEFT, RIGHT and OUT slots (FP64 device arrays; NULL where the plan reads
+ * none).  The mixed forms convert left/right (left_elems / right_elems
+ * doubles) to FP32 shadows first. */
+int qcm_ctx_run(qcm_ctx* ctx, qcm_plan* plan, const double* ket, const double* left, int64_t left_elems,
+                const double* right, int64_t right_elems, double* out, int32_t precision);
+
+/* One boundary update (BoundaryPropagator::updateLeftBoundary / updateRightBoundary,
+ * dmrg/framework/dmrg/SweepBasedAlgorithms/BoundaryPropagator.h:98-122 ->
+ * overlap_mpo_left_step / overlap_mpo_right_step): a plan of
+ * qcm_plan_boundary_left / _right run on the context; boundary is L[i] (left)
+ * or R[i+1] (right), out the new boundary (qcm_plan_out_layout). */
+int qcm_boundary_step(qcm_ctx* ctx, qcm_plan* plan, const double* mps, const double* boundary, int64_t boundary_elems,
+                      double* out, int32_t precision);
+
+/* Jacobi-Davidson eigensolver of one site problem (solve_ietl_jcd,
+ * dmrg/framework/dmrg/optimize/ietl_jacobi_davidson.h:16-77, with
+ * jacobi_davidson::calculate_eigenvalue, dmrg/framework/ietl/jacobi.h:361-451,
+ * zero GMRES steps as on the reference's live path): the smallest eigenpair of
+ * H_eff = the sigma plan on (left, right) in the given precision, from init (n
+ * doubles, the plan's ket layout), stopping when |r| <= tol |theta|, |r| < tol
+ * or after maxiter (<= 32) steps.  ortho: device vectors the solution is kept
+ * orthogonal to (excited states; <= 16).  Writes the eigenvector to out_vec
+ * (device), the eigenvalue and the iterations to the host.  Vector algebra
+ * and Gram-Schmidt run in FP64 on the context's stream; two host
+ * synchronisations per iteration (projected-matrix column, residual norm). */
+int qcm_jcd_solve(qcm_ctx* ctx, qcm_plan* sigma, const double* left, int64_t left_elems, const double* right,
+                  int64_t right_elems, int32_t precision, const double* init, int64_t n, double tol, int32_t maxiter,
+                  const double* const* ortho, int32_t n_ortho, double* out_vec, double* out_energy,
+                  int32_t* out_iters);
+
+/* TwoSiteTensor::split_mps_l2r / split_mps_r2l (dmrg/framework/dmrg/mp_tensors/
+ * twositetensor.hpp:141-180, with svd_truncate, dmrg/framework/dmrg/
+ * block_matrix/block_matrix_algorithms.h:163-333) of the reduced two-site
+ * tensor u (layout u, data u_dev; phys1/phys2 the sites' physical indices,
+ * left_i / right_i the pair's outer indices), entirely on the device: the
+ * split-prologue plan, the batched Jacobi SVD of the both-paired blocks, the
+ * device cut (Mmax, cutoff) and the assembly plan.  l2r != 0: A = U, B = S V;
+ * else A = U S, B = V.  The new site tensors (left-paired, with their indices)
+ * are owned by the result (qcm_split_result_tensor: which 0 = site i, 1 = site
+ * i+1; the same arrays as qcm_plan_out_tensor plus the device data pointer,
+ * valid until qcm_split_result_destroy); trunc receives bond dimension,
+ * truncated weight and fraction, and smallest_ev as the reference reports
+ * them.  Synchronises the context's stream. */
+typedef struct qcm_split_result qcm_split_result;
+int qcm_split(qcm_ctx* ctx, const qcm_index_t* phys1, const qcm_index_t* phys2, const qcm_index_t* left_i,
+              const qcm_index_t* right_i, const qcm_blocks_t* u, const double* u_dev, int32_t l2r, int64_t Mmax,
+              double cutoff, qcm_trunc_t* trunc, qcm_split_result** out);
+int qcm_split_result_tensor(const qcm_split_result* res, int32_t which, int32_t* nblocks, int32_t* q, int64_t* rows,
+                            int64_t* cols, int64_t* off, int32_t* n_idx3, int32_t* idx_q, int64_t* idx_size,
+                            const double** data);
+void qcm_split_result_destroy(qcm_split_result* res);
+
 /* ---------------------------------------------------------------- MPS-level steps
  * The linear maps around the eigensolver as plans (qcm_plan_upload /
  * qcm_plan_run, FP64): every map is planned once as gather tiles with its
@@ -447,15 +524,6 @@ int qcm_svd_run(qcm_svd* svd, const double* src, double* work, double* U, double
 int qcm_svd_last_sweeps(const qcm_svd* svd, int32_t* sweeps);
 void qcm_svd_destroy(qcm_svd* svd);
 
-/* Truncation results (truncation_results, dmrg/framework/dmrg/block_matrix/
- * block_matrix_algorithms.h:211-333). */
-typedef struct {
-    int64_t bond_dimension;
-    double truncated_weight;
-    double truncated_fraction;
-    double smallest_ev;
-    double evalscut;
-} qcm_trunc_t;
 
 /* The global cut of estimate_truncation on the device: vals_dev holds each
  * block's values in descending order, block k at [blk_off[k], blk_off[k+1])

@@ -174,6 +174,16 @@ class Engine:
         self.launches = 0
 
     # -- helpers ---------------------------------------------------------
+    def context(self) -> N.Context:
+        """The engine's native context (``qcm_ctx``) on the current stream."""
+        c = getattr(self, "_ctx", None)
+        if c is None:
+            with torch.cuda.device(self.device):
+                c = self._ctx = N.Context(self._stream())
+        else:
+            c.set_stream(self._stream())
+        return c
+
     def fmpo(self, mpo) -> N.FMpo:
         if isinstance(mpo, N.FMpo):     # already flattened (the native two-site builder)
             return mpo

@@ -10,9 +10,10 @@ stop when ||r|| <= tol*|theta| or ||r|| < tol or after maxiter steps, else
 t = -r + (r.u / u.u) u.
 
 Vectors are flat FP64 CUDA buffers in the two-site tensor's left-paired
-layout; dot products, norms and updates use the library's deterministic
-reductions.  The k x k (k <= maxiter) projected eigenproblem is solved on the
-host in FP64 (the reference uses LAPACK dsyevx there too).
+layout; the iteration runs in native code (``qcm_jcd_solve``) with the
+library's deterministic reductions.  The k x k (k <= maxiter) projected
+eigenproblem is solved on the host in FP64 (the reference uses LAPACK dsyevx
+there too).  ``VecOps`` exposes the vector kernels to the batched solver.
 """
 from __future__ import annotations
 
@@ -60,78 +61,34 @@ def solve_ietl_jcd(sp: SiteProblem, init: DeviceMPSTensor, tol: float = 1e-8, ma
                    ortho: Optional[Sequence[torch.Tensor]] = None, completeness: float = 1e-10):
     """Smallest eigenpair of H_eff; returns (theta, eigenvector tensor, iterations).
 
+    Runs the library's native Jacobi-Davidson (``qcm_jcd_solve``: the iteration of
+    ``jacobi.h:361-451`` with zero GMRES steps, every Gram-Schmidt and projection
+    coefficient kept on the device) on the engine's context, with the site
+    problem's sigma plan in the engine's precision.
+
     ``ortho``: flat vectors in ``init``'s layout the solution is kept orthogonal
     to (excited states, ``ietl_jacobi_davidson.h:28-49``): Gram-Schmidt among
-    themselves (dropped at norm <= ``completeness``), projected out of the start
-    vector, of every new basis vector and of A u before the residual
+    themselves (dropped at norm <= 1e-10), projected out of the start vector, of
+    every new basis vector and of A u before the residual
     (``SingleSiteVS::project``, ``jacobi.h:378, 393, 432``).  With nothing left of
     the start vector after the projection the solve is skipped: (<init|A init>,
     init, 0)."""
-    dev = init.data.device
-    ops = VecOps(dev)
-    n = init.n
-    local: List[torch.Tensor] = []
-    for o in list(ortho or [])[:max(n - 1, 0)]:
-        v = o.clone()
-        for q in local:
-            ops.axpby(-ops.dot(q, v), q, 1.0, v)
-        nv = ops.nrm2(v)
-        if nv > completeness:
-            ops.axpby(1.0 / nv, v, 0.0, v)
-            local.append(v)
-
-    def project(x: torch.Tensor):
-        for q in local:
-            ops.axpby(-ops.dot(q, x) / ops.dot(q, q), q, 1.0, x)
-
-    if local:
-        tmp = init.data.clone()
-        for q in local:
-            ops.axpby(-ops.dot(tmp, q), q, 1.0, tmp)
-        if ops.nrm2(tmp) < completeness:
-            return ops.dot(init.data, sp.apply(init).data), init, 0
-    V: List[torch.Tensor] = []
-    VA: List[torch.Tensor] = []
-    M = np.zeros((maxiter, maxiter))
-    kappa = 0.25
-    t = init.data.clone()
-    project(t)
-    it = 0
-    while True:
-        tau = ops.nrm2(t)
-        for i in range(it):
-            ops.axpby(-ops.dot(V[i], t), V[i], 1.0, t)
-        if ops.nrm2(t) < kappa * tau:
-            for i in range(it):
-                ops.axpby(-ops.dot(V[i], t), V[i], 1.0, t)
-        project(t)
-        nt = ops.nrm2(t)
-        ops.axpby(1.0 / nt, t, 0.0, t)
-        V.append(t)
-        va = sp.apply(init.like(t)).data
-        VA.append(va)
-        col = ops.multi_dot(V, va)
-        M[:it + 1, it] = col
-        k = it + 1
-        Ms = np.triu(M[:k, :k]) + np.triu(M[:k, :k], 1).T
-        w, z = np.linalg.eigh(Ms)
-        theta = float(w[0])
-        s = z[:, 0]
-        u = torch.empty(n, dtype=torch.float64, device=dev)
-        uA = torch.empty(n, dtype=torch.float64, device=dev)
-        ops.lincomb(V, s, u)
-        ops.lincomb(VA, s, uA)
-        project(uA)
-        ops.axpby(-theta, u, 1.0, uA)  # r = uA - theta u  (in uA)
-        it += 1
-        rn = ops.nrm2(uA)
-        if rn <= tol * abs(theta) or rn < tol or it >= maxiter:
-            return theta, init.like(u), it
-        ru = ops.dot(uA, u)
-        uu = ops.dot(u, u)
-        t = torch.empty(n, dtype=torch.float64, device=dev)
-        ops.axpby(-1.0, uA, 0.0, t)
-        ops.axpby(ru / uu, u, 1.0, t)
+    if completeness != 1e-10:
+        raise ValueError("the native solver drops constraint vectors below a norm of 1e-10")
+    eng = sp.engine
+    plan = eng.sigma_plan(init, sp.left, sp.right, sp.mpo)
+    ctx = eng.context()
+    out = torch.empty_like(init.data)
+    e, it = C.c_double(), C.c_int32()
+    ov = list(ortho or [])
+    arr = (C.c_void_p * max(len(ov), 1))(*[C.c_void_p(v.data_ptr()) for v in ov]) if ov else None
+    lt, rt = sp.left.data, sp.right.data
+    N.check(N.lib().qcm_jcd_solve(ctx.h, plan.h, C.c_void_p(lt.data_ptr()), lt.numel(), C.c_void_p(rt.data_ptr()),
+                                  rt.numel(), eng.precision, C.c_void_p(init.data.data_ptr()), init.n, float(tol),
+                                  int(maxiter), arr, len(ov), C.c_void_p(out.data_ptr()), C.byref(e), C.byref(it)),
+            "qcm_jcd_solve")
+    eng.launches += it.value * plan.last_kernels()
+    return e.value, init.like(out), it.value
 
 
 __all__ = ["solve_ietl_jcd", "VecOps"]

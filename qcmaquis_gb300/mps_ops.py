@@ -320,19 +320,69 @@ def as_dbm(t: DeviceMPSTensor) -> DBM:
     return block_views(t.layout, t.data)
 
 
+class _PlanRunner:
+    """Plans of the MPS-level maps, cached by layout content, and their scratch."""
+
+    def __init__(self, size: int = 16):
+        self.plans: Dict = {}
+        self.size = size
+        self.ws: Dict = {}
+
+    def plan(self, key, make):
+        p = self.plans.get(key)
+        if p is None:
+            p = make()
+            p.upload()
+            while len(self.plans) >= self.size:
+                self.plans.pop(next(iter(self.plans)))
+            self.plans[key] = p
+        else:
+            self.plans[key] = self.plans.pop(key)
+        return p
+
+    def scratch(self, device, sizes):
+        from .engine import Workspace
+        w = self.ws.get(device)
+        if w is None:
+            w = self.ws[device] = Workspace(device)
+        return w.get(list(sizes) + [1])[:3]
+
+
+_RUNNER = _PlanRunner()
+
+
+def _run_fp64(plan, device, ket=None, left=None, out=None, s2=None):
+    s0, s1, s2w = _RUNNER.scratch(device, plan.scratch)
+    ptr = lambda t: 0 if t is None else int(t.data_ptr())
+    plan.run_typed([ptr(ket), ptr(left), 0, ptr(out), ptr(s0), ptr(s1), ptr(s2 if s2 is not None else s2w), 0], 0,
+                   N.PREC_FP64, _stream(device))
+
+
 def make_two_site_mps(A: DeviceMPSTensor, B: DeviceMPSTensor) -> DeviceMPSTensor:
-    """theta = A(lp).B(rp), reshaped both->right and SU(2)-reduced, returned left-paired."""
-    Brp = reshape_l2r(B.phys_i, B.left_i, B.right_i, as_dbm(B))
-    theta = gemm(as_dbm(A), Brp)
-    rp = _both_to_right(A.phys_i, B.phys_i, A.left_i, B.right_i, theta)
-    phys2, red = reduce_right(A.phys_i, B.phys_i, A.left_i, B.right_i, rp)
-    # MPSTensor(phys2, left, right, red, RightPaired): left index from the blocks
-    new_left = red.left_basis()
-    possible_right = index_product(phys2, new_left)
-    right = B.right_i.copy()
-    common_subset(right, possible_right)
-    lp = reshape_r2l(phys2, new_left, right, red)
-    return from_dbm(phys2, new_left, right, lp)
+    """``TwoSiteTensor(mps1, mps2)`` + ``make_mps``: theta = A(lp).B(rp), reshaped
+    both->right, SU(2)-reduced (6j), returned left-paired -- one native plan
+    (``qcm_plan_two_site``: the grouped block product and three planned gather maps)."""
+    from .engine import _digest
+    key = ("theta", _digest(A.phys_i, A.left_i, A.right_i, A.layout, B.phys_i, B.left_i, B.right_i, B.layout))
+    plan = _RUNNER.plan(key, lambda: N.plan_two_site(A.phys_i, A.left_i, A.right_i, A.layout, B.phys_i, B.left_i,
+                                                     B.right_i, B.layout))
+    phys2, left, right, lay = N.out_tensor(plan)
+    out = torch.empty(max(plan.out_elems, 1), dtype=torch.float64, device=A.data.device)
+    _run_fp64(plan, A.data.device, ket=A.data, left=B.data, out=out)
+    return DeviceMPSTensor(phys2, left, right, lay, out)
+
+
+def split_theta(u: DeviceMPSTensor, A0: DeviceMPSTensor, B0: DeviceMPSTensor):
+    """``tst << u`` followed by ``reshape_left_to_both``: the both-paired matrix of the
+    two-site tensor (native plan ``qcm_plan_split_theta``: the 6j unreduce_left and the
+    reshape as planned gather maps).  Returns (plan, layout, flat device buffer)."""
+    from .engine import _digest
+    key = ("split", _digest(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, u.layout))
+    plan = _RUNNER.plan(key, lambda: N.plan_split_theta(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, u.layout))
+    _, _, _, lay = N.out_tensor(plan)
+    out = torch.empty(max(plan.out_elems, 1), dtype=torch.float64, device=u.data.device)
+    _run_fp64(plan, u.data.device, ket=u.data, out=out)
+    return plan, lay, out
 
 
 class Trunc:
@@ -474,24 +524,27 @@ def split(u: DeviceMPSTensor, A0: DeviceMPSTensor, B0: DeviceMPSTensor, Mmax: in
     (the left / right site's MPO tensor) are given and alpha != 0.  (The
     reference computes the alpha = 0 perturbation and adds zeros; skipping it
     gives the same matrix.)  Returns new (A, B, truncation results)."""
-    _, tst = unreduce_left(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, as_dbm(u))
-    both = _left_to_both(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, tst)
+    sp, blay, bflat = split_theta(u, A0, B0)
     p1, p2 = A0.phys_i, B0.phys_i
+    dev = u.data.device
     if truncation == "svd":
-        U, S, V, tr = svd_truncate(both, cutoff, Mmax)
-        if l2r:
-            SV = DBM()
-            for (lc, rc), b in zip(V.keys, V.blocks):
-                SV.insert(S[lc][:, None] * b, lc, rc)
-            A_lp = U
-            B_rp = SV
-        else:
-            US = DBM()
-            for (lc, rc), b in zip(U.keys, U.blocks):
-                US.insert(b * S[rc][None, :], lc, rc)
-            A_lp = US
-            B_rp = V
-    elif truncation in ("heev", "heev_truncation"):
+        # the whole split on the device: batched SVD, device cut, planned assembly
+        svd = N.BatchedSVD(blay.shapes, blay.offsets)
+        svd.run(bflat, _stream(dev))
+        keep, tr = svd.cut(Mmax, cutoff, 0, _stream(dev))
+        S_host = svd.S.cpu().numpy()
+        ap = N.plan_split_assemble(sp, svd.u_off[:len(keep)], svd.vt_off[:len(keep)], keep, S_host,
+                                   svd.s_off[:len(keep)], l2r)
+        ap.upload()
+        a_out = torch.empty(max(ap.out_elems, 1), dtype=torch.float64, device=dev)
+        b_out = torch.empty(max(ap.scratch[2], 1), dtype=torch.float64, device=dev)
+        _run_fp64(ap, dev, ket=svd.U, left=svd.Vt, out=a_out, s2=b_out)
+        pa, la, ra, lay_a = N.out_tensor(ap, 0)
+        pb, lb, rb, lay_b = N.out_tensor(ap, 1)
+        return (DeviceMPSTensor(pa, la, ra, lay_a, a_out), DeviceMPSTensor(pb, lb, rb, lay_b, b_out),
+                Trunc(int(tr.bond_dimension), tr.truncated_weight, tr.truncated_fraction, tr.smallest_ev))
+    both = block_views(blay, bflat)
+    if truncation in ("heev", "heev_truncation"):
         bt = _transpose(both)
         dm = gemm(both, bt) if l2r else gemm(bt, both)
         if alpha != 0.0 and boundary is not None:

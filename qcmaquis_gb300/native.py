@@ -127,6 +127,17 @@ def lib():
     L.qcm_plan_split_assemble.argtypes = [C.c_void_p, i64p, i64p, i64p, f64p, i64p, C.c_int32,
                                           C.POINTER(C.c_void_p)]
     L.qcm_plan_out_tensor.argtypes = [C.c_void_p, C.c_int32, i32p, i32p, i64p, i64p, i64p, i32p, i32p, i64p]
+    L.qcm_ctx_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+    L.qcm_ctx_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    L.qcm_ctx_destroy.argtypes = [C.c_void_p]
+    L.qcm_ctx_destroy.restype = None
+    L.qcm_ctx_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                              C.c_void_p, C.c_int32]
+    L.qcm_boundary_step.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                    C.c_int32]
+    L.qcm_jcd_solve.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32,
+                                C.c_void_p, C.c_int64, C.c_double, C.c_int32, C.POINTER(C.c_void_p), C.c_int32,
+                                C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32)]
     L.qcm_svd_create.argtypes = [C.c_int32, i64p, i64p, i64p, C.POINTER(C.c_void_p)]
     L.qcm_svd_sizes.argtypes = [C.c_void_p, i64p, i64p, i64p, i64p]
     L.qcm_svd_block_offsets.argtypes = [C.c_void_p, i64p, i64p, i64p]
@@ -138,6 +149,24 @@ def lib():
                                      C.POINTER(CTrunc), C.c_void_p]
     _lib = L
     return L
+
+
+class Context:
+    """Owner of a ``qcm_ctx`` (scratch, image buffer, FP32 boundary shadows and the
+    eigensolver's vectors on one device and stream)."""
+
+    def __init__(self, stream: int = 0):
+        h = C.c_void_p()
+        check(lib().qcm_ctx_create(C.c_void_p(stream) if stream else None, C.byref(h)), "qcm_ctx_create")
+        self.h = h
+
+    def set_stream(self, stream: int):
+        check(lib().qcm_ctx_set_stream(self.h, C.c_void_p(stream) if stream else None), "qcm_ctx_set_stream")
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.qcm_ctx_destroy(self.h)
+            self.h = None
 
 
 class CTrunc(C.Structure):

@@ -27,7 +27,7 @@ def _bm_dict(b):
 
 
 @pytest.mark.parametrize("seeds", [(11, 12), (3, 8)])
-def test_overlap_boundaries_and_vectors_match_oracle(seeds):
+def test_overlap_boundaries_and_vectors_match_oracle(seeds, monkeypatch):
     L, Ne = 6, 6
     model = QCModel(L, synthetic_integral_map(L, seed=3), Ne)
     mpo = make_mpo(model)
@@ -52,8 +52,16 @@ def test_overlap_boundaries_and_vectors_match_oracle(seeds):
     site = 2
     theta_ref = R.make_two_site_mps(psi[site], psi[site + 1])
     v_ref = ref.vectors(site, theta_ref)[0]
-    from qcmaquis_gb300.mps_ops import make_two_site_mps
-    theta = make_two_site_mps(dev(psi[site]), dev(psi[site + 1]))
+    # the two-site tensor itself is a native plan (GPU); it equals the oracle's
+    # (tests/test_mps_plans_cpu.py), so the oracle's stands in for it here
+    import qcmaquis_gb300.excited as X
+
+    def host_theta(a, b):
+        ha = R.MPSTensor(a.phys_i, a.left_i, a.right_i, a.to_block_matrix(), R.LEFT_PAIRED)
+        hb = R.MPSTensor(b.phys_i, b.left_i, b.right_i, b.to_block_matrix(), R.LEFT_PAIRED)
+        return dev(R.make_two_site_mps(ha, hb))
+    monkeypatch.setattr(X, "make_two_site_mps", host_theta)
+    theta = dev(theta_ref)
     v = got.vectors(site, theta)[0].numpy()
     lay = N.Layout.of(v_ref.copy().make_left_paired().data)
     assert list(lay.keys) == list(theta.layout.keys)

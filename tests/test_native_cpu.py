@@ -214,6 +214,20 @@ def test_cpp_layer_builds_a_plan(tmp_path):
     assert "out=4" in out.stdout
 
 
+def test_cpp_microiteration_host_compiles(tmp_path):
+    """The C++ host that runs a whole microiteration through the C ABI
+    (tests/capi_microiteration.cpp; run by the GPU tests) compiles and links."""
+    import subprocess
+    exe = tmp_path / "capi_microiteration"
+    libdir = os.path.join(ROOT, "qcmaquis_gb300")
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"), "-I" + cuda + "/include",
+                        os.path.join(ROOT, "tests", "capi_microiteration.cpp"), "-o", str(exe), "-L" + libdir,
+                        "-lqcm_gb300", "-Wl,-rpath," + libdir, "-L" + cuda + "/lib64", "-lcudart"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 _FMPO_ARRAYS = ("left_spin", "right_spin", "left_herm", "right_herm", "left_phase", "right_phase", "col_ptr",
                 "row_of", "term_ptr", "term_op", "term_scale", "op_spin", "op_blk_ptr", "blk_q", "blk_ent_ptr",
                 "ent", "ent_coeff")
