@@ -8,7 +8,8 @@ built on the GPU from that MPS.  A step is one sigma vector.  The inputs
 steps.
 
 Prints one JSON line (see the keys below).  ``--impl reference`` times the
-CPU restatement of the reference algorithm (the oracle) on a bounded sample.
+C++/OpenMP restatement of the reference algorithm (``oracle/sigma_ref.cpp``)
+on the host cores, on the same problem (layouts from a committed fixture).
 """
 from __future__ import annotations
 
@@ -162,39 +163,73 @@ def dgemm_peak_tflops():
     return 2.0 * n ** 3 / best / 1e12
 
 
-def cpu_oracle_sample(L: int, m: int, budget_s: float = 20.0):
-    """The oracle's sigma on the host cores, a bounded sample of the same workload."""
-    from oracle.cpu_sample import sigma_sample
-    return sigma_sample(L, m, budget_s=budget_s)
+class CppSigmaBaseline:
+    """The C++/OpenMP oracle sigma (``oracle/sigma_ref.cpp``: the reference's lbtm
+    algorithm, OpenMP over the right MPO bonds, block products in the host's
+    OpenBLAS) on this benchmark's exact problem: layouts and MPO tensor from the
+    committed fixture ``oracle/fixtures/sigma_L{L}_m{m}.npz``, ket and boundary
+    values seeded normal numbers (the work does not depend on them).  Loads
+    nothing of the library."""
+
+    def __init__(self, L: int, m: int, seed: int = 7):
+        import numpy as np
+        from oracle import cpu_sigma as CS
+        path = os.path.join(ROOT, "oracle", "fixtures", f"sigma_L{L}_m{m}.npz")
+        self.CS = CS
+        self.inp = CS.SigmaInputs(dict(np.load(path)))
+        rng = np.random.default_rng(seed)
+        self.x = rng.standard_normal(self.inp.psi_size)
+        self.Ld = rng.standard_normal(self.inp.L_size)
+        self.Rd = rng.standard_normal(self.inp.R_size)
+        self.L, self.m = L, m
+
+    def run(self):
+        t0 = time.perf_counter()
+        _, work = self.CS.sigma(self.inp, self.x, self.Ld, self.Rd)
+        return float(work[0] + work[1]), time.perf_counter() - t0, int(work[2])
+
+    def describe(self, times, threads):
+        return (f"C++17 -O3 -fopenmp oracle sigma (lbtm; OpenMP over the {self.inp.W.col_dim} right MPO bonds; "
+                f"{self.CS.host_blas()[1]}), the full L={self.L} m={self.m} middle-site sigma per run, "
+                f"{len(times)} runs, median {sorted(times)[len(times) // 2]:.2f} s, {threads} threads; layouts from "
+                f"oracle/fixtures, seeded random values")
+
+
+def cpu_oracle_sample(L: int, m: int, runs: int = 3):
+    """The C++ oracle's full sigma on the host cores, median of ``runs`` runs."""
+    b = CppSigmaBaseline(L, m)
+    res = [b.run() for _ in range(runs)]
+    times = [t for _, t, _ in res]
+    med = sorted(times)[len(times) // 2]
+    return {"value": res[0][0] / med / 1e12, "unit": UNIT, "cores": res[0][2], "kind": "port",
+            "sample": b.describe(times, res[0][2]), "seconds_per_sigma": med}
 
 
 def run_reference(args):
-    """CPU arm: the oracle port of the reference's sigma on the host cores
-    (the reference itself does not build here), on this workload; each step is
-    a bounded sample of one sigma."""
+    """CPU arm: the reference's sigma algorithm restated in C++/OpenMP (the
+    reference itself does not build here: Boost, GSL and HDF5 are absent) on the
+    host cores, on this benchmark's problem; each step is one full sigma."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from oracle.cpu_sample import SigmaSample
-    smp = SigmaSample(args.L, args.m)
-    budget = 12.0
+    b = CppSigmaBaseline(args.L, args.m)
     for _ in range(args.warmup):
-        smp.step(0.0)
+        b.run()
     flops = dt = 0.0
-    done = 0
+    times, threads = [], 1
     for _ in range(args.steps):
-        f, t, done = smp.step(budget)
+        f, t, threads = b.run()
         flops += f
         dt += t
+        times.append(t)
     value = flops / dt / 1e12
-    cpu = {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-           "sample": smp.describe(flops, dt, done, args.steps)}
+    cpu = {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": b.describe(times, threads)}
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded workload layouts, random boundary values)",
+            "data": "synthetic (the benchmark's layouts from a committed fixture, seeded random values)",
             "config": {"workload": f"sigma vector H_eff.psi, L={args.L} N={args.L} S=0 SU2U1, middle sites, "
-                                   f"m={args.m} (bounded CPU sample per step)", "L": args.L, "m": args.m},
+                                   f"m={args.m}", "L": args.L, "m": args.m, "l2": "CPU run"},
             "cpu_baseline": cpu,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -623,9 +658,14 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_oracle_sample(args.L, args.m, budget_s=15.0)
+            cpu = cpu_oracle_sample(args.L, args.m)
         except Exception as e:  # the baseline must not hide the GPU line
             cpu = {"error": str(e)}
+        if cpu and "seconds_per_sigma" in cpu:
+            # like for like: this run's sigma on the GPU against the CPU oracle's, per form
+            cpu["gpu_over_cpu_same_sigma"] = {args.precision: cpu["seconds_per_sigma"] / t_step}
+            if compare:
+                cpu["gpu_over_cpu_same_sigma"]["fp64"] = cpu["seconds_per_sigma"] / (compare["fp64_ms_per_step"] / 1e3)
 
     value = flops / t_step / 1e12 * world
     line = {
