@@ -5,10 +5,11 @@ column-major views into the buffer.  These operations restate:
 
 * ``TwoSiteTensor(mps1, mps2)`` + ``make_mps`` (theta = A.B, both->right
   reshape, SU(2) ``reduce_right``): ``mp_tensors/twositetensor.hpp:22-31, 132-139``,
-  ``mp_tensors/ts_reshape.h:231-290``, ``mp_tensors/ts_reduction.h:42-141``;
+  ``mp_tensors/ts_reshape.h:231-290``, ``mp_tensors/ts_reduction.h:42-141`` --
+  one native plan (``qcm_plan_two_site``);
 * ``operator<<`` (``unreduce_left``) and ``reshape_left_to_both``:
   ``mp_tensors/twositetensor.hpp:372-389``, ``ts_reduction.h:143-251``,
-  ``ts_reshape.h:89-145``;
+  ``ts_reshape.h:89-145`` -- one native plan (``qcm_plan_split_theta``);
 * ``split_mps_l2r/r2l`` with ``svd_truncate``: ``twositetensor.hpp:141-180``,
   ``block_matrix/block_matrix_algorithms.h:163-333``;
 * ``leftNormalizeAndReturn`` / ``rightNormalizeAndReturn`` / ``multiply_from_*``:
@@ -22,17 +23,13 @@ bookkeeping.
 """
 from __future__ import annotations
 
-import math
 from typing import Dict, List, Tuple
 
-import numpy as np
 import torch
 
 from . import native as N
 from .engine import DeviceMPSTensor
-from .symmetry import (Index, ProductBasis, adjoin, common_subset, fuse, fuse_neg_first, index_product, neg,
-                       spin)
-from .wigner import wigner6j
+from .symmetry import Index, ProductBasis, adjoin, common_subset, fuse, fuse_neg_first, index_product, neg
 
 
 class DBM:
@@ -167,147 +164,6 @@ def reshape_r2l(phys: Index, left_i: Index, right_i: Index, m1: DBM) -> DBM:
             for ss in range(sd):
                 ob[olo + ss * ld:olo + (ss + 1) * ld, :rd] = b[:ld, iro + ss * rd:iro + (ss + 1) * rd]
     return m2
-
-
-def _both_to_right(p1: Index, p2: Index, left_i: Index, right_i: Index, m1: DBM) -> DBM:
-    phys2 = index_product(p1, p2)
-    phys_pb = ProductBasis(p1, p2)
-    in_left = ProductBasis(p1, left_i)
-    in_right = ProductBasis(p2, right_i, fuse_neg_first)
-    out_right = ProductBasis(phys2, right_i, fuse_neg_first)
-    m2 = DBM()
-    for k, b in zip(m1.keys, m1.blocks):
-        for c1, sd1 in p1:
-            l = left_i.position(fuse(k[0], neg(c1)))
-            if l == len(left_i):
-                continue
-            for c2, sd2 in p2:
-                r = right_i.position(fuse(k[1], c2))
-                if r == len(right_i):
-                    continue
-                s_charge = fuse(c1, c2)
-                ol, orr = left_i[l][0], fuse(neg(s_charge), right_i[r][0])
-                ld, rd = left_i[l][1], right_i[r][1]
-                ob = m2.get_or_zeros(ol, orr, (ld, out_right.size(orr)), b.device)
-                ilo, iro = in_left(c1, left_i[l][0]), in_right(c2, right_i[r][0])
-                oro, opo = out_right(s_charge, right_i[r][0]), phys_pb(c1, c2)
-                for ss1 in range(sd1):
-                    for ss2 in range(sd2):
-                        so = opo + ss1 * sd2 + ss2
-                        ob[:ld, oro + so * rd:oro + (so + 1) * rd] = \
-                            b[ilo + ss1 * ld:ilo + (ss1 + 1) * ld, iro + ss2 * rd:iro + (ss2 + 1) * rd]
-    return m2
-
-
-def _left_to_both(p1: Index, p2: Index, left_i: Index, right_i: Index, m1: DBM) -> DBM:
-    phys2 = index_product(p1, p2)
-    phys_pb = ProductBasis(p1, p2)
-    in_left = ProductBasis(phys2, left_i)
-    out_right = ProductBasis(p2, right_i, fuse_neg_first)
-    out_left = ProductBasis(p1, left_i)
-    m2 = DBM()
-    for k, b in zip(m1.keys, m1.blocks):
-        r = right_i.position(k[1])
-        if r == len(right_i):
-            raise RuntimeError("two-site tensor inconsistent with right index")
-        for c1, sd1 in p1:
-            for c2, sd2 in p2:
-                s_charge = fuse(c1, c2)
-                l = left_i.position(fuse(k[0], neg(s_charge)))
-                if l == len(left_i):
-                    continue
-                ol, orr = fuse(c1, left_i[l][0]), fuse(neg(c2), right_i[r][0])
-                ld, rd = left_i[l][1], right_i[r][1]
-                ob = m2.get_or_zeros(ol, orr, (out_left.size(ol), out_right.size(orr)), b.device)
-                ilo, ipo = in_left(s_charge, left_i[l][0]), phys_pb(c1, c2)
-                olo, oro = out_left(c1, left_i[l][0]), out_right(c2, right_i[r][0])
-                for ss1 in range(sd1):
-                    for ss2 in range(sd2):
-                        si = ipo + ss1 * sd2 + ss2
-                        ob[olo + ss1 * ld:olo + (ss1 + 1) * ld, oro + ss2 * rd:oro + (ss2 + 1) * rd] = \
-                            b[ilo + si * ld:ilo + (si + 1) * ld, :rd]
-    return m2
-
-
-def _sign6(jl, jr, S1, S2):
-    return -1.0 if ((jl + jr + S1 + S2) // 2) % 2 else 1.0
-
-
-def reduce_right(p1: Index, p2: Index, left_i: Index, right_i: Index, m1: DBM):
-    phys2 = index_product(p1, p2)
-    phys_pb = ProductBasis(p1, p2)
-    in_right = ProductBasis(phys2, right_i, fuse_neg_first)
-    m2 = DBM()
-    for k, ib in zip(m1.keys, m1.blocks):
-        lc, in_r = k
-        ob = torch.zeros_like(ib)
-        m2.insert(ob, lc, in_r)
-        for s_charge, _ in phys2:
-            r = right_i.position(fuse(in_r, s_charge))
-            if r == len(right_i):
-                continue
-            iro, rs = in_right(s_charge, right_i[r][0]), right_i[r][1]
-            for c1, sd1 in p1:
-                for c2, sd2 in p2:
-                    if s_charge != fuse(c1, c2):
-                        continue
-                    ipo = phys_pb(c1, c2)
-                    S1, S2 = abs(spin(c1)), abs(spin(c2))
-                    jl, jm, jr = spin(lc), spin(lc) + spin(c1), spin(right_i[r][0])
-                    if jm < 0:
-                        continue
-                    if jl == jr and jl > 0 and S1 == 1 and S2 == 1:
-                        base = ipo if spin(c1) == 1 else ipo - 1
-                        outs = [(base + j // 2, j) for j in range(abs(S1 - S2), abs(S1 + S2) + 1, 2)]
-                    else:
-                        outs = [(ipo, abs(spin(c1) + spin(c2)))]
-                    for opo, j in outs:
-                        cc = math.sqrt((j + 1) * (jm + 1)) * wigner6j(jl, jr, j, S2, S1, jm) * _sign6(jl, jr, S1, S2)
-                        for ss1 in range(sd1):
-                            for ss2 in range(sd2):
-                                si, so = ipo + ss1 * sd2 + ss2, opo + ss1 * sd2 + ss2
-                                ob[:, iro + so * rs:iro + (so + 1) * rs] += cc * ib[:, iro + si * rs:iro + (si + 1) * rs]
-    return phys2, m2
-
-
-def unreduce_left(p1: Index, p2: Index, left_i: Index, right_i: Index, m1: DBM):
-    phys2 = index_product(p1, p2)
-    phys_pb = ProductBasis(p1, p2)
-    in_left = ProductBasis(phys2, left_i)
-    m2 = DBM()
-    for k, ib in zip(m1.keys, m1.blocks):
-        in_l, rc = k
-        ob = torch.zeros_like(ib)
-        m2.insert(ob, in_l, rc)
-        for s_charge, _ in phys2:
-            l = left_i.position(fuse(in_l, neg(s_charge)))
-            if l == len(left_i):
-                continue
-            ilo, ld = in_left(s_charge, left_i[l][0]), left_i[l][1]
-            for c1, sd1 in p1:
-                for c2, sd2 in p2:
-                    if s_charge != fuse(c1, c2):
-                        continue
-                    ipo = phys_pb(c1, c2)
-                    S1, S2 = abs(spin(c1)), abs(spin(c2))
-                    jl, jr = spin(left_i[l][0]), spin(rc)
-                    if jl == jr and jl > 0 and S1 == 1 and S2 == 1:
-                        j = 0 if spin(c1) == 1 else 2
-                        base = ipo if j == 0 else ipo - 1
-                        outs = [((base + 1) if jm == jl - 1 else base, j, jm) for jm in (jl - 1, jl + 1)]
-                    else:
-                        j = abs(spin(c1) + spin(c2))
-                        jm = jl + spin(c1)
-                        if jm < 0:
-                            continue
-                        outs = [(ipo, j, jm)]
-                    for opo, j, jm in outs:
-                        cc = math.sqrt((j + 1) * (jm + 1)) * wigner6j(jl, jr, j, S2, S1, jm) * _sign6(jl, jr, S1, S2)
-                        for ss1 in range(sd1):
-                            for ss2 in range(sd2):
-                                si, so = ipo + ss1 * sd2 + ss2, opo + ss1 * sd2 + ss2
-                                ob[ilo + so * ld:ilo + (so + 1) * ld, :] += cc * ib[ilo + si * ld:ilo + (si + 1) * ld, :]
-    return phys2, m2
 
 
 # ------------------------------------------------------------------ MPS-level operations
