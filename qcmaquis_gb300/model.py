@@ -481,9 +481,13 @@ class QCModel:
             add(four_terms, tuple(term.position(x) for x in range(4)) + tuple(term.tag(x) for x in range(4)), term)
 
         for (i, j, k, l), me, ukey in self._parsed():
-            for kind, t in self._integral_terms(i, j, k, l, me, ss, N):
+            terms = list(self._integral_terms(i, j, k, l, me, ss, N))
+            # the terms of a unit integral give the coefficient per unit of this
+            # integral (also for a value of zero, kept when the cutoff admits it)
+            units = terms if me != 0.0 else list(self._integral_terms(i, j, k, l, 1.0, ss, N))
+            for (kind, t), (_, tu) in zip(terms, units):
                 # the coefficient per unit of this integral, before terms are merged
-                t.src = {ukey: t.coeff / me}
+                t.src = {ukey: t.coeff / me if me != 0.0 else tu.coeff}
                 if kind == 1:
                     self.terms.append(t)
                 elif kind == 2:
