@@ -38,12 +38,13 @@ def parse():
     ap.add_argument("--sweep", action="store_true",
                     help="time one full two-site sweep (FP64 and BF16x3 sigma forms) instead of sigma calls")
     ap.add_argument("--jd-maxiter", type=int, default=10)
+    ap.add_argument("--shadow", action="store_true",
+                    help="--sweep: one mixed sweep with an FP64 shadow solve at every microiteration (precision check)")
     ap.add_argument("--nsweeps", type=int, default=1, help="--sweep: number of sweeps")
-    ap.add_argument("--forms", default="", help="--sweep: comma-separated subset of the forms to run")
+    ap.add_argument("--forms", default="", help="--sweep: comma-separated forms (fp64, mixed, mixed_parts, "
+                    "fp64_parts, fp64_heev, mixed_heev; default fp64,mixed,mixed_parts)")
     ap.add_argument("--plan-cache", type=int, default=0,
                     help="--sweep: sigma plans kept, keyed by layouts (0: the engine default of 2)")
-    ap.add_argument("--overlap-host", action="store_true",
-                    help="--sweep: also time the forms without per-part synchronisation")
     ap.add_argument("--ramp", default="", help="--sweep: bond dimension per sweep, e.g. 256,256,512,512,1024,1024")
     ap.add_argument("--no-images", action="store_true",
                     help="BF16x3: split operands inside the block-product kernel instead of pre-split images")
@@ -259,23 +260,23 @@ def run_sweep(args):
     out = {}
     ramp = [int(x) for x in args.ramp.split(",")] if args.ramp else None
     nsweeps = len(ramp) if ramp else args.nsweeps
-    # (name, sigma precision, boundary precision, truncation): the plain FP64 form with
-    # the reference's default SVD truncation against the mixed form (BF16x3 sigma
-    # vectors, everything else FP64) with the same truncation -- the headline pair;
-    # on single-sweep runs both forms also with the density-matrix (heev, noise 0)
-    # truncation, so that the sigma gain and the truncation choice are separate numbers
-    variants = (("fp64", 0, 0, "svd"), ("mixed", 2, 0, "svd"))
-    if nsweeps == 1:
-        variants += (("fp64_heev", 0, 0, "heev"), ("mixed_heev", 2, 0, "heev"))
-    variants = tuple(v + (True,) for v in variants)
-    if args.overlap_host:
-        # both forms with the device left running while the host builds the next plan (the
-        # headline), and the mixed form once more synchronised per part for its breakdown
-        variants = (("fp64", 0, 0, "svd", False), ("mixed", 2, 0, "svd", False),
-                    ("mixed_timed_parts", 2, 0, "svd", True))
+    # (name, sigma precision, boundary precision, truncation, per-part timing): the plain
+    # FP64 form with the reference's default SVD truncation against the mixed form
+    # (BF16x3 sigma vectors, everything else FP64) with the same truncation -- the
+    # headline pair, both run as in production (the host plans the next site problem
+    # while the device finishes the boundary update); the mixed form once more with
+    # the device synchronised after each part, for its time breakdown; and, on request
+    # (--forms), both forms with the density-matrix (heev, noise 0) truncation
+    variants = (("fp64", 0, 0, "svd", False), ("mixed", 2, 0, "svd", False), ("mixed_parts", 2, 0, "svd", True),
+                ("fp64_parts", 0, 0, "svd", True), ("fp64_heev", 0, 0, "heev", True),
+                ("mixed_heev", 2, 0, "heev", True))
+    if not args.forms:
+        variants = tuple(v for v in variants if v[0] in ("fp64", "mixed", "mixed_parts"))
     if args.forms:
         keep = set(args.forms.split(","))
         variants = tuple(v for v in variants if v[0] in keep)
+    if args.shadow:
+        variants = (("mixed_shadowed", 2, 0, "svd", True),)
     for name, prec, bprec, trunc, time_parts in variants:
         mps = [DeviceMPSTensor.from_host(t) for t in sites]
         p = SweepParams(nsweeps=nsweeps, max_bond_dimension=args.m, sweep_bond_dimensions=ramp,
@@ -284,8 +285,12 @@ def run_sweep(args):
                         alpha_initial=0.0, alpha_main=0.0, alpha_final=0.0)
         torch.cuda.synchronize()
         t1 = time.time()
+        shadow = None
+        if args.shadow:
+            from qcmaquis_gb300.engine import Engine
+            shadow = Engine("cuda", precision=0)
         rec, _ = run_dmrg(model, mpo, p, nelec, mps=mps, precision=prec, ts_mpo=ts, boundary_precision=bprec,
-                          time_parts=time_parts, plan_cache=args.plan_cache)
+                          time_parts=time_parts, plan_cache=args.plan_cache, shadow=shadow)
         torch.cuda.synchronize()
         out[name] = {"sweep_s": rec.sweep_seconds[-1], "sweep_seconds": rec.sweep_seconds, "wall_s": time.time() - t1,
                      "energy": rec.sweep_energy[-1], "sweep_energies": rec.sweep_energy,
@@ -296,6 +301,16 @@ def run_sweep(args):
                      "plan_hits": rec.plan_hits,
                      "boundary_plan_hits": rec.boundary_plan_hits,
                      "microiterations": len(rec.layout_digests)}
+        if rec.shadow:
+            sh = np.array(rec.shadow)
+            out[name]["shadow"] = {
+                "what": ("per microiteration: mixed Ritz value, FP64 Rayleigh quotient of the mixed eigenvector, "
+                         "FP64 eigensolver from the same start (Eh)"),
+                "max_abs_ritz_minus_fp64_eh": float(np.max(np.abs(sh[:, 0] - sh[:, 2]))),
+                "max_abs_rayleigh_minus_fp64_eh": float(np.max(np.abs(sh[:, 1] - sh[:, 2]))),
+                "median_abs_rayleigh_minus_fp64_eh": float(np.median(np.abs(sh[:, 1] - sh[:, 2]))),
+                "max_rayleigh_above_fp64_eh": float(np.max(sh[:, 1] - sh[:, 2])),
+                "energies": sh.tolist()}
         del mps
         torch.cuda.empty_cache()
     if "fp64" not in out or "mixed" not in out:

@@ -512,7 +512,8 @@ int qcm_plan_out_tensor(const qcm_plan* plan, int32_t which, int32_t* nblocks, i
  * descending, U (rows x k_k, ld rows) and Vt (k_k x cols, ld k_k), packed
  * block after block (qcm_svd_block_offsets).  The workspace holds the
  * rotated block and the accumulated rotations (qcm_svd_sizes).  Rounds run
- * until no pair of columns is rotated in a whole sweep (|a.b| <= 1e-15 |a||b|);
+ * until no pair of columns is rotated in a whole sweep (|a.b| <= sqrt(p) eps |a||b|,
+ * p = max(rows, cols), the threshold of LAPACK's one-sided Jacobi);
  * a block still rotating after 40 sweeps makes qcm_svd_run return
  * QCM_E_RANGE.  min(rows, cols) <= 4096 per block. */
 typedef struct qcm_svd qcm_svd;

@@ -16,8 +16,8 @@
 //     column pairs of every block (q' - 1 rounds per sweep, q' = q rounded up
 //     to even); a warp owns one pair, so every SM works on every round;
 //   * a block stops after a sweep that rotated no pair (|w_i.w_j| <= tol *
-//     |w_i| |w_j| for all pairs, tol = 1e-15); blocks with fewer columns run
-//     more sweeps in the same launches;
+//     |w_i| |w_j| for all pairs, tol = sqrt(p) eps as in LAPACK's dgesvj);
+//     blocks with fewer columns run more sweeps in the same launches;
 //   * the singular values are the column norms; they are sorted descending per
 //     block and U, S, Vt are written in the layout of gesvd('S','S').
 //
@@ -56,7 +56,11 @@ namespace qcm {
     } while (0)
 
 constexpr int SVD_MAX_SWEEPS = 40;
-constexpr double SVD_TOL = 1e-15;
+// rotation threshold |w_i.w_j| <= tol |w_i| |w_j| with tol = sqrt(p) * eps, the
+// threshold of LAPACK's one-sided Jacobi (dgesvj): below it the inner products
+// are rounding of the columns' own accuracy, and rotating on them only feeds
+// back rounding
+constexpr double SVD_EPS = 2.220446049250313e-16;
 constexpr int SVD_ROUND_THREADS = 256;   // 8 warps, one column pair each
 constexpr int SVD_FIN_THREADS = 512;
 constexpr int SVD_SORT_MAX = 4096;       // columns per block the finishing sort holds
@@ -163,7 +167,7 @@ svd_round_kernel(const SvdBlk* __restrict__ blks, const int32_t* __restrict__ pa
     al = warp_sum(al);
     be = warp_sum(be);
     ga = warp_sum(ga);
-    if (ga == 0.0 || fabs(ga) <= SVD_TOL * sqrt(al) * sqrt(be)) return;
+    if (ga == 0.0 || fabs(ga) <= sqrt((double)b.p) * SVD_EPS * sqrt(al) * sqrt(be)) return;
     const double zeta = (be - al) / (2.0 * ga);
     const double t = copysign(1.0, zeta) / (fabs(zeta) + hypot(1.0, zeta));
     const double c = 1.0 / sqrt(fma(t, t, 1.0));
@@ -353,7 +357,7 @@ struct qcm_svd {
     int32_t* d_pair_blk = nullptr;
     SvdState* d_state = nullptr;
     int32_t* d_ctl = nullptr;      // remaining, status
-    int32_t* h_ctl = nullptr;      // pinned copy
+    int32_t h_ctl[2] = {0, 0};     // host copy
     int device = -1;
     int32_t last_sweeps = 0;
 };
@@ -364,7 +368,6 @@ static void svd_free(qcm_svd* s) {
     cudaFree(s->d_pair_blk);
     cudaFree(s->d_state);
     cudaFree(s->d_ctl);
-    if (s->h_ctl) cudaFreeHost(s->h_ctl);
 }
 
 extern "C" {
@@ -460,7 +463,6 @@ int qcm_svd_run(qcm_svd* s, const double* src, double* work, double* U, double* 
         }
         FCT_CUDA(cudaMalloc(&s->d_state, sizeof(SvdState) * s->blks.size()));
         FCT_CUDA(cudaMalloc(&s->d_ctl, sizeof(int32_t) * 2));
-        FCT_CUDA(cudaMallocHost(&s->h_ctl, sizeof(int32_t) * 2));
         s->device = dev;
     } else if (dev != s->device) {
         set_error("qcm_svd_run: the factorisation was set up on another device");

@@ -95,6 +95,9 @@ class SweepRecord:
     # per microiteration: a digest of the sigma problem's layouts (psi, L, R) -- equal
     # digests at the same site in different sweeps could share one plan
     layout_digests: List[int] = field(default_factory=list)
+    # measurement runs with a shadow FP64 engine: per microiteration (Ritz value, FP64
+    # Rayleigh quotient of the eigenvector, FP64 eigenvalue from the same start)
+    shadow: List = field(default_factory=list)
     # wall time per part of the sweeps (host clock, device synchronised at each part's end)
     seconds: Dict[str, float] = field(default_factory=lambda: {"eigensolver": 0.0, "truncation": 0.0,
                                                                "boundary": 0.0, "plans": 0.0})
@@ -178,7 +181,7 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
              engine: Optional[Engine] = None, device="cuda", callback=None, precision: int = 0, ts_mpo=None,
              boundary_precision: Optional[int] = None, time_parts: bool = True, checkpoint: Optional[str] = None,
              start_sweep: int = 0, plan_cache: int = 0, ortho_states: Optional[List[List[DeviceMPSTensor]]] = None,
-             jd_residual_floor: Optional[float] = None):
+             jd_residual_floor: Optional[float] = None, shadow: Optional[Engine] = None):
     """Two-site sweeps.  ``precision`` selects the sigma-vector form (0 = FP64,
     1 = TF32, 2 = BF16x3 tensor cores); boundary updates, the eigensolver's
     vector algebra, the subspace problem, the truncation (SVD, or the
@@ -202,7 +205,12 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
     ``sba/SweepBasedEnergyMinimization.h:52-67``; ``excited.OverlapBoundaries``).
     ``jd_residual_floor``: the eigensolver stops once |r| <= max(tol, floor) |theta|;
     default ``JD_RESIDUAL_FLOOR`` of the sigma precision (0 for FP64: the
-    reference's stopping rule unchanged)."""
+    reference's stopping rule unchanged).
+    ``shadow`` (an FP64 engine; measurement runs only): at every microiteration also
+    evaluate the eigenvector's Rayleigh quotient with FP64 sigma vectors and solve the
+    same site problem, from the same start, with the FP64 eigensolver; the three
+    energies go to ``SweepRecord.shadow`` as (Ritz value, FP64 Rayleigh quotient of
+    the eigenvector, FP64 eigenvalue), without changing the sweep."""
     L = model.L
     phys = model.phys
     engine = engine or Engine(device, precision=precision)
@@ -252,6 +260,12 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
             rec.energies.append(theta + mpo.core_energy)
             rec.jd_iterations.append(iters)
             rec.sigma_calls += iters
+            if shadow is not None:
+                sp64 = SiteProblem(shadow, left[site], right[site + 2], ts_mpo[site])
+                hu = sp64.apply(u).data
+                e_var = float(torch.dot(u.data, hu) / torch.dot(u.data, u.data))
+                e64, _, _ = solve_ietl_jcd(sp64, psi, p.ietl_jcd_tol, p.ietl_jcd_maxiter, ortho)
+                rec.shadow.append((theta + mpo.core_energy, e_var + mpo.core_energy, e64 + mpo.core_energy))
             if p.twosite_truncation == "svd":
                 A, B, tr = O.split(u, mps[site], mps[site + 1], Mmax, cutoff, l2r)
             else:
@@ -266,21 +280,24 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
             t_c = time.time()
             rec.truncated_weight.append(tr.truncated_weight)
             rec.bond_dimension.append(tr.bond_dimension)
+            # mergeUnitaryFactor first (its factorisation waits for the device), then the
+            # boundary update, which is launched and left running: without part timing the
+            # host goes on to plan the next site problem while the device works
             if l2r:
-                left[site + 1] = engine.overlap_mpo_left_step(mps[site], left[site], mpo[site], precision=bprec)
                 if site + 2 < L:
                     mps[site + 1], t = O.left_normalize_and_return(mps[site + 1])
                     mps[site + 2] = O.multiply_from_left(mps[site + 2], t)
                 else:
                     mps[site + 1], _ = O.left_normalize_and_return(mps[site + 1])
+                left[site + 1] = engine.overlap_mpo_left_step(mps[site], left[site], mpo[site], precision=bprec)
             else:
-                right[site + 1] = engine.overlap_mpo_right_step(mps[site + 1], right[site + 2], mpo[site + 1],
-                                                                precision=bprec)
                 if site > 0:
                     mps[site], t = O.right_normalize_and_return(mps[site])
                     mps[site - 1] = O.multiply_from_right(mps[site - 1], t)
                 else:
                     mps[site], _ = O.right_normalize_and_return(mps[site])
+                right[site + 1] = engine.overlap_mpo_right_step(mps[site + 1], right[site + 2], mpo[site + 1],
+                                                                precision=bprec)
             if ovl:
                 # SweepBasedEnergyMinimization::propagateOtherTensors
                 if l2r:
