@@ -55,6 +55,10 @@ def parse():
                     help="32 independent L=12 problems: batched Davidson against separate solves")
     ap.add_argument("--adjoint", action="store_true",
                     help="converge an FP64 ground state and time the energy gradient dE/d(integrals)")
+    ap.add_argument("--adjoint-large", action="store_true",
+                    help="energy gradient at L=30, m=1024 with right environments recomputed from checkpoints")
+    ap.add_argument("--store-every", type=int, default=6,
+                    help="--adjoint-large: keep every k-th right environment, recompute the others")
     ap.add_argument("--L", type=int, default=24)
     ap.add_argument("--m", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -254,11 +258,12 @@ def run_sweep(args):
     model = QCModel(L, synthetic_integral_map(L, seed=1, diag_range=(-3.0, -0.3)), nelec)
     mpo = make_mpo(model)
     ts = make_ts_cache_fmpo(mpo, model.phys)
-    bonds = bond_indices(L, model.phys, (nelec, 0), args.m)
+    ramp = [int(x) for x in args.ramp.split(",")] if args.ramp else None
+    # the random start has the bond dimension of the first sweep
+    bonds = bond_indices(L, model.phys, (nelec, 0), ramp[0] if ramp else args.m)
     sites, _ = right_canonical_chain(model.phys, bonds, L, 0, np.random.default_rng(7))
     setup = time.time() - t0
     out = {}
-    ramp = [int(x) for x in args.ramp.split(",")] if args.ramp else None
     nsweeps = len(ramp) if ramp else args.nsweeps
     # (name, sigma precision, boundary precision, truncation, per-part timing): the plain
     # FP64 form with the reference's default SVD truncation against the mixed form
@@ -323,7 +328,7 @@ def run_sweep(args):
             "dtype": ("bf16x3 sigma products (fp32 accumulation); fp64 boundaries, eigensolver algebra, "
                       "SVD truncation, storage"),
             "data": "synthetic (seeded integrals, random right-normalised MPS)",
-            "config": {"workload": (f"{nsweeps} sweep(s) from a random MPS at m={args.m}"
+            "config": {"workload": (f"{nsweeps} sweep(s) from a random MPS at m={ramp[0] if ramp else args.m}"
                                     + (f", bond dimensions per sweep {ramp}" if ramp else f", Mmax {args.m}")
                                     + f", Davidson tol 1e-7, maxiter {args.jd_maxiter}, cutoff 1e-16; value = "
                                     "last sweep of the mixed form"), "L": L, "m": args.m},
@@ -425,6 +430,65 @@ def run_adjoint(args):
             "energy_from_rdms": e_rdm, "energy_from_rdms_err_eh": abs(e_rdm - res.energy),
             "rdm_check": ("tests/test_energy_gradient.py: LiH gradient vs exact-diagonalisation RDM sums and the "
                           "exact 2-RDM vs the reference's golden 2-RDM (dmrg/tests/test2.cpp:60-120)")}
+    print(json.dumps(line))
+
+
+def run_adjoint_large(args):
+    """dE/d(integrals) for every unique integral at L=30, N=30, S=0, m=1024 (a random
+    right-normalised MPS: the gradient of the energy functional at that state).  The
+    right environments are recomputed from every k-th stored one; a second pass keeps
+    them all, and the two gradients must agree bit for bit.  Reports both times, the
+    peak device memory of both, and the spread of the per-site energies (every site's
+    energy-gradient plan gives the same <Psi|H|Psi>)."""
+    import numpy as np
+    import torch
+    from qcmaquis_gb300.engine import DeviceMPSTensor, Engine
+    from qcmaquis_gb300.gradient import energy_gradient
+    from qcmaquis_gb300.integrals import synthetic_integral_map
+    from qcmaquis_gb300.model import QCModel
+    from qcmaquis_gb300.mps import bond_indices, right_canonical_chain
+    L, m = 30, 1024
+    t0 = time.time()
+    ints = synthetic_integral_map(L, seed=4)
+    model = QCModel(L, ints, L)
+    bonds = bond_indices(L, model.phys, (L, 0), m)
+    sites, _ = right_canonical_chain(model.phys, bonds, L, 0, np.random.default_rng(7))
+    eng = Engine("cuda:0")
+    mps = [DeviceMPSTensor.from_host(t) for t in sites]
+    setup = time.time() - t0
+    runs = {}
+    for k in (max(1, args.store_every), 1):
+        torch.cuda.synchronize()
+        torch.cuda.reset_peak_memory_stats()
+        base = torch.cuda.memory_allocated()
+        stats = {}
+        t1 = time.time()
+        res = energy_gradient(model, mps, L, engine=eng, store_every=k, stats=stats)
+        torch.cuda.synchronize()
+        runs[k] = (time.time() - t1, torch.cuda.max_memory_allocated() - base, res, stats)
+        if k == 1:
+            break
+    k = max(1, args.store_every)
+    t_k, peak_k, res_k, st_k = runs[k]
+    t_1, peak_1, res_1, st_1 = runs[1]
+    same = all(res_k.d_integrals[u] == res_1.d_integrals[u] for u in res_1.d_integrals)
+    env = st_1["env_bytes"]
+    line = {"metric": f"adjoint dE/d(integrals) s (L={L} N={L} S=0 SU2U1, m={m}, right environments "
+                      f"recomputed from every {k}th)",
+            "value": t_k, "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": "f64",
+            "data": "synthetic integrals (seeded), random right-normalised MPS at m=1024",
+            "config": {"workload": f"gradient of the energy at a fixed MPS, L={L}, m={m}, "
+                                   f"{len(ints)} integrals", "L": L, "m": m, "store_every": k},
+            "n_integrals": len(res_k.d_integrals), "energy": res_k.energy, "setup_s": setup,
+            "bitwise_equal_to_keep_all": bool(same),
+            "peak_device_bytes": {"recomputed": int(peak_k), "keep_all": int(peak_1)},
+            "seconds": {"recomputed": t_k, "keep_all": t_1},
+            "resident_environments": {"recomputed": st_k["peak_resident_environments"],
+                                      "keep_all": st_1["peak_resident_environments"]},
+            "right_environment_bytes": {"sum": int(sum(env.values())), "largest": int(max(env.values()))},
+            "mps_bytes": int(sum(t.data.numel() * 8 for t in mps)),
+            "site_energy_spread": float(np.ptp(st_k["site_energies"]) / res_k.norm),
+            "gradient_site_s": res_k.site_seconds}
     print(json.dumps(line))
 
 
@@ -537,6 +601,8 @@ def main():
         return run_sweep(args)
     if args.adjoint:
         return run_adjoint(args)
+    if args.adjoint_large:
+        return run_adjoint_large(args)
     if args.batch:
         return run_batch(args)
     if args.autotune:

@@ -384,3 +384,47 @@ def test_measured_2rdm_is_the_exact_2rdm_at_l6():
             G[b, c, a, d] = v
     assert not np.isnan(G).any()
     assert np.max(np.abs(G - g2)) < 1e-9
+
+
+@pytest.mark.gpu
+def test_gpu_gradient_with_recomputed_environments_is_unchanged():
+    """Keeping every third right environment and recomputing the others gives the
+    per-site term gradients of the keep-all pass bit for bit."""
+    from qcmaquis_gb300.engine import DeviceMPSTensor, Engine
+    from qcmaquis_gb300.gradient import term_gradients
+    L, Ne = 8, 8
+    model = QCModel(L, synthetic_integral_map(L, seed=5), Ne)
+    mpo = TaggedMPOMaker(model, merge_site_terms=False).create_mpo()
+    mps_host = initial_state(model, mpo, SweepParams(init_bond_dimension=12, seed=3), Ne, 0)
+    mps = [DeviceMPSTensor.from_host(t.copy().make_left_paired()) for t in mps_host]
+    eng = Engine("cuda:0")
+    a = term_gradients(mpo, mps, Ne, 0, eng, store_every=1)
+    b = term_gradients(mpo, mps, Ne, 0, eng, store_every=3)
+    for ga, gb in zip(a[0], b[0]):
+        assert np.array_equal(ga, gb)
+    assert a[2] == b[2]
+
+
+@pytest.mark.parametrize("L,k", [(30, 1), (30, 6), (30, 5), (7, 3), (2, 4), (1, 2)])
+def test_checkpointed_right_environments_schedule(L, k):
+    """Every R[i] read in the left-to-right order is the keep-all value, each site costs
+    at most one extra step, and at most L//k + k + 1 environments are resident."""
+    from qcmaquis_gb300.gradient import CheckpointedRight
+    calls = []
+
+    def step(j, b):
+        calls.append(j)
+        return (j, b)
+    want = {L: "end"}
+    for j in range(L - 1, 0, -1):
+        want[j] = (j, want[j + 1])
+    r = CheckpointedRight(step, "end", L, k)
+    assert len(calls) == L - 1
+    peak = r.resident()
+    for i in range(1, L + 1):
+        assert r[i] == want[i]
+        peak = max(peak, r.resident())
+        r.release(i)
+    assert peak <= (L // k + k + 1 if k > 1 else L)
+    assert len(calls) <= 2 * (L - 1)
+    assert r.resident() == 0
