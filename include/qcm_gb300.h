@@ -83,7 +83,11 @@ typedef struct {
  * entries [blk_ent_ptr[k], blk_ent_ptr[k+1]) with ent[4e..4e+3] =
  * (row, col, row_spin, col_spin) and value ent_coeff[e]
  * (block_matrix/sparse_operator.h:105-168).  Hermitian data follow
- * mp_tensors/mpotensor_detail.h:124-160 (partner index and phase). */
+ * mp_tensors/mpotensor_detail.h:124-160 (partner index and phase).
+ * symmetry selects the group of the charges (QCM_SYM_*): SU2U1 charges are
+ * (N, 2S) and the contractions carry the SU(2) couplings (ct/non-abelian);
+ * TwoU1 charges are (N_up, N_down), every coupling is 1, spins and phases are
+ * ignored (ct/abelian).  A zero-initialised field means SU2U1. */
 typedef struct {
     int32_t row_dim, col_dim;
     const int32_t* left_spin;
@@ -104,7 +108,11 @@ typedef struct {
     const int32_t* blk_ent_ptr;
     const int32_t* ent;
     const double* ent_coeff;
+    int32_t symmetry;
 } qcm_mpo_t;
+
+#define QCM_SYM_SU2U1 0
+#define QCM_SYM_TWOU1 1
 
 typedef struct qcm_plan qcm_plan;
 
@@ -447,11 +455,12 @@ int qcm_jcd_solve(qcm_ctx* ctx, qcm_plan* sigma, const double* left, int64_t lef
  * i+1; the same arrays as qcm_plan_out_tensor plus the device data pointer,
  * valid until qcm_split_result_destroy); trunc receives bond dimension,
  * truncated weight and fraction, and smallest_ev as the reference reports
- * them.  Synchronises the context's stream. */
+ * them.  symmetry (QCM_SYM_*) as for qcm_plan_split_theta.  Synchronises the
+ * context's stream. */
 typedef struct qcm_split_result qcm_split_result;
 int qcm_split(qcm_ctx* ctx, const qcm_index_t* phys1, const qcm_index_t* phys2, const qcm_index_t* left_i,
               const qcm_index_t* right_i, const qcm_blocks_t* u, const double* u_dev, int32_t l2r, int64_t Mmax,
-              double cutoff, qcm_trunc_t* trunc, qcm_split_result** out);
+              double cutoff, int32_t symmetry, qcm_trunc_t* trunc, qcm_split_result** out);
 int qcm_split_result_tensor(const qcm_split_result* res, int32_t which, int32_t* nblocks, int32_t* q, int64_t* rows,
                             int64_t* cols, int64_t* off, int32_t* n_idx3, int32_t* idx_q, int64_t* idx_size,
                             const double** data);
@@ -468,19 +477,24 @@ void qcm_split_result_destroy(qcm_split_result* res);
  * the SU(2) reduce_right 6j recoupling (mp_tensors/ts_reduction.h:42-141) and
  * the reshape to left-paired.  Slots: KET = A (left-paired), LEFT = B
  * (left-paired), OUT = the reduced two-site tensor; its layout and indices
- * through qcm_plan_out_tensor. */
+ * through qcm_plan_out_tensor.  With symmetry = QCM_SYM_TWOU1 there is no
+ * reduction: the two-site physical index is the product phys1 x phys2 and the
+ * tensor is reshaped straight to left-paired (make_mps_ of the abelian
+ * TwoSiteTensor, twositetensor.hpp:125-130). */
 int qcm_plan_two_site(const qcm_index_t* phys1, const qcm_index_t* a_left, const qcm_index_t* a_right,
                       const qcm_blocks_t* a, const qcm_index_t* phys2, const qcm_index_t* b_left,
-                      const qcm_index_t* b_right, const qcm_blocks_t* b, qcm_plan** plan);
+                      const qcm_index_t* b_right, const qcm_blocks_t* b, int32_t symmetry, qcm_plan** plan);
 
 /* The prologue of split_mps_l2r/r2l (twositetensor.hpp:141-180 with operator<<,
  * :372-389): the SU(2) unreduce_left recoupling (ts_reduction.h:143-251) and
  * reshape_left_to_both.  left_i / right_i are the outer indices of the pair
  * (left of site i, right of site i+1).  Slots: KET = the reduced two-site
  * tensor (left-paired), OUT = the both-paired matrix the truncation factorises
- * (its blocks through qcm_plan_out_tensor; they are the qcm_svd batch). */
+ * (its blocks through qcm_plan_out_tensor; they are the qcm_svd batch).
+ * QCM_SYM_TWOU1: no unreduce step (the abelian operator<<, twositetensor.hpp:
+ * 352-366), only the reshape. */
 int qcm_plan_split_theta(const qcm_index_t* phys1, const qcm_index_t* phys2, const qcm_index_t* left_i,
-                         const qcm_index_t* right_i, const qcm_blocks_t* u, qcm_plan** plan);
+                         const qcm_index_t* right_i, const qcm_blocks_t* u, int32_t symmetry, qcm_plan** plan);
 
 /* The epilogue of split_mps_l2r (l2r != 0: A = U, B = S V) or split_mps_r2l
  * (A = U S, B = V), after the truncation cut: from the qcm_svd of the split

@@ -231,8 +231,10 @@ def multiply_from_right(t: MPSTensor, N: BlockMatrix):
 
 
 # --------------------------------------------------------------------------- MPS init
-def allowed_sectors(L: int, phys: Index, right_end, Mmax: int) -> List[Index]:
-    """``allowed_sectors`` (``mp_tensors/mps_sectors.h:23-112``), one site type."""
+def allowed_sectors(L: int, phys: Index, right_end, Mmax: int, abelian: bool = False) -> List[Index]:
+    """``allowed_sectors`` (``mp_tensors/mps_sectors.h:23-112``), one site type; the
+    test that a sector's spin is not negative (``ChargeDetailClass::physical``) is
+    SU(2)'s and is skipped for an abelian group."""
     physc = phys.copy()
     physc.sort()
     cmax, cmin = physc[0][0], physc[len(physc) - 1][0]
@@ -257,7 +259,7 @@ def allowed_sectors(L: int, phys: Index, right_end, Mmax: int) -> List[Index]:
                 continue
             if fuse(c, cmini) > right_end:
                 continue
-            if spin(c) < 0:
+            if not abelian and spin(c) < 0:
                 continue
             keep.append([c, min(Mmax, s)])
         li.data = keep
@@ -273,7 +275,7 @@ def allowed_sectors(L: int, phys: Index, right_end, Mmax: int) -> List[Index]:
                 continue
             if fuse(c, neg(cmini)) < (0, 0):
                 continue
-            if spin(c) < 0:
+            if not abelian and spin(c) < 0:
                 continue
             keep.append([c, min(Mmax, s)])
         ri.data = keep
@@ -306,14 +308,14 @@ def new_mps_tensor(phys: Index, ld: Index, rd: Index, rng: Optional[np.random.Ge
     return MPSTensor(phys, left_i, right_i, data, LEFT_PAIRED)
 
 
-def default_mps_init(L, phys, right_end, init_bond_dimension, seed) -> List[MPSTensor]:
+def default_mps_init(L, phys, right_end, init_bond_dimension, seed, abelian: bool = False) -> List[MPSTensor]:
     """``default_mps_init`` (``mp_tensors/mps_initializers.h:34-81``).
 
     The element stream comes from numpy's PCG64 seeded with ``seed`` rather
     than boost's mt19937, so the initial MPS is this repository's own.
     """
     rng = np.random.default_rng(seed)
-    allowed = allowed_sectors(L, phys, right_end, init_bond_dimension)
+    allowed = allowed_sectors(L, phys, right_end, init_bond_dimension, abelian)
     mps = []
     for i in range(L):
         t = new_mps_tensor(phys, allowed[i], allowed[i + 1], rng)

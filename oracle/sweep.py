@@ -20,7 +20,18 @@ import numpy as np
 
 from .ts_mpo import make_ts_cache_mpo
 
+from . import abelian as A
 from . import dmrg_ref as R
+
+
+def _abelian(model_or_mpo) -> bool:
+    """TwoU1 models and their MPO tensors carry symmetry "2u1"."""
+    return getattr(model_or_mpo, "symmetry", "su2u1") == "2u1"
+
+
+def _engine(abelian: bool):
+    """The contraction functions of the group: the abelian engine or the SU(2) one."""
+    return A if abelian else R
 
 
 @dataclass
@@ -84,9 +95,10 @@ class SweepRecord:
 
 def expval(mps: List[R.MPSTensor], mpo) -> float:
     """``expval`` (``mp_tensors/mps_mpo_ops.h:57-68``) without the core energy."""
+    E = _engine(_abelian(mpo[0]))
     left = R.left_boundary(mps[0])
     for i in range(len(mps)):
-        left = R.overlap_mpo_left_step(mps[i], mps[i], left, mpo[i], is_hermitian=False)
+        left = E.overlap_mpo_left_step(mps[i], mps[i], left, mpo[i], is_hermitian=False)
     return sum(b.trace() for b in left[:1])
 
 
@@ -104,8 +116,12 @@ def overlap(mps: List[R.MPSTensor]) -> float:
 
 
 def initial_state(model, mpo, p: SweepParams, nelec: int, twoS: int):
+    """The random right-normalised start; SU2U1 targets (nelec, twoS), a TwoU1 model
+    its own (N_up, N_down)."""
     phys = model.phys
-    mps = R.default_mps_init(model.L, phys, (nelec, twoS), p.init_bond_dimension, p.seed)
+    ab = _abelian(model)
+    right_end = model.right_end if ab else (nelec, twoS)
+    mps = R.default_mps_init(model.L, phys, right_end, p.init_bond_dimension, p.seed, abelian=ab)
     R.normalize_right(mps)
     return mps
 
@@ -149,6 +165,10 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps=None,
     (``n_ortho_states`` / ``ortho_states``, ``sba/SweepBasedEnergyMinimization.h:52-67``)."""
     L = model.L
     phys = model.phys
+    ab = _abelian(model)
+    E = _engine(ab)
+    if ab and ortho_states:
+        raise ValueError("orthogonal states are implemented for SU2U1 only")
     if mps is None:
         mps = initial_state(model, mpo, p, nelec, twoS)
     ts_mpo = make_ts_cache_mpo(mpo, phys)
@@ -158,7 +178,7 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps=None,
     left[0] = R.left_boundary(mps[0])
     right[L] = R.right_boundary(mps[L - 1])
     for i in range(L - 1, 0, -1):
-        right[i] = R.overlap_mpo_right_step(mps[i], mps[i], right[i + 1], mpo[i])
+        right[i] = E.overlap_mpo_right_step(mps[i], mps[i], right[i + 1], mpo[i])
     rec = SweepRecord()
     nmicro = 2 * (L - 2) if L > 2 else 1
     for sweep in range(p.nsweeps):
@@ -170,17 +190,20 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps=None,
             change = (mi == L - 2) or (mi == nmicro - 1)
             l2r = forward and not change
             ts = ts_mpo[site]
-            psi = R.make_two_site_mps(mps[site], mps[site + 1])
+            psi = E.make_two_site_mps(mps[site], mps[site + 1])
 
             def apply_h(x, _l=left[site], _r=right[site + 2], _w=ts):
-                return R.site_hamil2(x, _l, _r, _w)
+                return E.site_hamil2(x, _l, _r, _w)
 
             ortho = ovl.vectors(site, psi) if ovl else None
             theta, u, iters = R.jcd_solve(apply_h, psi, p.ietl_jcd_tol, p.ietl_jcd_maxiter, ortho)
             rec.energies.append(theta + mpo.core_energy)
             u.make_left_paired()
             A0, B0 = mps[site], mps[site + 1]
-            _, tst = R.unreduce_left(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, u.data)
+            if ab:
+                tst = u.data
+            else:
+                _, tst = R.unreduce_left(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, u.data)
             if p.twosite_truncation == "svd":
                 A, B, trunc = R.split_mps(tst, A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, Mmax, cutoff, l2r)
             else:
@@ -193,9 +216,9 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps=None,
             rec.truncated_weight.append(trunc.truncated_weight)
             rec.bond_dimension.append(trunc.bond_dimension)
             if l2r:
-                left[site + 1] = R.overlap_mpo_left_step(mps[site], mps[site], left[site], mpo[site])
+                left[site + 1] = E.overlap_mpo_left_step(mps[site], mps[site], left[site], mpo[site])
             else:
-                right[site + 1] = R.overlap_mpo_right_step(mps[site + 1], mps[site + 1], right[site + 2],
+                right[site + 1] = E.overlap_mpo_right_step(mps[site + 1], mps[site + 1], right[site + 2],
                                                            mpo[site + 1])
             if ovl:
                 # SweepBasedEnergyMinimization::propagateOtherTensors

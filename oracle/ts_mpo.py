@@ -7,7 +7,8 @@ Restates, independently of the product package:
   column b3 of W2 share, of the spin-coupled Kronecker products of every
   (op1, op2) pair, one output operator per product spin s allowed by the bond
   spins, accumulated per s in ascending b2 order (``std::set``);
-* SU(2) ``op_kron`` (``bm/site_operator_algorithms.h:215-318``) with the
+* the abelian ``op_kron`` (``bm/site_operator_algorithms.h:167-205``) for TwoU1
+  tensors, and the SU(2) ``op_kron`` (``:215-318``) with the
   identity expansion, the per-block 9j coupling ``mod_coupling(j1, j2, J, k1,
   k2, k, j1', j2', J')``, the product-state spins of ``productSpin``
   (``bm/symmetry/spin_descriptor.h:106-117``) and the overall 6j factor;
@@ -144,6 +145,23 @@ def op_kron_su2(phys_a, phys_b, op_a, op_b, j: int, jpp: int, jp: int, k: int) -
     return OOp(blocks, OSpin(k, j, jp), basis)
 
 
+def op_kron_abelian(phys_a, phys_b, op_a, op_b) -> OOp:
+    """``op_kron`` of an abelian group (``bm/site_operator_algorithms.h:167-205``): the
+    Kronecker product placed at ProductBasis(phys_a, phys_b) offsets, block pair by
+    block pair, no couplings and no spins."""
+    A, B = _op_blocks(op_a), _op_blocks(op_b)
+    pb = ProductBasis(phys_a, phys_b)
+    blocks = BlockMatrix()
+    for (ia, oa), a in zip(A.keys, A.blocks):
+        for (ib, ob), b in zip(B.keys, B.blocks):
+            nl, nr = fuse(ia, ib), fuse(oa, ob)
+            tmp = np.zeros((pb.size(nl), pb.size(nr)))
+            r0, c0 = pb(ia, ib), pb(oa, ob)
+            tmp[r0:r0 + a.shape[0] * b.shape[0], c0:c0 + a.shape[1] * b.shape[1]] = np.kron(a, b)
+            blocks.match_and_add_block(tmp, nl, nr)
+    return OOp(blocks, OSpin(), {})
+
+
 def _remove_empty_blocks(op: OOp):
     k = 0
     while k < op.bm.n_blocks():
@@ -203,7 +221,10 @@ class OHerm:
 
 
 class OTensor:
-    """An MPO tensor: element (b1, b2) -> [(operator index, scale)], operators, bond spins."""
+    """An MPO tensor: element (b1, b2) -> [(operator index, scale)], operators, bond spins;
+    ``symmetry`` "su2u1" or "2u1" (abelian)."""
+
+    symmetry = "su2u1"
 
     def __init__(self, row_dim, col_dim, elements: Dict[Tuple[int, int], List[Tuple[int, float]]], ops: List[OOp],
                  herm: OHerm, left_spins, right_spins):
@@ -247,8 +268,10 @@ class OTensor:
 
 
 def make_twosite_mpo(mpo1, mpo2, phys1, phys2) -> OTensor:
-    """The two-site tensor of a neighbouring pair of single-site MPO tensors."""
+    """The two-site tensor of a neighbouring pair of single-site MPO tensors (abelian
+    Kronecker products when the tensors are of the "2u1" group, where every spin is 0)."""
     assert mpo1.col_dim == mpo2.row_dim
+    abelian = getattr(mpo1, "symmetry", "su2u1") == "2u1"
     ops: List[OOp] = []
     elements: Dict[Tuple[int, int], List[Tuple[int, float]]] = {}
     for b1 in range(mpo1.row_dim):
@@ -267,7 +290,10 @@ def make_twosite_mpo(mpo1, mpo2, phys1, phys2) -> OTensor:
                     for t2, s2 in mpo2.at(b2, b3):
                         o2 = mpo2.op(t2)
                         for s in allowed_spins(j, jp, o1.spin.get(), o2.spin.get()):
-                            prod = op_kron_su2(phys1, phys2, o1, o2, j, jpp, jp, s)
+                            if abelian:
+                                prod = op_kron_abelian(phys1, phys2, o1, o2)
+                            else:
+                                prod = op_kron_su2(phys1, phys2, o1, o2, j, jpp, jp, s)
                             _remove_empty_blocks(prod)
                             _add_into(per_s.setdefault(s, OOp()), prod, s1 * s2)
             for s in sorted(per_s):
@@ -275,7 +301,10 @@ def make_twosite_mpo(mpo1, mpo2, phys1, phys2) -> OTensor:
                 elements.setdefault((b1, b3), []).append((len(ops) - 1, 1.0))
     h1, h2 = mpo1.herm, mpo2.herm
     herm = OHerm(h1.LeftHerm, h2.RightHerm, h1.LeftPhase, h2.RightPhase)
-    return OTensor(mpo1.row_dim, mpo2.col_dim, elements, ops, herm, mpo1.left_spins, mpo2.right_spins)
+    t = OTensor(mpo1.row_dim, mpo2.col_dim, elements, ops, herm, mpo1.left_spins, mpo2.right_spins)
+    if abelian:
+        t.symmetry = "2u1"
+    return t
 
 
 def make_ts_cache_mpo(mpo, phys) -> List[OTensor]:
@@ -284,4 +313,5 @@ def make_ts_cache_mpo(mpo, phys) -> List[OTensor]:
 
 
 __all__ = ["OSpin", "OOp", "OHerm", "OTensor", "sparse_of", "allowed_spins", "product_spin", "op_kron_su2",
+           "op_kron_abelian",
            "make_twosite_mpo", "make_ts_cache_mpo"]

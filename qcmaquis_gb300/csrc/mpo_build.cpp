@@ -27,7 +27,7 @@ using qcm::Q;
 using qcm::set_error;
 
 struct qcm_mpo_buf {
-    int32_t row_dim = 0, col_dim = 0;
+    int32_t row_dim = 0, col_dim = 0, symmetry = QCM_SYM_SU2U1;
     std::vector<int32_t> left_spin, right_spin, left_herm, right_herm, left_phase, right_phase;
     // phase 1: distinct products (op1, op2, j, jpp, jp, s) and, per output operator
     // in the reference's table order (b1, b3 ascending, s ascending), its summands
@@ -89,6 +89,8 @@ void check_mpo(const qcm_mpo_t* w, const char* what) {
             if (w->term_op[t] < 0 || w->term_op[t] >= w->n_ops) throw std::runtime_error("mpo operator out of range");
     }
     if (w->n_ops > 0 && !w->op_spin) throw std::runtime_error(std::string("null op_spin in ") + what);
+    if (w->symmetry != QCM_SYM_SU2U1 && w->symmetry != QCM_SYM_TWOU1)
+        throw std::runtime_error(std::string("unknown symmetry in ") + what);
     check_ops(w, what);
 }
 
@@ -102,6 +104,8 @@ std::vector<std::vector<std::pair<int32_t, int32_t>>> rows_of(const qcm_mpo_t* w
 
 void phase1(qcm_mpo_buf& B, const qcm_mpo_t* w1, const qcm_mpo_t* w2) {
     if (w1->col_dim != w2->row_dim) throw std::runtime_error("the MPO tensors do not share a bond");
+    if (w1->symmetry != w2->symmetry) throw std::runtime_error("the MPO tensors are of different symmetry groups");
+    B.symmetry = w1->symmetry;
     B.row_dim = w1->row_dim;
     B.col_dim = w2->col_dim;
     B.left_spin.assign(w1->left_spin, w1->left_spin + w1->row_dim);
@@ -327,12 +331,14 @@ double mod_coupling9(int a, int b, int c, int d, int e, int f, int g, int h, int
 
 // op_kron for SU(2) (site_operator_algorithms.h): the spin-coupled Kronecker product
 // of operator o1 of W1 and o2 of W2 for bond spins (j, jpp, jp) and product spin k.
+// For an abelian group (abelian = true) the plain Kronecker product
+// (site_operator_algorithms.h:167-205): no identity expansion, couplings 1.
 void op_kron(const qcm_mpo_t* w1, const qcm_mpo_t* w2, int o1, int o2, int j, int jpp, int jp, int k,
-             const qcm::Idx& p1, const qcm::Idx& p2, const qcm::PB& pb, ProdOps& out) {
+             const qcm::Idx& p1, const qcm::Idx& p2, const qcm::PB& pb, ProdOps& out, bool abelian) {
     std::vector<DenseBlock> A = dense_op(w1, o1, p1), Bo = dense_op(w2, o2, p2);
     const int k1 = w1->op_spin[o1], k2 = w2->op_spin[o2];
-    if (k1 > 0 && k2 == 0) expand_identity(Bo, p2);
-    if (k1 == 0 && k2 > 0) expand_identity(A, p1);
+    if (!abelian && k1 > 0 && k2 == 0) expand_identity(Bo, p2);
+    if (!abelian && k1 == 0 && k2 > 0) expand_identity(A, p1);
     struct Acc { int64_t rows, cols; std::vector<double> v; std::vector<int32_t> rs, cs; };
     std::map<std::pair<Q, Q>, Acc, std::function<bool(const std::pair<Q, Q>&, const std::pair<Q, Q>&)>> blocks(
         [](const std::pair<Q, Q>& x, const std::pair<Q, Q>& y) {
@@ -353,9 +359,10 @@ void op_kron(const qcm_mpo_t* w1, const qcm_mpo_t* w2, int o1, int o2, int j, in
             }
             Acc& t = it->second;
             const int64_t io = pb(a.in, b.in), oo = pb(a.out, b.out);
-            const int J = product_spin(a.in, b.in), Jp = product_spin(a.out, b.out);
-            const double c9 = mod_coupling9(std::abs(a.in.s), std::abs(b.in.s), J, k1, k2, k, std::abs(a.out.s),
-                                            std::abs(b.out.s), Jp);
+            const int J = abelian ? 0 : product_spin(a.in, b.in), Jp = abelian ? 0 : product_spin(a.out, b.out);
+            const double c9 = abelian ? 1.0
+                                      : mod_coupling9(std::abs(a.in.s), std::abs(b.in.s), J, k1, k2, k,
+                                                      std::abs(a.out.s), std::abs(b.out.s), Jp);
             for (int64_t l1 = 0; l1 < a.rows; ++l1)
                 for (int64_t r1 = 0; r1 < a.cols; ++r1)
                     for (int64_t l2 = 0; l2 < b.rows; ++l2)
@@ -367,8 +374,8 @@ void op_kron(const qcm_mpo_t* w1, const qcm_mpo_t* w2, int o1, int o2, int j, in
             t.rs[(size_t)io] = J;
             t.cs[(size_t)oo] = Jp;
         }
-    double c6 = std::sqrt((jpp + 1.0) * (k + 1.0)) * qcm::wigner6j(j, jp, k, k2, k1, jpp);
-    if (((j + jp + k1 + k2) / 2) % 2) c6 = -c6;
+    double c6 = abelian ? 1.0 : std::sqrt((jpp + 1.0) * (k + 1.0)) * qcm::wigner6j(j, jp, k, k2, k1, jpp);
+    if (!abelian && ((j + jp + k1 + k2) / 2) % 2) c6 = -c6;
     out.op_spin.push_back(k);
     for (auto& [key, t] : blocks) {
         bool any = false;
@@ -461,6 +468,7 @@ int qcm_mpo_buf_view(const qcm_mpo_buf* B, qcm_mpo_t* view, int64_t* sizes) {
     view->blk_ent_ptr = B->blk_ent_ptr.data();
     view->ent = B->ent.data();
     view->ent_coeff = B->ent_coeff.data();
+    view->symmetry = B->symmetry;
     sizes[0] = (int64_t)B->row_of.size();        // elements
     sizes[1] = (int64_t)B->term_op.size();       // terms (= operators)
     sizes[2] = (int64_t)B->blk_q.size() / 4;     // operator blocks
@@ -488,7 +496,7 @@ int qcm_mpo_twosite(const qcm_mpo_t* w1, const qcm_mpo_t* w2, const qcm_index_t*
         ProdOps prods;
         for (size_t q = 0; q + 5 < B->keys.size(); q += 6) {
             const int32_t* k = &B->keys[q];
-            op_kron(w1, w2, k[0], k[1], k[2], k[3], k[4], k[5], p1, p2, pb, prods);
+            op_kron(w1, w2, k[0], k[1], k[2], k[3], k[4], k[5], p1, p2, pb, prods, w1->symmetry == QCM_SYM_TWOU1);
         }
         const qcm_mpo_t v = prods.view();
         phase2(*B, &v);

@@ -1,6 +1,8 @@
 // Plans of the MPS-level steps around the eigensolver: forming the two-site
 // tensor, undoing its SU(2) reduction before the truncation, and assembling the
-// two new site tensors after it.  Every step is a fixed linear map between two
+// two new site tensors after it.  For the abelian TwoU1 group the two-site
+// tensor is not reduced: its physical index is the plain product of the two
+// sites' and only the reshapes remain (twositetensor.hpp:125-130, 352-366).  Every step is a fixed linear map between two
 // block layouts (plus, for the two-site tensor, one grouped block product), so
 // it is planned once on the host as gather tiles -- each output tile the sum of
 // scaled source tiles, its couplings precomputed -- and runs as one gather
@@ -358,7 +360,7 @@ void add_map(qcm_plan* P, const std::vector<Piece>& ps, BM& out, int32_t dbuf, i
 // theta of sites (i, i+1) as the reduced two-site tensor, left-paired.
 // Slots: KET = A (left-paired), LEFT = B (left-paired), OUT = the two-site tensor.
 qcm_plan* build_theta(const Idx& p1, const Idx& a_left, const Idx& a_right, const BM& A, const Idx& p2,
-                      const Idx& b_left, const Idx& b_right, const BM& B) {
+                      const Idx& b_left, const Idx& b_right, const BM& B, bool abelian) {
     auto P = std::make_unique<qcm_plan>();
     P->kind = PK_THETA;
     int64_t s0 = 0, s1 = 0, s2 = 0, len = 0;
@@ -429,22 +431,29 @@ qcm_plan* build_theta(const Idx& p1, const Idx& a_left, const Idx& a_right, cons
         P->stages.push_back(zero_stage(QCM_BUF_S1, s1));
         P->stages.push_back(std::move(g));
     }
-    // both -> right (S2), reduce_right (S0), right -> left (OUT)
+    // both -> right (S2), reduce_right (S0; SU(2) only), right -> left (OUT)
     ps.clear();
     BM rp = map_both_to_right(p1, p2, a_left, b_right, th, QCM_BUF_S1, ps);
     add_map(P.get(), ps, rp, QCM_BUF_S2, len);
     s2 = std::max(s2, len);
-    ps.clear();
-    BM red = map_reduce_right(p1, p2, b_right, rp, QCM_BUF_S2, ps);
-    add_map(P.get(), ps, red, QCM_BUF_S0, len);
-    s0 = std::max(s0, len);
+    BM red;
+    int32_t red_buf = QCM_BUF_S2;
+    if (abelian) {
+        red = rp;
+    } else {
+        ps.clear();
+        red = map_reduce_right(p1, p2, b_right, rp, QCM_BUF_S2, ps);
+        add_map(P.get(), ps, red, QCM_BUF_S0, len);
+        s0 = std::max(s0, len);
+        red_buf = QCM_BUF_S0;
+    }
     Idx phys2 = index_product(p1, p2);
     Idx new_left = left_basis(red);
     Idx right = b_right;
     Idx possible_right = index_product(phys2, new_left);
     common_subset(right, possible_right);
     ps.clear();
-    BM lp = map_r2l(phys2, new_left, right, red, QCM_BUF_S0, ps);
+    BM lp = map_r2l(phys2, new_left, right, red, red_buf, ps);
     add_map(P.get(), ps, lp, QCM_BUF_OUT, len);
     P->out_elems = len;
     P->scratch[0] = s0;
@@ -459,16 +468,22 @@ qcm_plan* build_theta(const Idx& p1, const Idx& a_left, const Idx& a_right, cons
 
 // The both-paired two-site tensor (the matrix the truncation factorises) from the
 // reduced left-paired one.  Slots: KET = the reduced tensor, OUT = theta (both-paired).
-qcm_plan* build_split(const Idx& p1, const Idx& p2, const Idx& left_i, const Idx& right_i, const BM& u) {
+qcm_plan* build_split(const Idx& p1, const Idx& p2, const Idx& left_i, const Idx& right_i, const BM& u,
+                      bool abelian) {
     auto P = std::make_unique<qcm_plan>();
     P->kind = PK_SPLIT;
     int64_t len = 0;
     std::vector<Piece> ps;
-    BM tst = map_unreduce_left(p1, p2, left_i, u, QCM_BUF_KET, ps);
-    add_map(P.get(), ps, tst, QCM_BUF_S0, len);
-    P->scratch[0] = len;
+    BM tst = u;
+    int32_t tst_buf = QCM_BUF_KET;
+    if (!abelian) {
+        tst = map_unreduce_left(p1, p2, left_i, u, QCM_BUF_KET, ps);
+        add_map(P.get(), ps, tst, QCM_BUF_S0, len);
+        P->scratch[0] = len;
+        tst_buf = QCM_BUF_S0;
+    }
     ps.clear();
-    BM both = map_left_to_both(p1, p2, left_i, right_i, tst, QCM_BUF_S0, ps);
+    BM both = map_left_to_both(p1, p2, left_i, right_i, tst, tst_buf, ps);
     add_map(P.get(), ps, both, QCM_BUF_OUT, len);
     P->out_elems = len;
     P->out_bm = both.b;
@@ -564,6 +579,13 @@ qcm_plan* build_assemble(const Idx& p1, const Idx& p2, const Idx& left_i, const 
 
 using namespace qcm;
 
+// true for the abelian group; throws on an unknown one
+static bool check_symmetry(int32_t symmetry) {
+    if (symmetry != QCM_SYM_SU2U1 && symmetry != QCM_SYM_TWOU1)
+        throw std::runtime_error("unknown symmetry " + std::to_string(symmetry));
+    return symmetry == QCM_SYM_TWOU1;
+}
+
 static int mps_guard(const char* what, const std::function<qcm_plan*()>& f, qcm_plan** out) {
     if (!out) { set_error(std::string(what) + ": null output"); return QCM_E_INVALID; }
     *out = nullptr;
@@ -580,18 +602,19 @@ extern "C" {
 
 int qcm_plan_two_site(const qcm_index_t* phys1, const qcm_index_t* a_left, const qcm_index_t* a_right,
                       const qcm_blocks_t* a, const qcm_index_t* phys2, const qcm_index_t* b_left,
-                      const qcm_index_t* b_right, const qcm_blocks_t* b, qcm_plan** plan) {
+                      const qcm_index_t* b_right, const qcm_blocks_t* b, int32_t symmetry, qcm_plan** plan) {
     return mps_guard("qcm_plan_two_site", [&] {
         return build_theta(read_index(phys1), read_index(a_left), read_index(a_right), read_blocks(a),
-                           read_index(phys2), read_index(b_left), read_index(b_right), read_blocks(b));
+                           read_index(phys2), read_index(b_left), read_index(b_right), read_blocks(b),
+                           check_symmetry(symmetry));
     }, plan);
 }
 
 int qcm_plan_split_theta(const qcm_index_t* phys1, const qcm_index_t* phys2, const qcm_index_t* left_i,
-                         const qcm_index_t* right_i, const qcm_blocks_t* u, qcm_plan** plan) {
+                         const qcm_index_t* right_i, const qcm_blocks_t* u, int32_t symmetry, qcm_plan** plan) {
     return mps_guard("qcm_plan_split_theta", [&] {
         return build_split(read_index(phys1), read_index(phys2), read_index(left_i), read_index(right_i),
-                           read_blocks(u));
+                           read_blocks(u), check_symmetry(symmetry));
     }, plan);
 }
 

@@ -323,6 +323,22 @@ struct MpoV {
     }
     int lspin(int b) const { return m->left_spin[b]; }
     int rspin(int b) const { return m->right_spin[b]; }
+    // Abelian groups (TwoU1) have no spin couplings: every coupling is the term's
+    // scale, every triangle test passes and a Hermitian partner enters with
+    // scale 1 (conjugate_phases of common/boundary_times_mps.hpp:44-51 and the
+    // abelian lbtm/rbtm kernels, ct/abelian/apply_op.hpp:80-138).
+    bool abelian() const { return m->symmetry == QCM_SYM_TWOU1; }
+    bool allowed(int a, int b, int c) const { return abelian() || triangle(a, b, c); }
+    double conj_scale(int lc_s, int rc_s, int spin, int phase) const {
+        return abelian() ? 1.0 : conjugate_correction(lc_s, rc_s, spin) * phase;
+    }
+    void coupling(int j, int jp, int a, int k, int ap, int i, int ip, double scale, double out[4]) const {
+        if (abelian()) {
+            out[0] = out[1] = out[2] = out[3] = scale;
+            return;
+        }
+        set_coupling(j, std::abs(j - jp), jp, a, k, ap, i, std::abs(i - ip), ip, scale, out);
+    }
     bool lskip(int b) const { return m->left_herm[b] < b; }
     bool rskip(int b) const { return m->right_herm[b] < b; }
     int lconj(int b) const { return m->left_herm[b]; }
@@ -403,8 +419,7 @@ static std::vector<BM> plan_k1(const std::vector<BM>& L, const MpoV& W, bool her
         if (use_conj) {
             const BM& src = L[W.lconj((int)b1)];
             for (auto& x : src.b) {
-                double sc = phases ? conjugate_correction(x.lc.s, x.rc.s, W.lspin((int)b1)) * W.lphase((int)b1)
-                                   : 1.0;
+                double sc = phases ? W.conj_scale(x.lc.s, x.rc.s, W.lspin((int)b1), W.lphase((int)b1)) : 1.0;
                 Ab.push_back({(int)b1, x.lc, x.rc, x.off, x.rows, 0, sc, x.rows, x.cols, 0});
             }
         } else {
@@ -467,10 +482,15 @@ static std::vector<BM> plan_k1(const std::vector<BM>& L, const MpoV& W, bool her
 // K2: contr[b2] = sum_{b1,op} couplings x stripes of T[b1]  (lbtm_kernel).
 // prov (optional): per emitted term, in aterm order, the MPO term it comes from
 // (index into term_op/term_scale) and its coefficient per unit of that term's scale.
+// alloc_all: also the blocks the abelian kernel allocates whether or not a term
+// writes them (lbtm_kernel_allocate, ct/abelian/apply_op.hpp:23-66: for every
+// (b1, operator) of the column with a non-empty T[b1], one block per right
+// sector, at the operator's and T's constant charge shifts); they stay zero but
+// are part of a boundary's layout.
 static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const std::vector<int>& b2list,
                                const Idx& right_i, const Idx& out_left_i, const PB& in_right_pb,
                                const PB& out_left_pb, int t_buf, int c_buf, Stage& st, qcm_plan* P, int64_t& end,
-                               std::vector<std::pair<int32_t, double>>* prov = nullptr) {
+                               std::vector<std::pair<int32_t, double>>* prov = nullptr, bool alloc_all = false) {
     const qcm_mpo_t* m = W.m;
     std::vector<BM> C(m->col_dim);
     // the terms of one b2 column with their tile keys, sorted (stably) by key
@@ -497,6 +517,18 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
                 int op = m->term_op[tt];
                 double scale = m->term_scale[tt];
                 int k = m->op_spin[op];
+                if (alloc_all && !T[b1].b.empty() && m->op_blk_ptr[op] < m->op_blk_ptr[op + 1]) {
+                    const int w0 = m->op_blk_ptr[op];
+                    const Q op_delta = fuse(Q(m->blk_q[4 * w0 + 2], m->blk_q[4 * w0 + 3]),
+                                            neg(Q(m->blk_q[4 * w0], m->blk_q[4 * w0 + 1])));
+                    const Q t_delta = fuse(T[b1].b[0].rc, neg(T[b1].b[0].lc));
+                    const Q total = fuse(op_delta, neg(t_delta));
+                    for (auto& rs : right_i.d) {
+                        const Q out_l = fuse(rs.first, total);
+                        const size_t pl = out_left_i.position(out_l);
+                        if (pl != out_left_i.size()) out.blocks.push_back({out_l, rs.first, out_left_i.d[pl].second, rs.second});
+                    }
+                }
                 for (auto& tb : T[b1].b) {
                     Q lc = tb.lc, rc = tb.rc, mc = tb.rc;
                     int64_t l_size = tb.rows;
@@ -506,7 +538,7 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
                         size_t rb = right_i.position(out_r);
                         if (rb == right_i.size()) continue;
                         Q out_l = fuse(lc, pout);
-                        if (!triangle(out_r.s, ap, out_l.s)) continue;
+                        if (!W.allowed(out_r.s, ap, out_l.s)) continue;
                         const size_t pl = out_left_i.position(out_l);
                         if (pl == out_left_i.size()) continue;
                         int64_t r_size = right_i.d[rb].second;
@@ -515,7 +547,7 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
                         out.blocks.push_back({out_l, out_r, out_left_i.d[pl].second, r_size});
                         int i = lc.s, ip = out_l.s, j = mc.s, jp = out_r.s;
                         double cpl[4];
-                        set_coupling(j, std::abs(j - jp), jp, a, k, ap, i, std::abs(i - ip), ip, scale, cpl);
+                        W.coupling(j, jp, a, k, ap, i, ip, scale, cpl);
                         int64_t iro = in_right_pb(pin, out_r), olo = out_left_pb(pout, lc);
                         for (int en = m->blk_ent_ptr[wb]; en < m->blk_ent_ptr[wb + 1]; ++en) {
                             int ss1 = m->ent[4 * en], ss2 = m->ent[4 * en + 1];
@@ -854,7 +886,7 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
                     size_t k = rs.find(al, ar);
                     if (k == rs.b.size()) continue;
                     s.b_buf = QCM_BUF_RIGHT; s.tb = 1; s.b_off = rs.b[k].off; s.ldb = rs.b[k].rows;
-                    s.alpha = conjugate_correction(ar.s, al.s, W.rspin(b2)) * W.rphase(W.rconj(b2));
+                    s.alpha = W.conj_scale(ar.s, al.s, W.rspin(b2), W.rphase(W.rconj(b2)));
                     if (rs.b[k].cols != a.cols || rs.b[k].rows != ob.cols)
                         throw std::runtime_error("K3 dimension mismatch (adjoint)");
                 } else {
@@ -1071,8 +1103,11 @@ static qcm_plan* build_diag(const Idx& phys, const Idx& left_i, const Idx& right
                         const int k = m->op_spin[op];
                         const double pref = std::sqrt((ip + 1.0) * (j + 1.0) / ((i + 1.0) * (jp + 1.0))) *
                                             m->term_scale[tt];
-                        const double c0 = pref * mod_coupling(j, std::abs(j - jp), jp, a, k, ap, i, std::abs(i - ip), ip);
-                        const double c1 = pref * mod_coupling(j, 2, jp, a, k, ap, i, 2, ip);
+                        const double c0 = W.abelian() ? m->term_scale[tt]
+                                                      : pref * mod_coupling(j, std::abs(j - jp), jp, a, k, ap, i,
+                                                                            std::abs(i - ip), ip);
+                        const double c1 = W.abelian() ? m->term_scale[tt]
+                                                      : pref * mod_coupling(j, 2, jp, a, k, ap, i, 2, ip);
                         for (int wb = m->op_blk_ptr[op]; wb < m->op_blk_ptr[op + 1]; ++wb) {
                             Q pin(m->blk_q[4 * wb], m->blk_q[4 * wb + 1]), pout(m->blk_q[4 * wb + 2], m->blk_q[4 * wb + 3]);
                             if (!(pin == pc) || !(pin == pout)) continue;
@@ -1177,7 +1212,7 @@ static qcm_plan* build_grad(const Idx& phys, const Idx& left_i, const Idx& right
                     size_t k = rs.find(al, ar);
                     if (k == rs.b.size()) continue;
                     s.b_buf = QCM_BUF_RIGHT; s.tb = 0; s.b_off = rs.b[k].off; s.ldb = rs.b[k].rows;
-                    s.alpha = conjugate_correction(ar.s, al.s, W.rspin(b2)) * W.rphase(W.rconj(b2));
+                    s.alpha = W.conj_scale(ar.s, al.s, W.rspin(b2), W.rphase(W.rconj(b2)));
                     if (rs.b[k].cols != a.cols || rs.b[k].rows != ob.cols)
                         throw std::runtime_error("gradient: K3 dimension mismatch (adjoint)");
                 } else {
@@ -1258,7 +1293,7 @@ static qcm_plan* build_bleft(const Idx& phys, const Idx& left_i, const Idx& righ
     Stage s2; int64_t c_end = 0;
     const int32_t c_buf = tensor_mpo ? QCM_BUF_OUT : QCM_BUF_S2;
     std::vector<BM> C = plan_k2(T, W, b2list, right_i, out_left_i, in_right_pb, out_left_pb, QCM_BUF_S1,
-                                c_buf, s2, P, c_end);
+                                c_buf, s2, P, c_end, nullptr, W.abelian());
     Stage z2; z2.kind = ST_ZERO; z2.zbuf = c_buf; z2.zlen = c_end;
     if (tensor_mpo) {
         // C already carries its offsets in OUT, bond after bond
@@ -1296,7 +1331,7 @@ static qcm_plan* build_bleft(const Idx& phys, const Idx& left_i, const Idx& righ
             Q ar = a.rc;  // out_l
             size_t it = mps.left_lower_bound(ar);
             for (; it < mps.b.size() && mps.b[it].lc == ar; ++it) {
-                if (!triangle(a.lc.s, W.rspin(b2), mps.b[it].rc.s)) continue;
+                if (!W.allowed(a.lc.s, W.rspin(b2), mps.b[it].rc.s)) continue;
                 Blk nb;
                 nb.lc = a.lc;
                 nb.rc = mps.b[it].rc;
@@ -1399,7 +1434,7 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
                 nb.cols = use_conj ? bb.rows : bb.cols;
                 if (t[b2].find(nb.lc, nb.rc) != t[b2].b.size()) throw std::runtime_error("duplicate t block");
                 t[b2].insert(nb);
-                double s = use_conj ? conjugate_correction(bb.lc.s, bb.rc.s, W.rspin(b2)) * W.rphase(W.rconj(b2)) : 1.0;
+                double s = use_conj ? W.conj_scale(bb.lc.s, bb.rc.s, W.rspin(b2), W.rphase(W.rconj(b2))) : 1.0;
                 jobs.push_back({b2, nb.lc, nb.rc, ak, bb.off, bb.rows, use_conj ? 1 : 0, s, nb.cols});
             }
         }
@@ -1455,12 +1490,12 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
                         size_t lb = left_i.position(out_l);
                         if (lb == left_i.size()) continue;
                         Q out_r = fuse(rc, neg(pout));
-                        if (!triangle(out_l.s, a, out_r.s)) continue;
+                        if (!Wv.allowed(out_l.s, a, out_r.s)) continue;
                         if (!out_right_i.has(out_r)) continue;
                         int64_t l_size = left_i.d[lb].second;
                         int i = out_r.s, ip = rc.s, j = out_l.s, jp = mc.s;
                         double cpl[4];
-                        set_coupling(j, std::abs(j - jp), jp, a, k, ap, i, std::abs(i - ip), ip, scale, cpl);
+                        Wv.coupling(j, jp, a, k, ap, i, ip, scale, cpl);
                         int64_t ilo = in_left_pb(pin, out_l), oro = out_right_pb(pout, rc);
                         int64_t r_size = tb.cols;
                         if (buf[b1].find(out_l, out_r) == buf[b1].b.size()) {
@@ -1479,6 +1514,34 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
                             tv.terms.push_back({QCM_BUF_S1, tb.off + ilo + (int64_t)ss1 * l_size, tb.rows, alfa});
                             P->axpy_flops += 2.0 * l_size * r_size;
                         }
+                    }
+                }
+            }
+        }
+    }
+    if (Wv.abelian()) {
+        // rbtm_kernel_allocate (ct/abelian/apply_op.hpp:140-187): for every (b2, operator)
+        // of the row with a non-empty t[b2], one block per left sector at the constant
+        // charge shifts, whether or not a term writes it (zero, but part of the layout)
+        for (int b1 = 0; b1 < m->row_dim; ++b1) {
+            if (herm && !tensor_mpo && Wv.lskip(b1)) continue;
+            for (size_t r = 0; r < Wv.row_b2[b1].size(); ++r) {
+                const int b2 = Wv.row_b2[b1][r], e = Wv.row_elem[b1][r];
+                if (t[b2].b.empty()) continue;
+                const Q t_delta = fuse(t[b2].b[0].rc, neg(t[b2].b[0].lc));
+                for (int tt = m->term_ptr[e]; tt < m->term_ptr[e + 1]; ++tt) {
+                    const int op = m->term_op[tt];
+                    if (m->op_blk_ptr[op] == m->op_blk_ptr[op + 1]) continue;
+                    const int w0 = m->op_blk_ptr[op];
+                    const Q op_delta = fuse(Q(m->blk_q[4 * w0 + 2], m->blk_q[4 * w0 + 3]),
+                                            neg(Q(m->blk_q[4 * w0], m->blk_q[4 * w0 + 1])));
+                    const Q total = fuse(op_delta, neg(t_delta));
+                    for (auto& ls : left_i.d) {
+                        const Q out_r = fuse(ls.first, neg(total));
+                        if (!out_right_i.has(out_r) || buf[b1].find(ls.first, out_r) != buf[b1].b.size()) continue;
+                        Blk nb;
+                        nb.lc = ls.first; nb.rc = out_r; nb.rows = ls.second; nb.cols = out_right_i.size_of(out_r);
+                        buf[b1].insert(nb);
                     }
                 }
             }
@@ -1535,7 +1598,7 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
             Q ar = a.rc;
             size_t k = rp.find(ar, ar);
             if (k == rp.b.size()) continue;
-            if (!triangle(a.lc.s, Wv.lspin(b1), ar.s)) continue;
+            if (!Wv.allowed(a.lc.s, Wv.lspin(b1), ar.s)) continue;
             Blk nb;
             nb.lc = a.lc; nb.rc = ar; nb.rows = a.rows; nb.cols = rp.b[k].rows;
             out[b1].insert(nb);

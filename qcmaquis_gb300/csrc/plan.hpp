@@ -261,7 +261,8 @@ namespace qcm {
 void set_error(const std::string& msg);
 Idx read_index(const qcm_index_t* x);
 BM read_blocks(const qcm_blocks_t* x);
-qcm_plan* build_split(const Idx& p1, const Idx& p2, const Idx& left_i, const Idx& right_i, const BM& u);
+qcm_plan* build_split(const Idx& p1, const Idx& p2, const Idx& left_i, const Idx& right_i, const BM& u,
+                      bool abelian);
 qcm_plan* build_assemble(const Idx& p1, const Idx& p2, const Idx& left_i, const Idx& right_i, const BM& both,
                          const int64_t* u_off, const int64_t* vt_off, const int64_t* kdim, const int64_t* keep,
                          const double* S_host, const int64_t* s_off, bool l2r);

@@ -376,10 +376,14 @@ int qcm_boundary_step(qcm_ctx* c, qcm_plan* plan, const double* mps, const doubl
 
 int qcm_split(qcm_ctx* c, const qcm_index_t* phys1, const qcm_index_t* phys2, const qcm_index_t* left_i,
               const qcm_index_t* right_i, const qcm_blocks_t* u, const double* u_dev, int32_t l2r, int64_t Mmax,
-              double cutoff, qcm_trunc_t* trunc, qcm_split_result** out) {
+              double cutoff, int32_t symmetry, qcm_trunc_t* trunc, qcm_split_result** out) {
     int rc = check_ctx(c);
     if (rc) return rc;
     if (!u_dev || !trunc || !out) { set_error("qcm_split: null argument"); return QCM_E_INVALID; }
+    if (symmetry != QCM_SYM_SU2U1 && symmetry != QCM_SYM_TWOU1) {
+        set_error("qcm_split: unknown symmetry");
+        return QCM_E_INVALID;
+    }
     *out = nullptr;
     qcm_plan* sp = nullptr;
     qcm_svd* svd = nullptr;
@@ -396,7 +400,7 @@ int qcm_split(qcm_ctx* c, const qcm_index_t* phys1, const qcm_index_t* phys2, co
     };
     try {
         sp = build_split(read_index(phys1), read_index(phys2), read_index(left_i), read_index(right_i),
-                         read_blocks(u));
+                         read_blocks(u), symmetry == QCM_SYM_TWOU1);
     } catch (const std::exception& e) {
         set_error(std::string("qcm_split: ") + e.what());
         return cleanup(QCM_E_INVALID);

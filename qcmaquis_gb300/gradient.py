@@ -75,9 +75,11 @@ class CheckpointedRight:
     def __init__(self, step, last, L: int, k: int = 1, nbytes=None):
         self.step = step
         self.k = max(1, int(k))
+        self.nbytes = nbytes
         self.stored = {L: last}
         self.segment = {}
         self.env_bytes = {}
+        self.peak_bytes = 0
         cur = last
         for j in range(L - 1, 0, -1):
             cur = step(j, cur)
@@ -85,6 +87,7 @@ class CheckpointedRight:
                 self.env_bytes[j] = nbytes(cur)
             if self.k == 1 or j % self.k == 0:
                 self.stored[j] = cur
+            self._track()
 
     def __getitem__(self, i: int):
         if i in self.stored:
@@ -96,7 +99,14 @@ class CheckpointedRight:
             for jj in range(top - 1, i - 1, -1):
                 b = self.step(jj, b)
                 self.segment[jj] = b
+                self._track()
         return self.segment[i]
+
+    def _track(self):
+        """The most bytes the resident environments have held (with ``nbytes``)."""
+        if self.nbytes is not None:
+            held = sum(self.nbytes(b) for b in list(self.stored.values()) + list(self.segment.values()))
+            self.peak_bytes = max(self.peak_bytes, held)
 
     def release(self, i: int):
         self.stored.pop(i, None)
@@ -150,7 +160,8 @@ def term_gradients(mpo, mps: List[DeviceMPSTensor], nelec: int, twoS: int = 0, e
         del R
     torch.cuda.synchronize()
     if stats is not None:
-        stats.update(env_bytes=rights.env_bytes, peak_resident_environments=peak, site_energies=e_sites)
+        stats.update(env_bytes=rights.env_bytes, peak_resident_environments=peak, site_energies=e_sites,
+                     peak_environment_bytes=rights.peak_bytes)
     return grads, fmpos, e_sites, time.time() - t0
 
 

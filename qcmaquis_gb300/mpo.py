@@ -64,7 +64,10 @@ class Hermitian:
 
 
 class MPOTensor:
-    """Sparse (b1, b2) -> [(op, scale), ...] tensor with SU(2) bond spins."""
+    """Sparse (b1, b2) -> [(op, scale), ...] tensor with SU(2) bond spins (all 0 for
+    an abelian group; ``symmetry`` names the group: "su2u1" or "2u1")."""
+
+    symmetry = "su2u1"
 
     def __init__(self, ld: int, rd: int, prempo: List[Tuple[int, int, int, float]], op_table: List[SiteOperator],
                  herm: Optional[Hermitian], left_spins: List[SpinDescriptor], right_spins: List[SpinDescriptor]):
@@ -152,6 +155,7 @@ class TaggedMPOMaker:
 
     def __init__(self, model: QCModel, merge_site_terms: bool = True):
         self.L = model.L
+        self.symmetry = getattr(model, "symmetry", "su2u1")
         self.th: TagHandler = model.tag_handler
         self.identity = model.ops.ident
         self.identity_full = model.ops.ident_full
@@ -300,6 +304,9 @@ class TaggedMPOMaker:
         kind, pos_op, off = k
         conj = (kind, tuple((pp, th.herm_conj(t)) for pp, t in pos_op), off)
         phase = (1, 1)
+        if self.symmetry != "su2u1":
+            # abelian groups: a partner bond's boundary is the plain transpose
+            return conj, phase
         if len(pos_op) == 1:
             op1 = th.get_op(pos_op[0][1])
             if p < pos_op[0][0]:
@@ -381,6 +388,7 @@ class TaggedMPOMaker:
                 t = MPOTensor(ldim, 1, pre, table, h, left_spins, right_spins)
             else:
                 t = MPOTensor(ldim, rdim, pre, table, h, left_spins, right_spins)
+            t.symmetry = self.symmetry
             mpo.append(t)
             left = right
             left_spins = right_spins

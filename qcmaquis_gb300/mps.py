@@ -37,7 +37,9 @@ class HostMPSTensor:
         return self.data.norm()
 
 
-def allowed_sectors(L: int, phys: Index, right_end, Mmax: int) -> List[Index]:
+def allowed_sectors(L: int, phys: Index, right_end, Mmax: int, abelian: bool = False) -> List[Index]:
+    """``allowed_sectors``; ``abelian`` (TwoU1) drops the SU(2) test that a sector's
+    spin is not negative (``ChargeDetailClass::physical``)."""
     physc = phys.copy()
     physc.sort()
     cmax, cmin = physc[0][0], physc[len(physc) - 1][0]
@@ -55,7 +57,8 @@ def allowed_sectors(L: int, phys: Index, right_end, Mmax: int) -> List[Index]:
         cmaxi = fuse(cmaxi, neg(cmax))
         cmini = fuse(cmini, neg(cmin))
         li.data = [[c, min(Mmax, s)] for c, s in li
-                   if not (fuse(c, cmaxi) < right_end) and not (fuse(c, cmini) > right_end) and spin(c) >= 0]
+                   if not (fuse(c, cmaxi) < right_end) and not (fuse(c, cmini) > right_end)
+                   and (abelian or spin(c) >= 0)]
         left[i] = li
     cmaxi, cmini = maxt, mint
     for i in range(L - 1, -1, -1):
@@ -63,7 +66,8 @@ def allowed_sectors(L: int, phys: Index, right_end, Mmax: int) -> List[Index]:
         cmaxi = fuse(cmaxi, neg(cmax))
         cmini = fuse(cmini, neg(cmin))
         ri.data = [[c, min(Mmax, s)] for c, s in ri
-                   if not (fuse(c, neg(cmaxi)) > (0, 0)) and not (fuse(c, neg(cmini)) < (0, 0)) and spin(c) >= 0]
+                   if not (fuse(c, neg(cmaxi)) > (0, 0)) and not (fuse(c, neg(cmini)) < (0, 0))
+                   and (abelian or spin(c) >= 0)]
         right[i] = ri
         common_subset(left[i], right[i])
     out = []

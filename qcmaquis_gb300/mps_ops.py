@@ -214,27 +214,30 @@ def _run_fp64(plan, device, ket=None, left=None, out=None, s2=None):
                    N.PREC_FP64, _stream(device))
 
 
-def make_two_site_mps(A: DeviceMPSTensor, B: DeviceMPSTensor) -> DeviceMPSTensor:
+def make_two_site_mps(A: DeviceMPSTensor, B: DeviceMPSTensor, symmetry: int = N.SYM_SU2U1) -> DeviceMPSTensor:
     """``TwoSiteTensor(mps1, mps2)`` + ``make_mps``: theta = A(lp).B(rp), reshaped
-    both->right, SU(2)-reduced (6j), returned left-paired -- one native plan
-    (``qcm_plan_two_site``: the grouped block product and three planned gather maps)."""
+    both->right, SU(2)-reduced (6j; not for TwoU1), returned left-paired -- one native
+    plan (``qcm_plan_two_site``: the grouped block product and planned gather maps)."""
     from .engine import _digest
-    key = ("theta", _digest(A.phys_i, A.left_i, A.right_i, A.layout, B.phys_i, B.left_i, B.right_i, B.layout))
+    key = ("theta", symmetry,
+           _digest(A.phys_i, A.left_i, A.right_i, A.layout, B.phys_i, B.left_i, B.right_i, B.layout))
     plan = _RUNNER.plan(key, lambda: N.plan_two_site(A.phys_i, A.left_i, A.right_i, A.layout, B.phys_i, B.left_i,
-                                                     B.right_i, B.layout))
+                                                     B.right_i, B.layout, symmetry))
     phys2, left, right, lay = N.out_tensor(plan)
     out = torch.empty(max(plan.out_elems, 1), dtype=torch.float64, device=A.data.device)
     _run_fp64(plan, A.data.device, ket=A.data, left=B.data, out=out)
     return DeviceMPSTensor(phys2, left, right, lay, out)
 
 
-def split_theta(u: DeviceMPSTensor, A0: DeviceMPSTensor, B0: DeviceMPSTensor):
+def split_theta(u: DeviceMPSTensor, A0: DeviceMPSTensor, B0: DeviceMPSTensor, symmetry: int = N.SYM_SU2U1):
     """``tst << u`` followed by ``reshape_left_to_both``: the both-paired matrix of the
-    two-site tensor (native plan ``qcm_plan_split_theta``: the 6j unreduce_left and the
-    reshape as planned gather maps).  Returns (plan, layout, flat device buffer)."""
+    two-site tensor (native plan ``qcm_plan_split_theta``: the 6j unreduce_left, SU2U1
+    only, and the reshape as planned gather maps).  Returns (plan, layout, flat device
+    buffer)."""
     from .engine import _digest
-    key = ("split", _digest(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, u.layout))
-    plan = _RUNNER.plan(key, lambda: N.plan_split_theta(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, u.layout))
+    key = ("split", symmetry, _digest(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, u.layout))
+    plan = _RUNNER.plan(key, lambda: N.plan_split_theta(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, u.layout,
+                                                        symmetry))
     _, _, _, lay = N.out_tensor(plan)
     out = torch.empty(max(plan.out_elems, 1), dtype=torch.float64, device=u.data.device)
     _run_fp64(plan, u.data.device, ket=u.data, out=out)
@@ -371,7 +374,8 @@ def add_perturbation(dm: DBM, both: DBM, half, alpha: float, l2r: bool):
 
 
 def split(u: DeviceMPSTensor, A0: DeviceMPSTensor, B0: DeviceMPSTensor, Mmax: int, cutoff: float, l2r: bool,
-          truncation: str = "svd", alpha: float = 0.0, engine=None, boundary=None, mpo=None):
+          truncation: str = "svd", alpha: float = 0.0, engine=None, boundary=None, mpo=None,
+          symmetry: int = N.SYM_SU2U1):
     """``tst << u`` then the truncation of ``SweepMPSUpdater`` (``sba/SweepMPSUpdater.h:186-203``):
     ``split_mps_l2r/r2l`` (``truncation="svd"``, the reference's default) or
     ``predict_split_l2r/r2l`` (``"heev"``, ``twositetensor.hpp:184-297``), whose
@@ -379,8 +383,9 @@ def split(u: DeviceMPSTensor, A0: DeviceMPSTensor, B0: DeviceMPSTensor, Mmax: in
     (left boundary of the pair going right, right boundary going left) and ``mpo``
     (the left / right site's MPO tensor) are given and alpha != 0.  (The
     reference computes the alpha = 0 perturbation and adds zeros; skipping it
-    gives the same matrix.)  Returns new (A, B, truncation results)."""
-    sp, blay, bflat = split_theta(u, A0, B0)
+    gives the same matrix.)  ``symmetry``: ``native.SYM_*`` of the tensors.  Returns new
+    (A, B, truncation results)."""
+    sp, blay, bflat = split_theta(u, A0, B0, symmetry)
     p1, p2 = A0.phys_i, B0.phys_i
     dev = u.data.device
     if truncation == "svd":

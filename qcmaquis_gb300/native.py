@@ -45,7 +45,19 @@ class CMpo(C.Structure):
                 ("left_phase", i32p), ("right_phase", i32p),
                 ("col_ptr", i32p), ("row_of", i32p), ("term_ptr", i32p), ("term_op", i32p), ("term_scale", f64p),
                 ("n_ops", C.c_int32), ("op_spin", i32p), ("op_blk_ptr", i32p), ("blk_q", i32p),
-                ("blk_ent_ptr", i32p), ("ent", i32p), ("ent_coeff", f64p)]
+                ("blk_ent_ptr", i32p), ("ent", i32p), ("ent_coeff", f64p), ("symmetry", C.c_int32)]
+
+
+# symmetry groups of qcm_mpo_t.symmetry and the MPS-level plans
+SYM_SU2U1, SYM_TWOU1 = 0, 1
+
+
+def symmetry_code(name: str) -> int:
+    """QCM_SYM_* of a symmetry name ("su2u1", "2u1")."""
+    codes = {"su2u1": SYM_SU2U1, "2u1": SYM_TWOU1}
+    if name not in codes:
+        raise ValueError(f"unsupported symmetry {name!r}")
+    return codes[name]
 
 
 _lib = None
@@ -122,8 +134,9 @@ def lib():
     L.qcm_seg_multi_dot.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                     C.c_void_p, C.c_void_p]
     L.qcm_plan_two_site.argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks)] + [C.POINTER(CIndex)] * 3 + \
-        [C.POINTER(CBlocks), C.POINTER(C.c_void_p)]
-    L.qcm_plan_split_theta.argtypes = [C.POINTER(CIndex)] * 4 + [C.POINTER(CBlocks), C.POINTER(C.c_void_p)]
+        [C.POINTER(CBlocks), C.c_int32, C.POINTER(C.c_void_p)]
+    L.qcm_plan_split_theta.argtypes = [C.POINTER(CIndex)] * 4 + [C.POINTER(CBlocks), C.c_int32,
+                                                                  C.POINTER(C.c_void_p)]
     L.qcm_plan_split_assemble.argtypes = [C.c_void_p, i64p, i64p, i64p, f64p, i64p, C.c_int32,
                                           C.POINTER(C.c_void_p)]
     L.qcm_plan_out_tensor.argtypes = [C.c_void_p, C.c_int32, i32p, i32p, i64p, i64p, i64p, i32p, i32p, i64p]
@@ -393,6 +406,7 @@ class FMpo:
 
     def __init__(self, mpo):
         self.mpo = mpo
+        self.symmetry = symmetry_code(getattr(mpo, "symmetry", "su2u1"))
         self.left_spin = np.array([s.get() for s in mpo.left_spins], dtype=np.int32)
         self.right_spin = np.array([s.get() for s in mpo.right_spins], dtype=np.int32)
         self.left_herm = np.array(mpo.herm.LeftHerm, dtype=np.int32)
@@ -452,7 +466,7 @@ class FMpo:
                       _p(self.right_phase, i32p), _p(self.col_ptr, i32p), _p(self.row_of, i32p),
                       _p(self.term_ptr, i32p), _p(self.term_op, i32p), _p(self.term_scale, f64p),
                       self.n_ops, _p(self.op_spin, i32p), _p(self.op_blk_ptr, i32p), _p(self.blk_q, i32p),
-                      _p(self.blk_ent_ptr, i32p), _p(self.ent, i32p), _p(self.ent_coeff, f64p))
+                      _p(self.blk_ent_ptr, i32p), _p(self.ent, i32p), _p(self.ent_coeff, f64p), self.symmetry)
 
     @property
     def n_terms(self) -> int:
@@ -508,7 +522,7 @@ def make_twosite_fmpo(w1: FMpo, w2: FMpo, phys1: Index, phys2: Index = None, nat
 
 def _twosite_products(L, w1: FMpo, w2: FMpo, phys1: Index, phys2: Index, h):
     """qcm_mpo_twosite_begin / _keys / _finish with the products formed by op_kron_su2."""
-    from .site_operator import SpinDescriptor, op_kron_su2
+    from .site_operator import SpinDescriptor, op_kron_abelian, op_kron_su2
     nk = C.c_int32()
     check(L.qcm_mpo_twosite_begin(C.byref(w1.c), C.byref(w2.c), C.byref(h), C.byref(nk)), "qcm_mpo_twosite_begin")
     try:
@@ -518,8 +532,11 @@ def _twosite_products(L, w1: FMpo, w2: FMpo, phys1: Index, phys2: Index, h):
         for o1, o2, j, jpp, jp, sp in keys[:6 * nk.value].reshape(-1, 6).tolist():
             op1 = w1.mpo.op(w1.op_tags[o1])
             op2 = w2.mpo.op(w2.op_tags[o2])
-            prod = op_kron_su2(phys1, phys2, op1, op2, SpinDescriptor(j), SpinDescriptor(jpp), SpinDescriptor(jp),
-                               SpinDescriptor(sp, j, jp))
+            if w1.symmetry == SYM_TWOU1:
+                prod = op_kron_abelian(phys1, phys2, op1, op2)
+            else:
+                prod = op_kron_su2(phys1, phys2, op1, op2, SpinDescriptor(j), SpinDescriptor(jpp),
+                                   SpinDescriptor(jp), SpinDescriptor(sp, j, jp))
             prod.remove_empty_blocks()
             op_spin.append(sp)
             for (pin, pout), ents in zip(prod.bm.keys, prod.sparse()):
@@ -553,6 +570,7 @@ def _fmpo_from_buf(L, h) -> FMpo:
     ne, nt, nb, nent = sz[0], sz[1], sz[2], sz[3]
     f = FMpo.__new__(FMpo)
     f.mpo = _FlatTensor(v.row_dim, v.col_dim)
+    f.symmetry = int(v.symmetry)
     f.left_spin = _copy(v.left_spin, v.row_dim, np.int32)
     f.right_spin = _copy(v.right_spin, v.col_dim, np.int32)
     f.left_herm = _copy(v.left_herm, v.row_dim, np.int32)
@@ -749,24 +767,26 @@ def out_tensor(plan: "Plan", which: int = 0):
     return idx[0], idx[1], idx[2], Layout(keys, shapes, [int(x) for x in off[:nb]])
 
 
-def plan_two_site(a_phys, a_left, a_right, a_lay: "Layout", b_phys, b_left, b_right, b_lay: "Layout") -> "Plan":
-    """``qcm_plan_two_site``: the reduced two-site tensor of sites (i, i+1) from their
-    left-paired tensors (slots KET = A, LEFT = B, OUT = the two-site tensor)."""
+def plan_two_site(a_phys, a_left, a_right, a_lay: "Layout", b_phys, b_left, b_right, b_lay: "Layout",
+                  symmetry: int = SYM_SU2U1) -> "Plan":
+    """``qcm_plan_two_site``: the two-site tensor of sites (i, i+1) (SU(2)-reduced for
+    SU2U1) from their left-paired tensors (slots KET = A, LEFT = B, OUT = the two-site
+    tensor)."""
     f = [FIndex(x) for x in (a_phys, a_left, a_right, b_phys, b_left, b_right)]
     h = C.c_void_p()
     check(lib().qcm_plan_two_site(C.byref(f[0].c), C.byref(f[1].c), C.byref(f[2].c), C.byref(a_lay.c),
-                                  C.byref(f[3].c), C.byref(f[4].c), C.byref(f[5].c), C.byref(b_lay.c), C.byref(h)),
-          "qcm_plan_two_site")
+                                  C.byref(f[3].c), C.byref(f[4].c), C.byref(f[5].c), C.byref(b_lay.c),
+                                  int(symmetry), C.byref(h)), "qcm_plan_two_site")
     return Plan(h, "theta")
 
 
-def plan_split_theta(p1, p2, left_i, right_i, u_lay: "Layout") -> "Plan":
+def plan_split_theta(p1, p2, left_i, right_i, u_lay: "Layout", symmetry: int = SYM_SU2U1) -> "Plan":
     """``qcm_plan_split_theta``: the both-paired two-site tensor (slot OUT) from the
-    reduced left-paired one (slot KET)."""
+    left-paired one (slot KET)."""
     f = [FIndex(x) for x in (p1, p2, left_i, right_i)]
     h = C.c_void_p()
     check(lib().qcm_plan_split_theta(C.byref(f[0].c), C.byref(f[1].c), C.byref(f[2].c), C.byref(f[3].c),
-                                     C.byref(u_lay.c), C.byref(h)), "qcm_plan_split_theta")
+                                     C.byref(u_lay.c), int(symmetry), C.byref(h)), "qcm_plan_split_theta")
     return Plan(h, "split")
 
 

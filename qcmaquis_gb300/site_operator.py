@@ -247,5 +247,26 @@ def op_kron_su2(phys_A: Index, phys_B: Index, Ao: SiteOperator, Bo: SiteOperator
     return C
 
 
+def op_kron_abelian(phys_A: Index, phys_B: Index, Ao: SiteOperator, Bo: SiteOperator) -> SiteOperator:
+    """``op_kron`` of an abelian group (``block_matrix/site_operator_algorithms.h:167-205``):
+    the Kronecker product of the two operators in ProductBasis(phys_A, phys_B), block
+    pair by block pair summed into the fused sectors (no couplings, no spins)."""
+    pb = ProductBasis(phys_A, phys_B)
+    blocks = BlockMatrix()
+    for (inA, outA), a_blk in zip(Ao.bm.keys, Ao.bm.blocks):
+        for (inB, outB), b_blk in zip(Bo.bm.keys, Bo.bm.blocks):
+            new_left, new_right = fuse(inA, inB), fuse(outA, outB)
+            tmp = np.zeros((pb.size(new_left), pb.size(new_right)))
+            in_off, out_off = pb(inA, inB), pb(outA, outB)
+            for l1 in range(a_blk.shape[0]):
+                for r1 in range(a_blk.shape[1]):
+                    for l2 in range(b_blk.shape[0]):
+                        for r2 in range(b_blk.shape[1]):
+                            tmp[in_off + l1 * b_blk.shape[0] + l2, out_off + r1 * b_blk.shape[1] + r2] = \
+                                b_blk[l2, r2] * a_blk[l1, r1]
+            blocks.match_and_add_block(tmp, new_left, new_right)
+    return SiteOperator(blocks, SpinDescriptor(), {})
+
+
 __all__ = ["SpinDescriptor", "SiteOperator", "op_equal", "shape_equal", "product_spin",
-           "allowed_spins", "op_kron_su2"]
+           "allowed_spins", "op_kron_su2", "op_kron_abelian"]

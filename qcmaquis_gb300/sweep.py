@@ -110,12 +110,14 @@ class SweepRecord:
 JD_RESIDUAL_FLOOR = {N.PREC_FP64: 0.0, N.PREC_TF32: 5e-4, N.PREC_BF16X3: 2e-6, N.PREC_BF16X2: 1e-5}
 
 
-def default_mps_init(L, phys, right_end, init_bond_dimension, seed, device="cuda") -> List[DeviceMPSTensor]:
+def default_mps_init(L, phys, right_end, init_bond_dimension, seed, device="cuda",
+                     abelian: bool = False) -> List[DeviceMPSTensor]:
     """``default_mps_init`` (``mp_tensors/mps_initializers.h:34-81``): allowed sectors capped at
     ``init_bond_dimension``, uniform [0,1) entries (numpy PCG64 stream seeded with ``seed``,
-    filled block by block in column-major order), each site divided by its norm."""
+    filled block by block in column-major order), each site divided by its norm.
+    ``abelian``: TwoU1 charges."""
     rng = np.random.default_rng(seed)
-    allowed = allowed_sectors(L, phys, right_end, init_bond_dimension)
+    allowed = allowed_sectors(L, phys, right_end, init_bond_dimension, abelian=abelian)
     out = []
     for i in range(L):
         lb = index_product(phys, allowed[i])
@@ -221,9 +223,12 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
         engine.boundary_plan_cache_size = plan_cache
     engine_full = Engine(device, hermitian=False)
     bprec = 0 if boundary_precision is None else boundary_precision
-    right_end = (nelec, twoS)
+    # SU2U1: the target (N, 2S); TwoU1 models carry theirs, (N_up, N_down)
+    sym = N.symmetry_code(getattr(model, "symmetry", "su2u1"))
+    right_end = model.right_end if sym == N.SYM_TWOU1 else (nelec, twoS)
     if mps is None:
-        mps = default_mps_init(L, phys, right_end, p.init_bond_dimension, p.seed, device)
+        mps = default_mps_init(L, phys, right_end, p.init_bond_dimension, p.seed, device,
+                               abelian=sym == N.SYM_TWOU1)
         normalize_right(mps)
     if ts_mpo is None:
         ts_mpo = N.make_ts_cache_fmpo(mpo, phys)
@@ -247,7 +252,7 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
             l2r = forward and not change
             tp0 = engine.plan_seconds
             t_a = time.time()
-            psi = O.make_two_site_mps(mps[site], mps[site + 1])
+            psi = O.make_two_site_mps(mps[site], mps[site + 1], sym)
             rec.layout_digests.append(hash((site, tuple(psi.layout.keys), tuple(psi.layout.shapes),
                                             tuple(left[site].layout.keys), tuple(left[site].layout.shapes),
                                             tuple(right[site + 2].layout.keys), tuple(right[site + 2].layout.shapes))))
@@ -267,13 +272,13 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
                 e64, _, _ = solve_ietl_jcd(sp64, psi, p.ietl_jcd_tol, p.ietl_jcd_maxiter, ortho)
                 rec.shadow.append((theta + mpo.core_energy, e_var + mpo.core_energy, e64 + mpo.core_energy))
             if p.twosite_truncation == "svd":
-                A, B, tr = O.split(u, mps[site], mps[site + 1], Mmax, cutoff, l2r)
+                A, B, tr = O.split(u, mps[site], mps[site + 1], Mmax, cutoff, l2r, symmetry=sym)
             else:
                 # SweepMPSUpdater.h:192-203: the pair's left boundary and left site's MPO
                 # tensor going right, the right boundary and right site's tensor going left
                 bnd, w = (left[site], mpo[site]) if l2r else (right[site + 2], mpo[site + 1])
                 A, B, tr = O.split(u, mps[site], mps[site + 1], Mmax, cutoff, l2r, truncation=p.twosite_truncation,
-                                   alpha=get_alpha(p, sweep), engine=engine, boundary=bnd, mpo=w)
+                                   alpha=get_alpha(p, sweep), engine=engine, boundary=bnd, mpo=w, symmetry=sym)
             mps[site], mps[site + 1] = A, B
             if time_parts:
                 torch.cuda.synchronize()
@@ -342,9 +347,12 @@ def run_dmrg_single_site(model, mpo, p: SweepParams, nelec: int, twoS: int = 0,
     phys = model.phys
     engine = engine or Engine(device, precision=precision)
     engine_full = Engine(device, hermitian=False)
-    right_end = (nelec, twoS)
+    # SU2U1: the target (N, 2S); TwoU1 models carry theirs, (N_up, N_down)
+    sym = N.symmetry_code(getattr(model, "symmetry", "su2u1"))
+    right_end = model.right_end if sym == N.SYM_TWOU1 else (nelec, twoS)
     if mps is None:
-        mps = default_mps_init(L, phys, right_end, p.init_bond_dimension, p.seed, device)
+        mps = default_mps_init(L, phys, right_end, p.init_bond_dimension, p.seed, device,
+                               abelian=sym == N.SYM_TWOU1)
         normalize_right(mps)
     left: List = [None] * (L + 1)
     right: List = [None] * (L + 1)

@@ -160,7 +160,7 @@ int main(int argc, char** argv) {
         qcm_index_t al = in.index("A.left"), ar = in.index("A.right"), bl = in.index("B.left"),
                     br = in.index("B.right");
         qcm_blocks_t ab = in.blocks("A"), bb = in.blocks("B");
-        ok(qcm_plan_two_site(&phys, &al, &ar, &ab, &phys, &bl, &br, &bb, &tp), "qcm_plan_two_site");
+        ok(qcm_plan_two_site(&phys, &al, &ar, &ab, &phys, &bl, &br, &bb, QCM_SYM_SU2U1, &tp), "qcm_plan_two_site");
         Tensor psi = read_tensor([&](int32_t* nb, int32_t* q, int64_t* r, int64_t* c, int64_t* o, int32_t* n3,
                                      int32_t* iq, int64_t* is) {
             return qcm_plan_out_tensor(tp, 0, nb, q, r, c, o, n3, iq, is);
@@ -189,7 +189,8 @@ int main(int argc, char** argv) {
         // split_mps_l2r(Mmax, cutoff)
         qcm_trunc_t tr;
         qcm_split_result* res = nullptr;
-        ok(qcm_split(ctx, &phys, &phys, &al, &br, &pb, du, 1, (int64_t)in.d("Mmax"), in.d("cutoff"), &tr, &res),
+        ok(qcm_split(ctx, &phys, &phys, &al, &br, &pb, du, 1, (int64_t)in.d("Mmax"), in.d("cutoff"), QCM_SYM_SU2U1, &tr,
+                     &res),
            "qcm_split");
         const double* dA2 = nullptr;
         const double* dB2 = nullptr;
