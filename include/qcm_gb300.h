@@ -306,11 +306,13 @@ int qcm_plan_stage_dot(const qcm_plan* plan, int32_t stage, int64_t* out_desc, i
  * and tests): the block products of a GEMM stage, or the dense groups of a
  * gather-axpy stage.  counts4 = (panels, outputs, segments, tiles); call with
  * NULL arrays first.  panel: (src_off, img_off, src_buf, ld, R, K, kcontig, G);
- * output: (c_off, si, sj, c_buf, mrows, ncols, mode, rows, ctab); segment:
+ * output: (c_off, si, sj, c_buf, mrows, ncols, mode, rows, ctab, vrows) -- for
+ * mode 1 with vrows > 0 each column is a run of pitch `rows` of which the first
+ * vrows rows are stored; segment:
  * (a_img, b_img, a_G, b_G, kc, flags, a_panel, a_c0) with seg_alpha; tile:
  * (out, m0, n0, nt, s_begin, s_end).  A panel without an image has img_off -1. */
 int qcm_plan_stage_images(const qcm_plan* plan, int32_t stage, int64_t* counts4, int64_t* panel_desc /*8*n*/,
-                          int64_t* out_desc /*9*n*/, int64_t* seg_desc /*8*n*/, double* seg_alpha,
+                          int64_t* out_desc /*10*n*/, int64_t* seg_desc /*8*n*/, double* seg_alpha,
                           int64_t* tile_desc /*6*n*/);
 /* Auxiliary tables of the same: counts3 = (gather offsets, output-tile
  * offsets, constant-image bytes). */

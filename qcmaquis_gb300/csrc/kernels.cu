@@ -35,7 +35,7 @@ namespace qcm {
         }                                                                               \
     } while (0)
 
-struct DevAxpyOut { int64_t dst_off, ldd, rows, cols, t_begin, t_end; int32_t dst_buf, pad; };
+struct DevAxpyOut { int64_t dst_off, ldd, rows, cols, t_begin, t_end; int32_t dst_buf, pad; };  // pad: pitch
 struct DevAxpyTerm { int64_t src_off, lds; double alpha; int32_t src_buf, pad; };
 struct DevAxpyWork { int64_t out, c0, c1; };
 struct DevAxpyChunk { int32_t out, e0, n, pad; };
@@ -196,16 +196,29 @@ gather_axpy_uniform(BufTable bufs, const DevAxpyOut* __restrict__ outs, const De
     }
 }
 
-// Contiguous-source executor.  Every term of the stage reads a source tile
-// stored contiguously (ld = rows), so element e of an output tile is
-// sum_t alpha_t * src_t[e] over the tile's terms in order.  A work item owns
-// CG_CHUNK consecutive elements of one output tile; each thread keeps
-// CG_PER accumulators at stride CG_THREADS and reads every source with
-// immediate offsets from one per-term pointer (cached in shared memory).
+// Contiguous-source executor.  Every term of an output tile reads a source tile
+// stored contiguously with one pitch (its leading dimension: rows, or rows
+// rounded up to 4 elements for the 16-byte aligned K1 result), so element e of
+// the tile's pitch x cols run is sum_t alpha_t * src_t[e] over the tile's terms
+// in order, and the elements of the padding rows (e % pitch >= rows) are never
+// stored.  A work item owns CG_CHUNK consecutive elements of one tile; each
+// thread keeps CG_PER accumulators and reads every source through one per-term
+// pointer (cached in shared memory).  Work items whose sources are all 16-byte
+// aligned (DevAxpyChunk.pad = 1) read four elements per load.
 constexpr int CG_THREADS = 256;
 constexpr int CG_PER = 8;
 constexpr int CG_CHUNK = CG_THREADS * CG_PER;
 constexpr int CG_TCACHE = 256;
+
+template <class ACC, class SRC>
+__device__ __forceinline__ void cg_store(const BufTable& bufs, const DevAxpyOut& o, int pitch, int e, int n, ACC v) {
+    if (e >= n) return;
+    const int r = e % pitch, c = e / pitch;
+    if (r >= (int)o.rows) return;
+    const int64_t d = r + (int64_t)c * o.ldd;
+    if (slot_f32(bufs, o.dst_buf)) ((float*)bufs.p[o.dst_buf] + o.dst_off)[d] = (float)v;
+    else (bufs.p[o.dst_buf] + o.dst_off)[d] = (double)v;
+}
 
 template <class ACC, class SRC>
 __global__ void __launch_bounds__(CG_THREADS)
@@ -217,10 +230,13 @@ gather_axpy_contig(BufTable bufs, const DevAxpyOut* __restrict__ outs, const Dev
     const DevAxpyOut o = outs[w.out];
     const int tid = threadIdx.x;
     const int n = w.n;
+    const int pitch = o.pad > 0 ? o.pad : (int)o.rows;
     ACC acc[CG_PER];
 #pragma unroll
     for (int u = 0; u < CG_PER; ++u) acc[u] = ACC(0);
     const int64_t nterm = o.t_end - o.t_begin;
+    // the vector form: thread tid owns elements 4 tid + {0..3} and 4 tid + CG_CHUNK/2 + {0..3}
+    const bool vec = sizeof(SRC) == 4 && w.pad == 1;
     for (int64_t t0 = 0; t0 < nterm; t0 += CG_TCACHE) {
         const int tn = (int)min((int64_t)CG_TCACHE, nterm - t0);
         __syncthreads();
@@ -230,7 +246,41 @@ gather_axpy_contig(BufTable bufs, const DevAxpyOut* __restrict__ outs, const Dev
             s_alpha[tid] = (ACC)tt.alpha;
         }
         __syncthreads();
-        if (n == CG_CHUNK) {
+        if (vec) {
+            // every source is 16-byte aligned and the chunk's n is a multiple of 4 or
+            // ends inside the tile's last column: loads beyond n stay inside the
+            // source allocation (the pitch x cols run), and are not stored
+            const int i0 = 4 * tid, i1 = 4 * tid + CG_CHUNK / 2;
+            const bool in0 = i0 < n, in1 = i1 < n;
+            int t = 0;
+            for (; t + 2 <= tn; t += 2) {
+                const float* p0 = (const float*)s_ptr[t];
+                const float* p1 = (const float*)s_ptr[t + 1];
+                float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0, b0 = a0, b1 = a0;
+                if (in0) { a0 = __ldg((const float4*)(p0 + i0)); b0 = __ldg((const float4*)(p1 + i0)); }
+                if (in1) { a1 = __ldg((const float4*)(p0 + i1)); b1 = __ldg((const float4*)(p1 + i1)); }
+                const ACC x = s_alpha[t], y = s_alpha[t + 1];
+                acc[0] = fma(x, (ACC)a0.x, acc[0]); acc[1] = fma(x, (ACC)a0.y, acc[1]);
+                acc[2] = fma(x, (ACC)a0.z, acc[2]); acc[3] = fma(x, (ACC)a0.w, acc[3]);
+                acc[4] = fma(x, (ACC)a1.x, acc[4]); acc[5] = fma(x, (ACC)a1.y, acc[5]);
+                acc[6] = fma(x, (ACC)a1.z, acc[6]); acc[7] = fma(x, (ACC)a1.w, acc[7]);
+                acc[0] = fma(y, (ACC)b0.x, acc[0]); acc[1] = fma(y, (ACC)b0.y, acc[1]);
+                acc[2] = fma(y, (ACC)b0.z, acc[2]); acc[3] = fma(y, (ACC)b0.w, acc[3]);
+                acc[4] = fma(y, (ACC)b1.x, acc[4]); acc[5] = fma(y, (ACC)b1.y, acc[5]);
+                acc[6] = fma(y, (ACC)b1.z, acc[6]); acc[7] = fma(y, (ACC)b1.w, acc[7]);
+            }
+            if (t < tn) {
+                const float* p0 = (const float*)s_ptr[t];
+                float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0;
+                if (in0) a0 = __ldg((const float4*)(p0 + i0));
+                if (in1) a1 = __ldg((const float4*)(p0 + i1));
+                const ACC x = s_alpha[t];
+                acc[0] = fma(x, (ACC)a0.x, acc[0]); acc[1] = fma(x, (ACC)a0.y, acc[1]);
+                acc[2] = fma(x, (ACC)a0.z, acc[2]); acc[3] = fma(x, (ACC)a0.w, acc[3]);
+                acc[4] = fma(x, (ACC)a1.x, acc[4]); acc[5] = fma(x, (ACC)a1.y, acc[5]);
+                acc[6] = fma(x, (ACC)a1.z, acc[6]); acc[7] = fma(x, (ACC)a1.w, acc[7]);
+            }
+        } else if (n == CG_CHUNK) {
             int t = 0;
             for (; t + 2 <= tn; t += 2) {
                 const SRC* __restrict__ p0 = s_ptr[t] + tid;
@@ -264,25 +314,33 @@ gather_axpy_contig(BufTable bufs, const DevAxpyOut* __restrict__ outs, const Dev
             }
         }
     }
+    if (vec) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            cg_store<ACC, SRC>(bufs, o, pitch, w.e0 + 4 * tid + q, w.e0 + n, acc[q]);
+            cg_store<ACC, SRC>(bufs, o, pitch, w.e0 + 4 * tid + CG_CHUNK / 2 + q, w.e0 + n, acc[4 + q]);
+        }
+        return;
+    }
     const bool dst32 = slot_f32(bufs, o.dst_buf);
-    // element e of the tile sits at row e % rows, column e / rows: one division
+    // element e of the run sits at row e % pitch, column e / pitch: one division
     // for the first element, then steps of CG_THREADS elements with a carry
     const int rows = (int)o.rows;
     const int e_first = w.e0 + tid;
-    int rr = e_first % rows, cc = e_first / rows;
-    const int dr = CG_THREADS % rows, dc = CG_THREADS / rows;
+    int rr = e_first % pitch, cc = e_first / pitch;
+    const int dr = CG_THREADS % pitch, dc = CG_THREADS / pitch;
     float* __restrict__ D32 = (float*)bufs.p[o.dst_buf] + o.dst_off;
     double* __restrict__ D64 = bufs.p[o.dst_buf] + o.dst_off;
 #pragma unroll
     for (int u = 0; u < CG_PER; ++u) {
-        if (tid + u * CG_THREADS < n) {
+        if (tid + u * CG_THREADS < n && rr < rows) {
             const int64_t d = rr + (int64_t)cc * o.ldd;
             if (dst32) D32[d] = (float)acc[u];
             else D64[d] = (double)acc[u];
         }
         rr += dr;
         cc += dc;
-        if (rr >= rows) { rr -= rows; ++cc; }
+        if (rr >= pitch) { rr -= pitch; ++cc; }
     }
 }
 
@@ -352,11 +410,18 @@ __global__ void dot_reduce_kernel(const int64_t* __restrict__ ptr, const int64_t
 
 static bool build_chunk_work(const Stage& st, std::vector<DevAxpyChunk>& w) {
     const size_t nO = st.aout.size();
+    std::vector<int64_t> pitch(nO), nel(nO);
+    std::vector<int32_t> vec(nO, 0);
     for (size_t i = 0; i < nO; ++i) {
         const AxpyOut& a = st.aout[i];
-        if (a.rows * a.cols > 0x7fffffffLL || a.rows <= 0) return false;
-        for (int64_t t = a.t_begin; t < a.t_end; ++t)
-            if (st.aterm[t].lds != a.rows && a.cols > 1) return false;
+        pitch[i] = tile_pitch(st, a);
+        if (pitch[i] < 0 || a.rows <= 0 || pitch[i] * a.cols > 0x7fffffffLL) return false;
+        nel[i] = pitch[i] * (a.cols - 1) + a.rows;
+        // four elements per load when every source of the tile starts 16-byte aligned and
+        // four consecutive elements never straddle two columns
+        bool v = a.cols == 1 || pitch[i] % 4 == 0;
+        for (int64_t t = a.t_begin; t < a.t_end && v; ++t) v = st.aterm[t].src_off % 4 == 0;
+        vec[i] = v ? 1 : 0;
     }
     std::vector<int32_t> rootv;
     const std::vector<int32_t>* roots = &st.comp_root;
@@ -374,16 +439,15 @@ static bool build_chunk_work(const Stage& st, std::vector<DevAxpyChunk>& w) {
         size_t g1 = g0;
         int64_t maxc = 0;
         while (g1 < nO && root[order[g1]] == root[order[g0]]) {
-            const AxpyOut& a = st.aout[order[g1]];
-            maxc = std::max<int64_t>(maxc, (a.rows * a.cols + CG_CHUNK - 1) / CG_CHUNK);
+            maxc = std::max<int64_t>(maxc, (nel[order[g1]] + CG_CHUNK - 1) / CG_CHUNK);
             ++g1;
         }
         for (int64_t c = 0; c < maxc; ++c)
             for (size_t k = g0; k < g1; ++k) {
-                const AxpyOut& a = st.aout[order[k]];
-                const int64_t nel = a.rows * a.cols;
-                if (c * CG_CHUNK < nel)
-                    w.push_back({order[k], (int32_t)(c * CG_CHUNK), (int32_t)std::min<int64_t>(CG_CHUNK, nel - c * CG_CHUNK), 0});
+                const int64_t ne = nel[order[k]];
+                if (c * CG_CHUNK < ne)
+                    w.push_back({order[k], (int32_t)(c * CG_CHUNK), (int32_t)std::min<int64_t>(CG_CHUNK, ne - c * CG_CHUNK),
+                                 vec[order[k]]});
             }
         g0 = g1;
     }
@@ -536,7 +600,8 @@ static int upload_stage(Stage& st) {
         std::vector<DevAxpyWork> w;
         for (size_t i = 0; i < st.aout.size(); ++i) {
             const AxpyOut& a = st.aout[i];
-            o[i] = {a.dst_off, a.ldd, a.rows, a.cols, a.t_begin, a.t_end, a.dst_buf, 0};
+            const int64_t pt = tile_pitch(st, a);
+            o[i] = {a.dst_off, a.ldd, a.rows, a.cols, a.t_begin, a.t_end, a.dst_buf, (int32_t)(pt > 0 ? pt : 0)};
             // column chunks of at most ~8192 elements per work item
             int64_t cc = std::max<int64_t>(1, 8192 / std::max<int64_t>(1, a.rows));
             for (int64_t c0 = 0; c0 < a.cols; c0 += cc) w.push_back({(int64_t)i, c0, std::min(a.cols, c0 + cc)});

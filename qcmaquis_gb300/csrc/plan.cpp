@@ -36,6 +36,8 @@ namespace qcm {
 // benchmark size, because contiguous per-CTA tile ranges lose the L2 reuse of
 // the B operand across CTAs that the strided order has.
 static constexpr bool kAResident = false;
+// column alignment (elements) of the K1 result T in the sigma and boundary plans
+static constexpr int64_t kTAlign = 4;
 
 static thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
@@ -148,6 +150,17 @@ int64_t BM::assign_offsets(int64_t base) {
         check_block_extent(x);
         x.off = base;
         base += x.rows * x.cols;
+    }
+    return base;
+}
+
+int64_t BM::assign_offsets_aligned(int64_t base, int64_t align) {
+    if (align <= 1) return assign_offsets(base);
+    for (auto& x : b) {
+        check_block_extent(x);
+        x.ld = (x.rows + align - 1) / align * align;
+        x.off = (base + align - 1) / align * align;
+        base = x.off + x.ld * x.cols;
     }
     return base;
 }
@@ -407,9 +420,12 @@ static BM plan_reshape_l2r(const Idx& phys, const Idx& left_i, const Idx& right_
 // phases = false: the Hermitian partner L[conj(b1)] is used without the SU(2)
 // conjugate correction and bond phase (BoundaryMPSProduct with
 // correctConjugate = false, as the zero-site problem builds it).
+// align > 1: T's blocks get 16-byte aligned columns (leading dimension and offset
+// rounded up to align elements), so the K2 gather reads every source stripe with
+// aligned vector loads; the padding rows are never read into a result.
 static std::vector<BM> plan_k1(const std::vector<BM>& L, const MpoV& W, bool herm, const BM& rp, int rp_buf,
                                const Idx& ref, int t_buf, Stage& st, qcm_plan* P, int64_t& end,
-                               bool phases = true) {
+                               bool phases = true, int64_t align = 1) {
     std::vector<BM> T(L.size());
     struct Job { int b1; Q a, l; int64_t a_off, lda; int ta; double scale; int64_t M, K; size_t rpk; };
     std::vector<Job> jobs;
@@ -446,7 +462,7 @@ static std::vector<BM> plan_k1(const std::vector<BM>& L, const MpoV& W, bool her
         }
     }
     int64_t base = 0;
-    for (auto& t : T) base = t.assign_offsets(base);
+    for (auto& t : T) base = t.assign_offsets_aligned(base, align);
     end = base;
     st.kind = ST_GEMM;
     for (auto& j : jobs) {
@@ -455,7 +471,8 @@ static std::vector<BM> plan_k1(const std::vector<BM>& L, const MpoV& W, bool her
         GemmOut o;
         o.c_buf = t_buf;
         o.c_off = c.off;
-        o.ldc = c.rows;
+        o.ldc = c.pitch();
+        o.vec_store = align >= 4 && c.off % 4 == 0 && c.pitch() % 4 == 0 ? 1 : 0;
         o.M = c.rows;
         o.N = c.cols;
         o.s_begin = (int64_t)st.gseg.size();
@@ -497,7 +514,7 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
     // afterwards.  key = position of out_l in out_left_i (16 bits), of out_r in
     // right_i (16 bits), row offset (32 bits): ascending keys are the reference's
     // block order (both indices descend) with row offsets ascending.
-    struct KeyedTerm { uint64_t key; int64_t src_off; double alpha; int32_t rows, cols, tt; };
+    struct KeyedTerm { uint64_t key; int64_t src_off; double alpha; int32_t rows, cols, tt, lds; };
     if (out_left_i.size() >= (1u << 16) || right_i.size() >= (1u << 16))
         throw std::runtime_error("too many sectors for the K2 planner");
     for (int b2 : b2list)
@@ -532,6 +549,7 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
                 for (auto& tb : T[b1].b) {
                     Q lc = tb.lc, rc = tb.rc, mc = tb.rc;
                     int64_t l_size = tb.rows;
+                    const int64_t ldt = tb.pitch();
                     for (int wb = m->op_blk_ptr[op]; wb < m->op_blk_ptr[op + 1]; ++wb) {
                         Q pin(m->blk_q[4 * wb], m->blk_q[4 * wb + 1]), pout(m->blk_q[4 * wb + 2], m->blk_q[4 * wb + 3]);
                         Q out_r = fuse(rc, pin);
@@ -555,8 +573,8 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
                             if (alfa == 0.0) continue;
                             const uint64_t key = ((uint64_t)pl << 48) | ((uint64_t)rb << 32) |
                                                  (uint64_t)(uint32_t)(olo + ss2 * l_size);
-                            out.terms.push_back({key, tb.off + (iro + (int64_t)ss1 * r_size) * l_size, alfa,
-                                                 (int32_t)l_size, (int32_t)r_size, tt});
+                            out.terms.push_back({key, tb.off + (iro + (int64_t)ss1 * r_size) * ldt, alfa,
+                                                 (int32_t)l_size, (int32_t)r_size, tt, (int32_t)ldt});
                             out.flops += 2.0 * l_size * r_size;
                         }
                     }
@@ -700,7 +718,7 @@ static std::vector<BM> plan_k2(const std::vector<BM>& T, const MpoV& W, const st
             for (size_t k = a; k < b; ++k) {
                 const KeyedTerm& x = *ov[k];
                 if (prov) (*prov)[ti] = {x.tt, x.alpha / m->term_scale[x.tt]};
-                st.aterm[ti++] = {t_buf, x.src_off, x.rows, x.alpha};
+                st.aterm[ti++] = {t_buf, x.src_off, x.lds, x.alpha};
             }
             o.t_end = (int64_t)ti;
             bytes[i] += 8.0 * o.rows * o.cols * (double)(b - a + 1);
@@ -854,7 +872,7 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
     Idx ref;
     for (auto& b : rp.b) ref.d.push_back({b.lc, b.rows});
     Stage s1; int64_t t_end = 0;
-    std::vector<BM> T = plan_k1(L, W, herm, rp, QCM_BUF_S0, ref, QCM_BUF_S1, s1, P, t_end);
+    std::vector<BM> T = plan_k1(L, W, herm, rp, QCM_BUF_S0, ref, QCM_BUF_S1, s1, P, t_end, true, kTAlign);
     std::vector<int> b2list;
     for (int b2 = 0; b2 < m->col_dim; ++b2) b2list.push_back(b2);
     Stage s2; int64_t c_end = 0;
@@ -1286,7 +1304,7 @@ static qcm_plan* build_bleft(const Idx& phys, const Idx& left_i, const Idx& righ
     if (tensor_mpo) ref = left_i;
     else for (auto& b : rp.b) ref.d.push_back({b.lc, b.rows});
     Stage s1; int64_t t_end = 0;
-    std::vector<BM> T = plan_k1(L, W, herm, rp, QCM_BUF_S0, ref, QCM_BUF_S1, s1, P, t_end);
+    std::vector<BM> T = plan_k1(L, W, herm, rp, QCM_BUF_S0, ref, QCM_BUF_S1, s1, P, t_end, true, kTAlign);
     std::vector<int> b2list;
     for (int b2 = 0; b2 < m->col_dim; ++b2)
         if (tensor_mpo || !(herm && W.rskip(b2))) b2list.push_back(b2);
@@ -1708,7 +1726,8 @@ void build_image_tables(const Stage& st, ImgTables& t) {
         io.ctab = 0;
         io.mode = 0;
         io.rows = 0;
-        io.pad = 0;
+        // transposed tiles of a padded output store 4 contiguous rows per vector
+        io.pad = tr && o.vec_store ? 1 : 0;
         const int32_t oid = (int32_t)t.outs.size();
         t.outs.push_back(io);
         const int32_t s_begin = (int32_t)t.segs.size();
@@ -1786,6 +1805,15 @@ static float bf16_to_float(uint16_t h) {
     return x;
 }
 
+int64_t tile_pitch(const Stage& st, const AxpyOut& a) {
+    if (a.t_end == a.t_begin || a.cols <= 1) return a.rows;
+    const int64_t p = st.aterm[a.t_begin].lds;
+    if (p < a.rows || p > (a.rows + 3) / 4 * 4) return -1;
+    for (int64_t t = a.t_begin; t < a.t_end; ++t)
+        if (st.aterm[t].lds != p) return -1;
+    return p;
+}
+
 bool axpy_components(const Stage& st, std::vector<int32_t>& root) {
     const size_t nO = st.aout.size();
     const unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -1798,9 +1826,7 @@ bool axpy_components(const Stage& st, std::vector<int32_t>& root) {
     std::atomic<bool> contiguous{true};
     run([&](unsigned t) {
         for (size_t i = t; i < nO && contiguous.load(std::memory_order_relaxed); i += nt) {
-            const AxpyOut& a = st.aout[i];
-            for (int64_t k = a.t_begin; k < a.t_end; ++k)
-                if (st.aterm[k].lds != a.rows && a.cols > 1) { contiguous = false; break; }
+            if (tile_pitch(st, st.aout[i]) < 0) { contiguous = false; break; }
         }
     });
     if (!contiguous) return false;
@@ -1908,8 +1934,9 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         roots = &rootv;
     }
     auto find = [&](int32_t x) { return (*roots)[x]; };
-    // candidate groups: (component, rows, cols, dst_buf, src_buf) over heavy outputs
-    std::map<std::tuple<int32_t, int64_t, int64_t, int32_t, int32_t>, std::vector<int32_t>> groups;
+    // candidate groups: (component, rows, cols, dst_buf, src_buf, pitch) over heavy outputs;
+    // a tile is its sources' pitch x cols run, of which the rows < rows are stored
+    std::map<std::tuple<int32_t, int64_t, int64_t, int32_t, int32_t, int64_t>, std::vector<int32_t>> groups;
     for (size_t i = 0; i < nO; ++i) {
         const AxpyOut& a = st.aout[i];
         if (a.t_end - a.t_begin < min_terms || a.rows * a.cols <= 0) continue;
@@ -1918,7 +1945,9 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         for (int64_t k = a.t_begin; k < a.t_end; ++k) uniform &= st.aterm[k].src_buf == sb;
         if (!uniform) continue;
         if (a.ldd > 0x7fffffffLL) continue;
-        groups[std::make_tuple(find((int32_t)i), a.rows, a.cols, a.dst_buf, sb)].push_back((int32_t)i);
+        const int64_t pitch = tile_pitch(st, a);
+        if (pitch < 0) continue;
+        groups[std::make_tuple(find((int32_t)i), a.rows, a.cols, a.dst_buf, sb, pitch)].push_back((int32_t)i);
     }
     // per group (in parallel): its source list and the BF16 slices of its
     // coefficient matrix; then (in group order) the tables are appended
@@ -1929,13 +1958,14 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         int64_t S = 0, KC = 0;
         int32_t G = 0, Gb = 0;
     };
-    std::vector<const std::pair<const std::tuple<int32_t, int64_t, int64_t, int32_t, int32_t>, std::vector<int32_t>>*> glist;
+    std::vector<const std::pair<const std::tuple<int32_t, int64_t, int64_t, int32_t, int32_t, int64_t>,
+                                std::vector<int32_t>>*> glist;
     for (auto& kv : groups) glist.push_back(&kv);
     std::vector<Prep> prep(glist.size());
     auto prepare = [&](size_t gi) {
         const std::vector<int32_t>& O = glist[gi]->second;
-        const int64_t rows = std::get<1>(glist[gi]->first), cols = std::get<2>(glist[gi]->first);
-        const int64_t E = rows * cols;
+        const int64_t cols = std::get<2>(glist[gi]->first), pitch = std::get<5>(glist[gi]->first);
+        const int64_t E = pitch * cols;
         if (E > 0x7fffffffLL || O.size() < 8) return;
         Prep& pr = prep[gi];
         std::unordered_map<int64_t, int32_t> sid;
@@ -2018,7 +2048,8 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         const std::vector<int32_t>& O = glist[gi]->second;
         const int64_t rows = std::get<1>(glist[gi]->first), cols = std::get<2>(glist[gi]->first);
         const int32_t dst_buf = std::get<3>(glist[gi]->first), src_buf = std::get<4>(glist[gi]->first);
-        const int64_t E = rows * cols;
+        const int64_t pitch = std::get<5>(glist[gi]->first);
+        const int64_t E = pitch * cols;
         Prep& pr = prep[gi];
         const int64_t KC = pr.KC;
         const int32_t G = pr.G, Gb = pr.Gb;
@@ -2049,8 +2080,8 @@ void build_dense_groups(const Stage& st, int64_t min_terms, ImgTables& t, std::v
         io.mrows = (int32_t)E;
         io.ncols = (int32_t)O.size();
         io.mode = 1;
-        io.rows = (int32_t)rows;
-        io.pad = 0;
+        io.rows = (int32_t)pitch;
+        io.pad = pitch != rows ? (int32_t)rows : 0;   // rows stored of each pitch (0: all)
         for (int32_t o : O) {
             t.coltab.push_back(st.aout[o].dst_off);
             t.coltab.push_back(st.aout[o].ldd);
@@ -2232,7 +2263,8 @@ static qcm_plan* merge_sigma_plans(qcm_plan* const* plans, int32_t n, const int6
         for (int q = 0; q < 4; ++q) base[k][q] = caller_off[4 * k + q];
         for (int q = 0; q < 3; ++q) {
             base[k][QCM_BUF_S0 + q] = sc[q];
-            sc[q] += plans[k]->scratch[q];
+            // problems' scratch slices start 32-byte aligned (aligned vector loads of T)
+            sc[q] += (plans[k]->scratch[q] + 3) / 4 * 4;
         }
         P->out_elems = std::max(P->out_elems, base[k][QCM_BUF_OUT] + plans[k]->out_elems);
         P->gemm_flops += plans[k]->gemm_flops;
@@ -2432,8 +2464,8 @@ int qcm_plan_stage_images(const qcm_plan* p, int32_t stage, int64_t* counts, int
     if (od)
         for (size_t i = 0; i < t.outs.size(); ++i) {
             const ImgOut& x = t.outs[i];
-            const int64_t v[9] = {x.c_off, x.si, x.sj, x.c_buf, x.mrows, x.ncols, x.mode, x.rows, x.ctab};
-            for (int j = 0; j < 9; ++j) od[9 * i + j] = v[j];
+            const int64_t v[10] = {x.c_off, x.si, x.sj, x.c_buf, x.mrows, x.ncols, x.mode, x.rows, x.ctab, x.pad};
+            for (int j = 0; j < 10; ++j) od[10 * i + j] = v[j];
         }
     if (sd)
         for (size_t i = 0; i < t.segs.size(); ++i) {

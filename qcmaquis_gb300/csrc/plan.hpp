@@ -58,6 +58,8 @@ struct PB {
 struct Blk {
     Q lc, rc;
     int64_t rows = 0, cols = 0, off = 0;
+    int64_t ld = 0;   // leading dimension when padded (0: rows)
+    int64_t pitch() const { return ld ? ld : rows; }
 };
 
 // Block list in DualIndex order (descending on (lc, rc)).
@@ -67,6 +69,9 @@ struct BM {
     size_t left_lower_bound(Q lc) const;
     size_t insert(Blk x);  // returns position
     int64_t assign_offsets(int64_t base);  // sequential offsets, returns end
+    // offsets and leading dimensions rounded up to multiples of align elements
+    // (16-byte aligned columns for align = 4 FP32 elements); returns end
+    int64_t assign_offsets_aligned(int64_t base, int64_t align);
 };
 
 // Allocator that default-initialises (no zero fill when a table of PODs is resized
@@ -94,6 +99,10 @@ struct GemmOut {
     int32_t c_buf;
     int64_t c_off, ldc, M, N;
     int64_t s_begin, s_end;
+    // 1: the output's columns are 16-byte aligned and padded to a multiple of 4
+    // rows that nothing reads into a result (the K1 result T), so a store may
+    // write whole groups of 4 rows
+    int32_t vec_store = 0;
 };
 struct GemmSeg {
     int32_t a_buf, ta;
@@ -172,6 +181,10 @@ void build_dense_groups(const struct Stage& st, int64_t min_terms, ImgTables& t,
 // that share a source tile, transitively): root[i] = smallest output of i's
 // component.  Returns false when some term's source is not a contiguous tile.
 bool axpy_components(const struct Stage& st, std::vector<int32_t>& root);
+// The pitch of a gather output tile whose sources share one leading dimension
+// between rows and rows rounded up to 4 (the padded K1 result): the tile is then
+// a contiguous pitch x cols run of each source; -1 for other strided sources.
+int64_t tile_pitch(const struct Stage& st, const AxpyOut& a);
 
 struct Stage {
     int kind;

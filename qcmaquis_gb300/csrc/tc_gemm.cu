@@ -601,13 +601,15 @@ __device__ __forceinline__ void ti_store16(const TiArgs& a, const ImgOut& O, con
     float* __restrict__ C32 = (float*)a.p[O.c_buf] + O.c_off;
     double* __restrict__ C64 = a.p[O.c_buf] + O.c_off;
     if (O.mode == 1) {
-        // column j is one output tile: element i at (i % rows) + (i / rows)*ld_j of it
+        // column j is one output tile: element i at (i % rows) + (i / rows)*ld_j of it;
+        // with O.pad > 0 the tile is a run of pitch O.rows of which O.pad rows are stored
         const int i = i0 + lane;
         const int64_t ir = i % O.rows, ic = i / O.rows;
+        const bool row_ok = O.pad == 0 || ir < O.pad;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
             const int col = U.n0 + cbase + j;
-            if (i < O.mrows && col < O.ncols) {
+            if (i < O.mrows && col < O.ncols && row_ok) {
                 const int64_t off = __ldg(a.coltab + 2 * (O.ctab + col)) + ir + ic * __ldg(a.coltab + 2 * (O.ctab + col) + 1);
                 if (c32) ((float*)a.p[O.c_buf])[off] = hi[j] + lo[j];
                 else a.p[O.c_buf][off] = (double)hi[j] + (double)lo[j];
@@ -623,6 +625,36 @@ __device__ __forceinline__ void ti_store16(const TiArgs& a, const ImgOut& O, con
                 const int64_t off = (int64_t)i + (int64_t)col * O.sj;
                 if (c32) C32[off] = hi[j] + lo[j];
                 else C64[off] = (double)hi[j] + (double)lo[j];
+            }
+        }
+    } else if (O.pad == 1 && c32) {
+        // as below, for an output whose contiguous direction is padded to a multiple
+        // of 4 elements on 16-byte aligned columns (the K1 result): each lane stores
+        // 4 consecutive elements, 8 row runs per warp store instead of 2; the
+        // elements past ncols land in the padding (they are zero: the operand
+        // images are zero-padded)
+        const uint32_t sbase = smem_u32(stg);
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            asm volatile("st.shared.f32 [%0], %1;" :: "r"(sbase + (uint32_t)((lane * TI_EPI_LD + j) * 4)),
+                         "f"(hi[j] + lo[j]) : "memory");
+        __syncwarp();
+        const int q = lane & 3, r = lane >> 2;
+        const int col = U.n0 + cbase + 4 * q;
+        float vv[4][4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                asm volatile("ld.shared.f32 %0, [%1];" : "=f"(vv[k][e])
+                             : "r"(sbase + (uint32_t)(((r + 8 * k) * TI_EPI_LD + 4 * q + e) * 4)) : "memory");
+        __syncwarp();
+        if (col < (O.ncols + 3) / 4 * 4) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int row = i0 + r + 8 * k;
+                if (row < O.mrows)
+                    *(float4*)(C32 + (int64_t)row * O.si + col) = make_float4(vv[k][0], vv[k][1], vv[k][2], vv[k][3]);
             }
         }
     } else {

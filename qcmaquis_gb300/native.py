@@ -697,7 +697,7 @@ class Plan:
               "qcm_plan_stage_images")
         npn, no, ns, nu = [int(x) for x in cnt]
         pd = np.zeros((max(npn, 1), 8), dtype=np.int64)
-        od = np.zeros((max(no, 1), 9), dtype=np.int64)
+        od = np.zeros((max(no, 1), 10), dtype=np.int64)
         sd = np.zeros((max(ns, 1), 8), dtype=np.int64)
         sa = np.zeros(max(ns, 1))
         td = np.zeros((max(nu, 1), 6), dtype=np.int64)

@@ -151,6 +151,15 @@ def block_davidson(sig: SharedSigma, X0: torch.Tensor, tol: float = 1e-8, maxite
         return len(new)
 
     extend([X0[r] for r in range(k)])
+    # start vectors that span fewer than k directions (the roots' centre tensors at a
+    # chain end have few parameters) are completed with seeded random directions
+    gen = torch.Generator(device=dev).manual_seed(1234)
+    for _ in range(4 * k):
+        if len(V) >= k:
+            break
+        extend([torch.randn(n, dtype=torch.float64, device=dev, generator=gen) for _ in range(k - len(V))])
+    if len(V) < k:
+        raise ValueError(f"the site problem has fewer than {k} dimensions")
     theta = np.zeros(k)
     U = torch.zeros((k, n), dtype=torch.float64, device=dev)
     it = 0

@@ -112,7 +112,7 @@ def run_gemm_images(tab, bufs, image_bytes, nprod=6):
             img[slot(img_off, G, k // 32, s, r, k)] = vals if s == 0 else 0.0
     outs, segs, alpha = tab["outs"], tab["segs"], tab["alpha"]
     for (out, m0, n0, nt, sb, se) in tab["tiles"]:
-        c_off, si, sj, c_buf, mrows, ncols, mode, rows, ctab = [int(x) for x in outs[out]]
+        c_off, si, sj, c_buf, mrows, ncols, mode, rows, ctab, vrows = [int(x) for x in outs[out]]
         assert nt % 16 == 0 and 16 <= nt <= 128 and m0 % 128 == 0 and n0 % 8 == 0
         acc = np.zeros((128, nt))
         for s in range(sb, se):
@@ -136,6 +136,9 @@ def run_gemm_images(tab, bufs, image_bytes, nprod=6):
         i = np.arange(128)[:, None]
         j = np.arange(nt)[None, :]
         valid = (m0 + i < mrows) & (n0 + j < ncols)
+        if mode == 1 and vrows > 0:
+            # a pitch-`rows` run of which the first vrows rows of every column are stored
+            valid &= (m0 + i) % rows < vrows
         assert np.all(np.isfinite(acc[valid]))
         if mode == 0:
             dst = c_off + (m0 + i) * si + (n0 + j) * sj

@@ -74,7 +74,8 @@ def test_gpu_twou1_boundary_steps_match_oracle():
 def test_gpu_twou1_sweep_matches_oracle_and_fci():
     from qcmaquis_gb300 import sweep as G
     from oracle.sweep import SweepParams, run_dmrg
-    L, nu, nd, m = 6, 3, 2, 32
+    # m = 64 holds the whole space (4^3 states at the middle bond): DMRG is exact
+    L, nu, nd, m = 6, 3, 2, 64
     ints = synthetic_integral_map(L, seed=5)
     model = TwoU1Model(L, ints, nu, nd)
     mpo = TaggedMPOMaker(model).create_mpo()
