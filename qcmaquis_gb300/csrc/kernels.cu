@@ -211,16 +211,6 @@ constexpr int CG_CHUNK = CG_THREADS * CG_PER;
 constexpr int CG_TCACHE = 256;
 
 template <class ACC, class SRC>
-__device__ __forceinline__ void cg_store(const BufTable& bufs, const DevAxpyOut& o, int pitch, int e, int n, ACC v) {
-    if (e >= n) return;
-    const int r = e % pitch, c = e / pitch;
-    if (r >= (int)o.rows) return;
-    const int64_t d = r + (int64_t)c * o.ldd;
-    if (slot_f32(bufs, o.dst_buf)) ((float*)bufs.p[o.dst_buf] + o.dst_off)[d] = (float)v;
-    else (bufs.p[o.dst_buf] + o.dst_off)[d] = (double)v;
-}
-
-template <class ACC, class SRC>
 __global__ void __launch_bounds__(CG_THREADS)
 gather_axpy_contig(BufTable bufs, const DevAxpyOut* __restrict__ outs, const DevAxpyTerm* __restrict__ terms,
                    const DevAxpyChunk* __restrict__ work) {
@@ -315,10 +305,26 @@ gather_axpy_contig(BufTable bufs, const DevAxpyOut* __restrict__ outs, const Dev
         }
     }
     if (vec) {
+        // each group of 4 elements lies in one column (pitch and its start are
+        // multiples of 4): one division per group, rows masked at the padding
+        const bool d32 = slot_f32(bufs, o.dst_buf);
+        float* __restrict__ D32 = (float*)bufs.p[o.dst_buf] + o.dst_off;
+        double* __restrict__ D64 = bufs.p[o.dst_buf] + o.dst_off;
+        const int rows = (int)o.rows;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            cg_store<ACC, SRC>(bufs, o, pitch, w.e0 + 4 * tid + q, w.e0 + n, acc[q]);
-            cg_store<ACC, SRC>(bufs, o, pitch, w.e0 + 4 * tid + CG_CHUNK / 2 + q, w.e0 + n, acc[4 + q]);
+        for (int g = 0; g < 2; ++g) {
+            const int i = 4 * tid + g * (CG_CHUNK / 2);
+            if (i >= n) continue;
+            const int e = w.e0 + i;
+            const int r = e % pitch, c = e / pitch;
+            const int64_t d = r + (int64_t)c * o.ldd;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (r + q < rows && i + q < n) {
+                    if (d32) D32[d + q] = (float)acc[4 * g + q];
+                    else D64[d + q] = (double)acc[4 * g + q];
+                }
+            }
         }
         return;
     }
