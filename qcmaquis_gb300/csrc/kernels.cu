@@ -203,8 +203,9 @@ gather_axpy_uniform(BufTable bufs, const DevAxpyOut* __restrict__ outs, const De
 // in order, and the elements of the padding rows (e % pitch >= rows) are never
 // stored.  A work item owns CG_CHUNK consecutive elements of one tile; each
 // thread keeps CG_PER accumulators and reads every source through one per-term
-// pointer (cached in shared memory).  Work items whose sources are all 16-byte
-// aligned (DevAxpyChunk.pad = 1) read four elements per load.
+// pointer (cached in shared memory).  (Four-element vector loads over the
+// 16-byte aligned K1 result were measured slower: 14.2 against 13.2 ms per
+// sigma at the benchmark size.)
 constexpr int CG_THREADS = 256;
 constexpr int CG_PER = 8;
 constexpr int CG_CHUNK = CG_THREADS * CG_PER;
@@ -225,8 +226,6 @@ gather_axpy_contig(BufTable bufs, const DevAxpyOut* __restrict__ outs, const Dev
 #pragma unroll
     for (int u = 0; u < CG_PER; ++u) acc[u] = ACC(0);
     const int64_t nterm = o.t_end - o.t_begin;
-    // the vector form: thread tid owns elements 4 tid + {0..3} and 4 tid + CG_CHUNK/2 + {0..3}
-    const bool vec = sizeof(SRC) == 4 && w.pad == 1;
     for (int64_t t0 = 0; t0 < nterm; t0 += CG_TCACHE) {
         const int tn = (int)min((int64_t)CG_TCACHE, nterm - t0);
         __syncthreads();
@@ -236,41 +235,7 @@ gather_axpy_contig(BufTable bufs, const DevAxpyOut* __restrict__ outs, const Dev
             s_alpha[tid] = (ACC)tt.alpha;
         }
         __syncthreads();
-        if (vec) {
-            // every source is 16-byte aligned and the chunk's n is a multiple of 4 or
-            // ends inside the tile's last column: loads beyond n stay inside the
-            // source allocation (the pitch x cols run), and are not stored
-            const int i0 = 4 * tid, i1 = 4 * tid + CG_CHUNK / 2;
-            const bool in0 = i0 < n, in1 = i1 < n;
-            int t = 0;
-            for (; t + 2 <= tn; t += 2) {
-                const float* p0 = (const float*)s_ptr[t];
-                const float* p1 = (const float*)s_ptr[t + 1];
-                float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0, b0 = a0, b1 = a0;
-                if (in0) { a0 = __ldg((const float4*)(p0 + i0)); b0 = __ldg((const float4*)(p1 + i0)); }
-                if (in1) { a1 = __ldg((const float4*)(p0 + i1)); b1 = __ldg((const float4*)(p1 + i1)); }
-                const ACC x = s_alpha[t], y = s_alpha[t + 1];
-                acc[0] = fma(x, (ACC)a0.x, acc[0]); acc[1] = fma(x, (ACC)a0.y, acc[1]);
-                acc[2] = fma(x, (ACC)a0.z, acc[2]); acc[3] = fma(x, (ACC)a0.w, acc[3]);
-                acc[4] = fma(x, (ACC)a1.x, acc[4]); acc[5] = fma(x, (ACC)a1.y, acc[5]);
-                acc[6] = fma(x, (ACC)a1.z, acc[6]); acc[7] = fma(x, (ACC)a1.w, acc[7]);
-                acc[0] = fma(y, (ACC)b0.x, acc[0]); acc[1] = fma(y, (ACC)b0.y, acc[1]);
-                acc[2] = fma(y, (ACC)b0.z, acc[2]); acc[3] = fma(y, (ACC)b0.w, acc[3]);
-                acc[4] = fma(y, (ACC)b1.x, acc[4]); acc[5] = fma(y, (ACC)b1.y, acc[5]);
-                acc[6] = fma(y, (ACC)b1.z, acc[6]); acc[7] = fma(y, (ACC)b1.w, acc[7]);
-            }
-            if (t < tn) {
-                const float* p0 = (const float*)s_ptr[t];
-                float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0;
-                if (in0) a0 = __ldg((const float4*)(p0 + i0));
-                if (in1) a1 = __ldg((const float4*)(p0 + i1));
-                const ACC x = s_alpha[t];
-                acc[0] = fma(x, (ACC)a0.x, acc[0]); acc[1] = fma(x, (ACC)a0.y, acc[1]);
-                acc[2] = fma(x, (ACC)a0.z, acc[2]); acc[3] = fma(x, (ACC)a0.w, acc[3]);
-                acc[4] = fma(x, (ACC)a1.x, acc[4]); acc[5] = fma(x, (ACC)a1.y, acc[5]);
-                acc[6] = fma(x, (ACC)a1.z, acc[6]); acc[7] = fma(x, (ACC)a1.w, acc[7]);
-            }
-        } else if (n == CG_CHUNK) {
+        if (n == CG_CHUNK) {
             int t = 0;
             for (; t + 2 <= tn; t += 2) {
                 const SRC* __restrict__ p0 = s_ptr[t] + tid;
@@ -303,30 +268,6 @@ gather_axpy_contig(BufTable bufs, const DevAxpyOut* __restrict__ outs, const Dev
                     if (tid + u * CG_THREADS < n) acc[u] = fma(a0, (ACC)__ldg(p0 + u * CG_THREADS), acc[u]);
             }
         }
-    }
-    if (vec) {
-        // each group of 4 elements lies in one column (pitch and its start are
-        // multiples of 4): one division per group, rows masked at the padding
-        const bool d32 = slot_f32(bufs, o.dst_buf);
-        float* __restrict__ D32 = (float*)bufs.p[o.dst_buf] + o.dst_off;
-        double* __restrict__ D64 = bufs.p[o.dst_buf] + o.dst_off;
-        const int rows = (int)o.rows;
-#pragma unroll
-        for (int g = 0; g < 2; ++g) {
-            const int i = 4 * tid + g * (CG_CHUNK / 2);
-            if (i >= n) continue;
-            const int e = w.e0 + i;
-            const int r = e % pitch, c = e / pitch;
-            const int64_t d = r + (int64_t)c * o.ldd;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                if (r + q < rows && i + q < n) {
-                    if (d32) D32[d + q] = (float)acc[4 * g + q];
-                    else D64[d + q] = (double)acc[4 * g + q];
-                }
-            }
-        }
-        return;
     }
     const bool dst32 = slot_f32(bufs, o.dst_buf);
     // element e of the run sits at row e % pitch, column e / pitch: one division
@@ -417,17 +358,11 @@ __global__ void dot_reduce_kernel(const int64_t* __restrict__ ptr, const int64_t
 static bool build_chunk_work(const Stage& st, std::vector<DevAxpyChunk>& w) {
     const size_t nO = st.aout.size();
     std::vector<int64_t> pitch(nO), nel(nO);
-    std::vector<int32_t> vec(nO, 0);
     for (size_t i = 0; i < nO; ++i) {
         const AxpyOut& a = st.aout[i];
         pitch[i] = tile_pitch(st, a);
         if (pitch[i] < 0 || a.rows <= 0 || pitch[i] * a.cols > 0x7fffffffLL) return false;
         nel[i] = pitch[i] * (a.cols - 1) + a.rows;
-        // four elements per load when every source of the tile starts 16-byte aligned and
-        // four consecutive elements never straddle two columns
-        bool v = a.cols == 1 || pitch[i] % 4 == 0;
-        for (int64_t t = a.t_begin; t < a.t_end && v; ++t) v = st.aterm[t].src_off % 4 == 0;
-        vec[i] = v ? 1 : 0;
     }
     std::vector<int32_t> rootv;
     const std::vector<int32_t>* roots = &st.comp_root;
@@ -452,8 +387,7 @@ static bool build_chunk_work(const Stage& st, std::vector<DevAxpyChunk>& w) {
             for (size_t k = g0; k < g1; ++k) {
                 const int64_t ne = nel[order[k]];
                 if (c * CG_CHUNK < ne)
-                    w.push_back({order[k], (int32_t)(c * CG_CHUNK), (int32_t)std::min<int64_t>(CG_CHUNK, ne - c * CG_CHUNK),
-                                 vec[order[k]]});
+                    w.push_back({order[k], (int32_t)(c * CG_CHUNK), (int32_t)std::min<int64_t>(CG_CHUNK, ne - c * CG_CHUNK), 0});
             }
         g0 = g1;
     }

@@ -37,6 +37,7 @@ namespace qcm {
 // the B operand across CTAs that the strided order has.
 static constexpr bool kAResident = false;
 // column alignment (elements) of the K1 result T in the sigma and boundary plans
+// (16 bytes in FP32: vector stores in the image epilogue)
 static constexpr int64_t kTAlign = 4;
 
 static thread_local std::string g_err;
@@ -158,7 +159,9 @@ int64_t BM::assign_offsets_aligned(int64_t base, int64_t align) {
     if (align <= 1) return assign_offsets(base);
     for (auto& x : b) {
         check_block_extent(x);
-        x.ld = (x.rows + align - 1) / align * align;
+        // columns of fewer than 32 rows stay unpadded: their padding would be a large
+        // share of the tile, and the gather's short tiles read contiguous runs anyway
+        x.ld = x.rows < 32 ? x.rows : (x.rows + align - 1) / align * align;
         x.off = (base + align - 1) / align * align;
         base = x.off + x.ld * x.cols;
     }
@@ -420,9 +423,11 @@ static BM plan_reshape_l2r(const Idx& phys, const Idx& left_i, const Idx& right_
 // phases = false: the Hermitian partner L[conj(b1)] is used without the SU(2)
 // conjugate correction and bond phase (BoundaryMPSProduct with
 // correctConjugate = false, as the zero-site problem builds it).
-// align > 1: T's blocks get 16-byte aligned columns (leading dimension and offset
-// rounded up to align elements), so the K2 gather reads every source stripe with
-// aligned vector loads; the padding rows are never read into a result.
+// align > 1: T's blocks get 16-byte aligned columns (offset and, for blocks of 32
+// rows or more, leading dimension rounded up to align elements), so that the
+// image epilogue stores T four rows at a time; the padding rows are never read
+// into a result (the gather treats a padded source as a pitch x cols run and
+// stores only the tile's rows).
 static std::vector<BM> plan_k1(const std::vector<BM>& L, const MpoV& W, bool herm, const BM& rp, int rp_buf,
                                const Idx& ref, int t_buf, Stage& st, qcm_plan* P, int64_t& end,
                                bool phases = true, int64_t align = 1) {

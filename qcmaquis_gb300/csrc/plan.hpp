@@ -69,8 +69,9 @@ struct BM {
     size_t left_lower_bound(Q lc) const;
     size_t insert(Blk x);  // returns position
     int64_t assign_offsets(int64_t base);  // sequential offsets, returns end
-    // offsets and leading dimensions rounded up to multiples of align elements
-    // (16-byte aligned columns for align = 4 FP32 elements); returns end
+    // offsets rounded up to multiples of align elements and, for blocks of at least
+    // 32 rows, leading dimensions too (16-byte aligned columns for align = 4 FP32
+    // elements); returns end
     int64_t assign_offsets_aligned(int64_t base, int64_t align);
 };
 
