@@ -569,9 +569,13 @@ static int upload_stage(Stage& st) {
                 if (!lw.empty() && (rc = upload_vec(lw, &st.d_cw_light))) return rc;
                 st.n_cw_light = (int64_t)lw.size();
                 if ((rc = upload_images(st))) return rc;
+                // the dense groups' stream has the highest priority: whenever an SM frees
+                // up, their CTAs are placed before more gather CTAs, so the two overlap
                 cudaStream_t ss;
                 cudaEvent_t e0, e1;
-                QCM_CUDA(cudaStreamCreateWithFlags(&ss, cudaStreamNonBlocking));
+                int least = 0, greatest = 0;
+                QCM_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+                QCM_CUDA(cudaStreamCreateWithPriority(&ss, cudaStreamNonBlocking, greatest));
                 st.side_stream = ss;
                 QCM_CUDA(cudaEventCreateWithFlags(&e0, cudaEventDisableTiming));
                 st.ev_fork = e0;
@@ -626,27 +630,29 @@ static int launch_axpy(const Stage& st, const BufTable& bt, int precision, cudaS
         const auto* CW = (const DevAxpyChunk*)st.d_cw;
         unsigned gc = (unsigned)st.n_cw;
         if (img_form(precision) && bt.p[QCM_BUF_IMG] && st.d_iunit) {
-            // BF16x3 / BF16x2 with images: the dense groups on the tensor cores (on the caller's
-            // stream) and the gather of the other outputs on the stage's side stream,
-            // forked from and joined back into the caller's stream (disjoint outputs)
+            // BF16x3 / BF16x2 with images: the dense groups on the tensor cores on the stage's
+            // high-priority side stream, and the gather of the other outputs on the caller's
+            // stream, the side stream forked from and joined back into it (disjoint outputs)
             cudaStream_t ss = (cudaStream_t)st.side_stream;
             const bool fork = ss && st.n_cw_light > 0;
             if (fork) {
                 QCM_CUDA(cudaEventRecord((cudaEvent_t)st.ev_fork, s));
                 QCM_CUDA(cudaStreamWaitEvent(ss, (cudaEvent_t)st.ev_fork, 0));
+                const int rc = tc_img_launch(st, bt.p, bt.f32mask, (void*)ss, img_products(precision));
                 const auto* LW = (const DevAxpyChunk*)st.d_cw_light;
                 const unsigned gl = (unsigned)st.n_cw_light;
-                if (src32) gather_axpy_contig<float, float><<<gl, CG_THREADS, 0, ss>>>(bt, O, T, LW);
-                else gather_axpy_contig<float, double><<<gl, CG_THREADS, 0, ss>>>(bt, O, T, LW);
-                QCM_CUDA(cudaGetLastError());
-            }
-            int rc = tc_img_launch(st, bt.p, bt.f32mask, (void*)s, img_products(precision));
-            if (fork) {
+                if (src32) gather_axpy_contig<float, float><<<gl, CG_THREADS, 0, s>>>(bt, O, T, LW);
+                else gather_axpy_contig<float, double><<<gl, CG_THREADS, 0, s>>>(bt, O, T, LW);
+                const cudaError_t le = cudaGetLastError();
+                // join even after a failed launch, so that no work is left forked
                 QCM_CUDA(cudaEventRecord((cudaEvent_t)st.ev_join, ss));
                 QCM_CUDA(cudaStreamWaitEvent(s, (cudaEvent_t)st.ev_join, 0));
+                if (rc) return rc;
+                if (le != cudaSuccess) { set_error(std::string("gather launch: ") + cudaGetErrorString(le)); return QCM_E_CUDA; }
+                return QCM_OK;
             }
+            int rc = tc_img_launch(st, bt.p, bt.f32mask, (void*)s, img_products(precision));
             if (rc) return rc;
-            if (fork) return QCM_OK;
             CW = (const DevAxpyChunk*)st.d_cw_light;
             gc = (unsigned)st.n_cw_light;
             if (gc == 0) return QCM_OK;
