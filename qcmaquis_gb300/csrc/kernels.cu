@@ -41,7 +41,7 @@ struct DevAxpyWork { int64_t out, c0, c1; };
 struct DevAxpyChunk { int32_t out, e0, n, pad; };
 struct DevGemmOut { int64_t c_off, ldc, M, N, s_begin, s_end; int32_t c_buf, pad; };
 struct DevGemmSeg { int64_t a_off, lda, b_off, ldb, K; double alpha; int32_t a_buf, ta, b_buf, tb; };
-struct DevGemmWork { int64_t out, m0, n0; };
+struct DevGemmWork { int64_t out, m0, n0; int32_t tm, tn; };   // tile extents: tm % 16 == 0, tn % 32 == 0
 
 // Buffer table of one plan run.  Bit i of f32mask marks slot i as FP32 (the
 // mixed-precision forms keep boundary shadows and all intermediates in FP32);
@@ -396,15 +396,26 @@ static bool build_chunk_work(const Stage& st, std::vector<DevAxpyChunk>& w) {
 
 // ------------------------------------------------------------------ FP64 grouped GEMM
 constexpr int GT_M = 64, GT_N = 64, GT_K = 16;
+constexpr int GT_LD = GT_M + 2;   // shared row stride: even (16-byte aligned two-double reads)
 
+// One tile of a grouped FP64 product per CTA, of extent tm x tn (tm a multiple of
+// 16, tn of 32, both at most 64: a block's last tiles are cut to its size, so
+// that little of the FP64 work is spent on padding -- GB300's FP64 rate bounds
+// this form).  Warp w owns the 16 x 32 sub-tile (16 (w & 3), 32 (w >> 2)) and
+// sits out the products when that lies outside the tile; lane l accumulates
+// rows 4 (l & 3) .. + 3 and columns 4 (l >> 2) .. + 3 of it with DFMA, reading
+// its four A and four B values of a K-step as two 16-byte shared loads each.
 __global__ void __launch_bounds__(256)
 gemm_f64_kernel(BufTable bufs, const DevGemmOut* __restrict__ outs, const DevGemmSeg* __restrict__ segs,
                 const DevGemmWork* __restrict__ work) {
-    __shared__ double sA[GT_K][GT_M + 1];
-    __shared__ double sB[GT_K][GT_N + 1];
+    __shared__ __align__(16) double sA[GT_K][GT_LD];
+    __shared__ __align__(16) double sB[GT_K][GT_LD];
     const DevGemmWork w = work[blockIdx.x];
     const DevGemmOut o = outs[w.out];
-    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r0 = 16 * (warp & 3) + 4 * (lane & 3);
+    const int c0 = 32 * (warp >> 2) + 4 * (lane >> 2);
+    const bool active = 16 * (warp & 3) < w.tm && 32 * (warp >> 2) < w.tn;
     double acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -416,47 +427,54 @@ gemm_f64_kernel(BufTable bufs, const DevGemmOut* __restrict__ outs, const DevGem
         const double* __restrict__ B = bufs.p[g.b_buf] + g.b_off;
         const double alpha = g.alpha;
         for (int64_t k0 = 0; k0 < g.K; k0 += GT_K) {
-            // load A tile (GT_M x GT_K): element (m, k)
+            // A tile (GT_M x GT_K): element (m, k); rows past M read as zero
             for (int idx = threadIdx.x; idx < GT_M * GT_K; idx += 256) {
                 int m, k;
                 if (g.ta) { k = idx % GT_K; m = idx / GT_K; } else { m = idx % GT_M; k = idx / GT_M; }
-                int64_t gm = w.m0 + m, gk = k0 + k;
+                const int64_t gm = w.m0 + m, gk = k0 + k;
                 double v = 0.0;
-                if (gm < o.M && gk < g.K) v = g.ta ? A[gk + gm * g.lda] : A[gm + gk * g.lda];
+                if (m < w.tm && gm < o.M && gk < g.K) v = g.ta ? A[gk + gm * g.lda] : A[gm + gk * g.lda];
                 sA[k][m] = v * alpha;
             }
             for (int idx = threadIdx.x; idx < GT_N * GT_K; idx += 256) {
                 int n, k;
                 if (g.tb) { n = idx % GT_N; k = idx / GT_N; } else { k = idx % GT_K; n = idx / GT_K; }
-                int64_t gn = w.n0 + n, gk = k0 + k;
+                const int64_t gn = w.n0 + n, gk = k0 + k;
                 double v = 0.0;
-                if (gn < o.N && gk < g.K) v = g.tb ? B[gn + gk * g.ldb] : B[gk + gn * g.ldb];
+                if (n < w.tn && gn < o.N && gk < g.K) v = g.tb ? B[gn + gk * g.ldb] : B[gk + gn * g.ldb];
                 sB[k][n] = v;
             }
             __syncthreads();
+            if (active) {
 #pragma unroll
-            for (int k = 0; k < GT_K; ++k) {
-                double a[4], b[4];
+                for (int k = 0; k < GT_K; ++k) {
+                    const double2 a01 = *(const double2*)&sA[k][r0];
+                    const double2 a23 = *(const double2*)&sA[k][r0 + 2];
+                    const double2 b01 = *(const double2*)&sB[k][c0];
+                    const double2 b23 = *(const double2*)&sB[k][c0 + 2];
+                    const double a[4] = {a01.x, a01.y, a23.x, a23.y};
+                    const double b[4] = {b01.x, b01.y, b23.x, b23.y};
 #pragma unroll
-                for (int i = 0; i < 4; ++i) a[i] = sA[k][tx + 16 * i];
+                    for (int i = 0; i < 4; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) b[j] = sB[k][ty + 16 * j];
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+                        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+                }
             }
             __syncthreads();
         }
     }
+    if (!active) return;
     double* __restrict__ C = bufs.p[o.c_buf] + o.c_off;
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+        const int64_t gn = w.n0 + c0 + j;
+        if (c0 + j >= w.tn || gn >= o.N) continue;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            int64_t gm = w.m0 + tx + 16 * i, gn = w.n0 + ty + 16 * j;
-            if (gm < o.M && gn < o.N) C[gm + gn * o.ldc] = acc[i][j];
+        for (int i = 0; i < 4; ++i) {
+            const int64_t gm = w.m0 + r0 + i;
+            if (r0 + i < w.tm && gm < o.M) C[gm + gn * o.ldc] = acc[i][j];
         }
+    }
 }
 
 // ------------------------------------------------------------------ plan upload / run
@@ -590,8 +608,15 @@ static int upload_stage(Stage& st) {
         for (size_t i = 0; i < st.gout.size(); ++i) {
             const GemmOut& g = st.gout[i];
             o[i] = {g.c_off, g.ldc, g.M, g.N, g.s_begin, g.s_end, g.c_buf, 0};
-            for (int64_t m0 = 0; m0 < g.M; m0 += GT_M)
-                for (int64_t n0 = 0; n0 < g.N; n0 += GT_N) w.push_back({(int64_t)i, m0, n0});
+            // tiles of at most 64 x 64, the last ones of a block cut to it (rows in steps of 16,
+            // columns in steps of 32): the FP64 products spend little work on padding
+            for (int64_t m0 = 0; m0 < g.M; m0 += GT_M) {
+                const int32_t tm = (int32_t)std::min<int64_t>(GT_M, (g.M - m0 + 15) / 16 * 16);
+                for (int64_t n0 = 0; n0 < g.N; n0 += GT_N) {
+                    const int32_t tn = (int32_t)std::min<int64_t>(GT_N, (g.N - n0 + 31) / 32 * 32);
+                    w.push_back({(int64_t)i, m0, n0, tm, tn});
+                }
+            }
         }
         for (size_t i = 0; i < st.gseg.size(); ++i) {
             const GemmSeg& g = st.gseg[i];
