@@ -151,12 +151,20 @@ int qcm_plan_sigma(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm
 /* Plan-shape options of a sigma plan (0 = default).  split_k_segs: the largest
  * number of block products summed into one K3 output before it is split into
  * partial tiles (default 32); dense_min_terms: the fewest K2 terms an output tile
- * needs to join a dense tensor-core group (default 64).  Chosen per problem shape
- * by the autotuner of the Python layer (qcmaquis_gb300/autotune.py). */
+ * needs to join a dense tensor-core group (default 64); n_tile_max: the widest N
+ * of a tensor-core tile of the block products (16..128 in steps of 16, default
+ * 128; wider blocks are cut into tiles of balanced width); k1_schedule: how the
+ * K1 tiles go to the CTAs of the persistent image executor (0 = round robin, the
+ * default; 1 = contiguous cost-balanced ranges with each A tile kept in shared
+ * memory while its tiles run, where every K1 tile is one short block product).
+ * Chosen per problem shape by the autotuner of the Python layer
+ * (qcmaquis_gb300/autotune.py). */
 typedef struct {
     int32_t split_k_segs;
     int32_t dense_min_terms;
-    int32_t reserved[6];
+    int32_t n_tile_max;
+    int32_t k1_schedule;
+    int32_t reserved[4];
 } qcm_plan_opts_t;
 
 /* qcm_plan_sigma with plan-shape options (NULL: the defaults). */

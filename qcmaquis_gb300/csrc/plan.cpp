@@ -35,7 +35,7 @@ namespace qcm {
 // A-resident mode for single-segment stages (K1).  Off: measured slower at the
 // benchmark size, because contiguous per-CTA tile ranges lose the L2 reuse of
 // the B operand across CTAs that the strided order has.
-static constexpr bool kAResident = false;
+static constexpr bool kAResident = false;   // default of the K1 schedule option
 // column alignment (elements) of the K1 result T in the sigma and boundary plans
 // (16 bytes in FP32: vector stores in the image epilogue)
 static constexpr int64_t kTAlign = 4;
@@ -854,7 +854,8 @@ static void add_zero_tiles(Stage& k2, const Stage& k3, int32_t buf) {
 
 static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& right_i, const BM& psi,
                              const std::vector<BM>& L, const std::vector<BM>& R, const MpoV& W, bool herm,
-                             int64_t split_k_segs = 32, int64_t dense_min_terms = 64) {
+                             int64_t split_k_segs = 32, int64_t dense_min_terms = 64, int n_tile_max = 128,
+                             bool k1_resident = kAResident) {
     auto* P = new qcm_plan();
     P->kind = PK_SIGMA;
     const qcm_mpo_t* m = W.m;
@@ -939,8 +940,8 @@ static qcm_plan* build_sigma(const Idx& phys, const Idx& left_i, const Idx& righ
     P->scratch[2] = c_end;
     add_zero_tiles(s2, s3, QCM_BUF_S2);
     z2.zlen = 0;  // the zero tiles of K2 clear what K3 reads; the rest of contr is never read
-    build_image_tables(s1, s1.img);
-    build_image_tables(s3, s3.img);
+    build_image_tables(s1, s1.img, n_tile_max, k1_resident);
+    build_image_tables(s3, s3.img, n_tile_max, false);
     axpy_components(s2, s2.comp_root);
     build_dense_groups(s2, dense_min_terms, s2.img, s2.heavy);
     P->image_bytes = std::max(std::max(s1.img.bytes, s3.img.bytes), s2.img.bytes);
@@ -1668,7 +1669,7 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
 // stage's C = op(A) op(B) is computed as C^T = op(B)^T op(A)^T (less padding;
 // the other choice, with coalesced column stores, was measured slower for K1).
 // Panels that several segments read with the same orientation share one image.
-void build_image_tables(const Stage& st, ImgTables& t) {
+void build_image_tables(const Stage& st, ImgTables& t, int n_tile_max, bool a_resident) {
     t = ImgTables();
     struct Key {
         int32_t buf, ld, R, K, kc;
@@ -1762,8 +1763,8 @@ void build_image_tables(const Stage& st, ImgTables& t) {
             t.segs.push_back(s);
         }
         const int32_t s_end = (int32_t)t.segs.size();
-        // N tiles of balanced width (multiples of 16, at most 128): e.g. 160 = 80 + 80
-        const int32_t nnt = (io.ncols + 127) / 128;
+        // N tiles of balanced width (multiples of 16, at most n_tile_max): e.g. 160 = 80 + 80
+        const int32_t nnt = (io.ncols + n_tile_max - 1) / n_tile_max;
         const int32_t per = ((io.ncols + nnt - 1) / nnt + 15) / 16 * 16;
         for (int32_t m0 = 0; m0 < io.mrows; m0 += 128)
             for (int32_t n0 = 0; n0 < io.ncols; n0 += per) {
@@ -1781,7 +1782,7 @@ void build_image_tables(const Stage& st, ImgTables& t) {
         throw std::runtime_error("image executor: tables too large");
     // A-resident mode when every tile is a single short segment (K1: each T tile is one
     // block product; the same psi tile is the A operand of hundreds of products)
-    bool ares = kAResident && !t.units.empty();
+    bool ares = a_resident && !t.units.empty();
     for (const ImgUnit& u : t.units)
         ares = ares && u.s_end - u.s_begin == 1 && t.segs[u.s_begin].kc <= IMG_ARES_MAX;
     if (ares) {
@@ -2160,19 +2161,23 @@ int qcm_plan_sigma_opts(const qcm_index_t* phys, const qcm_index_t* left_i, cons
                         const qcm_mpo_t* mpo, int32_t hermitian, const qcm_plan_opts_t* opts, qcm_plan** plan) {
     if (!plan) { set_error("null plan pointer"); return QCM_E_INVALID; }
     int64_t sk = 32, dm = 64;
+    int ntm = 128, k1s = 0;
     if (opts) {
         if (opts->split_k_segs > 0) sk = opts->split_k_segs;
         if (opts->dense_min_terms > 0) dm = opts->dense_min_terms;
+        if (opts->n_tile_max > 0) ntm = opts->n_tile_max;
+        k1s = opts->k1_schedule;
     }
-    if (sk < 2 || sk > (1 << 20) || dm < 8) {
-        set_error("qcm_plan_sigma_opts: split_k_segs must be in [2, 2^20], dense_min_terms >= 8");
+    if (sk < 2 || sk > (1 << 20) || dm < 8 || ntm < 16 || ntm > 128 || ntm % 16 || (k1s != 0 && k1s != 1)) {
+        set_error("qcm_plan_sigma_opts: split_k_segs must be in [2, 2^20], dense_min_terms >= 8, n_tile_max a "
+                  "multiple of 16 in [16, 128], k1_schedule 0 or 1");
         *plan = nullptr;
         return QCM_E_INVALID;
     }
     try {
         MpoV W(mpo);
         *plan = build_sigma(read_index(phys), read_index(left_i), read_index(right_i), read_blocks(psi),
-                            read_boundary(left), read_boundary(right), W, hermitian != 0, sk, dm);
+                            read_boundary(left), read_boundary(right), W, hermitian != 0, sk, dm, ntm, k1s == 1);
         return QCM_OK;
     } catch (const std::exception& e) {
         set_error(std::string("qcm_plan_sigma_opts: ") + e.what());

@@ -171,7 +171,9 @@ struct ImgTables {
     std::vector<int64_t> cost;    // prefix sums of the tile costs (size tiles + 1)
 };
 constexpr int IMG_ARES_MAX = 5;
-void build_image_tables(const struct Stage& st, ImgTables& t);
+// n_tile_max: widest N of a tile (16..128, multiple of 16); a_resident: the K1 A-resident
+// schedule when every tile is one short block product
+void build_image_tables(const struct Stage& st, ImgTables& t, int n_tile_max = 128, bool a_resident = false);
 // Dense groups of a gather-axpy stage: output tiles that share their sources
 // (a connected component of the output/source graph), have at least
 // min_terms terms and one tile shape become one block product

@@ -206,12 +206,12 @@ class Engine:
             self._plans[key] = self._plans.pop(key)   # most recently used last
             self.plan_hits += 1
         if p is None:
-            sk = dm = 0
+            opts = {}
             if self.autotuner is not None:
-                sk, dm = self.autotuner.choice(self, ket, L, R, mpo)
+                opts = self.autotuner.choice(self, ket, L, R, mpo)
             t0 = time.time()
             p = N.plan_sigma(ket.phys_i, ket.left_i, ket.right_i, ket.layout, L.layout, R.layout, self.fmpo(mpo),
-                             self.hermitian, split_k_segs=sk, dense_min_terms=dm)
+                             self.hermitian, **opts)
             p.upload()
             self.plan_seconds += time.time() - t0
             p._keep = (mpo,)

@@ -802,16 +802,18 @@ def plan_split_assemble(split: "Plan", u_off, vt_off, keep, S_host, s_off, l2r: 
 
 
 class CPlanOpts(C.Structure):
-    _fields_ = [("split_k_segs", C.c_int32), ("dense_min_terms", C.c_int32), ("reserved", C.c_int32 * 6)]
+    _fields_ = [("split_k_segs", C.c_int32), ("dense_min_terms", C.c_int32), ("n_tile_max", C.c_int32),
+                ("k1_schedule", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 def plan_sigma(phys: Index, left_i: Index, right_i: Index, psi: Layout, L: BoundaryLayout, R: BoundaryLayout,
-               mpo: FMpo, hermitian: bool = True, split_k_segs: int = 0, dense_min_terms: int = 0) -> Plan:
+               mpo: FMpo, hermitian: bool = True, split_k_segs: int = 0, dense_min_terms: int = 0,
+               n_tile_max: int = 0, k1_schedule: int = 0) -> Plan:
     """``qcm_plan_sigma`` (``qcm_plan_sigma_opts`` when a plan-shape option is given)."""
     fp, fl, fr = FIndex(phys), FIndex(left_i), FIndex(right_i)
     h = C.c_void_p()
-    if split_k_segs or dense_min_terms:
-        o = CPlanOpts(int(split_k_segs), int(dense_min_terms))
+    if split_k_segs or dense_min_terms or n_tile_max or k1_schedule:
+        o = CPlanOpts(int(split_k_segs), int(dense_min_terms), int(n_tile_max), int(k1_schedule))
         check(lib().qcm_plan_sigma_opts(C.byref(fp.c), C.byref(fl.c), C.byref(fr.c), C.byref(psi.c), C.byref(L.c),
                                         C.byref(R.c), C.byref(mpo.c), 1 if hermitian else 0, C.byref(o),
                                         C.byref(h)), "qcm_plan_sigma_opts")

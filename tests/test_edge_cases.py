@@ -147,6 +147,33 @@ def test_plan_shape_options_keep_sigma_and_change_the_plan():
     assert shape_key(lay, Ll, Rl, ts, 2) != shape_key(lay, Ll, Rl, ts, 0)
 
 
+def test_tile_width_and_k1_schedule_options_keep_sigma():
+    """The autotuner's tile-shape and schedule knobs: no tile wider than n_tile_max (so
+    at least as many tiles), the K1 A-resident schedule reorders K1's tiles, the sigma is unchanged
+    (image tables interpreted on the CPU); invalid values are refused."""
+    psi, left, right, ts, ots = _random_site_problem(L=6, N=6, m=64, site=2)
+    psi = psi.copy().make_left_paired()
+    lay, Ll, Rl = N.Layout.of(psi.data), N.BoundaryLayout.of(left), N.BoundaryLayout.of(right)
+    ref = lay.pack(R.site_hamil2(psi, left, right, ots).data)
+    tiles = {}
+    for ntm, k1s in [(0, 0), (32, 0), (16, 0), (0, 1)]:
+        p = N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, N.FMpo(ts), True,
+                         n_tile_max=ntm, k1_schedule=k1s)
+        bufs = [lay.pack(psi.data), Ll.pack(left), Rl.pack(right), np.full(p.out_elems, np.nan)] + \
+            [np.full(max(s, 1), np.nan) for s in p.scratch]
+        run_plan(p, bufs, images=True)
+        assert np.linalg.norm(bufs[3] - ref) <= 1e-7 * np.linalg.norm(ref)
+        tabs = [p.stage_images(i)["tiles"] for i, k in enumerate(p.stage_kinds()) if k == "gemm"]
+        tiles[(ntm, k1s)] = sum(len(t) for t in tabs)
+        # every tile at most n_tile_max wide (column 3 of a tile: its N width)
+        assert max(int(t[3]) for tab in tabs for t in tab) <= (ntm or 128)
+    assert tiles[(16, 0)] >= tiles[(32, 0)] >= tiles[(0, 0)]
+    assert tiles[(0, 1)] == tiles[(0, 0)]
+    for bad in ({"n_tile_max": 24}, {"n_tile_max": 256}, {"k1_schedule": 2}):
+        with pytest.raises(RuntimeError):
+            N.plan_sigma(psi.phys_i, psi.left_i, psi.right_i, lay, Ll, Rl, N.FMpo(ts), True, **bad)
+
+
 @pytest.mark.gpu
 def test_autotuned_engine_gives_the_same_sigma(tmp_path):
     import torch
@@ -158,6 +185,7 @@ def test_autotuned_engine_gives_the_same_sigma(tmp_path):
     a = Engine("cuda:0", precision=N.PREC_BF16X3)
     b = Engine("cuda:0", precision=N.PREC_BF16X3)
     b.autotuner = Autotuner(path=str(tmp_path / "tune.json"), candidates=[(4, 16), (32, 64)], reps=2)
+    # the tile-width and K1-schedule candidates are measured too (tensor-core forms)
     sa = a.site_hamil2(x, Lb, Rb, ts).data
     sb = b.site_hamil2(x, Lb, Rb, ts).data
     assert torch.linalg.norm(sa - sb).item() <= 1e-5 * torch.linalg.norm(sa).item()
