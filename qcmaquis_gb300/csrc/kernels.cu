@@ -260,26 +260,9 @@ gather_axpy_contig(BufTable bufs, const DevAxpyOut* __restrict__ outs, const Dev
                 for (int u = 0; u < CG_PER; ++u) acc[u] = fma(a0, (ACC)__ldg(p0 + u * CG_THREADS), acc[u]);
             }
         } else {
-            // a short chunk (most work items): four terms per iteration, the loads of the
-            // elements past n predicated off, so that many loads are in flight per thread
-            int t = 0;
-            for (; t + 4 <= tn; t += 4) {
-                SRC x[4][CG_PER];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const SRC* __restrict__ p = s_ptr[t + q] + tid;
-#pragma unroll
-                    for (int u = 0; u < CG_PER; ++u)
-                        x[q][u] = tid + u * CG_THREADS < n ? __ldg(p + u * CG_THREADS) : SRC(0);
-                }
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const ACC a = s_alpha[t + q];
-#pragma unroll
-                    for (int u = 0; u < CG_PER; ++u) acc[u] = fma(a, (ACC)x[q][u], acc[u]);
-                }
-            }
-            for (; t < tn; ++t) {
+            // a short chunk: one term per iteration (four terms per iteration, with the
+            // loads past n predicated off, measured slower: K2 6.29 against 5.86 ms)
+            for (int t = 0; t < tn; ++t) {
                 const SRC* __restrict__ p0 = s_ptr[t] + tid;
                 const ACC a0 = s_alpha[t];
 #pragma unroll
