@@ -87,7 +87,10 @@ typedef struct {
  * symmetry selects the group of the charges (QCM_SYM_*): SU2U1 charges are
  * (N, 2S) and the contractions carry the SU(2) couplings (ct/non-abelian);
  * TwoU1 charges are (N_up, N_down), every coupling is 1, spins and phases are
- * ignored (ct/abelian).  A zero-initialised field means SU2U1. */
+ * ignored (ct/abelian); U1 charges are (N, 0) -- the reference's single int
+ * charge (block_matrix/symmetry/u1.h) in the first component, the second held at
+ * zero, so blocks sort as the reference's U1 blocks do -- and contract as TwoU1.
+ * A zero-initialised field means SU2U1. */
 typedef struct {
     int32_t row_dim, col_dim;
     const int32_t* left_spin;
@@ -113,6 +116,7 @@ typedef struct {
 
 #define QCM_SYM_SU2U1 0
 #define QCM_SYM_TWOU1 1
+#define QCM_SYM_U1 2
 
 typedef struct qcm_plan qcm_plan;
 
@@ -490,7 +494,7 @@ void qcm_split_result_destroy(qcm_split_result* res);
  * through qcm_plan_out_tensor.  With symmetry = QCM_SYM_TWOU1 there is no
  * reduction: the two-site physical index is the product phys1 x phys2 and the
  * tensor is reshaped straight to left-paired (make_mps_ of the abelian
- * TwoSiteTensor, twositetensor.hpp:125-130). */
+ * TwoSiteTensor, twositetensor.hpp:125-130); QCM_SYM_U1 likewise. */
 int qcm_plan_two_site(const qcm_index_t* phys1, const qcm_index_t* a_left, const qcm_index_t* a_right,
                       const qcm_blocks_t* a, const qcm_index_t* phys2, const qcm_index_t* b_left,
                       const qcm_index_t* b_right, const qcm_blocks_t* b, int32_t symmetry, qcm_plan** plan);
@@ -501,8 +505,8 @@ int qcm_plan_two_site(const qcm_index_t* phys1, const qcm_index_t* a_left, const
  * (left of site i, right of site i+1).  Slots: KET = the reduced two-site
  * tensor (left-paired), OUT = the both-paired matrix the truncation factorises
  * (its blocks through qcm_plan_out_tensor; they are the qcm_svd batch).
- * QCM_SYM_TWOU1: no unreduce step (the abelian operator<<, twositetensor.hpp:
- * 352-366), only the reshape. */
+ * QCM_SYM_TWOU1 and QCM_SYM_U1: no unreduce step (the abelian operator<<,
+ * twositetensor.hpp:352-366), only the reshape. */
 int qcm_plan_split_theta(const qcm_index_t* phys1, const qcm_index_t* phys2, const qcm_index_t* left_i,
                          const qcm_index_t* right_i, const qcm_blocks_t* u, int32_t symmetry, qcm_plan** plan);
 

@@ -25,8 +25,8 @@ from . import dmrg_ref as R
 
 
 def _abelian(model_or_mpo) -> bool:
-    """TwoU1 models and their MPO tensors carry symmetry "2u1"."""
-    return getattr(model_or_mpo, "symmetry", "su2u1") == "2u1"
+    """TwoU1 and U1 models and their MPO tensors carry symmetry "2u1" / "u1"."""
+    return getattr(model_or_mpo, "symmetry", "su2u1") != "su2u1"
 
 
 def _engine(abelian: bool):

@@ -222,7 +222,7 @@ class OHerm:
 
 class OTensor:
     """An MPO tensor: element (b1, b2) -> [(operator index, scale)], operators, bond spins;
-    ``symmetry`` "su2u1" or "2u1" (abelian)."""
+    ``symmetry`` "su2u1", or "2u1" / "u1" (abelian)."""
 
     symmetry = "su2u1"
 
@@ -269,9 +269,11 @@ class OTensor:
 
 def make_twosite_mpo(mpo1, mpo2, phys1, phys2) -> OTensor:
     """The two-site tensor of a neighbouring pair of single-site MPO tensors (abelian
-    Kronecker products when the tensors are of the "2u1" group, where every spin is 0)."""
+    Kronecker products when the tensors are of an abelian group, "2u1" or "u1", where
+    every spin is 0)."""
     assert mpo1.col_dim == mpo2.row_dim
-    abelian = getattr(mpo1, "symmetry", "su2u1") == "2u1"
+    group = getattr(mpo1, "symmetry", "su2u1")
+    abelian = group != "su2u1"
     ops: List[OOp] = []
     elements: Dict[Tuple[int, int], List[Tuple[int, float]]] = {}
     for b1 in range(mpo1.row_dim):
@@ -302,8 +304,7 @@ def make_twosite_mpo(mpo1, mpo2, phys1, phys2) -> OTensor:
     h1, h2 = mpo1.herm, mpo2.herm
     herm = OHerm(h1.LeftHerm, h2.RightHerm, h1.LeftPhase, h2.RightPhase)
     t = OTensor(mpo1.row_dim, mpo2.col_dim, elements, ops, herm, mpo1.left_spins, mpo2.right_spins)
-    if abelian:
-        t.symmetry = "2u1"
+    t.symmetry = group
     return t
 
 

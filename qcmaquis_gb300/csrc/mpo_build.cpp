@@ -89,7 +89,7 @@ void check_mpo(const qcm_mpo_t* w, const char* what) {
             if (w->term_op[t] < 0 || w->term_op[t] >= w->n_ops) throw std::runtime_error("mpo operator out of range");
     }
     if (w->n_ops > 0 && !w->op_spin) throw std::runtime_error(std::string("null op_spin in ") + what);
-    if (w->symmetry != QCM_SYM_SU2U1 && w->symmetry != QCM_SYM_TWOU1)
+    if (w->symmetry != QCM_SYM_SU2U1 && w->symmetry != QCM_SYM_TWOU1 && w->symmetry != QCM_SYM_U1)
         throw std::runtime_error(std::string("unknown symmetry in ") + what);
     check_ops(w, what);
 }
@@ -496,7 +496,7 @@ int qcm_mpo_twosite(const qcm_mpo_t* w1, const qcm_mpo_t* w2, const qcm_index_t*
         ProdOps prods;
         for (size_t q = 0; q + 5 < B->keys.size(); q += 6) {
             const int32_t* k = &B->keys[q];
-            op_kron(w1, w2, k[0], k[1], k[2], k[3], k[4], k[5], p1, p2, pb, prods, w1->symmetry == QCM_SYM_TWOU1);
+            op_kron(w1, w2, k[0], k[1], k[2], k[3], k[4], k[5], p1, p2, pb, prods, w1->symmetry != QCM_SYM_SU2U1);
         }
         const qcm_mpo_t v = prods.view();
         phase2(*B, &v);

@@ -580,11 +580,7 @@ qcm_plan* build_assemble(const Idx& p1, const Idx& p2, const Idx& left_i, const 
 using namespace qcm;
 
 // true for the abelian group; throws on an unknown one
-static bool check_symmetry(int32_t symmetry) {
-    if (symmetry != QCM_SYM_SU2U1 && symmetry != QCM_SYM_TWOU1)
-        throw std::runtime_error("unknown symmetry " + std::to_string(symmetry));
-    return symmetry == QCM_SYM_TWOU1;
-}
+static bool check_symmetry(int32_t symmetry) { return abelian_symmetry(symmetry); }
 
 static int mps_guard(const char* what, const std::function<qcm_plan*()>& f, qcm_plan** out) {
     if (!out) { set_error(std::string(what) + ": null output"); return QCM_E_INVALID; }

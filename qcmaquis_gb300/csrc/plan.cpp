@@ -32,6 +32,12 @@
 
 namespace qcm {
 
+bool abelian_symmetry(int32_t symmetry) {
+    if (symmetry == QCM_SYM_SU2U1) return false;
+    if (symmetry == QCM_SYM_TWOU1 || symmetry == QCM_SYM_U1) return true;
+    throw std::runtime_error("unknown symmetry " + std::to_string(symmetry));
+}
+
 // A-resident mode for single-segment stages (K1).  Off: measured slower at the
 // benchmark size, because contiguous per-CTA tile ranges lose the L2 reuse of
 // the B operand across CTAs that the strided order has.
@@ -324,6 +330,7 @@ struct MpoV {
     std::vector<std::vector<int>> row_elem;      // b1 -> element ids (matching row_b2)
     MpoV(const qcm_mpo_t* m_) : m(m_) {
         if (!m) throw std::runtime_error("null mpo");
+        abelian_symmetry(m->symmetry);
         row_b2.resize(m->row_dim);
         row_elem.resize(m->row_dim);
         for (int b2 = 0; b2 < m->col_dim; ++b2)
@@ -339,11 +346,11 @@ struct MpoV {
     }
     int lspin(int b) const { return m->left_spin[b]; }
     int rspin(int b) const { return m->right_spin[b]; }
-    // Abelian groups (TwoU1) have no spin couplings: every coupling is the term's
+    // Abelian groups (TwoU1, U1) have no spin couplings: every coupling is the term's
     // scale, every triangle test passes and a Hermitian partner enters with
     // scale 1 (conjugate_phases of common/boundary_times_mps.hpp:44-51 and the
     // abelian lbtm/rbtm kernels, ct/abelian/apply_op.hpp:80-138).
-    bool abelian() const { return m->symmetry == QCM_SYM_TWOU1; }
+    bool abelian() const { return m->symmetry != QCM_SYM_SU2U1; }
     bool allowed(int a, int b, int c) const { return abelian() || triangle(a, b, c); }
     double conj_scale(int lc_s, int rc_s, int spin, int phase) const {
         return abelian() ? 1.0 : conjugate_correction(lc_s, rc_s, spin) * phase;

@@ -30,6 +30,10 @@ struct Q {
     bool operator!=(const Q& o) const { return !(*this == o); }
 };
 inline Q fuse(Q a, Q b) { return Q(a.n + b.n, a.s + b.s); }
+
+// QCM_SYM_* of a tensor or plan: true for the abelian groups (TwoU1, U1), which
+// share the abelian contraction rules; throws on a code that names no group.
+bool abelian_symmetry(int32_t symmetry);
 inline Q neg(Q a) { return Q(-a.n, -a.s); }
 inline bool triangle(int a, int b, int c) { return ((a + b + c) % 2 == 0) && std::abs(a - b) <= c && c <= a + b; }
 

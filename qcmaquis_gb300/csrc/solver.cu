@@ -380,7 +380,7 @@ int qcm_split(qcm_ctx* c, const qcm_index_t* phys1, const qcm_index_t* phys2, co
     int rc = check_ctx(c);
     if (rc) return rc;
     if (!u_dev || !trunc || !out) { set_error("qcm_split: null argument"); return QCM_E_INVALID; }
-    if (symmetry != QCM_SYM_SU2U1 && symmetry != QCM_SYM_TWOU1) {
+    if (symmetry != QCM_SYM_SU2U1 && symmetry != QCM_SYM_TWOU1 && symmetry != QCM_SYM_U1) {
         set_error("qcm_split: unknown symmetry");
         return QCM_E_INVALID;
     }
@@ -400,7 +400,7 @@ int qcm_split(qcm_ctx* c, const qcm_index_t* phys1, const qcm_index_t* phys2, co
     };
     try {
         sp = build_split(read_index(phys1), read_index(phys2), read_index(left_i), read_index(right_i),
-                         read_blocks(u), symmetry == QCM_SYM_TWOU1);
+                         read_blocks(u), symmetry != QCM_SYM_SU2U1);
     } catch (const std::exception& e) {
         set_error(std::string("qcm_split: ") + e.what());
         return cleanup(QCM_E_INVALID);

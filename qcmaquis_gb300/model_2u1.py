@@ -59,13 +59,15 @@ def _ladder() -> Dict[str, np.ndarray]:
     return {"cu": cu, "cd": cd, "du": cu.T.copy(), "dd": cd.T.copy(), "F": fill, "I": np.eye(4)}
 
 
-def dense_to_op(m: np.ndarray) -> SiteOperator:
-    """SiteOperator (blocks keyed (phys_in, phys_out)) of a dense <out|O|in> matrix."""
+def dense_to_op(m: np.ndarray, states=STATES) -> SiteOperator:
+    """SiteOperator (blocks keyed (phys_in, phys_out)) of a dense <out|O|in> matrix over
+    a local basis of one state per charge (``states``: the charge of each position)."""
     bm = BlockMatrix()
-    for i in range(4):
-        for o in range(4):
+    d = len(states)
+    for i in range(d):
+        for o in range(d):
             if m[o, i] != 0.0:
-                bm.insert_block(np.array([[float(m[o, i])]]), STATES[i], STATES[o])
+                bm.insert_block(np.array([[float(m[o, i])]]), states[i], states[o])
     return SiteOperator(bm, SpinDescriptor(), {})
 
 
@@ -75,8 +77,9 @@ class _OpRegistry:
     operator is registered together with its transpose (its Hermitian partner), so
     the partner of a tag is exactly its adjoint."""
 
-    def __init__(self, th: TagHandler):
+    def __init__(self, th: TagHandler, states=STATES):
         self.th = th
+        self.states = states
         self.by_key: Dict[bytes, Tuple[int, float]] = {}
         self.dense: List[np.ndarray] = []
 
@@ -93,13 +96,13 @@ class _OpRegistry:
         if k in self.by_key:
             t, f0 = self.by_key[k]
             return t, first / f0
-        t = self.th.register_op(dense_to_op(m), FERMIONIC if fermionic else BOSONIC)
+        t = self.th.register_op(dense_to_op(m, self.states), FERMIONIC if fermionic else BOSONIC)
         self.by_key[k] = (t, first)
         self.dense.append(m)
         mt = m.T.copy()
         kt, firstt = self._key(mt)
         if kt not in self.by_key:
-            tt = self.th.register_op(dense_to_op(mt), FERMIONIC if fermionic else BOSONIC)
+            tt = self.th.register_op(dense_to_op(mt, self.states), FERMIONIC if fermionic else BOSONIC)
             self.by_key[kt] = (tt, firstt)
             self.th.hermitian_pair(t, tt)
         return t, 1.0
@@ -130,40 +133,44 @@ def expand_integrals(L: int, ints) -> Tuple[np.ndarray, np.ndarray, float, Dict]
     return t, V, core, src
 
 
-class TwoU1Model:
-    """The TwoU1 quantum-chemistry model: ``L`` orbitals, ``n_up`` and ``n_down``
-    electrons (the reference's ``u1_total_charge1`` / ``u1_total_charge2``)."""
+class AbelianChemModel:
+    """The terms of the quantum-chemistry Hamiltonian over an abelian group, from its
+    spin-orbital operator form.  A subclass fixes the local basis (``states``: the
+    charge of each local state, one state per charge), the local matrices
+    (``_ladder``: identity "I", fill "F" and the ladder operators) and where a spin
+    orbital lives (``_so``); the spin orbitals are ordered for the Jordan-Wigner
+    string as the sites are, and within a site in ``_so``'s order."""
 
-    symmetry = "2u1"
+    symmetry = ""
+    states: List = []
 
-    def __init__(self, L: int, integrals: Dict[Tuple[int, int, int, int], float], n_up: int, n_down: int,
-                 integral_cutoff: float = 1e-20):
-        self.L = L
-        self.n_up, self.n_down = n_up, n_down
-        self.nelec = n_up + n_down
-        self.right_end = (n_up, n_down)
-        self.phys = phys_index()
-        self.integrals = integrals
-        self.integral_cutoff = integral_cutoff
+    def _so(self, p: int, spin: int, create: bool) -> Tuple[int, str]:
+        """(site, ladder name) of c+_{p spin} (``create``) or c_{p spin}."""
+        raise NotImplementedError
+
+    def _ladder(self) -> Dict[str, np.ndarray]:
+        raise NotImplementedError
+
+    def _init_operators(self):
         self.tag_handler = TagHandler()
-        self._reg = _OpRegistry(self.tag_handler)
-        lad = _ladder()
+        self._reg = _OpRegistry(self.tag_handler, self.states)
+        lad = self._ladder()
         self._lad = lad
         self.ops = Operators()
         self.ops.ident, _ = self._reg.tag(lad["I"], False)
         self.ops.ident_full = self.ops.ident
         self.ops.fill, _ = self._reg.tag(lad["F"], False)
         self.terms: List[Term] = []
-        self._create_terms()
 
     def _site_ops(self, ladder: List[Tuple[int, str]]):
         """One (site, local matrix, fermionic) per site of a product of ladder operators
         given in operator order as (site, name), or None if the product vanishes."""
         lad = self._lad
+        d = len(self.states)
         sites = sorted({s for s, _ in ladder})
         out = []
         for k in sites:
-            m = np.eye(4)
+            m = np.eye(d)
             nferm = 0
             for s, name in ladder:
                 if s == k:
@@ -176,9 +183,10 @@ class TwoU1Model:
             out.append((k, m, nferm % 2 == 1))
         return out
 
-    def _create_terms(self):
-        L = self.L
-        t, V, core, src = expand_integrals(L, self.integrals)
+    def _create_terms(self, norb: int):
+        """H = sum_pq t_pq sum_s c+_ps c_qs + 1/2 sum_pqrs (pq|rs) sum_st c+_ps c+_rt c_ts c_qs
+        + E_core over ``norb`` spatial orbitals."""
+        t, V, core, src = expand_integrals(norb, self.integrals)
         merged: Dict[Tuple, Term] = {}
 
         def add(coeff: float, ladder, key):
@@ -205,23 +213,22 @@ class TwoU1Model:
 
         self._unit = {k: v for k, v in self.integrals.items()}
         cut = self.integral_cutoff
-        for p in range(L):
-            for q in range(L):
+        for p in range(norb):
+            for q in range(norb):
                 if abs(t[p, q]) > cut:
-                    for c, d in (("cu", "du"), ("cd", "dd")):
-                        add(t[p, q], [(p, c), (q, d)], src[(p, q)])
-        cre = {0: "cu", 1: "cd"}
-        ann = {0: "du", 1: "dd"}
-        for p in range(L):
-            for q in range(L):
-                for r in range(L):
-                    for s in range(L):
+                    for sp in (0, 1):
+                        add(t[p, q], [self._so(p, sp, True), self._so(q, sp, False)], src[(p, q)])
+        for p in range(norb):
+            for q in range(norb):
+                for r in range(norb):
+                    for s in range(norb):
                         v = V[p, q, r, s]
                         if abs(v) <= cut:
                             continue
                         for sa in (0, 1):
                             for sb in (0, 1):
-                                add(0.5 * v, [(p, cre[sa]), (r, cre[sb]), (s, ann[sb]), (q, ann[sa])],
+                                add(0.5 * v, [self._so(p, sa, True), self._so(r, sb, True),
+                                              self._so(s, sb, False), self._so(q, sa, False)],
                                     src[(p, q, r, s)])
         if core != 0.0 or () in src:
             term = Term(core, False)
@@ -231,4 +238,30 @@ class TwoU1Model:
         self.terms.extend(x for x in merged.values() if x.coeff != 0.0)
 
 
-__all__ = ["TwoU1Model", "phys_index", "expand_integrals", "dense_to_op"]
+class TwoU1Model(AbelianChemModel):
+    """The TwoU1 quantum-chemistry model: ``L`` orbitals, ``n_up`` and ``n_down``
+    electrons (the reference's ``u1_total_charge1`` / ``u1_total_charge2``)."""
+
+    symmetry = "2u1"
+    states = STATES
+
+    def __init__(self, L: int, integrals: Dict[Tuple[int, int, int, int], float], n_up: int, n_down: int,
+                 integral_cutoff: float = 1e-20):
+        self.L = L
+        self.n_up, self.n_down = n_up, n_down
+        self.nelec = n_up + n_down
+        self.right_end = (n_up, n_down)
+        self.phys = phys_index()
+        self.integrals = integrals
+        self.integral_cutoff = integral_cutoff
+        self._init_operators()
+        self._create_terms(L)
+
+    def _ladder(self) -> Dict[str, np.ndarray]:
+        return _ladder()
+
+    def _so(self, p: int, spin: int, create: bool) -> Tuple[int, str]:
+        return p, ("c" if create else "d") + ("u" if spin == 0 else "d")
+
+
+__all__ = ["AbelianChemModel", "TwoU1Model", "phys_index", "expand_integrals", "dense_to_op"]

@@ -65,7 +65,7 @@ class Hermitian:
 
 class MPOTensor:
     """Sparse (b1, b2) -> [(op, scale), ...] tensor with SU(2) bond spins (all 0 for
-    an abelian group; ``symmetry`` names the group: "su2u1" or "2u1")."""
+    an abelian group; ``symmetry`` names the group: "su2u1", "2u1" or "u1")."""
 
     symmetry = "su2u1"
 

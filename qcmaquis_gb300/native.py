@@ -49,12 +49,12 @@ class CMpo(C.Structure):
 
 
 # symmetry groups of qcm_mpo_t.symmetry and the MPS-level plans
-SYM_SU2U1, SYM_TWOU1 = 0, 1
+SYM_SU2U1, SYM_TWOU1, SYM_U1 = 0, 1, 2
 
 
 def symmetry_code(name: str) -> int:
-    """QCM_SYM_* of a symmetry name ("su2u1", "2u1")."""
-    codes = {"su2u1": SYM_SU2U1, "2u1": SYM_TWOU1}
+    """QCM_SYM_* of a symmetry name ("su2u1", "2u1", "u1")."""
+    codes = {"su2u1": SYM_SU2U1, "2u1": SYM_TWOU1, "u1": SYM_U1}
     if name not in codes:
         raise ValueError(f"unsupported symmetry {name!r}")
     return codes[name]
@@ -532,7 +532,7 @@ def _twosite_products(L, w1: FMpo, w2: FMpo, phys1: Index, phys2: Index, h):
         for o1, o2, j, jpp, jp, sp in keys[:6 * nk.value].reshape(-1, 6).tolist():
             op1 = w1.mpo.op(w1.op_tags[o1])
             op2 = w2.mpo.op(w2.op_tags[o2])
-            if w1.symmetry == SYM_TWOU1:
+            if w1.symmetry != SYM_SU2U1:
                 prod = op_kron_abelian(phys1, phys2, op1, op2)
             else:
                 prod = op_kron_su2(phys1, phys2, op1, op2, SpinDescriptor(j), SpinDescriptor(jpp),

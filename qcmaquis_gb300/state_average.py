@@ -295,14 +295,14 @@ def run_sa_dmrg(model, mpo, p, nelec: int, twoS: int = 0, nroots: int = 2, weigh
     k = int(nroots)
     w = [1.0 / k] * k if weights is None else [float(x) / sum(weights) for x in weights]
     sym = N.symmetry_code(getattr(model, "symmetry", "su2u1"))
-    right_end = model.right_end if sym == N.SYM_TWOU1 else (nelec, twoS)
+    right_end = model.right_end if sym != N.SYM_SU2U1 else (nelec, twoS)
     engine = engine or Engine(device, precision=precision)
     engine_full = Engine(device, hermitian=False)
     # a mixed-precision sigma cannot resolve residuals below its own error
     jd_tol = max(p.ietl_jcd_tol, JD_RESIDUAL_FLOOR.get(engine.precision, 0.0))
     if mps is None:
         mps = default_mps_init(L, model.phys, right_end, p.init_bond_dimension, p.seed, device,
-                               abelian=sym == N.SYM_TWOU1)
+                               abelian=sym != N.SYM_SU2U1)
         normalize_right(mps)
     if ts_mpo is None:
         ts_mpo = N.make_ts_cache_fmpo(mpo, model.phys)

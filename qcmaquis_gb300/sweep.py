@@ -223,12 +223,12 @@ def run_dmrg(model, mpo, p: SweepParams, nelec: int, twoS: int = 0, mps: Optiona
         engine.boundary_plan_cache_size = plan_cache
     engine_full = Engine(device, hermitian=False)
     bprec = 0 if boundary_precision is None else boundary_precision
-    # SU2U1: the target (N, 2S); TwoU1 models carry theirs, (N_up, N_down)
+    # SU2U1: the target (N, 2S); abelian models carry theirs ((N_up, N_down) or (N, 0))
     sym = N.symmetry_code(getattr(model, "symmetry", "su2u1"))
-    right_end = model.right_end if sym == N.SYM_TWOU1 else (nelec, twoS)
+    right_end = model.right_end if sym != N.SYM_SU2U1 else (nelec, twoS)
     if mps is None:
         mps = default_mps_init(L, phys, right_end, p.init_bond_dimension, p.seed, device,
-                               abelian=sym == N.SYM_TWOU1)
+                               abelian=sym != N.SYM_SU2U1)
         normalize_right(mps)
     if ts_mpo is None:
         ts_mpo = N.make_ts_cache_fmpo(mpo, phys)
@@ -347,12 +347,12 @@ def run_dmrg_single_site(model, mpo, p: SweepParams, nelec: int, twoS: int = 0,
     phys = model.phys
     engine = engine or Engine(device, precision=precision)
     engine_full = Engine(device, hermitian=False)
-    # SU2U1: the target (N, 2S); TwoU1 models carry theirs, (N_up, N_down)
+    # SU2U1: the target (N, 2S); abelian models carry theirs ((N_up, N_down) or (N, 0))
     sym = N.symmetry_code(getattr(model, "symmetry", "su2u1"))
-    right_end = model.right_end if sym == N.SYM_TWOU1 else (nelec, twoS)
+    right_end = model.right_end if sym != N.SYM_SU2U1 else (nelec, twoS)
     if mps is None:
         mps = default_mps_init(L, phys, right_end, p.init_bond_dimension, p.seed, device,
-                               abelian=sym == N.SYM_TWOU1)
+                               abelian=sym != N.SYM_SU2U1)
         normalize_right(mps)
     left: List = [None] * (L + 1)
     right: List = [None] * (L + 1)
