@@ -480,18 +480,53 @@ gemm_f64_kernel(BufTable bufs, const DevGemmOut* __restrict__ outs, const DevGem
 }
 
 // ------------------------------------------------------------------ plan upload / run
-void free_stage_device(Stage& st) {
-    if (st.d_a) cudaFree(st.d_a);
-    if (st.d_b) cudaFree(st.d_b);
-    if (st.d_c) cudaFree(st.d_c);
-    if (st.d_tcw) cudaFree(st.d_tcw);
-    if (st.d_cw) cudaFree(st.d_cw);
-    for (void** d : {&st.d_ipanel, &st.d_ibuild, &st.d_iout, &st.d_iseg, &st.d_iunit, &st.d_igather, &st.d_icoltab,
-                     &st.d_icimg, &st.d_cw_light, &st.d_icost, &st.d_dterm, &st.d_dptr, &st.d_didx, &st.d_dw}) {
-        if (*d) cudaFree(*d);
+// Plan tables live in a memory pool of the library, one per device, and move through
+// two non-blocking streams of its own: the upload stream (allocation and copy; the
+// upload waits for this stream only, not for the caller's work) and the free stream
+// (stream-ordered frees, after events recorded at the end of the plan's runs).
+// cudaMalloc, cudaFree and cudaMemcpy each wait for the device or for the legacy
+// stream; with them a host that plans the next site problem while the device runs
+// the current boundary update waited for that update at every plan it dropped.
+struct PlanMem {
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t up = nullptr;
+    cudaStream_t fr = nullptr;
+};
+static std::mutex g_pm_mu;
+static PlanMem g_pm[64];
+static thread_local const PlanMem* t_up = nullptr;  // the target of upload_vec while qcm_plan_upload runs
+
+static int plan_mem(int dev, PlanMem** out) {
+    if (dev < 0 || dev >= 64) { set_error("device ordinal out of range"); return QCM_E_RANGE; }
+    std::lock_guard<std::mutex> lk(g_pm_mu);
+    PlanMem& m = g_pm[dev];
+    if (!m.pool) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool;
+        QCM_CUDA(cudaMemPoolCreate(&pool, &props));
+        // keep up to 4 GiB of freed tables for the next plans instead of returning them to
+        // the device at every synchronisation
+        uint64_t keep = uint64_t(4) << 30;
+        QCM_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+        if (!m.up) QCM_CUDA(cudaStreamCreateWithFlags(&m.up, cudaStreamNonBlocking));
+        if (!m.fr) QCM_CUDA(cudaStreamCreateWithFlags(&m.fr, cudaStreamNonBlocking));
+        m.pool = pool;
+    }
+    *out = &m;
+    return QCM_OK;
+}
+
+static void free_stage_device(Stage& st, cudaStream_t fr) {
+    for (void** d : {&st.d_a, &st.d_b, &st.d_c, &st.d_tcw, &st.d_cw, &st.d_ipanel, &st.d_ibuild, &st.d_iout,
+                     &st.d_iseg, &st.d_iunit, &st.d_igather, &st.d_icoltab, &st.d_icimg, &st.d_cw_light,
+                     &st.d_icost, &st.d_dterm, &st.d_dptr, &st.d_didx, &st.d_dw}) {
+        if (*d) cudaFreeAsync(*d, fr);
         *d = nullptr;
     }
-    st.d_a = st.d_b = st.d_c = st.d_tcw = st.d_cw = nullptr;
     st.n_cw = 0;
     st.n_cw_light = 0;
     if (st.ev_fork) cudaEventDestroy((cudaEvent_t)st.ev_fork);
@@ -500,12 +535,44 @@ void free_stage_device(Stage& st) {
     st.ev_fork = st.ev_join = st.side_stream = nullptr;
 }
 
+void release_plan_device(qcm_plan* p) {
+    if (p->device < 0) return;
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (cur != p->device) cudaSetDevice(p->device);
+    PlanMem* pm = nullptr;
+    if (plan_mem(p->device, &pm) == QCM_OK) {
+        if (p->captured) {
+            cudaDeviceSynchronize();
+        } else {
+            for (auto& se : p->run_ev) cudaStreamWaitEvent(pm->fr, (cudaEvent_t)se.second, 0);
+            // copies of a failed upload may still be in flight on the upload stream
+            cudaEvent_t e = nullptr;
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess) {
+                cudaEventRecord(e, pm->up);
+                cudaStreamWaitEvent(pm->fr, e, 0);
+                cudaEventDestroy(e);
+            }
+        }
+        for (auto& st : p->stages) free_stage_device(st, pm->fr);
+    }
+    for (auto& se : p->run_ev) cudaEventDestroy((cudaEvent_t)se.second);
+    p->run_ev.clear();
+    if (cur >= 0 && cur != p->device) cudaSetDevice(cur);
+}
+
+// pageable source: cudaMemcpyAsync has staged the bytes when it returns, so v may go
 template <class T, class A>
 static int upload_vec(const std::vector<T, A>& v, void** d) {
+    if (!t_up) { set_error("plan tables uploaded outside qcm_plan_upload"); return QCM_E_STATE; }
     size_t bytes = std::max<size_t>(v.size(), 1) * sizeof(T);
-    cudaError_t e = cudaMalloc(d, bytes);
-    if (e != cudaSuccess) { set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e)); return QCM_E_NOMEM; }
-    if (!v.empty()) QCM_CUDA(cudaMemcpy(*d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    cudaError_t e = cudaMallocFromPoolAsync(d, bytes, t_up->pool, t_up->up);
+    if (e != cudaSuccess) {
+        *d = nullptr;
+        set_error(std::string("cudaMallocFromPoolAsync: ") + cudaGetErrorString(e));
+        return QCM_E_NOMEM;
+    }
+    if (!v.empty()) QCM_CUDA(cudaMemcpyAsync(*d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, t_up->up));
     return QCM_OK;
 }
 
@@ -922,12 +989,21 @@ int qcm_plan_upload(qcm_plan* p) {
     if (p->uploaded) return QCM_OK;
     int dev = 0;
     QCM_CUDA(cudaGetDevice(&dev));
+    PlanMem* pm = nullptr;
+    int rc = plan_mem(dev, &pm);
+    if (rc) return rc;
+    p->device = dev;  // what a failed upload left is freed on this device
+    t_up = pm;
     for (auto& st : p->stages) {
-        int rc = upload_stage(st);
-        if (rc) return rc;
+        rc = upload_stage(st);
+        if (rc) break;
     }
+    t_up = nullptr;
+    if (rc) return rc;
+    // the tables are on the device when the upload returns (a wait for the upload
+    // stream alone), so runs need no ordering against it, captured runs included
+    QCM_CUDA(cudaStreamSynchronize(pm->up));
     p->uploaded = true;
-    p->device = dev;
     return QCM_OK;
 }
 
@@ -966,6 +1042,11 @@ int qcm_plan_run_typed(qcm_plan* p, double* const* bufs, uint32_t f32mask, int32
     for (int i = 0; i < QCM_NBUF; ++i) bt.p[i] = bufs[i];
     bt.f32mask = f32mask;
     cudaStream_t s = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    QCM_CUDA(cudaStreamIsCapturing(s, &cap));
+    // a graph keeps reading the tables after the capture: such a plan's teardown
+    // waits for the device instead of for events of its runs
+    if (cap != cudaStreamCaptureStatusNone) p->captured = true;
     p->last_kernels = 0;
     for (int32_t si = first; si <= last; ++si) {
         Stage& st = p->stages[si];
@@ -985,6 +1066,16 @@ int qcm_plan_run_typed(qcm_plan* p, double* const* bufs, uint32_t f32mask, int32
             rc = launch_gemm(st, bt, precision, s);
         }
         if (rc) return rc;
+    }
+    if (cap == cudaStreamCaptureStatusNone) {
+        cudaEvent_t ev = nullptr;
+        for (auto& se : p->run_ev)
+            if (se.first == (void*)s) { ev = (cudaEvent_t)se.second; break; }
+        if (!ev) {
+            QCM_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            p->run_ev.push_back({(void*)s, (void*)ev});
+        }
+        QCM_CUDA(cudaEventRecord(ev, s));
     }
     return QCM_OK;
 }

@@ -2651,7 +2651,7 @@ int qcm_plan_stage_gemm(const qcm_plan* p, int32_t s, int64_t* od, int64_t* sd, 
 
 void qcm_plan_destroy(qcm_plan* p) {
     if (!p) return;
-    for (auto& s : p->stages) free_stage_device(s);
+    release_plan_device(p);
     delete p;
 }
 

@@ -275,6 +275,10 @@ struct qcm_plan {
     qcm::Idx out2_phys, out2_left, out2_right;
     bool uploaded = false;
     int device = -1;
+    // (stream, event recorded on it after the plan's last run there): the teardown
+    // frees the tables once every stream has passed its event
+    std::vector<std::pair<void*, void*>> run_ev;
+    bool captured = false;  // ran inside a stream capture: the teardown waits for the device
 };
 
 namespace qcm {
@@ -290,7 +294,8 @@ double wigner6j(int, int, int, int, int, int);
 double wigner9j(int, int, int, int, int, int, int, int, int);
 void set_coupling(int a, int b, int c, int d, int e, int f, int g, int h, int i, double init, double out[4]);
 double conjugate_correction(int lc_spin, int rc_spin, int tensor_spin);
-void free_stage_device(Stage& st);
+// releases a plan's device tables (stream-ordered after its runs; see qcm_plan_destroy)
+void release_plan_device(struct ::qcm_plan* p);
 int tc_build_work(const Stage& st, std::vector<int64_t>& w);
 int tc_img_launch(const Stage& st, double* const* bufs, uint32_t f32mask, void* stream, int nprod = 6);
 int tc_launch(const void* d_out, const void* d_seg, const void* d_work, int64_t n_work, double* const* bufs,
