@@ -519,6 +519,25 @@ int qcm_plan_split_theta(const qcm_index_t* phys1, const qcm_index_t* phys2, con
 int qcm_plan_split_assemble(const qcm_plan* split, const int64_t* u_off, const int64_t* vt_off, const int64_t* keep,
                             const double* S_host, const int64_t* s_off, int32_t l2r, qcm_plan** plan);
 
+/* The product of a site tensor with a block-diagonal bond factor N, the second
+ * half of mergeUnitaryFactor (SweepBasedAlgorithms/SweepMPSUpdater.h:237-250):
+ * from_left != 0: MPSTensor::multiply_from_left (mp_tensors/mpstensor.hpp:
+ * 314-321): N . T over T's left bond (T made right-paired, N's left basis the new
+ * left index, the result back to left-paired); from_left = 0: multiply_from_right
+ * (:302-309): T . N over the right bond.  Blocks multiply where N's right charge
+ * (from_left) or left charge meets T's.  Slots: KET = T (left-paired), LEFT = N;
+ * OUT = the new tensor, left-paired (layout and indices through
+ * qcm_plan_out_tensor).  FP64 grouped products and gather maps. */
+int qcm_plan_mps_multiply(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                          const qcm_blocks_t* t, const qcm_blocks_t* n, int32_t from_left, qcm_plan** plan);
+
+/* A site tensor between its pairings (reshape_left_to_right / reshape_right_to_left,
+ * mp_tensors/reshapes.h): to_right != 0: KET left-paired -> OUT right-paired;
+ * else KET right-paired -> OUT left-paired.  The indices are unchanged; the output
+ * blocks through qcm_plan_out_tensor. */
+int qcm_plan_mps_reshape(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                         const qcm_blocks_t* t, int32_t to_right, qcm_plan** plan);
+
 /* Output tensor of an MPS-level plan: block list (q: 4 per block, rows, cols,
  * element offsets) and its three indices (physical, left, right) concatenated:
  * n_idx3[i] sectors each, charges idx_q (2 per sector) and sizes idx_size.

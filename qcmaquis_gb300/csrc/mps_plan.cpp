@@ -19,6 +19,10 @@
 //     reshape_left_to_both                       ts_reshape.h:89-145
 //   split_mps_l2r/r2l epilogue                 twositetensor.hpp:141-180
 //     A = U, B = S V (l2r) or A = U S, B = V (r2l), B reshaped right -> left
+//   mergeUnitaryFactor                         SweepBasedAlgorithms/SweepMPSUpdater.h:237-250
+//     multiply_from_left: N . T_rp, reshaped back  mpstensor.hpp:314-321
+//     multiply_from_right: T_lp . N                mpstensor.hpp:302-309
+//     the reshapes of right normalisation          mpstensor.hpp:239-258
 //
 // Every output block of a map is cleared first (a ZERO stage), so elements that
 // no tile writes read as zero, as the reference's freshly allocated blocks do.
@@ -355,6 +359,67 @@ void add_map(qcm_plan* P, const std::vector<Piece>& ps, BM& out, int32_t dbuf, i
     if (!tm.dst.empty()) P->stages.push_back(tm.stage(dbuf, P));
 }
 
+// C = A . B, block by block where A's right charge is B's left charge (the charge
+// matching of block_matrix_algorithms.h:47-80): C's blocks into cbuf (cleared first),
+// one grouped-product output per C block summing its segments in the order found.
+void add_product(qcm_plan* P, const BM& A, int32_t abuf, const BM& B, int32_t bbuf, int32_t cbuf, BM& C,
+                 int64_t& len) {
+    struct Job { size_t a, b; };
+    std::vector<Job> jobs;
+    for (size_t ka = 0; ka < A.b.size(); ++ka) {
+        const Blk& a = A.b[ka];
+        for (size_t kb = B.left_lower_bound(a.rc); kb < B.b.size() && B.b[kb].lc == a.rc; ++kb) {
+            const Blk& b = B.b[kb];
+            if (a.cols != b.rows) throw std::runtime_error("block product: inner dimensions differ");
+            if (C.find(a.lc, b.rc) == C.b.size()) {
+                Blk nb;
+                nb.lc = a.lc;
+                nb.rc = b.rc;
+                nb.rows = a.rows;
+                nb.cols = b.cols;
+                C.insert(nb);
+            }
+            jobs.push_back({ka, kb});
+        }
+    }
+    len = C.assign_offsets(0);
+    P->stages.push_back(zero_stage(cbuf, len));
+    Stage g;
+    g.kind = ST_GEMM;
+    std::vector<std::vector<GemmSeg>> segs(C.b.size());
+    for (auto& j : jobs) {
+        const Blk& a = A.b[j.a];
+        const Blk& b = B.b[j.b];
+        GemmSeg s;
+        s.a_buf = abuf;
+        s.ta = 0;
+        s.a_off = a.off;
+        s.lda = a.rows;
+        s.b_buf = bbuf;
+        s.tb = 0;
+        s.b_off = b.off;
+        s.ldb = b.rows;
+        s.K = a.cols;
+        s.alpha = 1.0;
+        segs[C.find(a.lc, b.rc)].push_back(s);
+        P->gemm_flops += 2.0 * a.rows * b.cols * a.cols;
+    }
+    for (size_t c = 0; c < C.b.size(); ++c) {
+        if (segs[c].empty()) continue;
+        GemmOut o;
+        o.c_buf = cbuf;
+        o.c_off = C.b[c].off;
+        o.ldc = C.b[c].rows;
+        o.M = C.b[c].rows;
+        o.N = C.b[c].cols;
+        o.s_begin = (int64_t)g.gseg.size();
+        for (auto& s : segs[c]) g.gseg.push_back(s);
+        o.s_end = (int64_t)g.gseg.size();
+        g.gout.push_back(o);
+    }
+    if (!g.gout.empty()) P->stages.push_back(std::move(g));
+}
+
 }  // namespace
 
 // theta of sites (i, i+1) as the reduced two-site tensor, left-paired.
@@ -575,6 +640,72 @@ qcm_plan* build_assemble(const Idx& p1, const Idx& p2, const Idx& left_i, const 
     return P.release();
 }
 
+// The product of a site tensor T (left-paired, slot KET) with a block-diagonal bond
+// factor N (slot LEFT) -- the second half of mergeUnitaryFactor.  from_left:
+// N . T over T's left bond (MPSTensor::multiply_from_left: T made right-paired,
+// the product, the left index = N's left basis, back to left-paired); else T . N
+// over its right bond (multiply_from_right: the right index = N's right basis).
+// The left (right) index of the result keeps the sectors the new bond reaches, as
+// the reference's MPSTensor constructor does.  OUT = the new tensor, left-paired.
+qcm_plan* build_multiply(const Idx& phys, const Idx& left_i, const Idx& right_i, const BM& t, const BM& n,
+                         bool from_left) {
+    auto P = std::make_unique<qcm_plan>();
+    P->kind = PK_MPS;
+    int64_t len = 0;
+    std::vector<Piece> ps;
+    if (from_left) {
+        BM rp = map_l2r(phys, left_i, right_i, t, QCM_BUF_KET, ps);
+        add_map(P.get(), ps, rp, QCM_BUF_S0, len);
+        P->scratch[0] = len;
+        BM prod;
+        add_product(P.get(), n, QCM_BUF_LEFT, rp, QCM_BUF_S0, QCM_BUF_S1, prod, len);
+        P->scratch[1] = len;
+        Idx new_left = left_basis(prod);
+        Idx right = right_i;
+        Idx reach = index_product(phys, new_left);
+        common_subset(right, reach);
+        ps.clear();
+        BM lp = map_r2l(phys, new_left, right, prod, QCM_BUF_S1, ps);
+        add_map(P.get(), ps, lp, QCM_BUF_OUT, len);
+        P->out_elems = len;
+        P->out_bm = lp.b;
+        P->out_left = new_left;
+        P->out_right = right;
+    } else {
+        BM prod;
+        add_product(P.get(), t, QCM_BUF_KET, n, QCM_BUF_LEFT, QCM_BUF_OUT, prod, len);
+        P->out_elems = len;
+        Idx new_right = right_basis(prod);
+        Idx left = left_i;
+        Idx reach = index_product(adjoin(phys), new_right);
+        common_subset(left, reach);
+        P->out_bm = prod.b;
+        P->out_left = left;
+        P->out_right = new_right;
+    }
+    P->out_phys = phys;
+    return P.release();
+}
+
+// A site tensor between its two pairings (reshape_left_to_right / reshape_right_to_left,
+// mp_tensors/reshapes.h): to_right: KET left-paired -> OUT right-paired; else KET
+// right-paired -> OUT left-paired.  Same indices in and out.
+qcm_plan* build_reshape(const Idx& phys, const Idx& left_i, const Idx& right_i, const BM& t, bool to_right) {
+    auto P = std::make_unique<qcm_plan>();
+    P->kind = PK_MPS;
+    int64_t len = 0;
+    std::vector<Piece> ps;
+    BM out = to_right ? map_l2r(phys, left_i, right_i, t, QCM_BUF_KET, ps)
+                      : map_r2l(phys, left_i, right_i, t, QCM_BUF_KET, ps);
+    add_map(P.get(), ps, out, QCM_BUF_OUT, len);
+    P->out_elems = len;
+    P->out_bm = out.b;
+    P->out_phys = phys;
+    P->out_left = left_i;
+    P->out_right = right_i;
+    return P.release();
+}
+
 }  // namespace qcm
 
 using namespace qcm;
@@ -638,11 +769,27 @@ int qcm_plan_split_assemble(const qcm_plan* split, const int64_t* u_off, const i
     }, plan);
 }
 
+int qcm_plan_mps_multiply(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                          const qcm_blocks_t* t, const qcm_blocks_t* n, int32_t from_left, qcm_plan** plan) {
+    return mps_guard("qcm_plan_mps_multiply", [&] {
+        return build_multiply(read_index(phys), read_index(left_i), read_index(right_i), read_blocks(t),
+                              read_blocks(n), from_left != 0);
+    }, plan);
+}
+
+int qcm_plan_mps_reshape(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
+                         const qcm_blocks_t* t, int32_t to_right, qcm_plan** plan) {
+    return mps_guard("qcm_plan_mps_reshape", [&] {
+        return build_reshape(read_index(phys), read_index(left_i), read_index(right_i), read_blocks(t),
+                             to_right != 0);
+    }, plan);
+}
+
 // Output tensors of an MPS-level plan: which = 0 (OUT) or 1 (the second output of
 // an assembly plan, in S2).  Call with NULL arrays for the counts.
 int qcm_plan_out_tensor(const qcm_plan* p, int32_t which, int32_t* nblocks, int32_t* q, int64_t* rows, int64_t* cols,
                         int64_t* off, int32_t* n_idx3, int32_t* idx_q, int64_t* idx_size) {
-    if (!p || (p->kind != PK_THETA && p->kind != PK_SPLIT && p->kind != PK_ASSEMBLE)) {
+    if (!p || (p->kind != PK_THETA && p->kind != PK_SPLIT && p->kind != PK_ASSEMBLE && p->kind != PK_MPS)) {
         set_error("qcm_plan_out_tensor: not an MPS-level plan");
         return QCM_E_STATE;
     }

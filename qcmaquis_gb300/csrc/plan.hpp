@@ -249,9 +249,10 @@ struct Stage {
 // PK_GRAD: gradient of <psi| H_eff |psi> with respect to every MPO term scale
 // PK_DIAG: the diagonal of H_eff (FP64 only)
 // PK_THETA: two-site tensor from two site tensors; PK_SPLIT: both-paired two-site
-// tensor from the reduced one; PK_ASSEMBLE: the site tensors of a truncated split
+// tensor from the reduced one; PK_ASSEMBLE: the site tensors of a truncated split;
+// PK_MPS: one site tensor from another (a reshape, or the product with a factor)
 enum PlanKind { PK_SIGMA = 0, PK_BLEFT = 1, PK_BRIGHT = 2, PK_GRAD = 3, PK_DIAG = 4, PK_THETA = 5, PK_SPLIT = 6,
-                PK_ASSEMBLE = 7 };
+                PK_ASSEMBLE = 7, PK_MPS = 8 };
 
 }  // namespace qcm
 

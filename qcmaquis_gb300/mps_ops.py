@@ -13,31 +13,38 @@ column-major views into the buffer.  These operations restate:
 * ``split_mps_l2r/r2l`` with ``svd_truncate``: ``twositetensor.hpp:141-180``,
   ``block_matrix/block_matrix_algorithms.h:163-333``;
 * ``leftNormalizeAndReturn`` / ``rightNormalizeAndReturn`` / ``multiply_from_*``:
-  ``mp_tensors/mpstensor.hpp:219-330``.
+  ``mp_tensors/mpstensor.hpp:219-330`` -- the batched SVD, the factor as one
+  scaling of its output, and native plans for the reshapes and the product
+  (``qcm_plan_mps_reshape``, ``qcm_plan_mps_multiply``).
 
 Dense factorisations (SVD, density-matrix eigendecomposition, the QR/LQ of the
 canonicalisation) run in the library's batched FP64 Jacobi SVD (``qcm_svd_*``)
-and the truncation cut in its device cut (``qcm_truncation_cut``); block
-products through torch.matmul.  Nothing here runs on the CPU except index
-bookkeeping.
+and the truncation cut in its device cut (``qcm_truncation_cut``); the block
+products of the density-matrix truncation through torch.matmul.  Nothing here
+runs on the CPU except index bookkeeping.
 """
 from __future__ import annotations
 
-from typing import Dict, List, Tuple
+from typing import Dict, List, Optional, Tuple
 
+import numpy as np
 import torch
 
 from . import native as N
-from .engine import DeviceMPSTensor
+from .engine import DeviceMPSTensor, _digest
 from .symmetry import Index, ProductBasis, adjoin, common_subset, fuse, fuse_neg_first, index_product, neg
 
 
 class DBM:
-    """Block matrix on the device: sorted keys, per-block tensors (views allowed)."""
+    """Block matrix on the device: sorted keys, per-block tensors (views allowed).
+    ``layout`` / ``flat``: set when the blocks are views of one flat buffer in that
+    layout (what the native plans read)."""
 
     def __init__(self):
         self.keys: List = []
         self.blocks: List[torch.Tensor] = []
+        self.layout: Optional[N.Layout] = None
+        self.flat: Optional[torch.Tensor] = None
 
     def find(self, lc, rc) -> int:
         k = (lc, rc)
@@ -480,51 +487,97 @@ def predict_new_state(u: DeviceMPSTensor, mpo, left, right, alpha: float, cutoff
     return from_dbm(phys, new_left, new_right, reshape_r2l(phys, new_left, new_right, Ut)), gemm(M, U), tr
 
 
+def _flat_dbm(layout: N.Layout, flat: torch.Tensor) -> DBM:
+    """Block views of a flat buffer that keep the buffer and its layout."""
+    d = block_views(layout, flat)
+    d.layout, d.flat = layout, flat
+    return d
+
+
+def _scale_by_s(buf: torch.Tensor, S: torch.Tensor, shapes, offs, s_off, rows: bool) -> torch.Tensor:
+    """The packed column-major blocks of ``buf`` with row t (``rows``: S Vt) or column t
+    (U S) of block i scaled by S[s_off[i] + t], as one device operation."""
+    idx = np.zeros(max(buf.numel(), 1), dtype=np.int64)
+    for (r, c), o, so in zip(shapes, offs, s_off):
+        idx[o:o + r * c] = so + (np.tile(np.arange(r), c) if rows else np.repeat(np.arange(c), r))
+    return buf * S[torch.from_numpy(idx[:buf.numel()]).to(buf.device)]
+
+
+def _run_mps_plan(key, make, device, ket, left=None) -> DeviceMPSTensor:
+    p = _RUNNER.plan(key, make)
+    phys, li, ri, lay = N.out_tensor(p)
+    out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=device)
+    _run_fp64(p, device, ket=ket, left=left, out=out)
+    return DeviceMPSTensor(phys, li, ri, lay, out[:lay.size])
+
+
 def left_normalize_and_return(t: DeviceMPSTensor) -> Tuple[DeviceMPSTensor, DBM]:
     """``leftNormalizeAndReturn`` (``mp_tensors/mpstensor.hpp:219-236``): every left-paired
     block M = Q R with Q having orthonormal columns.  The factorisation is the batched
     device SVD, Q = U and R = S Vt: the same bond dimensions and the same product Q R
     as the reference's QR, in a different (orthogonal) gauge of the new bond, which no
-    energy, overlap or truncation weight depends on."""
+    energy, overlap or truncation weight depends on.  Q is the SVD's U buffer itself
+    (packed block after block in the tensor's block order) and R one scaling of Vt."""
     svd = N.BatchedSVD(t.layout.shapes, t.layout.offsets)
     svd.run(t.data, _stream(t.data.device))
-    Q, R = DBM(), DBM()
-    for k, (lc, rc) in enumerate(t.layout.keys):
-        Q.insert(svd.u(k), lc, rc)
-        R.insert(svd.s(k)[:, None] * svd.vt(k), rc, rc)
-    new_right = Q.right_basis()
-    return from_dbm(t.phys_i, t.left_i, new_right, Q), R
+    n = len(t.layout.keys)
+    ks = [min(r, c) for r, c in t.layout.shapes]
+    q_lay = N.Layout(t.layout.keys, [(r, k) for (r, _), k in zip(t.layout.shapes, ks)])
+    r_shapes = [(k, c) for (_, c), k in zip(t.layout.shapes, ks)]
+    r_lay = N.Layout([(rc, rc) for _, rc in t.layout.keys], r_shapes)
+    assert q_lay.offsets == [int(x) for x in svd.u_off[:n]] and r_lay.offsets == [int(x) for x in svd.vt_off[:n]]
+    Rf = _scale_by_s(svd.Vt[:r_lay.size], svd.S, r_shapes, r_lay.offsets, svd.s_off[:n], rows=True)
+    new_right = Index.from_sorted([(rc, k) for (_, rc), k in zip(t.layout.keys, ks)])
+    return DeviceMPSTensor(t.phys_i, t.left_i, new_right, q_lay, svd.U[:q_lay.size]), _flat_dbm(r_lay, Rf)
 
 
 def right_normalize_and_return(t: DeviceMPSTensor) -> Tuple[DeviceMPSTensor, DBM]:
-    """``rightNormalizeAndReturn`` (``mp_tensors/mpstensor.hpp:238-258``): every
+    """``rightNormalizeAndReturn`` (``mp_tensors/mpstensor.hpp:239-258``): every
     right-paired block M = L Q with Q having orthonormal rows, from the batched device
-    SVD (L = U S, Q = Vt; the gauge remark of ``left_normalize_and_return`` applies)."""
-    rp = reshape_l2r(t.phys_i, t.left_i, t.right_i, as_dbm(t))
-    svd = batched_svd(rp)
-    Lm, Q = DBM(), DBM()
-    for k, (lc, rc) in enumerate(rp.keys):
-        Lm.insert(svd.u(k) * svd.s(k)[None, :], lc, lc)
-        Q.insert(svd.vt(k), lc, rc)
-    new_left = Q.left_basis()
-    return from_dbm(t.phys_i, new_left, t.right_i, reshape_r2l(t.phys_i, new_left, t.right_i, Q)), Lm
+    SVD (L = U S, Q = Vt; the gauge remark of ``left_normalize_and_return`` applies).
+    The reshapes are native gather plans; L is one scaling of U."""
+    dev = t.data.device
+    rp = _run_mps_plan(("rs", 1, _digest(t.phys_i, t.left_i, t.right_i, t.layout)),
+                       lambda: N.plan_mps_reshape(t.phys_i, t.left_i, t.right_i, t.layout, True), dev, t.data)
+    svd = N.BatchedSVD(rp.layout.shapes, rp.layout.offsets)
+    svd.run(rp.data, _stream(dev))
+    n = len(rp.layout.keys)
+    ks = [min(r, c) for r, c in rp.layout.shapes]
+    l_shapes = [(r, k) for (r, _), k in zip(rp.layout.shapes, ks)]
+    l_lay = N.Layout([(lc, lc) for lc, _ in rp.layout.keys], l_shapes)
+    q_lay = N.Layout(rp.layout.keys, [(k, c) for (_, c), k in zip(rp.layout.shapes, ks)])
+    assert l_lay.offsets == [int(x) for x in svd.u_off[:n]] and q_lay.offsets == [int(x) for x in svd.vt_off[:n]]
+    Lf = _scale_by_s(svd.U[:l_lay.size], svd.S, l_shapes, l_lay.offsets, svd.s_off[:n], rows=False)
+    new_left = Index.from_sorted([(lc, k) for (lc, _), k in zip(rp.layout.keys, ks)])
+    Q = _run_mps_plan(("rs", 0, _digest(t.phys_i, new_left, t.right_i, q_lay)),
+                      lambda: N.plan_mps_reshape(t.phys_i, new_left, t.right_i, q_lay, False), dev,
+                      svd.Vt[:q_lay.size])
+    return Q, _flat_dbm(l_lay, Lf)
+
+
+def _flat_of(Nm: DBM) -> DBM:
+    if Nm.flat is not None:
+        return Nm
+    lay, flat = Nm.to_flat()
+    return _flat_dbm(lay, flat)
 
 
 def multiply_from_left(t: DeviceMPSTensor, Nm: DBM) -> DeviceMPSTensor:
-    rp = reshape_l2r(t.phys_i, t.left_i, t.right_i, as_dbm(t))
-    tmp = gemm(Nm, rp)
-    new_left = tmp.left_basis()
-    right = t.right_i.copy()
-    common_subset(right, index_product(t.phys_i, new_left))
-    return from_dbm(t.phys_i, new_left, right, reshape_r2l(t.phys_i, new_left, right, tmp))
+    """``MPSTensor::multiply_from_left`` (``mp_tensors/mpstensor.hpp:314-321``): N . T
+    over the left bond, one native plan (reshape, grouped block product, reshape)."""
+    Nf = _flat_of(Nm)
+    return _run_mps_plan(("mul", 1, _digest(t.phys_i, t.left_i, t.right_i, t.layout, Nf.layout)),
+                         lambda: N.plan_mps_multiply(t.phys_i, t.left_i, t.right_i, t.layout, Nf.layout, True),
+                         t.data.device, t.data, Nf.flat)
 
 
 def multiply_from_right(t: DeviceMPSTensor, Nm: DBM) -> DeviceMPSTensor:
-    tmp = gemm(as_dbm(t), Nm)
-    new_right = tmp.right_basis()
-    left = t.left_i.copy()
-    common_subset(left, index_product(adjoin(t.phys_i), new_right))
-    return from_dbm(t.phys_i, left, new_right, tmp)
+    """``MPSTensor::multiply_from_right`` (``mp_tensors/mpstensor.hpp:302-309``): T . N
+    over the right bond, one grouped block product."""
+    Nf = _flat_of(Nm)
+    return _run_mps_plan(("mul", 0, _digest(t.phys_i, t.left_i, t.right_i, t.layout, Nf.layout)),
+                         lambda: N.plan_mps_multiply(t.phys_i, t.left_i, t.right_i, t.layout, Nf.layout, False),
+                         t.data.device, t.data, Nf.flat)
 
 
 __all__ = ["DBM", "block_views", "make_two_site_mps", "split", "svd_truncate", "heev_truncate", "add_perturbation",

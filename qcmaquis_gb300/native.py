@@ -140,6 +140,10 @@ def lib():
     L.qcm_plan_split_assemble.argtypes = [C.c_void_p, i64p, i64p, i64p, f64p, i64p, C.c_int32,
                                           C.POINTER(C.c_void_p)]
     L.qcm_plan_out_tensor.argtypes = [C.c_void_p, C.c_int32, i32p, i32p, i64p, i64p, i64p, i32p, i32p, i64p]
+    L.qcm_plan_mps_multiply.argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks)] * 2 + \
+        [C.c_int32, C.POINTER(C.c_void_p)]
+    L.qcm_plan_mps_reshape.argtypes = [C.POINTER(CIndex)] * 3 + [C.POINTER(CBlocks), C.c_int32,
+                                                                  C.POINTER(C.c_void_p)]
     L.qcm_ctx_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
     L.qcm_ctx_set_stream.argtypes = [C.c_void_p, C.c_void_p]
     L.qcm_ctx_destroy.argtypes = [C.c_void_p]
@@ -799,6 +803,27 @@ def plan_split_assemble(split: "Plan", u_off, vt_off, keep, S_host, s_off, l2r: 
     check(lib().qcm_plan_split_assemble(split.h, _p(a[0], i64p), _p(a[1], i64p), _p(a[2], i64p), _p(sv, f64p),
                                         _p(a[3], i64p), 1 if l2r else 0, C.byref(h)), "qcm_plan_split_assemble")
     return Plan(h, "assemble")
+
+
+def plan_mps_multiply(phys, left_i, right_i, t_lay: "Layout", n_lay: "Layout", from_left: bool) -> "Plan":
+    """``qcm_plan_mps_multiply``: N . T (``from_left``, ``multiply_from_left``) or T . N
+    (``multiply_from_right``) for the left-paired site tensor T (slot KET) and the
+    block-diagonal bond factor N (slot LEFT); OUT = the new tensor, left-paired."""
+    f = [FIndex(x) for x in (phys, left_i, right_i)]
+    h = C.c_void_p()
+    check(lib().qcm_plan_mps_multiply(C.byref(f[0].c), C.byref(f[1].c), C.byref(f[2].c), C.byref(t_lay.c),
+                                      C.byref(n_lay.c), 1 if from_left else 0, C.byref(h)), "qcm_plan_mps_multiply")
+    return Plan(h, "mps")
+
+
+def plan_mps_reshape(phys, left_i, right_i, lay: "Layout", to_right: bool) -> "Plan":
+    """``qcm_plan_mps_reshape``: a site tensor (slot KET) from left- to right-paired
+    (``to_right``) or back (slot OUT)."""
+    f = [FIndex(x) for x in (phys, left_i, right_i)]
+    h = C.c_void_p()
+    check(lib().qcm_plan_mps_reshape(C.byref(f[0].c), C.byref(f[1].c), C.byref(f[2].c), C.byref(lay.c),
+                                     1 if to_right else 0, C.byref(h)), "qcm_plan_mps_reshape")
+    return Plan(h, "mps")
 
 
 class CPlanOpts(C.Structure):

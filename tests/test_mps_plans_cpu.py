@@ -114,3 +114,62 @@ def test_split_assembly_matches_oracle(l2r, Mmax):
         _same_layout(ol, ref.data)
         want = ol.pack(ref.data)
         assert np.linalg.norm(buf[:ol.size] - want) <= 1e-13 * np.linalg.norm(want), which
+
+
+# ``qcm_plan_mps_multiply`` / ``qcm_plan_mps_reshape``: the two halves of
+# mergeUnitaryFactor (``sba/SweepMPSUpdater.h:237-250``) against the oracle's
+# ``multiply_from_left`` / ``multiply_from_right`` (``mt/mpstensor.hpp:302-321``)
+# and its reshapes, on the oracle's own QR / LQ factors.
+@pytest.mark.parametrize("site", [0, 2, 3])
+def test_multiply_from_left_plan_matches_oracle(site):
+    model, mps = _mps()
+    A = mps[site].copy()
+    t = R.left_normalize_and_return(A)
+    T = mps[site + 1].copy().make_left_paired()
+    lt, ln = N.Layout.of(T.data), N.Layout.of(t)
+    p = N.plan_mps_multiply(T.phys_i, T.left_i, T.right_i, lt, ln, True)
+    ref = T.copy()
+    R.multiply_from_left(ref, t)
+    ref.make_left_paired()
+    phys, left, right, lay = N.out_tensor(p)
+    assert phys == ref.phys_i and left == ref.left_i and right == ref.right_i
+    _same_layout(lay, ref.data)
+    bufs = _run(p, {0: lt.pack(T.data), 1: ln.pack(t)})
+    want = lay.pack(ref.data)
+    assert np.linalg.norm(bufs[3][:lay.size] - want) <= 1e-13 * np.linalg.norm(want)
+
+
+@pytest.mark.parametrize("site", [1, 3, 5])
+def test_multiply_from_right_plan_matches_oracle(site):
+    model, mps = _mps()
+    B = mps[site].copy()
+    lm = R.right_normalize_and_return(B)
+    T = mps[site - 1].copy().make_left_paired()
+    lt, ln = N.Layout.of(T.data), N.Layout.of(lm)
+    p = N.plan_mps_multiply(T.phys_i, T.left_i, T.right_i, lt, ln, False)
+    ref = T.copy()
+    R.multiply_from_right(ref, lm)
+    ref.make_left_paired()
+    phys, left, right, lay = N.out_tensor(p)
+    assert phys == ref.phys_i and left == ref.left_i and right == ref.right_i
+    _same_layout(lay, ref.data)
+    bufs = _run(p, {0: lt.pack(T.data), 1: ln.pack(lm)})
+    want = lay.pack(ref.data)
+    assert np.linalg.norm(bufs[3][:lay.size] - want) <= 1e-13 * np.linalg.norm(want)
+
+
+@pytest.mark.parametrize("site", [0, 2, 5])
+def test_reshape_plans_match_oracle(site):
+    model, mps = _mps()
+    T = mps[site].copy().make_left_paired()
+    lt = N.Layout.of(T.data)
+    rp = T.copy().make_right_paired()
+    p = N.plan_mps_reshape(T.phys_i, T.left_i, T.right_i, lt, True)
+    _, _, _, lay = N.out_tensor(p)
+    _same_layout(lay, rp.data)
+    got = _run(p, {0: lt.pack(T.data)})[3][:lay.size]
+    assert np.array_equal(got, lay.pack(rp.data))
+    back = N.plan_mps_reshape(T.phys_i, T.left_i, T.right_i, lay, False)
+    _, _, _, lay2 = N.out_tensor(back)
+    _same_layout(lay2, T.data)
+    assert np.array_equal(_run(back, {0: got})[3][:lay2.size], lt.pack(T.data))
