@@ -562,7 +562,11 @@ int qcm_plan_out_tensor(const qcm_plan* plan, int32_t which, int32_t* nblocks, i
  * until no pair of columns is rotated in a whole sweep (|a.b| <= sqrt(p) eps |a||b|,
  * p = max(rows, cols), the threshold of LAPACK's one-sided Jacobi);
  * a block still rotating after 40 sweeps makes qcm_svd_run return
- * QCM_E_RANGE.  min(rows, cols) <= 4096 per block. */
+ * QCM_E_RANGE.  min(rows, cols) <= 4096 per block.  A round pairs panels of
+ * bw columns, each pair rotated in shared memory (bw = 16 or 8, the widest whose
+ * panels of W and V fit for the tallest block; qcm_svd_panel_width), or single
+ * columns (bw = 0) when neither fits; qcm_svd_set_panel_width picks another width
+ * (0, 2, 4, 8, 16) before the first run (the same factorisation up to rounding). */
 typedef struct qcm_svd qcm_svd;
 int qcm_svd_create(int32_t nblocks, const int64_t* rows, const int64_t* cols, const int64_t* src_off, qcm_svd** out);
 int qcm_svd_sizes(const qcm_svd* svd, int64_t* work_elems, int64_t* u_elems, int64_t* s_elems, int64_t* vt_elems);
@@ -570,6 +574,8 @@ int qcm_svd_block_offsets(const qcm_svd* svd, int64_t* s_off, int64_t* u_off, in
 int qcm_svd_run(qcm_svd* svd, const double* src, double* work, double* U, double* S, double* Vt, void* stream);
 /* Sweeps of the widest block in the last run (host polls once per such sweep). */
 int qcm_svd_last_sweeps(const qcm_svd* svd, int32_t* sweeps);
+int qcm_svd_set_panel_width(qcm_svd* svd, int32_t bw);
+int qcm_svd_panel_width(const qcm_svd* svd, int32_t* bw);
 void qcm_svd_destroy(qcm_svd* svd);
 
 

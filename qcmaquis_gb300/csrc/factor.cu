@@ -12,9 +12,21 @@
 //   * the working matrix W (p x q, p >= q: the block, or its transpose when it
 //     has fewer rows than columns) has its columns pairwise orthogonalised by
 //     plane rotations, which are accumulated into V (q x q, starting at I);
-//   * one kernel launch is one round of a round-robin tournament over the
-//     column pairs of every block (q' - 1 rounds per sweep, q' = q rounded up
-//     to even); a warp owns one pair, so every SM works on every round;
+//   * the columns are cut into panels of bw columns (bw = 16 or 8 by default: the
+//     widest whose two panels of W and V fit in shared memory; 4 or 2 on request)
+//     and one kernel
+//     launch is one round of a round-robin tournament over the panel pairs of
+//     every block (nb' - 1 rounds per sweep, nb' = the panel count rounded up to
+//     even).  The CTA of a panel pair loads its 2 bw columns of W and of V into
+//     shared memory and rotates there the column pairs across the two panels
+//     (and, in a sweep's first round, those inside each panel) -- the same
+//     rotations, from fresh inner products of the current columns -- then writes
+//     the columns back.  Every column pair is rotated once per sweep, the work
+//     of the single-column rounds in 1/bw of their launches and traffic.  A
+//     batch whose widest block is too tall for two panels of 8 columns uses
+//     single column pairs, one warp per pair and one round per launch
+//     (q' - 1 rounds per sweep, q' = q rounded up to even).  GB300's FP64 rate
+//     bounds both forms: the panels save launches (a tenth) rather than time;
 //   * a block stops after a sweep that rotated no pair (|w_i.w_j| <= tol *
 //     |w_i| |w_j| for all pairs, tol = sqrt(p) eps as in LAPACK's dgesvj);
 //     blocks with fewer columns run more sweeps in the same launches;
@@ -64,6 +76,7 @@ constexpr double SVD_EPS = 2.220446049250313e-16;
 constexpr int SVD_ROUND_THREADS = 256;   // 8 warps, one column pair each
 constexpr int SVD_FIN_THREADS = 512;
 constexpr int SVD_SORT_MAX = 4096;       // columns per block the finishing sort holds
+constexpr int64_t SVD_PANEL_SMEM = 200 * 1024;   // shared bytes of two panels of W and of V
 constexpr int CUT_THREADS = 1024;
 constexpr int CUT_MAX = 16384;           // values the device cut sorts in shared memory
 
@@ -76,6 +89,8 @@ struct SvdBlk {
     int64_t vt_off;      // Vt: k x n, ld = k
     int64_t pair_base;   // first pair of this block in a round's flat pair list
     int32_t m, n, p, q, qpad, trans;
+    int64_t ppair_base;  // panel rounds: first panel pair of this block in a round's list
+    int32_t nb, nbpad;   // panel rounds: panels of bw columns, rounded up to even
 };
 
 // per-block state: done flag and rotation counters of three consecutive sweeps
@@ -185,6 +200,134 @@ svd_round_kernel(const SvdBlk* __restrict__ blks, const int32_t* __restrict__ pa
         vj[e] = sn * x + c * y;
     }
     if (lane == 0) atomicAdd(&s.rot[sweep % 3], 1);
+}
+
+// One round of the panel tournament for every unfinished block (see the file comment):
+// CTA = one pair (I, J) of panels of bw columns, 32 bw threads; shared memory holds
+// the 2 bw columns of W (ld = ldx >= p) and of V (ld = ldv >= q).  Every column pair
+// of a block is rotated once per sweep, as in the single-column rounds: the cross
+// pairs (a of I, b of J) in each round, bw inner rounds of the cyclic shift b = a + rr,
+// warp a owning pair a; the pairs inside a panel in the first round of a sweep, a
+// round-robin of bw - 1 inner rounds over each of I and J (warps 0 .. bw/2 - 1 on I,
+// the others on J).  The same rotation (fresh inner products, the same threshold),
+// applied to the W and V columns in shared memory; the columns go back if any rotated.
+__global__ void svd_panel_round_kernel(const SvdBlk* __restrict__ blks, const int32_t* __restrict__ pair_blk,
+                                       int64_t n_pairs, double* __restrict__ work, SvdState* __restrict__ st,
+                                       int32_t* __restrict__ remaining, int32_t* __restrict__ status, int64_t g,
+                                       int bw, int ldx, int ldv) {
+    extern __shared__ double smem[];
+    __shared__ int s_flag;
+    const int64_t cta = blockIdx.x;
+    if (cta >= n_pairs) return;
+    const int bi = pair_blk[cta];
+    const SvdBlk b = blks[bi];
+    SvdState& s = st[bi];
+    if (threadIdx.x == 0) s_flag = *(volatile int32_t*)&s.done;
+    __syncthreads();
+    if (s_flag) return;
+    const int64_t R = b.nbpad - 1;
+    const int64_t r = g % R, sweep = g / R;
+    const int64_t pidx = cta - b.ppair_base;
+    if (r == 0) {
+        // the previous sweep's rotation count is final (written by earlier launches)
+        const bool converged = sweep > 0 && s.rot[(sweep + 2) % 3] == 0;
+        const bool exhausted = sweep >= SVD_MAX_SWEEPS;
+        if (converged || exhausted) {
+            if (pidx == 0 && threadIdx.x == 0) {
+                s.done = 1;
+                s.sweeps = (int32_t)sweep;
+                atomicSub(remaining, 1);
+                if (!converged) atomicMax(status, bi + 1);
+            }
+            return;
+        }
+        if (pidx == 0 && threadIdx.x == 0) s.rot[(sweep + 1) % 3] = 0;
+    }
+    auto seat = [&](int64_t k) -> int64_t { return k == 0 ? 0 : 1 + (k - 1 + r) % R; };
+    int64_t I = seat(pidx), J = seat(b.nbpad - 1 - pidx);
+    if (I > J) { const int64_t t = I; I = J; J = t; }
+    const int nc = 2 * bw, p = b.p, q = b.q;
+    // local column c: column I bw + c of the first panel or J bw + c - bw of the second;
+    // columns at or past q (the padding panel, the last panel's tail) are absent
+    auto gcol = [&](int c) -> int64_t { return c < bw ? I * bw + c : J * bw + (c - bw); };
+    auto valid = [&](int c) -> bool { return gcol(c) < q; };
+    double* sX = smem;
+    double* sV = smem + (size_t)nc * ldx;
+    for (int c = 0; c < nc; ++c) {
+        const bool ok = valid(c);
+        const double* src = work + b.w_off + (ok ? gcol(c) : 0) * (int64_t)p;
+        for (int e = threadIdx.x; e < p; e += blockDim.x) sX[(size_t)c * ldx + e] = ok ? src[e] : 0.0;
+        const double* vsrc = work + b.v_off + (ok ? gcol(c) : 0) * (int64_t)q;
+        for (int e = threadIdx.x; e < q; e += blockDim.x) sV[(size_t)c * ldv + e] = ok ? vsrc[e] : 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_flag = 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const double thr = sqrt((double)p) * SVD_EPS;
+    bool rotated = false;
+    auto rotate = [&](int i, int j) {
+        double* __restrict__ xi = sX + (size_t)i * ldx;
+        double* __restrict__ xj = sX + (size_t)j * ldx;
+        double al = 0.0, be = 0.0, ga = 0.0;
+        for (int e = lane; e < p; e += 32) {
+            const double x = xi[e], y = xj[e];
+            al = fma(x, x, al);
+            be = fma(y, y, be);
+            ga = fma(x, y, ga);
+        }
+        al = warp_sum(al);
+        be = warp_sum(be);
+        ga = warp_sum(ga);
+        if (ga == 0.0 || fabs(ga) <= thr * sqrt(al) * sqrt(be)) return;
+        const double zeta = (be - al) / (2.0 * ga);
+        const double t = copysign(1.0, zeta) / (fabs(zeta) + hypot(1.0, zeta));
+        const double c = 1.0 / sqrt(fma(t, t, 1.0));
+        const double sn = c * t;
+        for (int e = lane; e < p; e += 32) {
+            const double x = xi[e], y = xj[e];
+            xi[e] = c * x - sn * y;
+            xj[e] = sn * x + c * y;
+        }
+        double* __restrict__ vi = sV + (size_t)i * ldv;
+        double* __restrict__ vj = sV + (size_t)j * ldv;
+        for (int e = lane; e < q; e += 32) {
+            const double x = vi[e], y = vj[e];
+            vi[e] = c * x - sn * y;
+            vj[e] = sn * x + c * y;
+        }
+        rotated = true;
+    };
+    if (r == 0 && bw > 1) {
+        // pairs inside each panel: warps [0, bw/2) on I, [bw/2, bw) on J
+        const int half = bw / 2, side = warp / half, k = warp % half, Rw = bw - 1;
+        for (int rr = 0; rr < Rw; ++rr) {
+            const int k1 = bw - 1 - k;
+            int i = k == 0 ? 0 : 1 + (k - 1 + rr) % Rw;
+            int j = 1 + (k1 - 1 + rr) % Rw;
+            if (i > j) { const int t = i; i = j; j = t; }
+            i += side * bw;
+            j += side * bw;
+            if (valid(i) && valid(j)) rotate(i, j);
+            __syncthreads();
+        }
+    }
+    // cross pairs: warp a rotates (a, bw + (a + rr) % bw)
+    for (int rr = 0; rr < bw; ++rr) {
+        const int i = warp, j = bw + (warp + rr) % bw;
+        if (valid(i) && valid(j)) rotate(i, j);
+        __syncthreads();
+    }
+    if (rotated && lane == 0) s_flag = 1;
+    __syncthreads();
+    if (!s_flag) return;
+    for (int c = 0; c < nc; ++c) {
+        if (!valid(c)) continue;
+        double* dst = work + b.w_off + gcol(c) * (int64_t)p;
+        for (int e = threadIdx.x; e < p; e += blockDim.x) dst[e] = sX[(size_t)c * ldx + e];
+        double* vdst = work + b.v_off + gcol(c) * (int64_t)q;
+        for (int e = threadIdx.x; e < q; e += blockDim.x) vdst[e] = sV[(size_t)c * ldv + e];
+    }
+    if (threadIdx.x == 0) atomicAdd(&s.rot[sweep % 3], 1);
 }
 
 // Column norms, descending sort, and U / S / Vt in gesvd's layout.
@@ -353,6 +496,11 @@ struct qcm_svd {
     std::vector<SvdBlk> blks;
     std::vector<int32_t> pair_blk;
     int64_t work_elems = 0, u_elems = 0, s_elems = 0, vt_elems = 0, n_pairs = 0, max_rounds = 0;
+    // panel rounds (bw > 0; 0: single column pairs)
+    int32_t bw = 0, ldx = 0, ldv = 0;
+    std::vector<int32_t> ppair_blk;
+    int64_t n_ppairs = 0, max_prounds = 0;
+    int32_t* d_ppair_blk = nullptr;
     SvdBlk* d_blks = nullptr;
     int32_t* d_pair_blk = nullptr;
     SvdState* d_state = nullptr;
@@ -366,8 +514,36 @@ static void svd_free(qcm_svd* s) {
     if (!s) return;
     cudaFree(s->d_blks);
     cudaFree(s->d_pair_blk);
+    cudaFree(s->d_ppair_blk);
     cudaFree(s->d_state);
     cudaFree(s->d_ctl);
+}
+
+// panel pair lists of every block with q > 1 (bw = 0: none, single column pairs run)
+static void svd_set_panels(qcm_svd* s, int32_t bw) {
+    s->bw = bw;
+    s->ppair_blk.clear();
+    s->n_ppairs = 0;
+    s->max_prounds = 0;
+    s->ldx = 0;
+    s->ldv = 0;
+    if (bw <= 0) return;
+    int64_t pairs = 0, rounds = 0;
+    for (size_t k = 0; k < s->blks.size(); ++k) {
+        SvdBlk& b = s->blks[k];
+        b.nb = (b.q + bw - 1) / bw;
+        b.nbpad = b.nb + (b.nb & 1);
+        b.ppair_base = pairs;
+        if (b.q > 1) {
+            for (int32_t p = 0; p < b.nbpad / 2; ++p) s->ppair_blk.push_back((int32_t)k);
+            pairs += b.nbpad / 2;
+            rounds = std::max<int64_t>(rounds, b.nbpad - 1);
+            s->ldx = std::max<int32_t>(s->ldx, b.p);
+            s->ldv = std::max<int32_t>(s->ldv, b.q);
+        }
+    }
+    s->n_ppairs = pairs;
+    s->max_prounds = rounds;
 }
 
 extern "C" {
@@ -424,7 +600,41 @@ int qcm_svd_create(int32_t nblocks, const int64_t* rows, const int64_t* cols, co
     s->vt_elems = vt;
     s->n_pairs = pairs;
     s->max_rounds = rounds;
+    // the widest panels whose two panels of W and of V fit in shared memory, if at
+    // least 8 columns wide: narrower panels (tall blocks) leave one CTA of few warps per
+    // SM and measured slower than single column pairs
+    int64_t pmax = 0, qmax = 0;
+    for (auto& b : s->blks)
+        if (b.q > 1) { pmax = std::max<int64_t>(pmax, b.p); qmax = std::max<int64_t>(qmax, b.q); }
+    int32_t bw = 0;
+    for (int32_t cand : {16, 8})
+        if (2 * cand * (pmax + qmax) * (int64_t)sizeof(double) <= SVD_PANEL_SMEM) { bw = cand; break; }
+    svd_set_panels(s, bw);
     *out = s;
+    return QCM_OK;
+}
+
+int qcm_svd_set_panel_width(qcm_svd* s, int32_t bw) {
+    if (!s) { set_error("null svd"); return QCM_E_INVALID; }
+    if (s->d_blks) { set_error("qcm_svd_set_panel_width: the factorisation has already run"); return QCM_E_STATE; }
+    if (bw != 0 && bw != 2 && bw != 4 && bw != 8 && bw != 16) {
+        set_error("qcm_svd_set_panel_width: width must be 0, 2, 4, 8 or 16");
+        return QCM_E_INVALID;
+    }
+    int64_t pmax = 0, qmax = 0;
+    for (auto& b : s->blks)
+        if (b.q > 1) { pmax = std::max<int64_t>(pmax, b.p); qmax = std::max<int64_t>(qmax, b.q); }
+    if (bw > 0 && 2 * bw * (pmax + qmax) * (int64_t)sizeof(double) > SVD_PANEL_SMEM) {
+        set_error("qcm_svd_set_panel_width: two panels of the tallest block exceed shared memory");
+        return QCM_E_RANGE;
+    }
+    svd_set_panels(s, bw);
+    return QCM_OK;
+}
+
+int qcm_svd_panel_width(const qcm_svd* s, int32_t* bw) {
+    if (!s || !bw) { set_error("null argument"); return QCM_E_INVALID; }
+    *bw = s->bw;
     return QCM_OK;
 }
 
@@ -461,6 +671,11 @@ int qcm_svd_run(qcm_svd* s, const double* src, double* work, double* U, double* 
             FCT_CUDA(cudaMemcpy(s->d_pair_blk, s->pair_blk.data(), sizeof(int32_t) * s->pair_blk.size(),
                                 cudaMemcpyHostToDevice));
         }
+        if (!s->ppair_blk.empty()) {
+            FCT_CUDA(cudaMalloc(&s->d_ppair_blk, sizeof(int32_t) * s->ppair_blk.size()));
+            FCT_CUDA(cudaMemcpy(s->d_ppair_blk, s->ppair_blk.data(), sizeof(int32_t) * s->ppair_blk.size(),
+                                cudaMemcpyHostToDevice));
+        }
         FCT_CUDA(cudaMalloc(&s->d_state, sizeof(SvdState) * s->blks.size()));
         FCT_CUDA(cudaMalloc(&s->d_ctl, sizeof(int32_t) * 2));
         s->device = dev;
@@ -485,11 +700,21 @@ int qcm_svd_run(qcm_svd* s, const double* src, double* work, double* U, double* 
     s->last_sweeps = 0;
     if (active > 0) {
         const unsigned grid = (unsigned)((s->n_pairs * 32 + SVD_ROUND_THREADS - 1) / SVD_ROUND_THREADS);
+        const size_t psmem = (size_t)(2 * s->bw * ((int64_t)s->ldx + s->ldv)) * sizeof(double);
+        if (s->bw > 0)
+            FCT_CUDA(cudaFuncSetAttribute(svd_panel_round_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)psmem));
+        const int64_t rounds = s->bw > 0 ? s->max_prounds : s->max_rounds;
         // rounds in chunks of one sweep of the widest block; then ask whether any block is left
         for (int chunk = 0; chunk <= SVD_MAX_SWEEPS + 1; ++chunk) {
-            for (int64_t r = 0; r < s->max_rounds; ++r, ++g) {
-                svd_round_kernel<<<grid, SVD_ROUND_THREADS, 0, st>>>(s->d_blks, s->d_pair_blk, s->n_pairs, work,
-                                                                     s->d_state, s->d_ctl, s->d_ctl + 1, g);
+            for (int64_t r = 0; r < rounds; ++r, ++g) {
+                if (s->bw > 0)
+                    svd_panel_round_kernel<<<(unsigned)s->n_ppairs, 32 * s->bw, psmem, st>>>(
+                        s->d_blks, s->d_ppair_blk, s->n_ppairs, work, s->d_state, s->d_ctl, s->d_ctl + 1, g, s->bw,
+                        s->ldx, s->ldv);
+                else
+                    svd_round_kernel<<<grid, SVD_ROUND_THREADS, 0, st>>>(s->d_blks, s->d_pair_blk, s->n_pairs, work,
+                                                                         s->d_state, s->d_ctl, s->d_ctl + 1, g);
             }
             FCT_CUDA(cudaGetLastError());
             FCT_CUDA(cudaMemcpyAsync(s->h_ctl, s->d_ctl, sizeof(int32_t) * 2, cudaMemcpyDeviceToHost, st));

@@ -23,6 +23,7 @@
 #include <functional>
 #include <map>
 #include <mutex>
+#include <numeric>
 #include <stdexcept>
 #include <thread>
 #include <tuple>
@@ -36,6 +37,32 @@ bool abelian_symmetry(int32_t symmetry) {
     if (symmetry == QCM_SYM_SU2U1) return false;
     if (symmetry == QCM_SYM_TWOU1 || symmetry == QCM_SYM_U1) return true;
     throw std::runtime_error("unknown symmetry " + std::to_string(symmetry));
+}
+
+// f(0) .. f(n - 1) on up to 16 host threads, tasks taken in order from a shared
+// counter; the first exception a task throws is rethrown here
+static void parallel_for(size_t n, const std::function<void(size_t)>& f) {
+    std::atomic<size_t> next{0};
+    std::mutex err_mu;
+    std::string err;
+    auto worker = [&]() {
+        for (;;) {
+            const size_t i = next.fetch_add(1);
+            if (i >= n) return;
+            try {
+                f(i);
+            } catch (const std::exception& ex) {
+                std::lock_guard<std::mutex> g(err_mu);
+                if (err.empty()) err = ex.what();
+            }
+        }
+    };
+    const unsigned nt = (unsigned)std::min<size_t>(n, std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto& th : pool) th.join();
+    if (!err.empty()) throw std::runtime_error(err);
 }
 
 // A-resident mode for single-segment stages (K1).  Off: measured slower at the
@@ -1488,22 +1515,19 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
         s1.gout.push_back(o);
         P->gemm_flops += 2.0 * c.rows * c.cols * a.cols;
     }
-    // rbtm tasks into buf[b1](out_l, out_r)
-    using TileKey = std::tuple<int, Q, Q, int64_t>;  // b1, out_l, out_r, col offset
-    struct TileKeyLess {
-        bool operator()(const TileKey& a, const TileKey& b) const {
-            if (std::get<0>(a) != std::get<0>(b)) return std::get<0>(a) < std::get<0>(b);
-            if (std::get<1>(a) != std::get<1>(b)) return std::get<1>(a) > std::get<1>(b);
-            if (std::get<2>(a) != std::get<2>(b)) return std::get<2>(a) > std::get<2>(b);
-            return std::get<3>(a) < std::get<3>(b);
-        }
-    };
-    struct TileVal { int64_t rows, cols; std::vector<AxpyTerm> terms; };
-    std::map<TileKey, TileVal, TileKeyLess> tiles;
+    // rbtm tasks into buf[b1](out_l, out_r), one host task per b1: its terms in loop
+    // order, each keyed by its tile (out_l, out_r, column offset), then stably ordered
+    // by tile as the reference's block order (both charges descending, offsets
+    // ascending); the tiles go out in b1 order
+    struct RTerm { Q out_l, out_r; int64_t col, rows, cols; AxpyTerm t; };
+    struct RowOut { std::vector<RTerm> terms; std::vector<uint32_t> order; double flops = 0.0; };
+    std::vector<RowOut> rows_out(m->row_dim);
     std::vector<BM> buf(m->row_dim);
     MpoV const& Wv = W;
-    for (int b1 = 0; b1 < m->row_dim; ++b1) {
-        if (herm && !tensor_mpo && Wv.lskip(b1)) continue;
+    parallel_for((size_t)m->row_dim, [&](size_t b1s) {
+        const int b1 = (int)b1s;
+        if (herm && !tensor_mpo && Wv.lskip(b1)) return;
+        RowOut& ro = rows_out[b1];
         int a = Wv.lspin(b1);
         for (size_t r = 0; r < Wv.row_b2[b1].size(); ++r) {
             int b2 = Wv.row_b2[b1][r];
@@ -1538,24 +1562,18 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
                             int ss1 = m->ent[4 * en], ss2 = m->ent[4 * en + 1];
                             double alfa = m->ent_coeff[en] * cpl[spin_case(m->ent[4 * en + 2], m->ent[4 * en + 3])];
                             if (alfa == 0.0) continue;
-                            TileKey key(b1, out_l, out_r, oro + (int64_t)ss2 * r_size);
-                            auto& tv = tiles[key];
-                            tv.rows = l_size;
-                            tv.cols = r_size;
-                            tv.terms.push_back({QCM_BUF_S1, tb.off + ilo + (int64_t)ss1 * l_size, tb.rows, alfa});
-                            P->axpy_flops += 2.0 * l_size * r_size;
+                            ro.terms.push_back({out_l, out_r, oro + (int64_t)ss2 * r_size, l_size, r_size,
+                                                {QCM_BUF_S1, tb.off + ilo + (int64_t)ss1 * l_size, tb.rows, alfa}});
+                            ro.flops += 2.0 * l_size * r_size;
                         }
                     }
                 }
             }
         }
-    }
-    if (Wv.abelian()) {
-        // rbtm_kernel_allocate (ct/abelian/apply_op.hpp:140-187): for every (b2, operator)
-        // of the row with a non-empty t[b2], one block per left sector at the constant
-        // charge shifts, whether or not a term writes it (zero, but part of the layout)
-        for (int b1 = 0; b1 < m->row_dim; ++b1) {
-            if (herm && !tensor_mpo && Wv.lskip(b1)) continue;
+        if (Wv.abelian()) {
+            // rbtm_kernel_allocate (ct/abelian/apply_op.hpp:140-187): for every (b2, operator)
+            // of the row with a non-empty t[b2], one block per left sector at the constant
+            // charge shifts, whether or not a term writes it (zero, but part of the layout)
             for (size_t r = 0; r < Wv.row_b2[b1].size(); ++r) {
                 const int b2 = Wv.row_b2[b1][r], e = Wv.row_elem[b1][r];
                 if (t[b2].b.empty()) continue;
@@ -1577,26 +1595,52 @@ static qcm_plan* build_bright(const Idx& phys, const Idx& left_i, const Idx& rig
                 }
             }
         }
-    }
+        ro.order.resize(ro.terms.size());
+        std::iota(ro.order.begin(), ro.order.end(), 0u);
+        const std::vector<RTerm>& ts = ro.terms;
+        std::stable_sort(ro.order.begin(), ro.order.end(), [&](uint32_t x, uint32_t y) {
+            const RTerm &u = ts[x], &v = ts[y];
+            if (!(u.out_l == v.out_l)) return u.out_l > v.out_l;
+            if (!(u.out_r == v.out_r)) return u.out_r > v.out_r;
+            return u.col < v.col;
+        });
+    });
     int64_t b_end = 0;
     for (auto& x : buf) b_end = x.assign_offsets(b_end);
     const int32_t buf_slot = tensor_mpo ? QCM_BUF_OUT : QCM_BUF_S2;
     Stage z2; z2.kind = ST_ZERO; z2.zbuf = buf_slot; z2.zlen = b_end;
     Stage s2; s2.kind = ST_AXPY;
-    for (auto& kv : tiles) {
-        int b1 = std::get<0>(kv.first);
-        const Blk& d = buf[b1].b[buf[b1].find(std::get<1>(kv.first), std::get<2>(kv.first))];
-        AxpyOut o;
-        o.dst_buf = buf_slot;
-        o.dst_off = d.off + std::get<3>(kv.first) * d.rows;
-        o.ldd = d.rows;
-        o.rows = kv.second.rows;
-        o.cols = kv.second.cols;
-        o.t_begin = (int64_t)s2.aterm.size();
-        for (auto& x : kv.second.terms) s2.aterm.push_back(x);
-        o.t_end = (int64_t)s2.aterm.size();
-        s2.aout.push_back(o);
-        P->axpy_bytes += 8.0 * o.rows * o.cols * (double)(kv.second.terms.size() + 1);
+    {
+        size_t nterms = 0;
+        for (const RowOut& ro : rows_out) nterms += ro.terms.size();
+        s2.aterm.reserve(nterms);
+    }
+    for (int b1 = 0; b1 < m->row_dim; ++b1) {
+        const RowOut& ro = rows_out[b1];
+        P->axpy_flops += ro.flops;
+        for (size_t g0 = 0; g0 < ro.order.size();) {
+            const RTerm& k0 = ro.terms[ro.order[g0]];
+            size_t g1 = g0 + 1;
+            while (g1 < ro.order.size()) {
+                const RTerm& k1 = ro.terms[ro.order[g1]];
+                if (!(k1.out_l == k0.out_l) || !(k1.out_r == k0.out_r) || k1.col != k0.col) break;
+                ++g1;
+            }
+            const Blk& d = buf[b1].b[buf[b1].find(k0.out_l, k0.out_r)];
+            const RTerm& last = ro.terms[ro.order[g1 - 1]];
+            AxpyOut o;
+            o.dst_buf = buf_slot;
+            o.dst_off = d.off + k0.col * d.rows;
+            o.ldd = d.rows;
+            o.rows = last.rows;
+            o.cols = last.cols;
+            o.t_begin = (int64_t)s2.aterm.size();
+            for (size_t g = g0; g < g1; ++g) s2.aterm.push_back(ro.terms[ro.order[g]].t);
+            o.t_end = (int64_t)s2.aterm.size();
+            s2.aout.push_back(o);
+            P->axpy_bytes += 8.0 * o.rows * o.cols * (double)(g1 - g0 + 1);
+            g0 = g1;
+        }
     }
     if (tensor_mpo) {
         P->out_blk_ptr.assign(1, 0);

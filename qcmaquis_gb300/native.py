@@ -160,6 +160,8 @@ def lib():
     L.qcm_svd_block_offsets.argtypes = [C.c_void_p, i64p, i64p, i64p]
     L.qcm_svd_run.argtypes = [C.c_void_p] + [C.c_void_p] * 6
     L.qcm_svd_last_sweeps.argtypes = [C.c_void_p, i32p]
+    L.qcm_svd_set_panel_width.argtypes = [C.c_void_p, C.c_int32]
+    L.qcm_svd_panel_width.argtypes = [C.c_void_p, i32p]
     L.qcm_svd_destroy.argtypes = [C.c_void_p]
     L.qcm_svd_destroy.restype = None
     L.qcm_truncation_cut.argtypes = [C.c_void_p, C.c_int32, i64p, C.c_int64, C.c_double, C.c_int32, i64p,
@@ -198,7 +200,7 @@ class BatchedSVD:
     U, S, Vt packed block after block; ``u(k)``, ``s(k)``, ``vt(k)`` are views of block
     k (U: rows x k_k, S: k_k descending, Vt: k_k x cols)."""
 
-    def __init__(self, shapes, offsets):
+    def __init__(self, shapes, offsets, panel_width=None):
         self.shapes = [(int(r), int(c)) for r, c in shapes]
         n = len(self.shapes)
         rows = np.array([r for r, _ in self.shapes] or [0], dtype=np.int64)
@@ -207,6 +209,8 @@ class BatchedSVD:
         h = C.c_void_p()
         check(lib().qcm_svd_create(n, _p(rows, i64p), _p(cols, i64p), _p(offs, i64p), C.byref(h)), "qcm_svd_create")
         self.h = h
+        if panel_width is not None:
+            check(lib().qcm_svd_set_panel_width(h, int(panel_width)), "qcm_svd_set_panel_width")
         w, u, sv, vt = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
         check(lib().qcm_svd_sizes(h, C.byref(w), C.byref(u), C.byref(sv), C.byref(vt)), "qcm_svd_sizes")
         self.sizes = (w.value, u.value, sv.value, vt.value)
@@ -249,6 +253,12 @@ class BatchedSVD:
         k = min(r, c)
         o = int(self.vt_off[i])
         return self.Vt[o:o + k * c].view(c, k).t()
+
+    def panel_width(self) -> int:
+        """Columns per panel of the tournament rounds (0: single column pairs)."""
+        bw = C.c_int32()
+        check(lib().qcm_svd_panel_width(self.h, C.byref(bw)), "qcm_svd_panel_width")
+        return bw.value
 
     def sweeps(self) -> int:
         n = C.c_int32()

@@ -30,15 +30,63 @@ def _blocks(seed=0, grade=10.0):
     return out
 
 
-def _run(blocks):
+def _run(blocks, panel_width=None):
     from qcmaquis_gb300 import native as N
     offs = np.cumsum([0] + [b.size for b in blocks])
     flat = np.concatenate([np.ravel(b, order="F") for b in blocks] + [np.zeros(1)])
     src = torch.tensor(flat, dtype=torch.float64, device="cuda")
-    svd = N.BatchedSVD([b.shape for b in blocks], offs[:-1])
+    svd = N.BatchedSVD([b.shape for b in blocks], offs[:-1], panel_width=panel_width)
     svd.run(src, torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     return svd
+
+
+def _check_svd(svd, blocks):
+    for k, a in enumerate(blocks):
+        r, c = a.shape
+        if min(r, c) == 0:
+            continue
+        U, S, Vt = svd.u(k).cpu().numpy(), svd.s(k).cpu().numpy(), svd.vt(k).cpu().numpy()
+        ref = np.linalg.svd(a, compute_uv=False)
+        s0 = ref[0]
+        assert np.all(np.diff(S) <= 0), k
+        assert np.max(np.abs(S - ref)) <= 1e-13 * s0, (k, np.max(np.abs(S - ref)) / s0)
+        big = ref > 1e-6 * s0
+        assert np.max(np.abs(S[big] - ref[big]) / ref[big]) <= 1e-12, k
+        assert np.linalg.norm(U @ np.diag(S) @ Vt - a) <= 1e-13 * np.linalg.norm(a), k
+        nz = S > 1e-13 * s0
+        assert np.allclose(U[:, nz].T @ U[:, nz], np.eye(int(nz.sum())), atol=1e-12), k
+        assert np.allclose(Vt[nz] @ Vt[nz].T, np.eye(int(nz.sum())), atol=1e-12), k
+
+
+
+@pytest.mark.parametrize("bw", [0, 2, 4, 8, 16])
+def test_every_panel_width_matches_lapack(bw):
+    """The panel rounds (bw columns per panel, each panel pair swept in shared memory)
+    and the single-column rounds (bw = 0) give the same factorisation: graded,
+    rank-deficient and tall / wide blocks, column counts that are not multiples of
+    the panel width, one batch."""
+    rng = np.random.default_rng(5)
+    blocks = _blocks(seed=2)
+    if bw == 16:
+        # two 16-column panels of W and V of a 460 x 451 block exceed shared memory
+        blocks = [a if a.shape != (460, 451) else rng.standard_normal((230, 180)) for a in blocks]
+    # exactly rank 3 and rank 40 blocks (the rest of the spectrum is rounding)
+    blocks.append(rng.standard_normal((50, 3)) @ rng.standard_normal((3, 37)))
+    blocks.append(rng.standard_normal((200, 40)) @ rng.standard_normal((40, 90)))
+    svd = _run(blocks, panel_width=bw)
+    assert svd.panel_width() == bw
+    assert 1 <= svd.sweeps() <= 40
+    _check_svd(svd, blocks)
+
+
+def test_default_panel_width_is_the_widest_that_fits():
+    from qcmaquis_gb300 import native as N
+    assert N.BatchedSVD([(200, 150), (5, 3)], [0, 200 * 150]).panel_width() == 16
+    assert N.BatchedSVD([(460, 451), (5, 3)], [0, 460 * 451]).panel_width() == 8
+    assert N.BatchedSVD([(1200, 40)], [0]).panel_width() == 8
+    assert N.BatchedSVD([(5000, 30)], [0]).panel_width() == 0
+    assert N.BatchedSVD([(20000, 3)], [0]).panel_width() == 0
 
 
 def test_batched_svd_matches_lapack():
