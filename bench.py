@@ -43,6 +43,9 @@ def parse():
     ap.add_argument("--nsweeps", type=int, default=1, help="--sweep: number of sweeps")
     ap.add_argument("--forms", default="", help="--sweep: comma-separated forms (fp64, mixed, mixed_parts, "
                     "fp64_parts, fp64_heev, mixed_heev; default fp64,mixed,mixed_parts)")
+    ap.add_argument("--kernel-profile", action="store_true",
+                    help="--sweep: run the forms under torch.profiler (CUDA activity) and report device seconds "
+                         "and launches per kernel (timings of such a run are not benchmark values)")
     ap.add_argument("--plan-cache", type=int, default=0,
                     help="--sweep: sigma plans kept, keyed by layouts (0: the engine default of 2)")
     ap.add_argument("--ramp", default="", help="--sweep: bond dimension per sweep, e.g. 256,256,512,512,1024,1024")
@@ -298,9 +301,24 @@ def run_sweep(args):
         if args.shadow:
             from qcmaquis_gb300.engine import Engine
             shadow = Engine("cuda", precision=0)
+        prof = None
+        if args.kernel_profile:
+            from torch.profiler import ProfilerActivity, profile
+            prof = profile(activities=[ProfilerActivity.CUDA])
+            prof.__enter__()
         rec, _ = run_dmrg(model, mpo, p, nelec, mps=mps, precision=prec, ts_mpo=ts, boundary_precision=bprec,
                           time_parts=time_parts, plan_cache=args.plan_cache, shadow=shadow)
         torch.cuda.synchronize()
+        kernels = None
+        if prof is not None:
+            prof.__exit__(None, None, None)
+            kernels = {}
+            for a in prof.key_averages():
+                dt = getattr(a, "self_device_time_total", None)
+                if dt is None:
+                    dt = getattr(a, "self_cuda_time_total", 0.0)
+                if dt and dt > 0:
+                    kernels[a.key.split("(")[0]] = [round(dt / 1e6, 4), int(a.count)]
         out[name] = {"sweep_s": rec.sweep_seconds[-1], "sweep_seconds": rec.sweep_seconds, "wall_s": time.time() - t1,
                      "energy": rec.sweep_energy[-1], "sweep_energies": rec.sweep_energy,
                      "last_micro_energy": rec.energies[-1], "sigma_calls": rec.sigma_calls,
@@ -310,6 +328,8 @@ def run_sweep(args):
                      "plan_hits": rec.plan_hits,
                      "boundary_plan_hits": rec.boundary_plan_hits,
                      "microiterations": len(rec.layout_digests)}
+        if kernels is not None:
+            out[name]["kernel_device_s"] = dict(sorted(kernels.items(), key=lambda kv: -kv[1][0]))
         if rec.shadow:
             sh = np.array(rec.shadow)
             out[name]["shadow"] = {
