@@ -231,6 +231,68 @@ void qcm_mpo_buf_destroy(qcm_mpo_buf* buf);
 int qcm_mpo_twosite(const qcm_mpo_t* w1, const qcm_mpo_t* w2, const qcm_index_t* phys1, const qcm_index_t* phys2,
                     qcm_mpo_buf** out);
 
+/* Single-site MPO tensors from the model's terms (TaggedMPOMaker,
+ * dmrg/framework/dmrg/models/generate_mpo/tagged_mpo_maker_optim.hpp:
+ * add_term / add_generic_term with their fork keys and filling strings,
+ * :168-187, :472-560, :594-638; finalize, :640-669; create_mpo with the bond
+ * numbering in key order, the bond spins and the Hermitian bond pairs, :189-300,
+ * with the phases of conjugate_key, :671-735).
+ *
+ * The tag table describes the operators the terms name: per tag whether it is
+ * fermionic, its spin (2S, action) -- two int32 per tag --, its Hermitian
+ * conjugate tag and pdiff = N(in) - N(out) of its first block (the particle
+ * number change the SU(2) bond phases read); and the tags of the identity, the
+ * identity of spin > 1 bonds and the fermionic filling.
+ *
+ * qcm_mpo_maker_add_terms takes terms of two or more operators, CSR style
+ * (term t = positions/tags [term_ptr[t], term_ptr[t+1]), sorted by position
+ * inside the call, stable), with the coefficient on the operator the reference
+ * attaches it to and a caller label per term (-1: none) carried to that scale.
+ * One-site terms are the caller's (they need its operator algebra): it passes
+ * each site's (TL, TR) element list to qcm_mpo_maker_site_terms, then
+ * qcm_mpo_maker_finish with the final tag table (site operators registered
+ * since create added), the smallest last position and the largest first
+ * position over all terms (one-site terms included).  qcm_mpo_maker_site views
+ * one site's tensor, valid until qcm_mpo_maker_destroy: elements column-major,
+ * each element's (tag, scale, label) terms in the reference's MPOTensor order
+ * (latest insertion first), the outgoing bonds' spins (2S, action), Hermitian
+ * partners and phases (bond_dim entries; the incoming bonds' are the previous
+ * site's).  row_dim / col_dim are 1 at the chain ends. */
+typedef struct {
+    int32_t n_tags;
+    const int32_t* fermionic;  /* n_tags */
+    const int32_t* spin;       /* 2 * n_tags: (2S, action) */
+    const int32_t* herm_conj;  /* n_tags */
+    const int32_t* pdiff;      /* n_tags */
+    int32_t identity, identity_full, fill;
+    int32_t symmetry;          /* QCM_SYM_*: abelian groups pair bonds with phase 1 */
+} qcm_tag_table_t;
+
+typedef struct {
+    int32_t row_dim, col_dim, bond_dim;
+    int32_t n_elem;
+    const int32_t* elem_b1;    /* n_elem */
+    const int32_t* elem_b2;    /* n_elem */
+    const int32_t* elem_ptr;   /* n_elem + 1, into the term arrays */
+    const int32_t* term_tag;
+    const double* term_scale;
+    const int32_t* term_label;
+    const int32_t* right_spin; /* 2 * bond_dim */
+    const int32_t* right_herm; /* bond_dim */
+    const int32_t* right_phase;/* bond_dim */
+} qcm_mpo_site_t;
+
+typedef struct qcm_mpo_maker qcm_mpo_maker;
+int qcm_mpo_maker_create(int32_t L, const qcm_tag_table_t* tags, qcm_mpo_maker** out);
+int qcm_mpo_maker_add_terms(qcm_mpo_maker* maker, int32_t n_terms, const int32_t* term_ptr, const int32_t* pos,
+                            const int32_t* tag, const double* coeff, const int32_t* label);
+int qcm_mpo_maker_site_terms(qcm_mpo_maker* maker, int32_t site, int32_t n, const int32_t* tag, const double* scale,
+                             const int32_t* label);
+int qcm_mpo_maker_finish(qcm_mpo_maker* maker, const qcm_tag_table_t* tags, int32_t leftmost_right,
+                         int32_t rightmost_left);
+int qcm_mpo_maker_site(const qcm_mpo_maker* maker, int32_t site, qcm_mpo_site_t* view);
+void qcm_mpo_maker_destroy(qcm_mpo_maker* maker);
+
 /* Diagonal of H_eff (Engine::diagonal_hamiltonian, dmrg/framework/dmrg/mp_tensors/
  * contractions/non-abelian/engine.hpp:221-226 -> SU2::diagonal_hamiltonian,
  * non-abelian/h_diag.hpp:118-158), the arguments of qcm_plan_sigma without

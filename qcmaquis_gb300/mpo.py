@@ -13,6 +13,7 @@
 """
 from __future__ import annotations
 
+import itertools
 from typing import Dict, List, Optional, Tuple
 
 import numpy as np
@@ -110,6 +111,43 @@ class MPOTensor:
             self.herm = Hermitian.identity(ld, rd)
         self._sparse_cache: Dict[int, list] = {}
 
+    @classmethod
+    def from_elements(cls, ld: int, rd: int, op_table: List[SiteOperator], herm: Optional[Hermitian],
+                      left_spins: List[SpinDescriptor], right_spins: List[SpinDescriptor], elem_b1, elem_b2, elem_ptr,
+                      term_tag, term_scale, term_label) -> "MPOTensor":
+        """The tensor from column-major elements whose term lists are already in
+        this class's order (as the native maker writes them); the same object
+        the constructor builds from the equivalent entry list."""
+        t = cls.__new__(cls)
+        t.row_dim, t.col_dim = ld, rd
+        t.op_table = op_table
+        t.left_spins = list(left_spins)
+        t.right_spins = list(right_spins)
+        terms = list(zip(term_tag, term_scale))
+        labs = [None if x < 0 else x for x in term_label]
+        keys = list(zip(elem_b1, elem_b2))
+        ptr = elem_ptr
+        t.elements = {k: terms[ptr[e]:ptr[e + 1]] for e, k in enumerate(keys)}
+        t.labels = {k: labs[ptr[e]:ptr[e + 1]] for e, k in enumerate(keys)}
+        b1 = np.asarray(elem_b1, dtype=np.int64)
+        b2 = np.asarray(elem_b2, dtype=np.int64)
+        cb = np.searchsorted(b2, np.arange(rd + 1)).tolist()          # elements are column-major
+        t.cols = [elem_b1[cb[c]:cb[c + 1]] for c in range(rd)]
+        order = np.lexsort((b2, b1))
+        rb = np.searchsorted(b1[order], np.arange(ld + 1)).tolist()
+        by_row = b2[order].tolist()
+        t.row_index = [set(by_row[rb[r]:rb[r + 1]]) for r in range(ld)]
+        t.row_nnz = np.bincount(b1, minlength=ld).tolist()
+        t.col_nnz = np.bincount(b2, minlength=rd).tolist()
+        t.num_one_rows = sum(1 for x in t.row_nnz if x == 1)
+        t.num_one_cols = sum(1 for x in t.col_nnz if x == 1)
+        if herm is not None and len(herm.LeftHerm) == ld and len(herm.RightHerm) == rd:
+            t.herm = herm
+        else:
+            t.herm = Hermitian.identity(ld, rd)
+        t._sparse_cache = {}
+        return t
+
     def has(self, b1, b2) -> bool:
         return (b1, b2) in self.elements
 
@@ -153,7 +191,7 @@ class TaggedMPOMaker:
     each term's coefficient must stay a separate MPO scale, as for gradients).
     Every coefficient-carrying scale is labelled with its model term's index."""
 
-    def __init__(self, model: QCModel, merge_site_terms: bool = True):
+    def __init__(self, model: QCModel, merge_site_terms: bool = True, native: bool = True):
         self.L = model.L
         self.symmetry = getattr(model, "symmetry", "su2u1")
         self.th: TagHandler = model.tag_handler
@@ -170,10 +208,43 @@ class TaggedMPOMaker:
         self.site_term_lists: Dict[int, list] = {}
         self.core_labels: List[int] = []
         self._label = None
-        for idx, t in enumerate(model.terms):
-            self._label = idx
-            self.add_term(t)
+        self.native = native
+        if native:
+            self._collect_native(model)
+        else:
+            for idx, t in enumerate(model.terms):
+                self._label = idx
+                self.add_term(t)
         self._label = None
+
+    def _collect_native(self, model: QCModel):
+        """The native maker's input: one-site terms are added here (they need the
+        operator algebra), the terms of two or more operators are flattened for
+        ``qcm_mpo_maker_add_terms``."""
+        ptr, flat, coeff, label = [0], [], [], []
+        lr, rl = self.L, 0
+        for idx, t in enumerate(model.terms):
+            ops = t.ops
+            if len(ops) == 1:
+                self._label = idx
+                self._add_1term(t)
+                p = ops[0][0]
+                lr, rl = min(lr, p), max(rl, p)
+                continue
+            flat.extend(ops)
+            ptr.append(len(flat))
+            coeff.append(t.coeff)
+            label.append(idx)
+        pt = np.fromiter(itertools.chain.from_iterable(flat), dtype=np.int32, count=2 * len(flat)).reshape(-1, 2)
+        pos, tag = np.ascontiguousarray(pt[:, 0]), np.ascontiguousarray(pt[:, 1])
+        if len(coeff):
+            starts = np.asarray(ptr[:-1], dtype=np.int64)
+            lr = min(lr, int(np.maximum.reduceat(pos, starts).min()))
+            rl = max(rl, int(np.minimum.reduceat(pos, starts).max()))
+        self._native_terms = (np.asarray(ptr, dtype=np.int32), pos, tag, np.asarray(coeff, dtype=np.float64),
+                              np.asarray(label, dtype=np.int32))
+        self.leftmost_right, self.rightmost_left = lr, rl
+        self._native_terms = (ptr, pos, tag, coeff, label)
 
     # -- prempo helpers ------------------------------------------------------
     def _insert(self, p, kk, val, attach):
@@ -329,7 +400,38 @@ class TaggedMPOMaker:
                 phase = (-1, -1)
         return conj, phase
 
+    def _create_native(self) -> MPO:
+        """create_mpo through the native maker (``qcm_mpo_maker_*``): the same
+        tensors as the Python restatement below, element for element."""
+        from . import native as N
+        site_terms = {}
+        for p in sorted(self.site_terms):
+            site_terms[p] = [(self.th.register_op(self.site_terms[p], 0), 1.0, None)]
+        for p in sorted(self.site_term_lists):
+            site_terms[p] = list(self.site_term_lists[p])
+        self.finalized = True
+        tags = N.FTagTable(self.th, self.identity, self.identity_full, self.filling, self.symmetry)
+        sites = N.mpo_maker_sites(self.L, tags, self._native_terms, site_terms, self.leftmost_right,
+                                  self.rightmost_left)
+        mpo = MPO()
+        table = self.th.ops
+        left_spins = [SpinDescriptor()]
+        LeftHerm, LeftPhase = [0], [1]
+        for (ld, rd, eb1, eb2, eptr, ttag, tscale, tlabel, rspin, rherm, rphase) in sites:
+            right_spins = [SpinDescriptor.raw(a, b) for a, b in rspin]
+            h = Hermitian(LeftHerm, rherm, LeftPhase, rphase)
+            t = MPOTensor.from_elements(ld, rd, table, h, left_spins, right_spins, eb1, eb2, eptr, ttag, tscale,
+                                        tlabel)
+            t.symmetry = self.symmetry
+            mpo.append(t)
+            left_spins, LeftHerm, LeftPhase = right_spins, rherm, rphase
+        mpo.core_energy = self.core_energy
+        mpo.core_labels = list(self.core_labels)
+        return mpo
+
     def create_mpo(self) -> MPO:
+        if self.native:
+            return self._create_native()
         if not self.finalized:
             self._finalize()
         mpo = MPO()

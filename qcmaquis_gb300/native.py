@@ -48,6 +48,18 @@ class CMpo(C.Structure):
                 ("blk_ent_ptr", i32p), ("ent", i32p), ("ent_coeff", f64p), ("symmetry", C.c_int32)]
 
 
+class CTagTable(C.Structure):
+    _fields_ = [("n_tags", C.c_int32), ("fermionic", i32p), ("spin", i32p), ("herm_conj", i32p), ("pdiff", i32p),
+                ("identity", C.c_int32), ("identity_full", C.c_int32), ("fill", C.c_int32), ("symmetry", C.c_int32)]
+
+
+class CMpoSite(C.Structure):
+    _fields_ = [("row_dim", C.c_int32), ("col_dim", C.c_int32), ("bond_dim", C.c_int32), ("n_elem", C.c_int32),
+                ("elem_b1", i32p), ("elem_b2", i32p), ("elem_ptr", i32p), ("term_tag", i32p),
+                ("term_scale", f64p), ("term_label", i32p), ("right_spin", i32p), ("right_herm", i32p),
+                ("right_phase", i32p)]
+
+
 # symmetry groups of qcm_mpo_t.symmetry and the MPS-level plans
 SYM_SU2U1, SYM_TWOU1, SYM_U1 = 0, 1, 2
 
@@ -99,6 +111,13 @@ def lib():
                                   C.POINTER(C.c_void_p)]
     L.qcm_mpo_buf_destroy.argtypes = [C.c_void_p]
     L.qcm_mpo_buf_destroy.restype = None
+    L.qcm_mpo_maker_create.argtypes = [C.c_int32, C.POINTER(CTagTable), C.POINTER(C.c_void_p)]
+    L.qcm_mpo_maker_add_terms.argtypes = [C.c_void_p, C.c_int32, i32p, i32p, i32p, f64p, i32p]
+    L.qcm_mpo_maker_site_terms.argtypes = [C.c_void_p, C.c_int32, C.c_int32, i32p, f64p, i32p]
+    L.qcm_mpo_maker_finish.argtypes = [C.c_void_p, C.POINTER(CTagTable), C.c_int32, C.c_int32]
+    L.qcm_mpo_maker_site.argtypes = [C.c_void_p, C.c_int32, C.POINTER(CMpoSite)]
+    L.qcm_mpo_maker_destroy.argtypes = [C.c_void_p]
+    L.qcm_mpo_maker_destroy.restype = None
     L.qcm_plan_merge.argtypes = [C.POINTER(C.c_void_p), C.c_int32, i64p, C.POINTER(C.c_void_p)]
     L.qcm_plan_sizes.argtypes = [C.c_void_p, i64p, i64p]
     L.qcm_plan_image_bytes.argtypes = [C.c_void_p, i64p]
@@ -509,6 +528,72 @@ def _copy(ptr, n, dtype):
     if n <= 0:
         return np.zeros(1, dtype=dtype)
     return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+
+class FTagTable:
+    """The operator table a term list names, as the native MPO maker reads it
+    (``qcm_tag_table_t``): per tag fermionic, spin (2S, action), Hermitian
+    conjugate and the particle-number change of its first block."""
+
+    def __init__(self, th, identity: int, identity_full: int, fill: int, symmetry: str):
+        from .symmetry import particle_number
+        n = len(th.ops)
+        self.ferm = np.array([1 if th.is_fermionic(t) else 0 for t in range(n)], dtype=np.int32)
+        self.spin = np.array([(op.spin.get(), op.spin.action()) for op in th.ops], dtype=np.int32).reshape(-1)
+        self.herm = np.array([th.herm_conj(t) for t in range(n)], dtype=np.int32)
+        pd = []
+        for op in th.ops:
+            keys = op.bm.keys
+            pd.append(particle_number(keys[0][0]) - particle_number(keys[0][1]) if keys else 0)
+        self.pdiff = np.array(pd, dtype=np.int32)
+        self.c = CTagTable(n, _p(self.ferm, i32p), _p(self.spin, i32p), _p(self.herm, i32p), _p(self.pdiff, i32p),
+                           identity, identity_full, fill, symmetry_code(symmetry))
+
+
+def mpo_maker_sites(L_sites: int, tags: FTagTable, terms, site_terms, leftmost_right: int, rightmost_left: int):
+    """Single-site MPO tensors from the native maker (``qcm_mpo_maker_*``).
+
+    ``terms`` = (term_ptr, pos, tag, coeff, label) arrays of the terms of two or
+    more operators; ``site_terms`` = {site: [(tag, scale, label or None), ...]}.
+    Returns per site (row_dim, col_dim, elem_b1, elem_b2, elem_ptr, term_tag,
+    term_scale, term_label, right_spin (bond_dim x 2), right_herm, right_phase),
+    the arrays as Python lists."""
+    L = lib()
+    h = C.c_void_p()
+    check(L.qcm_mpo_maker_create(L_sites, C.byref(tags.c), C.byref(h)), "qcm_mpo_maker_create")
+    try:
+        ptr = np.ascontiguousarray(terms[0], dtype=np.int32)
+        pos = np.ascontiguousarray(terms[1], dtype=np.int32)
+        tag = np.ascontiguousarray(terms[2], dtype=np.int32)
+        coeff = np.ascontiguousarray(terms[3], dtype=np.float64)
+        label = np.ascontiguousarray(terms[4], dtype=np.int32)
+        if len(coeff):
+            check(L.qcm_mpo_maker_add_terms(h, len(coeff), _p(ptr, i32p), _p(pos, i32p), _p(tag, i32p),
+                                            _p(coeff, f64p), _p(label, i32p)), "qcm_mpo_maker_add_terms")
+        for site in sorted(site_terms):
+            ents = site_terms[site]
+            st = np.array([e[0] for e in ents], dtype=np.int32)
+            ss = np.array([e[1] for e in ents], dtype=np.float64)
+            sl = np.array([-1 if e[2] is None else e[2] for e in ents], dtype=np.int32)
+            check(L.qcm_mpo_maker_site_terms(h, site, len(ents), _p(st, i32p), _p(ss, f64p), _p(sl, i32p)),
+                  "qcm_mpo_maker_site_terms")
+        check(L.qcm_mpo_maker_finish(h, C.byref(tags.c), leftmost_right, rightmost_left), "qcm_mpo_maker_finish")
+        out = []
+        for p in range(L_sites):
+            v = CMpoSite()
+            check(L.qcm_mpo_maker_site(h, p, C.byref(v)), "qcm_mpo_maker_site")
+            ne, nb = v.n_elem, v.bond_dim
+            eptr = _copy(v.elem_ptr, ne + 1, np.int32)
+            nt = int(eptr[-1])
+            out.append((v.row_dim, v.col_dim, _copy(v.elem_b1, ne, np.int32)[:ne].tolist(),
+                        _copy(v.elem_b2, ne, np.int32)[:ne].tolist(), eptr.tolist(),
+                        _copy(v.term_tag, nt, np.int32)[:nt].tolist(), _copy(v.term_scale, nt, np.float64)[:nt].tolist(),
+                        _copy(v.term_label, nt, np.int32)[:nt].tolist(),
+                        _copy(v.right_spin, 2 * nb, np.int32)[:2 * nb].reshape(-1, 2).tolist(),
+                        _copy(v.right_herm, nb, np.int32)[:nb].tolist(), _copy(v.right_phase, nb, np.int32)[:nb].tolist()))
+        return out
+    finally:
+        L.qcm_mpo_maker_destroy(h)
 
 
 def make_twosite_fmpo(w1: FMpo, w2: FMpo, phys1: Index, phys2: Index = None, native_kron: bool = False) -> FMpo:
