@@ -600,6 +600,28 @@ int qcm_plan_mps_multiply(const qcm_index_t* phys, const qcm_index_t* left_i, co
 int qcm_plan_mps_reshape(const qcm_index_t* phys, const qcm_index_t* left_i, const qcm_index_t* right_i,
                          const qcm_blocks_t* t, int32_t to_right, qcm_plan** plan);
 
+/* Charge-matched product of two block matrices, OUT = op(A) op(B) with op the
+ * transpose where ta / tb != 0 (block_matrix gemm and transpose,
+ * dmrg/framework/dmrg/block_matrix/block_matrix_algorithms.h:47-80, :118-128):
+ * every pair of blocks whose inner charges agree adds its product to the output
+ * block (left charge of op(A), right charge of op(B)).  A in slot KET, B in slot
+ * LEFT; output blocks through qcm_plan_out_tensor (indices empty).  FP64; run
+ * with qcm_plan_run / qcm_ctx_run.  Used for the products of the density-matrix
+ * truncation: U^T theta, theta U. */
+int qcm_plan_block_gemm(const qcm_blocks_t* a, int32_t ta, const qcm_blocks_t* b, int32_t tb, qcm_plan** plan);
+
+/* Density matrix of the heev truncation (TwoSiteTensor::predict_split_l2r/r2l,
+ * dmrg/framework/dmrg/mp_tensors/twositetensor.hpp:184-297; predict_new_state_*,
+ * mp_tensors/contractions/common/prediction.hpp:19-125): OUT = theta theta^T (l2r,
+ * theta left-paired) or theta^T theta (r2l, theta right-paired), theta in slot KET;
+ * with alpha != 0 and half != NULL, plus alpha sum_b h_b h_b^T (l2r) or
+ * alpha sum_b h_b^T h_b (r2l) over the boundary tensor product h in slot RIGHT
+ * (qcm_plan_boundary_tensor_mpo's output): per bond b, every pair of h[b]'s blocks
+ * sharing their right (l2r) / left (r2l) charge whose output charges (ci, cj) are
+ * a block of theta.  Output blocks through qcm_plan_out_tensor.  FP64. */
+int qcm_plan_density_matrix(const qcm_blocks_t* theta, int32_t l2r, const qcm_boundary_t* half, double alpha,
+                            qcm_plan** plan);
+
 /* Output tensor of an MPS-level plan: block list (q: 4 per block, rows, cols,
  * element offsets) and its three indices (physical, left, right) concatenated:
  * n_idx3[i] sectors each, charges idx_q (2 per sector) and sizes idx_size.

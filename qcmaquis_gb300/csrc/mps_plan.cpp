@@ -27,6 +27,7 @@
 // Every output block of a map is cleared first (a ZERO stage), so elements that
 // no tile writes read as zero, as the reference's freshly allocated blocks do.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <functional>
 #include <map>
@@ -706,6 +707,175 @@ qcm_plan* build_reshape(const Idx& phys, const Idx& left_i, const Idx& right_i, 
     return P.release();
 }
 
+// Output blocks of a grouped product, created on first use; every block's
+// segments are summed in the order they were added (one zero stage, then one
+// grouped GEMM stage; blocks no segment writes stay zero).
+namespace {
+struct ProductOut {
+    BM C;
+    std::map<std::array<int32_t, 4>, std::vector<GemmSeg>> segs;
+    double flops = 0.0;
+
+    void add(Q lc, Q rc, int64_t rows, int64_t cols, const GemmSeg& s) {
+        const size_t k = C.find(lc, rc);
+        if (k == C.b.size()) {
+            Blk nb;
+            nb.lc = lc;
+            nb.rc = rc;
+            nb.rows = rows;
+            nb.cols = cols;
+            C.insert(nb);
+        } else if (C.b[k].rows != rows || C.b[k].cols != cols) {
+            throw std::runtime_error("block product: products of one output block differ in shape");
+        }
+        segs[{lc.n, lc.s, rc.n, rc.s}].push_back(s);
+        flops += 2.0 * rows * cols * s.K;
+    }
+
+    qcm_plan* finish() {
+        auto P = std::make_unique<qcm_plan>();
+        P->kind = PK_MPS;
+        const int64_t len = C.assign_offsets(0);
+        P->stages.push_back(zero_stage(QCM_BUF_OUT, len));
+        Stage g;
+        g.kind = ST_GEMM;
+        for (const Blk& c : C.b) {
+            const auto& v = segs[{c.lc.n, c.lc.s, c.rc.n, c.rc.s}];
+            if (v.empty() || c.rows == 0 || c.cols == 0) continue;
+            GemmOut o;
+            o.c_buf = QCM_BUF_OUT;
+            o.c_off = c.off;
+            o.ldc = c.rows;
+            o.M = c.rows;
+            o.N = c.cols;
+            o.s_begin = (int64_t)g.gseg.size();
+            for (const GemmSeg& x : v)
+                if (x.K > 0) g.gseg.push_back(x);
+            o.s_end = (int64_t)g.gseg.size();
+            if (o.s_end > o.s_begin) g.gout.push_back(o);
+        }
+        if (!g.gout.empty()) P->stages.push_back(std::move(g));
+        P->gemm_flops = flops;
+        P->out_elems = len;
+        P->out_bm = C.b;
+        return P.release();
+    }
+};
+
+GemmSeg seg(int32_t abuf, const Blk& a, bool ta, int32_t bbuf, const Blk& b, bool tb, int64_t K, double alpha) {
+    GemmSeg s;
+    s.a_buf = abuf;
+    s.ta = ta ? 1 : 0;
+    s.a_off = a.off;
+    s.lda = a.rows;
+    s.b_buf = bbuf;
+    s.tb = tb ? 1 : 0;
+    s.b_off = b.off;
+    s.ldb = b.rows;
+    s.K = K;
+    s.alpha = alpha;
+    return s;
+}
+}  // namespace
+
+// The charge-matched product of two block matrices, op(A) op(B) with op a
+// transpose where asked (block_matrix gemm, block_matrix/block_matrix_algorithms.h:
+// 47-80, with transpose(), :118-128): every pair of blocks whose inner charges
+// agree adds its product to the output block (left charge of op(A), right charge
+// of op(B)).  A in slot KET, B in slot LEFT, the product in OUT (blocks in DualIndex
+// order, through qcm_plan_out_tensor).  Pairs are taken in A's order, then B's.
+qcm_plan* build_block_gemm(const BM& A, bool ta, const BM& B, bool tb) {
+    ProductOut out;
+    // op(B) blocks by their left charge, in B's order
+    std::map<std::pair<int, int>, std::vector<size_t>> by_left;
+    for (size_t k = 0; k < B.b.size(); ++k) {
+        const Q l = tb ? B.b[k].rc : B.b[k].lc;
+        by_left[{l.n, l.s}].push_back(k);
+    }
+    for (const Blk& a : A.b) {
+        const Q al = ta ? a.rc : a.lc, ar = ta ? a.lc : a.rc;
+        const int64_t am = ta ? a.cols : a.rows, ak = ta ? a.rows : a.cols;
+        auto it = by_left.find({ar.n, ar.s});
+        if (it == by_left.end()) continue;
+        for (size_t kb : it->second) {
+            const Blk& b = B.b[kb];
+            const Q br = tb ? b.lc : b.rc;
+            const int64_t bk = tb ? b.cols : b.rows, bn = tb ? b.rows : b.cols;
+            if (ak != bk) throw std::runtime_error("block product: inner dimensions differ");
+            out.add(al, br, am, bn, seg(QCM_BUF_KET, a, ta, QCM_BUF_LEFT, b, tb, ak, 1.0));
+        }
+    }
+    return out.finish();
+}
+
+// The density matrix of the heev truncation (TwoSiteTensor::predict_split_l2r /
+// _r2l, mp_tensors/twositetensor.hpp:184-297, and predict_new_state_l2r/r2l_sweep,
+// contractions/common/prediction.hpp:19-125): rho = theta theta^T (l2r, theta
+// left-paired) or theta^T theta (r2l, theta right-paired), theta in slot KET;
+// with alpha != 0, plus alpha sum_b h_b h_b^T (l2r) or alpha sum_b h_b^T h_b (r2l)
+// over the blocks of the boundary tensor product h (left/right_boundary_tensor_mpo,
+// slot RIGHT): for every bond b, the pairs of h[b]'s blocks that share their right
+// charge (l2r) or left charge (r2l), restricted to the output charges (ci, cj)
+// that theta holds as a block, and added to rho(ci, cj), created if absent.
+qcm_plan* build_density_matrix(const BM& theta, bool l2r, const std::vector<BM>* half, double alpha) {
+    ProductOut out;
+    if (l2r) {
+        // rho(ci, cj) = sum over rc of theta(ci, rc) theta(cj, rc)^T, in the order of
+        // theta's blocks and, for one rc, of decreasing cj
+        std::map<std::pair<int, int>, std::vector<size_t>> by_right;
+        for (size_t k = 0; k < theta.b.size(); ++k) by_right[{theta.b[k].rc.n, theta.b[k].rc.s}].push_back(k);
+        for (const Blk& a : theta.b)
+            for (size_t kb : by_right[{a.rc.n, a.rc.s}]) {
+                const Blk& b = theta.b[kb];
+                out.add(a.lc, b.lc, a.rows, b.rows, seg(QCM_BUF_KET, a, false, QCM_BUF_KET, b, true, a.cols, 1.0));
+            }
+    } else {
+        // rho(ci, cj) = sum over lc of theta(lc, ci)^T theta(lc, cj): the transposed
+        // blocks in their own order (decreasing (rc, lc)), then theta's with that lc
+        std::vector<size_t> order(theta.b.size());
+        for (size_t k = 0; k < order.size(); ++k) order[k] = k;
+        std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+            const Blk& a = theta.b[x];
+            const Blk& b = theta.b[y];
+            return a.rc > b.rc || (a.rc == b.rc && a.lc > b.lc);
+        });
+        for (size_t ka : order) {
+            const Blk& a = theta.b[ka];
+            for (size_t kb = theta.left_lower_bound(a.lc); kb < theta.b.size() && theta.b[kb].lc == a.lc; ++kb) {
+                const Blk& b = theta.b[kb];
+                out.add(a.rc, b.rc, a.cols, b.cols, seg(QCM_BUF_KET, a, true, QCM_BUF_KET, b, false, a.rows, 1.0));
+            }
+        }
+    }
+    if (alpha != 0.0 && half) {
+        for (const BM& hb : *half) {
+            // groups of blocks with one right (l2r) / left (r2l) charge, in order of first appearance
+            std::vector<std::pair<Q, std::vector<size_t>>> groups;
+            for (size_t k = 0; k < hb.b.size(); ++k) {
+                const Q g = l2r ? hb.b[k].rc : hb.b[k].lc;
+                auto it = std::find_if(groups.begin(), groups.end(), [&](const auto& x) { return x.first == g; });
+                if (it == groups.end()) groups.push_back({g, {k}});
+                else it->second.push_back(k);
+            }
+            for (const auto& grp : groups)
+                for (size_t i : grp.second)
+                    for (size_t j : grp.second) {
+                        const Blk& vi = hb.b[i];
+                        const Blk& vj = hb.b[j];
+                        const Q ci = l2r ? vi.lc : vi.rc, cj = l2r ? vj.lc : vj.rc;
+                        if (theta.find(ci, cj) == theta.b.size()) continue;
+                        if (l2r)
+                            out.add(ci, cj, vi.rows, vj.rows,
+                                    seg(QCM_BUF_RIGHT, vi, false, QCM_BUF_RIGHT, vj, true, vi.cols, alpha));
+                        else
+                            out.add(ci, cj, vi.cols, vj.cols,
+                                    seg(QCM_BUF_RIGHT, vi, true, QCM_BUF_RIGHT, vj, false, vi.rows, alpha));
+                    }
+        }
+    }
+    return out.finish();
+}
+
 }  // namespace qcm
 
 using namespace qcm;
@@ -782,6 +952,20 @@ int qcm_plan_mps_reshape(const qcm_index_t* phys, const qcm_index_t* left_i, con
     return mps_guard("qcm_plan_mps_reshape", [&] {
         return build_reshape(read_index(phys), read_index(left_i), read_index(right_i), read_blocks(t),
                              to_right != 0);
+    }, plan);
+}
+
+int qcm_plan_block_gemm(const qcm_blocks_t* a, int32_t ta, const qcm_blocks_t* b, int32_t tb, qcm_plan** plan) {
+    return mps_guard("qcm_plan_block_gemm", [&] { return build_block_gemm(read_blocks(a), ta != 0, read_blocks(b), tb != 0); },
+                     plan);
+}
+
+int qcm_plan_density_matrix(const qcm_blocks_t* theta, int32_t l2r, const qcm_boundary_t* half, double alpha,
+                            qcm_plan** plan) {
+    return mps_guard("qcm_plan_density_matrix", [&] {
+        std::vector<BM> h;
+        if (half && alpha != 0.0) h = read_boundary(half);
+        return build_density_matrix(read_blocks(theta), l2r != 0, (half && alpha != 0.0) ? &h : nullptr, alpha);
     }, plan);
 }
 

@@ -330,7 +330,7 @@ BM read_blocks(const qcm_blocks_t* x) {
     }
     return r;
 }
-static std::vector<BM> read_boundary(const qcm_boundary_t* x) {
+std::vector<BM> read_boundary(const qcm_boundary_t* x) {
     if (!x) throw std::runtime_error("null boundary");
     std::vector<BM> r(x->aux);
     for (int b = 0; b < x->aux; ++b) {

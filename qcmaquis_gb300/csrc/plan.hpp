@@ -286,6 +286,9 @@ namespace qcm {
 void set_error(const std::string& msg);
 Idx read_index(const qcm_index_t* x);
 BM read_blocks(const qcm_blocks_t* x);
+std::vector<BM> read_boundary(const qcm_boundary_t* x);
+qcm_plan* build_block_gemm(const BM& a, bool ta, const BM& b, bool tb);
+qcm_plan* build_density_matrix(const BM& theta, bool l2r, const std::vector<BM>* half, double alpha);
 qcm_plan* build_split(const Idx& p1, const Idx& p2, const Idx& left_i, const Idx& right_i, const BM& u,
                       bool abelian);
 qcm_plan* build_assemble(const Idx& p1, const Idx& p2, const Idx& left_i, const Idx& right_i, const BM& both,

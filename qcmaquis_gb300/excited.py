@@ -21,7 +21,7 @@ from typing import List, Sequence
 import torch
 
 from .engine import DeviceMPSTensor
-from .mps_ops import DBM, _transpose, as_dbm, block_views, gemm, make_two_site_mps, reshape_l2r, reshape_r2l
+from .mps_ops import DBM, as_dbm, block_views, gemm, make_two_site_mps, reshape_l2r, reshape_r2l
 from .symmetry import Index, ProductBasis, fuse, neg
 
 
@@ -37,15 +37,15 @@ def overlap_left_step(bra: DeviceMPSTensor, ket: DeviceMPSTensor, left: DBM) -> 
     ket_rp = reshape_l2r(ket.phys_i, ket.left_i, ket.right_i, as_dbm(ket))
     t1 = gemm(left, ket_rp)
     t3 = reshape_r2l(ket.phys_i, bra.left_i, ket.right_i, t1)
-    return gemm(_transpose(as_dbm(bra)), t3)
+    return gemm(as_dbm(bra), t3, ta=True)
 
 
 def overlap_right_step(bra: DeviceMPSTensor, ket: DeviceMPSTensor, right: DBM) -> DBM:
     """``common::overlap_right_step`` (``ct/common/move_boundary.hpp:45-62``)."""
-    t1 = gemm(as_dbm(ket), _transpose(right))
+    t1 = gemm(as_dbm(ket), right, tb=True)
     t3 = reshape_l2r(ket.phys_i, ket.left_i, bra.right_i, t1)
     bra_rp = reshape_l2r(bra.phys_i, bra.left_i, bra.right_i, as_dbm(bra))
-    return gemm(bra_rp, _transpose(t3))
+    return gemm(bra_rp, t3, tb=True)
 
 
 def _pad_left(phys: Index, in_left_i: Index, in_right_i: Index, psi: DeviceMPSTensor, m1: DBM) -> torch.Tensor:
@@ -78,7 +78,7 @@ def site_ortho_boundaries(psi: DeviceMPSTensor, theta: DeviceMPSTensor, o_left: 
     t = gemm(o_left, reshape_l2r(theta.phys_i, theta.left_i, theta.right_i, as_dbm(theta)))
     li = o_left.left_basis()
     t2 = reshape_r2l(psi.phys_i, li, theta.right_i, t)
-    t3 = gemm(t2, _transpose(o_right))
+    t3 = gemm(t2, o_right, tb=True)
     return _pad_left(psi.phys_i, li, o_right.left_basis(), psi, t3)
 
 

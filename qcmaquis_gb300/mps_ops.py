@@ -20,8 +20,9 @@ column-major views into the buffer.  These operations restate:
 Dense factorisations (SVD, density-matrix eigendecomposition, the QR/LQ of the
 canonicalisation) run in the library's batched FP64 Jacobi SVD (``qcm_svd_*``)
 and the truncation cut in its device cut (``qcm_truncation_cut``); the block
-products of the density-matrix truncation through torch.matmul.  Nothing here
-runs on the CPU except index bookkeeping.
+products of the density-matrix truncation (rho with its noise term, U^T theta,
+theta U) in native grouped FP64 block products (``qcm_plan_density_matrix``,
+``qcm_plan_block_gemm``).  Nothing here runs on the CPU except index bookkeeping.
 """
 from __future__ import annotations
 
@@ -110,22 +111,36 @@ def block_views(layout: N.Layout, flat: torch.Tensor) -> DBM:
     return d
 
 
-def gemm(A: DBM, B: DBM) -> DBM:
-    """Charge-matched block product (``block_matrix_algorithms.h:47-80``)."""
-    C = DBM()
-    for k, (ka, a) in enumerate(zip(A.keys, A.blocks)):
-        ar = ka[1]
-        it = B.left_lower_bound(ar)
-        while it < len(B.keys) and B.keys[it][0] == ar:
-            lc, rc = ka[0], B.keys[it][1]
-            prod = a @ B.blocks[it]
-            p = C.find(lc, rc)
-            if p < len(C.keys):
-                C.blocks[p] = C.blocks[p] + prod
-            else:
-                C.insert(prod, lc, rc)
-            it += 1
-    return C
+def gemm(A: DBM, B: DBM, ta: bool = False, tb: bool = False) -> DBM:
+    """Charge-matched block product op(A) op(B), op the transpose where asked
+    (``block_matrix_algorithms.h:47-80``): one native grouped FP64 block product
+    (``qcm_plan_block_gemm``).  The result's blocks are views of one flat buffer."""
+    Af, Bf = _flat_of(A), _flat_of(B)
+    dev = Af.flat.device
+    key = ("gemm", bool(ta), bool(tb), _digest(Af.layout), _digest(Bf.layout))
+    p = _RUNNER.plan(key, lambda: N.plan_block_gemm(Af.layout, ta, Bf.layout, tb))
+    _, _, _, lay = N.out_tensor(p)
+    out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=dev)
+    _run_fp64(p, dev, ket=Af.flat, left=Bf.flat, out=out)
+    return _flat_dbm(lay, out)
+
+
+def density_matrix(M: DBM, l2r: bool, half=None, alpha: float = 0.0) -> DBM:
+    """rho = M M^T (``l2r``) or M^T M, plus alpha sum_b h_b h_b^T (or h_b^T h_b) over the
+    blocks of ``half`` (the device boundary of ``left/right_boundary_tensor_mpo``)
+    whose charges M holds (``twositetensor.hpp:195-221, 255-281``,
+    ``ct/common/prediction.hpp:19-125``): one native grouped FP64 block product
+    (``qcm_plan_density_matrix``)."""
+    Mf = _flat_of(M)
+    dev = Mf.flat.device
+    noisy = half is not None and alpha != 0.0
+    hl = half.layout if noisy else None
+    key = ("dm", bool(l2r), _digest(Mf.layout), _digest(hl) if noisy else None, float(alpha) if noisy else 0.0)
+    p = _RUNNER.plan(key, lambda: N.plan_density_matrix(Mf.layout, l2r, hl, alpha if noisy else 0.0))
+    _, _, _, lay = N.out_tensor(p)
+    out = torch.empty(max(p.out_elems, 1), dtype=torch.float64, device=dev)
+    _run_fp64(p, dev, ket=Mf.flat, right=half.data if noisy else None, out=out)
+    return _flat_dbm(lay, out)
 
 
 # ------------------------------------------------------------------ reshapes
@@ -180,7 +195,7 @@ def from_dbm(phys: Index, left_i: Index, right_i: Index, lp: DBM, layout_like=No
 
 
 def as_dbm(t: DeviceMPSTensor) -> DBM:
-    return block_views(t.layout, t.data)
+    return _flat_dbm(t.layout, t.data)
 
 
 class _PlanRunner:
@@ -214,11 +229,11 @@ class _PlanRunner:
 _RUNNER = _PlanRunner()
 
 
-def _run_fp64(plan, device, ket=None, left=None, out=None, s2=None):
+def _run_fp64(plan, device, ket=None, left=None, out=None, s2=None, right=None):
     s0, s1, s2w = _RUNNER.scratch(device, plan.scratch)
     ptr = lambda t: 0 if t is None else int(t.data_ptr())
-    plan.run_typed([ptr(ket), ptr(left), 0, ptr(out), ptr(s0), ptr(s1), ptr(s2 if s2 is not None else s2w), 0], 0,
-                   N.PREC_FP64, _stream(device))
+    plan.run_typed([ptr(ket), ptr(left), ptr(right), ptr(out), ptr(s0), ptr(s1),
+                    ptr(s2 if s2 is not None else s2w), 0], 0, N.PREC_FP64, _stream(device))
 
 
 def make_two_site_mps(A: DeviceMPSTensor, B: DeviceMPSTensor, symmetry: int = N.SYM_SU2U1) -> DeviceMPSTensor:
@@ -267,8 +282,8 @@ def batched_svd(M: DBM):
     """FP64 SVD of every block of M in one batch on the GPU (``qcm_svd_*``, one-sided
     Jacobi, hand-written; replaces the per-block LAPACK gesvd/heevd/geqrf of the
     reference).  Returns the ``native.BatchedSVD`` with U, S (descending), Vt."""
-    lay, flat = M.to_flat()
-    svd = N.BatchedSVD([tuple(b.shape) for b in M.blocks], lay.offsets)
+    lay, flat = (M.layout, M.flat) if M.flat is not None else M.to_flat()
+    svd = N.BatchedSVD(lay.shapes, lay.offsets)
     svd.run(flat, _stream(flat.device))
     return svd
 
@@ -302,15 +317,17 @@ def heev_truncate(dm: DBM, cutoff: float, Mmax: int):
     returned in both weight fields, as the reference does."""
     svd = batched_svd(dm)
     keep, tr = svd.cut(Mmax, cutoff, 1, _stream(svd.S.device))
-    U = DBM()
+    keys, shapes, offs = [], [], []
     S: Dict = {}
     for k, (key, kk) in enumerate(zip(dm.keys, keep)):
         kk = int(kk)
         if kk == 0:
             continue
-        lc, rc = key
-        U.insert(svd.u(k)[:, :kk], lc, rc)
-        S[rc] = svd.s(k)[:kk]
+        keys.append(key)
+        shapes.append((dm.blocks[k].shape[0], kk))   # the first kk columns of U (ld = rows)
+        offs.append(int(svd.u_off[k]))
+        S[key[1]] = svd.s(k)[:kk]
+    U = _flat_dbm(N.Layout(keys, shapes, offs), svd.U)
     return U, S, Trunc(int(tr.bond_dimension), tr.truncated_fraction, tr.truncated_fraction, tr.smallest_ev)
 
 
@@ -319,65 +336,6 @@ def _transpose(M: DBM) -> DBM:
     for (lc, rc), b in zip(M.keys, M.blocks):
         T.insert(b.t(), rc, lc)
     return T
-
-
-# concatenated operand size of one perturbation product (elements)
-_PERTURB_CHUNK = 1 << 26
-
-
-def add_perturbation(dm: DBM, both: DBM, half, alpha: float, l2r: bool):
-    """dm += alpha sum_b h_b h_b^T (l2r) or alpha sum_b h_b^T h_b (r2l) on the blocks
-    whose charges theta holds (``twositetensor.hpp:195-221, 255-281``).  ``half`` is
-    the device boundary of ``left/right_boundary_tensor_mpo``.  Products that land
-    on one dm block are summed as one GEMM over the concatenated h blocks."""
-    keys = set(both.keys)
-    diag: Dict = {}
-    cross: List = []
-    lay = half.layout
-    for b in range(lay.aux):
-        groups: Dict = {}
-        for k in range(lay.blk_ptr[b], lay.blk_ptr[b + 1]):
-            (lc, rc), (r, c), o = lay.keys[k], lay.shapes[k], lay.offsets[k]
-            v = half.data[o:o + r * c].view(c, r).t()
-            # l2r pairs blocks of one column charge; r2l blocks of one row charge
-            groups.setdefault(rc if l2r else lc, []).append((lc if l2r else rc, v))
-        for g in groups.values():
-            for i, (ci, vi) in enumerate(g):
-                for cj, vj in g:
-                    if (ci, cj) not in keys:
-                        continue
-                    if vi is vj:
-                        diag.setdefault(ci, []).append(vi)
-                    else:
-                        cross.append((ci, cj, vi, vj))
-    for c, vs in diag.items():
-        p = dm.find(c, c)
-        if p == len(dm.keys):
-            n = vs[0].shape[0] if l2r else vs[0].shape[1]
-            p = dm.insert(torch.zeros((n, n), dtype=torch.float64, device=vs[0].device), c, c)
-        dst = dm.blocks[p]
-        i = 0
-        while i < len(vs):
-            j, n = i, 0
-            while j < len(vs) and (j == i or n + vs[j].numel() <= _PERTURB_CHUNK):
-                n += vs[j].numel()
-                j += 1
-            X = torch.cat(vs[i:j], dim=1 if l2r else 0)
-            if l2r:
-                dst.addmm_(X, X.t(), alpha=alpha)
-            else:
-                dst.addmm_(X.t(), X, alpha=alpha)
-            i = j
-    for ci, cj, vi, vj in cross:
-        p = dm.find(ci, cj)
-        if p == len(dm.keys):
-            r = vi.shape[0] if l2r else vi.shape[1]
-            cdim = vj.shape[0] if l2r else vj.shape[1]
-            p = dm.insert(torch.zeros((r, cdim), dtype=torch.float64, device=vi.device), ci, cj)
-        if l2r:
-            dm.blocks[p].addmm_(vi, vj.t(), alpha=alpha)
-        else:
-            dm.blocks[p].addmm_(vi.t(), vj, alpha=alpha)
 
 
 def split(u: DeviceMPSTensor, A0: DeviceMPSTensor, B0: DeviceMPSTensor, Mmax: int, cutoff: float, l2r: bool,
@@ -411,10 +369,9 @@ def split(u: DeviceMPSTensor, A0: DeviceMPSTensor, B0: DeviceMPSTensor, Mmax: in
         pb, lb, rb, lay_b = N.out_tensor(ap, 1)
         return (DeviceMPSTensor(pa, la, ra, lay_a, a_out), DeviceMPSTensor(pb, lb, rb, lay_b, b_out),
                 Trunc(int(tr.bond_dimension), tr.truncated_weight, tr.truncated_fraction, tr.smallest_ev))
-    both = block_views(blay, bflat)
+    both = _flat_dbm(blay, bflat)
     if truncation in ("heev", "heev_truncation"):
-        bt = _transpose(both)
-        dm = gemm(both, bt) if l2r else gemm(bt, both)
+        half = None
         if alpha != 0.0 and boundary is not None:
             if engine is None or mpo is None:
                 raise ValueError("the heev perturbation needs the engine and the site's MPO tensor")
@@ -432,13 +389,13 @@ def split(u: DeviceMPSTensor, A0: DeviceMPSTensor, B0: DeviceMPSTensor, Mmax: in
                 common_subset(t_right, index_product(p2, t_left))
                 tmp = from_dbm(p2, t_left, t_right, reshape_r2l(p2, t_left, t_right, both))
                 half = engine.boundary_tensor_mpo(tmp, boundary, mpo, "right")
-            add_perturbation(dm, both, half, alpha, l2r)
-            del half
+        dm = density_matrix(both, l2r, half, alpha)
+        del half
         U, _, tr = heev_truncate(dm, cutoff, Mmax)
         del dm
         if l2r:
             A_lp = U
-            B_rp = gemm(_transpose(U), both)
+            B_rp = gemm(U, both, ta=True)
         else:
             B_rp = _transpose(U)
             A_lp = gemm(both, U)
@@ -466,12 +423,11 @@ def predict_new_state(u: DeviceMPSTensor, mpo, left, right, alpha: float, cutoff
     eigendecomposition cut, the new site U (l2r) or U^T (r2l) and the factor U^T M
     (l2r) or M U (r2l).  Returns (new site, factor, truncation results)."""
     M = as_dbm(u) if l2r else reshape_l2r(u.phys_i, u.left_i, u.right_i, as_dbm(u))
-    Mt = _transpose(M)
-    dm = gemm(M, Mt) if l2r else gemm(Mt, M)
+    half = None
     if alpha != 0.0:
         half = engine.boundary_tensor_mpo(u, left if l2r else right, mpo, "left" if l2r else "right")
-        add_perturbation(dm, M, half, alpha, l2r)
-        del half
+    dm = density_matrix(M, l2r, half, alpha)
+    del half
     U, _, tr = heev_truncate(dm, cutoff, Mmax)
     del dm
     phys = u.phys_i
@@ -479,7 +435,7 @@ def predict_new_state(u: DeviceMPSTensor, mpo, left, right, alpha: float, cutoff
         new_right = U.right_basis()
         new_left = u.left_i.copy()
         common_subset(new_left, index_product(adjoin(phys), new_right))
-        return from_dbm(phys, new_left, new_right, U), gemm(_transpose(U), M), tr
+        return from_dbm(phys, new_left, new_right, U), gemm(U, M, ta=True), tr
     Ut = _transpose(U)
     new_left = Ut.left_basis()
     new_right = u.right_i.copy()
@@ -558,7 +514,9 @@ def right_normalize_and_return(t: DeviceMPSTensor) -> Tuple[DeviceMPSTensor, DBM
 
 
 def _flat_of(Nm: DBM) -> DBM:
-    if Nm.flat is not None:
+    """Nm itself when its blocks are still exactly the views of its flat buffer,
+    else a packed copy."""
+    if Nm.flat is not None and Nm.layout is not None and list(Nm.keys) == Nm.layout.keys:
         return Nm
     lay, flat = Nm.to_flat()
     return _flat_dbm(lay, flat)
@@ -582,6 +540,6 @@ def multiply_from_right(t: DeviceMPSTensor, Nm: DBM) -> DeviceMPSTensor:
                          t.data.device, t.data, Nf.flat)
 
 
-__all__ = ["DBM", "block_views", "make_two_site_mps", "split", "svd_truncate", "heev_truncate", "add_perturbation",
+__all__ = ["DBM", "block_views", "make_two_site_mps", "split", "svd_truncate", "heev_truncate", "density_matrix", "gemm",
            "predict_new_state",
            "left_normalize_and_return", "right_normalize_and_return", "multiply_from_left", "multiply_from_right", "reshape_l2r", "reshape_r2l"]

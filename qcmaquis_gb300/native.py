@@ -111,6 +111,10 @@ def lib():
                                   C.POINTER(C.c_void_p)]
     L.qcm_mpo_buf_destroy.argtypes = [C.c_void_p]
     L.qcm_mpo_buf_destroy.restype = None
+    L.qcm_plan_block_gemm.argtypes = [C.POINTER(CBlocks), C.c_int32, C.POINTER(CBlocks), C.c_int32,
+                                      C.POINTER(C.c_void_p)]
+    L.qcm_plan_density_matrix.argtypes = [C.POINTER(CBlocks), C.c_int32, C.POINTER(CBoundary), C.c_double,
+                                          C.POINTER(C.c_void_p)]
     L.qcm_mpo_maker_create.argtypes = [C.c_int32, C.POINTER(CTagTable), C.POINTER(C.c_void_p)]
     L.qcm_mpo_maker_add_terms.argtypes = [C.c_void_p, C.c_int32, i32p, i32p, i32p, f64p, i32p]
     L.qcm_mpo_maker_site_terms.argtypes = [C.c_void_p, C.c_int32, C.c_int32, i32p, f64p, i32p]
@@ -918,6 +922,25 @@ def plan_mps_reshape(phys, left_i, right_i, lay: "Layout", to_right: bool) -> "P
     h = C.c_void_p()
     check(lib().qcm_plan_mps_reshape(C.byref(f[0].c), C.byref(f[1].c), C.byref(f[2].c), C.byref(lay.c),
                                      1 if to_right else 0, C.byref(h)), "qcm_plan_mps_reshape")
+    return Plan(h, "mps")
+
+
+def plan_block_gemm(a_lay: "Layout", ta: bool, b_lay: "Layout", tb: bool) -> "Plan":
+    """``qcm_plan_block_gemm``: OUT = op(A) op(B), charge-matched (A in slot KET, B in
+    slot LEFT); the output layout through ``out_tensor``."""
+    h = C.c_void_p()
+    check(lib().qcm_plan_block_gemm(C.byref(a_lay.c), 1 if ta else 0, C.byref(b_lay.c), 1 if tb else 0,
+                                    C.byref(h)), "qcm_plan_block_gemm")
+    return Plan(h, "mps")
+
+
+def plan_density_matrix(theta: "Layout", l2r: bool, half: "BoundaryLayout" = None, alpha: float = 0.0) -> "Plan":
+    """``qcm_plan_density_matrix``: rho = theta theta^T (``l2r``) or theta^T theta (theta
+    in slot KET), plus alpha sum_b h_b h_b^T (h in slot RIGHT) when ``half`` is given."""
+    h = C.c_void_p()
+    hp = C.byref(half.c) if (half is not None and alpha != 0.0) else None
+    check(lib().qcm_plan_density_matrix(C.byref(theta.c), 1 if l2r else 0, hp, float(alpha), C.byref(h)),
+          "qcm_plan_density_matrix")
     return Plan(h, "mps")
 
 

@@ -163,10 +163,7 @@ def overlap(mps: List[DeviceMPSTensor]) -> float:
         rp = O.reshape_l2r(t.phys_i, t.left_i, t.right_i, O.as_dbm(t))
         t1 = O.gemm(Lb, rp)
         t3 = O.reshape_r2l(t.phys_i, t.left_i, t.right_i, t1)
-        At = O.DBM()
-        for (lc, rc), b in zip(t.layout.keys, O.as_dbm(t).blocks):
-            At.insert(b.t(), rc, lc)
-        Lb = O.gemm(At, t3)
+        Lb = O.gemm(O.as_dbm(t), t3, ta=True)
     return float(sum(torch.trace(b).item() for b in Lb.blocks))
 
 

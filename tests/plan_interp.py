@@ -147,3 +147,21 @@ def run_gemm_images(tab, bufs, image_bytes, nprod=6):
             jj = ctab + np.minimum(n0 + j, ncols - 1)
             dst = tab["coltab"][2 * jj] + (e % rows) + (e // rows) * tab["coltab"][2 * jj + 1]
         bufs[c_buf][dst[valid]] = acc[valid]
+
+
+def patch_cpu_plans(monkeypatch):
+    """Run the MPS-level plans of ``qcmaquis_gb300.mps_ops`` on CPU tensors through
+    this interpreter (no upload, no device): lets the Python layer's calls of the
+    plans (their slots, layouts and offsets) be checked without a GPU."""
+    from qcmaquis_gb300 import mps_ops as O
+    from qcmaquis_gb300 import native as N
+
+    def interp(plan, device, ket=None, left=None, out=None, s2=None, right=None):
+        bufs = [None if t is None else t.numpy() for t in (ket, left, right, out)]
+        bufs += [np.full(max(x, 1), np.nan) for x in plan.scratch] + [None]
+        if s2 is not None:
+            bufs[6] = s2.numpy()
+        run_plan(plan, bufs)
+
+    monkeypatch.setattr(O, "_run_fp64", interp)
+    monkeypatch.setattr(N.Plan, "upload", lambda self: None)

@@ -1,7 +1,7 @@
 """The excited-state pieces of the device path (``qcmaquis_gb300.excited``: overlap
-boundaries and constraint vectors, per-block torch products) against the
-oracle's ``overlap_left_step`` / ``overlap_right_step`` / ``site_ortho_boundaries``.
-The functions are device-agnostic torch code; here they run on CPU tensors to
+boundaries and constraint vectors) against the oracle's ``overlap_left_step`` /
+``overlap_right_step`` / ``site_ortho_boundaries``.  They run here on CPU tensors,
+their block products (native plans) executed by the task-table interpreter, to
 check their index and layout logic without a GPU."""
 import numpy as np
 import pytest
@@ -16,6 +16,7 @@ from qcmaquis_gb300 import native as N
 
 from oracle import dmrg_ref as R
 from oracle.sweep import OverlapBoundaries as RefOverlap, SweepParams, initial_state
+from plan_interp import patch_cpu_plans
 
 
 def _dbm_dict(d):
@@ -28,6 +29,7 @@ def _bm_dict(b):
 
 @pytest.mark.parametrize("seeds", [(11, 12), (3, 8)])
 def test_overlap_boundaries_and_vectors_match_oracle(seeds, monkeypatch):
+    patch_cpu_plans(monkeypatch)
     L, Ne = 6, 6
     model = QCModel(L, synthetic_integral_map(L, seed=3), Ne)
     mpo = make_mpo(model)

@@ -177,6 +177,147 @@ def test_tensor_mpo_plan_rejects_a_bad_side():
     assert "side" in lib.qcm_last_error().decode()
 
 
+def _run_interp(p, slots):
+    bufs = [slots.get(i) for i in range(3)] + [np.full(max(p.out_elems, 1), np.nan)]
+    bufs += [np.full(max(x, 1), np.nan) for x in p.scratch] + [None]
+    run_plan(p, bufs)
+    return bufs[3]
+
+
+def _both_and_half(l2r):
+    """The two-site problem's both-paired theta and the bra-free boundary product h
+    its perturbation reads (as predict_split_mps builds them)."""
+    model, mpo, mps, psi, left, right = _pair_problem()
+    A0, B0 = mps[2], mps[3]
+    both = R._reshape_left_to_both(A0.phys_i, B0.phys_i, A0.left_i, B0.right_i, _tst(psi, A0, B0))
+    if l2r:
+        tmp = R.MPSTensor.from_block(A0.phys_i, A0.left_i, index_product(adjoin(B0.phys_i), B0.right_i), both,
+                                     R.LEFT_PAIRED)
+        half = R.left_boundary_tensor_mpo(tmp, left, mpo[2])
+    else:
+        tmp = R.MPSTensor.from_block(B0.phys_i, index_product(A0.phys_i, A0.left_i), B0.right_i, both,
+                                     R.RIGHT_PAIRED)
+        half = R.right_boundary_tensor_mpo(tmp, right, mpo[3])
+    return both, half
+
+
+@pytest.mark.parametrize("l2r", [True, False])
+@pytest.mark.parametrize("alpha", [0.0, 1e-2])
+def test_density_matrix_plan_matches_oracle(l2r, alpha):
+    """qcm_plan_density_matrix = the oracle's rho with its noise term (predict_split_mps:
+    theta theta^T or theta^T theta plus alpha h h^T on the blocks theta holds), layout
+    block for block, values to 1e-13 relative, through the task-table interpreter."""
+    both, half = _both_and_half(l2r)
+    bt = both.transpose()
+    ref = R.bm_gemm(both, bt) if l2r else R.bm_gemm(bt, both)
+    for h in half:
+        ht = h.transpose()
+        tdm = R.bm_gemm(h, ht) if l2r else R.bm_gemm(ht, h)
+        for (lc, rc), b in zip(tdm.keys, tdm.blocks):
+            if both.find_block(lc, rc) == both.n_blocks():
+                continue
+            q = ref.find_block(lc, rc)
+            if q == ref.n_blocks():
+                ref.insert_block(alpha * b, lc, rc)
+            else:
+                ref.blocks[q] = ref.blocks[q] + alpha * b
+    lay, hl = N.Layout.of(both), N.BoundaryLayout.of(half)
+    p = N.plan_density_matrix(lay, l2r, hl, alpha)
+    _, _, _, ol = N.out_tensor(p)
+    assert list(ol.keys) == list(ref.keys)
+    assert list(ol.shapes) == [b.shape for b in ref.blocks]
+    got = _run_interp(p, {0: lay.pack(both), 2: hl.pack(half)})[:ol.size]
+    want = ol.pack(ref)
+    assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+    if alpha:
+        plain = N.plan_density_matrix(lay, l2r)
+        # the noise adds products to the grouped GEMM (last column of an output: its segment end)
+        assert plain.stages()[-1][1][-1][-1] < p.stages()[-1][1][-1][-1]
+
+
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
+def test_block_gemm_plan_matches_oracle(ta, tb):
+    """qcm_plan_block_gemm = bm_gemm of the (transposed where asked) operands."""
+    both, _ = _both_and_half(True)
+    bt = both.transpose()
+    a = bt if ta else both       # op(A) = theta in every case
+    b = both if tb else bt       # op(B) = theta^T
+    ref = R.bm_gemm(both, bt)
+    la, lb = N.Layout.of(a), N.Layout.of(b)
+    p = N.plan_block_gemm(la, ta, lb, tb)
+    _, _, _, ol = N.out_tensor(p)
+    assert list(ol.keys) == list(ref.keys)
+    got = _run_interp(p, {0: la.pack(a), 1: lb.pack(b)})[:ol.size]
+    want = ol.pack(ref)
+    assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+    # a product with a factor of another shape: U^T theta for the heev cut's U
+    U, _, _ = R.heev_truncate(ref, 1e-12, 6)
+    lu = N.Layout.of(U)
+    p = N.plan_block_gemm(lu, True, la if not ta else N.Layout.of(both), False)
+    _, _, _, ol = N.out_tensor(p)
+    ref2 = R.bm_gemm(U.transpose(), both)
+    assert list(ol.keys) == list(ref2.keys)
+    got = _run_interp(p, {0: lu.pack(U), 1: N.Layout.of(both).pack(both)})[:ol.size]
+    assert np.abs(got - ol.pack(ref2)).max() <= 1e-13 * max(np.abs(ol.pack(ref2)).max(), 1e-300)
+
+
+def test_block_gemm_plan_rejects_mismatched_inner_dimensions():
+    both, _ = _both_and_half(True)
+    lay = N.Layout.of(both)
+    bad = N.Layout(lay.keys, [(r + 1, c) for r, c in lay.shapes])
+    with pytest.raises(RuntimeError, match="inner dimensions"):
+        N.plan_block_gemm(lay, False, bad, False)
+
+
+@pytest.mark.parametrize("l2r", [True, False])
+def test_heev_products_wiring_on_the_interpreter(l2r, monkeypatch):
+    """The Python layer's density matrix and block products (mps_ops.density_matrix,
+    mps_ops.gemm with transpose flags) on CPU tensors, their plans executed by the
+    task-table interpreter in place of the device: slots, layouts and offsets as
+    the GPU path passes them, values equal to the oracle's."""
+    import types
+    import torch
+    from qcmaquis_gb300 import mps_ops as O
+    from plan_interp import patch_cpu_plans
+    patch_cpu_plans(monkeypatch)
+    both, half = _both_and_half(l2r)
+    lay, hl = N.Layout.of(both), N.BoundaryLayout.of(half)
+    M = O._flat_dbm(lay, torch.from_numpy(lay.pack(both)))
+    h = types.SimpleNamespace(layout=hl, data=torch.from_numpy(hl.pack(half)))
+    alpha = 1e-2
+    dm = O.density_matrix(M, l2r, h, alpha)
+    bt = both.transpose()
+    ref = R.bm_gemm(both, bt) if l2r else R.bm_gemm(bt, both)
+    for hb in half:
+        tdm = R.bm_gemm(hb, hb.transpose()) if l2r else R.bm_gemm(hb.transpose(), hb)
+        for (lc, rc), b in zip(tdm.keys, tdm.blocks):
+            if both.find_block(lc, rc) == both.n_blocks():
+                continue
+            q = ref.find_block(lc, rc)
+            if q == ref.n_blocks():
+                ref.insert_block(alpha * b, lc, rc)
+            else:
+                ref.blocks[q] = ref.blocks[q] + alpha * b
+    assert dm.keys == ref.keys
+    for a, b in zip(dm.blocks, ref.blocks):
+        assert np.abs(a.numpy() - b).max() <= 1e-13 * np.abs(b).max()
+    # the heev cut's factor products: U^T theta (l2r), theta U (r2l), U as the first
+    # kk columns of each block of a packed factor buffer (as the batched SVD leaves it)
+    U, _, _ = R.heev_truncate(ref, 1e-12, 6)
+    keys, shapes, offs, flat, o = [], [], [], [], 0
+    for (lc, rc), b in zip(U.keys, U.blocks):
+        r, kk = b.shape
+        full = np.concatenate([b, np.full((r, 2), np.nan)], axis=1)   # columns past kk never read
+        keys.append((lc, rc)); shapes.append((r, kk)); offs.append(o)
+        flat.append(np.ravel(full, order="F")); o += full.size
+    Ud = O._flat_dbm(N.Layout(keys, shapes, offs), torch.from_numpy(np.concatenate(flat)))
+    got = O.gemm(Ud, M, ta=True) if l2r else O.gemm(M, Ud)
+    want = R.bm_gemm(U.transpose(), both) if l2r else R.bm_gemm(both, U)
+    assert got.keys == want.keys
+    for a, b in zip(got.blocks, want.blocks):
+        assert np.abs(a.numpy() - b).max() <= 1e-13 * max(np.abs(b).max(), 1e-300)
+
+
 # ------------------------------------------------------------------ GPU
 def _host_theta(A, B):
     """Two-site product of device tensors, on the host."""
