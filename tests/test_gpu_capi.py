@@ -1,7 +1,11 @@
 """One two-site microiteration driven by a C++ host through the C ABI only
 (``tests/capi_microiteration.cpp``: ``qcm_plan_two_site``, ``qcm_plan_sigma`` +
 ``qcm_jcd_solve``, ``qcm_split``, ``qcm_plan_boundary_left`` +
-``qcm_boundary_step``), against the oracle's microiteration on the same inputs:
+``qcm_boundary_step``), and the same microiteration written against the
+reference-facing C++ classes over that ABI (``tests/capi_engine.cpp``:
+``TwoSiteTensor``, ``SiteProblem``, ``solve_ietl_jcd``, ``split_mps_l2r``,
+``Engine::overlap_mpo_left_step`` of ``include/qcm_gb300_engine.hpp``), against
+the oracle's microiteration on the same inputs:
 
 * LiH (the reference's ``dmrg/tests/test2.cpp`` system) at its converged state:
   the eigenvalue plus the core energy reproduces the reference's golden energy;
@@ -88,13 +92,15 @@ def _mpo(f, name, fm):
         _put(f, name + "." + k, getattr(fm, k))
 
 
-@pytest.fixture(scope="module")
-def host_exe(tmp_path_factory):
-    exe = tmp_path_factory.mktemp("capi") / "capi_microiteration"
+@pytest.fixture(scope="module", params=["capi_microiteration", "capi_engine"])
+def host_exe(request, tmp_path_factory):
+    """The host program: the raw C ABI (capi_microiteration.cpp) or the
+    reference-facing C++ classes over it (capi_engine.cpp, qcm_gb300_engine.hpp)."""
+    exe = tmp_path_factory.mktemp("capi") / request.param
     libdir = os.path.join(ROOT, "qcmaquis_gb300")
     cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
     r = subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), "-I" + cuda + "/include",
-                        os.path.join(ROOT, "tests", "capi_microiteration.cpp"), "-o", str(exe), "-L" + libdir,
+                        os.path.join(ROOT, "tests", request.param + ".cpp"), "-o", str(exe), "-L" + libdir,
                         "-lqcm_gb300", "-Wl,-rpath," + libdir, "-L" + cuda + "/lib64", "-lcudart",
                         "-Wl,-rpath," + cuda + "/lib64"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr

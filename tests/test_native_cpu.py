@@ -214,15 +214,18 @@ def test_cpp_layer_builds_a_plan(tmp_path):
     assert "out=4" in out.stdout
 
 
-def test_cpp_microiteration_host_compiles(tmp_path):
-    """The C++ host that runs a whole microiteration through the C ABI
-    (tests/capi_microiteration.cpp; run by the GPU tests) compiles and links."""
+@pytest.mark.parametrize("prog", ["capi_microiteration", "capi_engine"])
+def test_cpp_microiteration_host_compiles(tmp_path, prog):
+    """The C++ hosts that run a whole microiteration through the C ABI
+    (tests/capi_microiteration.cpp) and through the reference-facing C++ classes
+    (tests/capi_engine.cpp, include/qcm_gb300_engine.hpp) compile and link (the
+    GPU tests run them)."""
     import subprocess
-    exe = tmp_path / "capi_microiteration"
+    exe = tmp_path / prog
     libdir = os.path.join(ROOT, "qcmaquis_gb300")
     cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
-    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"), "-I" + cuda + "/include",
-                        os.path.join(ROOT, "tests", "capi_microiteration.cpp"), "-o", str(exe), "-L" + libdir,
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-I" + os.path.join(ROOT, "include"), "-I" + cuda + "/include",
+                        os.path.join(ROOT, "tests", prog + ".cpp"), "-o", str(exe), "-L" + libdir,
                         "-lqcm_gb300", "-Wl,-rpath," + libdir, "-L" + cuda + "/lib64", "-lcudart"],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
