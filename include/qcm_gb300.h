@@ -257,7 +257,9 @@ int qcm_mpo_twosite(const qcm_mpo_t* w1, const qcm_mpo_t* w2, const qcm_index_t*
  * each element's (tag, scale, label) terms in the reference's MPOTensor order
  * (latest insertion first), the outgoing bonds' spins (2S, action), Hermitian
  * partners and phases (bond_dim entries; the incoming bonds' are the previous
- * site's).  row_dim / col_dim are 1 at the chain ends. */
+ * site's).  row_dim / col_dim are 1 at the chain ends.  A maker is finished once:
+ * after a failed qcm_mpo_maker_finish it refuses further calls (QCM_E_STATE) and
+ * is only destroyed. */
 typedef struct {
     int32_t n_tags;
     const int32_t* fermionic;  /* n_tags */

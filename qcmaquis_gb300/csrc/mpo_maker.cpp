@@ -97,6 +97,7 @@ struct qcm_mpo_maker {
     // per site: (incoming key << 32 | outgoing key) -> element list in insertion order
     std::vector<std::unordered_map<uint64_t, std::vector<Val>>> prempo;
     bool built = false;
+    bool finishing = false;   // finish was called: the element lists hold the chain-end identities
     std::vector<SiteOut> out;
 
     int32_t intern(const Key& k) {
@@ -358,7 +359,7 @@ int qcm_mpo_maker_add_terms(qcm_mpo_maker* M, int32_t n_terms, const int32_t* te
         set_error("qcm_mpo_maker_add_terms: null argument");
         return QCM_E_INVALID;
     }
-    if (M->built) { set_error("qcm_mpo_maker_add_terms: tensors already built"); return QCM_E_STATE; }
+    if (M->built || M->finishing) { set_error("qcm_mpo_maker_add_terms: maker already finished"); return QCM_E_STATE; }
     try {
         if (n_terms > 0 && term_ptr[0] != 0) throw std::runtime_error("term_ptr[0] != 0");
         std::vector<std::pair<int32_t, int32_t>> ops;
@@ -380,7 +381,7 @@ int qcm_mpo_maker_add_terms(qcm_mpo_maker* M, int32_t n_terms, const int32_t* te
 int qcm_mpo_maker_site_terms(qcm_mpo_maker* M, int32_t site, int32_t n, const int32_t* tag, const double* scale,
                              const int32_t* label) {
     if (!M || n <= 0 || !tag || !scale || !label) { set_error("qcm_mpo_maker_site_terms: null argument"); return QCM_E_INVALID; }
-    if (M->built) { set_error("qcm_mpo_maker_site_terms: tensors already built"); return QCM_E_STATE; }
+    if (M->built || M->finishing) { set_error("qcm_mpo_maker_site_terms: maker already finished"); return QCM_E_STATE; }
     if (site < 0 || site >= M->L) { set_error("qcm_mpo_maker_site_terms: site out of range"); return QCM_E_INVALID; }
     auto& d = M->prempo[site];
     const uint64_t kk = qcm_mpo_maker::pair_key(KEY_TL, KEY_TR);
@@ -393,7 +394,11 @@ int qcm_mpo_maker_site_terms(qcm_mpo_maker* M, int32_t site, int32_t n, const in
 
 int qcm_mpo_maker_finish(qcm_mpo_maker* M, const qcm_tag_table_t* tags, int32_t leftmost_right, int32_t rightmost_left) {
     if (!M) { set_error("qcm_mpo_maker_finish: null handle"); return QCM_E_INVALID; }
-    if (M->built) { set_error("qcm_mpo_maker_finish: tensors already built"); return QCM_E_STATE; }
+    if (M->built || M->finishing) {
+        set_error("qcm_mpo_maker_finish: called before on this maker (after a failed finish, destroy it)");
+        return QCM_E_STATE;
+    }
+    M->finishing = true;
     try {
         if (tags) {
             TagTable t = read_tags(tags);

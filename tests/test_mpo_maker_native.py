@@ -114,3 +114,30 @@ def _site_terms_twice(N, tags):
         N.check(L.qcm_mpo_maker_site_terms(h, 1, 1, N._p(t, N.i32p), N._p(s, N.f64p), N._p(lab, N.i32p)))
     finally:
         L.qcm_mpo_maker_destroy(h)
+
+
+def test_native_maker_is_finished_once():
+    """A failed finish leaves the maker refusing further calls instead of
+    building on its partial state."""
+    import ctypes as C
+    from qcmaquis_gb300 import native as N
+    model = QCModel(4, synthetic_integral_map(4, seed=1), 4)
+    th = model.tag_handler
+    tags = N.FTagTable(th, model.ops.ident, model.ops.ident_full, model.ops.fill, "su2u1")
+    L = N.lib()
+    h = C.c_void_p()
+    N.check(L.qcm_mpo_maker_create(4, C.byref(tags.c), C.byref(h)))
+    try:
+        t = np.array([0], dtype=np.int32)
+        s = np.array([1.0])
+        lab = np.array([-1], dtype=np.int32)
+        N.check(L.qcm_mpo_maker_site_terms(h, 1, 1, N._p(t, N.i32p), N._p(s, N.f64p), N._p(lab, N.i32p)))
+        # a leftmost_right before the chain start puts the trivial right key's identity
+        # on site 0, where no bond leads to it: refused
+        rc = L.qcm_mpo_maker_finish(h, C.byref(tags.c), -1, 0)
+        assert rc != 0
+        assert L.qcm_mpo_maker_finish(h, C.byref(tags.c), 3, 0) != 0
+        assert "destroy" in L.qcm_last_error().decode()
+        assert L.qcm_mpo_maker_site_terms(h, 2, 1, N._p(t, N.i32p), N._p(s, N.f64p), N._p(lab, N.i32p)) != 0
+    finally:
+        L.qcm_mpo_maker_destroy(h)
