@@ -318,6 +318,33 @@ def test_heev_products_wiring_on_the_interpreter(l2r, monkeypatch):
         assert np.abs(a.numpy() - b).max() <= 1e-13 * max(np.abs(b).max(), 1e-300)
 
 
+def test_block_plans_on_empty_and_unmatched_inputs():
+    """Empty operands and operands whose inner charges never agree give empty
+    products (no blocks, nothing to run); a perturbation block outside theta's
+    charges is not added."""
+    empty = N.Layout([], [])
+    for p in (N.plan_block_gemm(empty, False, empty, True), N.plan_density_matrix(empty, True),
+              N.plan_density_matrix(empty, False)):
+        _, _, _, lay = N.out_tensor(p)
+        assert lay.keys == [] and p.out_elems == 0
+    a = N.Layout([((2, 0), (1, 1))], [(3, 2)])
+    b = N.Layout([((0, 0), (1, 1))], [(2, 4)])     # op(B) = B: inner charge (0, 0) never meets (1, 1)
+    _, _, _, lay = N.out_tensor(N.plan_block_gemm(a, False, b, False))
+    assert lay.keys == []
+    _, _, _, lay = N.out_tensor(N.plan_block_gemm(a, True, b, True))   # (1,1)x(2,0) . (1,1)x(0,0): inner (2,0) vs (1,1)
+    assert lay.keys == []
+    # a half boundary whose only pair lands on charges theta does not hold adds nothing
+    theta = N.Layout([((2, 0), (2, 0))], [(3, 3)])
+    half = N.BoundaryLayout([N.Layout([((4, 0), (1, 1))], [(2, 5)])])
+    p = N.plan_density_matrix(theta, True, half, 0.5)
+    _, _, _, lay = N.out_tensor(p)
+    assert lay.keys == [((2, 0), (2, 0))]
+    x = np.arange(9.0)
+    got = _run_interp(p, {0: x, 2: np.ones(10)})[:9].reshape(3, 3, order="F")
+    X = x.reshape(3, 3, order="F")
+    assert np.allclose(got, X @ X.T, rtol=0, atol=1e-13)
+
+
 # ------------------------------------------------------------------ GPU
 def _host_theta(A, B):
     """Two-site product of device tensors, on the host."""
