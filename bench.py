@@ -25,6 +25,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "H_eff.psi TFLOP/s (sigma vector, L=24 N=24 S=0 SU2U1, m=1024, middle sites)"
+
+
+def metric_name(L: int, m: int) -> str:
+    """The sigma metric's name for the workload run (METRIC at the default sizes)."""
+    return f"H_eff.psi TFLOP/s (sigma vector, L={L} N={L} S=0 SU2U1, m={m}, middle sites)"
 UNIT = "TFLOP/s"
 
 
@@ -142,17 +147,56 @@ def measured_peaks():
     return {}
 
 
-def captured_traffic(L: int, m: int):
-    """DRAM bytes per sigma of the roofline kernel (K1 + K3 stages) from the committed
-    summary of one ncu capture of this workload, or None for another size."""
-    path = os.path.join(ROOT, "profiles", f"sigma_bf16x3_L{L}_m{m}_traffic.md")
-    if not os.path.exists(path):
-        return None
+def k1_k3_stream_bytes(plan, left_elems: int, right_elems: int) -> int:
+    """Bytes the K1 and K3 stages of a BF16x3 sigma plan stream by design: their
+    BF16 slice images written and read back once (2 x the image bytes of the two
+    GEMM stages, each panel ceil(K/32) x 3 slices x G x 512 bytes), T written, and
+    the ket, contr, sigma and both boundaries moved once in FP32 (4 bytes per
+    element).  The unit the measured DRAM traffic of these stages is scaled by."""
+    img = 0
+    for si, kind in enumerate(plan.stage_kinds()):
+        if kind != "gemm":
+            continue
+        end = 0
+        for src_off, img_off, src_buf, ld, R, K, kcontig, G in plan.stage_images(si)["panels"].tolist():
+            if img_off >= 0:
+                end = max(end, img_off + ((K + 31) // 32) * 3 * G * 512)
+        img += end
+    s0, s1, s2 = plan.scratch
+    return int(2 * img + 4 * (s0 + s1 + s2 + plan.out_elems + left_elems + right_elems))
+
+
+def _traffic_summary(path):
+    vals = {}
     with open(path) as f:
         for line in f:
-            if line.startswith("traffic_bytes_k1_k3 ="):
-                return int(line.split("=")[1])
-    return None
+            for key in ("traffic_bytes_k1_k3", "k1_k3_stream_bytes"):
+                if line.startswith(key + " ="):
+                    vals[key] = int(line.split("=")[1])
+    return vals
+
+
+def captured_traffic(L: int, m: int, stream_bytes: int):
+    """DRAM bytes per sigma of the roofline kernel (K1 + K3 stages: image builds and
+    tcgen05 products) from a committed ncu summary, and where they come from.
+
+    The capture is of a smaller case of the same workload (the full one holds
+    16 GB on the device), scaled by the ratio of the two workloads' design stream
+    bytes (``k1_k3_stream_bytes``): measured traffic over stream bytes is 1.035
+    at m=512 and 1.054 at m=1024, so the traffic grows in proportion to them.
+    None if there is no summary."""
+    import glob
+    exact = os.path.join(ROOT, "profiles", f"sigma_bf16x3_L{L}_m{m}_traffic.md")
+    cands = [exact] if os.path.exists(exact) else sorted(
+        glob.glob(os.path.join(ROOT, "profiles", f"sigma_bf16x3_L{L}_m*_traffic.md")))
+    for path in cands:
+        v = _traffic_summary(path)
+        if "traffic_bytes_k1_k3" in v and v.get("k1_k3_stream_bytes"):
+            per = v["traffic_bytes_k1_k3"] / v["k1_k3_stream_bytes"]
+            how = ("measured" if path == exact
+                   else f"scaled by the design stream bytes of the K1 and K3 stages, {per:.3f} DRAM bytes each")
+            return per * stream_bytes, f"{os.path.relpath(path, ROOT)} ({how})"
+    return None, None
 
 
 def dgemm_peak_tflops():
@@ -236,7 +280,7 @@ def run_reference(args):
         times.append(t)
     value = flops / dt / 1e12
     cpu = {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": b.describe(times, threads)}
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+    line = {"impl": "reference", "metric": metric_name(args.L, args.m), "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (the benchmark's layouts from a committed fixture, seeded random values)",
@@ -709,6 +753,7 @@ def main():
     plan = eng.sigma_plan(w.psi, w.left, w.right, w.ts_mpo)
     setup_s = time.time() - t0
     flops = plan.gemm_flops + plan.axpy_flops
+    k1_k3_bytes = k1_k3_stream_bytes(plan, w.left.layout.size, w.right.layout.size)
     out = torch.empty(plan.out_elems, dtype=torch.float64, device=eng.device)
     stream = torch.cuda.current_stream()
 
@@ -801,12 +846,12 @@ def main():
         peak = peaks.get("bf16_tflops", 1900.0)
         nprod = 6 if prec == N.PREC_BF16X3 else (3 if prec == N.PREC_BF16X2 else 1)
         ach = plan.gemm_flops * nprod / gemm_t / 1e12
-        traffic = captured_traffic(args.L, args.m) if (prec == N.PREC_BF16X3 and not args.no_images) else None
+        traffic, tsrc = (captured_traffic(args.L, args.m, k1_k3_bytes) if (prec == N.PREC_BF16X3 and not args.no_images)
+                         else (None, None))
         roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                 "traffic": traffic,
-                "traffic_source": (f"profiles/sigma_bf16x3_L{args.L}_m{args.m}_traffic.md (ncu dram__bytes_read.sum "
-                                   "+ dram__bytes_write.sum over the K1 and K3 launches of one sigma)")
-                if traffic else None,
+                "traffic_source": (f"{tsrc}: ncu dram__bytes_read.sum + dram__bytes_write.sum over the K1 and K3 "
+                                   "launches of one sigma") if traffic else None,
                 "traffic_gbs": traffic / gemm_t / 1e9 if traffic else None,
                 "kernel": ("tc_img_kernel + build_images_kernel (tcgen05 K1 + K3 block products from "
                            "bulk-copied BF16 slice images)" if (prec in (N.PREC_BF16X3, N.PREC_BF16X2)
@@ -830,12 +875,13 @@ def main():
 
     value = flops / t_step / 1e12 * world
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": metric_name(args.L, args.m), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak" if world > 1 else "weak", "vs_baseline": None,
         "dtype": {"fp64": "f64", "tf32": "tf32", "bf16x3": "bf16x3", "bf16x2": "bf16x2"}[args.precision],
         "data": "synthetic (seeded integrals and random MPS; no dataset)",
-        "config": {"workload": "sigma vector H_eff.psi, L=24 N=24 S=0 SU2U1, middle sites (11,12), m=1024",
+        "config": {"workload": f"sigma vector H_eff.psi, L={args.L} N={args.L} S=0 SU2U1, middle sites "
+                               f"({args.L // 2 - 1},{args.L // 2}), m={args.m}",
                    **w.describe(), "precision": args.precision,
                    "l2": "working set of one sigma (boundaries, T, contr, operand images: about 16 GB) far above L2; no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU",
@@ -849,7 +895,8 @@ def main():
         # in FP64 (3 x 8 B per element-term); sources are shared across terms and
         # served from L2, so this is an element-term rate, not DRAM traffic
         "axpy_element_term_rate_gbs_naive": axpy_gbs,
-        "work": {"gemm_flops": plan.gemm_flops, "axpy_flops": plan.axpy_flops, "axpy_bytes": plan.axpy_bytes},
+        "work": {"gemm_flops": plan.gemm_flops, "axpy_flops": plan.axpy_flops, "axpy_bytes": plan.axpy_bytes,
+                 "k1_k3_stream_bytes": k1_k3_bytes},
         "clocks": clk.summary(),
         "vs_fp64_gpu": compare,
         "device_status": st,
