@@ -284,6 +284,44 @@ typedef struct {
     const int32_t* right_phase;/* bond_dim */
 } qcm_mpo_site_t;
 
+/* Terms of the SU2U1 quantum-chemistry Hamiltonian (qc_su2 model,
+ * dmrg/framework/dmrg/models/chem/su2u1/model.hpp:52-203, with the SU(2) term
+ * makers and spin sums of models/chem/su2u1/term_maker.h:120-395, :548-793): the
+ * n_int integrals (idx: four 1-based orbital indices each, 0 = unused, as in
+ * the reference's integral map; val: their values; |val| <= cutoff skipped)
+ * become operator terms.  One-site terms come first in integral order; the
+ * two-, three- and four-operator terms follow, equal terms merged (coefficients
+ * summed), in ascending order of (positions, tags).  Off-diagonal one-body
+ * integrals are folded into two-body terms with weight 1/(nelec-1)
+ * (model.hpp:96-139).  Each term lists, per integral it came from (index into
+ * the input), its coefficient per unit of that integral.  The tag table names
+ * the model's operators: bundles[b][f] for b = create, destroy, count, flip,
+ * e2d, d2e, docc, create_count, destroy_count and f = couple_up, couple_down,
+ * fill_couple_up, fill_couple_down, no_couple, fill_no_couple (-1 where a
+ * bundle has no such operator). */
+typedef struct {
+    int32_t ident, count, docc;
+    int32_t bundles[9][6];
+} qcm_chem_tags_t;
+
+typedef struct {
+    int64_t n_terms;
+    const int32_t* term_ptr;   /* n_terms + 1, into pos / tag */
+    const int32_t* pos;
+    const int32_t* tag;
+    const double* coeff;       /* n_terms */
+    const int32_t* fermionic;  /* n_terms */
+    const int64_t* src_ptr;    /* n_terms + 1, into src_idx / src_val */
+    const int64_t* src_idx;    /* integral index */
+    const double* src_val;     /* coefficient per unit of that integral */
+} qcm_term_view_t;
+
+typedef struct qcm_term_buf qcm_term_buf;
+int qcm_chem_terms(int32_t L, int32_t nelec, int64_t n_int, const int32_t* idx, const double* val, double cutoff,
+                   const qcm_chem_tags_t* tags, qcm_term_buf** out);
+int qcm_term_buf_view(const qcm_term_buf* buf, qcm_term_view_t* view);
+void qcm_term_buf_destroy(qcm_term_buf* buf);
+
 typedef struct qcm_mpo_maker qcm_mpo_maker;
 int qcm_mpo_maker_create(int32_t L, const qcm_tag_table_t* tags, qcm_mpo_maker** out);
 int qcm_mpo_maker_add_terms(qcm_mpo_maker* maker, int32_t n_terms, const int32_t* term_ptr, const int32_t* pos,

@@ -19,7 +19,7 @@ i.e. no point-group labels) are supported, which covers every workload here.
 from __future__ import annotations
 
 import math
-from typing import Dict, List, Tuple
+from typing import Dict, List, Optional, Tuple
 
 import numpy as np
 
@@ -433,7 +433,11 @@ class QCModel:
     """The SU2U1 quantum-chemistry model of ``models/chem/su2u1/model.hpp``."""
 
     def __init__(self, L: int, integrals: Dict[Tuple[int, int, int, int], float], nelec: int,
-                 integral_cutoff: float = 1e-20):
+                 integral_cutoff: float = 1e-20, native: bool = True):
+        """``native``: the terms come from the library's generator (``qcm_chem_terms``,
+        kept as flat arrays that the native MPO maker reads directly; ``terms`` is
+        built from them on first use); else from the Python restatement below.
+        Both give the same terms, coefficients and provenance in the same order."""
         self.L = L
         self.nelec = nelec
         self.tag_handler = TagHandler()
@@ -442,8 +446,34 @@ class QCModel:
         self.phys = phys_index()
         self.integrals = integrals
         self.integral_cutoff = integral_cutoff
-        self.terms: List[Term] = []
-        self._create_terms()
+        self._terms: Optional[List[Term]] = None
+        self.term_arrays = None
+        if native:
+            from . import native as N
+            self.term_arrays = N.chem_terms(L, nelec, integrals, integral_cutoff, self.ops, self.col)
+        else:
+            self._terms = []
+            self._create_terms()
+
+    @property
+    def terms(self) -> List[Term]:
+        if self._terms is None:
+            self._terms = self._terms_from_arrays()
+        return self._terms
+
+    def _terms_from_arrays(self) -> List[Term]:
+        a = self.term_arrays
+        ptr, pos, tag = a.term_ptr.tolist(), a.pos.tolist(), a.tag.tolist()
+        coeff, ferm = a.coeff.tolist(), a.fermionic.tolist()
+        sptr, sidx, sval = a.src_ptr.tolist(), a.src_idx.tolist(), a.src_val.tolist()
+        keys = a.keys
+        out = []
+        for t in range(len(coeff)):
+            term = Term(coeff[t], bool(ferm[t]))
+            term.ops = list(zip(pos[ptr[t]:ptr[t + 1]], tag[ptr[t]:ptr[t + 1]]))
+            term.src = {keys[sidx[q]]: sval[q] for q in range(sptr[t], sptr[t + 1])}
+            out.append(term)
+        return out
 
     # parse_integrals (models/chem/parse_integrals.h:43-214), identity orbital order
     def _parsed(self):

@@ -221,6 +221,9 @@ class TaggedMPOMaker:
         """The native maker's input: one-site terms are added here (they need the
         operator algebra), the terms of two or more operators are flattened for
         ``qcm_mpo_maker_add_terms``."""
+        arrays = getattr(model, "term_arrays", None)
+        if arrays is not None and getattr(model, "_terms", None) is None:
+            return self._collect_arrays(arrays)
         ptr, flat, coeff, label = [0], [], [], []
         lr, rl = self.L, 0
         for idx, t in enumerate(model.terms):
@@ -399,6 +402,35 @@ class TaggedMPOMaker:
             if op1.spin.get() == 1 and op2.spin.get() == 1 and op2.spin.action() == 1 and d1 == d2:
                 phase = (-1, -1)
         return conj, phase
+
+    def _collect_arrays(self, a):
+        """``_collect_native`` from the model's flat term arrays (the native term
+        generator's output), without Python term objects."""
+        nops = np.diff(a.term_ptr.astype(np.int64))
+        one = np.nonzero(nops == 1)[0]
+        lr, rl = self.L, 0
+        for idx in one.tolist():
+            q = int(a.term_ptr[idx])
+            t = Term(float(a.coeff[idx]), bool(a.fermionic[idx]))
+            t.push(int(a.pos[q]), int(a.tag[q]))
+            self._label = idx
+            self._add_1term(t)
+            lr, rl = min(lr, t.position(0)), max(rl, t.position(0))
+        if np.any(nops < 1):
+            raise RuntimeError("a model term without operators")
+        multi = np.nonzero(nops >= 2)[0]
+        op_mask = np.repeat(nops >= 2, nops)
+        pos = np.ascontiguousarray(a.pos[op_mask], dtype=np.int32)
+        tag = np.ascontiguousarray(a.tag[op_mask], dtype=np.int32)
+        ptr = np.zeros(len(multi) + 1, dtype=np.int32)
+        np.cumsum(nops[multi], out=ptr[1:])
+        if len(multi):
+            starts = ptr[:-1].astype(np.int64)
+            lr = min(lr, int(np.maximum.reduceat(pos, starts).min()))
+            rl = max(rl, int(np.minimum.reduceat(pos, starts).max()))
+        self.leftmost_right, self.rightmost_left = lr, rl
+        self._native_terms = (ptr, pos, tag, np.ascontiguousarray(a.coeff[multi], dtype=np.float64),
+                              multi.astype(np.int32))
 
     def _create_native(self) -> MPO:
         """create_mpo through the native maker (``qcm_mpo_maker_*``): the same

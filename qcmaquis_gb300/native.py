@@ -60,6 +60,15 @@ class CMpoSite(C.Structure):
                 ("right_phase", i32p)]
 
 
+class CChemTags(C.Structure):
+    _fields_ = [("ident", C.c_int32), ("count", C.c_int32), ("docc", C.c_int32), ("bundles", (C.c_int32 * 6) * 9)]
+
+
+class CTermView(C.Structure):
+    _fields_ = [("n_terms", C.c_int64), ("term_ptr", i32p), ("pos", i32p), ("tag", i32p), ("coeff", f64p),
+                ("fermionic", i32p), ("src_ptr", i64p), ("src_idx", i64p), ("src_val", f64p)]
+
+
 # symmetry groups of qcm_mpo_t.symmetry and the MPS-level plans
 SYM_SU2U1, SYM_TWOU1, SYM_U1 = 0, 1, 2
 
@@ -115,6 +124,11 @@ def lib():
                                       C.POINTER(C.c_void_p)]
     L.qcm_plan_density_matrix.argtypes = [C.POINTER(CBlocks), C.c_int32, C.POINTER(CBoundary), C.c_double,
                                           C.POINTER(C.c_void_p)]
+    L.qcm_chem_terms.argtypes = [C.c_int32, C.c_int32, C.c_int64, i32p, f64p, C.c_double, C.POINTER(CChemTags),
+                                 C.POINTER(C.c_void_p)]
+    L.qcm_term_buf_view.argtypes = [C.c_void_p, C.POINTER(CTermView)]
+    L.qcm_term_buf_destroy.argtypes = [C.c_void_p]
+    L.qcm_term_buf_destroy.restype = None
     L.qcm_mpo_maker_create.argtypes = [C.c_int32, C.POINTER(CTagTable), C.POINTER(C.c_void_p)]
     L.qcm_mpo_maker_add_terms.argtypes = [C.c_void_p, C.c_int32, i32p, i32p, i32p, f64p, i32p]
     L.qcm_mpo_maker_site_terms.argtypes = [C.c_void_p, C.c_int32, C.c_int32, i32p, f64p, i32p]
@@ -552,6 +566,57 @@ class FTagTable:
         self.pdiff = np.array(pd, dtype=np.int32)
         self.c = CTagTable(n, _p(self.ferm, i32p), _p(self.spin, i32p), _p(self.herm, i32p), _p(self.pdiff, i32p),
                            identity, identity_full, fill, symmetry_code(symmetry))
+
+
+CHEM_BUNDLES = ("create", "destroy", "count", "flip", "e2d", "d2e", "docc", "create_count", "destroy_count")
+CHEM_FIELDS = ("couple_up", "couple_down", "fill_couple_up", "fill_couple_down", "no_couple", "fill_no_couple")
+
+
+class TermArrays:
+    """Model terms as flat arrays (``qcm_chem_terms``): term t has operators
+    (pos, tag)[term_ptr[t]:term_ptr[t+1]], coefficient coeff[t], fermionic[t], and
+    per unit of integral keys[src_idx[s]] the coefficient src_val[s],
+    s in [src_ptr[t], src_ptr[t+1])."""
+
+    def __init__(self, term_ptr, pos, tag, coeff, fermionic, src_ptr, src_idx, src_val, keys):
+        self.term_ptr, self.pos, self.tag, self.coeff = term_ptr, pos, tag, coeff
+        self.fermionic, self.src_ptr, self.src_idx, self.src_val, self.keys = fermionic, src_ptr, src_idx, src_val, keys
+
+    def __len__(self):
+        return len(self.coeff)
+
+
+def chem_terms(L_sites: int, nelec: int, integrals: dict, cutoff: float, ops, col) -> TermArrays:
+    """The SU2U1 chemistry model's terms from its integral map (``qcm_chem_terms``):
+    the same terms, coefficients and per-integral provenance as ``model.QCModel``'s
+    Python generator, in the same order."""
+    keys = list(integrals.keys())
+    idx = np.array([list(k) for k in keys] or [[0, 0, 0, 0]], dtype=np.int32).reshape(-1)
+    val = np.array([float(integrals[k]) for k in keys] or [0.0], dtype=np.float64)
+    tags = CChemTags()
+    tags.ident, tags.count, tags.docc = ops.ident, ops.count, ops.docc
+    for b, name in enumerate(CHEM_BUNDLES):
+        bundle = getattr(col, name)
+        for f, field in enumerate(CHEM_FIELDS):
+            x = getattr(bundle, field)
+            tags.bundles[b][f] = -1 if x is None else int(x)
+    L = lib()
+    h = C.c_void_p()
+    check(L.qcm_chem_terms(L_sites, nelec, len(keys), _p(idx, i32p), _p(val, f64p), float(cutoff), C.byref(tags),
+                           C.byref(h)), "qcm_chem_terms")
+    try:
+        v = CTermView()
+        check(L.qcm_term_buf_view(h, C.byref(v)), "qcm_term_buf_view")
+        n = int(v.n_terms)
+        ptr = _copy(v.term_ptr, n + 1, np.int32)[:n + 1]
+        nops = int(ptr[-1])
+        sptr = _copy(v.src_ptr, n + 1, np.int64)[:n + 1]
+        ns = int(sptr[-1])
+        return TermArrays(ptr, _copy(v.pos, nops, np.int32)[:nops], _copy(v.tag, nops, np.int32)[:nops],
+                          _copy(v.coeff, n, np.float64)[:n], _copy(v.fermionic, n, np.int32)[:n], sptr,
+                          _copy(v.src_idx, ns, np.int64)[:ns], _copy(v.src_val, ns, np.float64)[:ns], keys)
+    finally:
+        L.qcm_term_buf_destroy(h)
 
 
 def mpo_maker_sites(L_sites: int, tags: FTagTable, terms, site_terms, leftmost_right: int, rightmost_left: int):
