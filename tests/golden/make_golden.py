@@ -5,7 +5,8 @@ Reads, as text, the reference test sources:
 * ``dmrg/tests/Fixtures/LiHFixture.h:29-94`` -- LiH CAS integrals (L=4, N=2)
   and ``:112`` reference energy;
 * ``dmrg/tests/Fixtures/H2Fixture.h:26-35`` -- H2 integrals (L=2, N=2);
-* ``dmrg/tests/test1.cpp:93`` -- H2 ground-state energy;
+* ``dmrg/tests/test1.cpp:93`` -- H2 ground-state energy; ``:95-118`` -- the sum of
+  its 1-RDM elements (0,0) and (1,1) and its 2-RDM element (0,0,0,0);
 * ``dmrg/tests/test_wigner.cpp:21-45`` -- 24 Wigner 9j values;
 * ``dmrg/tests/test2.cpp:60-120`` -- the LiH (SU2U1) ground-state 2-RDM
   (measurement ``twoptdm``): index quadruples and values;
@@ -61,6 +62,10 @@ def main():
     if len(rdm_idx) != len(rdm_val):
         raise SystemExit(f"2-RDM parse mismatch: {len(rdm_idx)} indices, {len(rdm_val)} values")
 
+    # test1.cpp: the H2 1-RDM's diagonal sum and the 2-RDM element {0,0,0,0}
+    h2_1rdm_trace = float(re.search(r"BOOST_CHECK_CLOSE\(value,\s*(" + NUM + r")\s*,", t1).group(1))
+    h2_2rdm_0000 = float(re.findall(r"BOOST_CHECK_CLOSE\(value,\s*(" + NUM + r")\s*,", t1)[1])
+
     s1 = re.search(r"ref_energy_excited_state\s*=\s*su2\s*\?\s*(" + NUM + ")", t2)
     lih_s1 = float(s1.group(1))
 
@@ -72,6 +77,8 @@ def main():
                "cite": "dmrg/tests/Fixtures/H2Fixture.h:26-35; dmrg/tests/test1.cpp:93"},
         "wigner9j": {"cases": wig, "rel_tol_percent": 1e-6, "cite": "dmrg/tests/test_wigner.cpp:21-45"},
         "lih_2rdm": {"index": rdm_idx, "value": rdm_val, "cite": "dmrg/tests/test2.cpp:60-120 (twoptdm)"},
+        "h2_rdm": {"onerdm_00_plus_11": h2_1rdm_trace, "twordm_0000": h2_2rdm_0000, "rel_tol_percent": 1e-7,
+                   "cite": "dmrg/tests/test1.cpp:95-118"},
         "lih_s1": {"energy": lih_s1, "rel_tol_percent": 1e-7,
                    "cite": "dmrg/tests/test2.cpp:122-139 (SU2U1 excited singlet, one orthogonal state)"},
     }

@@ -308,6 +308,33 @@ def test_rdm_measurement_reproduces_the_reference_lih_2rdm(golden):
         assert abs(v - g1[p, q]) < 1e-8, ((p, q), v, g1[p, q])
 
 
+def test_rdm_measurement_reproduces_the_reference_h2_values(golden):
+    """The H2 checks of dmrg/tests/test1.cpp:95-118 on the measured RDMs of the
+    H2 ground state: gamma_00 + gamma_11 = 2 and the 2-RDM element (0,0,0,0) =
+    1.1796482258, to the reference's 1e-7 % (BOOST_CHECK_CLOSE)."""
+    from conftest import integral_map
+    from oracle.sweep import SweepParams as OP, overlap, run_dmrg
+    from qcmaquis_gb300 import rdm as RD
+    g = golden["h2"]
+    model = QCModel(g["L"], integral_map(g["integrals"]), g["nelec"])
+    rec, mps = run_dmrg(model, TaggedMPOMaker(model).create_mpo(),
+                        OP(nsweeps=4, max_bond_dimension=16, ietl_jcd_tol=1e-13, ietl_jcd_maxiter=20),
+                        nelec=g["nelec"])
+    assert abs(rec.sweep_energy[-1] - g["energy"]) < 1e-9
+    ref = golden["h2_rdm"]
+    tol = ref["rel_tol_percent"] / 100.0
+    values = {}
+    for rank in (1, 2):
+        elems, terms, owner = RD.rdm_terms(model, rank)
+        mpo = RD.measurement_mpo(model, terms)
+        grads, fmpos = _oracle_term_gradients(mpo, mps)
+        vals = RD.elements_from_term_gradients(mpo, terms, owner, len(elems), grads, fmpos, overlap(mps))
+        values.update({tuple(e): float(v) for e, v in zip(elems, vals)})
+    trace = values[(0, 0)] + values[(1, 1)]
+    assert abs(trace - ref["onerdm_00_plus_11"]) <= tol * abs(ref["onerdm_00_plus_11"])
+    assert abs(values[(0, 0, 0, 0)] - ref["twordm_0000"]) <= tol * abs(ref["twordm_0000"])
+
+
 @pytest.mark.gpu
 def test_gpu_rdm_measurement_reproduces_the_reference_lih_2rdm(golden):
     from conftest import integral_map
