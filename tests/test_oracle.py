@@ -192,6 +192,23 @@ def test_single_site_sweeps_reach_exact_diagonalisation():
     assert abs(rec.sweep_energy[-1] - fci_energies(L, ints, N, 0, 1)[0]) < 1e-9
 
 
+def test_single_and_two_site_lih_agree(golden):
+    """dmrg/tests/ElectronicDMRG/testLiH.cpp:27-47: single-site and two-site
+    optimisation of LiH reach the same energy (the reference's tolerance, 1e-8 %),
+    both the reference's golden energy."""
+    from conftest import integral_map
+    from oracle.sweep import SweepParams as OP, run_dmrg, run_dmrg_single_site
+    g = golden["lih"]
+    model = QCModel(g["L"], integral_map(g["integrals"]), g["nelec"])
+    mpo = make_mpo(model)
+    ts, _ = run_dmrg(model, mpo, OP(nsweeps=4, max_bond_dimension=32, ietl_jcd_tol=1e-12), nelec=g["nelec"])
+    ss, _ = run_dmrg_single_site(model, mpo, OP(nsweeps=6, max_bond_dimension=32, ietl_jcd_tol=1e-12,
+                                                alpha_main=0.0, alpha_final=0.0), nelec=g["nelec"])
+    e_ts, e_ss = ts.sweep_energy[-1], ss.sweep_energy[-1]
+    assert abs(e_ss - e_ts) <= 1e-10 * abs(e_ts)
+    assert abs(e_ts - g["energy"]) <= 1e-10 * abs(g["energy"])
+
+
 def _zero_site_problem(L=6, N=6, seed=3, m=16, bond=2, herm=True):
     """State, bond matrix C between sites ``bond`` and ``bond + 1``, L[bond+1], R[bond+1]
     and the MPO, as ``test_siteproblem.cpp:97-154`` prepares them: the sites left of
