@@ -143,6 +143,7 @@ class AbelianChemModel:
 
     symmetry = ""
     states: List = []
+    _memo_enabled = True   # memoised local operators (``_site_tags``); False: recomputed for every term
 
     def _so(self, p: int, spin: int, create: bool) -> Tuple[int, str]:
         """(site, ladder name) of c+_{p spin} (``create``) or c_{p spin}."""
@@ -161,6 +162,7 @@ class AbelianChemModel:
         self.ops.ident_full = self.ops.ident
         self.ops.fill, _ = self._reg.tag(lad["F"], False)
         self.terms: List[Term] = []
+        self._memo: Dict[Tuple, Tuple] = {}
 
     def _site_ops(self, ladder: List[Tuple[int, str]]):
         """One (site, local matrix, fermionic) per site of a product of ladder operators
@@ -183,6 +185,39 @@ class AbelianChemModel:
             out.append((k, m, nferm % 2 == 1))
         return out
 
+    def _site_tags(self, ladder: List[Tuple[int, str]]):
+        """(site, tag, scale) per site of a product of ladder operators, or None if the
+        product vanishes -- ``_site_ops`` followed by the registry lookup, memoised
+        per site on the operator pattern that fixes the local matrix there (the
+        names of the operators on the site and a filling for every later operator,
+        in operator order).  The first appearance of a pattern registers its
+        operator exactly as the unmemoised form does, so tags come out the same."""
+        if not self._memo_enabled:
+            so = self._site_ops(ladder)
+            if so is None:
+                return None
+            return [(k, *self._reg.tag(m, ferm)) for k, m, ferm in so]
+        out = []
+        for k in sorted({s for s, _ in ladder}):
+            sig = tuple(name if s == k else "F" for s, name in ladder if s >= k)
+            hit = self._memo.get(sig)
+            if hit is None:
+                lad = self._lad
+                m = np.eye(len(self.states))
+                nferm = 0
+                for name in sig:
+                    m = m @ lad[name]
+                    nferm += name != "F"
+                if not np.any(m != 0.0):
+                    hit = (None, 0.0)
+                else:
+                    hit = self._reg.tag(m, nferm % 2 == 1)
+                self._memo[sig] = hit
+            if hit[0] is None:
+                return None
+            out.append((k, hit[0], hit[1]))
+        return out
+
     def _create_terms(self, norb: int):
         """H = sum_pq t_pq sum_s c+_ps c_qs + 1/2 sum_pqrs (pq|rs) sum_st c+_ps c+_rt c_ts c_qs
         + E_core over ``norb`` spatial orbitals."""
@@ -192,13 +227,12 @@ class AbelianChemModel:
         def add(coeff: float, ladder, key):
             if abs(coeff) <= 0.0:
                 return
-            so = self._site_ops(ladder)
-            if so is None:
+            st = self._site_tags(ladder)
+            if st is None:
                 return
             term = Term(coeff, False)
             scale = 1.0
-            for k, m, ferm in so:
-                tag, sc = self._reg.tag(m, ferm)
+            for k, tag, sc in st:
                 scale *= sc
                 term.push(k, tag)
             term.coeff = coeff * scale

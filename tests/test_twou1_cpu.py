@@ -234,3 +234,29 @@ def test_unknown_symmetry_is_rejected():
     la, lb = N.Layout.of(Ta.data), N.Layout.of(Tb.data)
     with pytest.raises(RuntimeError, match="unknown symmetry"):
         N.plan_two_site(Ta.phys_i, Ta.left_i, Ta.right_i, la, Tb.phys_i, Tb.left_i, Tb.right_i, lb, 7)
+
+
+@pytest.mark.parametrize("kind", ["2u1", "u1"])
+def test_memoised_local_operators_give_the_same_model(kind, monkeypatch):
+    """The abelian term builder's memoised local operators (per-site operator
+    patterns) give the same terms, coefficients, provenance and operator table
+    as recomputing every product."""
+    import math
+    from qcmaquis_gb300.model_2u1 import AbelianChemModel
+    from qcmaquis_gb300.model_u1 import U1SpinOrbitalModel
+
+    def make():
+        if kind == "2u1":
+            return TwoU1Model(7, synthetic_integral_map(7, seed=7), 4, 3)
+        return U1SpinOrbitalModel(4, synthetic_integral_map(4, seed=4), 3)
+    monkeypatch.setattr(AbelianChemModel, "_memo_enabled", False)
+    a = make()
+    monkeypatch.setattr(AbelianChemModel, "_memo_enabled", True)
+    b = make()
+    assert len(a.terms) == len(b.terms)
+    for x, y in zip(a.terms, b.terms):
+        assert x.ops == y.ops
+        assert (x.coeff, math.copysign(1.0, x.coeff)) == (y.coeff, math.copysign(1.0, y.coeff))
+        assert list(x.src.items()) == list(y.src.items())
+    assert len(a.tag_handler.ops) == len(b.tag_handler.ops)
+    assert a.tag_handler.herm == b.tag_handler.herm and a.tag_handler.sign == b.tag_handler.sign
