@@ -371,7 +371,10 @@ def run_sweep(args):
                      "repeated_layouts": len(rec.layout_digests) - len(set(rec.layout_digests)),
                      "plan_hits": rec.plan_hits,
                      "boundary_plan_hits": rec.boundary_plan_hits,
-                     "microiterations": len(rec.layout_digests)}
+                     "microiterations": len(rec.layout_digests),
+                     # the metric's rates over the whole run: sweeps and sigma vectors per second
+                     "sweeps_per_s": len(rec.sweep_seconds) / sum(rec.sweep_seconds),
+                     "sigma_per_s": rec.sigma_calls / sum(rec.sweep_seconds)}
         if kernels is not None:
             out[name]["kernel_device_s"] = dict(sorted(kernels.items(), key=lambda kv: -kv[1][0]))
         if rec.shadow:
